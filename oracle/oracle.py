@@ -1,0 +1,279 @@
+"""TEST INFRASTRUCTURE ONLY: ctypes front end of the CPU oracle (pz_oracle.cpp).
+
+The oracle is the checker for the GPU library and the CPU baseline of the
+benchmark.  It is imported by tests/, by ``__graft_entry__.smoke()`` and by the
+CPU-baseline leg of ``bench.py`` only; the product (``neopz_gb300``) never
+imports it.
+"""
+import ctypes
+import os
+import subprocess
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+_SRC = os.path.join(_HERE, "pz_oracle.cpp")
+_LIB = os.path.join(_HERE, "_build", "liborc.so")
+
+ORC_POISSON, ORC_DARCY, ORC_ELAST3D, ORC_MOCK = 1, 2, 3, 4
+ORC_F_NONE, ORC_F_CONST, ORC_F_SINPROD = 0, 1, 2
+T_LINE, T_QUAD, T_CUBE = 1, 2, 3
+BIGNUMBER = 10.0 ** 17 * 2 / 3  # TPZMaterial::fBigNumber default for double
+
+
+class orc_material(ctypes.Structure):
+    _fields_ = [("id", ctypes.c_int), ("kind", ctypes.c_int), ("dim", ctypes.c_int),
+                ("scale", ctypes.c_double), ("E", ctypes.c_double), ("nu", ctypes.c_double),
+                ("force", ctypes.c_double * 3), ("forcing", ctypes.c_int),
+                ("forcing_porder", ctypes.c_int), ("coef_const", ctypes.c_double),
+                ("bignumber", ctypes.c_double), ("mock_ek", ctypes.c_double * 4)]
+
+
+class orc_bc(ctypes.Structure):
+    _fields_ = [("id", ctypes.c_int), ("matid", ctypes.c_int), ("type", ctypes.c_int),
+                ("val1", ctypes.c_double * 9), ("val2", ctypes.c_double * 3)]
+
+
+class orc_grid_spec(ctypes.Structure):
+    _fields_ = [("dim", ctypes.c_int), ("ndiv", ctypes.c_int * 3),
+                ("minX", ctypes.c_double * 3), ("maxX", ctypes.c_double * 3),
+                ("matids", ctypes.c_int * 7), ("create_bc", ctypes.c_int),
+                ("default_order", ctypes.c_int), ("nmat", ctypes.c_int),
+                ("mats", orc_material * 4), ("nbc", ctypes.c_int), ("bcs", orc_bc * 8),
+                ("elem_coef", ctypes.POINTER(ctypes.c_double)),
+                ("elem_order", ctypes.POINTER(ctypes.c_int))]
+
+
+def build(force=False):
+    """Compile the oracle with g++ (works on x86_64 and aarch64)."""
+    os.makedirs(os.path.dirname(_LIB), exist_ok=True)
+    if force or not os.path.exists(_LIB) or os.path.getmtime(_LIB) < os.path.getmtime(_SRC):
+        subprocess.check_call(["g++", "-O2", "-std=c++17", "-fPIC", "-shared", "-pthread",
+                               _SRC, "-o", _LIB])
+    return _LIB
+
+
+_lib = None
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        build()
+        L = ctypes.CDLL(_LIB)
+        vp, i64, i32, dp = ctypes.c_void_p, ctypes.c_int64, ctypes.c_int, ctypes.c_double
+        P = ctypes.POINTER
+        L.orc_mesh_create.restype = vp
+        L.orc_mesh_create.argtypes = [P(orc_grid_spec)]
+        L.orc_mesh_free.argtypes = [vp]
+        for f in ("orc_neq", "orc_ncel", "orc_nconnects", "orc_nnodes"):
+            getattr(L, f).restype = i64
+            getattr(L, f).argtypes = [vp]
+        L.orc_nstate.restype = i32
+        L.orc_nstate.argtypes = [vp]
+        L.orc_cel_info.restype = i32
+        L.orc_cel_info.argtypes = [vp, i64, P(i32), P(i32), P(i64), vp, vp]
+        L.orc_block_info.argtypes = [vp, vp, vp]
+        L.orc_nodes.argtypes = [vp, vp]
+        L.orc_calc_stiff.restype = i32
+        L.orc_calc_stiff.argtypes = [vp, i64, vp, vp]
+        L.orc_shape.restype = i32
+        L.orc_shape.argtypes = [i32, vp, vp, vp, vp, vp, i32]
+        L.orc_contribute.argtypes = [i32, i32, dp, dp, dp, dp, i32, vp, vp, vp, vp, vp]
+        L.orc_gauss.restype = i32
+        L.orc_gauss.argtypes = [i32, vp, vp]
+        L.orc_pattern.restype = i64
+        L.orc_pattern.argtypes = [vp, i32, vp, vp]
+        L.orc_assemble.restype = i32
+        L.orc_assemble.argtypes = [vp, i32, vp, vp, vp, vp, i32]
+        L.orc_spmv.argtypes = [i64, i32, vp, vp, vp, vp, vp]
+        L.orc_cg_jacobi.restype = i32
+        L.orc_cg_jacobi.argtypes = [i64, i32, vp, vp, vp, vp, vp, i64, dp, i32, P(i64), P(dp), vp]
+        L.orc_gmres_jacobi.restype = i32
+        L.orc_gmres_jacobi.argtypes = [i64, i32, vp, vp, vp, vp, vp, i32, i64, dp, P(i64), P(dp)]
+        _lib = L
+    return _lib
+
+
+def _p(a):
+    return a.ctypes.data_as(ctypes.c_void_p) if a is not None else None
+
+
+def material(id, kind, dim, scale=1.0, E=1.0, nu=0.3, force=(0.0, 0.0, 0.0), forcing=ORC_F_NONE,
+             forcing_porder=0, coef_const=1.0, bignumber=BIGNUMBER, mock_ek=(0, 0, 0, 0)):
+    m = orc_material()
+    m.id, m.kind, m.dim, m.scale, m.E, m.nu = id, kind, dim, scale, E, nu
+    for i in range(3):
+        m.force[i] = force[i]
+    m.forcing, m.forcing_porder, m.coef_const, m.bignumber = forcing, forcing_porder, coef_const, bignumber
+    for i in range(4):
+        m.mock_ek[i] = mock_ek[i]
+    return m
+
+
+def bc(id, matid, type, val2=(0.0, 0.0, 0.0), val1=None):
+    b = orc_bc()
+    b.id, b.matid, b.type = id, matid, type
+    for i in range(3):
+        b.val2[i] = val2[i]
+    if val1 is not None:
+        for i in range(9):
+            b.val1[i] = val1[i]
+    return b
+
+
+class OracleMesh:
+    """A grid mesh + computational mesh + equation numbering built by the oracle."""
+
+    def __init__(self, dim, ndiv, minX, maxX, matids, create_bc, order, mats, bcs,
+                 elem_coef=None, elem_order=None):
+        L = lib()
+        s = orc_grid_spec()
+        s.dim = dim
+        for i in range(3):
+            s.ndiv[i] = ndiv[i] if i < len(ndiv) else 1
+            s.minX[i] = minX[i]
+            s.maxX[i] = maxX[i]
+        for i, mid in enumerate(matids):
+            s.matids[i] = mid
+        s.create_bc = int(create_bc)
+        s.default_order = order
+        s.nmat = len(mats)
+        for i, m in enumerate(mats):
+            s.mats[i] = m
+        s.nbc = len(bcs)
+        for i, b in enumerate(bcs):
+            s.bcs[i] = b
+        self._coef = None if elem_coef is None else np.ascontiguousarray(elem_coef, dtype=np.float64)
+        self._order = None if elem_order is None else np.ascontiguousarray(elem_order, dtype=np.int32)
+        if self._coef is not None:
+            s.elem_coef = self._coef.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+        if self._order is not None:
+            s.elem_order = self._order.ctypes.data_as(ctypes.POINTER(ctypes.c_int))
+        self.h = L.orc_mesh_create(ctypes.byref(s))
+        self.neq = L.orc_neq(self.h)
+        self.ncel = L.orc_ncel(self.h)
+        self.nconnects = L.orc_nconnects(self.h)
+        self.nstate = L.orc_nstate(self.h)
+
+    def __del__(self):
+        if getattr(self, "h", None):
+            lib().orc_mesh_free(self.h)
+            self.h = None
+
+    def blocks(self):
+        pos = np.zeros(self.nconnects, np.int64)
+        size = np.zeros(self.nconnects, np.int64)
+        lib().orc_block_info(self.h, _p(pos), _p(size))
+        return pos, size
+
+    def nodes(self):
+        n = lib().orc_nnodes(self.h)
+        xyz = np.zeros((n, 3))
+        lib().orc_nodes(self.h, _p(xyz))
+        return xyz
+
+    def cel(self, ic):
+        t, b, g = ctypes.c_int(), ctypes.c_int(), ctypes.c_int64()
+        conn = np.zeros(27, np.int64)
+        dest = np.zeros(27 * 64 * 3, np.int64)
+        n = lib().orc_cel_info(self.h, ic, ctypes.byref(t), ctypes.byref(b), ctypes.byref(g), _p(conn), _p(dest))
+        ns = {T_LINE: 3, T_QUAD: 9, T_CUBE: 27}[t.value]
+        return dict(type=t.value, is_bc=b.value, gel=g.value, conn=conn[:ns].copy(), dest=dest[:n].copy())
+
+    def calc_stiff(self, ic):
+        ek = np.zeros((192, 192))
+        ef = np.zeros(192)
+        n = lib().orc_calc_stiff(self.h, ic, _p(ek), _p(ef))
+        # the C side writes an n x n column-major matrix at the start of the buffer
+        flat = ek.reshape(-1)[: n * n].reshape(n, n).T.copy()
+        return flat, ef[:n].copy()
+
+    def pattern(self, sym):
+        nnz = lib().orc_pattern(self.h, int(sym), None, None)
+        ia = np.zeros(self.neq + 1, np.int64)
+        ja = np.zeros(nnz, np.int64)
+        lib().orc_pattern(self.h, int(sym), _p(ia), _p(ja))
+        return ia, ja
+
+    def assemble(self, sym, ia, ja, nthreads=0):
+        a = np.zeros(int(ia[-1]))
+        f = np.zeros(self.neq)
+        lib().orc_assemble(self.h, int(sym), _p(ia), _p(ja), _p(a), _p(f), int(nthreads))
+        return a, f
+
+
+def spmv(sym, ia, ja, a, x):
+    z = np.zeros(len(ia) - 1)
+    lib().orc_spmv(len(ia) - 1, int(sym), _p(ia), _p(ja), _p(a), _p(np.ascontiguousarray(x, np.float64)), _p(z))
+    return z
+
+
+def cg_jacobi(sym, ia, ja, a, b, maxit, tol, jacobi_residual=False, history=False):
+    n = len(ia) - 1
+    x = np.zeros(n)
+    it, res = ctypes.c_int64(), ctypes.c_double()
+    hist = np.zeros(maxit) if history else None
+    rc = lib().orc_cg_jacobi(n, int(sym), _p(ia), _p(ja), _p(a), _p(np.ascontiguousarray(b)), _p(x), maxit, tol,
+                             int(jacobi_residual), ctypes.byref(it), ctypes.byref(res), _p(hist))
+    out = dict(x=x, iters=it.value, resid=res.value, rc=rc)
+    if history:
+        out["hist"] = hist[: it.value].copy()
+    return out
+
+
+def gmres_jacobi(sym, ia, ja, a, b, m, maxit, tol):
+    n = len(ia) - 1
+    x = np.zeros(n)
+    it, res = ctypes.c_int64(), ctypes.c_double()
+    rc = lib().orc_gmres_jacobi(n, int(sym), _p(ia), _p(ja), _p(a), _p(np.ascontiguousarray(b)), _p(x), m, maxit,
+                                tol, ctypes.byref(it), ctypes.byref(res))
+    return dict(x=x, iters=it.value, resid=res.value, rc=rc)
+
+
+def gauss(order):
+    loc = np.zeros(64)
+    w = np.zeros(64)
+    n = lib().orc_gauss(order, _p(loc), _p(w))
+    return loc[:n].copy(), w[:n].copy()
+
+
+def shape(type, ids, orders, pt):
+    ids = np.ascontiguousarray(ids, np.int64)
+    orders = np.ascontiguousarray(orders, np.int32)
+    pt = np.ascontiguousarray(pt, np.float64)
+    phi = np.zeros(216)
+    dphi = np.zeros(3 * 216)
+    n = lib().orc_shape(type, _p(ids), _p(orders), _p(pt), _p(phi), _p(dphi), 216)
+    return phi[:n].copy(), dphi.reshape(3, 216)[:, :n].copy()
+
+
+# ---------------------------------------------------------------------------
+# The synthetic workloads, as the reference user programs would build them.
+# ---------------------------------------------------------------------------
+def poisson2d(n=64, p=2):
+    """64x64 quads, H1 p, f = 2 pi^2 sin(pi x) sin(pi y) (pOrder 2), u = 0 penalty Dirichlet."""
+    mats = [material(1, ORC_POISSON, 2, forcing=ORC_F_SINPROD, force=(1.0, 0, 0), forcing_porder=2)]
+    bcs = [bc(-1, 1, 0)]
+    return OracleMesh(2, (n, n), (0, 0, 0), (1, 1, 0), [1, -1, -1, -1, -1], True, p, mats, bcs)
+
+
+def elasticity3d(n, p=2, E=None, nu=0.3, top_traction=True, side_bc=False):
+    """Unit cube n^3 hexes, clamped z=0 face (type 0), traction (0,0,-1) on top (type 1),
+    body force (0,0,-1); E per element (array) or 1."""
+    mats = [material(1, ORC_ELAST3D, 3, E=1.0, nu=nu, force=(0, 0, -1.0), forcing=ORC_F_CONST)]
+    bcs = [bc(-1, 1, 0)]
+    if top_traction:
+        bcs.append(bc(-3, 1, 1, val2=(0, 0, -1.0)))
+    matids = [1, -1, -2, -2, -2, -2, -3]
+    return OracleMesh(3, (n, n, n), (0, 0, 0), (1, 1, 1), matids, True, p, mats, bcs, elem_coef=E)
+
+
+def darcy(dim, n, p, perm, rhs=1.0):
+    """-div(k grad u) = rhs on the unit square/cube with u = 0 penalty Dirichlet on every face."""
+    mats = [material(1, ORC_DARCY, dim, forcing=ORC_F_CONST, force=(rhs, 0, 0))]
+    bcs = [bc(-1, 1, 0)]
+    if dim == 2:
+        return OracleMesh(2, (n, n), (0, 0, 0), (1, 1, 0), [1, -1, -1, -1, -1], True, p, mats, bcs, elem_coef=perm)
+    return OracleMesh(3, (n, n, n), (0, 0, 0), (1, 1, 1), [1, -1, -1, -1, -1, -1, -1], True, p, mats, bcs,
+                      elem_coef=perm)

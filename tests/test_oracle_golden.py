@@ -1,0 +1,179 @@
+"""Pins the CPU oracle against the reference's own known answers (CPU only).
+
+* golden matrices of the reference's Catch2 tests (committed fixture);
+* counts printed by the reference library on the benchmark grids;
+* properties the reference's tests rely on (quadrature exactness, H1
+  conformity of the hierarchical shapes across shared sides).
+"""
+import json
+import os
+
+import numpy as np
+import pytest
+
+from oracle import oracle as O
+
+GOLD = json.load(open(os.path.join(os.path.dirname(__file__), "golden", "reference_unit_golden.json")))
+
+
+def _contribute(kind, dim, coef, nu, weight, phi, dphix, force=(0, 0, 0), scale=1.0):
+    nshape = len(phi)
+    n = 3 * nshape if kind == O.ORC_ELAST3D else nshape
+    ek = np.zeros(n * n)
+    ef = np.zeros(n)
+    phi = np.ascontiguousarray(phi, np.float64)
+    dphix = np.ascontiguousarray(dphix, np.float64)
+    f = np.ascontiguousarray(force, np.float64)
+    O.lib().orc_contribute(kind, dim, scale, coef, nu, weight, nshape, O._p(phi), O._p(dphix), O._p(f),
+                           O._p(ek), O._p(ef))
+    return ek.reshape(n, n).T.copy(), ef
+
+
+def test_cube_elasticity_9x9_golden():
+    g = GOLD["cube_elasticity_9x9"]
+    ek, _ = _contribute(O.ORC_ELAST3D, 3, g["E"], g["nu"], g["weight"], np.zeros(3), np.eye(3))
+    assert np.allclose(ek, ek.T, atol=1e-8)
+    assert np.max(np.abs(ek - np.array(g["matrix"]))) <= g["margin"]
+
+
+def test_darcy_master_quad_golden():
+    g = GOLD["darcy_master_quad_4x4"]
+    loc, w = O.gauss(g["intrule_order"])
+    n = len(loc)
+    ek = np.zeros((4, 4))
+    for ip in range(n * n):  # TPZIntQuad ordering: eta fastest
+        ik, ie = ip // n, ip % n
+        phi, dphi = O.shape(O.T_QUAD, g["ids"], [1] * 5, [loc[ik], loc[ie]])
+        e, _ = _contribute(O.ORC_DARCY, 2, g["perm"], 0.0, w[ik] * w[ie], phi, dphi)
+        ek += e
+    assert np.max(np.abs(ek - np.array(g["matrix"]))) <= g["margin"]
+
+
+@pytest.mark.parametrize("sym", [True, False])
+def test_known_matrix_1d(sym):
+    g = GOLD["known_matrix_1d"]
+    ek = np.array(g["mock_ek"]).reshape(-1)
+    mats = [O.material(1, O.ORC_MOCK, 1, mock_ek=tuple(ek))]
+    m = O.OracleMesh(1, (g["n_el"], 1, 1), (0, 0, 0), (g["n_el"], 0, 0), [1], False, g["order"], mats, [])
+    assert m.neq == g["n_el"] + 1
+    ia, ja = m.pattern(sym)
+    a, _ = m.assemble(sym, ia, ja)
+    A = np.zeros((m.neq, m.neq))
+    for r in range(m.neq):
+        for k in range(ia[r], ia[r + 1]):
+            A[r, ja[k]] = a[k]
+            if sym:
+                A[ja[k], r] = a[k]
+    n = m.neq
+    assert A[0, 0] == g["diag_end"] and A[n - 1, n - 1] == g["diag_end"]
+    for i in range(1, n - 1):
+        assert A[i, i] == g["diag_mid"] and A[i, i - 1] == g["offdiag"] and A[i, i + 1] == g["offdiag"]
+
+
+def test_poisson2d_reference_counts():
+    g = GOLD["reference_run_counts"]["poisson2d_q2_64"]
+    m = O.poisson2d(64, 2)
+    assert m.neq == g["neq"]
+    ia, ja = m.pattern(True)
+    assert len(ja) == g["nnz_upper"]
+    a, f = m.assemble(True, ia, ja)
+    r = O.cg_jacobi(True, ia, ja, a, f, 20000, 1e-10)
+    assert r["iters"] == g["cg_iters_1e10"]
+    # the discrete solution approximates sin(pi x) sin(pi y): peak 1
+    assert abs(r["x"].max() - 1.0) < 1e-6
+
+
+@pytest.mark.slow
+def test_elasticity16_reference_counts():
+    g = GOLD["reference_run_counts"]["elast3d_q2_16"]
+    m = O.elasticity3d(16, 2)
+    assert m.neq == g["neq"]
+    ia, ja = m.pattern(True)
+    assert len(ja) == g["nnz_upper"]
+    a, f = m.assemble(True, ia, ja, nthreads=4)
+    r = O.cg_jacobi(True, ia, ja, a, f, 5000, 1e-8)
+    assert r["iters"] == g["cg_iters_1e8"]
+
+
+def test_threaded_assembly_equals_serial():
+    # StructMatrixUnitTest "Compare parallel and serial matrices": |diff| <= 10 eps
+    m = O.elasticity3d(4, 2)
+    ia, ja = m.pattern(True)
+    a0, f0 = m.assemble(True, ia, ja, nthreads=0)
+    a4, f4 = m.assemble(True, ia, ja, nthreads=4)
+    assert np.array_equal(a0, a4) and np.array_equal(f0, f4)
+
+
+def test_sym_and_full_patterns_agree():
+    m = O.elasticity3d(3, 2)
+    ia, ja = m.pattern(True)
+    ib, jb = m.pattern(False)
+    a, f = m.assemble(True, ia, ja)
+    b, g = m.assemble(False, ib, jb)
+    x = np.random.default_rng(0).standard_normal(m.neq)
+    assert np.allclose(O.spmv(True, ia, ja, a, x), O.spmv(False, ib, jb, b, x), rtol=1e-12, atol=1e-9)
+    assert np.array_equal(f, g)
+    # full rows sorted, upper rows start at the diagonal
+    for r in range(m.neq):
+        assert np.all(np.diff(jb[ib[r]:ib[r + 1]]) > 0)
+        assert ja[ia[r]] == r
+
+
+@pytest.mark.parametrize("npts", [1, 2, 3, 4, 5])
+def test_gauss_exactness(npts):
+    order = 2 * npts - 2
+    loc, w = O.gauss(order)
+    assert len(loc) == npts
+    for k in range(2 * npts):
+        exact = 0.0 if k % 2 else 2.0 / (k + 1)
+        assert abs(np.sum(w * loc ** k) - exact) < 1e-14
+
+
+@pytest.mark.parametrize("p", [2, 3])
+def test_h1_conformity_across_shared_face(p):
+    """Two hexes sharing the face x=+1 / x=-1 of their master elements: the traces of the
+    shapes of the shared connects must coincide (orientation from global node ids)."""
+    rng = np.random.default_rng(p)
+    gid = rng.permutation(12)
+    # element A: x in [-1,1]; element B: x in [1,3]; shared face nodes 1,2,6,5 of A = 0,3,7,4 of B
+    A = [gid[i] for i in (0, 1, 2, 3, 4, 5, 6, 7)]
+    B = [gid[i] for i in (1, 8, 9, 2, 5, 10, 11, 6)]
+    orders = [p] * 19
+    # shapes of A on its face 22 (x=+1) vs B on its face 24 (x=-1), same physical point (y, z)
+    for (y, z) in [(-0.3, 0.7), (0.5, -0.2), (0.9, 0.1)]:
+        pa, _ = O.shape(O.T_CUBE, A, orders, [1.0, y, z])
+        pb, _ = O.shape(O.T_CUBE, B, orders, [-1.0, y, z])
+        # map connect-wise: corner shapes of shared nodes
+        for la, lb in [(1, 0), (2, 3), (6, 7), (5, 4)]:
+            assert abs(pa[la] - pb[lb]) < 1e-13
+        # shapes attached to the shared face connect and its edges
+        def side_range(orders_, side):
+            first = 8 + sum(_nconn(s, p) for s in range(8, side))
+            return first, first + _nconn(side, p)
+        for sa, sb in [(22, 24), (9, 11), (14, 15), (17, 19), (13, 12)]:
+            fa, la_ = side_range(orders, sa)
+            fb, lb_ = side_range(orders, sb)
+            assert np.allclose(pa[fa:la_], pb[fb:lb_], atol=1e-12), (sa, sb)
+
+
+def _nconn(side, p):
+    if side < 8:
+        return 1
+    if side < 20:
+        return p - 1
+    if side < 26:
+        return (p - 1) ** 2
+    return (p - 1) ** 3
+
+
+def test_shape_derivatives_match_finite_differences():
+    ids = [5, 2, 7, 0, 3, 6, 1, 4]
+    orders = [3] * 19
+    x = np.array([0.21, -0.37, 0.55])
+    phi, dphi = O.shape(O.T_CUBE, ids, orders, x)
+    h = 1e-6
+    for d in range(3):
+        e = np.zeros(3)
+        e[d] = h
+        fd = (O.shape(O.T_CUBE, ids, orders, x + e)[0] - O.shape(O.T_CUBE, ids, orders, x - e)[0]) / (2 * h)
+        assert np.allclose(fd, dphi[d], atol=1e-7)
