@@ -1,0 +1,199 @@
+/*
+ * gpz.h -- C ABI of the GB300 (sm_103a) implementation of the NeoPZ linear
+ * FEM hot path: global assembly (TPZLinearAnalysis::Assemble through
+ * TPZStructMatrix into TPZSYsmpMatrix / TPZFYsmpMatrix CSR) and the
+ * iterative solve (TPZStepSolver CG / GMRES with Jacobi or block Jacobi).
+ *
+ * Plain C types only: pointers, sizes and POD structs.  Every call returns a
+ * status code (GPZ_OK = 0, negative = error, positive = solver did not
+ * converge) and never throws.  One context owns one CUDA stream and every
+ * device buffer it allocates; a context is used by one host thread at a time.
+ *
+ * The reference interfaces each entry point replaces are cited beside it
+ * (paths relative to the NeoPZ source tree).
+ */
+#ifndef GPZ_H
+#define GPZ_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes --------------------------------------------------------
+ * The reference aborts through DebugStop() (Common/pzerror.cpp:7-27); the C++
+ * plugin classes map negative codes back to DebugStop(). */
+#define GPZ_OK 0
+#define GPZ_NOT_CONVERGED 1            /* CG/GMRES hit max_iter (cg.h:129-131 returns 1) */
+#define GPZ_E_INVALID (-1)             /* bad argument / inconsistent descriptor */
+#define GPZ_E_CUDA (-2)                /* CUDA runtime error */
+#define GPZ_E_NOMEM (-3)               /* device allocation failed */
+#define GPZ_E_UNSUPPORTED_MATERIAL (-4)
+#define GPZ_E_UNSUPPORTED_ELEMENT (-5)
+#define GPZ_E_NOT_READY (-6)           /* call order violated (e.g. assemble before pattern) */
+#define GPZ_E_DEVICE_CHECK (-7)        /* a kernel's own bounds / invariant check failed */
+#define GPZ_E_NO_DEVICE (-8)           /* no CUDA device visible */
+#define GPZ_E_BREAKDOWN (-9)           /* NaN / non-positive curvature in the Krylov recurrence */
+
+/* ---- element types (TPZShapeLinear / TPZShapeQuad / TPZShapeCube) -------- */
+#define GPZ_EL_LINE 1
+#define GPZ_EL_QUAD 2
+#define GPZ_EL_HEX 3
+
+/* ---- material kinds ------------------------------------------------------ */
+#define GPZ_MAT_POISSON 1   /* TPZMatPoisson::Contribute  Material/Poisson/TPZMatPoisson.cpp:19-43 */
+#define GPZ_MAT_DARCY 2     /* TPZDarcyFlow::Contribute   Material/DarcyFlow/TPZDarcyFlow.cpp:19-47 */
+#define GPZ_MAT_ELAST3D 3   /* TPZElasticity3D CODE3      Material/Elasticity/TPZElasticity3D.cpp:269-400 */
+
+/* forcing functions the device evaluates at the physical integration point */
+#define GPZ_F_NONE 0
+#define GPZ_F_CONST 1       /* force[0..2] */
+#define GPZ_F_SINPROD 2     /* force[0] * d pi^2 prod_k sin(pi x_k) */
+
+typedef struct {
+  int32_t kind;           /* GPZ_MAT_* */
+  int32_t dim;            /* TPZMatPoisson/TPZDarcyFlow fDim */
+  double scale;           /* TPZMatPoisson::fScale */
+  double E, nu;           /* TPZElasticity3D fE, fPoisson (E overridden per element by el_coef) */
+  double coef_const;      /* constant permeability (TPZIsotropicPermeability) */
+  double force[3];
+  int32_t forcing;        /* GPZ_F_* */
+  int32_t forcing_porder; /* SetForcingFunction(f, pOrder): raises the integration order */
+  double bignumber;       /* TPZMaterial::fBigNumber (Material/TPZMaterial.h:125) */
+} gpz_material;
+
+typedef struct {
+  int32_t type;           /* 0 Dirichlet (penalty), 1 Neumann (TPZBndCondT types) */
+  int32_t material;       /* index of the volume material in gpz_mesh_desc::mats */
+  double val1[9];
+  double val2[3];
+} gpz_bc;
+
+/* The computational mesh as the TPZCompMesh holds it after AutoBuild: one
+ * entry per computational element (volume and boundary) in element order,
+ * each with its corner nodes (TPZGeoEl::NodeIndex), preferred order and the
+ * connect (sequence number) of every side (TPZCompEl::ConnectIndex ->
+ * TPZConnect::SequenceNumber), plus the block structure (TPZBlock Position /
+ * Size).  This is exactly what TPZCompMesh::ComputeElGraph and
+ * TPZElementMatrix::ComputeDestinationIndices (Mesh/pzelmat.cpp:37-96) read. */
+typedef struct {
+  int32_t dim;              /* 1, 2 or 3 */
+  int32_t nstate;           /* 1 (scalar) or 3 (elasticity) */
+  int64_t nnodes;
+  const double *node_xyz;   /* [nnodes][3] */
+  int64_t nel;
+  const int32_t *el_type;   /* GPZ_EL_* */
+  const int32_t *el_mat;    /* >= 0: volume material index; < 0: -(bc index) - 1 */
+  const int64_t *el_nodes;  /* [nel][8] corner node indices (unused slots -1) */
+  const int32_t *el_order;  /* [nel] preferred interpolation order (fPreferredOrder) */
+  const int64_t *el_conn;   /* [nel][27] connect sequence number of each side */
+  const double *el_coef;    /* [nel] per-element permeability / Young modulus, or NULL */
+  int64_t nconnects;
+  const int32_t *conn_order;/* [nconnects] TPZConnect::Order */
+  const int64_t *block_pos; /* [nconnects] TPZBlock::Position */
+  const int32_t *block_size;/* [nconnects] TPZBlock::Size = NShape * NState */
+  int64_t neq;
+  int32_t nmat;
+  const gpz_material *mats;
+  int32_t nbc;
+  const gpz_bc *bcs;
+} gpz_mesh_desc;
+
+typedef struct gpz_ctx gpz_ctx;
+
+/* ---- context ------------------------------------------------------------- */
+int gpz_ctx_create(gpz_ctx **out, int device);
+int gpz_ctx_destroy(gpz_ctx *ctx);
+const char *gpz_get_error_string(int code);
+const char *gpz_last_error_detail(gpz_ctx *ctx);
+/* The CUDA stream (cudaStream_t) every call of this context is ordered on. */
+void *gpz_ctx_stream(gpz_ctx *ctx);
+/* Number of kernels this context has launched since creation (graph nodes count). */
+int64_t gpz_kernel_launches(gpz_ctx *ctx);
+
+/* ---- mesh ---------------------------------------------------------------
+ * Replaces the host-side extraction of TPZStructMatrix::Assemble: copies the
+ * element / connect / block arrays to the device, builds the element buckets
+ * (type, order signature, material) and the atomic-free element colouring
+ * (TPZStructMatrix::ComputeElementColors, StrMatrix/TPZStructMatrix.cpp:104-161). */
+int gpz_mesh_upload(gpz_ctx *ctx, const gpz_mesh_desc *desc);
+
+/* ---- sparsity pattern ----------------------------------------------------
+ * Replaces TPZSSpStructMatrix::Create / SetupMatrixData (sym = 1, upper
+ * triangle; StrMatrix/TPZSSpStructMatrix.cpp:31-193) and
+ * TPZSpStructMatrix::SetupMatrixData (sym = 0, full rows;
+ * StrMatrix/TPZSpStructMatrix.cpp:53-190), built on the device from the
+ * element graph (TPZCompMesh::ComputeElGraph, TPZRenumbering::ConvertGraph).
+ * Returns the number of stored entries in *nnz_out. */
+int gpz_pattern_build(gpz_ctx *ctx, int sym, int64_t *nnz_out);
+/* Alternatively adopt a host pattern (IA, JA as TPZSYsmpMatrix::IA()/JA()). */
+int gpz_pattern_upload(gpz_ctx *ctx, int sym, int64_t neq, const int64_t *IA, const int64_t *JA);
+/* Copy the device pattern to the host (IA: neq+1, JA: nnz, as int64). */
+int gpz_pattern_download(gpz_ctx *ctx, int64_t *IA, int64_t *JA);
+
+/* ---- assembly -------------------------------------------------------------
+ * Replaces TPZStructMatrixOR::Assemble (StrMatrix/pzstrmatrixor.cpp:43-71,106-365)
+ * with its TPZCompEl::CalcStiff (Mesh/pzinterpolationspace.cpp:403-473),
+ * TPZMaterial::Contribute/ContributeBC, TPZSYsmpMatrix::AddKel
+ * (Matrix/pzsysmp.cpp:369-411; entries |v| < 1e-12 skipped as IsZero does),
+ * TPZFMatrix::AddFel and TPZSYsmpMatrix::ComputeDiagonal (EndCreateAssemble).
+ * precision: GPZ_PREC_FP64 (the parity path) or GPZ_PREC_MIXED (FP64 matrix for
+ * the true residual plus an FP32 copy built for the inner solves). */
+#define GPZ_PREC_FP64 0
+#define GPZ_PREC_MIXED 1
+int gpz_assemble(gpz_ctx *ctx, int precision);
+/* Download the assembled values (nnz doubles) and the load vector (neq). */
+int gpz_matrix_download(gpz_ctx *ctx, double *A);
+int gpz_rhs_download(gpz_ctx *ctx, double *F);
+/* Overwrite the device load vector (a user right-hand side). */
+int gpz_rhs_upload(gpz_ctx *ctx, const double *F);
+
+/* ---- SpMV -----------------------------------------------------------------
+ * TPZSYsmpMatrix::MultAdd / TPZFYsmpMatrix::MultAdd (Matrix/pzsysmp.cpp:189-232,
+ * Matrix/pzysmp.cpp:527-624):  z = alpha A x + beta y, host vectors. */
+int gpz_spmv(gpz_ctx *ctx, double alpha, const double *x, double beta, const double *y, double *z);
+
+/* ---- solve ----------------------------------------------------------------
+ * TPZStepSolver::Solve (Solvers/pzstepsolver.cpp:64-169) with SetCG / SetGMRES
+ * and a Jacobi (SetJacobi(1,0,0)) or block-Jacobi preconditioner. */
+#define GPZ_SOLVER_CG 1            /* Solvers/LinearSolvers/cg.h:29-132 */
+#define GPZ_SOLVER_GMRES 2         /* Solvers/LinearSolvers/gmres.h:68-168 */
+#define GPZ_SOLVER_MIXED_CG 3      /* FP32-value SpMV CG, FP64 x/dots, reliable FP64 residual updates */
+#define GPZ_SOLVER_LEARNED_FCG 4   /* flexible CG with the learned correction + Jacobi, FP64 residual */
+#define GPZ_PRECOND_JACOBI 1       /* TPZMatrix::SolveJacobi, one sweep (Matrix/pzmatrix.cpp:643-667) */
+#define GPZ_PRECOND_BLOCK_JACOBI 2 /* connect blocks, TPZBlockDiagonal (Matrix/pzblockdiag.h:21) */
+
+typedef struct {
+  int32_t solver;          /* GPZ_SOLVER_* */
+  int32_t precond;         /* GPZ_PRECOND_* */
+  int64_t max_iter;
+  double tol;              /* stop when ||r||/||b|| <= tol (recursive r, as cg.h:100) */
+  int32_t gmres_krylov;    /* GMRES restart length (SetGMRES numvectors) */
+  int32_t check_every;     /* iterations per graph launch between convergence checks */
+  double reliable_delta;   /* mixed CG: true-residual update when ||r|| < delta * max||r|| */
+  int32_t use_graph;       /* capture the iteration batch in a CUDA graph */
+  int32_t from_current;    /* FromCurrent: start from x instead of zero */
+} gpz_solver_opts;
+
+typedef struct {
+  int64_t iterations;      /* fNumIterations */
+  double resid;            /* final recursive ||r||/||b|| (fTol on return) */
+  double true_resid;       /* ||b - A x|| / ||b|| recomputed in FP64 on the device */
+  double seconds;          /* device time of the solve */
+  int64_t spmv_fp64;       /* FP64 SpMVs performed */
+  int64_t spmv_fp32;       /* FP32-value SpMVs performed */
+  int64_t reliable_updates;
+} gpz_solve_report;
+
+/* b: host load vector (NULL = use the assembled device rhs); x: host solution
+ * (in: initial guess if from_current, out: solution; may be NULL to keep the
+ * solution on the device only). */
+int gpz_solve(gpz_ctx *ctx, const gpz_solver_opts *opts, const double *b, double *x, gpz_solve_report *rep);
+/* Download the device solution of the last solve. */
+int gpz_solution_download(gpz_ctx *ctx, double *x);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* GPZ_H */

@@ -1,0 +1,337 @@
+// C ABI entry points (include/gpz.h).  No exception crosses this boundary.
+#include <cstring>
+
+#include "gpz_internal.h"
+#include "gpz_shapes.h"
+
+namespace gpz {
+void solver_prepare(Ctx &c, bool mixed);
+
+Ctx::~Ctx() {
+  for (Bucket *b : buckets) delete b;
+  buckets.clear();
+}
+}  // namespace gpz
+
+using namespace gpz;
+
+struct gpz_ctx {
+  Ctx c;
+};
+
+namespace {
+
+template <class F>
+int guarded(gpz_ctx *ctx, F &&f) {
+  if (!ctx) return GPZ_E_INVALID;
+  try {
+    GPZ_CUDA_TRY(cudaSetDevice(ctx->c.device));
+    int rc = f(ctx->c);
+    return rc;
+  } catch (const Error &e) {
+    ctx->c.last_error = e.msg;
+    if (e.code == GPZ_E_CUDA || e.code == GPZ_E_NOMEM) cudaGetLastError();  // clear a non-sticky error
+    return e.code;
+  } catch (const std::bad_alloc &) {
+    ctx->c.last_error = "host allocation failed";
+    return GPZ_E_NOMEM;
+  } catch (...) {
+    ctx->c.last_error = "unexpected host exception";
+    return GPZ_E_INVALID;
+  }
+}
+
+}  // namespace
+
+extern "C" {
+
+const char *gpz_get_error_string(int code) {
+  switch (code) {
+    case GPZ_OK: return "ok";
+    case GPZ_NOT_CONVERGED: return "iterative solver did not converge within max_iter";
+    case GPZ_E_INVALID: return "invalid argument";
+    case GPZ_E_CUDA: return "CUDA runtime error";
+    case GPZ_E_NOMEM: return "device memory allocation failed";
+    case GPZ_E_UNSUPPORTED_MATERIAL: return "material or boundary condition has no device implementation";
+    case GPZ_E_UNSUPPORTED_ELEMENT: return "element type/order has no device kernel";
+    case GPZ_E_NOT_READY: return "call order violated (mesh -> pattern -> assemble -> solve)";
+    case GPZ_E_DEVICE_CHECK: return "a device-side bounds or invariant check failed";
+    case GPZ_E_NO_DEVICE: return "no CUDA device";
+    case GPZ_E_BREAKDOWN: return "Krylov breakdown (non-positive curvature or non-finite residual)";
+    default: return "unknown status";
+  }
+}
+
+int gpz_ctx_create(gpz_ctx **out, int device) {
+  if (!out) return GPZ_E_INVALID;
+  *out = nullptr;
+  int n = 0;
+  if (cudaGetDeviceCount(&n) != cudaSuccess || n == 0) {
+    cudaGetLastError();
+    return GPZ_E_NO_DEVICE;
+  }
+  if (device < 0 || device >= n) return GPZ_E_INVALID;
+  gpz_ctx *ctx = new (std::nothrow) gpz_ctx();
+  if (!ctx) return GPZ_E_NOMEM;
+  ctx->c.device = device;
+  int rc = guarded(ctx, [](Ctx &c) {
+    GPZ_CUDA_TRY(cudaStreamCreateWithFlags(&c.stream, cudaStreamNonBlocking));
+    c.d_err.alloc(1);
+    c.d_err.zero(c.stream);
+    GPZ_CUDA_TRY(cudaStreamSynchronize(c.stream));
+    return GPZ_OK;
+  });
+  if (rc != GPZ_OK) {
+    delete ctx;
+    return rc;
+  }
+  *out = ctx;
+  return GPZ_OK;
+}
+
+int gpz_ctx_destroy(gpz_ctx *ctx) {
+  if (!ctx) return GPZ_E_INVALID;
+  cudaSetDevice(ctx->c.device);
+  if (ctx->c.stream) cudaStreamSynchronize(ctx->c.stream);
+  cudaStream_t s = ctx->c.stream;
+  delete ctx;  // frees every device buffer
+  if (s) cudaStreamDestroy(s);
+  return GPZ_OK;
+}
+
+const char *gpz_last_error_detail(gpz_ctx *ctx) { return ctx ? ctx->c.last_error.c_str() : ""; }
+void *gpz_ctx_stream(gpz_ctx *ctx) { return ctx ? (void *)ctx->c.stream : nullptr; }
+int64_t gpz_kernel_launches(gpz_ctx *ctx) { return ctx ? ctx->c.launches : 0; }
+
+int gpz_mesh_upload(gpz_ctx *ctx, const gpz_mesh_desc *d) {
+  return guarded(ctx, [d](Ctx &c) {
+    GPZ_REQUIRE(d, GPZ_E_INVALID, "null descriptor");
+    GPZ_REQUIRE(d->dim >= 1 && d->dim <= 3, GPZ_E_INVALID, "dim");
+    GPZ_REQUIRE(d->nstate == 1 || d->nstate == 3, GPZ_E_INVALID, "nstate");
+    GPZ_REQUIRE(d->nel >= 0 && d->nnodes >= 0 && d->nconnects >= 0 && d->neq >= 0, GPZ_E_INVALID, "sizes");
+    GPZ_REQUIRE(d->neq < INT32_MAX, GPZ_E_INVALID, "neq must fit 32-bit column indices");
+    GPZ_REQUIRE(d->node_xyz && d->el_type && d->el_mat && d->el_nodes && d->el_order && d->el_conn &&
+                    d->conn_order && d->block_pos && d->block_size && (d->nmat == 0 || d->mats),
+                GPZ_E_INVALID, "null array");
+    // TPZBlock positions are consecutive in sequence-number order; the pattern
+    // builder relies on it (columns sorted by connect = sorted by equation).
+    int64_t pos = 0;
+    for (int64_t i = 0; i < d->nconnects; i++) {
+      GPZ_REQUIRE(d->block_pos[i] == pos, GPZ_E_INVALID, "block positions must be consecutive in connect order");
+      GPZ_REQUIRE(d->block_size[i] >= 0, GPZ_E_INVALID, "block size");
+      pos += d->block_size[i];
+    }
+    GPZ_REQUIRE(pos == d->neq, GPZ_E_INVALID, "sum of block sizes != neq");
+    for (int64_t e = 0; e < d->nel; e++) {
+      int t = d->el_type[e];
+      GPZ_REQUIRE(t == GPZ_EL_LINE || t == GPZ_EL_QUAD || t == GPZ_EL_HEX, GPZ_E_UNSUPPORTED_ELEMENT, "element type");
+      const ElemTopo &tp = topo(t);
+      for (int k = 0; k < tp.ncorner; k++) {
+        int64_t nd = d->el_nodes[e * 8 + k];
+        GPZ_REQUIRE(nd >= 0 && nd < d->nnodes, GPZ_E_INVALID, "corner node index");
+      }
+      for (int s = 0; s < tp.nsides; s++) {
+        int64_t cn = d->el_conn[e * 27 + s];
+        GPZ_REQUIRE(cn >= 0 && cn < d->nconnects, GPZ_E_INVALID, "connect index");
+      }
+      GPZ_REQUIRE(d->el_order[e] >= 1 && d->el_order[e] <= 3, GPZ_E_UNSUPPORTED_ELEMENT, "order must be 1..3");
+    }
+    c.dim = d->dim;
+    c.nstate = d->nstate;
+    c.nel = d->nel;
+    c.nnodes = d->nnodes;
+    c.nconnects = d->nconnects;
+    c.neq = d->neq;
+    c.mats.assign(d->mats, d->mats + d->nmat);
+    c.bcs.assign(d->bcs, d->bcs + d->nbc);
+    c.h_el_type.assign(d->el_type, d->el_type + d->nel);
+    c.h_el_mat.assign(d->el_mat, d->el_mat + d->nel);
+    c.h_el_conn.assign(d->el_conn, d->el_conn + d->nel * 27);
+    c.h_block_pos.assign(d->block_pos, d->block_pos + d->nconnects);
+    c.h_block_size.assign(d->block_size, d->block_size + d->nconnects);
+    cudaStream_t s = c.stream;
+    c.d_xyz.upload(d->node_xyz, d->nnodes * 3, s);
+    c.d_el_type.upload(d->el_type, d->nel, s);
+    c.d_el_mat.upload(d->el_mat, d->nel, s);
+    c.d_el_nodes.upload(d->el_nodes, d->nel * 8, s);
+    c.d_el_conn.upload(d->el_conn, d->nel * 27, s);
+    c.d_conn_order.upload(d->conn_order, d->nconnects, s);
+    c.d_block_size.upload(d->block_size, d->nconnects, s);
+    c.d_block_pos.upload(d->block_pos, d->nconnects, s);
+    if (d->el_coef) c.d_coef.upload(d->el_coef, d->nel, s);
+    else c.d_coef.release();
+    build_buckets(c, *d);
+    c.have_mesh = true;
+    c.have_pattern = c.have_matrix = c.have_solution = c.have_a32 = c.have_bjinv = false;
+    return GPZ_OK;
+  });
+}
+
+int gpz_pattern_build(gpz_ctx *ctx, int sym, int64_t *nnz_out) {
+  return guarded(ctx, [&](Ctx &c) {
+    GPZ_REQUIRE(c.have_mesh, GPZ_E_NOT_READY, "no mesh");
+    build_pattern(c);
+    build_upper(c);
+    build_element_offsets(c);
+    c.user_sym = sym ? 1 : 0;
+    c.have_pattern = true;
+    c.have_matrix = false;
+    if (nnz_out) *nnz_out = sym ? c.nnz_upper : c.nnz;
+    return GPZ_OK;
+  });
+}
+
+int gpz_pattern_upload(gpz_ctx *ctx, int sym, int64_t neq, const int64_t *IA, const int64_t *JA) {
+  return guarded(ctx, [&](Ctx &c) {
+    GPZ_REQUIRE(c.have_mesh, GPZ_E_NOT_READY, "no mesh");
+    GPZ_REQUIRE(neq == c.neq && IA && JA, GPZ_E_INVALID, "pattern size");
+    GPZ_REQUIRE(!sym, GPZ_E_INVALID, "upload the full pattern (TPZFYsmpMatrix layout); the upper one is derived");
+    int64_t nnz = IA[neq];
+    std::vector<int32_t> ja32(nnz);
+    for (int64_t k = 0; k < nnz; k++) {
+      GPZ_REQUIRE(JA[k] >= 0 && JA[k] < neq, GPZ_E_INVALID, "column index");
+      ja32[k] = (int32_t)JA[k];
+    }
+    c.nnz = nnz;
+    c.d_ia.upload(IA, neq + 1, c.stream);
+    c.d_ja.upload(ja32.data(), nnz, c.stream);
+    build_upper(c);
+    build_element_offsets(c);
+    c.user_sym = 0;
+    c.have_pattern = true;
+    c.have_matrix = false;
+    return GPZ_OK;
+  });
+}
+
+int gpz_pattern_download(gpz_ctx *ctx, int64_t *IA, int64_t *JA) {
+  return guarded(ctx, [&](Ctx &c) {
+    GPZ_REQUIRE(c.have_pattern, GPZ_E_NOT_READY, "no pattern");
+    GPZ_REQUIRE(IA && JA, GPZ_E_INVALID, "null output");
+    const DBuf<int64_t> &ia = c.user_sym ? c.d_ia_up : c.d_ia;
+    const DBuf<int32_t> &ja = c.user_sym ? c.d_ja_up : c.d_ja;
+    int64_t nnz = c.user_sym ? c.nnz_upper : c.nnz;
+    GPZ_CUDA_TRY(cudaMemcpyAsync(IA, ia.p, (c.neq + 1) * sizeof(int64_t), cudaMemcpyDeviceToHost, c.stream));
+    std::vector<int32_t> tmp(nnz);
+    if (nnz) GPZ_CUDA_TRY(cudaMemcpyAsync(tmp.data(), ja.p, nnz * sizeof(int32_t), cudaMemcpyDeviceToHost, c.stream));
+    GPZ_CUDA_TRY(cudaStreamSynchronize(c.stream));
+    for (int64_t k = 0; k < nnz; k++) JA[k] = tmp[k];
+    return GPZ_OK;
+  });
+}
+
+int gpz_assemble(gpz_ctx *ctx, int precision) {
+  return guarded(ctx, [&](Ctx &c) {
+    GPZ_REQUIRE(c.have_pattern, GPZ_E_NOT_READY, "no pattern");
+    GPZ_REQUIRE(precision == GPZ_PREC_FP64 || precision == GPZ_PREC_MIXED, GPZ_E_INVALID, "precision");
+    assemble_fp64(c);
+    if (precision == GPZ_PREC_MIXED) make_fp32_copy(c);
+    GPZ_CUDA_TRY(cudaStreamSynchronize(c.stream));
+    check_device_flag(c, "assembly");
+    c.have_matrix = true;
+    return GPZ_OK;
+  });
+}
+
+namespace {
+__global__ void k_gather_upper(const double *__restrict__ a, const int64_t *__restrict__ diagpos,
+                               const int64_t *__restrict__ ia, const int64_t *__restrict__ ia_up, int64_t neq,
+                               double *__restrict__ out) {
+  int64_t r = blockIdx.x;
+  if (r >= neq) return;
+  int64_t d = diagpos[r], n = ia[r + 1] - d, o = ia_up[r];
+  for (int64_t k = threadIdx.x; k < n; k += blockDim.x) out[o + k] = a[d + k];
+}
+}  // namespace
+
+int gpz_matrix_download(gpz_ctx *ctx, double *A) {
+  return guarded(ctx, [&](Ctx &c) {
+    GPZ_REQUIRE(c.have_matrix, GPZ_E_NOT_READY, "not assembled");
+    GPZ_REQUIRE(A, GPZ_E_INVALID, "null output");
+    if (!c.user_sym) {
+      GPZ_CUDA_TRY(cudaMemcpyAsync(A, c.d_a.p, c.nnz * sizeof(double), cudaMemcpyDeviceToHost, c.stream));
+    } else {
+      DBuf<double> up;
+      up.alloc(std::max<int64_t>(c.nnz_upper, 1));
+      if (c.neq) {
+        k_gather_upper<<<(unsigned)c.neq, 128, 0, c.stream>>>(c.d_a.p, c.d_diagpos.p, c.d_ia.p, c.d_ia_up.p, c.neq,
+                                                              up.p);
+        c.launches++;
+        GPZ_CUDA_TRY(cudaGetLastError());
+      }
+      GPZ_CUDA_TRY(cudaMemcpyAsync(A, up.p, c.nnz_upper * sizeof(double), cudaMemcpyDeviceToHost, c.stream));
+      GPZ_CUDA_TRY(cudaStreamSynchronize(c.stream));
+    }
+    GPZ_CUDA_TRY(cudaStreamSynchronize(c.stream));
+    return GPZ_OK;
+  });
+}
+
+int gpz_rhs_download(gpz_ctx *ctx, double *F) {
+  return guarded(ctx, [&](Ctx &c) {
+    GPZ_REQUIRE(c.have_matrix, GPZ_E_NOT_READY, "not assembled");
+    GPZ_CUDA_TRY(cudaMemcpyAsync(F, c.d_f.p, c.neq * sizeof(double), cudaMemcpyDeviceToHost, c.stream));
+    GPZ_CUDA_TRY(cudaStreamSynchronize(c.stream));
+    return GPZ_OK;
+  });
+}
+
+int gpz_rhs_upload(gpz_ctx *ctx, const double *F) {
+  return guarded(ctx, [&](Ctx &c) {
+    GPZ_REQUIRE(c.have_matrix, GPZ_E_NOT_READY, "not assembled");
+    GPZ_REQUIRE(F, GPZ_E_INVALID, "null input");
+    GPZ_CUDA_TRY(cudaMemcpyAsync(c.d_f.p, F, c.neq * sizeof(double), cudaMemcpyHostToDevice, c.stream));
+    GPZ_CUDA_TRY(cudaStreamSynchronize(c.stream));
+    return GPZ_OK;
+  });
+}
+
+int gpz_spmv(gpz_ctx *ctx, double alpha, const double *x, double beta, const double *y, double *z) {
+  return guarded(ctx, [&](Ctx &c) {
+    GPZ_REQUIRE(c.have_matrix, GPZ_E_NOT_READY, "not assembled");
+    GPZ_REQUIRE(x && z, GPZ_E_INVALID, "null vector");
+    DBuf<double> dx, dy, dz;
+    dx.upload(x, c.neq, c.stream);
+    if (y && beta != 0.0) dy.upload(y, c.neq, c.stream);
+    dz.alloc(std::max<int64_t>(c.neq, 1));
+    spmv_device(c, dx.p, dz.p, alpha, beta, (y && beta != 0.0) ? dy.p : nullptr);
+    GPZ_CUDA_TRY(cudaMemcpyAsync(z, dz.p, c.neq * sizeof(double), cudaMemcpyDeviceToHost, c.stream));
+    GPZ_CUDA_TRY(cudaStreamSynchronize(c.stream));
+    return GPZ_OK;
+  });
+}
+
+int gpz_solve(gpz_ctx *ctx, const gpz_solver_opts *opts, const double *b, double *x, gpz_solve_report *rep) {
+  return guarded(ctx, [&](Ctx &c) {
+    GPZ_REQUIRE(c.have_matrix, GPZ_E_NOT_READY, "not assembled");
+    GPZ_REQUIRE(opts && opts->max_iter >= 0 && opts->tol >= 0, GPZ_E_INVALID, "options");
+    bool mixed = opts->solver == GPZ_SOLVER_MIXED_CG;
+    solver_prepare(c, mixed);
+    cudaStream_t s = c.stream;
+    if (b) GPZ_CUDA_TRY(cudaMemcpyAsync(c.sw.b.p, b, c.neq * sizeof(double), cudaMemcpyHostToDevice, s));
+    else GPZ_CUDA_TRY(cudaMemcpyAsync(c.sw.b.p, c.d_f.p, c.neq * sizeof(double), cudaMemcpyDeviceToDevice, s));
+    if (opts->from_current) {
+      GPZ_REQUIRE(x, GPZ_E_INVALID, "from_current needs x");
+      GPZ_CUDA_TRY(cudaMemcpyAsync(c.sw.x.p, x, c.neq * sizeof(double), cudaMemcpyHostToDevice, s));
+    }
+    gpz_solve_report r{};
+    int rc = gpz::solve(c, *opts, r);
+    if (x) {
+      GPZ_CUDA_TRY(cudaMemcpyAsync(x, c.sw.x.p, c.neq * sizeof(double), cudaMemcpyDeviceToHost, s));
+      GPZ_CUDA_TRY(cudaStreamSynchronize(s));
+    }
+    if (rep) *rep = r;
+    return rc;
+  });
+}
+
+int gpz_solution_download(gpz_ctx *ctx, double *x) {
+  return guarded(ctx, [&](Ctx &c) {
+    GPZ_REQUIRE(c.have_solution, GPZ_E_NOT_READY, "no solution");
+    GPZ_CUDA_TRY(cudaMemcpyAsync(x, c.sw.x.p, c.neq * sizeof(double), cudaMemcpyDeviceToHost, c.stream));
+    GPZ_CUDA_TRY(cudaStreamSynchronize(c.stream));
+    return GPZ_OK;
+  });
+}
+
+}  // extern "C"

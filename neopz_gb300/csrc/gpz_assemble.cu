@@ -1,0 +1,578 @@
+// Element integration and atomic-free coloured scatter (FP64 parity path).
+//
+// One CTA per element.  Per integration point: the geometric Jacobian from the
+// corner coordinates (TPZGeoEl::Jacobian, Mesh/pzgeoel.cpp:1167-1345), the
+// physical gradients dphix = jacinv^T dphi (Mesh/TPZCompElH1.cpp:139-149) and
+// the weight w |detJ| (Mesh/pzinterpolationspace.cpp:454-470).  Then, per pair
+// of shapes (a <= b), the gradient Gram S_ab = sum_q w_q g_a g_b^T from which the
+// material block is formed (TPZMatPoisson / TPZDarcyFlow / TPZElasticity3D
+// CODE3), and the block plus its transpose are added into the full CSR through
+// the element's block-offset table.  Elements of one colour share no connect,
+// so the read-modify-write needs no atomics.  Entries with |v| < 1e-12 are
+// skipped exactly as TPZSYsmpMatrix::AddKel does (Matrix/pzsysmp.cpp:369-411).
+#include <algorithm>
+#include <cmath>
+#include <map>
+
+#include "gpz_internal.h"
+#include "gpz_shapes.h"
+
+namespace gpz {
+
+bool BucketKey::operator<(const BucketKey &o) const {
+  if (type != o.type) return type < o.type;
+  if (is_bc != o.is_bc) return is_bc < o.is_bc;
+  if (mat_kind != o.mat_kind) return mat_kind < o.mat_kind;
+  if (intorder != o.intorder) return intorder < o.intorder;
+  for (int i = 0; i < 19; i++)
+    if (orders[i] != o.orders[i]) return orders[i] < o.orders[i];
+  for (int i = 0; i < 19; i++)
+    if (trans[i] != o.trans[i]) return trans[i] < o.trans[i];
+  return false;
+}
+
+namespace {
+
+struct ElemArgs {
+  const double *phi, *dphi, *w;
+  const int *sside, *sk;
+  int nq, ncorner, nsides;
+  const double *xyz;
+  const int64_t *el_nodes, *el_conn, *bpos;
+  const int32_t *el_mat;
+  const double *coef;
+  int kind, mdim, forcing, bc_type;
+  double scale, E, nu, coef_const, big;
+  double force[3], val2[3];
+  const int64_t *ia, *offbase;
+  const int32_t *off;
+  double *a, *f;
+  int64_t nnz, neq;
+  int *err;
+};
+
+// Geometric Jacobian at one point: returns |detJ| and fills jinv (row-major dim x dim)
+template <int DIM>
+__device__ double jacobian_at(const double *cx /*[nc][3]*/, const double *dcorner /*[DIM][nc]*/, int nc,
+                              double jinv[3][3]) {
+  double gx[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
+  for (int k = 0; k < nc; k++)
+    for (int j = 0; j < 3; j++)
+      for (int d = 0; d < DIM; d++) gx[j][d] += cx[k * 3 + j] * dcorner[d * 8 + k];
+  double det;
+  if (DIM == 1) {
+    double n = sqrt(gx[0][0] * gx[0][0] + gx[1][0] * gx[1][0] + gx[2][0] * gx[2][0]);
+    det = n;
+    jinv[0][0] = 1.0 / n;
+  } else if (DIM == 2) {
+    double n1 = 0.0, d12 = 0.0, n2 = 0.0;
+    for (int i = 0; i < 3; i++) { n1 += gx[i][0] * gx[i][0]; d12 += gx[i][0] * gx[i][1]; }
+    n1 = sqrt(n1);
+    for (int i = 0; i < 3; i++) {
+      double v = gx[i][1] - d12 * (gx[i][0] / n1) / n1;
+      n2 += v * v;
+    }
+    n2 = sqrt(n2);
+    double j00 = n1, j01 = d12 / n1, j11 = n2;
+    det = j00 * j11;
+    jinv[0][0] = j11 / det;
+    jinv[1][1] = j00 / det;
+    jinv[0][1] = -j01 / det;
+    jinv[1][0] = 0.0;
+  } else {
+    const double(&a)[3][3] = gx;
+    det = -a[0][2] * a[1][1] * a[2][0] + a[0][1] * a[1][2] * a[2][0] + a[0][2] * a[1][0] * a[2][1] -
+          a[0][0] * a[1][2] * a[2][1] - a[0][1] * a[1][0] * a[2][2] + a[0][0] * a[1][1] * a[2][2];
+    jinv[0][0] = (-a[1][2] * a[2][1] + a[1][1] * a[2][2]) / det;
+    jinv[0][1] = (a[0][2] * a[2][1] - a[0][1] * a[2][2]) / det;
+    jinv[0][2] = (-a[0][2] * a[1][1] + a[0][1] * a[1][2]) / det;
+    jinv[1][0] = (a[1][2] * a[2][0] - a[1][0] * a[2][2]) / det;
+    jinv[1][1] = (-a[0][2] * a[2][0] + a[0][0] * a[2][2]) / det;
+    jinv[1][2] = (a[0][2] * a[1][0] - a[0][0] * a[1][2]) / det;
+    jinv[2][0] = (-a[1][1] * a[2][0] + a[1][0] * a[2][1]) / det;
+    jinv[2][1] = (a[0][1] * a[2][0] - a[0][0] * a[2][1]) / det;
+    jinv[2][2] = (-a[0][1] * a[1][0] + a[0][0] * a[1][1]) / det;
+  }
+  return fabs(det);
+}
+
+__device__ __forceinline__ void corner_grad(int nc, int dim, const double *pt, double *phic, double *dc /*[3][8]*/) {
+  // master corners in the reference's node order
+  const signed char sx[8] = {-1, 1, 1, -1, -1, 1, 1, -1}, sy[8] = {-1, -1, 1, 1, -1, -1, 1, 1},
+                    sz[8] = {-1, -1, -1, -1, 1, 1, 1, 1};
+  for (int k = 0; k < nc; k++) {
+    double s[3] = {(double)sx[k], (double)sy[k], (double)sz[k]};
+    if (dim == 1) s[0] = (k == 0) ? -1.0 : 1.0;
+    double f[3], g[3];
+    for (int a = 0; a < dim; a++) { f[a] = (1.0 + s[a] * pt[a]) / 2.0; g[a] = s[a] / 2.0; }
+    double v = 1.0;
+    for (int a = 0; a < dim; a++) v *= f[a];
+    phic[k] = v;
+    for (int a = 0; a < dim; a++) {
+      double d = g[a];
+      for (int b = 0; b < dim; b++)
+        if (b != a) d *= f[b];
+      dc[a * 8 + k] = d;
+    }
+  }
+}
+
+__device__ __forceinline__ void forcing_at(const ElemArgs &P, const double *x, double *fv) {
+  fv[0] = fv[1] = fv[2] = 0.0;
+  if (P.forcing == GPZ_F_CONST) {
+    fv[0] = P.force[0]; fv[1] = P.force[1]; fv[2] = P.force[2];
+  } else if (P.forcing == GPZ_F_SINPROD) {
+    const double pi = 3.141592653589793238462643383279502884;
+    double v = P.force[0] * (P.mdim == 2 ? 2.0 * pi * pi : 3.0 * pi * pi) * sin(pi * x[0]) * sin(pi * x[1]);
+    if (P.mdim == 3) v *= sin(pi * x[2]);
+    fv[0] = v;
+  }
+}
+
+// NSH shapes, DIM element dimension, NST states per shape, BC boundary element
+template <int NSH, int DIM, int NST, bool BC>
+__global__ void __launch_bounds__(128) k_elem_fp64(ElemArgs P, const int64_t *__restrict__ elems, int64_t nelems) {
+  extern __shared__ double sm[];
+  const int nq = P.nq;
+  double *sG = sm;                                    // [nq][NSH][DIM] (volume)
+  double *sW = sG + (BC ? 0 : nq * NSH * DIM);        // [nq]
+  double *sX = sW + nq;                               // [nq][3]
+  double *sC = sX + nq * 3;                           // [8][3] corners
+  int64_t *sRow = (int64_t *)(sC + 24);               // [NSH] first equation of each shape
+  int *sSide = (int *)(sRow + NSH);                   // [NSH]
+  __shared__ double sCoef;
+  __shared__ int64_t sOffBase;
+
+  const int64_t ie = blockIdx.x;
+  if (ie >= nelems) return;
+  const int64_t e = elems[ie];
+  const int tid = threadIdx.x;
+  const int nc = P.ncorner;
+
+  if (tid < nc * 3) {
+    int k = tid / 3, j = tid % 3;
+    int64_t node = P.el_nodes[e * 8 + k];
+    sC[k * 3 + j] = P.xyz[node * 3 + j];
+  }
+  if (tid < NSH) {
+    int side = P.sside[tid];
+    int64_t cn = P.el_conn[e * 27 + side];
+    sRow[tid] = P.bpos[cn] + (int64_t)P.sk[tid] * NST;
+    sSide[tid] = side;
+  }
+  if (tid == 0) {
+    sOffBase = P.offbase[e];
+    double cf = P.kind == GPZ_MAT_ELAST3D ? P.E : P.coef_const;
+    if (!BC && P.coef) cf = P.coef[e];
+    sCoef = cf;
+  }
+  __syncthreads();
+
+  // per-point geometry
+  for (int q = tid; q < nq; q += blockDim.x) {
+    double pt[3] = {0, 0, 0};
+    // reference point recovered from the corner table is not needed: use dcorner at the point
+    // (the bucket tables hold the point implicitly through phi of the corner shapes)
+    double phic[8], dc[3 * 8];
+    // corner shapes are the first nc shapes of the table; their gradients give J
+    for (int k = 0; k < nc; k++) {
+      phic[k] = P.phi[q * NSH + k];
+      for (int d = 0; d < DIM; d++) dc[d * 8 + k] = P.dphi[(q * DIM + d) * NSH + k];
+    }
+    (void)pt;
+    double jinv[3][3];
+    double det = jacobian_at<DIM>(sC, dc, nc, jinv);
+    sW[q] = P.w[q] * det;
+    for (int j = 0; j < 3; j++) {
+      double x = 0.0;
+      for (int k = 0; k < nc; k++) x += phic[k] * sC[k * 3 + j];
+      sX[q * 3 + j] = x;
+    }
+    if (!BC) {
+      // store jinv temporarily in sG is not possible; compute gradients directly
+      for (int a = 0; a < NSH; a++)
+        for (int d = 0; d < DIM; d++) {
+          double g = 0.0;
+          for (int j = 0; j < DIM; j++) g += jinv[j][d] * P.dphi[(q * DIM + j) * NSH + a];
+          sG[(q * NSH + a) * DIM + d] = g;
+        }
+    }
+  }
+  __syncthreads();
+
+  const double coef = sCoef;
+  // ---- load vector
+  for (int idx = tid; idx < NSH * NST; idx += blockDim.x) {
+    int a = idx / NST, s = idx % NST;
+    double acc = 0.0;
+    if (!BC) {
+      for (int q = 0; q < nq; q++) {
+        double fv[3];
+        forcing_at(P, &sX[q * 3], fv);
+        double ph = P.phi[q * NSH + a];
+        if (P.kind == GPZ_MAT_POISSON) acc += sW[q] * P.scale * ph * fv[0];
+        else if (P.kind == GPZ_MAT_DARCY) acc += sW[q] * fv[0] * ph;
+        else acc += sW[q] * (fv[s] * ph);
+      }
+    } else {
+      double m = 0.0;
+      for (int q = 0; q < nq; q++) m += P.phi[q * NSH + a] * sW[q];
+      if (P.bc_type == 0) acc = P.big * P.val2[s] * m;
+      else if (P.bc_type == 1) acc = P.val2[s] * m * (P.kind == GPZ_MAT_POISSON ? P.scale : 1.0);
+    }
+    int64_t row = sRow[a] + s;
+    if (row < 0 || row >= P.neq) {
+      atomicOr(P.err, 16);
+      continue;
+    }
+    P.f[row] += acc;
+  }
+  if (BC && P.bc_type != 0) return;
+
+  // ---- matrix: pairs a <= b
+  double C1 = 0, C2 = 0, C3 = 0;
+  if (!BC && P.kind == GPZ_MAT_ELAST3D) {
+    double E = coef, nu = P.nu;
+    C1 = E / (2. + 2. * nu);
+    C2 = E * nu / (-1. + nu + 2. * nu * nu);
+    C3 = E * (nu - 1.) / (-1. + nu + 2. * nu * nu);
+  }
+  const int ns = P.nsides;
+  for (int idx = tid; idx < NSH * NSH; idx += blockDim.x) {
+    const int a = idx / NSH, b = idx % NSH;
+    if (a > b) continue;
+    double K[NST][NST];
+    if (BC) {
+      double m = 0.0;
+      for (int q = 0; q < nq; q++) m += sW[q] * P.phi[q * NSH + a] * P.phi[q * NSH + b];
+      for (int s = 0; s < NST; s++)
+        for (int t = 0; t < NST; t++) K[s][t] = (s == t) ? P.big * m : 0.0;
+    } else if (NST == 1) {
+      double acc = 0.0;
+      for (int q = 0; q < nq; q++) {
+        const double *ga = &sG[(q * NSH + a) * DIM], *gb = &sG[(q * NSH + b) * DIM];
+        double d = 0.0;
+        for (int x = 0; x < DIM; x++) d += ga[x] * gb[x];
+        acc += sW[q] * d;
+      }
+      K[0][0] = (P.kind == GPZ_MAT_POISSON ? P.scale : coef) * acc;
+    } else {
+      double S[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
+      for (int q = 0; q < nq; q++) {
+        const double *ga = &sG[(q * NSH + a) * DIM], *gb = &sG[(q * NSH + b) * DIM];
+        const double w = sW[q];
+        double wa0 = w * ga[0], wa1 = w * ga[1], wa2 = w * ga[2];
+        S[0][0] += wa0 * gb[0]; S[0][1] += wa0 * gb[1]; S[0][2] += wa0 * gb[2];
+        S[1][0] += wa1 * gb[0]; S[1][1] += wa1 * gb[1]; S[1][2] += wa1 * gb[2];
+        S[2][0] += wa2 * gb[0]; S[2][1] += wa2 * gb[1]; S[2][2] += wa2 * gb[2];
+      }
+      double tr = S[0][0] + S[1][1] + S[2][2];
+      for (int s = 0; s < NST; s++)
+        for (int t = 0; t < NST; t++)
+          K[s][t] = (s == t) ? (tr - S[s][s]) * C1 + S[s][s] * C3 : S[t][s] * C1 - S[s][t] * C2;
+    }
+    // scatter the (a,b) block and, off the diagonal, its transpose into (b,a)
+    const int sa = sSide[a], sb = sSide[b];
+    const int32_t oab = P.off[sOffBase + sa * ns + sb];
+    const int32_t oba = P.off[sOffBase + sb * ns + sa];
+    if (oab < 0 || oba < 0) {
+      atomicOr(P.err, 32);
+      continue;
+    }
+    const int ka = P.sk[a] * NST, kb = P.sk[b] * NST;
+    for (int s = 0; s < NST; s++) {
+      const int64_t ra = sRow[a] + s;
+      const int64_t base = P.ia[ra] + oab + kb;
+      for (int t = 0; t < NST; t++) {
+        double v = K[s][t];
+        if (fabs(v) < 1.e-12) continue;
+        int64_t slot = base + t;
+        if (slot < 0 || slot >= P.nnz) {
+          atomicOr(P.err, 64);
+          continue;
+        }
+        P.a[slot] += v;
+      }
+    }
+    if (a != b) {
+      for (int t = 0; t < NST; t++) {
+        const int64_t rb = sRow[b] + t;
+        const int64_t base = P.ia[rb] + oba + ka;
+        for (int s = 0; s < NST; s++) {
+          double v = K[s][t];
+          if (fabs(v) < 1.e-12) continue;
+          int64_t slot = base + s;
+          if (slot < 0 || slot >= P.nnz) {
+            atomicOr(P.err, 64);
+            continue;
+          }
+          P.a[slot] += v;
+        }
+      }
+    }
+  }
+}
+
+size_t smem_bytes(int nsh, int dim, int nq, bool bc) {
+  size_t d = (bc ? 0 : (size_t)nq * nsh * dim) + nq + (size_t)nq * 3 + 24;
+  return d * sizeof(double) + (size_t)nsh * (sizeof(int64_t) + sizeof(int)) + 16;
+}
+
+typedef void (*ElemKernel)(ElemArgs, const int64_t *, int64_t);
+
+template <int NSH, int DIM, int NST, bool BC>
+ElemKernel pick() {
+  return k_elem_fp64<NSH, DIM, NST, BC>;
+}
+
+ElemKernel select_kernel(int type, int nshape, int nstate, bool bc) {
+  // volume hexes (3D) and quads (2D); boundary quads (3D faces) and lines (2D edges)
+  if (type == GPZ_EL_HEX && !bc) {
+    if (nstate == 1) {
+      if (nshape == 8) return pick<8, 3, 1, false>();
+      if (nshape == 27) return pick<27, 3, 1, false>();
+      if (nshape == 64) return pick<64, 3, 1, false>();
+    } else {
+      if (nshape == 8) return pick<8, 3, 3, false>();
+      if (nshape == 27) return pick<27, 3, 3, false>();
+      if (nshape == 64) return pick<64, 3, 3, false>();
+    }
+  }
+  if (type == GPZ_EL_QUAD && !bc && nstate == 1) {
+    if (nshape == 4) return pick<4, 2, 1, false>();
+    if (nshape == 9) return pick<9, 2, 1, false>();
+    if (nshape == 16) return pick<16, 2, 1, false>();
+  }
+  if (type == GPZ_EL_QUAD && bc) {
+    if (nstate == 1) {
+      if (nshape == 4) return pick<4, 2, 1, true>();
+      if (nshape == 9) return pick<9, 2, 1, true>();
+      if (nshape == 16) return pick<16, 2, 1, true>();
+    } else {
+      if (nshape == 4) return pick<4, 2, 3, true>();
+      if (nshape == 9) return pick<9, 2, 3, true>();
+      if (nshape == 16) return pick<16, 2, 3, true>();
+    }
+  }
+  if (type == GPZ_EL_LINE && bc && nstate == 1) {
+    if (nshape == 2) return pick<2, 1, 1, true>();
+    if (nshape == 3) return pick<3, 1, 1, true>();
+    if (nshape == 4) return pick<4, 1, 1, true>();
+  }
+  return nullptr;
+}
+
+__global__ void k_extract_diag(const double *__restrict__ a, const int64_t *__restrict__ diagpos, int64_t neq,
+                               double *__restrict__ dinv) {
+  int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (r < neq) dinv[r] = 1.0 / a[diagpos[r]];
+}
+
+__global__ void k_to_fp32(const double *__restrict__ a, float *__restrict__ b, int64_t n) {
+  int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (; i < n; i += stride) b[i] = (float)a[i];
+}
+
+}  // namespace
+
+void build_buckets(Ctx &c, const gpz_mesh_desc &d) {
+  for (Bucket *b : c.buckets) delete b;
+  c.buckets.clear();
+  std::map<BucketKey, int> index;
+  std::vector<int> el_bucket(c.nel, -1);
+  for (int64_t e = 0; e < c.nel; e++) {
+    BucketKey k{};
+    k.type = d.el_type[e];
+    GPZ_REQUIRE(k.type == GPZ_EL_LINE || k.type == GPZ_EL_QUAD || k.type == GPZ_EL_HEX, GPZ_E_UNSUPPORTED_ELEMENT,
+                "element type");
+    const ElemTopo &t = topo(k.type);
+    k.is_bc = d.el_mat[e] < 0;
+    const gpz_material *m;
+    if (k.is_bc) {
+      int ib = -d.el_mat[e] - 1;
+      GPZ_REQUIRE(ib < d.nbc, GPZ_E_INVALID, "bc index");
+      int im = d.bcs[ib].material;
+      GPZ_REQUIRE(im >= 0 && im < d.nmat, GPZ_E_INVALID, "bc material index");
+      m = &d.mats[im];
+      GPZ_REQUIRE(d.bcs[ib].type == 0 || d.bcs[ib].type == 1, GPZ_E_UNSUPPORTED_MATERIAL, "bc type");
+    } else {
+      GPZ_REQUIRE(d.el_mat[e] < d.nmat, GPZ_E_INVALID, "material index");
+      m = &d.mats[d.el_mat[e]];
+    }
+    k.mat_kind = m->kind;
+    GPZ_REQUIRE(m->kind == GPZ_MAT_POISSON || m->kind == GPZ_MAT_DARCY || m->kind == GPZ_MAT_ELAST3D,
+                GPZ_E_UNSUPPORTED_MATERIAL, "material kind");
+    int p = d.el_order[e];
+    if (k.is_bc || m->kind == GPZ_MAT_ELAST3D) k.intorder = 2 * p;
+    else k.intorder = (p < m->forcing_porder) ? m->forcing_porder + p : 2 * p;
+    for (int s = t.ncorner; s < t.nsides; s++) {
+      int64_t cn = d.el_conn[e * 27 + s];
+      int o = d.conn_order[cn];
+      k.orders[s - t.ncorner] = o;
+      k.trans[s - t.ncorner] = side_nshape(k.type, s, o) > 1 ? side_orientation(k.type, s, &d.el_nodes[e * 8]) : 0;
+    }
+    auto it = index.find(k);
+    int bi;
+    if (it == index.end()) {
+      bi = (int)c.buckets.size();
+      index[k] = bi;
+      Bucket *b = new Bucket();
+      b->key = k;
+      b->nsides = t.nsides;
+      b->ncorner = t.ncorner;
+      b->dim = t.dim;
+      b->nstate = c.nstate;
+      std::vector<double> pts;
+      gauss_rule(k.type, k.intorder, pts, b->w);
+      b->nq = (int)b->w.size();
+      GPZ_REQUIRE(b->nq <= kMaxQp, GPZ_E_UNSUPPORTED_ELEMENT, "too many integration points");
+      double phi[kMaxShapes], dphi[3 * kMaxShapes];
+      int so[kMaxShapes], sk[kMaxShapes];
+      for (int q = 0; q < b->nq; q++) {
+        int n = eval_shapes(k.type, k.orders, k.trans, &pts[q * t.dim], phi, dphi, kMaxShapes, so, sk);
+        if (q == 0) {
+          b->nshape = n;
+          b->shape_side.assign(so, so + n);
+          b->shape_k.assign(sk, sk + n);
+          b->phi.resize((size_t)b->nq * n);
+          b->dphi.resize((size_t)b->nq * t.dim * n);
+        }
+        for (int a = 0; a < n; a++) {
+          b->phi[q * n + a] = phi[a];
+          for (int dd = 0; dd < t.dim; dd++) b->dphi[(q * t.dim + dd) * n + a] = dphi[dd * kMaxShapes + a];
+        }
+      }
+      b->ndof = b->nshape * c.nstate;
+      GPZ_REQUIRE(select_kernel(k.type, b->nshape, c.nstate, k.is_bc) != nullptr, GPZ_E_UNSUPPORTED_ELEMENT,
+                  "no kernel for this element bucket");
+      c.buckets.push_back(b);
+    } else {
+      bi = it->second;
+    }
+    el_bucket[e] = bi;
+  }
+  // greedy first-fit colouring by shared non-empty connects (the idea of
+  // TPZStructMatrix::ComputeElementColors, StrMatrix/TPZStructMatrix.cpp:104-161)
+  std::vector<uint64_t> used(c.nconnects, 0);
+  std::vector<int> colour(c.nel, 0);
+  int ncol = 0;
+  for (int64_t e = 0; e < c.nel; e++) {
+    int ns = topo(d.el_type[e]).nsides;
+    uint64_t mask = 0;
+    for (int s = 0; s < ns; s++) {
+      int64_t cn = d.el_conn[e * 27 + s];
+      if (d.block_size[cn] > 0) mask |= used[cn];
+    }
+    GPZ_REQUIRE(~mask != 0, GPZ_E_INVALID, "more than 64 element colours");
+    int col = __builtin_ctzll(~mask);
+    colour[e] = col;
+    ncol = std::max(ncol, col + 1);
+    for (int s = 0; s < ns; s++) {
+      int64_t cn = d.el_conn[e * 27 + s];
+      if (d.block_size[cn] > 0) used[cn] |= (1ull << col);
+    }
+  }
+  c.ncolours = ncol;
+  for (Bucket *b : c.buckets) b->colour_begin.assign(ncol + 1, 0);
+  for (int64_t e = 0; e < c.nel; e++) c.buckets[el_bucket[e]]->colour_begin[colour[e] + 1]++;
+  for (Bucket *b : c.buckets) {
+    for (int k = 0; k < ncol; k++) b->colour_begin[k + 1] += b->colour_begin[k];
+    b->elems.assign(b->colour_begin[ncol], 0);
+  }
+  std::vector<std::vector<int64_t>> fillpos(c.buckets.size());
+  for (size_t i = 0; i < c.buckets.size(); i++)
+    fillpos[i].assign(c.buckets[i]->colour_begin.begin(), c.buckets[i]->colour_begin.end() - 1);
+  for (int64_t e = 0; e < c.nel; e++) {
+    int bi = el_bucket[e];
+    c.buckets[bi]->elems[fillpos[bi][colour[e]]++] = e;
+  }
+  for (Bucket *b : c.buckets) {
+    b->d_phi.upload(b->phi.data(), b->phi.size(), c.stream);
+    b->d_dphi.upload(b->dphi.data(), b->dphi.size(), c.stream);
+    b->d_w.upload(b->w.data(), b->w.size(), c.stream);
+    b->d_shape_side.upload(b->shape_side.data(), b->shape_side.size(), c.stream);
+    b->d_shape_k.upload(b->shape_k.data(), b->shape_k.size(), c.stream);
+    b->d_elems.upload(b->elems.data(), b->elems.size(), c.stream);
+  }
+  GPZ_CUDA_TRY(cudaStreamSynchronize(c.stream));
+}
+
+void assemble_fp64(Ctx &c) {
+  cudaStream_t s = c.stream;
+  c.d_a.alloc(std::max<int64_t>(c.nnz, 1));
+  c.d_f.alloc(std::max<int64_t>(c.neq, 1));
+  c.d_a.zero(s);
+  c.d_f.zero(s);
+  for (int col = 0; col < c.ncolours; col++) {
+    for (Bucket *b : c.buckets) {
+      int64_t e0 = b->colour_begin[col], e1 = b->colour_begin[col + 1];
+      if (e1 == e0) continue;
+      ElemArgs P{};
+      P.phi = b->d_phi.p;
+      P.dphi = b->d_dphi.p;
+      P.w = b->d_w.p;
+      P.sside = b->d_shape_side.p;
+      P.sk = b->d_shape_k.p;
+      P.nq = b->nq;
+      P.ncorner = b->ncorner;
+      P.nsides = b->nsides;
+      P.xyz = c.d_xyz.p;
+      P.el_nodes = c.d_el_nodes.p;
+      P.el_conn = c.d_el_conn.p;
+      P.bpos = c.d_block_pos.p;
+      P.el_mat = c.d_el_mat.p;
+      P.coef = c.d_coef.p;
+      int64_t e_any = b->elems[e0];
+      int mi = c.h_el_mat[e_any];
+      const gpz_material *m;
+      if (mi < 0) {
+        const gpz_bc &bc = c.bcs[-mi - 1];
+        m = &c.mats[bc.material];
+        P.bc_type = bc.type;
+        for (int k = 0; k < 3; k++) P.val2[k] = bc.val2[k];
+      } else {
+        m = &c.mats[mi];
+      }
+      P.kind = m->kind;
+      P.mdim = m->dim;
+      P.forcing = m->forcing;
+      P.scale = m->scale;
+      P.E = m->E;
+      P.nu = m->nu;
+      P.coef_const = m->coef_const;
+      P.big = m->kind == GPZ_MAT_ELAST3D ? 1.e12 : m->bignumber;  // TPZElasticity3D.cpp:632
+      for (int k = 0; k < 3; k++) P.force[k] = m->force[k];
+      P.ia = c.d_ia.p;
+      P.offbase = c.d_offbase.p;
+      P.off = c.d_off.p;
+      P.a = c.d_a.p;
+      P.f = c.d_f.p;
+      P.nnz = c.nnz;
+      P.neq = c.neq;
+      P.err = c.d_err.p;
+      ElemKernel k = select_kernel(b->key.type, b->nshape, c.nstate, b->key.is_bc);
+      size_t sh = smem_bytes(b->nshape, b->dim, b->nq, b->key.is_bc);
+      if (sh > 48 * 1024) GPZ_CUDA_TRY(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sh));
+      k<<<(unsigned)(e1 - e0), 128, sh, s>>>(P, b->d_elems.p + e0, e1 - e0);
+      c.launches++;
+      GPZ_CUDA_TRY(cudaGetLastError());
+    }
+  }
+  c.d_dinv.alloc(std::max<int64_t>(c.neq, 1));
+  k_extract_diag<<<grid_for(c.neq, 256), 256, 0, s>>>(c.d_a.p, c.d_diagpos.p, c.neq, c.d_dinv.p);
+  c.launches++;
+  GPZ_CUDA_TRY(cudaGetLastError());
+  c.have_a32 = false;
+  c.have_bjinv = false;
+}
+
+void make_fp32_copy(Ctx &c) {
+  c.d_a32.alloc(std::max<int64_t>(c.nnz, 1));
+  k_to_fp32<<<152 * 8, 256, 0, c.stream>>>(c.d_a.p, c.d_a32.p, c.nnz);
+  c.launches++;
+  GPZ_CUDA_TRY(cudaGetLastError());
+  c.have_a32 = true;
+}
+
+}  // namespace gpz

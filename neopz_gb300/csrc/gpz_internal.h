@@ -1,0 +1,176 @@
+// Internal declarations of libgpz (the sm_103a implementation behind include/gpz.h).
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <string>
+#include <vector>
+
+#include "../../include/gpz.h"
+
+namespace gpz {
+
+// ---------------------------------------------------------------- errors
+struct Error {
+  int code;
+  std::string msg;
+};
+
+#define GPZ_CUDA_TRY(expr)                                                                  \
+  do {                                                                                      \
+    cudaError_t _e = (expr);                                                                \
+    if (_e != cudaSuccess) {                                                                \
+      throw ::gpz::Error{_e == cudaErrorMemoryAllocation ? GPZ_E_NOMEM : GPZ_E_CUDA,        \
+                         std::string(#expr) + ": " + cudaGetErrorString(_e)};               \
+    }                                                                                       \
+  } while (0)
+
+#define GPZ_REQUIRE(cond, code, text)                  \
+  do {                                                 \
+    if (!(cond)) throw ::gpz::Error{(code), (text)};   \
+  } while (0)
+
+// ---------------------------------------------------------------- device buffers
+template <class T>
+struct DBuf {
+  T *p = nullptr;
+  size_t n = 0;
+  DBuf() = default;
+  DBuf(const DBuf &) = delete;
+  DBuf &operator=(const DBuf &) = delete;
+  ~DBuf() { release(); }
+  void release() {
+    if (p) cudaFree(p);
+    p = nullptr;
+    n = 0;
+  }
+  void alloc(size_t count) {
+    if (count == n && p) return;
+    release();
+    if (count == 0) return;
+    GPZ_CUDA_TRY(cudaMalloc((void **)&p, count * sizeof(T)));
+    n = count;
+  }
+  void upload(const T *h, size_t count, cudaStream_t s) {
+    alloc(count);
+    if (count) GPZ_CUDA_TRY(cudaMemcpyAsync(p, h, count * sizeof(T), cudaMemcpyHostToDevice, s));
+  }
+  void zero(cudaStream_t s) {
+    if (n) GPZ_CUDA_TRY(cudaMemsetAsync(p, 0, n * sizeof(T), s));
+  }
+};
+
+// ---------------------------------------------------------------- element buckets
+// Elements that share element type, side orders, side orientations, material
+// kind and role (volume / boundary) share their shape tables and their kernel.
+constexpr int kMaxShapes = 64;   // hex p=3: 64 scalar shapes
+constexpr int kMaxQp = 64;       // hex 4x4x4 Gauss points
+
+struct BucketKey {
+  int type, is_bc, mat_kind, intorder;
+  int orders[19];      // order of each non-corner side
+  int trans[19];       // orientation id of each non-corner side (0 when irrelevant)
+  bool operator<(const BucketKey &o) const;
+};
+
+struct Bucket {
+  BucketKey key;
+  int nsides = 0, ncorner = 0, dim = 0, nshape = 0, nq = 0, nstate = 1, ndof = 0;
+  // host tables
+  std::vector<double> phi, dphi, w;          // [nq][nshape], [nq][dim][nshape], [nq]
+  std::vector<int> shape_side, shape_k;      // shape -> side, index inside the side
+  // device tables
+  DBuf<double> d_phi, d_dphi, d_w;
+  DBuf<int> d_shape_side, d_shape_k;
+  // elements of this bucket grouped by colour
+  std::vector<int64_t> elems;                // global element indices
+  std::vector<int64_t> colour_begin;         // [ncolours+1]
+  DBuf<int64_t> d_elems;
+};
+
+// ---------------------------------------------------------------- solver workspace
+struct SolverWork {
+  DBuf<double> r, z, p, q, x, b, t;
+  DBuf<float> p32;
+  DBuf<double> partial;        // per-CTA partial sums
+  DBuf<double> scal;           // device scalars (see gpz_solver.cu)
+  DBuf<unsigned int> counter;  // last-block counters
+  DBuf<int64_t> iscal;         // device integer scalars
+  size_t nblk = 0;
+};
+
+// ---------------------------------------------------------------- the context
+struct Ctx {
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  std::string last_error;
+  int64_t launches = 0;
+
+  // mesh
+  bool have_mesh = false;
+  int dim = 0, nstate = 1;
+  int64_t nel = 0, nnodes = 0, nconnects = 0, neq = 0;
+  std::vector<gpz_material> mats;
+  std::vector<gpz_bc> bcs;
+  std::vector<int32_t> h_el_type, h_el_mat;
+  std::vector<int64_t> h_el_conn;            // [nel][27]
+  std::vector<int64_t> h_block_pos;
+  std::vector<int32_t> h_block_size;
+  DBuf<double> d_xyz, d_coef;
+  DBuf<int64_t> d_el_nodes, d_el_conn, d_block_pos;
+  DBuf<int32_t> d_el_type, d_el_mat, d_block_size, d_conn_order;
+  std::vector<Bucket *> buckets;
+  int ncolours = 0;
+  DBuf<int> d_err;                           // device-side check flag
+
+  // pattern (always the full CSR; the upper triangle is derived when requested)
+  bool have_pattern = false;
+  int user_sym = 0;
+  int64_t nnz = 0, nnz_upper = 0;
+  DBuf<int64_t> d_ia;                        // [neq+1]
+  DBuf<int32_t> d_ja;                        // [nnz]
+  DBuf<int64_t> d_ia_up;
+  DBuf<int32_t> d_ja_up;
+  DBuf<int64_t> d_diagpos;                   // [neq] slot of the diagonal entry
+  DBuf<int64_t> d_offbase;                   // [nel] start of the element's offset table
+  DBuf<int32_t> d_off;                       // element side-pair offsets inside a block row
+
+  // values
+  bool have_matrix = false;
+  DBuf<double> d_a, d_f, d_dinv;
+  DBuf<float> d_a32;                         // FP32 copy for the inner solves
+  bool have_a32 = false;
+  DBuf<double> d_bjinv;                      // block-Jacobi inverses [nconnects][bs*bs]
+  bool have_bjinv = false;
+  int bj_bs = 0;
+
+  SolverWork sw;
+  bool have_solution = false;
+
+  ~Ctx();
+};
+
+// pattern.cu
+void build_pattern(Ctx &c);
+void build_upper(Ctx &c);
+void build_element_offsets(Ctx &c);
+// assemble.cu
+void build_buckets(Ctx &c, const gpz_mesh_desc &d);
+void assemble_fp64(Ctx &c);
+void make_fp32_copy(Ctx &c);
+void build_block_jacobi(Ctx &c);
+// solver.cu
+void spmv_device(Ctx &c, const double *x, double *y, double alpha, double beta, const double *yin);
+int solve(Ctx &c, const gpz_solver_opts &o, gpz_solve_report &rep);
+// scan.cu
+void exclusive_scan_i64(const int64_t *in, int64_t *out, int64_t n, cudaStream_t s, Ctx &c);
+void check_device_flag(Ctx &c, const char *where);
+
+inline int grid_for(int64_t n, int threads) {
+  int64_t g = (n + threads - 1) / threads;
+  if (g < 1) g = 1;
+  if (g > 2147483647LL) g = 2147483647LL;
+  return (int)g;
+}
+
+}  // namespace gpz

@@ -1,0 +1,322 @@
+"""ctypes binding of the C ABI (include/gpz.h) and of the host grid builder.
+
+This is the Python face of the product used by the benchmark and the tests;
+every numerical operation runs in libgpz.so on the GPU.  Loading fails loudly
+when the shared libraries have not been built, and creating a context fails
+when no CUDA device is visible: there is no CPU path.
+"""
+import ctypes
+import os
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIBGPZ = os.path.join(_HERE, "_build", "libgpz.so")
+LIBHOST = os.path.join(_HERE, "_build", "libgpzhost.so")
+
+GPZ_OK, GPZ_NOT_CONVERGED = 0, 1
+GPZ_EL_LINE, GPZ_EL_QUAD, GPZ_EL_HEX = 1, 2, 3
+GPZ_MAT_POISSON, GPZ_MAT_DARCY, GPZ_MAT_ELAST3D = 1, 2, 3
+GPZ_F_NONE, GPZ_F_CONST, GPZ_F_SINPROD = 0, 1, 2
+GPZ_PREC_FP64, GPZ_PREC_MIXED = 0, 1
+GPZ_SOLVER_CG, GPZ_SOLVER_GMRES, GPZ_SOLVER_MIXED_CG, GPZ_SOLVER_LEARNED_FCG = 1, 2, 3, 4
+GPZ_PRECOND_JACOBI, GPZ_PRECOND_BLOCK_JACOBI = 1, 2
+BIGNUMBER = 10.0 ** 17 * 2 / 3  # TPZMaterial::fBigNumber default for double
+
+
+class gpz_material(ctypes.Structure):
+    _fields_ = [("kind", ctypes.c_int32), ("dim", ctypes.c_int32), ("scale", ctypes.c_double),
+                ("E", ctypes.c_double), ("nu", ctypes.c_double), ("coef_const", ctypes.c_double),
+                ("force", ctypes.c_double * 3), ("forcing", ctypes.c_int32), ("forcing_porder", ctypes.c_int32),
+                ("bignumber", ctypes.c_double)]
+
+
+class gpz_bc(ctypes.Structure):
+    _fields_ = [("type", ctypes.c_int32), ("material", ctypes.c_int32), ("val1", ctypes.c_double * 9),
+                ("val2", ctypes.c_double * 3)]
+
+
+_P = ctypes.POINTER
+
+
+class gpz_mesh_desc(ctypes.Structure):
+    _fields_ = [("dim", ctypes.c_int32), ("nstate", ctypes.c_int32), ("nnodes", ctypes.c_int64),
+                ("node_xyz", _P(ctypes.c_double)), ("nel", ctypes.c_int64), ("el_type", _P(ctypes.c_int32)),
+                ("el_mat", _P(ctypes.c_int32)), ("el_nodes", _P(ctypes.c_int64)), ("el_order", _P(ctypes.c_int32)),
+                ("el_conn", _P(ctypes.c_int64)), ("el_coef", _P(ctypes.c_double)), ("nconnects", ctypes.c_int64),
+                ("conn_order", _P(ctypes.c_int32)), ("block_pos", _P(ctypes.c_int64)),
+                ("block_size", _P(ctypes.c_int32)), ("neq", ctypes.c_int64), ("nmat", ctypes.c_int32),
+                ("mats", _P(gpz_material)), ("nbc", ctypes.c_int32), ("bcs", _P(gpz_bc))]
+
+
+class gpz_solver_opts(ctypes.Structure):
+    _fields_ = [("solver", ctypes.c_int32), ("precond", ctypes.c_int32), ("max_iter", ctypes.c_int64),
+                ("tol", ctypes.c_double), ("gmres_krylov", ctypes.c_int32), ("check_every", ctypes.c_int32),
+                ("reliable_delta", ctypes.c_double), ("use_graph", ctypes.c_int32), ("from_current", ctypes.c_int32)]
+
+
+class gpz_solve_report(ctypes.Structure):
+    _fields_ = [("iterations", ctypes.c_int64), ("resid", ctypes.c_double), ("true_resid", ctypes.c_double),
+                ("seconds", ctypes.c_double), ("spmv_fp64", ctypes.c_int64), ("spmv_fp32", ctypes.c_int64),
+                ("reliable_updates", ctypes.c_int64)]
+
+
+class gpzh_grid_spec(ctypes.Structure):
+    _fields_ = [("dim", ctypes.c_int32), ("ndiv", ctypes.c_int32 * 3), ("minX", ctypes.c_double * 3),
+                ("maxX", ctypes.c_double * 3), ("matids", ctypes.c_int32 * 7), ("create_bc", ctypes.c_int32),
+                ("default_order", ctypes.c_int32), ("nmat", ctypes.c_int32), ("mat_id", ctypes.c_int32 * 4),
+                ("mats", gpz_material * 4), ("nbc", ctypes.c_int32), ("bc_id", ctypes.c_int32 * 8),
+                ("bcs", gpz_bc * 8), ("elem_coef", _P(ctypes.c_double)), ("elem_order", _P(ctypes.c_int32))]
+
+
+class GpzError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__(f"gpz error {code}: {msg}")
+        self.code = code
+
+
+_lib = None
+_host = None
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIBGPZ):
+            raise ImportError(f"{LIBGPZ} is not built: run `python -c 'import __graft_entry__ as g; g.build()'`")
+        L = ctypes.CDLL(LIBGPZ)
+        vp, i64, i32, dp = ctypes.c_void_p, ctypes.c_int64, ctypes.c_int, ctypes.c_double
+        L.gpz_ctx_create.argtypes = [_P(vp), i32]
+        L.gpz_ctx_destroy.argtypes = [vp]
+        L.gpz_get_error_string.restype = ctypes.c_char_p
+        L.gpz_get_error_string.argtypes = [i32]
+        L.gpz_last_error_detail.restype = ctypes.c_char_p
+        L.gpz_last_error_detail.argtypes = [vp]
+        L.gpz_ctx_stream.restype = vp
+        L.gpz_ctx_stream.argtypes = [vp]
+        L.gpz_kernel_launches.restype = i64
+        L.gpz_kernel_launches.argtypes = [vp]
+        L.gpz_mesh_upload.argtypes = [vp, _P(gpz_mesh_desc)]
+        L.gpz_pattern_build.argtypes = [vp, i32, _P(i64)]
+        L.gpz_pattern_upload.argtypes = [vp, i32, i64, vp, vp]
+        L.gpz_pattern_download.argtypes = [vp, vp, vp]
+        L.gpz_assemble.argtypes = [vp, i32]
+        L.gpz_matrix_download.argtypes = [vp, vp]
+        L.gpz_rhs_download.argtypes = [vp, vp]
+        L.gpz_rhs_upload.argtypes = [vp, vp]
+        L.gpz_spmv.argtypes = [vp, dp, vp, dp, vp, vp]
+        L.gpz_solve.argtypes = [vp, _P(gpz_solver_opts), vp, vp, _P(gpz_solve_report)]
+        L.gpz_solution_download.argtypes = [vp, vp]
+        _lib = L
+    return _lib
+
+
+def host():
+    global _host
+    if _host is None:
+        lib()
+        if not os.path.exists(LIBHOST):
+            raise ImportError(f"{LIBHOST} is not built")
+        H = ctypes.CDLL(LIBHOST)
+        vp, i64 = ctypes.c_void_p, ctypes.c_int64
+        H.gpzh_grid_build.restype = vp
+        H.gpzh_grid_build.argtypes = [_P(gpzh_grid_spec)]
+        H.gpzh_grid_free.argtypes = [vp]
+        H.gpzh_grid_desc.argtypes = [vp, _P(gpz_mesh_desc)]
+        for f in ("gpzh_grid_neq", "gpzh_grid_nel", "gpzh_grid_nvol"):
+            getattr(H, f).restype = i64
+            getattr(H, f).argtypes = [vp]
+        H.gpzh_grid_dest.restype = ctypes.c_int
+        H.gpzh_grid_dest.argtypes = [vp, i64, vp]
+        _host = H
+    return _host
+
+
+def _p(a):
+    return None if a is None else a.ctypes.data_as(ctypes.c_void_p)
+
+
+def material(kind, dim, scale=1.0, E=1.0, nu=0.3, coef_const=1.0, force=(0.0, 0.0, 0.0), forcing=GPZ_F_NONE,
+             forcing_porder=0, bignumber=BIGNUMBER):
+    m = gpz_material()
+    m.kind, m.dim, m.scale, m.E, m.nu, m.coef_const = kind, dim, scale, E, nu, coef_const
+    for i in range(3):
+        m.force[i] = force[i]
+    m.forcing, m.forcing_porder, m.bignumber = forcing, forcing_porder, bignumber
+    return m
+
+
+def bc(type, material_index, val2=(0.0, 0.0, 0.0)):
+    b = gpz_bc()
+    b.type, b.material = type, material_index
+    for i in range(3):
+        b.val2[i] = val2[i]
+    return b
+
+
+class Grid:
+    """A computational mesh on a grid domain built by the host library (pz_grid.cpp)."""
+
+    def __init__(self, dim, ndiv, minX, maxX, matids, create_bc, order, mats, bcs, elem_coef=None,
+                 elem_order=None):
+        H = host()
+        s = gpzh_grid_spec()
+        s.dim = dim
+        for i in range(3):
+            s.ndiv[i] = ndiv[i] if i < len(ndiv) else 1
+            s.minX[i], s.maxX[i] = minX[i], maxX[i]
+        for i, m in enumerate(matids):
+            s.matids[i] = m
+        s.create_bc, s.default_order = int(create_bc), order
+        s.nmat = len(mats)
+        for i, (mid, m) in enumerate(mats):
+            s.mat_id[i], s.mats[i] = mid, m
+        s.nbc = len(bcs)
+        for i, (bid, b) in enumerate(bcs):
+            s.bc_id[i], s.bcs[i] = bid, b
+        self._coef = None if elem_coef is None else np.ascontiguousarray(elem_coef, np.float64)
+        self._order = None if elem_order is None else np.ascontiguousarray(elem_order, np.int32)
+        if self._coef is not None:
+            s.elem_coef = self._coef.ctypes.data_as(_P(ctypes.c_double))
+        if self._order is not None:
+            s.elem_order = self._order.ctypes.data_as(_P(ctypes.c_int32))
+        self.h = H.gpzh_grid_build(ctypes.byref(s))
+        if not self.h:
+            raise GpzError(-3, "grid build failed")
+        self.neq = H.gpzh_grid_neq(self.h)
+        self.nel = H.gpzh_grid_nel(self.h)
+        self.nvol = H.gpzh_grid_nvol(self.h)
+        self.desc = gpz_mesh_desc()
+        H.gpzh_grid_desc(self.h, ctypes.byref(self.desc))
+
+    def dest(self, e):
+        d = np.zeros(64 * 3 * 27, np.int64)
+        n = host().gpzh_grid_dest(self.h, e, _p(d))
+        return d[:n].copy()
+
+    def __del__(self):
+        if getattr(self, "h", None):
+            host().gpzh_grid_free(self.h)
+            self.h = None
+
+
+class Context:
+    """One gpz context (one CUDA stream, its device buffers)."""
+
+    def __init__(self, device=0):
+        L = lib()
+        h = ctypes.c_void_p()
+        rc = L.gpz_ctx_create(ctypes.byref(h), device)
+        if rc != GPZ_OK:
+            raise GpzError(rc, L.gpz_get_error_string(rc).decode())
+        self.h = h
+        self.neq = 0
+        self.nnz = 0
+
+    def _check(self, rc, allow=()):
+        if rc != GPZ_OK and rc not in allow:
+            L = lib()
+            raise GpzError(rc, L.gpz_get_error_string(rc).decode() + ": " + L.gpz_last_error_detail(self.h).decode())
+        return rc
+
+    def close(self):
+        if getattr(self, "h", None):
+            lib().gpz_ctx_destroy(self.h)
+            self.h = None
+
+    __del__ = close
+
+    @property
+    def stream(self):
+        return lib().gpz_ctx_stream(self.h)
+
+    def launches(self):
+        return lib().gpz_kernel_launches(self.h)
+
+    def upload_mesh(self, grid):
+        self._grid = grid
+        self._check(lib().gpz_mesh_upload(self.h, ctypes.byref(grid.desc)))
+        self.neq = grid.neq
+
+    def build_pattern(self, sym):
+        nnz = ctypes.c_int64()
+        self._check(lib().gpz_pattern_build(self.h, int(sym), ctypes.byref(nnz)))
+        self.nnz = nnz.value
+        return self.nnz
+
+    def pattern(self):
+        ia = np.zeros(self.neq + 1, np.int64)
+        ja = np.zeros(self.nnz, np.int64)
+        self._check(lib().gpz_pattern_download(self.h, _p(ia), _p(ja)))
+        return ia, ja
+
+    def assemble(self, precision=GPZ_PREC_FP64):
+        self._check(lib().gpz_assemble(self.h, precision))
+
+    def matrix(self):
+        a = np.zeros(self.nnz)
+        self._check(lib().gpz_matrix_download(self.h, _p(a)))
+        return a
+
+    def rhs(self):
+        f = np.zeros(self.neq)
+        self._check(lib().gpz_rhs_download(self.h, _p(f)))
+        return f
+
+    def spmv(self, x, alpha=1.0, beta=0.0, y=None):
+        z = np.zeros(self.neq)
+        x = np.ascontiguousarray(x, np.float64)
+        yy = None if y is None else np.ascontiguousarray(y, np.float64)
+        self._check(lib().gpz_spmv(self.h, alpha, _p(x), beta, _p(yy), _p(z)))
+        return z
+
+    def solve(self, solver=GPZ_SOLVER_CG, precond=GPZ_PRECOND_JACOBI, max_iter=20000, tol=1e-8, b=None,
+              check_every=32, reliable_delta=1e-3, use_graph=True, x0=None, want_x=True, gmres_krylov=30):
+        o = gpz_solver_opts()
+        o.solver, o.precond, o.max_iter, o.tol = solver, precond, max_iter, tol
+        o.gmres_krylov, o.check_every, o.reliable_delta, o.use_graph = gmres_krylov, check_every, reliable_delta, \
+            int(use_graph)
+        o.from_current = int(x0 is not None)
+        rep = gpz_solve_report()
+        x = None
+        if want_x or x0 is not None:
+            x = np.zeros(self.neq) if x0 is None else np.array(x0, np.float64)
+        bb = None if b is None else np.ascontiguousarray(b, np.float64)
+        rc = self._check(lib().gpz_solve(self.h, ctypes.byref(o), _p(bb), _p(x), ctypes.byref(rep)),
+                         allow=(GPZ_NOT_CONVERGED,))
+        return dict(rc=rc, x=x, iterations=rep.iterations, resid=rep.resid, true_resid=rep.true_resid,
+                    seconds=rep.seconds, spmv_fp64=rep.spmv_fp64, spmv_fp32=rep.spmv_fp32,
+                    reliable_updates=rep.reliable_updates)
+
+
+# ---------------------------------------------------------------------------
+# Synthetic workloads (the user programs of the reference's configurations).
+# ---------------------------------------------------------------------------
+def poisson2d(n=64, p=2):
+    """Unit square, n x n quads, H1 p, f = 2 pi^2 sin(pi x) sin(pi y) (pOrder 2), u = 0 penalty Dirichlet."""
+    mats = [(1, material(GPZ_MAT_POISSON, 2, forcing=GPZ_F_SINPROD, force=(1.0, 0, 0), forcing_porder=2))]
+    bcs = [(-1, bc(0, 0))]
+    return Grid(2, (n, n), (0, 0, 0), (1, 1, 0), [1, -1, -1, -1, -1], True, p, mats, bcs)
+
+
+def elasticity3d(n, p=2, E=None, nu=0.3, top_traction=True):
+    """Unit cube, n^3 hexes, E per element (or 1), nu, body force (0,0,-1), z=0 clamped, traction (0,0,-1) on top."""
+    mats = [(1, material(GPZ_MAT_ELAST3D, 3, E=1.0, nu=nu, force=(0, 0, -1.0), forcing=GPZ_F_CONST))]
+    bcs = [(-1, bc(0, 0))]
+    if top_traction:
+        bcs.append((-3, bc(1, 0, (0, 0, -1.0))))
+    return Grid(3, (n, n, n), (0, 0, 0), (1, 1, 1), [1, -1, -2, -2, -2, -2, -3], True, p, mats, bcs, elem_coef=E)
+
+
+def darcy(dim, n, p, perm, rhs=1.0):
+    """-div(k grad u) = rhs on the unit square/cube, u = 0 penalty Dirichlet on the whole boundary."""
+    mats = [(1, material(GPZ_MAT_DARCY, dim, forcing=GPZ_F_CONST, force=(rhs, 0, 0)))]
+    bcs = [(-1, bc(0, 0))]
+    if dim == 2:
+        return Grid(2, (n, n), (0, 0, 0), (1, 1, 0), [1, -1, -1, -1, -1], True, p, mats, bcs, elem_coef=perm)
+    return Grid(3, (n, n, n), (0, 0, 0), (1, 1, 1), [1, -1, -1, -1, -1, -1, -1], True, p, mats, bcs, elem_coef=perm)
+
+
+def lognormal(ncells, sigma, seed):
+    """Per-element coefficients exp(N(0, sigma^2)), i.i.d. from a seeded PCG64 stream."""
+    return np.exp(sigma * np.random.default_rng(seed).standard_normal(ncells))

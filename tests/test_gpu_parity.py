@@ -1,0 +1,149 @@
+"""Parity of the GPU path (libgpz.so through its C ABI) with the CPU oracle.
+
+Tolerances (FP64 path):
+* CSR row pointers and column indices: bit-exact (TPZSSpStructMatrix upper and
+  TPZSpStructMatrix full patterns);
+* matrix values: per row, max |a_gpu - a_ref| <= 1e-12 * max |a_ref| of that row
+  (the GPU sums element contributions in colour order, the reference in
+  element order, and forms the Gram before the material combination);
+* load vector: max |f_gpu - f_ref| <= 1e-12 * max |f_ref|;
+* Jacobi-PCG: same stopping rule, iteration count within +-1 of the oracle,
+  solution within 1e-8 relative.
+"""
+import numpy as np
+import pytest
+
+from oracle import oracle as O
+
+pytestmark = pytest.mark.gpu
+
+
+def _gpz():
+    from neopz_gb300 import gpz
+    return gpz
+
+
+def _row_rel(ia, a, ref):
+    worst = 0.0
+    for r in range(len(ia) - 1):
+        s, e = ia[r], ia[r + 1]
+        m = np.max(np.abs(ref[s:e]))
+        d = np.max(np.abs(a[s:e] - ref[s:e]))
+        if m > 0:
+            worst = max(worst, d / m)
+        else:
+            assert d == 0.0
+    return worst
+
+
+def _cases():
+    g = _gpz()
+    rng = np.random.default_rng(7)
+    k2 = np.exp(rng.standard_normal(16 * 16))
+    k3 = np.exp(rng.standard_normal(4 ** 3))
+    E3 = np.exp(rng.standard_normal(3 ** 3))
+    return {
+        "poisson2d_p1": (lambda: O.poisson2d(16, 1), lambda: g.poisson2d(16, 1)),
+        "poisson2d_p2": (lambda: O.poisson2d(16, 2), lambda: g.poisson2d(16, 2)),
+        "poisson2d_p3": (lambda: O.poisson2d(8, 3), lambda: g.poisson2d(8, 3)),
+        "darcy2d_p2": (lambda: O.darcy(2, 16, 2, k2), lambda: g.darcy(2, 16, 2, k2)),
+        "darcy3d_p2": (lambda: O.darcy(3, 4, 2, k3), lambda: g.darcy(3, 4, 2, k3)),
+        "elast3d_p1": (lambda: O.elasticity3d(3, 1, E=E3), lambda: g.elasticity3d(3, 1, E=E3)),
+        "elast3d_p2": (lambda: O.elasticity3d(3, 2, E=E3), lambda: g.elasticity3d(3, 2, E=E3)),
+        "elast3d_p3": (lambda: O.elasticity3d(2, 3), lambda: g.elasticity3d(2, 3)),
+    }
+
+
+CASES = ["poisson2d_p1", "poisson2d_p2", "poisson2d_p3", "darcy2d_p2", "darcy3d_p2", "elast3d_p1", "elast3d_p2",
+         "elast3d_p3"]
+
+
+@pytest.fixture(scope="module")
+def built():
+    import __graft_entry__
+    __graft_entry__.build()
+    return _cases()
+
+
+@pytest.mark.parametrize("sym", [True, False])
+@pytest.mark.parametrize("case", CASES)
+def test_pattern_matrix_rhs(built, case, sym):
+    g = _gpz()
+    mk_o, mk_g = built[case]
+    om, grid = mk_o(), mk_g()
+    ctx = g.Context(0)
+    ctx.upload_mesh(grid)
+    nnz = ctx.build_pattern(sym)
+    ia, ja = ctx.pattern()
+    oia, oja = om.pattern(sym)
+    assert nnz == len(oja)
+    assert np.array_equal(ia, oia) and np.array_equal(ja, oja)
+    ctx.assemble(g.GPZ_PREC_FP64)
+    a, f = ctx.matrix(), ctx.rhs()
+    oa, of = om.assemble(sym, oia, oja)
+    assert _row_rel(oia, a, oa) <= 1e-12
+    assert np.max(np.abs(f - of)) <= 1e-12 * max(np.max(np.abs(of)), 1e-300)
+    # SpMV (TPZSYsmpMatrix / TPZFYsmpMatrix::MultAdd) on a random vector
+    x = np.random.default_rng(1).standard_normal(om.neq)
+    z = ctx.spmv(x)
+    zr = O.spmv(sym, oia, oja, oa, x)
+    assert np.max(np.abs(z - zr)) <= 1e-11 * np.max(np.abs(zr))
+    ctx.close()
+
+
+@pytest.mark.parametrize("case", ["poisson2d_p2", "darcy2d_p2", "elast3d_p2", "elast3d_p3"])
+def test_jacobi_pcg_matches_oracle(built, case):
+    g = _gpz()
+    mk_o, mk_g = built[case]
+    om, grid = mk_o(), mk_g()
+    ctx = g.Context(0)
+    ctx.upload_mesh(grid)
+    ctx.build_pattern(True)
+    ctx.assemble(g.GPZ_PREC_FP64)
+    tol = 1e-10
+    sol = ctx.solve(tol=tol, max_iter=20000)
+    oia, oja = om.pattern(True)
+    oa, of = om.assemble(True, oia, oja)
+    ref = O.cg_jacobi(True, oia, oja, oa, of, 20000, tol)
+    assert sol["rc"] == 0 and ref["rc"] == 0
+    assert abs(sol["iterations"] - ref["iters"]) <= 1
+    assert np.linalg.norm(sol["x"] - ref["x"]) <= 1e-8 * np.linalg.norm(ref["x"])
+    ctx.close()
+
+
+def test_jacobi_pcg_graph_and_eager_agree(built):
+    g = _gpz()
+    grid = built["elast3d_p2"][1]()
+    ctx = g.Context(0)
+    ctx.upload_mesh(grid)
+    ctx.build_pattern(False)
+    ctx.assemble()
+    s1 = ctx.solve(tol=1e-9, use_graph=True, check_every=16)
+    s2 = ctx.solve(tol=1e-9, use_graph=False, check_every=7)
+    assert s1["iterations"] == s2["iterations"]
+    assert np.array_equal(s1["x"], s2["x"])  # deterministic reductions
+    ctx.close()
+
+
+@pytest.mark.parametrize("case", ["poisson2d_p2", "elast3d_p2", "darcy3d_p2"])
+def test_mixed_cg_reaches_true_fp64_residual(built, case):
+    g = _gpz()
+    mk_o, mk_g = built[case]
+    om, grid = mk_o(), mk_g()
+    ctx = g.Context(0)
+    ctx.upload_mesh(grid)
+    ctx.build_pattern(True)
+    ctx.assemble(g.GPZ_PREC_MIXED)
+    tol = 1e-8
+    sol = ctx.solve(solver=g.GPZ_SOLVER_MIXED_CG, tol=tol, max_iter=20000, reliable_delta=1e-2)
+    assert sol["rc"] == 0
+    assert sol["true_resid"] <= tol
+    assert sol["spmv_fp32"] > 0 and sol["reliable_updates"] >= 1
+    oia, oja = om.pattern(True)
+    oa, of = om.assemble(True, oia, oja)
+    ref = O.cg_jacobi(True, oia, oja, oa, of, 20000, 1e-12)
+    # error against the FP64 oracle solution, stated: bounded by cond * tol; the
+    # test asks for the true-residual criterion and a small forward error
+    err = np.linalg.norm(sol["x"] - ref["x"]) / np.linalg.norm(ref["x"])
+    assert err <= 1e-5, err
+    ctx.close()
