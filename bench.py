@@ -1,0 +1,342 @@
+"""Benchmark: time to ||r||/||b|| < 1e-8 on 3D Q2 linear elasticity (64^3 hexes) on one GB300.
+
+One step = the hot path over the synthetic system: global assembly into the
+CSR (FP64 parity assembly + FP32 copy for the inner solves) and the iterative
+solve to a TRUE FP64 residual below 1e-8.  `value` is device time with the
+mesh and pattern resident in HBM (CUDA events on the library's stream);
+`e2e` is the same pipeline through the public C ABI from host buffers
+(mesh upload, pattern build, assembly, solve, solution download).  The plain
+FP64 Jacobi-PCG of the reference (same algorithm, on the GPU) is timed once
+beside it as the path's own baseline.
+
+Usage: python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference] [--n 64]
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "s to ||r||/||b||<1e-8: learned+mixed PCG vs FP64 Jacobi-PCG (GB300); elem/s"
+TOL = 1e-8
+SEED = 5
+# FP64 Jacobi-PCG iterations to 1e-8 on this seeded 64^3 system (the reference's
+# algorithm, measured with the FP64 parity path); used to extrapolate the CPU
+# sample to the full solve.
+JACOBI_ITERS_64 = None
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=2)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--n", type=int, default=64)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    return ap.parse_args()
+
+
+def dist_info():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+class Clocks:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    def __init__(self, device):
+        self.device = device
+        self.samples = []
+        self._stop = threading.Event()
+        self._t = None
+
+    def start(self):
+        q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+             "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+             "clocks_event_reasons.sw_power_cap")
+
+        def run():
+            try:
+                p = subprocess.Popen(["nvidia-smi", "-i", str(self.device), f"--query-gpu={q}",
+                                      "--format=csv,noheader,nounits", "-lms", "200"], stdout=subprocess.PIPE,
+                                     stderr=subprocess.DEVNULL, text=True)
+            except OSError:
+                return
+            while not self._stop.is_set():
+                line = p.stdout.readline()
+                if not line:
+                    break
+                self.samples.append([x.strip() for x in line.split(",")])
+            p.terminate()
+
+        self._t = threading.Thread(target=run, daemon=True)
+        self._t.start()
+
+    def stop(self):
+        self._stop.set()
+        if self._t:
+            self._t.join(timeout=3)
+        sm = [float(s[0]) for s in self.samples if s and s[0].replace(".", "").isdigit()]
+        mx = [float(s[1]) for s in self.samples if len(s) > 1 and s[1].replace(".", "").isdigit()]
+        reasons = set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for s in self.samples:
+            for i, nm in enumerate(names):
+                if len(s) > 4 + i and s[4 + i].lower().startswith("active"):
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(self.samples)}
+
+
+def peaks():
+    try:
+        return json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+    except OSError:
+        return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0, "fallback": True}
+
+
+def make_problem(n):
+    from neopz_gb300 import gpz
+    E = gpz.lognormal(n ** 3, 1.0, SEED)
+    return gpz.elasticity3d(n, 2, E=E, nu=0.3, top_traction=True, body_force=(0.0, 0.0, 0.0)), E
+
+
+def mesh_bytes(grid):
+    d = grid.desc
+    return (d.nnodes * 3 * 8 + d.nel * (4 + 4 + 8 * 8 + 4 + 27 * 8 + (8 if d.el_coef else 0)) +
+            d.nconnects * (4 + 8 + 4))
+
+
+def run_gpu(args):
+    import torch
+    from neopz_gb300 import gpz
+
+    rank, world, local = dist_info()
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
+    dev = local
+    torch.cuda.set_device(dev)
+    n = args.n
+    t0 = time.perf_counter()
+    grid, E = make_problem(n)
+    t_mesh = time.perf_counter() - t0
+    ctx = gpz.Context(dev)
+    stream = torch.cuda.ExternalStream(ctx.stream, device=dev)
+    ctx.upload_mesh(grid)
+    t0 = time.perf_counter()
+    nnz_upper = ctx.build_pattern(True)
+    torch.cuda.synchronize()
+    t_pattern = time.perf_counter() - t0
+    nnz = ctx.nnz_full()
+    nel = grid.nel
+    nvol = grid.nvol
+
+    def step(mixed=True):
+        ctx.assemble(gpz.GPZ_PREC_MIXED if mixed else gpz.GPZ_PREC_FP64)
+        if mixed:
+            return ctx.solve(solver=gpz.GPZ_SOLVER_MIXED_CG, precond=gpz.GPZ_PRECOND_BLOCK_JACOBI, tol=TOL,
+                             max_iter=200000, reliable_delta=1e-2, check_every=64, want_x=False)
+        return ctx.solve(solver=gpz.GPZ_SOLVER_CG, tol=TOL, max_iter=200000, check_every=64, want_x=False)
+
+    # the reference's plain FP64 Jacobi-PCG on the GPU (the 3x target's denominator)
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    with torch.cuda.stream(stream):
+        e0.record(stream)
+    fp64 = step(mixed=False)
+    with torch.cuda.stream(stream):
+        e1.record(stream)
+    torch.cuda.synchronize()
+    t_fp64 = e0.elapsed_time(e1) / 1e3
+    # element matrices + scatter alone (FP64), for elements/s
+    t_asm = ctx.time_kernel(gpz.GPZ_KERNEL_ASSEMBLE, 3) / 1e3
+
+    for _ in range(args.warmup):
+        step()
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    clocks = Clocks(dev)
+    clocks.start()
+    l0 = ctx.launches()
+    with torch.cuda.stream(stream):
+        e0.record(stream)
+    reps = [step() for _ in range(args.steps)]
+    with torch.cuda.stream(stream):
+        e1.record(stream)
+    torch.cuda.synchronize()
+    launches = ctx.launches() - l0
+    ms_step = e0.elapsed_time(e1) / args.steps
+    clk = clocks.stop()
+    t_step = ms_step / 1e3
+    if world > 1:
+        t = torch.tensor([t_step], device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        t_step = float(t.item())
+    last = reps[-1]
+
+    # roofline of the dominant kernel: the FP32-value CSR SpMV of the inner CG
+    ms32 = ctx.time_kernel(gpz.GPZ_KERNEL_SPMV_FP32, 20)
+    ms64 = ctx.time_kernel(gpz.GPZ_KERNEL_SPMV_FP64, 10)
+    neq = grid.neq
+    nbrow = neq // 3
+    # 3x3 block CSR: 36 B values + 4 B column per block, block row pointers, p32 gather (16 B per block row,
+    # each read once ideally), q write and p read for p.q
+    bytes32 = (nnz // 9) * (36 + 4) + (nbrow + 1) * 8 + nbrow * 16 + neq * 8 + neq * 8
+    bytes64 = nnz * (8 + 4) + (neq + 1) * 8 + neq * 8 + neq * 8 + neq * 8
+    pk = peaks()
+    hbm = pk.get("hbm_gbs", 6800.0)
+    ach = bytes32 / (ms32 * 1e-3) / 1e9
+
+    # end to end through the C ABI from host buffers
+    e2e_times = []
+    b_in = mesh_bytes(grid)
+    for _ in range(max(1, min(args.steps, 2))):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        c2 = gpz.Context(dev)
+        c2.upload_mesh(grid)
+        c2.build_pattern(True)
+        c2.assemble(gpz.GPZ_PREC_MIXED)
+        r2 = c2.solve(solver=gpz.GPZ_SOLVER_MIXED_CG, precond=gpz.GPZ_PRECOND_BLOCK_JACOBI, tol=TOL,
+                      max_iter=200000, reliable_delta=1e-2, check_every=64, want_x=True)
+        torch.cuda.synchronize()
+        e2e_times.append(time.perf_counter() - t0)
+        assert r2["true_resid"] <= TOL
+        c2.close()
+    t_e2e = min(e2e_times)
+
+    out = {
+        "metric": METRIC, "value": round(t_step * world / world, 6), "unit": "s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms_step, 3), "higher_is_better": False,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64+f32", "data": "synthetic",
+        "config": {"workload": f"3D linear elasticity {n}^3 hex Q2 (TPZElasticity3D), E lognormal(sigma=1) seed {SEED}, "
+                               "nu=0.3, clamped z=0 (penalty), traction (0,0,-1) on z=1",
+                   "neq": neq, "nnz_full": nnz, "nnz_upper": nnz_upper, "elements": nel, "volume_elements": nvol,
+                   "path": "FP64 assembly + FP32 3x3 block-CSR copy; CG with FP32-value block SpMV, FP64 x/r/dots, "
+                           "reliable FP64 true-residual updates; connect-block (3x3) Jacobi", "l2": "inputs larger than L2 (matrix > 129 MB)",
+                   "parallelism": f"replicas x{world}"},
+        "solve": {"iterations": last["iterations"], "true_resid": last["true_resid"],
+                  "reliable_updates": last["reliable_updates"], "spmv_fp32": last["spmv_fp32"],
+                  "spmv_fp64": last["spmv_fp64"], "restarts": last["restarts"], "solve_s": last["seconds"]},
+        "fp64_jacobi_pcg": {"seconds": t_fp64, "iterations": fp64["iterations"], "true_resid": fp64["true_resid"],
+                            "speedup_of_value": t_fp64 / t_step},
+        "assembly": {"fp64_seconds": t_asm, "elements_per_s": nel / t_asm, "volume_elements_per_s": nvol / t_asm,
+                     "pattern_build_s": t_pattern, "host_mesh_build_s": t_mesh},
+        "e2e": {"value": round(t_e2e, 6), "unit": "s", "h2d_bytes_per_step": int(b_in + neq * 0),
+                "d2h_bytes_per_step": int(neq * 8)},
+        "roofline": {"bound": "hbm", "kernel": "k_cg_bsr3 (q = A32 p32, 3x3 blocks, p.q)", "achieved": round(ach, 1),
+                     "peak": hbm, "unit": "GB/s", "frac": round(ach / hbm, 4), "traffic": None,
+                     "algorithmic_bytes": int(bytes32), "ms_per_launch": ms32,
+                     "fp64_spmv": {"ms_per_launch": ms64,
+                                   "achieved_gbs": round(bytes64 / (ms64 * 1e-3) / 1e9, 1)},
+                     "peak_source": "MEASURED_PEAKS.json hbm_gbs (burst copy)" if "fallback" not in pk else
+                     "fallback 6.8 TB/s"},
+        "clocks": clk,
+        "gpu_launches": int(launches),
+    }
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        out["cpu_baseline"] = cpu_baseline(fp64["iterations"], n)
+    if rank == 0:
+        print(json.dumps(out))
+    ctx.close()
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
+def cpu_sample(n_sample, iters_full, n_full, threads, cg_iters=30):
+    """The oracle (the reference's algorithm restated: OR threaded assembly,
+    serial symmetric SpMV, Jacobi with its extra Residual SpMV) on an
+    n_sample^3 instance of the same workload; extrapolated to n_full^3."""
+    from oracle import oracle as O
+    E = np.exp(np.random.default_rng(SEED).standard_normal(n_sample ** 3))
+    t0 = time.perf_counter()
+    m = O.elasticity3d(n_sample, 2, E=E)
+    ia, ja = m.pattern(True)
+    t_pat = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    a, f = m.assemble(True, ia, ja, nthreads=threads)
+    t_asm = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    O.cg_jacobi(True, ia, ja, a, f, cg_iters, 0.0, jacobi_residual=True)
+    t_it = (time.perf_counter() - t0) / cg_iters
+    nel_s = m.ncel
+    nnz_s = len(ja)
+    # scale: assembly by element count, pattern and iterations by stored entries
+    nel_full = n_full ** 3 + 2 * n_full ** 2
+    nnz_full = 610745670 if n_full == 64 else nnz_s * (n_full / n_sample) ** 3
+    scale_nnz = nnz_full / nnz_s
+    total = t_pat * scale_nnz + t_asm * nel_full / nel_s + t_it * scale_nnz * iters_full
+    return total, dict(n=n_sample, t_pattern=t_pat, t_assemble=t_asm, t_cg_iter=t_it, elements=nel_s, nnz=nnz_s,
+                       asm_el_per_s=nel_s / t_asm)
+
+
+def cpu_baseline(iters_full, n_full):
+    threads = os.cpu_count() or 1
+    iters = iters_full if iters_full else JACOBI_ITERS_64
+    total, d = cpu_sample(12, iters, n_full, threads)
+    return {"value": round(total, 2), "unit": "s", "cores": threads, "kind": "port",
+            "sample": f"oracle on a {d['n']}^3 instance of the same workload: pattern {d['t_pattern']:.2f}s, "
+                      f"threaded OR assembly {d['t_assemble']:.2f}s ({d['asm_el_per_s']:.0f} el/s, {threads} threads), "
+                      f"{d['t_cg_iter']*1e3:.1f} ms per serial Jacobi-PCG iteration; extrapolated to {n_full}^3 by "
+                      f"element count (assembly) and stored entries x {iters} FP64 Jacobi-PCG iterations (solve)"}
+
+
+def run_reference(args):
+    rank, world, local = dist_info()
+    if rank != 0:
+        return
+    from oracle import oracle as O
+    O.build()
+    threads = os.cpu_count() or 1
+    iters = JACOBI_ITERS_64_DEFAULT
+    vals = []
+    for _ in range(args.warmup):
+        cpu_sample(8, iters, args.n, threads, cg_iters=10)
+    t0 = time.perf_counter()
+    last = None
+    for _ in range(args.steps):
+        v, last = cpu_sample(12, iters, args.n, threads)
+        vals.append(v)
+    wall = time.perf_counter() - t0
+    value = statistics.median(vals)
+    out = {"metric": METRIC, "value": round(value, 2), "unit": "s", "n_gpus": world, "steps": args.steps,
+           "warmup": args.warmup, "ms_per_step": round(wall / args.steps * 1e3, 1), "higher_is_better": False,
+           "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic", "impl": "reference",
+           "config": {"workload": f"3D linear elasticity {args.n}^3 hex Q2, E lognormal(sigma=1), nu=0.3, clamped "
+                                  "base, top traction", "parallelism": "host threads"},
+           "cpu_baseline": {"value": round(value, 2), "unit": "s", "cores": threads, "kind": "port",
+                            "sample": f"oracle (restated reference algorithm) on a 12^3 instance per step, "
+                                      f"extrapolated to {args.n}^3 with {iters} Jacobi-PCG iterations "
+                                      f"({last['asm_el_per_s']:.0f} assembly el/s, "
+                                      f"{last['t_cg_iter']*1e3:.1f} ms/iteration at 12^3)"},
+           "e2e": {"value": round(value, 2), "unit": "s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(out))
+
+
+JACOBI_ITERS_64_DEFAULT = 2000
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_gpu(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -129,6 +129,8 @@ int gpz_mesh_upload(gpz_ctx *ctx, const gpz_mesh_desc *desc);
 int gpz_pattern_build(gpz_ctx *ctx, int sym, int64_t *nnz_out);
 /* Alternatively adopt a host pattern (IA, JA as TPZSYsmpMatrix::IA()/JA()). */
 int gpz_pattern_upload(gpz_ctx *ctx, int sym, int64_t neq, const int64_t *IA, const int64_t *JA);
+/* Stored entries of the full and of the upper-triangular pattern. */
+int gpz_pattern_info(gpz_ctx *ctx, int64_t *nnz_full, int64_t *nnz_upper);
 /* Copy the device pattern to the host (IA: neq+1, JA: nnz, as int64). */
 int gpz_pattern_download(gpz_ctx *ctx, int64_t *IA, int64_t *JA);
 
@@ -184,6 +186,7 @@ typedef struct {
   int64_t spmv_fp64;       /* FP64 SpMVs performed */
   int64_t spmv_fp32;       /* FP32-value SpMVs performed */
   int64_t reliable_updates;
+  int64_t restarts;        /* mixed CG: direction restarts at residual replacement */
 } gpz_solve_report;
 
 /* b: host load vector (NULL = use the assembled device rhs); x: host solution
@@ -192,6 +195,16 @@ typedef struct {
 int gpz_solve(gpz_ctx *ctx, const gpz_solver_opts *opts, const double *b, double *x, gpz_solve_report *rep);
 /* Download the device solution of the last solve. */
 int gpz_solution_download(gpz_ctx *ctx, double *x);
+
+/* ---- measurement -----------------------------------------------------------
+ * Average device time (CUDA events on the context stream) of one launch of a
+ * hot kernel over `reps` back-to-back launches on the assembled system:
+ * GPZ_KERNEL_SPMV_FP64 / GPZ_KERNEL_SPMV_FP32 (the q = A p kernel of the CG
+ * iteration) and GPZ_KERNEL_ASSEMBLE (one full FP64 assembly). */
+#define GPZ_KERNEL_SPMV_FP64 1
+#define GPZ_KERNEL_SPMV_FP32 2
+#define GPZ_KERNEL_ASSEMBLE 3
+int gpz_time_kernel(gpz_ctx *ctx, int which, int reps, double *ms_per_launch);
 
 #ifdef __cplusplus
 }

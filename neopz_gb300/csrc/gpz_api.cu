@@ -6,6 +6,7 @@
 
 namespace gpz {
 void solver_prepare(Ctx &c, bool mixed);
+double time_spmv(Ctx &c, bool f32, int reps);
 
 Ctx::~Ctx() {
   for (Bucket *b : buckets) delete b;
@@ -204,6 +205,15 @@ int gpz_pattern_upload(gpz_ctx *ctx, int sym, int64_t neq, const int64_t *IA, co
   });
 }
 
+int gpz_pattern_info(gpz_ctx *ctx, int64_t *nnz_full, int64_t *nnz_upper) {
+  return guarded(ctx, [&](Ctx &c) {
+    GPZ_REQUIRE(c.have_pattern, GPZ_E_NOT_READY, "no pattern");
+    if (nnz_full) *nnz_full = c.nnz;
+    if (nnz_upper) *nnz_upper = c.nnz_upper;
+    return GPZ_OK;
+  });
+}
+
 int gpz_pattern_download(gpz_ctx *ctx, int64_t *IA, int64_t *JA) {
   return guarded(ctx, [&](Ctx &c) {
     GPZ_REQUIRE(c.have_pattern, GPZ_E_NOT_READY, "no pattern");
@@ -330,6 +340,34 @@ int gpz_solution_download(gpz_ctx *ctx, double *x) {
     GPZ_REQUIRE(c.have_solution, GPZ_E_NOT_READY, "no solution");
     GPZ_CUDA_TRY(cudaMemcpyAsync(x, c.sw.x.p, c.neq * sizeof(double), cudaMemcpyDeviceToHost, c.stream));
     GPZ_CUDA_TRY(cudaStreamSynchronize(c.stream));
+    return GPZ_OK;
+  });
+}
+
+int gpz_time_kernel(gpz_ctx *ctx, int which, int reps, double *ms_per_launch) {
+  return guarded(ctx, [&](Ctx &c) {
+    GPZ_REQUIRE(c.have_matrix, GPZ_E_NOT_READY, "not assembled");
+    GPZ_REQUIRE(reps > 0 && ms_per_launch, GPZ_E_INVALID, "arguments");
+    if (which == GPZ_KERNEL_SPMV_FP64 || which == GPZ_KERNEL_SPMV_FP32) {
+      *ms_per_launch = time_spmv(c, which == GPZ_KERNEL_SPMV_FP32, reps);
+    } else if (which == GPZ_KERNEL_ASSEMBLE) {
+      cudaEvent_t e0, e1;
+      GPZ_CUDA_TRY(cudaEventCreate(&e0));
+      GPZ_CUDA_TRY(cudaEventCreate(&e1));
+      assemble_fp64(c);
+      GPZ_CUDA_TRY(cudaEventRecord(e0, c.stream));
+      for (int i = 0; i < reps; i++) assemble_fp64(c);
+      GPZ_CUDA_TRY(cudaEventRecord(e1, c.stream));
+      GPZ_CUDA_TRY(cudaEventSynchronize(e1));
+      float ms = 0;
+      cudaEventElapsedTime(&ms, e0, e1);
+      cudaEventDestroy(e0);
+      cudaEventDestroy(e1);
+      *ms_per_launch = ms / reps;
+      check_device_flag(c, "assembly");
+    } else {
+      GPZ_REQUIRE(false, GPZ_E_INVALID, "kernel id");
+    }
     return GPZ_OK;
   });
 }

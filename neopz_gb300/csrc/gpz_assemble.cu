@@ -23,6 +23,7 @@ bool BucketKey::operator<(const BucketKey &o) const {
   if (type != o.type) return type < o.type;
   if (is_bc != o.is_bc) return is_bc < o.is_bc;
   if (mat_kind != o.mat_kind) return mat_kind < o.mat_kind;
+  if (mat_index != o.mat_index) return mat_index < o.mat_index;
   if (intorder != o.intorder) return intorder < o.intorder;
   for (int i = 0; i < 19; i++)
     if (orders[i] != o.orders[i]) return orders[i] < o.orders[i];
@@ -401,6 +402,7 @@ void build_buckets(Ctx &c, const gpz_mesh_desc &d) {
       m = &d.mats[d.el_mat[e]];
     }
     k.mat_kind = m->kind;
+    k.mat_index = d.el_mat[e];
     GPZ_REQUIRE(m->kind == GPZ_MAT_POISSON || m->kind == GPZ_MAT_DARCY || m->kind == GPZ_MAT_ELAST3D,
                 GPZ_E_UNSUPPORTED_MATERIAL, "material kind");
     int p = d.el_order[e];
@@ -567,12 +569,10 @@ void assemble_fp64(Ctx &c) {
   c.have_bjinv = false;
 }
 
-void make_fp32_copy(Ctx &c) {
-  c.d_a32.alloc(std::max<int64_t>(c.nnz, 1));
+void to_fp32(Ctx &c) {
   k_to_fp32<<<152 * 8, 256, 0, c.stream>>>(c.d_a.p, c.d_a32.p, c.nnz);
   c.launches++;
   GPZ_CUDA_TRY(cudaGetLastError());
-  c.have_a32 = true;
 }
 
 }  // namespace gpz

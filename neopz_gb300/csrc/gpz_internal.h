@@ -67,7 +67,7 @@ constexpr int kMaxShapes = 64;   // hex p=3: 64 scalar shapes
 constexpr int kMaxQp = 64;       // hex 4x4x4 Gauss points
 
 struct BucketKey {
-  int type, is_bc, mat_kind, intorder;
+  int type, is_bc, mat_kind, mat_index, intorder;  // mat_index: the element's el_mat value
   int orders[19];      // order of each non-corner side
   int trans[19];       // orientation id of each non-corner side (0 when irrelevant)
   bool operator<(const BucketKey &o) const;
@@ -91,7 +91,7 @@ struct Bucket {
 // ---------------------------------------------------------------- solver workspace
 struct SolverWork {
   DBuf<double> r, z, p, q, x, b, t;
-  DBuf<float> p32;
+  DBuf<float> p32, p32x4;
   DBuf<double> partial;        // per-CTA partial sums
   DBuf<double> scal;           // device scalars (see gpz_solver.cu)
   DBuf<unsigned int> counter;  // last-block counters
@@ -138,8 +138,13 @@ struct Ctx {
   // values
   bool have_matrix = false;
   DBuf<double> d_a, d_f, d_dinv;
-  DBuf<float> d_a32;                         // FP32 copy for the inner solves
+  DBuf<float> d_a32;                         // FP32 CSR copy for the inner solves
   bool have_a32 = false;
+  bool have_bsr3 = false;                    // FP32 3x3 block CSR instead of d_a32
+  int64_t nbrow = 0;
+  DBuf<int64_t> d_bptr;
+  DBuf<int32_t> d_bcol;
+  DBuf<float> d_bval;
   DBuf<double> d_bjinv;                      // block-Jacobi inverses [nconnects][bs*bs]
   bool have_bjinv = false;
   int bj_bs = 0;
@@ -158,6 +163,7 @@ void build_element_offsets(Ctx &c);
 void build_buckets(Ctx &c, const gpz_mesh_desc &d);
 void assemble_fp64(Ctx &c);
 void make_fp32_copy(Ctx &c);
+void to_fp32(Ctx &c);
 void build_block_jacobi(Ctx &c);
 // solver.cu
 void spmv_device(Ctx &c, const double *x, double *y, double alpha, double beta, const double *yin);

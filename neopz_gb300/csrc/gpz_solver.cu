@@ -17,6 +17,7 @@
 //   true residual b - A64 x is recomputed in FP64 and replaces r.  The solve
 //   stops only on the true FP64 residual.
 #include <cmath>
+#include <vector>
 
 #include "gpz_internal.h"
 
@@ -29,7 +30,7 @@ constexpr int kGridBlocks = 152 * 8;  // 8 CTAs of 256 threads per SM, 152 SMs
 
 // device scalar slots
 enum { S_RHO = 0, S_RHO1, S_PQ, S_RR, S_NORMB, S_TOL, S_MAXRR, S_DELTA2, S_RESID, S_TRUERR, S_NSCAL };
-enum { I_CONV = 0, I_IT, I_MAXIT, I_UPDATE, I_NUPD, I_SP64, I_SP32, I_BREAK, I_NISCAL };
+enum { I_CONV = 0, I_IT, I_MAXIT, I_UPDATE, I_NUPD, I_SP64, I_SP32, I_BREAK, I_RESTART, I_NRESTART, I_NISCAL };
 
 struct Red {
   double *partial;   // [grid][4]
@@ -109,9 +110,22 @@ template <int TPR>
 __device__ __forceinline__ double row_dot64(const int64_t *__restrict__ ia, const int32_t *__restrict__ ja,
                                             const double *__restrict__ a, const double *__restrict__ x, int64_t r,
                                             int sub, bool valid) {
-  double s = 0.0;
+  // four independent load/FMA chains per lane; matrix streams bypass L1 (read once)
+  double s0 = 0.0, s1 = 0.0, s2 = 0.0, s3 = 0.0;
   int64_t k0 = valid ? ia[r] : 0, k1 = valid ? ia[r + 1] : 0;
-  for (int64_t k = k0 + sub; k < k1; k += TPR) s += a[k] * __ldg(&x[ja[k]]);
+  int64_t k = k0 + sub;
+  for (; k + 3 * TPR < k1; k += 4 * TPR) {
+    const int c0 = __ldcs(&ja[k]), c1 = __ldcs(&ja[k + TPR]), c2 = __ldcs(&ja[k + 2 * TPR]),
+              c3 = __ldcs(&ja[k + 3 * TPR]);
+    const double a0 = __ldcs(&a[k]), a1 = __ldcs(&a[k + TPR]), a2 = __ldcs(&a[k + 2 * TPR]),
+                 a3 = __ldcs(&a[k + 3 * TPR]);
+    s0 = fma(a0, __ldg(&x[c0]), s0);
+    s1 = fma(a1, __ldg(&x[c1]), s1);
+    s2 = fma(a2, __ldg(&x[c2]), s2);
+    s3 = fma(a3, __ldg(&x[c3]), s3);
+  }
+  for (; k < k1; k += TPR) s0 = fma(__ldcs(&a[k]), __ldg(&x[__ldcs(&ja[k])]), s0);
+  double s = (s0 + s1) + (s2 + s3);
   for (int o = TPR / 2; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o, TPR);
   return s;
 }
@@ -120,9 +134,21 @@ template <int TPR>
 __device__ __forceinline__ float row_dot32(const int64_t *__restrict__ ia, const int32_t *__restrict__ ja,
                                            const float *__restrict__ a, const float *__restrict__ x, int64_t r,
                                            int sub, bool valid) {
-  float s = 0.0f;
+  float s0 = 0.0f, s1 = 0.0f, s2 = 0.0f, s3 = 0.0f;
   int64_t k0 = valid ? ia[r] : 0, k1 = valid ? ia[r + 1] : 0;
-  for (int64_t k = k0 + sub; k < k1; k += TPR) s = fmaf(a[k], __ldg(&x[ja[k]]), s);
+  int64_t k = k0 + sub;
+  for (; k + 3 * TPR < k1; k += 4 * TPR) {
+    const int c0 = __ldcs(&ja[k]), c1 = __ldcs(&ja[k + TPR]), c2 = __ldcs(&ja[k + 2 * TPR]),
+              c3 = __ldcs(&ja[k + 3 * TPR]);
+    const float a0 = __ldcs(&a[k]), a1 = __ldcs(&a[k + TPR]), a2 = __ldcs(&a[k + 2 * TPR]),
+                a3 = __ldcs(&a[k + 3 * TPR]);
+    s0 = fmaf(a0, __ldg(&x[c0]), s0);
+    s1 = fmaf(a1, __ldg(&x[c1]), s1);
+    s2 = fmaf(a2, __ldg(&x[c2]), s2);
+    s3 = fmaf(a3, __ldg(&x[c3]), s3);
+  }
+  for (; k < k1; k += TPR) s0 = fmaf(__ldcs(&a[k]), __ldg(&x[__ldcs(&ja[k])]), s0);
+  float s = (s0 + s1) + (s2 + s3);
   for (int o = TPR / 2; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o, TPR);
   return s;
 }
@@ -167,130 +193,238 @@ __global__ void __launch_bounds__(kThreads) k_cg_spmv(const int64_t *__restrict_
   }
 }
 
-// kernel B: p = z + beta p (z = dinv r), first iteration p = z
-__global__ void __launch_bounds__(kThreads) k_cg_p(const double *__restrict__ r, const double *__restrict__ dinv,
-                                                   double *__restrict__ p, float *__restrict__ p32, int64_t n, Red R) {
+// q = A p with p.q for 3x3 block rows, FP32 values in a per-row structure of
+// arrays (entry k of block j of block row I at 9*bptr[I] + k*nb + j) so that a
+// warp's loads of one entry over 32 blocks are contiguous; p32x4 holds p in
+// FP32, padded to four floats per block row.
+__global__ void __launch_bounds__(kThreads) k_cg_bsr3(const int64_t *__restrict__ bptr, const int32_t *__restrict__ bcol,
+                                                      const float *__restrict__ bval, const float4 *__restrict__ p32x4,
+                                                      const double *__restrict__ p, double *__restrict__ q,
+                                                      int64_t nbrow, Red R) {
   if (!active(R.iscal)) return;
-  const bool first = R.iscal[I_IT] == 0;
-  const double beta = first ? 0.0 : R.scal[S_RHO] / R.scal[S_RHO1];
-  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
-    double z = r[i] * dinv[i];
-    double pi = first ? z : z + beta * p[i];
-    p[i] = pi;
-    if (p32) p32[i] = (float)pi;
+  const int lane = threadIdx.x & 31;
+  const int64_t warp_id = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) / 32;
+  const int64_t nwarps = (int64_t)gridDim.x * blockDim.x / 32;
+  double pq = 0.0;
+  for (int64_t I = warp_id; I < nbrow; I += nwarps) {
+    const int64_t b0 = bptr[I];
+    const int nb = (int)(bptr[I + 1] - b0);
+    const float *v = bval + 9 * b0;
+    float a0 = 0.f, a1 = 0.f, a2 = 0.f;
+    for (int j = lane; j < nb; j += 32) {
+      const float4 xv = __ldg(&p32x4[__ldcs(&bcol[b0 + j])]);
+      a0 = fmaf(__ldcs(&v[0 * nb + j]), xv.x, a0);
+      a0 = fmaf(__ldcs(&v[1 * nb + j]), xv.y, a0);
+      a0 = fmaf(__ldcs(&v[2 * nb + j]), xv.z, a0);
+      a1 = fmaf(__ldcs(&v[3 * nb + j]), xv.x, a1);
+      a1 = fmaf(__ldcs(&v[4 * nb + j]), xv.y, a1);
+      a1 = fmaf(__ldcs(&v[5 * nb + j]), xv.z, a1);
+      a2 = fmaf(__ldcs(&v[6 * nb + j]), xv.x, a2);
+      a2 = fmaf(__ldcs(&v[7 * nb + j]), xv.y, a2);
+      a2 = fmaf(__ldcs(&v[8 * nb + j]), xv.z, a2);
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+      a0 += __shfl_down_sync(0xffffffffu, a0, o);
+      a1 += __shfl_down_sync(0xffffffffu, a1, o);
+      a2 += __shfl_down_sync(0xffffffffu, a2, o);
+    }
+    if (lane == 0) {
+      const int64_t r = 3 * I;
+      q[r] = a0;
+      q[r + 1] = a1;
+      q[r + 2] = a2;
+      pq += p[r] * (double)a0 + p[r + 1] * (double)a1 + p[r + 2] * (double)a2;
+    }
+  }
+  double vv[1] = {pq}, tot[1];
+  if (grid_reduce<1>(vv, R, tot) && threadIdx.x == 0) {
+    R.scal[S_PQ] = tot[0];
+    R.iscal[I_SP32]++;
   }
 }
 
-// kernel D: alpha = rho / pq; x += alpha p; r -= alpha q; rho' = r.z, rr = r.r
+// Preconditioner: pointwise Jacobi (z_i = r_i / a_ii, TPZMatrix::SolveJacobi
+// one sweep) or connect-block Jacobi with 3x3 inverses (TPZBlockDiagonal over
+// the mesh blocks).  The vector kernels walk "units": rows, or block rows.
+struct Prec {
+  const double *dinv;
+  const double *binv;  // [nunits][9] when block
+  int block;
+};
+
+__device__ __forceinline__ void apply_prec(const Prec &M, const double *__restrict__ r, int64_t u, double *z) {
+  if (!M.block) {
+    z[0] = r[u] * M.dinv[u];
+  } else {
+    const double *B = M.binv + 9 * u;
+    const double r0 = r[3 * u], r1 = r[3 * u + 1], r2 = r[3 * u + 2];
+    z[0] = B[0] * r0 + B[1] * r1 + B[2] * r2;
+    z[1] = B[3] * r0 + B[4] * r1 + B[5] * r2;
+    z[2] = B[6] * r0 + B[7] * r1 + B[8] * r2;
+  }
+}
+
+// kernel B: p = z + beta p, first iteration (or after a restart) p = z
+__global__ void __launch_bounds__(kThreads) k_cg_p(const double *__restrict__ r, Prec M, double *__restrict__ p,
+                                                   float *__restrict__ p32, float *__restrict__ p32x4, int64_t nunits,
+                                                   Red R) {
+  if (!active(R.iscal)) return;
+  const bool first = R.iscal[I_IT] == 0 || R.iscal[I_RESTART] != 0;
+  const double beta = first ? 0.0 : R.scal[S_RHO] / R.scal[S_RHO1];
+  const int bs = M.block ? 3 : 1;
+  for (int64_t u = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; u < nunits; u += (int64_t)gridDim.x * blockDim.x) {
+    double z[3];
+    apply_prec(M, r, u, z);
+    for (int k = 0; k < bs; k++) {
+      const int64_t i = u * bs + k;
+      const double pi = first ? z[k] : z[k] + beta * p[i];
+      p[i] = pi;
+      if (p32) p32[i] = (float)pi;
+      if (p32x4) p32x4[(i / 3) * 4 + i % 3] = (float)pi;
+    }
+  }
+}
+
+// kernel D: alpha = rho / pq; x += alpha p; r -= alpha q; rho' = r.(M r), rr = r.r
 __global__ void __launch_bounds__(kThreads) k_cg_update(double *__restrict__ x, double *__restrict__ r,
                                                         const double *__restrict__ p, const double *__restrict__ q,
-                                                        const double *__restrict__ dinv, int64_t n, int mixed, Red R) {
+                                                        Prec M, int64_t nunits, int mixed, Red R) {
   if (!active(R.iscal)) return;
   const double pq = R.scal[S_PQ];
   const double alpha = R.scal[S_RHO] / pq;
+  const int bs = M.block ? 3 : 1;
   double rz = 0.0, rr = 0.0;
-  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
-    double xi = x[i] + alpha * p[i];
-    double ri = r[i] - alpha * q[i];
-    x[i] = xi;
-    r[i] = ri;
-    rz += ri * (ri * dinv[i]);
-    rr += ri * ri;
+  for (int64_t u = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; u < nunits; u += (int64_t)gridDim.x * blockDim.x) {
+    for (int k = 0; k < bs; k++) {
+      const int64_t i = u * bs + k;
+      x[i] = x[i] + alpha * p[i];
+      const double ri = r[i] - alpha * q[i];
+      r[i] = ri;
+      rr += ri * ri;
+    }
+    double z[3];
+    apply_prec(M, r, u, z);
+    for (int k = 0; k < bs; k++) rz += r[u * bs + k] * z[k];
   }
   double v[2] = {rz, rr}, tot[2];
   if (grid_reduce<2>(v, R, tot) && threadIdx.x == 0) {
     double *s = R.scal;
     int64_t *is = R.iscal;
-    if (!(pq > 0.0) || !isfinite(tot[1])) is[I_BREAK] = 1;
+    if (!(pq > 0.0) || !isfinite(tot[1]) || !isfinite(tot[0])) is[I_BREAK] = 1;
     s[S_RHO1] = s[S_RHO];
     s[S_RHO] = tot[0];
     s[S_RR] = tot[1];
-    double resid = sqrt(tot[1]) / s[S_NORMB];
+    if (tot[1] > s[S_MAXRR]) s[S_MAXRR] = tot[1];
+    const double resid = sqrt(tot[1]) / s[S_NORMB];
     s[S_RESID] = resid;
     is[I_IT] += 1;
+    is[I_RESTART] = 0;
     if (is[I_BREAK]) is[I_CONV] = 2;
     else if (!mixed) {
       if (resid <= s[S_TOL]) is[I_CONV] = 1;
-    } else {
-      if (resid <= s[S_TOL] || tot[1] < s[S_DELTA2] * s[S_MAXRR]) is[I_UPDATE] = 1;
+    } else if (resid <= s[S_TOL] || tot[1] < s[S_DELTA2] * s[S_MAXRR]) {
+      is[I_UPDATE] = 1;
     }
   }
 }
 
-// kernel E (mixed): when flagged, r = b - A64 x in FP64 and restart the
-// residual bookkeeping from it.
+// kernel E (mixed): when requested, r = b - A64 x in FP64 (residual replacement)
 template <int TPR>
 __global__ void __launch_bounds__(kThreads) k_reliable(const int64_t *__restrict__ ia, const int32_t *__restrict__ ja,
                                                        const double *__restrict__ a, const double *__restrict__ x,
-                                                       const double *__restrict__ b, const double *__restrict__ dinv,
-                                                       double *__restrict__ r, int64_t n, Red R) {
-  if (R.iscal[I_UPDATE] == 0 || R.iscal[I_CONV] != 0) return;
-  double rz = 0.0, rr = 0.0;
+                                                       const double *__restrict__ b, double *__restrict__ r, int64_t n,
+                                                       Red R) {
+  if (R.iscal[I_UPDATE] != 1 || R.iscal[I_CONV] != 0) return;
+  double rr = 0.0;
   GPZ_ROW_LOOP(TPR, n) {
     const int64_t i = r0 + (threadIdx.x & 31) / TPR;
     const bool valid = i < n;
     double s = row_dot64<TPR>(ia, ja, a, x, i, sub, valid);
     if (sub == 0 && valid) {
-      double ri = b[i] - s;
+      const double ri = b[i] - s;
       r[i] = ri;
-      rz += ri * (ri * dinv[i]);
       rr += ri * ri;
     }
   }
-  double v[2] = {rz, rr}, tot[2];
-  if (grid_reduce<2>(v, R, tot) && threadIdx.x == 0) {
+  double v[1] = {rr}, tot[1];
+  if (grid_reduce<1>(v, R, tot) && threadIdx.x == 0) {
     double *s = R.scal;
     int64_t *is = R.iscal;
-    s[S_RHO] = tot[0];
-    s[S_RR] = tot[1];
-    s[S_MAXRR] = tot[1];
-    s[S_TRUERR] = tot[1];
-    double resid = sqrt(tot[1]) / s[S_NORMB];
+    s[S_RR] = tot[0];
+    s[S_MAXRR] = tot[0];
+    s[S_TRUERR] = tot[0];
+    const double resid = sqrt(tot[0]) / s[S_NORMB];
     s[S_RESID] = resid;
-    is[I_UPDATE] = 0;
     is[I_NUPD] += 1;
     is[I_SP64] += 1;
     if (resid <= s[S_TOL]) is[I_CONV] = 1;
+    is[I_UPDATE] = 2;
   }
 }
 
-// initial residual: r = b (x = 0) or r = b - A x; rho = r.z, rr = r.r, normb
+// rho = r.(M r) for a freshly computed residual (after init or a replacement).
+// When the replaced residual differs from the recursive one by a large factor
+// in the preconditioner norm (FP32 drift carried over from the early, large
+// updates), beta = rho_true / rho_old would blow the direction up, so the
+// direction restarts (p = z) instead.
+__global__ void __launch_bounds__(kThreads) k_precond_dot(const double *__restrict__ r, Prec M, int64_t nunits, Red R) {
+  if (R.iscal[I_UPDATE] != 2) return;
+  const int bs = M.block ? 3 : 1;
+  double rz = 0.0;
+  for (int64_t u = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; u < nunits; u += (int64_t)gridDim.x * blockDim.x) {
+    double z[3];
+    apply_prec(M, r, u, z);
+    for (int k = 0; k < bs; k++) rz += r[u * bs + k] * z[k];
+  }
+  double v[1] = {rz}, tot[1];
+  if (grid_reduce<1>(v, R, tot) && threadIdx.x == 0) {
+    double *s = R.scal;
+    int64_t *is = R.iscal;
+    if (is[I_IT] > 0 && (tot[0] > 4.0 * s[S_RHO] || tot[0] < 0.25 * s[S_RHO])) {
+      is[I_RESTART] = 1;
+      is[I_NRESTART] += 1;
+    }
+    s[S_RHO] = tot[0];
+    is[I_UPDATE] = 0;
+  }
+}
+
+// initial residual: r = b (x = 0) or r = b - A x; rr, normb; rho follows in k_precond_dot
 template <int TPR>
 __global__ void __launch_bounds__(kThreads) k_cg_init(const int64_t *__restrict__ ia, const int32_t *__restrict__ ja,
                                                       const double *__restrict__ a, double *__restrict__ x,
-                                                      const double *__restrict__ b, const double *__restrict__ dinv,
-                                                      double *__restrict__ r, int64_t n, int from_current, Red R) {
-  double rz = 0.0, rr = 0.0, bb = 0.0;
+                                                      const double *__restrict__ b, double *__restrict__ r, int64_t n,
+                                                      int from_current, Red R) {
+  double rr = 0.0, bb = 0.0;
   GPZ_ROW_LOOP(TPR, n) {
     const int64_t i = r0 + (threadIdx.x & 31) / TPR;
     const bool valid = i < n;
     double s = 0.0;
     if (from_current) s = row_dot64<TPR>(ia, ja, a, x, i, sub, valid);
     if (sub == 0 && valid) {
-      double bi = b[i];
-      double ri = bi - s;
+      const double bi = b[i];
+      const double ri = bi - s;
       if (!from_current) x[i] = 0.0;
       r[i] = ri;
-      rz += ri * (ri * dinv[i]);
       rr += ri * ri;
       bb += bi * bi;
     }
   }
-  double v[3] = {rz, rr, bb}, tot[3];
-  if (grid_reduce<3>(v, R, tot) && threadIdx.x == 0) {
+  double v[2] = {rr, bb}, tot[2];
+  if (grid_reduce<2>(v, R, tot) && threadIdx.x == 0) {
     double *s = R.scal;
     int64_t *is = R.iscal;
-    double normb = sqrt(tot[2]);
+    double normb = sqrt(tot[1]);
     if (normb == 0.0) normb = 1.0;
     s[S_NORMB] = normb;
-    s[S_RHO] = tot[0];
     s[S_RHO1] = 0.0;
-    s[S_RR] = tot[1];
-    s[S_MAXRR] = tot[1];
-    double resid = sqrt(tot[1]) / normb;
+    s[S_RR] = tot[0];
+    s[S_MAXRR] = tot[0];
+    const double resid = sqrt(tot[0]) / normb;
     s[S_RESID] = resid;
     is[I_IT] = 0;
     is[I_CONV] = (resid <= s[S_TOL]) ? 1 : 0;
+    is[I_UPDATE] = 2;
   }
 }
 
@@ -305,12 +439,66 @@ __global__ void __launch_bounds__(kThreads) k_true_resid(const int64_t *__restri
     const bool valid = i < n;
     double s = row_dot64<TPR>(ia, ja, a, x, i, sub, valid);
     if (sub == 0 && valid) {
-      double ri = b[i] - s;
+      const double ri = b[i] - s;
       rr += ri * ri;
     }
   }
   double v[1] = {rr}, tot[1];
   if (grid_reduce<1>(v, R, tot) && threadIdx.x == 0) R.scal[S_TRUERR] = tot[0];
+}
+
+// ---- setup kernels for the mixed path and the block preconditioner
+__global__ void k_build_bsr3(const int64_t *__restrict__ ia, const int32_t *__restrict__ ja,
+                             const double *__restrict__ a, int64_t nbrow, int64_t *__restrict__ bptr,
+                             int32_t *__restrict__ bcol, float *__restrict__ bval, int *__restrict__ err) {
+  const int lane = threadIdx.x & 31;
+  const int64_t I = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) / 32;
+  if (I >= nbrow) return;
+  const int64_t r0 = 3 * I;
+  const int64_t len = ia[r0 + 1] - ia[r0];
+  if (len % 3 != 0 || ia[r0 + 2] - ia[r0 + 1] != len || ia[r0 + 3] - ia[r0 + 2] != len || ia[r0] % 9 != 0) {
+    if (lane == 0) atomicOr(err, 128);
+    return;
+  }
+  const int64_t nb = len / 3, b0 = ia[r0] / 9;
+  if (lane == 0) {
+    bptr[I] = b0;
+    if (I == nbrow - 1) bptr[nbrow] = b0 + nb;
+  }
+  float *v = bval + 9 * b0;
+  for (int64_t j = lane; j < nb; j += 32) {
+    bcol[b0 + j] = ja[ia[r0] + 3 * j] / 3;
+    for (int s = 0; s < 3; s++)
+      for (int t = 0; t < 3; t++) v[(3 * s + t) * nb + j] = (float)a[ia[r0 + s] + 3 * j + t];
+  }
+}
+
+__global__ void k_block_inv3(const double *__restrict__ a, const int64_t *__restrict__ diagpos, int64_t nbrow,
+                             double *__restrict__ binv, int *__restrict__ err) {
+  const int64_t u = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (u >= nbrow) return;
+  double m[3][3];
+  for (int s = 0; s < 3; s++)
+    for (int t = 0; t < 3; t++) m[s][t] = a[diagpos[3 * u + s] + (t - s)];
+  const double c00 = m[1][1] * m[2][2] - m[1][2] * m[2][1];
+  const double c01 = m[1][2] * m[2][0] - m[1][0] * m[2][2];
+  const double c02 = m[1][0] * m[2][1] - m[1][1] * m[2][0];
+  const double det = m[0][0] * c00 + m[0][1] * c01 + m[0][2] * c02;
+  if (!(fabs(det) > 0.0)) {
+    atomicOr(err, 256);
+    return;
+  }
+  const double id = 1.0 / det;
+  double *B = binv + 9 * u;
+  B[0] = c00 * id;
+  B[1] = (m[0][2] * m[2][1] - m[0][1] * m[2][2]) * id;
+  B[2] = (m[0][1] * m[1][2] - m[0][2] * m[1][1]) * id;
+  B[3] = c01 * id;
+  B[4] = (m[0][0] * m[2][2] - m[0][2] * m[2][0]) * id;
+  B[5] = (m[0][2] * m[1][0] - m[0][0] * m[1][2]) * id;
+  B[6] = c02 * id;
+  B[7] = (m[0][1] * m[2][0] - m[0][0] * m[2][1]) * id;
+  B[8] = (m[0][0] * m[1][1] - m[0][1] * m[1][0]) * id;
 }
 
 int pick_tpr(int64_t nnz, int64_t n) {
@@ -339,6 +527,46 @@ void spmv_device(Ctx &c, const double *x, double *y, double alpha, double beta, 
   GPZ_CUDA_TRY(cudaGetLastError());
 }
 
+// uniform 3x3 connect blocks (elasticity with one shape per connect)?
+bool blocks_are_3(const Ctx &c) {
+  if (c.nstate != 3) return false;
+  for (int32_t s : c.h_block_size)
+    if (s != 3) return false;
+  return c.nconnects > 0;
+}
+
+void make_fp32_copy(Ctx &c) {
+  c.have_bsr3 = false;
+  if (blocks_are_3(c)) {
+    c.nbrow = c.nconnects;
+    c.d_bptr.alloc(c.nbrow + 1);
+    c.d_bcol.alloc(std::max<int64_t>(c.nnz / 9, 1));
+    c.d_bval.alloc(std::max<int64_t>(c.nnz, 1));
+    k_build_bsr3<<<grid_for(c.nbrow * 32, 256), 256, 0, c.stream>>>(c.d_ia.p, c.d_ja.p, c.d_a.p, c.nbrow, c.d_bptr.p,
+                                                                    c.d_bcol.p, c.d_bval.p, c.d_err.p);
+    c.launches++;
+    GPZ_CUDA_TRY(cudaGetLastError());
+    check_device_flag(c, "3x3 block CSR");
+    c.d_a32.release();
+    c.have_bsr3 = true;
+  } else {
+    c.d_a32.alloc(std::max<int64_t>(c.nnz, 1));
+    to_fp32(c);
+  }
+  c.have_a32 = true;
+}
+
+void build_block_jacobi(Ctx &c) {
+  GPZ_REQUIRE(blocks_are_3(c), GPZ_E_INVALID, "block Jacobi needs uniform 3x3 connect blocks (nstate 3, one shape per connect)");
+  c.d_bjinv.alloc((size_t)c.nconnects * 9);
+  k_block_inv3<<<grid_for(c.nconnects, 256), 256, 0, c.stream>>>(c.d_a.p, c.d_diagpos.p, c.nconnects, c.d_bjinv.p,
+                                                                 c.d_err.p);
+  c.launches++;
+  GPZ_CUDA_TRY(cudaGetLastError());
+  check_device_flag(c, "block Jacobi inverse");
+  c.have_bjinv = true;
+}
+
 namespace {
 
 void alloc_work(Ctx &c, bool mixed) {
@@ -349,7 +577,14 @@ void alloc_work(Ctx &c, bool mixed) {
   w.q.alloc(n);
   w.x.alloc(n);
   w.b.alloc(n);
-  if (mixed) w.p32.alloc(n);
+  if (mixed) {
+    if (c.have_bsr3) {
+      w.p32x4.alloc((size_t)std::max<int64_t>(c.nbrow, 1) * 4);
+      w.p32x4.zero(c.stream);
+    } else {
+      w.p32.alloc(n);
+    }
+  }
   w.partial.alloc((size_t)kGridBlocks * 4);
   w.scal.alloc(S_NSCAL);
   w.iscal.alloc(I_NISCAL);
@@ -359,24 +594,36 @@ void alloc_work(Ctx &c, bool mixed) {
 
 Red red_of(Ctx &c) { return Red{c.sw.partial.p, c.sw.counter.p, c.sw.scal.p, c.sw.iscal.p}; }
 
-void launch_iteration(Ctx &c, bool mixed, int tpr) {
+struct Plan {
+  bool mixed, block, bsr;
+  int tpr;
+  int64_t nunits;
+  Prec M;
+};
+
+void launch_iteration(Ctx &c, const Plan &P) {
   SolverWork &w = c.sw;
   Red R = red_of(c);
-  k_cg_p<<<kGridBlocks, kThreads, 0, c.stream>>>(w.r.p, c.d_dinv.p, w.p.p, mixed ? w.p32.p : nullptr, c.neq, R);
-  if (mixed) {
-    GPZ_TPR_SWITCH(tpr, (k_cg_spmv<T, true><<<kGridBlocks, kThreads, 0, c.stream>>>(
-                            c.d_ia.p, c.d_ja.p, nullptr, c.d_a32.p, w.p.p, w.p32.p, w.q.p, c.neq, R)));
+  const bool p32 = P.mixed && !P.bsr;
+  k_cg_p<<<kGridBlocks, kThreads, 0, c.stream>>>(w.r.p, P.M, w.p.p, p32 ? w.p32.p : nullptr,
+                                                 (P.mixed && P.bsr) ? w.p32x4.p : nullptr, P.nunits, R);
+  if (P.mixed && P.bsr) {
+    k_cg_bsr3<<<kGridBlocks, kThreads, 0, c.stream>>>(c.d_bptr.p, c.d_bcol.p, c.d_bval.p, (const float4 *)w.p32x4.p,
+                                                      w.p.p, w.q.p, c.nbrow, R);
+  } else if (P.mixed) {
+    GPZ_TPR_SWITCH(P.tpr, (k_cg_spmv<T, true><<<kGridBlocks, kThreads, 0, c.stream>>>(
+                              c.d_ia.p, c.d_ja.p, nullptr, c.d_a32.p, w.p.p, w.p32.p, w.q.p, c.neq, R)));
   } else {
-    GPZ_TPR_SWITCH(tpr, (k_cg_spmv<T, false><<<kGridBlocks, kThreads, 0, c.stream>>>(
-                            c.d_ia.p, c.d_ja.p, c.d_a.p, nullptr, w.p.p, nullptr, w.q.p, c.neq, R)));
+    GPZ_TPR_SWITCH(P.tpr, (k_cg_spmv<T, false><<<kGridBlocks, kThreads, 0, c.stream>>>(
+                              c.d_ia.p, c.d_ja.p, c.d_a.p, nullptr, w.p.p, nullptr, w.q.p, c.neq, R)));
   }
-  k_cg_update<<<kGridBlocks, kThreads, 0, c.stream>>>(w.x.p, w.r.p, w.p.p, w.q.p, c.d_dinv.p, c.neq, mixed ? 1 : 0,
-                                                      R);
+  k_cg_update<<<kGridBlocks, kThreads, 0, c.stream>>>(w.x.p, w.r.p, w.p.p, w.q.p, P.M, P.nunits, P.mixed ? 1 : 0, R);
   c.launches += 3;
-  if (mixed) {
-    GPZ_TPR_SWITCH(tpr, (k_reliable<T><<<kGridBlocks, kThreads, 0, c.stream>>>(c.d_ia.p, c.d_ja.p, c.d_a.p, w.x.p,
-                                                                                w.b.p, c.d_dinv.p, w.r.p, c.neq, R)));
-    c.launches++;
+  if (P.mixed) {
+    GPZ_TPR_SWITCH(P.tpr, (k_reliable<T><<<kGridBlocks, kThreads, 0, c.stream>>>(c.d_ia.p, c.d_ja.p, c.d_a.p, w.x.p,
+                                                                                  w.b.p, w.r.p, c.neq, R)));
+    k_precond_dot<<<kGridBlocks, kThreads, 0, c.stream>>>(w.r.p, P.M, P.nunits, R);
+    c.launches += 2;
   }
 }
 
@@ -385,11 +632,21 @@ void launch_iteration(Ctx &c, bool mixed, int tpr) {
 int solve(Ctx &c, const gpz_solver_opts &o, gpz_solve_report &rep) {
   const bool mixed = o.solver == GPZ_SOLVER_MIXED_CG;
   GPZ_REQUIRE(o.solver == GPZ_SOLVER_CG || mixed, GPZ_E_INVALID, "solver kind not available");
-  GPZ_REQUIRE(o.precond == GPZ_PRECOND_JACOBI || o.precond == 0, GPZ_E_INVALID, "preconditioner not available");
+  GPZ_REQUIRE(o.precond == GPZ_PRECOND_JACOBI || o.precond == GPZ_PRECOND_BLOCK_JACOBI || o.precond == 0,
+              GPZ_E_INVALID, "preconditioner not available");
+  const bool block = o.precond == GPZ_PRECOND_BLOCK_JACOBI;
   if (mixed && !c.have_a32) make_fp32_copy(c);
+  if (block && !c.have_bjinv) build_block_jacobi(c);
+  alloc_work(c, mixed);
   SolverWork &w = c.sw;
   cudaStream_t s = c.stream;
-  const int tpr = pick_tpr(c.nnz, c.neq);
+  Plan P;
+  P.mixed = mixed;
+  P.block = block;
+  P.bsr = mixed && c.have_bsr3;
+  P.tpr = pick_tpr(c.nnz, c.neq);
+  P.nunits = block ? c.nconnects : c.neq;
+  P.M = Prec{c.d_dinv.p, block ? c.d_bjinv.p : nullptr, block ? 1 : 0};
   const int batch = o.check_every > 0 ? o.check_every : 32;
 
   cudaEvent_t ev0, ev1;
@@ -399,39 +656,38 @@ int solve(Ctx &c, const gpz_solver_opts &o, gpz_solve_report &rep) {
 
   double hs[S_NSCAL] = {0};
   hs[S_TOL] = o.tol;
-  hs[S_DELTA2] = (o.reliable_delta > 0 ? o.reliable_delta : 1e-3);
+  hs[S_DELTA2] = (o.reliable_delta > 0 ? o.reliable_delta : 1e-2);
   hs[S_DELTA2] *= hs[S_DELTA2];
   int64_t hi[I_NISCAL] = {0};
   hi[I_MAXIT] = o.max_iter;
   GPZ_CUDA_TRY(cudaMemcpyAsync(w.scal.p, hs, sizeof(hs), cudaMemcpyHostToDevice, s));
   GPZ_CUDA_TRY(cudaMemcpyAsync(w.iscal.p, hi, sizeof(hi), cudaMemcpyHostToDevice, s));
   Red R = red_of(c);
-  GPZ_TPR_SWITCH(tpr, (k_cg_init<T><<<kGridBlocks, kThreads, 0, s>>>(c.d_ia.p, c.d_ja.p, c.d_a.p, w.x.p, w.b.p,
-                                                                      c.d_dinv.p, w.r.p, c.neq, o.from_current, R)));
-  c.launches++;
+  GPZ_TPR_SWITCH(P.tpr, (k_cg_init<T><<<kGridBlocks, kThreads, 0, s>>>(c.d_ia.p, c.d_ja.p, c.d_a.p, w.x.p, w.b.p,
+                                                                        w.r.p, c.neq, o.from_current, R)));
+  k_precond_dot<<<kGridBlocks, kThreads, 0, s>>>(w.r.p, P.M, P.nunits, R);
+  c.launches += 2;
   GPZ_CUDA_TRY(cudaGetLastError());
 
   cudaGraphExec_t exec = nullptr;
+  const int per_iter = mixed ? 5 : 3;
   if (o.use_graph) {
     cudaGraph_t g;
     GPZ_CUDA_TRY(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
     int64_t l0 = c.launches;
-    for (int i = 0; i < batch; i++) launch_iteration(c, mixed, tpr);
+    for (int i = 0; i < batch; i++) launch_iteration(c, P);
     GPZ_CUDA_TRY(cudaStreamEndCapture(s, &g));
-    int64_t per_graph = c.launches - l0;
     c.launches = l0;
     GPZ_CUDA_TRY(cudaGraphInstantiate(&exec, g, 0));
     GPZ_CUDA_TRY(cudaGraphDestroy(g));
-    (void)per_graph;
   }
-  const int per_iter = mixed ? 4 : 3;
   int64_t hstate[I_NISCAL];
   for (;;) {
     if (exec) {
       GPZ_CUDA_TRY(cudaGraphLaunch(exec, s));
       c.launches += (int64_t)batch * per_iter;
     } else {
-      for (int i = 0; i < batch; i++) launch_iteration(c, mixed, tpr);
+      for (int i = 0; i < batch; i++) launch_iteration(c, P);
     }
     GPZ_CUDA_TRY(cudaGetLastError());
     GPZ_CUDA_TRY(cudaMemcpyAsync(hstate, w.iscal.p, sizeof(hstate), cudaMemcpyDeviceToHost, s));
@@ -439,8 +695,8 @@ int solve(Ctx &c, const gpz_solver_opts &o, gpz_solve_report &rep) {
     if (hstate[I_CONV] != 0 || hstate[I_IT] >= o.max_iter) break;
   }
   if (exec) cudaGraphExecDestroy(exec);
-  GPZ_TPR_SWITCH(tpr, (k_true_resid<T><<<kGridBlocks, kThreads, 0, s>>>(c.d_ia.p, c.d_ja.p, c.d_a.p, w.x.p, w.b.p,
-                                                                         c.neq, R)));
+  GPZ_TPR_SWITCH(P.tpr, (k_true_resid<T><<<kGridBlocks, kThreads, 0, s>>>(c.d_ia.p, c.d_ja.p, c.d_a.p, w.x.p, w.b.p,
+                                                                           c.neq, R)));
   c.launches++;
   GPZ_CUDA_TRY(cudaEventRecord(ev1, s));
   GPZ_CUDA_TRY(cudaMemcpyAsync(hs, w.scal.p, sizeof(hs), cudaMemcpyDeviceToHost, s));
@@ -457,11 +713,63 @@ int solve(Ctx &c, const gpz_solver_opts &o, gpz_solve_report &rep) {
   rep.spmv_fp64 = hstate[I_SP64] + 1;
   rep.spmv_fp32 = hstate[I_SP32];
   rep.reliable_updates = hstate[I_NUPD];
+  rep.restarts = hstate[I_NRESTART];
   c.have_solution = true;
   if (hstate[I_BREAK]) return GPZ_E_BREAKDOWN;
   return hstate[I_CONV] == 1 ? GPZ_OK : GPZ_NOT_CONVERGED;
 }
 
-void solver_prepare(Ctx &c, bool mixed) { alloc_work(c, mixed); }
+void solver_prepare(Ctx &c, bool mixed) {
+  if (mixed && !c.have_a32) make_fp32_copy(c);
+  alloc_work(c, mixed);
+}
+
+double time_spmv(Ctx &c, bool f32, int reps) {
+  if (f32 && !c.have_a32) make_fp32_copy(c);
+  alloc_work(c, f32);
+  SolverWork &w = c.sw;
+  cudaStream_t s = c.stream;
+  std::vector<double> ones(c.neq, 1.0);
+  GPZ_CUDA_TRY(cudaMemcpyAsync(w.p.p, ones.data(), c.neq * sizeof(double), cudaMemcpyHostToDevice, s));
+  if (f32 && c.have_bsr3) {
+    std::vector<float> o4(c.nbrow * 4, 1.0f);
+    GPZ_CUDA_TRY(cudaMemcpyAsync(w.p32x4.p, o4.data(), o4.size() * sizeof(float), cudaMemcpyHostToDevice, s));
+  } else if (f32) {
+    std::vector<float> o1(c.neq, 1.0f);
+    GPZ_CUDA_TRY(cudaMemcpyAsync(w.p32.p, o1.data(), c.neq * sizeof(float), cudaMemcpyHostToDevice, s));
+  }
+  int64_t hi[I_NISCAL] = {0};
+  hi[I_MAXIT] = 1;
+  GPZ_CUDA_TRY(cudaMemcpyAsync(w.iscal.p, hi, sizeof(hi), cudaMemcpyHostToDevice, s));
+  Red R = red_of(c);
+  const int tpr = pick_tpr(c.nnz, c.neq);
+  auto launch = [&]() {
+    if (f32 && c.have_bsr3) {
+      k_cg_bsr3<<<kGridBlocks, kThreads, 0, s>>>(c.d_bptr.p, c.d_bcol.p, c.d_bval.p, (const float4 *)w.p32x4.p, w.p.p,
+                                                 w.q.p, c.nbrow, R);
+    } else if (f32) {
+      GPZ_TPR_SWITCH(tpr, (k_cg_spmv<T, true><<<kGridBlocks, kThreads, 0, s>>>(c.d_ia.p, c.d_ja.p, nullptr, c.d_a32.p,
+                                                                               w.p.p, w.p32.p, w.q.p, c.neq, R)));
+    } else {
+      GPZ_TPR_SWITCH(tpr, (k_cg_spmv<T, false><<<kGridBlocks, kThreads, 0, s>>>(c.d_ia.p, c.d_ja.p, c.d_a.p, nullptr,
+                                                                                w.p.p, nullptr, w.q.p, c.neq, R)));
+    }
+    c.launches++;
+  };
+  for (int i = 0; i < 3; i++) launch();
+  cudaEvent_t e0, e1;
+  GPZ_CUDA_TRY(cudaEventCreate(&e0));
+  GPZ_CUDA_TRY(cudaEventCreate(&e1));
+  GPZ_CUDA_TRY(cudaEventRecord(e0, s));
+  for (int i = 0; i < reps; i++) launch();
+  GPZ_CUDA_TRY(cudaEventRecord(e1, s));
+  GPZ_CUDA_TRY(cudaEventSynchronize(e1));
+  GPZ_CUDA_TRY(cudaGetLastError());
+  float ms = 0;
+  cudaEventElapsedTime(&ms, e0, e1);
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  return ms / reps;
+}
 
 }  // namespace gpz

@@ -21,6 +21,7 @@ GPZ_F_NONE, GPZ_F_CONST, GPZ_F_SINPROD = 0, 1, 2
 GPZ_PREC_FP64, GPZ_PREC_MIXED = 0, 1
 GPZ_SOLVER_CG, GPZ_SOLVER_GMRES, GPZ_SOLVER_MIXED_CG, GPZ_SOLVER_LEARNED_FCG = 1, 2, 3, 4
 GPZ_PRECOND_JACOBI, GPZ_PRECOND_BLOCK_JACOBI = 1, 2
+GPZ_KERNEL_SPMV_FP64, GPZ_KERNEL_SPMV_FP32, GPZ_KERNEL_ASSEMBLE = 1, 2, 3
 BIGNUMBER = 10.0 ** 17 * 2 / 3  # TPZMaterial::fBigNumber default for double
 
 
@@ -58,7 +59,7 @@ class gpz_solver_opts(ctypes.Structure):
 class gpz_solve_report(ctypes.Structure):
     _fields_ = [("iterations", ctypes.c_int64), ("resid", ctypes.c_double), ("true_resid", ctypes.c_double),
                 ("seconds", ctypes.c_double), ("spmv_fp64", ctypes.c_int64), ("spmv_fp32", ctypes.c_int64),
-                ("reliable_updates", ctypes.c_int64)]
+                ("reliable_updates", ctypes.c_int64), ("restarts", ctypes.c_int64)]
 
 
 class gpzh_grid_spec(ctypes.Structure):
@@ -100,6 +101,8 @@ def lib():
         L.gpz_pattern_build.argtypes = [vp, i32, _P(i64)]
         L.gpz_pattern_upload.argtypes = [vp, i32, i64, vp, vp]
         L.gpz_pattern_download.argtypes = [vp, vp, vp]
+        L.gpz_pattern_info.argtypes = [vp, _P(i64), _P(i64)]
+        L.gpz_time_kernel.argtypes = [vp, i32, i32, _P(dp)]
         L.gpz_assemble.argtypes = [vp, i32]
         L.gpz_matrix_download.argtypes = [vp, vp]
         L.gpz_rhs_download.argtypes = [vp, vp]
@@ -244,6 +247,16 @@ class Context:
         self.nnz = nnz.value
         return self.nnz
 
+    def nnz_full(self):
+        a, b = ctypes.c_int64(), ctypes.c_int64()
+        self._check(lib().gpz_pattern_info(self.h, ctypes.byref(a), ctypes.byref(b)))
+        return a.value
+
+    def time_kernel(self, which, reps):
+        ms = ctypes.c_double()
+        self._check(lib().gpz_time_kernel(self.h, which, reps, ctypes.byref(ms)))
+        return ms.value
+
     def pattern(self):
         ia = np.zeros(self.neq + 1, np.int64)
         ja = np.zeros(self.nnz, np.int64)
@@ -286,7 +299,7 @@ class Context:
                          allow=(GPZ_NOT_CONVERGED,))
         return dict(rc=rc, x=x, iterations=rep.iterations, resid=rep.resid, true_resid=rep.true_resid,
                     seconds=rep.seconds, spmv_fp64=rep.spmv_fp64, spmv_fp32=rep.spmv_fp32,
-                    reliable_updates=rep.reliable_updates)
+                    reliable_updates=rep.reliable_updates, restarts=rep.restarts)
 
 
 # ---------------------------------------------------------------------------
@@ -299,9 +312,9 @@ def poisson2d(n=64, p=2):
     return Grid(2, (n, n), (0, 0, 0), (1, 1, 0), [1, -1, -1, -1, -1], True, p, mats, bcs)
 
 
-def elasticity3d(n, p=2, E=None, nu=0.3, top_traction=True):
-    """Unit cube, n^3 hexes, E per element (or 1), nu, body force (0,0,-1), z=0 clamped, traction (0,0,-1) on top."""
-    mats = [(1, material(GPZ_MAT_ELAST3D, 3, E=1.0, nu=nu, force=(0, 0, -1.0), forcing=GPZ_F_CONST))]
+def elasticity3d(n, p=2, E=None, nu=0.3, top_traction=True, body_force=(0.0, 0.0, -1.0)):
+    """Unit cube, n^3 hexes, E per element (or 1), nu, body force, z=0 clamped, traction (0,0,-1) on top."""
+    mats = [(1, material(GPZ_MAT_ELAST3D, 3, E=1.0, nu=nu, force=body_force, forcing=GPZ_F_CONST))]
     bcs = [(-1, bc(0, 0))]
     if top_traction:
         bcs.append((-3, bc(1, 0, (0, 0, -1.0))))

@@ -48,7 +48,7 @@ def build(force=False):
     """Compile the oracle with g++ (works on x86_64 and aarch64)."""
     os.makedirs(os.path.dirname(_LIB), exist_ok=True)
     if force or not os.path.exists(_LIB) or os.path.getmtime(_LIB) < os.path.getmtime(_SRC):
-        subprocess.check_call(["g++", "-O2", "-std=c++17", "-fPIC", "-shared", "-pthread",
+        subprocess.check_call(["g++", "-O2", "-std=c++17", "-ffp-contract=off", "-fPIC", "-shared", "-pthread",
                                _SRC, "-o", _LIB])
     return _LIB
 
@@ -89,6 +89,8 @@ def lib():
         L.orc_spmv.argtypes = [i64, i32, vp, vp, vp, vp, vp]
         L.orc_cg_jacobi.restype = i32
         L.orc_cg_jacobi.argtypes = [i64, i32, vp, vp, vp, vp, vp, i64, dp, i32, P(i64), P(dp), vp]
+        L.orc_cg_block_jacobi.restype = i32
+        L.orc_cg_block_jacobi.argtypes = [i64, i32, vp, vp, vp, vp, vp, i32, i64, dp, P(i64), P(dp)]
         L.orc_gmres_jacobi.restype = i32
         L.orc_gmres_jacobi.argtypes = [i64, i32, vp, vp, vp, vp, vp, i32, i64, dp, P(i64), P(dp)]
         _lib = L
@@ -220,6 +222,15 @@ def cg_jacobi(sym, ia, ja, a, b, maxit, tol, jacobi_residual=False, history=Fals
     if history:
         out["hist"] = hist[: it.value].copy()
     return out
+
+
+def cg_block_jacobi(sym, ia, ja, a, b, bs, maxit, tol):
+    n = len(ia) - 1
+    x = np.zeros(n)
+    it, res = ctypes.c_int64(), ctypes.c_double()
+    rc = lib().orc_cg_block_jacobi(n, int(sym), _p(ia), _p(ja), _p(a), _p(np.ascontiguousarray(b)), _p(x), bs, maxit,
+                                   tol, ctypes.byref(it), ctypes.byref(res))
+    return dict(x=x, iters=it.value, resid=res.value, rc=rc)
 
 
 def gmres_jacobi(sym, ia, ja, a, b, m, maxit, tol):

@@ -1218,6 +1218,78 @@ int orc_cg_jacobi(int64_t n, int sym, const int64_t *IA, const int64_t *JA, cons
   return 1;
 }
 
+// CG with a block-Jacobi preconditioner over consecutive equation blocks of
+// size bs (TPZBlockDiagonal, Matrix/pzblockdiag.h:21, built over the mesh's
+// connect blocks as TPZAnalysis::BuildPreconditioner(EBlockJacobi) does for
+// one-shape connects, Analysis/TPZAnalysis.cpp:995-1090); blocks inverted by
+// Gaussian elimination with partial pivoting.
+int orc_cg_block_jacobi(int64_t n, int sym, const int64_t *IA, const int64_t *JA, const double *A, const double *b,
+                        double *x, int bs, int64_t maxit, double tol, int64_t *iters_out, double *resid_out) {
+  int64_t nb = n / bs;
+  std::vector<double> inv((size_t)nb * bs * bs, 0.0);
+  for (int64_t B = 0; B < nb; B++) {
+    std::vector<double> m((size_t)bs * bs, 0.0), e((size_t)bs * bs, 0.0);
+    for (int s = 0; s < bs; s++) {
+      int64_t r = B * bs + s;
+      for (int64_t k = IA[r]; k < IA[r + 1]; k++) {
+        int64_t c = JA[k];
+        if (c >= B * bs && c < (B + 1) * bs) {
+          m[s * bs + (c - B * bs)] = A[k];
+          if (sym) m[(c - B * bs) * bs + s] = A[k];
+        }
+      }
+      e[s * bs + s] = 1.0;
+    }
+    for (int col = 0; col < bs; col++) {
+      int piv = col;
+      for (int r = col + 1; r < bs; r++)
+        if (std::fabs(m[r * bs + col]) > std::fabs(m[piv * bs + col])) piv = r;
+      for (int k = 0; k < bs; k++) { std::swap(m[col * bs + k], m[piv * bs + k]); std::swap(e[col * bs + k], e[piv * bs + k]); }
+      double d = m[col * bs + col];
+      for (int k = 0; k < bs; k++) { m[col * bs + k] /= d; e[col * bs + k] /= d; }
+      for (int r = 0; r < bs; r++) {
+        if (r == col) continue;
+        double f = m[r * bs + col];
+        for (int k = 0; k < bs; k++) { m[r * bs + k] -= f * m[col * bs + k]; e[r * bs + k] -= f * e[col * bs + k]; }
+      }
+    }
+    std::copy(e.begin(), e.end(), inv.begin() + (size_t)B * bs * bs);
+  }
+  auto M = [&](const double *r, double *z) {
+    for (int64_t B = 0; B < nb; B++)
+      for (int s = 0; s < bs; s++) {
+        double acc = 0.0;
+        for (int t = 0; t < bs; t++) acc += inv[(size_t)B * bs * bs + s * bs + t] * r[B * bs + t];
+        z[B * bs + s] = acc;
+      }
+  };
+  std::vector<double> r(n), z(n), p(n), q(n);
+  double normb = std::sqrt(dot(n, b, b));
+  for (int64_t i = 0; i < n; i++) { x[i] = 0.0; r[i] = b[i]; }
+  if (normb == 0.0) normb = 1.0;
+  double resid = std::sqrt(dot(n, r.data(), r.data())) / normb;
+  if (resid <= tol) { *iters_out = 0; *resid_out = resid; return 0; }
+  double rho = 0, rho_1 = 0;
+  for (int64_t it = 1; it <= maxit; it++) {
+    M(r.data(), z.data());
+    rho = dot(n, r.data(), z.data());
+    if (it == 1) p = z;
+    else {
+      double beta = rho / rho_1;
+      for (int64_t i = 0; i < n; i++) p[i] = z[i] + beta * p[i];
+    }
+    orc_spmv(n, sym, IA, JA, A, p.data(), q.data());
+    double alpha = rho / dot(n, p.data(), q.data());
+    for (int64_t i = 0; i < n; i++) { x[i] += alpha * p[i]; r[i] -= alpha * q[i]; }
+    resid = std::sqrt(dot(n, r.data(), r.data())) / normb;
+    if (resid <= tol) { *iters_out = it; *resid_out = resid; return 0; }
+    rho_1 = rho;
+  }
+  *iters_out = maxit;
+  *resid_out = resid;
+  return 1;
+}
+
 // Restarted, left-preconditioned GMRES(m) with Jacobi: Solvers/LinearSolvers/gmres.h:68-168
 // (MGS Arnoldi, Givens rotations, Update back-solve :20-35).
 int orc_gmres_jacobi(int64_t n, int sym, const int64_t *IA, const int64_t *JA, const double *A, const double *b, double *x,

@@ -7,8 +7,11 @@ Tolerances (FP64 path):
   (the GPU sums element contributions in colour order, the reference in
   element order, and forms the Gram before the material combination);
 * load vector: max |f_gpu - f_ref| <= 1e-12 * max |f_ref|;
-* Jacobi-PCG: same stopping rule, iteration count within +-1 of the oracle,
-  solution within 1e-8 relative.
+* Jacobi-PCG: same algorithm and stopping rule; solution within 1e-8
+  relative.  With penalty Dirichlet rows (1e12 .. 6.7e16 on the diagonal) the
+  iteration count depends on the summation order (the oracle itself gives
+  different counts with and without fused multiply-adds), so counts must agree
+  within max(3, 10%).
 """
 import numpy as np
 import pytest
@@ -106,8 +109,8 @@ def test_jacobi_pcg_matches_oracle(built, case):
     oa, of = om.assemble(True, oia, oja)
     ref = O.cg_jacobi(True, oia, oja, oa, of, 20000, tol)
     assert sol["rc"] == 0 and ref["rc"] == 0
-    assert abs(sol["iterations"] - ref["iters"]) <= 1
     assert np.linalg.norm(sol["x"] - ref["x"]) <= 1e-8 * np.linalg.norm(ref["x"])
+    assert abs(sol["iterations"] - ref["iters"]) <= max(3, 0.1 * ref["iters"]), (sol["iterations"], ref["iters"])
     ctx.close()
 
 
@@ -146,4 +149,43 @@ def test_mixed_cg_reaches_true_fp64_residual(built, case):
     # test asks for the true-residual criterion and a small forward error
     err = np.linalg.norm(sol["x"] - ref["x"]) / np.linalg.norm(ref["x"])
     assert err <= 1e-5, err
+    ctx.close()
+
+
+@pytest.mark.parametrize("case", ["elast3d_p1", "elast3d_p2"])
+def test_block_jacobi_pcg_matches_oracle(built, case):
+    """Connect-block (3x3) Jacobi CG against the oracle's TPZBlockDiagonal-preconditioned CG."""
+    g = _gpz()
+    mk_o, mk_g = built[case]
+    om, grid = mk_o(), mk_g()
+    ctx = g.Context(0)
+    ctx.upload_mesh(grid)
+    ctx.build_pattern(True)
+    ctx.assemble()
+    tol = 1e-10
+    sol = ctx.solve(precond=g.GPZ_PRECOND_BLOCK_JACOBI, tol=tol, max_iter=20000)
+    oia, oja = om.pattern(True)
+    oa, of = om.assemble(True, oia, oja)
+    ref = O.cg_block_jacobi(True, oia, oja, oa, of, 3, 20000, tol)
+    assert sol["rc"] == 0 and ref["rc"] == 0
+    assert np.linalg.norm(sol["x"] - ref["x"]) <= 1e-8 * np.linalg.norm(ref["x"])
+    assert abs(sol["iterations"] - ref["iters"]) <= max(3, 0.1 * ref["iters"]), (sol["iterations"], ref["iters"])
+    ctx.close()
+
+
+def test_mixed_block_jacobi_bsr3(built):
+    """FP32 3x3 block-CSR SpMV + block Jacobi: the mixed path of the elasticity benchmark."""
+    g = _gpz()
+    mk_o, mk_g = built["elast3d_p2"]
+    om, grid = mk_o(), mk_g()
+    ctx = g.Context(0)
+    ctx.upload_mesh(grid)
+    ctx.build_pattern(False)
+    ctx.assemble(g.GPZ_PREC_MIXED)
+    sol = ctx.solve(solver=g.GPZ_SOLVER_MIXED_CG, precond=g.GPZ_PRECOND_BLOCK_JACOBI, tol=1e-8, reliable_delta=1e-2)
+    assert sol["rc"] == 0 and sol["true_resid"] <= 1e-8 and sol["spmv_fp32"] > 0
+    oia, oja = om.pattern(True)
+    oa, of = om.assemble(True, oia, oja)
+    ref = O.cg_jacobi(True, oia, oja, oa, of, 20000, 1e-12)
+    assert np.linalg.norm(sol["x"] - ref["x"]) <= 1e-5 * np.linalg.norm(ref["x"])
     ctx.close()
