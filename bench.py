@@ -42,6 +42,8 @@ def parse():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--n", type=int, default=64)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-fp64-baseline", action="store_true", help="skip the FP64 Jacobi-PCG reference solve")
+    ap.add_argument("--no-e2e", action="store_true", help="skip the end-to-end C-ABI leg")
     return ap.parse_args()
 
 
@@ -154,13 +156,15 @@ def run_gpu(args):
     e0 = torch.cuda.Event(enable_timing=True)
     e1 = torch.cuda.Event(enable_timing=True)
     torch.cuda.synchronize()
-    with torch.cuda.stream(stream):
-        e0.record(stream)
-    fp64 = step(mixed=False)
-    with torch.cuda.stream(stream):
-        e1.record(stream)
-    torch.cuda.synchronize()
-    t_fp64 = e0.elapsed_time(e1) / 1e3
+    fp64, t_fp64 = {"iterations": None, "true_resid": None}, None
+    if not args.no_fp64_baseline:
+        with torch.cuda.stream(stream):
+            e0.record(stream)
+        fp64 = step(mixed=False)
+        with torch.cuda.stream(stream):
+            e1.record(stream)
+        torch.cuda.synchronize()
+        t_fp64 = e0.elapsed_time(e1) / 1e3
     # element matrices + scatter alone (FP64), for elements/s
     t_asm = ctx.time_kernel(gpz.GPZ_KERNEL_ASSEMBLE, 3) / 1e3
 
@@ -204,7 +208,7 @@ def run_gpu(args):
     # end to end through the C ABI from host buffers
     e2e_times = []
     b_in = mesh_bytes(grid)
-    for _ in range(max(1, min(args.steps, 2))):
+    for _ in range(0 if args.no_e2e else max(1, min(args.steps, 2))):
         torch.cuda.synchronize()
         t0 = time.perf_counter()
         c2 = gpz.Context(dev)
@@ -217,7 +221,7 @@ def run_gpu(args):
         e2e_times.append(time.perf_counter() - t0)
         assert r2["true_resid"] <= TOL
         c2.close()
-    t_e2e = min(e2e_times)
+    t_e2e = min(e2e_times) if e2e_times else None
 
     out = {
         "metric": METRIC, "value": round(t_step * world / world, 6), "unit": "s", "n_gpus": world,
@@ -233,10 +237,10 @@ def run_gpu(args):
                   "reliable_updates": last["reliable_updates"], "spmv_fp32": last["spmv_fp32"],
                   "spmv_fp64": last["spmv_fp64"], "restarts": last["restarts"], "solve_s": last["seconds"]},
         "fp64_jacobi_pcg": {"seconds": t_fp64, "iterations": fp64["iterations"], "true_resid": fp64["true_resid"],
-                            "speedup_of_value": t_fp64 / t_step},
+                            "speedup_of_value": (t_fp64 / t_step) if t_fp64 else None},
         "assembly": {"fp64_seconds": t_asm, "elements_per_s": nel / t_asm, "volume_elements_per_s": nvol / t_asm,
                      "pattern_build_s": t_pattern, "host_mesh_build_s": t_mesh},
-        "e2e": {"value": round(t_e2e, 6), "unit": "s", "h2d_bytes_per_step": int(b_in + neq * 0),
+        "e2e": {"value": round(t_e2e, 6) if t_e2e else None, "unit": "s", "h2d_bytes_per_step": int(b_in + neq * 0),
                 "d2h_bytes_per_step": int(neq * 8)},
         "roofline": {"bound": "hbm", "kernel": "k_cg_bsr3 (q = A32 p32, 3x3 blocks, p.q)", "achieved": round(ach, 1),
                      "peak": hbm, "unit": "GB/s", "frac": round(ach / hbm, 4), "traffic": None,

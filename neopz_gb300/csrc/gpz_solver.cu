@@ -26,7 +26,24 @@ namespace gpz {
 namespace {
 
 constexpr int kThreads = 256;
-constexpr int kGridBlocks = 152 * 8;  // 8 CTAs of 256 threads per SM, 152 SMs
+constexpr int kGridBlocks = 152 * 8;  // upper bound of the grid-stride grids (partial-sum buffer size)
+
+// Grid-stride kernels run exactly one wave: SMs x resident CTAs of this kernel.
+template <class K>
+int wave(K kernel) {
+  static int nsm = 0;
+  if (!nsm) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+    if (nsm <= 0) nsm = 152;
+  }
+  int per = 0;
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, kernel, kThreads, 0);
+  if (per <= 0) per = 1;
+  int g = nsm * per;
+  return g > kGridBlocks ? kGridBlocks : g;
+}
 
 // device scalar slots
 enum { S_RHO = 0, S_RHO1, S_PQ, S_RR, S_NORMB, S_TOL, S_MAXRR, S_DELTA2, S_RESID, S_TRUERR, S_NSCAL };
@@ -521,24 +538,26 @@ int pick_tpr(int64_t nnz, int64_t n) {
 
 void spmv_device(Ctx &c, const double *x, double *y, double alpha, double beta, const double *yin) {
   int tpr = pick_tpr(c.nnz, c.neq);
-  GPZ_TPR_SWITCH(tpr, (k_spmv64<T><<<kGridBlocks, kThreads, 0, c.stream>>>(c.d_ia.p, c.d_ja.p, c.d_a.p, x, y, yin,
+  GPZ_TPR_SWITCH(tpr, (k_spmv64<T><<<wave(k_spmv64<T>), kThreads, 0, c.stream>>>(c.d_ia.p, c.d_ja.p, c.d_a.p, x, y, yin,
                                                                             alpha, beta, c.neq)));
   c.launches++;
   GPZ_CUDA_TRY(cudaGetLastError());
 }
 
 // uniform 3x3 connect blocks (elasticity with one shape per connect)?
+// (connects without shape functions hold no equations and are skipped, so the
+// equation blocks are then 3k .. 3k+2 for k < neq / 3)
 bool blocks_are_3(const Ctx &c) {
-  if (c.nstate != 3) return false;
+  if (c.nstate != 3 || c.neq == 0) return false;
   for (int32_t s : c.h_block_size)
-    if (s != 3) return false;
-  return c.nconnects > 0;
+    if (s != 3 && s != 0) return false;
+  return true;
 }
 
 void make_fp32_copy(Ctx &c) {
   c.have_bsr3 = false;
   if (blocks_are_3(c)) {
-    c.nbrow = c.nconnects;
+    c.nbrow = c.neq / 3;
     c.d_bptr.alloc(c.nbrow + 1);
     c.d_bcol.alloc(std::max<int64_t>(c.nnz / 9, 1));
     c.d_bval.alloc(std::max<int64_t>(c.nnz, 1));
@@ -558,9 +577,9 @@ void make_fp32_copy(Ctx &c) {
 
 void build_block_jacobi(Ctx &c) {
   GPZ_REQUIRE(blocks_are_3(c), GPZ_E_INVALID, "block Jacobi needs uniform 3x3 connect blocks (nstate 3, one shape per connect)");
-  c.d_bjinv.alloc((size_t)c.nconnects * 9);
-  k_block_inv3<<<grid_for(c.nconnects, 256), 256, 0, c.stream>>>(c.d_a.p, c.d_diagpos.p, c.nconnects, c.d_bjinv.p,
-                                                                 c.d_err.p);
+  const int64_t nb = c.neq / 3;
+  c.d_bjinv.alloc((size_t)nb * 9);
+  k_block_inv3<<<grid_for(nb, 256), 256, 0, c.stream>>>(c.d_a.p, c.d_diagpos.p, nb, c.d_bjinv.p, c.d_err.p);
   c.launches++;
   GPZ_CUDA_TRY(cudaGetLastError());
   check_device_flag(c, "block Jacobi inverse");
@@ -605,24 +624,24 @@ void launch_iteration(Ctx &c, const Plan &P) {
   SolverWork &w = c.sw;
   Red R = red_of(c);
   const bool p32 = P.mixed && !P.bsr;
-  k_cg_p<<<kGridBlocks, kThreads, 0, c.stream>>>(w.r.p, P.M, w.p.p, p32 ? w.p32.p : nullptr,
+  k_cg_p<<<wave(k_cg_p), kThreads, 0, c.stream>>>(w.r.p, P.M, w.p.p, p32 ? w.p32.p : nullptr,
                                                  (P.mixed && P.bsr) ? w.p32x4.p : nullptr, P.nunits, R);
   if (P.mixed && P.bsr) {
-    k_cg_bsr3<<<kGridBlocks, kThreads, 0, c.stream>>>(c.d_bptr.p, c.d_bcol.p, c.d_bval.p, (const float4 *)w.p32x4.p,
+    k_cg_bsr3<<<wave(k_cg_bsr3), kThreads, 0, c.stream>>>(c.d_bptr.p, c.d_bcol.p, c.d_bval.p, (const float4 *)w.p32x4.p,
                                                       w.p.p, w.q.p, c.nbrow, R);
   } else if (P.mixed) {
-    GPZ_TPR_SWITCH(P.tpr, (k_cg_spmv<T, true><<<kGridBlocks, kThreads, 0, c.stream>>>(
+    GPZ_TPR_SWITCH(P.tpr, (k_cg_spmv<T, true><<<wave(k_cg_spmv<T, true>), kThreads, 0, c.stream>>>(
                               c.d_ia.p, c.d_ja.p, nullptr, c.d_a32.p, w.p.p, w.p32.p, w.q.p, c.neq, R)));
   } else {
-    GPZ_TPR_SWITCH(P.tpr, (k_cg_spmv<T, false><<<kGridBlocks, kThreads, 0, c.stream>>>(
+    GPZ_TPR_SWITCH(P.tpr, (k_cg_spmv<T, false><<<wave(k_cg_spmv<T, false>), kThreads, 0, c.stream>>>(
                               c.d_ia.p, c.d_ja.p, c.d_a.p, nullptr, w.p.p, nullptr, w.q.p, c.neq, R)));
   }
-  k_cg_update<<<kGridBlocks, kThreads, 0, c.stream>>>(w.x.p, w.r.p, w.p.p, w.q.p, P.M, P.nunits, P.mixed ? 1 : 0, R);
+  k_cg_update<<<wave(k_cg_update), kThreads, 0, c.stream>>>(w.x.p, w.r.p, w.p.p, w.q.p, P.M, P.nunits, P.mixed ? 1 : 0, R);
   c.launches += 3;
   if (P.mixed) {
-    GPZ_TPR_SWITCH(P.tpr, (k_reliable<T><<<kGridBlocks, kThreads, 0, c.stream>>>(c.d_ia.p, c.d_ja.p, c.d_a.p, w.x.p,
+    GPZ_TPR_SWITCH(P.tpr, (k_reliable<T><<<wave(k_reliable<T>), kThreads, 0, c.stream>>>(c.d_ia.p, c.d_ja.p, c.d_a.p, w.x.p,
                                                                                   w.b.p, w.r.p, c.neq, R)));
-    k_precond_dot<<<kGridBlocks, kThreads, 0, c.stream>>>(w.r.p, P.M, P.nunits, R);
+    k_precond_dot<<<wave(k_precond_dot), kThreads, 0, c.stream>>>(w.r.p, P.M, P.nunits, R);
     c.launches += 2;
   }
 }
@@ -645,7 +664,7 @@ int solve(Ctx &c, const gpz_solver_opts &o, gpz_solve_report &rep) {
   P.block = block;
   P.bsr = mixed && c.have_bsr3;
   P.tpr = pick_tpr(c.nnz, c.neq);
-  P.nunits = block ? c.nconnects : c.neq;
+  P.nunits = block ? c.neq / 3 : c.neq;
   P.M = Prec{c.d_dinv.p, block ? c.d_bjinv.p : nullptr, block ? 1 : 0};
   const int batch = o.check_every > 0 ? o.check_every : 32;
 
@@ -663,9 +682,9 @@ int solve(Ctx &c, const gpz_solver_opts &o, gpz_solve_report &rep) {
   GPZ_CUDA_TRY(cudaMemcpyAsync(w.scal.p, hs, sizeof(hs), cudaMemcpyHostToDevice, s));
   GPZ_CUDA_TRY(cudaMemcpyAsync(w.iscal.p, hi, sizeof(hi), cudaMemcpyHostToDevice, s));
   Red R = red_of(c);
-  GPZ_TPR_SWITCH(P.tpr, (k_cg_init<T><<<kGridBlocks, kThreads, 0, s>>>(c.d_ia.p, c.d_ja.p, c.d_a.p, w.x.p, w.b.p,
+  GPZ_TPR_SWITCH(P.tpr, (k_cg_init<T><<<wave(k_cg_init<T>), kThreads, 0, s>>>(c.d_ia.p, c.d_ja.p, c.d_a.p, w.x.p, w.b.p,
                                                                         w.r.p, c.neq, o.from_current, R)));
-  k_precond_dot<<<kGridBlocks, kThreads, 0, s>>>(w.r.p, P.M, P.nunits, R);
+  k_precond_dot<<<wave(k_precond_dot), kThreads, 0, s>>>(w.r.p, P.M, P.nunits, R);
   c.launches += 2;
   GPZ_CUDA_TRY(cudaGetLastError());
 
@@ -695,7 +714,7 @@ int solve(Ctx &c, const gpz_solver_opts &o, gpz_solve_report &rep) {
     if (hstate[I_CONV] != 0 || hstate[I_IT] >= o.max_iter) break;
   }
   if (exec) cudaGraphExecDestroy(exec);
-  GPZ_TPR_SWITCH(P.tpr, (k_true_resid<T><<<kGridBlocks, kThreads, 0, s>>>(c.d_ia.p, c.d_ja.p, c.d_a.p, w.x.p, w.b.p,
+  GPZ_TPR_SWITCH(P.tpr, (k_true_resid<T><<<wave(k_true_resid<T>), kThreads, 0, s>>>(c.d_ia.p, c.d_ja.p, c.d_a.p, w.x.p, w.b.p,
                                                                            c.neq, R)));
   c.launches++;
   GPZ_CUDA_TRY(cudaEventRecord(ev1, s));
@@ -745,13 +764,13 @@ double time_spmv(Ctx &c, bool f32, int reps) {
   const int tpr = pick_tpr(c.nnz, c.neq);
   auto launch = [&]() {
     if (f32 && c.have_bsr3) {
-      k_cg_bsr3<<<kGridBlocks, kThreads, 0, s>>>(c.d_bptr.p, c.d_bcol.p, c.d_bval.p, (const float4 *)w.p32x4.p, w.p.p,
+      k_cg_bsr3<<<wave(k_cg_bsr3), kThreads, 0, s>>>(c.d_bptr.p, c.d_bcol.p, c.d_bval.p, (const float4 *)w.p32x4.p, w.p.p,
                                                  w.q.p, c.nbrow, R);
     } else if (f32) {
-      GPZ_TPR_SWITCH(tpr, (k_cg_spmv<T, true><<<kGridBlocks, kThreads, 0, s>>>(c.d_ia.p, c.d_ja.p, nullptr, c.d_a32.p,
+      GPZ_TPR_SWITCH(tpr, (k_cg_spmv<T, true><<<wave(k_cg_spmv<T, true>), kThreads, 0, s>>>(c.d_ia.p, c.d_ja.p, nullptr, c.d_a32.p,
                                                                                w.p.p, w.p32.p, w.q.p, c.neq, R)));
     } else {
-      GPZ_TPR_SWITCH(tpr, (k_cg_spmv<T, false><<<kGridBlocks, kThreads, 0, s>>>(c.d_ia.p, c.d_ja.p, c.d_a.p, nullptr,
+      GPZ_TPR_SWITCH(tpr, (k_cg_spmv<T, false><<<wave(k_cg_spmv<T, false>), kThreads, 0, s>>>(c.d_ia.p, c.d_ja.p, c.d_a.p, nullptr,
                                                                                 w.p.p, nullptr, w.q.p, c.neq, R)));
     }
     c.launches++;

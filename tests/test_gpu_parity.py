@@ -11,7 +11,9 @@ Tolerances (FP64 path):
   relative.  With penalty Dirichlet rows (1e12 .. 6.7e16 on the diagonal) the
   iteration count depends on the summation order (the oracle itself gives
   different counts with and without fused multiply-adds), so counts must agree
-  within max(3, 10%).
+  within max(3, 10%) -- 30% for the 6.7e16-penalty Poisson/Darcy systems,
+  where sequential, numpy and GPU row sums already give 34 / 28 / 27
+  iterations on the 16x16 Q2 case.
 """
 import numpy as np
 import pytest
@@ -110,7 +112,8 @@ def test_jacobi_pcg_matches_oracle(built, case):
     ref = O.cg_jacobi(True, oia, oja, oa, of, 20000, tol)
     assert sol["rc"] == 0 and ref["rc"] == 0
     assert np.linalg.norm(sol["x"] - ref["x"]) <= 1e-8 * np.linalg.norm(ref["x"])
-    assert abs(sol["iterations"] - ref["iters"]) <= max(3, 0.1 * ref["iters"]), (sol["iterations"], ref["iters"])
+    frac = 0.3 if case.startswith(("poisson", "darcy")) else 0.1
+    assert abs(sol["iterations"] - ref["iters"]) <= max(3, frac * ref["iters"]), (sol["iterations"], ref["iters"])
     ctx.close()
 
 
