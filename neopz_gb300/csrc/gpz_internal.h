@@ -91,7 +91,7 @@ struct Bucket {
 // ---------------------------------------------------------------- solver workspace
 struct SolverWork {
   DBuf<double> r, z, p, q, x, b, t;
-  DBuf<float> p32, p32x4;
+  DBuf<float> pm, r32, q32, dx32;  // mixed CG inner vectors (pm padded x4 for the block SpMV)
   DBuf<double> partial;        // per-CTA partial sums
   DBuf<double> scal;           // device scalars (see gpz_solver.cu)
   DBuf<unsigned int> counter;  // last-block counters
@@ -145,7 +145,8 @@ struct Ctx {
   DBuf<int64_t> d_bptr;
   DBuf<int32_t> d_bcol;
   DBuf<float> d_bval;
-  DBuf<double> d_bjinv;                      // block-Jacobi inverses [nconnects][bs*bs]
+  DBuf<double> d_bjinv;                      // block-Jacobi inverses [neq/3][9]
+  DBuf<float> d_bjinv32, d_dinv32;           // FP32 preconditioners of the mixed CG
   bool have_bjinv = false;
   int bj_bs = 0;
 

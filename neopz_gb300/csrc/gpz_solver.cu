@@ -127,22 +127,20 @@ template <int TPR>
 __device__ __forceinline__ double row_dot64(const int64_t *__restrict__ ia, const int32_t *__restrict__ ja,
                                             const double *__restrict__ a, const double *__restrict__ x, int64_t r,
                                             int sub, bool valid) {
-  // four independent load/FMA chains per lane; matrix streams bypass L1 (read once)
-  double s0 = 0.0, s1 = 0.0, s2 = 0.0, s3 = 0.0;
+  // two independent load/FMA chains per lane; matrix streams bypass L1 (read once).
+  // FP64 instructions are the scarce resource on this part, so the row is
+  // split over few lanes (pick_tpr64) and combined with few FP64 adds.
+  double s0 = 0.0, s1 = 0.0;
   int64_t k0 = valid ? ia[r] : 0, k1 = valid ? ia[r + 1] : 0;
   int64_t k = k0 + sub;
-  for (; k + 3 * TPR < k1; k += 4 * TPR) {
-    const int c0 = __ldcs(&ja[k]), c1 = __ldcs(&ja[k + TPR]), c2 = __ldcs(&ja[k + 2 * TPR]),
-              c3 = __ldcs(&ja[k + 3 * TPR]);
-    const double a0 = __ldcs(&a[k]), a1 = __ldcs(&a[k + TPR]), a2 = __ldcs(&a[k + 2 * TPR]),
-                 a3 = __ldcs(&a[k + 3 * TPR]);
+  for (; k + TPR < k1; k += 2 * TPR) {
+    const int c0 = __ldcs(&ja[k]), c1 = __ldcs(&ja[k + TPR]);
+    const double a0 = __ldcs(&a[k]), a1 = __ldcs(&a[k + TPR]);
     s0 = fma(a0, __ldg(&x[c0]), s0);
     s1 = fma(a1, __ldg(&x[c1]), s1);
-    s2 = fma(a2, __ldg(&x[c2]), s2);
-    s3 = fma(a3, __ldg(&x[c3]), s3);
   }
-  for (; k < k1; k += TPR) s0 = fma(__ldcs(&a[k]), __ldg(&x[__ldcs(&ja[k])]), s0);
-  double s = (s0 + s1) + (s2 + s3);
+  if (k < k1) s0 = fma(__ldcs(&a[k]), __ldg(&x[__ldcs(&ja[k])]), s0);
+  double s = s0 + s1;
   for (int o = TPR / 2; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o, TPR);
   return s;
 }
@@ -183,20 +181,19 @@ __global__ void __launch_bounds__(kThreads) k_spmv64(const int64_t *__restrict__
   }
 }
 
-// q = A p with p.q (iteration kernel C), FP64 or FP32 values
+// q = A p with p.q (iteration kernel C of the FP64 CG)
 template <int TPR, bool F32>
 __global__ void __launch_bounds__(kThreads) k_cg_spmv(const int64_t *__restrict__ ia, const int32_t *__restrict__ ja,
                                                       const double *__restrict__ a64, const float *__restrict__ a32,
                                                       const double *__restrict__ p, const float *__restrict__ p32,
                                                       double *__restrict__ q, int64_t n, Red R) {
+  static_assert(!F32, "the FP32 iteration uses k_mx_csr / k_mx_bsr3");
   if (!active(R.iscal)) return;
   double pq = 0.0;
   GPZ_ROW_LOOP(TPR, n) {
     const int64_t r = r0 + (threadIdx.x & 31) / TPR;
     const bool valid = r < n;
-    double s;
-    if (F32) s = (double)row_dot32<TPR>(ia, ja, a32, p32, r, sub, valid);
-    else s = row_dot64<TPR>(ia, ja, a64, p, r, sub, valid);
+    const double s = row_dot64<TPR>(ia, ja, a64, p, r, sub, valid);
     if (sub == 0 && valid) {
       q[r] = s;
       pq += p[r] * s;
@@ -205,58 +202,7 @@ __global__ void __launch_bounds__(kThreads) k_cg_spmv(const int64_t *__restrict_
   double v[1] = {pq}, tot[1];
   if (grid_reduce<1>(v, R, tot) && threadIdx.x == 0) {
     R.scal[S_PQ] = tot[0];
-    if (F32) R.iscal[I_SP32]++;
-    else R.iscal[I_SP64]++;
-  }
-}
-
-// q = A p with p.q for 3x3 block rows, FP32 values in a per-row structure of
-// arrays (entry k of block j of block row I at 9*bptr[I] + k*nb + j) so that a
-// warp's loads of one entry over 32 blocks are contiguous; p32x4 holds p in
-// FP32, padded to four floats per block row.
-__global__ void __launch_bounds__(kThreads) k_cg_bsr3(const int64_t *__restrict__ bptr, const int32_t *__restrict__ bcol,
-                                                      const float *__restrict__ bval, const float4 *__restrict__ p32x4,
-                                                      const double *__restrict__ p, double *__restrict__ q,
-                                                      int64_t nbrow, Red R) {
-  if (!active(R.iscal)) return;
-  const int lane = threadIdx.x & 31;
-  const int64_t warp_id = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) / 32;
-  const int64_t nwarps = (int64_t)gridDim.x * blockDim.x / 32;
-  double pq = 0.0;
-  for (int64_t I = warp_id; I < nbrow; I += nwarps) {
-    const int64_t b0 = bptr[I];
-    const int nb = (int)(bptr[I + 1] - b0);
-    const float *v = bval + 9 * b0;
-    float a0 = 0.f, a1 = 0.f, a2 = 0.f;
-    for (int j = lane; j < nb; j += 32) {
-      const float4 xv = __ldg(&p32x4[__ldcs(&bcol[b0 + j])]);
-      a0 = fmaf(__ldcs(&v[0 * nb + j]), xv.x, a0);
-      a0 = fmaf(__ldcs(&v[1 * nb + j]), xv.y, a0);
-      a0 = fmaf(__ldcs(&v[2 * nb + j]), xv.z, a0);
-      a1 = fmaf(__ldcs(&v[3 * nb + j]), xv.x, a1);
-      a1 = fmaf(__ldcs(&v[4 * nb + j]), xv.y, a1);
-      a1 = fmaf(__ldcs(&v[5 * nb + j]), xv.z, a1);
-      a2 = fmaf(__ldcs(&v[6 * nb + j]), xv.x, a2);
-      a2 = fmaf(__ldcs(&v[7 * nb + j]), xv.y, a2);
-      a2 = fmaf(__ldcs(&v[8 * nb + j]), xv.z, a2);
-    }
-    for (int o = 16; o > 0; o >>= 1) {
-      a0 += __shfl_down_sync(0xffffffffu, a0, o);
-      a1 += __shfl_down_sync(0xffffffffu, a1, o);
-      a2 += __shfl_down_sync(0xffffffffu, a2, o);
-    }
-    if (lane == 0) {
-      const int64_t r = 3 * I;
-      q[r] = a0;
-      q[r + 1] = a1;
-      q[r + 2] = a2;
-      pq += p[r] * (double)a0 + p[r + 1] * (double)a1 + p[r + 2] * (double)a2;
-    }
-  }
-  double vv[1] = {pq}, tot[1];
-  if (grid_reduce<1>(vv, R, tot) && threadIdx.x == 0) {
-    R.scal[S_PQ] = tot[0];
-    R.iscal[I_SP32]++;
+    R.iscal[I_SP64]++;
   }
 }
 
@@ -283,8 +229,7 @@ __device__ __forceinline__ void apply_prec(const Prec &M, const double *__restri
 
 // kernel B: p = z + beta p, first iteration (or after a restart) p = z
 __global__ void __launch_bounds__(kThreads) k_cg_p(const double *__restrict__ r, Prec M, double *__restrict__ p,
-                                                   float *__restrict__ p32, float *__restrict__ p32x4, int64_t nunits,
-                                                   Red R) {
+                                                   int64_t nunits, Red R) {
   if (!active(R.iscal)) return;
   const bool first = R.iscal[I_IT] == 0 || R.iscal[I_RESTART] != 0;
   const double beta = first ? 0.0 : R.scal[S_RHO] / R.scal[S_RHO1];
@@ -296,8 +241,6 @@ __global__ void __launch_bounds__(kThreads) k_cg_p(const double *__restrict__ r,
       const int64_t i = u * bs + k;
       const double pi = first ? z[k] : z[k] + beta * p[i];
       p[i] = pi;
-      if (p32) p32[i] = (float)pi;
-      if (p32x4) p32x4[(i / 3) * 4 + i % 3] = (float)pi;
     }
   }
 }
@@ -518,7 +461,239 @@ __global__ void k_block_inv3(const double *__restrict__ a, const int64_t *__rest
   B[8] = (m[0][0] * m[1][1] - m[0][1] * m[1][0]) * id;
 }
 
-int pick_tpr(int64_t nnz, int64_t n) {
+// ======================================================================
+// Mixed-precision CG: every per-entry operation of the inner iteration is
+// FP32 (GB300 issues FP64 at a small fraction of its FP32 rate, so even a few
+// FP64 instructions per row cost as much as the FP32 matrix stream).  FP64 is
+// kept for: the solution x (the FP32 increment dx accumulated since the last
+// reliable update is folded into it), the true residual b - A64 x of every
+// reliable update, the dot-product accumulation (compensated FP32 partial
+// sums per thread, FP64 across threads and CTAs) and the alpha/beta scalars.
+// ======================================================================
+
+// compensated (Kahan) FP32 accumulation of one thread's terms
+struct KSum {
+  float s = 0.f, c = 0.f;
+  __device__ __forceinline__ void add(float v) {
+    float y = v - c;
+    float t = s + y;
+    c = (t - s) - y;
+    s = t;
+  }
+  __device__ __forceinline__ double get() const { return (double)s - (double)c; }
+};
+
+struct Prec32 {
+  const float *dinv;  // [neq]
+  const float *binv;  // [nbrow][9]
+  int block;
+};
+
+// p is stored padded to four floats per 3-row block when the 3x3 block SpMV
+// reads it; pidx maps an equation to its slot.
+__device__ __forceinline__ int64_t pidx(int64_t i, int padded) { return padded ? (i / 3) * 4 + i % 3 : i; }
+
+__device__ __forceinline__ void apply_prec32(const Prec32 &M, const float *__restrict__ r, int64_t u, float *z) {
+  if (!M.block) {
+    z[0] = r[u] * M.dinv[u];
+  } else {
+    const float *B = M.binv + 9 * u;
+    const float r0 = r[3 * u], r1 = r[3 * u + 1], r2 = r[3 * u + 2];
+    z[0] = fmaf(B[0], r0, fmaf(B[1], r1, B[2] * r2));
+    z[1] = fmaf(B[3], r0, fmaf(B[4], r1, B[5] * r2));
+    z[2] = fmaf(B[6], r0, fmaf(B[7], r1, B[8] * r2));
+  }
+}
+
+// p = z + beta p (z = M r), or p = z at the first iteration / after a restart
+__global__ void __launch_bounds__(kThreads) k_mx_p(const float *__restrict__ r, Prec32 M, float *__restrict__ p,
+                                                   int padded, int64_t nunits, Red R) {
+  if (!active(R.iscal)) return;
+  const bool first = R.iscal[I_IT] == 0 || R.iscal[I_RESTART] != 0;
+  const float beta = first ? 0.f : (float)(R.scal[S_RHO] / R.scal[S_RHO1]);
+  const int bs = M.block ? 3 : 1;
+  for (int64_t u = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; u < nunits; u += (int64_t)gridDim.x * blockDim.x) {
+    float z[3];
+    apply_prec32(M, r, u, z);
+    for (int k = 0; k < bs; k++) {
+      const int64_t j = pidx(u * bs + k, padded);
+      p[j] = first ? z[k] : fmaf(beta, p[j], z[k]);
+    }
+  }
+}
+
+// q = A32 p over 3x3 block rows; a warp owns a tile of 32 block rows, lane t
+// keeps row t's result so the epilogue (q store, p.q) runs with all lanes.
+__global__ void __launch_bounds__(kThreads) k_mx_bsr3(const int64_t *__restrict__ bptr, const int32_t *__restrict__ bcol,
+                                                      const float *__restrict__ bval, const float4 *__restrict__ p4,
+                                                      float *__restrict__ q, int64_t nbrow, Red R) {
+  if (!active(R.iscal)) return;
+  const int lane = threadIdx.x & 31;
+  const int64_t warp_id = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) / 32;
+  const int64_t nwarps = (int64_t)gridDim.x * blockDim.x / 32;
+  KSum pq;
+  for (int64_t I0 = warp_id * 32; I0 < nbrow; I0 += nwarps * 32) {
+    const int nrow = (int)min((int64_t)32, nbrow - I0);
+    const int64_t mybeg = lane < nrow ? bptr[I0 + lane] : 0;
+    const int64_t myend = lane < nrow ? bptr[I0 + lane + 1] : 0;
+    float m0 = 0.f, m1 = 0.f, m2 = 0.f;
+    for (int t = 0; t < nrow; t++) {
+      const int64_t b0 = __shfl_sync(0xffffffffu, mybeg, t);
+      const int nb = (int)(__shfl_sync(0xffffffffu, myend, t) - b0);
+      const float *v = bval + 9 * b0;
+      float a0 = 0.f, a1 = 0.f, a2 = 0.f;
+      for (int j = lane; j < nb; j += 32) {
+        const float4 xv = __ldg(&p4[__ldcs(&bcol[b0 + j])]);
+        a0 = fmaf(__ldcs(&v[0 * nb + j]), xv.x, a0);
+        a0 = fmaf(__ldcs(&v[1 * nb + j]), xv.y, a0);
+        a0 = fmaf(__ldcs(&v[2 * nb + j]), xv.z, a0);
+        a1 = fmaf(__ldcs(&v[3 * nb + j]), xv.x, a1);
+        a1 = fmaf(__ldcs(&v[4 * nb + j]), xv.y, a1);
+        a1 = fmaf(__ldcs(&v[5 * nb + j]), xv.z, a1);
+        a2 = fmaf(__ldcs(&v[6 * nb + j]), xv.x, a2);
+        a2 = fmaf(__ldcs(&v[7 * nb + j]), xv.y, a2);
+        a2 = fmaf(__ldcs(&v[8 * nb + j]), xv.z, a2);
+      }
+      for (int o = 16; o > 0; o >>= 1) {
+        a0 += __shfl_xor_sync(0xffffffffu, a0, o);
+        a1 += __shfl_xor_sync(0xffffffffu, a1, o);
+        a2 += __shfl_xor_sync(0xffffffffu, a2, o);
+      }
+      if (lane == t) {
+        m0 = a0;
+        m1 = a1;
+        m2 = a2;
+      }
+    }
+    if (lane < nrow) {
+      const int64_t I = I0 + lane;
+      q[3 * I] = m0;
+      q[3 * I + 1] = m1;
+      q[3 * I + 2] = m2;
+      const float4 pv = p4[I];
+      pq.add(pv.x * m0);
+      pq.add(pv.y * m1);
+      pq.add(pv.z * m2);
+    }
+  }
+  double vv[1] = {pq.get()}, tot[1];
+  if (grid_reduce<1>(vv, R, tot) && threadIdx.x == 0) {
+    R.scal[S_PQ] = tot[0];
+    R.iscal[I_SP32]++;
+  }
+}
+
+// q = A32 p over scalar CSR rows (FP32 values, TPR lanes per row)
+template <int TPR>
+__global__ void __launch_bounds__(kThreads) k_mx_csr(const int64_t *__restrict__ ia, const int32_t *__restrict__ ja,
+                                                     const float *__restrict__ a32, const float *__restrict__ p,
+                                                     float *__restrict__ q, int64_t n, Red R) {
+  if (!active(R.iscal)) return;
+  KSum pq;
+  GPZ_ROW_LOOP(TPR, n) {
+    const int64_t r = r0 + (threadIdx.x & 31) / TPR;
+    const bool valid = r < n;
+    const float s = row_dot32<TPR>(ia, ja, a32, p, r, sub, valid);
+    if (sub == 0 && valid) {
+      q[r] = s;
+      pq.add(p[r] * s);
+    }
+  }
+  double vv[1] = {pq.get()}, tot[1];
+  if (grid_reduce<1>(vv, R, tot) && threadIdx.x == 0) {
+    R.scal[S_PQ] = tot[0];
+    R.iscal[I_SP32]++;
+  }
+}
+
+// alpha = rho / pq; dx += alpha p; r -= alpha q; rho' = r.(M r), rr = r.r
+__global__ void __launch_bounds__(kThreads) k_mx_update(float *__restrict__ dx, float *__restrict__ r,
+                                                        const float *__restrict__ p, const float *__restrict__ q,
+                                                        Prec32 M, int padded, int64_t nunits, Red R) {
+  if (!active(R.iscal)) return;
+  const double pq = R.scal[S_PQ];
+  const float alpha = (float)(R.scal[S_RHO] / pq);
+  const int bs = M.block ? 3 : 1;
+  KSum rz, rr;
+  for (int64_t u = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; u < nunits; u += (int64_t)gridDim.x * blockDim.x) {
+    for (int k = 0; k < bs; k++) {
+      const int64_t i = u * bs + k;
+      const float pi = p[pidx(i, padded)];
+      dx[i] = fmaf(alpha, pi, dx[i]);
+      const float ri = fmaf(-alpha, q[i], r[i]);
+      r[i] = ri;
+      rr.add(ri * ri);
+    }
+    float z[3];
+    apply_prec32(M, r, u, z);
+    for (int k = 0; k < bs; k++) rz.add(r[u * bs + k] * z[k]);
+  }
+  double v[2] = {rz.get(), rr.get()}, tot[2];
+  if (grid_reduce<2>(v, R, tot) && threadIdx.x == 0) {
+    double *s = R.scal;
+    int64_t *is = R.iscal;
+    if (!(pq > 0.0) || !isfinite(tot[1]) || !isfinite(tot[0])) is[I_BREAK] = 1;
+    s[S_RHO1] = s[S_RHO];
+    s[S_RHO] = tot[0];
+    s[S_RR] = tot[1];
+    if (tot[1] > s[S_MAXRR]) s[S_MAXRR] = tot[1];
+    const double resid = sqrt(tot[1]) / s[S_NORMB];
+    s[S_RESID] = resid;
+    is[I_IT] += 1;
+    is[I_RESTART] = 0;
+    if (is[I_BREAK]) is[I_CONV] = 2;
+    else if (resid <= s[S_TOL] || tot[1] < s[S_DELTA2] * s[S_MAXRR]) is[I_UPDATE] = 1;
+  }
+}
+
+// fold the FP32 increment into the FP64 solution (when an update is requested,
+// or unconditionally with force = 1 at the end of a solve)
+__global__ void __launch_bounds__(kThreads) k_mx_foldx(double *__restrict__ x, float *__restrict__ dx, int64_t n,
+                                                       int force, Red R) {
+  if (!force && (R.iscal[I_UPDATE] != 1 || R.iscal[I_CONV] != 0)) return;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    x[i] += (double)dx[i];
+    dx[i] = 0.f;
+  }
+}
+
+// r32 = r64 after a true-residual computation; rho = r.(M r) and the restart rule
+__global__ void __launch_bounds__(kThreads) k_mx_r32(const double *__restrict__ r64, float *__restrict__ r32,
+                                                     Prec32 M, int64_t nunits, Red R) {
+  if (R.iscal[I_UPDATE] != 2) return;
+  const int bs = M.block ? 3 : 1;
+  KSum rz;
+  for (int64_t u = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; u < nunits; u += (int64_t)gridDim.x * blockDim.x) {
+    for (int k = 0; k < bs; k++) r32[u * bs + k] = (float)r64[u * bs + k];
+    float z[3];
+    apply_prec32(M, r32, u, z);
+    for (int k = 0; k < bs; k++) rz.add(r32[u * bs + k] * z[k]);
+  }
+  double v[1] = {rz.get()}, tot[1];
+  if (grid_reduce<1>(v, R, tot) && threadIdx.x == 0) {
+    double *s = R.scal;
+    int64_t *is = R.iscal;
+    if (is[I_IT] > 0 && (tot[0] > 4.0 * s[S_RHO] || tot[0] < 0.25 * s[S_RHO])) {
+      is[I_RESTART] = 1;
+      is[I_NRESTART] += 1;
+    }
+    s[S_RHO] = tot[0];
+    is[I_UPDATE] = 0;
+  }
+}
+
+__global__ void k_to_f32(const double *__restrict__ a, float *__restrict__ b, int64_t n) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    b[i] = (float)a[i];
+}
+
+int pick_tpr(int64_t nnz, int64_t n) {  // FP64 rows: few lanes per row
+  double avg = n ? (double)nnz / (double)n : 0.0;
+  if (avg > 24) return 8;
+  return 4;
+}
+
+int pick_tpr32(int64_t nnz, int64_t n) {  // FP32 rows: coalescing first
   double avg = n ? (double)nnz / (double)n : 0.0;
   if (avg > 48) return 32;
   if (avg > 20) return 16;
@@ -597,12 +772,10 @@ void alloc_work(Ctx &c, bool mixed) {
   w.x.alloc(n);
   w.b.alloc(n);
   if (mixed) {
-    if (c.have_bsr3) {
-      w.p32x4.alloc((size_t)std::max<int64_t>(c.nbrow, 1) * 4);
-      w.p32x4.zero(c.stream);
-    } else {
-      w.p32.alloc(n);
-    }
+    w.pm.alloc(c.have_bsr3 ? (size_t)std::max<int64_t>(c.nbrow, 1) * 4 : (size_t)n);
+    w.r32.alloc(n);
+    w.q32.alloc(n);
+    w.dx32.alloc(n);
   }
   w.partial.alloc((size_t)kGridBlocks * 4);
   w.scal.alloc(S_NSCAL);
@@ -615,35 +788,39 @@ Red red_of(Ctx &c) { return Red{c.sw.partial.p, c.sw.counter.p, c.sw.scal.p, c.s
 
 struct Plan {
   bool mixed, block, bsr;
-  int tpr;
+  int tpr, tpr32;
   int64_t nunits;
   Prec M;
+  Prec32 M32;
 };
 
 void launch_iteration(Ctx &c, const Plan &P) {
   SolverWork &w = c.sw;
   Red R = red_of(c);
-  const bool p32 = P.mixed && !P.bsr;
-  k_cg_p<<<wave(k_cg_p), kThreads, 0, c.stream>>>(w.r.p, P.M, w.p.p, p32 ? w.p32.p : nullptr,
-                                                 (P.mixed && P.bsr) ? w.p32x4.p : nullptr, P.nunits, R);
-  if (P.mixed && P.bsr) {
-    k_cg_bsr3<<<wave(k_cg_bsr3), kThreads, 0, c.stream>>>(c.d_bptr.p, c.d_bcol.p, c.d_bval.p, (const float4 *)w.p32x4.p,
-                                                      w.p.p, w.q.p, c.nbrow, R);
-  } else if (P.mixed) {
-    GPZ_TPR_SWITCH(P.tpr, (k_cg_spmv<T, true><<<wave(k_cg_spmv<T, true>), kThreads, 0, c.stream>>>(
-                              c.d_ia.p, c.d_ja.p, nullptr, c.d_a32.p, w.p.p, w.p32.p, w.q.p, c.neq, R)));
-  } else {
+  if (!P.mixed) {
+    k_cg_p<<<wave(k_cg_p), kThreads, 0, c.stream>>>(w.r.p, P.M, w.p.p, P.nunits, R);
     GPZ_TPR_SWITCH(P.tpr, (k_cg_spmv<T, false><<<wave(k_cg_spmv<T, false>), kThreads, 0, c.stream>>>(
                               c.d_ia.p, c.d_ja.p, c.d_a.p, nullptr, w.p.p, nullptr, w.q.p, c.neq, R)));
+    k_cg_update<<<wave(k_cg_update), kThreads, 0, c.stream>>>(w.x.p, w.r.p, w.p.p, w.q.p, P.M, P.nunits, 0, R);
+    c.launches += 3;
+    return;
   }
-  k_cg_update<<<wave(k_cg_update), kThreads, 0, c.stream>>>(w.x.p, w.r.p, w.p.p, w.q.p, P.M, P.nunits, P.mixed ? 1 : 0, R);
-  c.launches += 3;
-  if (P.mixed) {
-    GPZ_TPR_SWITCH(P.tpr, (k_reliable<T><<<wave(k_reliable<T>), kThreads, 0, c.stream>>>(c.d_ia.p, c.d_ja.p, c.d_a.p, w.x.p,
-                                                                                  w.b.p, w.r.p, c.neq, R)));
-    k_precond_dot<<<wave(k_precond_dot), kThreads, 0, c.stream>>>(w.r.p, P.M, P.nunits, R);
-    c.launches += 2;
+  const int padded = P.bsr ? 1 : 0;
+  k_mx_p<<<wave(k_mx_p), kThreads, 0, c.stream>>>(w.r32.p, P.M32, w.pm.p, padded, P.nunits, R);
+  if (P.bsr) {
+    k_mx_bsr3<<<wave(k_mx_bsr3), kThreads, 0, c.stream>>>(c.d_bptr.p, c.d_bcol.p, c.d_bval.p, (const float4 *)w.pm.p,
+                                                          w.q32.p, c.nbrow, R);
+  } else {
+    GPZ_TPR_SWITCH(P.tpr32, (k_mx_csr<T><<<wave(k_mx_csr<T>), kThreads, 0, c.stream>>>(c.d_ia.p, c.d_ja.p, c.d_a32.p,
+                                                                                      w.pm.p, w.q32.p, c.neq, R)));
   }
+  k_mx_update<<<wave(k_mx_update), kThreads, 0, c.stream>>>(w.dx32.p, w.r32.p, w.pm.p, w.q32.p, P.M32, padded,
+                                                            P.nunits, R);
+  k_mx_foldx<<<wave(k_mx_foldx), kThreads, 0, c.stream>>>(w.x.p, w.dx32.p, c.neq, 0, R);
+  GPZ_TPR_SWITCH(P.tpr, (k_reliable<T><<<wave(k_reliable<T>), kThreads, 0, c.stream>>>(c.d_ia.p, c.d_ja.p, c.d_a.p,
+                                                                                        w.x.p, w.b.p, w.r.p, c.neq, R)));
+  k_mx_r32<<<wave(k_mx_r32), kThreads, 0, c.stream>>>(w.r.p, w.r32.p, P.M32, P.nunits, R);
+  c.launches += 6;
 }
 
 }  // namespace
@@ -664,8 +841,23 @@ int solve(Ctx &c, const gpz_solver_opts &o, gpz_solve_report &rep) {
   P.block = block;
   P.bsr = mixed && c.have_bsr3;
   P.tpr = pick_tpr(c.nnz, c.neq);
+  P.tpr32 = pick_tpr32(c.nnz, c.neq);
   P.nunits = block ? c.neq / 3 : c.neq;
   P.M = Prec{c.d_dinv.p, block ? c.d_bjinv.p : nullptr, block ? 1 : 0};
+  if (mixed) {
+    // FP32 copies of the preconditioner
+    if (block) {
+      c.d_bjinv32.alloc((size_t)P.nunits * 9);
+      k_to_f32<<<wave(k_to_f32), kThreads, 0, s>>>(c.d_bjinv.p, c.d_bjinv32.p, (int64_t)P.nunits * 9);
+    } else {
+      c.d_dinv32.alloc(std::max<int64_t>(c.neq, 1));
+      k_to_f32<<<wave(k_to_f32), kThreads, 0, s>>>(c.d_dinv.p, c.d_dinv32.p, c.neq);
+    }
+    c.launches++;
+    P.M32 = Prec32{block ? nullptr : c.d_dinv32.p, block ? c.d_bjinv32.p : nullptr, block ? 1 : 0};
+    w.dx32.zero(s);
+    w.pm.zero(s);
+  }
   const int batch = o.check_every > 0 ? o.check_every : 32;
 
   cudaEvent_t ev0, ev1;
@@ -682,14 +874,16 @@ int solve(Ctx &c, const gpz_solver_opts &o, gpz_solve_report &rep) {
   GPZ_CUDA_TRY(cudaMemcpyAsync(w.scal.p, hs, sizeof(hs), cudaMemcpyHostToDevice, s));
   GPZ_CUDA_TRY(cudaMemcpyAsync(w.iscal.p, hi, sizeof(hi), cudaMemcpyHostToDevice, s));
   Red R = red_of(c);
-  GPZ_TPR_SWITCH(P.tpr, (k_cg_init<T><<<wave(k_cg_init<T>), kThreads, 0, s>>>(c.d_ia.p, c.d_ja.p, c.d_a.p, w.x.p, w.b.p,
-                                                                        w.r.p, c.neq, o.from_current, R)));
-  k_precond_dot<<<wave(k_precond_dot), kThreads, 0, s>>>(w.r.p, P.M, P.nunits, R);
+  GPZ_TPR_SWITCH(P.tpr, (k_cg_init<T><<<wave(k_cg_init<T>), kThreads, 0, s>>>(c.d_ia.p, c.d_ja.p, c.d_a.p, w.x.p,
+                                                                               w.b.p, w.r.p, c.neq, o.from_current,
+                                                                               R)));
+  if (mixed) k_mx_r32<<<wave(k_mx_r32), kThreads, 0, s>>>(w.r.p, w.r32.p, P.M32, P.nunits, R);
+  else k_precond_dot<<<wave(k_precond_dot), kThreads, 0, s>>>(w.r.p, P.M, P.nunits, R);
   c.launches += 2;
   GPZ_CUDA_TRY(cudaGetLastError());
 
   cudaGraphExec_t exec = nullptr;
-  const int per_iter = mixed ? 5 : 3;
+  const int per_iter = mixed ? 6 : 3;
   if (o.use_graph) {
     cudaGraph_t g;
     GPZ_CUDA_TRY(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
@@ -714,8 +908,12 @@ int solve(Ctx &c, const gpz_solver_opts &o, gpz_solve_report &rep) {
     if (hstate[I_CONV] != 0 || hstate[I_IT] >= o.max_iter) break;
   }
   if (exec) cudaGraphExecDestroy(exec);
-  GPZ_TPR_SWITCH(P.tpr, (k_true_resid<T><<<wave(k_true_resid<T>), kThreads, 0, s>>>(c.d_ia.p, c.d_ja.p, c.d_a.p, w.x.p, w.b.p,
-                                                                           c.neq, R)));
+  if (mixed) {
+    k_mx_foldx<<<wave(k_mx_foldx), kThreads, 0, s>>>(w.x.p, w.dx32.p, c.neq, 1, R);
+    c.launches++;
+  }
+  GPZ_TPR_SWITCH(P.tpr, (k_true_resid<T><<<wave(k_true_resid<T>), kThreads, 0, s>>>(c.d_ia.p, c.d_ja.p, c.d_a.p,
+                                                                                     w.x.p, w.b.p, c.neq, R)));
   c.launches++;
   GPZ_CUDA_TRY(cudaEventRecord(ev1, s));
   GPZ_CUDA_TRY(cudaMemcpyAsync(hs, w.scal.p, sizeof(hs), cudaMemcpyDeviceToHost, s));
@@ -750,12 +948,9 @@ double time_spmv(Ctx &c, bool f32, int reps) {
   cudaStream_t s = c.stream;
   std::vector<double> ones(c.neq, 1.0);
   GPZ_CUDA_TRY(cudaMemcpyAsync(w.p.p, ones.data(), c.neq * sizeof(double), cudaMemcpyHostToDevice, s));
-  if (f32 && c.have_bsr3) {
-    std::vector<float> o4(c.nbrow * 4, 1.0f);
-    GPZ_CUDA_TRY(cudaMemcpyAsync(w.p32x4.p, o4.data(), o4.size() * sizeof(float), cudaMemcpyHostToDevice, s));
-  } else if (f32) {
-    std::vector<float> o1(c.neq, 1.0f);
-    GPZ_CUDA_TRY(cudaMemcpyAsync(w.p32.p, o1.data(), c.neq * sizeof(float), cudaMemcpyHostToDevice, s));
+  if (f32) {
+    std::vector<float> o1(w.pm.n, 1.0f);
+    GPZ_CUDA_TRY(cudaMemcpyAsync(w.pm.p, o1.data(), o1.size() * sizeof(float), cudaMemcpyHostToDevice, s));
   }
   int64_t hi[I_NISCAL] = {0};
   hi[I_MAXIT] = 1;
@@ -764,11 +959,11 @@ double time_spmv(Ctx &c, bool f32, int reps) {
   const int tpr = pick_tpr(c.nnz, c.neq);
   auto launch = [&]() {
     if (f32 && c.have_bsr3) {
-      k_cg_bsr3<<<wave(k_cg_bsr3), kThreads, 0, s>>>(c.d_bptr.p, c.d_bcol.p, c.d_bval.p, (const float4 *)w.p32x4.p, w.p.p,
-                                                 w.q.p, c.nbrow, R);
+      k_mx_bsr3<<<wave(k_mx_bsr3), kThreads, 0, s>>>(c.d_bptr.p, c.d_bcol.p, c.d_bval.p, (const float4 *)w.pm.p, w.q32.p,
+                                                     c.nbrow, R);
     } else if (f32) {
-      GPZ_TPR_SWITCH(tpr, (k_cg_spmv<T, true><<<wave(k_cg_spmv<T, true>), kThreads, 0, s>>>(c.d_ia.p, c.d_ja.p, nullptr, c.d_a32.p,
-                                                                               w.p.p, w.p32.p, w.q.p, c.neq, R)));
+      GPZ_TPR_SWITCH(pick_tpr32(c.nnz, c.neq), (k_mx_csr<T><<<wave(k_mx_csr<T>), kThreads, 0, s>>>(c.d_ia.p, c.d_ja.p, c.d_a32.p, w.pm.p,
+                                                                              w.q32.p, c.neq, R)));
     } else {
       GPZ_TPR_SWITCH(tpr, (k_cg_spmv<T, false><<<wave(k_cg_spmv<T, false>), kThreads, 0, s>>>(c.d_ia.p, c.d_ja.p, c.d_a.p, nullptr,
                                                                                 w.p.p, nullptr, w.q.p, c.neq, R)));
