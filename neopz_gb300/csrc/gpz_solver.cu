@@ -46,7 +46,8 @@ int wave(K kernel) {
 }
 
 // device scalar slots
-enum { S_RHO = 0, S_RHO1, S_PQ, S_RR, S_NORMB, S_TOL, S_MAXRR, S_DELTA2, S_RESID, S_TRUERR, S_NSCAL };
+// alpha and beta are formed once, by the CTA that finishes the reduction they depend on
+enum { S_RHO = 0, S_RHO1, S_PQ, S_RR, S_NORMB, S_TOL, S_MAXRR, S_DELTA2, S_RESID, S_TRUERR, S_ALPHA, S_BETA, S_NSCAL };
 enum { I_CONV = 0, I_IT, I_MAXIT, I_UPDATE, I_NUPD, I_SP64, I_SP32, I_BREAK, I_RESTART, I_NRESTART, I_NISCAL };
 
 struct Red {
@@ -202,6 +203,7 @@ __global__ void __launch_bounds__(kThreads) k_cg_spmv(const int64_t *__restrict_
   double v[1] = {pq}, tot[1];
   if (grid_reduce<1>(v, R, tot) && threadIdx.x == 0) {
     R.scal[S_PQ] = tot[0];
+    R.scal[S_ALPHA] = R.scal[S_RHO] / tot[0];
     R.iscal[I_SP64]++;
   }
 }
@@ -232,7 +234,7 @@ __global__ void __launch_bounds__(kThreads) k_cg_p(const double *__restrict__ r,
                                                    int64_t nunits, Red R) {
   if (!active(R.iscal)) return;
   const bool first = R.iscal[I_IT] == 0 || R.iscal[I_RESTART] != 0;
-  const double beta = first ? 0.0 : R.scal[S_RHO] / R.scal[S_RHO1];
+  const double beta = first ? 0.0 : R.scal[S_BETA];
   const int bs = M.block ? 3 : 1;
   for (int64_t u = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; u < nunits; u += (int64_t)gridDim.x * blockDim.x) {
     double z[3];
@@ -251,7 +253,7 @@ __global__ void __launch_bounds__(kThreads) k_cg_update(double *__restrict__ x, 
                                                         Prec M, int64_t nunits, int mixed, Red R) {
   if (!active(R.iscal)) return;
   const double pq = R.scal[S_PQ];
-  const double alpha = R.scal[S_RHO] / pq;
+  const double alpha = R.scal[S_ALPHA];
   const int bs = M.block ? 3 : 1;
   double rz = 0.0, rr = 0.0;
   for (int64_t u = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; u < nunits; u += (int64_t)gridDim.x * blockDim.x) {
@@ -273,6 +275,7 @@ __global__ void __launch_bounds__(kThreads) k_cg_update(double *__restrict__ x, 
     if (!(pq > 0.0) || !isfinite(tot[1]) || !isfinite(tot[0])) is[I_BREAK] = 1;
     s[S_RHO1] = s[S_RHO];
     s[S_RHO] = tot[0];
+    s[S_BETA] = tot[0] / s[S_RHO1];
     s[S_RR] = tot[1];
     if (tot[1] > s[S_MAXRR]) s[S_MAXRR] = tot[1];
     const double resid = sqrt(tot[1]) / s[S_NORMB];
@@ -345,6 +348,7 @@ __global__ void __launch_bounds__(kThreads) k_precond_dot(const double *__restri
       is[I_NRESTART] += 1;
     }
     s[S_RHO] = tot[0];
+    s[S_BETA] = s[S_RHO1] != 0.0 ? tot[0] / s[S_RHO1] : 0.0;
     is[I_UPDATE] = 0;
   }
 }
@@ -510,7 +514,7 @@ __global__ void __launch_bounds__(kThreads) k_mx_p(const float *__restrict__ r, 
                                                    int padded, int64_t nunits, Red R) {
   if (!active(R.iscal)) return;
   const bool first = R.iscal[I_IT] == 0 || R.iscal[I_RESTART] != 0;
-  const float beta = first ? 0.f : (float)(R.scal[S_RHO] / R.scal[S_RHO1]);
+  const float beta = first ? 0.f : (float)R.scal[S_BETA];
   const int bs = M.block ? 3 : 1;
   for (int64_t u = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; u < nunits; u += (int64_t)gridDim.x * blockDim.x) {
     float z[3];
@@ -524,7 +528,7 @@ __global__ void __launch_bounds__(kThreads) k_mx_p(const float *__restrict__ r, 
 
 // q = A32 p over 3x3 block rows; a warp owns a tile of 32 block rows, lane t
 // keeps row t's result so the epilogue (q store, p.q) runs with all lanes.
-__global__ void __launch_bounds__(kThreads) k_mx_bsr3(const int64_t *__restrict__ bptr, const int32_t *__restrict__ bcol,
+__global__ void __launch_bounds__(kThreads, 6) k_mx_bsr3(const int64_t *__restrict__ bptr, const int32_t *__restrict__ bcol,
                                                       const float *__restrict__ bval, const float4 *__restrict__ p4,
                                                       float *__restrict__ q, int64_t nbrow, Red R) {
   if (!active(R.iscal)) return;
@@ -579,6 +583,7 @@ __global__ void __launch_bounds__(kThreads) k_mx_bsr3(const int64_t *__restrict_
   double vv[1] = {pq.get()}, tot[1];
   if (grid_reduce<1>(vv, R, tot) && threadIdx.x == 0) {
     R.scal[S_PQ] = tot[0];
+    R.scal[S_ALPHA] = R.scal[S_RHO] / tot[0];
     R.iscal[I_SP32]++;
   }
 }
@@ -602,6 +607,7 @@ __global__ void __launch_bounds__(kThreads) k_mx_csr(const int64_t *__restrict__
   double vv[1] = {pq.get()}, tot[1];
   if (grid_reduce<1>(vv, R, tot) && threadIdx.x == 0) {
     R.scal[S_PQ] = tot[0];
+    R.scal[S_ALPHA] = R.scal[S_RHO] / tot[0];
     R.iscal[I_SP32]++;
   }
 }
@@ -612,7 +618,7 @@ __global__ void __launch_bounds__(kThreads) k_mx_update(float *__restrict__ dx, 
                                                         Prec32 M, int padded, int64_t nunits, Red R) {
   if (!active(R.iscal)) return;
   const double pq = R.scal[S_PQ];
-  const float alpha = (float)(R.scal[S_RHO] / pq);
+  const float alpha = (float)R.scal[S_ALPHA];
   const int bs = M.block ? 3 : 1;
   KSum rz, rr;
   for (int64_t u = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; u < nunits; u += (int64_t)gridDim.x * blockDim.x) {
@@ -635,6 +641,7 @@ __global__ void __launch_bounds__(kThreads) k_mx_update(float *__restrict__ dx, 
     if (!(pq > 0.0) || !isfinite(tot[1]) || !isfinite(tot[0])) is[I_BREAK] = 1;
     s[S_RHO1] = s[S_RHO];
     s[S_RHO] = tot[0];
+    s[S_BETA] = tot[0] / s[S_RHO1];
     s[S_RR] = tot[1];
     if (tot[1] > s[S_MAXRR]) s[S_MAXRR] = tot[1];
     const double resid = sqrt(tot[1]) / s[S_NORMB];
@@ -678,6 +685,7 @@ __global__ void __launch_bounds__(kThreads) k_mx_r32(const double *__restrict__ 
       is[I_NRESTART] += 1;
     }
     s[S_RHO] = tot[0];
+    s[S_BETA] = s[S_RHO1] != 0.0 ? tot[0] / s[S_RHO1] : 0.0;
     is[I_UPDATE] = 0;
   }
 }
