@@ -140,11 +140,11 @@ struct Ctx {
   DBuf<double> d_a, d_f, d_dinv;
   DBuf<float> d_a32;                         // FP32 CSR copy for the inner solves
   bool have_a32 = false;
-  bool have_bsr3 = false;                    // FP32 3x3 block CSR instead of d_a32
-  int64_t nbrow = 0;
-  DBuf<int64_t> d_bptr;
-  DBuf<int32_t> d_bcol;
-  DBuf<float> d_bval;
+  bool have_bsr3 = false;                    // FP32 3x3 blocks in sliced ELL instead of d_a32
+  int64_t nbrow = 0, nslice = 0, sell_plane = 0;
+  DBuf<int64_t> d_soff;                      // [nslice+1] first block of each slice
+  DBuf<int32_t> d_slen, d_sperm, d_scol;     // slice lengths, rows of each slice, block columns
+  DBuf<float> d_sval;                        // 9 planes of sell_plane floats
   DBuf<double> d_bjinv;                      // block-Jacobi inverses [neq/3][9]
   DBuf<float> d_bjinv32, d_dinv32;           // FP32 preconditioners of the mixed CG
   bool have_bjinv = false;

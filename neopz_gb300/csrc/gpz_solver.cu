@@ -16,6 +16,7 @@
 //   since the last update, or the recursive residual meets the tolerance, the
 //   true residual b - A64 x is recomputed in FP64 and replaces r.  The solve
 //   stops only on the true FP64 residual.
+#include <algorithm>
 #include <cmath>
 #include <vector>
 
@@ -188,7 +189,7 @@ __global__ void __launch_bounds__(kThreads) k_cg_spmv(const int64_t *__restrict_
                                                       const double *__restrict__ a64, const float *__restrict__ a32,
                                                       const double *__restrict__ p, const float *__restrict__ p32,
                                                       double *__restrict__ q, int64_t n, Red R) {
-  static_assert(!F32, "the FP32 iteration uses k_mx_csr / k_mx_bsr3");
+  static_assert(!F32, "the FP32 iteration uses k_mx_csr / k_mx_sell3");
   if (!active(R.iscal)) return;
   double pq = 0.0;
   GPZ_ROW_LOOP(TPR, n) {
@@ -412,28 +413,38 @@ __global__ void __launch_bounds__(kThreads) k_true_resid(const int64_t *__restri
 }
 
 // ---- setup kernels for the mixed path and the block preconditioner
-__global__ void k_build_bsr3(const int64_t *__restrict__ ia, const int32_t *__restrict__ ja,
-                             const double *__restrict__ a, int64_t nbrow, int64_t *__restrict__ bptr,
-                             int32_t *__restrict__ bcol, float *__restrict__ bval, int *__restrict__ err) {
-  const int lane = threadIdx.x & 31;
-  const int64_t I = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) / 32;
-  if (I >= nbrow) return;
-  const int64_t r0 = 3 * I;
-  const int64_t len = ia[r0 + 1] - ia[r0];
-  if (len % 3 != 0 || ia[r0 + 2] - ia[r0 + 1] != len || ia[r0 + 3] - ia[r0 + 2] != len || ia[r0] % 9 != 0) {
-    if (lane == 0) atomicOr(err, 128);
-    return;
+// fill the sliced-ELL planes from the full FP64 CSR (rows 3I..3I+2 of block
+// row I share their columns; block column j covers columns 3j'..3j'+2)
+__global__ void k_fill_sell3(const int64_t *__restrict__ ia, const int32_t *__restrict__ ja,
+                             const double *__restrict__ a, const int64_t *__restrict__ soff,
+                             const int32_t *__restrict__ slen, const int32_t *__restrict__ sperm, int64_t nslice,
+                             int64_t plane, int32_t *__restrict__ scol, float *__restrict__ sval, int *__restrict__ err) {
+  const int64_t g = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const int64_t sl = g / 32;
+  const int t = (int)(g % 32);
+  if (sl >= nslice) return;
+  const int I = sperm[sl * 32 + t];
+  const int len = slen[sl];
+  int64_t r0 = 0, nb = 0;
+  if (I >= 0) {
+    r0 = 3 * (int64_t)I;
+    const int64_t l0 = ia[r0 + 1] - ia[r0];
+    if (l0 % 3 != 0 || ia[r0 + 2] - ia[r0 + 1] != l0 || ia[r0 + 3] - ia[r0 + 2] != l0 || l0 / 3 > len) {
+      atomicOr(err, 128);
+      return;
+    }
+    nb = l0 / 3;
   }
-  const int64_t nb = len / 3, b0 = ia[r0] / 9;
-  if (lane == 0) {
-    bptr[I] = b0;
-    if (I == nbrow - 1) bptr[nbrow] = b0 + nb;
-  }
-  float *v = bval + 9 * b0;
-  for (int64_t j = lane; j < nb; j += 32) {
-    bcol[b0 + j] = ja[ia[r0] + 3 * j] / 3;
-    for (int s = 0; s < 3; s++)
-      for (int t = 0; t < 3; t++) v[(3 * s + t) * nb + j] = (float)a[ia[r0 + s] + 3 * j + t];
+  for (int j = 0; j < len; j++) {
+    const int64_t e = soff[sl] + (int64_t)j * 32 + t;
+    if (j < nb) {
+      scol[e] = ja[ia[r0] + 3 * j] / 3;
+      for (int s = 0; s < 3; s++)
+        for (int u = 0; u < 3; u++) sval[(3 * s + u) * plane + e] = (float)a[ia[r0 + s] + 3 * j + u];
+    } else {
+      scol[e] = I >= 0 ? I : 0;  // padding: zero block on a cached column
+      for (int k = 0; k < 9; k++) sval[k * plane + e] = 0.f;
+    }
   }
 }
 
@@ -526,58 +537,50 @@ __global__ void __launch_bounds__(kThreads) k_mx_p(const float *__restrict__ r, 
   }
 }
 
-// q = A32 p over 3x3 block rows; a warp owns a tile of 32 block rows, lane t
-// keeps row t's result so the epilogue (q store, p.q) runs with all lanes.
-__global__ void __launch_bounds__(kThreads, 6) k_mx_bsr3(const int64_t *__restrict__ bptr, const int32_t *__restrict__ bcol,
-                                                      const float *__restrict__ bval, const float4 *__restrict__ p4,
-                                                      float *__restrict__ q, int64_t nbrow, Red R) {
+// q = A32 p for 3x3 blocks in sliced ELL: slices of 32 block rows (sorted by
+// length inside windows so a slice pads little), lane t owns row t of its
+// slice and walks the slice's block columns; entry k (0..8) of the blocks of a
+// slice column lives in plane k, so every load of a warp is 32 consecutive
+// floats and every lane runs a long, independent FMA chain (no reductions).
+__global__ void __launch_bounds__(kThreads) k_mx_sell3(const int64_t *__restrict__ soff, const int32_t *__restrict__ slen,
+                                                       const int32_t *__restrict__ sperm, const int32_t *__restrict__ scol,
+                                                       const float *__restrict__ sval, int64_t plane,
+                                                       const float4 *__restrict__ p4, float *__restrict__ q,
+                                                       int64_t nslice, Red R) {
   if (!active(R.iscal)) return;
   const int lane = threadIdx.x & 31;
   const int64_t warp_id = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) / 32;
   const int64_t nwarps = (int64_t)gridDim.x * blockDim.x / 32;
   KSum pq;
-  for (int64_t I0 = warp_id * 32; I0 < nbrow; I0 += nwarps * 32) {
-    const int nrow = (int)min((int64_t)32, nbrow - I0);
-    const int64_t mybeg = lane < nrow ? bptr[I0 + lane] : 0;
-    const int64_t myend = lane < nrow ? bptr[I0 + lane + 1] : 0;
-    float m0 = 0.f, m1 = 0.f, m2 = 0.f;
-    for (int t = 0; t < nrow; t++) {
-      const int64_t b0 = __shfl_sync(0xffffffffu, mybeg, t);
-      const int nb = (int)(__shfl_sync(0xffffffffu, myend, t) - b0);
-      const float *v = bval + 9 * b0;
-      float a0 = 0.f, a1 = 0.f, a2 = 0.f;
-      for (int j = lane; j < nb; j += 32) {
-        const float4 xv = __ldg(&p4[__ldcs(&bcol[b0 + j])]);
-        a0 = fmaf(__ldcs(&v[0 * nb + j]), xv.x, a0);
-        a0 = fmaf(__ldcs(&v[1 * nb + j]), xv.y, a0);
-        a0 = fmaf(__ldcs(&v[2 * nb + j]), xv.z, a0);
-        a1 = fmaf(__ldcs(&v[3 * nb + j]), xv.x, a1);
-        a1 = fmaf(__ldcs(&v[4 * nb + j]), xv.y, a1);
-        a1 = fmaf(__ldcs(&v[5 * nb + j]), xv.z, a1);
-        a2 = fmaf(__ldcs(&v[6 * nb + j]), xv.x, a2);
-        a2 = fmaf(__ldcs(&v[7 * nb + j]), xv.y, a2);
-        a2 = fmaf(__ldcs(&v[8 * nb + j]), xv.z, a2);
-      }
-      for (int o = 16; o > 0; o >>= 1) {
-        a0 += __shfl_xor_sync(0xffffffffu, a0, o);
-        a1 += __shfl_xor_sync(0xffffffffu, a1, o);
-        a2 += __shfl_xor_sync(0xffffffffu, a2, o);
-      }
-      if (lane == t) {
-        m0 = a0;
-        m1 = a1;
-        m2 = a2;
-      }
+  for (int64_t sl = warp_id; sl < nslice; sl += nwarps) {
+    const int64_t off = soff[sl] + lane;
+    const int len = slen[sl];
+    const int I = sperm[sl * 32 + lane];
+    const int32_t *cp = scol + off;
+    const float *vp = sval + off;
+    float a0 = 0.f, a1 = 0.f, a2 = 0.f;
+#pragma unroll 2
+    for (int j = 0; j < len; j++) {
+      const int64_t e = (int64_t)j * 32;
+      const float4 xv = __ldg(&p4[__ldcs(cp + e)]);
+      a0 = fmaf(__ldcs(vp + e), xv.x, a0);
+      a0 = fmaf(__ldcs(vp + plane + e), xv.y, a0);
+      a0 = fmaf(__ldcs(vp + 2 * plane + e), xv.z, a0);
+      a1 = fmaf(__ldcs(vp + 3 * plane + e), xv.x, a1);
+      a1 = fmaf(__ldcs(vp + 4 * plane + e), xv.y, a1);
+      a1 = fmaf(__ldcs(vp + 5 * plane + e), xv.z, a1);
+      a2 = fmaf(__ldcs(vp + 6 * plane + e), xv.x, a2);
+      a2 = fmaf(__ldcs(vp + 7 * plane + e), xv.y, a2);
+      a2 = fmaf(__ldcs(vp + 8 * plane + e), xv.z, a2);
     }
-    if (lane < nrow) {
-      const int64_t I = I0 + lane;
-      q[3 * I] = m0;
-      q[3 * I + 1] = m1;
-      q[3 * I + 2] = m2;
+    if (I >= 0) {
+      q[3 * (int64_t)I] = a0;
+      q[3 * (int64_t)I + 1] = a1;
+      q[3 * (int64_t)I + 2] = a2;
       const float4 pv = p4[I];
-      pq.add(pv.x * m0);
-      pq.add(pv.y * m1);
-      pq.add(pv.z * m2);
+      pq.add(pv.x * a0);
+      pq.add(pv.y * a1);
+      pq.add(pv.z * a2);
     }
   }
   double vv[1] = {pq.get()}, tot[1];
@@ -740,15 +743,46 @@ bool blocks_are_3(const Ctx &c) {
 void make_fp32_copy(Ctx &c) {
   c.have_bsr3 = false;
   if (blocks_are_3(c)) {
+    // sliced ELL of 3x3 blocks: block-row lengths from the row pointers, rows
+    // sorted by length (descending, stable) inside windows of 2048
     c.nbrow = c.neq / 3;
-    c.d_bptr.alloc(c.nbrow + 1);
-    c.d_bcol.alloc(std::max<int64_t>(c.nnz / 9, 1));
-    c.d_bval.alloc(std::max<int64_t>(c.nnz, 1));
-    k_build_bsr3<<<grid_for(c.nbrow * 32, 256), 256, 0, c.stream>>>(c.d_ia.p, c.d_ja.p, c.d_a.p, c.nbrow, c.d_bptr.p,
-                                                                    c.d_bcol.p, c.d_bval.p, c.d_err.p);
+    std::vector<int64_t> ia(c.neq + 1);
+    GPZ_CUDA_TRY(cudaMemcpyAsync(ia.data(), c.d_ia.p, (c.neq + 1) * sizeof(int64_t), cudaMemcpyDeviceToHost, c.stream));
+    GPZ_CUDA_TRY(cudaStreamSynchronize(c.stream));
+    std::vector<int32_t> nb(c.nbrow);
+    for (int64_t I = 0; I < c.nbrow; I++) nb[I] = (int32_t)((ia[3 * I + 1] - ia[3 * I]) / 3);
+    const int64_t W = 2048;
+    std::vector<int32_t> perm(c.nbrow);
+    for (int64_t I = 0; I < c.nbrow; I++) perm[I] = (int32_t)I;
+    for (int64_t w0 = 0; w0 < c.nbrow; w0 += W) {
+      int64_t w1 = std::min<int64_t>(w0 + W, c.nbrow);
+      std::stable_sort(perm.begin() + w0, perm.begin() + w1, [&](int32_t x, int32_t y) { return nb[x] > nb[y]; });
+    }
+    c.nslice = (c.nbrow + 31) / 32;
+    perm.resize(c.nslice * 32, -1);
+    std::vector<int32_t> slen(c.nslice);
+    std::vector<int64_t> soff(c.nslice + 1, 0);
+    for (int64_t sl = 0; sl < c.nslice; sl++) {
+      int32_t m = 0;
+      for (int t = 0; t < 32; t++) {
+        int32_t I = perm[sl * 32 + t];
+        if (I >= 0) m = std::max(m, nb[I]);
+      }
+      slen[sl] = m;
+      soff[sl + 1] = soff[sl] + 32 * (int64_t)m;
+    }
+    c.sell_plane = soff[c.nslice];
+    c.d_sperm.upload(perm.data(), perm.size(), c.stream);
+    c.d_slen.upload(slen.data(), slen.size(), c.stream);
+    c.d_soff.upload(soff.data(), soff.size(), c.stream);
+    c.d_scol.alloc(std::max<int64_t>(c.sell_plane, 1));
+    c.d_sval.alloc((size_t)std::max<int64_t>(c.sell_plane, 1) * 9);
+    k_fill_sell3<<<grid_for(c.nslice * 32, 256), 256, 0, c.stream>>>(c.d_ia.p, c.d_ja.p, c.d_a.p, c.d_soff.p,
+                                                                     c.d_slen.p, c.d_sperm.p, c.nslice, c.sell_plane,
+                                                                     c.d_scol.p, c.d_sval.p, c.d_err.p);
     c.launches++;
     GPZ_CUDA_TRY(cudaGetLastError());
-    check_device_flag(c, "3x3 block CSR");
+    check_device_flag(c, "sliced ELL of 3x3 blocks");
     c.d_a32.release();
     c.have_bsr3 = true;
   } else {
@@ -816,8 +850,9 @@ void launch_iteration(Ctx &c, const Plan &P) {
   const int padded = P.bsr ? 1 : 0;
   k_mx_p<<<wave(k_mx_p), kThreads, 0, c.stream>>>(w.r32.p, P.M32, w.pm.p, padded, P.nunits, R);
   if (P.bsr) {
-    k_mx_bsr3<<<wave(k_mx_bsr3), kThreads, 0, c.stream>>>(c.d_bptr.p, c.d_bcol.p, c.d_bval.p, (const float4 *)w.pm.p,
-                                                          w.q32.p, c.nbrow, R);
+    k_mx_sell3<<<wave(k_mx_sell3), kThreads, 0, c.stream>>>(c.d_soff.p, c.d_slen.p, c.d_sperm.p, c.d_scol.p,
+                                                            c.d_sval.p, c.sell_plane, (const float4 *)w.pm.p, w.q32.p,
+                                                            c.nslice, R);
   } else {
     GPZ_TPR_SWITCH(P.tpr32, (k_mx_csr<T><<<wave(k_mx_csr<T>), kThreads, 0, c.stream>>>(c.d_ia.p, c.d_ja.p, c.d_a32.p,
                                                                                       w.pm.p, w.q32.p, c.neq, R)));
@@ -967,8 +1002,8 @@ double time_spmv(Ctx &c, bool f32, int reps) {
   const int tpr = pick_tpr(c.nnz, c.neq);
   auto launch = [&]() {
     if (f32 && c.have_bsr3) {
-      k_mx_bsr3<<<wave(k_mx_bsr3), kThreads, 0, s>>>(c.d_bptr.p, c.d_bcol.p, c.d_bval.p, (const float4 *)w.pm.p, w.q32.p,
-                                                     c.nbrow, R);
+      k_mx_sell3<<<wave(k_mx_sell3), kThreads, 0, s>>>(c.d_soff.p, c.d_slen.p, c.d_sperm.p, c.d_scol.p, c.d_sval.p,
+                                                       c.sell_plane, (const float4 *)w.pm.p, w.q32.p, c.nslice, R);
     } else if (f32) {
       GPZ_TPR_SWITCH(pick_tpr32(c.nnz, c.neq), (k_mx_csr<T><<<wave(k_mx_csr<T>), kThreads, 0, s>>>(c.d_ia.p, c.d_ja.p, c.d_a32.p, w.pm.p,
                                                                               w.q32.p, c.neq, R)));
