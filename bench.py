@@ -241,13 +241,15 @@ def run_gpu(args):
                      "pattern_build_s": t_pattern, "host_mesh_build_s": t_mesh},
         "e2e": {"value": round(t_e2e, 6) if t_e2e else None, "unit": "s", "h2d_bytes_per_step": int(b_in + neq * 0),
                 "d2h_bytes_per_step": int(neq * 8)},
-        "roofline": {"bound": "hbm", "kernel": "k_cg_bsr3 (q = A32 p32, 3x3 blocks, p.q)", "achieved": round(ach, 1),
+        "roofline": {"bound": "hbm", "kernel": "mixed-CG FP32 3x3-block SpMV (autotuned layout), q = A32 p32 with p.q",
+                     "achieved": round(ach, 1),
                      "peak": hbm, "unit": "GB/s", "frac": round(ach / hbm, 4), "traffic": None,
                      "algorithmic_bytes": int(bytes32), "ms_per_launch": ms32,
                      "fp64_spmv": {"ms_per_launch": ms64,
                                    "achieved_gbs": round(bytes64 / (ms64 * 1e-3) / 1e9, 1)},
                      "peak_source": "MEASURED_PEAKS.json hbm_gbs (burst copy)" if "fallback" not in pk else
                      "fallback 6.8 TB/s"},
+        "spmv_autotune_ms": ctx.tuning_report(),
         "clocks": clk,
         "gpu_launches": int(launches),
     }

@@ -205,6 +205,9 @@ int gpz_solution_download(gpz_ctx *ctx, double *x);
 #define GPZ_KERNEL_SPMV_FP32 2
 #define GPZ_KERNEL_ASSEMBLE 3
 int gpz_time_kernel(gpz_ctx *ctx, int which, int reps, double *ms_per_launch);
+/* JSON text of the SpMV autotuner's measurements (ms per launch of every
+ * candidate layout / kernel of the mixed CG) for the assembled system. */
+int gpz_tuning_report(gpz_ctx *ctx, char *buf, int64_t len);
 
 #ifdef __cplusplus
 }

@@ -372,4 +372,15 @@ int gpz_time_kernel(gpz_ctx *ctx, int which, int reps, double *ms_per_launch) {
   });
 }
 
+int gpz_tuning_report(gpz_ctx *ctx, char *buf, int64_t len) {
+  return guarded(ctx, [&](Ctx &c) {
+    GPZ_REQUIRE(buf && len > 0, GPZ_E_INVALID, "buffer");
+    std::string r = c.tune_report.empty() ? std::string("{}") : c.tune_report;
+    int64_t n = std::min<int64_t>((int64_t)r.size(), len - 1);
+    std::memcpy(buf, r.data(), n);
+    buf[n] = 0;
+    return GPZ_OK;
+  });
+}
+
 }  // extern "C"

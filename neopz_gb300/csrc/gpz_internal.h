@@ -140,11 +140,21 @@ struct Ctx {
   DBuf<double> d_a, d_f, d_dinv;
   DBuf<float> d_a32;                         // FP32 CSR copy for the inner solves
   bool have_a32 = false;
-  bool have_bsr3 = false;                    // FP32 3x3 blocks in sliced ELL instead of d_a32
-  int64_t nbrow = 0, nslice = 0, sell_plane = 0;
-  DBuf<int64_t> d_soff;                      // [nslice+1] first block of each slice
-  DBuf<int32_t> d_slen, d_sperm, d_scol;     // slice lengths, rows of each slice, block columns
-  DBuf<float> d_sval;                        // 9 planes of sell_plane floats
+  // FP32 3x3 blocks for the mixed CG (instead of d_a32), in the layout the
+  // SpMV autotuner measured fastest on this matrix
+  bool have_bsr3 = false;
+  int spmv32_variant = 0;                    // 0 block CSR, 1 block CSR two rows in flight, 2 sliced ELL
+  std::string tune_report;
+  int64_t nbrow = 0;
+  DBuf<int64_t> d_bptr;                      // block CSR: [nbrow+1]
+  DBuf<int32_t> d_bcol;
+  DBuf<float> d_bval;                        // per block row: 9 planes of its blocks
+  struct Sell {
+    int64_t nslice = 0, plane = 0, window = 0;
+    DBuf<int64_t> soff;                      // [nslice+1] first block of each slice
+    DBuf<int32_t> slen, sperm, scol;         // slice lengths, rows of each slice, block columns
+    DBuf<float> sval;                        // 9 planes of `plane` floats
+  } sell;
   DBuf<double> d_bjinv;                      // block-Jacobi inverses [neq/3][9]
   DBuf<float> d_bjinv32, d_dinv32;           // FP32 preconditioners of the mixed CG
   bool have_bjinv = false;

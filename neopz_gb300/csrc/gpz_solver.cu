@@ -413,6 +413,31 @@ __global__ void __launch_bounds__(kThreads) k_true_resid(const int64_t *__restri
 }
 
 // ---- setup kernels for the mixed path and the block preconditioner
+__global__ void k_build_bsr3(const int64_t *__restrict__ ia, const int32_t *__restrict__ ja,
+                             const double *__restrict__ a, int64_t nbrow, int64_t *__restrict__ bptr,
+                             int32_t *__restrict__ bcol, float *__restrict__ bval, int *__restrict__ err) {
+  const int lane = threadIdx.x & 31;
+  const int64_t I = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) / 32;
+  if (I >= nbrow) return;
+  const int64_t r0 = 3 * I;
+  const int64_t len = ia[r0 + 1] - ia[r0];
+  if (len % 3 != 0 || ia[r0 + 2] - ia[r0 + 1] != len || ia[r0 + 3] - ia[r0 + 2] != len || ia[r0] % 9 != 0) {
+    if (lane == 0) atomicOr(err, 128);
+    return;
+  }
+  const int64_t nb = len / 3, b0 = ia[r0] / 9;
+  if (lane == 0) {
+    bptr[I] = b0;
+    if (I == nbrow - 1) bptr[nbrow] = b0 + nb;
+  }
+  float *v = bval + 9 * b0;
+  for (int64_t j = lane; j < nb; j += 32) {
+    bcol[b0 + j] = ja[ia[r0] + 3 * j] / 3;
+    for (int s = 0; s < 3; s++)
+      for (int t = 0; t < 3; t++) v[(3 * s + t) * nb + j] = (float)a[ia[r0 + s] + 3 * j + t];
+  }
+}
+
 // fill the sliced-ELL planes from the full FP64 CSR (rows 3I..3I+2 of block
 // row I share their columns; block column j covers columns 3j'..3j'+2)
 __global__ void k_fill_sell3(const int64_t *__restrict__ ia, const int32_t *__restrict__ ja,
@@ -534,6 +559,148 @@ __global__ void __launch_bounds__(kThreads) k_mx_p(const float *__restrict__ r, 
       const int64_t j = pidx(u * bs + k, padded);
       p[j] = first ? z[k] : fmaf(beta, p[j], z[k]);
     }
+  }
+}
+
+// q = A32 p over 3x3 block rows; a warp owns a tile of 32 block rows, lane t
+// keeps row t's result so the epilogue (q store, p.q) runs with all lanes.
+__global__ void __launch_bounds__(kThreads) k_mx_bsr3(const int64_t *__restrict__ bptr, const int32_t *__restrict__ bcol,
+                                                      const float *__restrict__ bval, const float4 *__restrict__ p4,
+                                                      float *__restrict__ q, int64_t nbrow, Red R) {
+  if (!active(R.iscal)) return;
+  const int lane = threadIdx.x & 31;
+  const int64_t warp_id = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) / 32;
+  const int64_t nwarps = (int64_t)gridDim.x * blockDim.x / 32;
+  KSum pq;
+  for (int64_t I0 = warp_id * 32; I0 < nbrow; I0 += nwarps * 32) {
+    const int nrow = (int)min((int64_t)32, nbrow - I0);
+    const int64_t mybeg = lane < nrow ? bptr[I0 + lane] : 0;
+    const int64_t myend = lane < nrow ? bptr[I0 + lane + 1] : 0;
+    float m0 = 0.f, m1 = 0.f, m2 = 0.f;
+    for (int t = 0; t < nrow; t++) {
+      const int64_t b0 = __shfl_sync(0xffffffffu, mybeg, t);
+      const int nb = (int)(__shfl_sync(0xffffffffu, myend, t) - b0);
+      const float *v = bval + 9 * b0;
+      float a0 = 0.f, a1 = 0.f, a2 = 0.f;
+      for (int j = lane; j < nb; j += 32) {
+        const float4 xv = __ldg(&p4[__ldcs(&bcol[b0 + j])]);
+        a0 = fmaf(__ldcs(&v[0 * nb + j]), xv.x, a0);
+        a0 = fmaf(__ldcs(&v[1 * nb + j]), xv.y, a0);
+        a0 = fmaf(__ldcs(&v[2 * nb + j]), xv.z, a0);
+        a1 = fmaf(__ldcs(&v[3 * nb + j]), xv.x, a1);
+        a1 = fmaf(__ldcs(&v[4 * nb + j]), xv.y, a1);
+        a1 = fmaf(__ldcs(&v[5 * nb + j]), xv.z, a1);
+        a2 = fmaf(__ldcs(&v[6 * nb + j]), xv.x, a2);
+        a2 = fmaf(__ldcs(&v[7 * nb + j]), xv.y, a2);
+        a2 = fmaf(__ldcs(&v[8 * nb + j]), xv.z, a2);
+      }
+      for (int o = 16; o > 0; o >>= 1) {
+        a0 += __shfl_xor_sync(0xffffffffu, a0, o);
+        a1 += __shfl_xor_sync(0xffffffffu, a1, o);
+        a2 += __shfl_xor_sync(0xffffffffu, a2, o);
+      }
+      if (lane == t) {
+        m0 = a0;
+        m1 = a1;
+        m2 = a2;
+      }
+    }
+    if (lane < nrow) {
+      const int64_t I = I0 + lane;
+      q[3 * I] = m0;
+      q[3 * I + 1] = m1;
+      q[3 * I + 2] = m2;
+      const float4 pv = p4[I];
+      pq.add(pv.x * m0);
+      pq.add(pv.y * m1);
+      pq.add(pv.z * m2);
+    }
+  }
+  double vv[1] = {pq.get()}, tot[1];
+  if (grid_reduce<1>(vv, R, tot) && threadIdx.x == 0) {
+    R.scal[S_PQ] = tot[0];
+    R.scal[S_ALPHA] = R.scal[S_RHO] / tot[0];
+    R.iscal[I_SP32]++;
+  }
+}
+
+// the same with two block rows in flight per warp (row t and row t + 16 of the
+// tile processed together), doubling the independent loads per lane
+__global__ void __launch_bounds__(kThreads) k_mx_bsr3x2(const int64_t *__restrict__ bptr, const int32_t *__restrict__ bcol,
+                                                        const float *__restrict__ bval, const float4 *__restrict__ p4,
+                                                        float *__restrict__ q, int64_t nbrow, Red R) {
+  if (!active(R.iscal)) return;
+  const int lane = threadIdx.x & 31;
+  const int64_t warp_id = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) / 32;
+  const int64_t nwarps = (int64_t)gridDim.x * blockDim.x / 32;
+  KSum pq;
+  for (int64_t I0 = warp_id * 32; I0 < nbrow; I0 += nwarps * 32) {
+    const int nrow = (int)min((int64_t)32, nbrow - I0);
+    const int64_t mybeg = lane < nrow ? bptr[I0 + lane] : 0;
+    const int64_t myend = lane < nrow ? bptr[I0 + lane + 1] : 0;
+    float m0 = 0.f, m1 = 0.f, m2 = 0.f;
+    for (int t = 0; t < 16; t++) {
+      const int tb = t + 16;
+      const int64_t b0 = __shfl_sync(0xffffffffu, mybeg, t), e0 = __shfl_sync(0xffffffffu, myend, t);
+      const int64_t b1 = __shfl_sync(0xffffffffu, mybeg, tb), e1 = __shfl_sync(0xffffffffu, myend, tb);
+      const int na = t < nrow ? (int)(e0 - b0) : 0;
+      const int nbb = tb < nrow ? (int)(e1 - b1) : 0;
+      const float *va = bval + 9 * b0, *vb = bval + 9 * b1;
+      float a0 = 0.f, a1 = 0.f, a2 = 0.f, c0 = 0.f, c1 = 0.f, c2 = 0.f;
+      const int nmax = na > nbb ? na : nbb;
+      for (int j = lane; j < nmax; j += 32) {
+        if (j < na) {
+          const float4 xv = __ldg(&p4[__ldcs(&bcol[b0 + j])]);
+          a0 = fmaf(__ldcs(&va[0 * na + j]), xv.x, a0);
+          a0 = fmaf(__ldcs(&va[1 * na + j]), xv.y, a0);
+          a0 = fmaf(__ldcs(&va[2 * na + j]), xv.z, a0);
+          a1 = fmaf(__ldcs(&va[3 * na + j]), xv.x, a1);
+          a1 = fmaf(__ldcs(&va[4 * na + j]), xv.y, a1);
+          a1 = fmaf(__ldcs(&va[5 * na + j]), xv.z, a1);
+          a2 = fmaf(__ldcs(&va[6 * na + j]), xv.x, a2);
+          a2 = fmaf(__ldcs(&va[7 * na + j]), xv.y, a2);
+          a2 = fmaf(__ldcs(&va[8 * na + j]), xv.z, a2);
+        }
+        if (j < nbb) {
+          const float4 xv = __ldg(&p4[__ldcs(&bcol[b1 + j])]);
+          c0 = fmaf(__ldcs(&vb[0 * nbb + j]), xv.x, c0);
+          c0 = fmaf(__ldcs(&vb[1 * nbb + j]), xv.y, c0);
+          c0 = fmaf(__ldcs(&vb[2 * nbb + j]), xv.z, c0);
+          c1 = fmaf(__ldcs(&vb[3 * nbb + j]), xv.x, c1);
+          c1 = fmaf(__ldcs(&vb[4 * nbb + j]), xv.y, c1);
+          c1 = fmaf(__ldcs(&vb[5 * nbb + j]), xv.z, c1);
+          c2 = fmaf(__ldcs(&vb[6 * nbb + j]), xv.x, c2);
+          c2 = fmaf(__ldcs(&vb[7 * nbb + j]), xv.y, c2);
+          c2 = fmaf(__ldcs(&vb[8 * nbb + j]), xv.z, c2);
+        }
+      }
+      for (int o = 16; o > 0; o >>= 1) {
+        a0 += __shfl_xor_sync(0xffffffffu, a0, o);
+        a1 += __shfl_xor_sync(0xffffffffu, a1, o);
+        a2 += __shfl_xor_sync(0xffffffffu, a2, o);
+        c0 += __shfl_xor_sync(0xffffffffu, c0, o);
+        c1 += __shfl_xor_sync(0xffffffffu, c1, o);
+        c2 += __shfl_xor_sync(0xffffffffu, c2, o);
+      }
+      if (lane == t) { m0 = a0; m1 = a1; m2 = a2; }
+      if (lane == tb) { m0 = c0; m1 = c1; m2 = c2; }
+    }
+    if (lane < nrow) {
+      const int64_t I = I0 + lane;
+      q[3 * I] = m0;
+      q[3 * I + 1] = m1;
+      q[3 * I + 2] = m2;
+      const float4 pv = p4[I];
+      pq.add(pv.x * m0);
+      pq.add(pv.y * m1);
+      pq.add(pv.z * m2);
+    }
+  }
+  double vv[1] = {pq.get()}, tot[1];
+  if (grid_reduce<1>(vv, R, tot) && threadIdx.x == 0) {
+    R.scal[S_PQ] = tot[0];
+    R.scal[S_ALPHA] = R.scal[S_RHO] / tot[0];
+    R.iscal[I_SP32]++;
   }
 }
 
@@ -740,51 +907,150 @@ bool blocks_are_3(const Ctx &c) {
   return true;
 }
 
+// Sliced ELL of 3x3 blocks: block-row lengths from the row pointers, rows
+// sorted by length (descending, stable) inside windows of `window` rows.
+void build_sell(Ctx &c, Ctx::Sell &S, int64_t window) {
+  std::vector<int64_t> ia(c.neq + 1);
+  GPZ_CUDA_TRY(cudaMemcpyAsync(ia.data(), c.d_ia.p, (c.neq + 1) * sizeof(int64_t), cudaMemcpyDeviceToHost, c.stream));
+  GPZ_CUDA_TRY(cudaStreamSynchronize(c.stream));
+  std::vector<int32_t> nb(c.nbrow);
+  for (int64_t I = 0; I < c.nbrow; I++) nb[I] = (int32_t)((ia[3 * I + 1] - ia[3 * I]) / 3);
+  std::vector<int32_t> perm(c.nbrow);
+  for (int64_t I = 0; I < c.nbrow; I++) perm[I] = (int32_t)I;
+  for (int64_t w0 = 0; w0 < c.nbrow; w0 += window) {
+    int64_t w1 = std::min<int64_t>(w0 + window, c.nbrow);
+    std::stable_sort(perm.begin() + w0, perm.begin() + w1, [&](int32_t x, int32_t y) { return nb[x] > nb[y]; });
+  }
+  S.window = window;
+  S.nslice = (c.nbrow + 31) / 32;
+  perm.resize(S.nslice * 32, -1);
+  std::vector<int32_t> slen(S.nslice);
+  std::vector<int64_t> soff(S.nslice + 1, 0);
+  for (int64_t sl = 0; sl < S.nslice; sl++) {
+    int32_t m = 0;
+    for (int t = 0; t < 32; t++) {
+      int32_t I = perm[sl * 32 + t];
+      if (I >= 0) m = std::max(m, nb[I]);
+    }
+    slen[sl] = m;
+    soff[sl + 1] = soff[sl] + 32 * (int64_t)m;
+  }
+  S.plane = soff[S.nslice];
+  S.sperm.upload(perm.data(), perm.size(), c.stream);
+  S.slen.upload(slen.data(), slen.size(), c.stream);
+  S.soff.upload(soff.data(), soff.size(), c.stream);
+  S.scol.alloc(std::max<int64_t>(S.plane, 1));
+  S.sval.alloc((size_t)std::max<int64_t>(S.plane, 1) * 9);
+  k_fill_sell3<<<grid_for(S.nslice * 32, 256), 256, 0, c.stream>>>(c.d_ia.p, c.d_ja.p, c.d_a.p, S.soff.p, S.slen.p,
+                                                                   S.sperm.p, S.nslice, S.plane, S.scol.p, S.sval.p,
+                                                                   c.d_err.p);
+  c.launches++;
+  GPZ_CUDA_TRY(cudaGetLastError());
+  check_device_flag(c, "sliced ELL of 3x3 blocks");
+}
+
+void alloc_work(Ctx &c, bool mixed);
+Red red_of(Ctx &c);
+
+// one launch of the FP32 3x3 SpMV variant v: q32 = A32 pm
+void launch_spmv32(Ctx &c, int v, const Ctx::Sell &S, Red R, cudaStream_t s) {
+  SolverWork &w = c.sw;
+  if (v == 0) {
+    k_mx_bsr3<<<wave(k_mx_bsr3), kThreads, 0, s>>>(c.d_bptr.p, c.d_bcol.p, c.d_bval.p, (const float4 *)w.pm.p, w.q32.p,
+                                                   c.nbrow, R);
+  } else if (v == 1) {
+    k_mx_bsr3x2<<<wave(k_mx_bsr3x2), kThreads, 0, s>>>(c.d_bptr.p, c.d_bcol.p, c.d_bval.p, (const float4 *)w.pm.p,
+                                                       w.q32.p, c.nbrow, R);
+  } else {
+    k_mx_sell3<<<wave(k_mx_sell3), kThreads, 0, s>>>(S.soff.p, S.slen.p, S.sperm.p, S.scol.p, S.sval.p, S.plane,
+                                                     (const float4 *)w.pm.p, w.q32.p, S.nslice, R);
+  }
+  c.launches++;
+}
+
+// Autotuner of the mixed CG's SpMV: every candidate layout / kernel is built
+// and timed (CUDA events, 5 launches after 2 warm-up launches) on this matrix;
+// the fastest is kept and the other layouts are released.
+void tune_spmv32(Ctx &c) {
+  cudaStream_t s = c.stream;
+  alloc_work(c, true);
+  SolverWork &w = c.sw;
+  std::vector<float> ones(w.pm.n, 1.0f);
+  GPZ_CUDA_TRY(cudaMemcpyAsync(w.pm.p, ones.data(), ones.size() * sizeof(float), cudaMemcpyHostToDevice, s));
+  int64_t hi[I_NISCAL] = {0};
+  hi[I_MAXIT] = 1;
+  GPZ_CUDA_TRY(cudaMemcpyAsync(w.iscal.p, hi, sizeof(hi), cudaMemcpyHostToDevice, s));
+  Red R = red_of(c);
+  Ctx::Sell cand[2];
+  const int64_t windows[2] = {64, 2048};
+  struct Res { int v; int64_t window; float ms; };
+  std::vector<Res> res;
+  cudaEvent_t e0, e1;
+  GPZ_CUDA_TRY(cudaEventCreate(&e0));
+  GPZ_CUDA_TRY(cudaEventCreate(&e1));
+  auto time_it = [&](int v, const Ctx::Sell &S) {
+    for (int i = 0; i < 2; i++) launch_spmv32(c, v, S, R, s);
+    GPZ_CUDA_TRY(cudaEventRecord(e0, s));
+    for (int i = 0; i < 5; i++) launch_spmv32(c, v, S, R, s);
+    GPZ_CUDA_TRY(cudaEventRecord(e1, s));
+    GPZ_CUDA_TRY(cudaEventSynchronize(e1));
+    GPZ_CUDA_TRY(cudaGetLastError());
+    float ms = 0;
+    cudaEventElapsedTime(&ms, e0, e1);
+    return ms / 5;
+  };
+  res.push_back({0, 0, time_it(0, cand[0])});
+  res.push_back({1, 0, time_it(1, cand[0])});
+  for (int k = 0; k < 2; k++) {
+    build_sell(c, cand[k], windows[k]);
+    res.push_back({2, windows[k], time_it(2, cand[k])});
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  size_t best = 0;
+  for (size_t i = 1; i < res.size(); i++)
+    if (res[i].ms < res[best].ms) best = i;
+  c.spmv32_variant = res[best].v;
+  std::string rep = "{";
+  for (size_t i = 0; i < res.size(); i++) {
+    const char *nm = res[i].v == 0 ? "block_csr" : (res[i].v == 1 ? "block_csr_2rows" : "sliced_ell");
+    rep += std::string(i ? ", " : "") + "\"" + nm + (res[i].v == 2 ? "_w" + std::to_string(res[i].window) : "") +
+           "\": " + std::to_string(res[i].ms);
+  }
+  c.tune_report = rep + "}";
+  if (c.spmv32_variant == 2) {
+    int k = res[best].window == windows[0] ? 0 : 1;
+    Ctx::Sell &S = cand[k];
+    c.sell.nslice = S.nslice;
+    c.sell.plane = S.plane;
+    c.sell.window = S.window;
+    std::swap(c.sell.soff.p, S.soff.p); std::swap(c.sell.soff.n, S.soff.n);
+    std::swap(c.sell.slen.p, S.slen.p); std::swap(c.sell.slen.n, S.slen.n);
+    std::swap(c.sell.sperm.p, S.sperm.p); std::swap(c.sell.sperm.n, S.sperm.n);
+    std::swap(c.sell.scol.p, S.scol.p); std::swap(c.sell.scol.n, S.scol.n);
+    std::swap(c.sell.sval.p, S.sval.p); std::swap(c.sell.sval.n, S.sval.n);
+    c.d_bptr.release();
+    c.d_bcol.release();
+    c.d_bval.release();
+  }
+}
+
 void make_fp32_copy(Ctx &c) {
   c.have_bsr3 = false;
   if (blocks_are_3(c)) {
-    // sliced ELL of 3x3 blocks: block-row lengths from the row pointers, rows
-    // sorted by length (descending, stable) inside windows of 2048
     c.nbrow = c.neq / 3;
-    std::vector<int64_t> ia(c.neq + 1);
-    GPZ_CUDA_TRY(cudaMemcpyAsync(ia.data(), c.d_ia.p, (c.neq + 1) * sizeof(int64_t), cudaMemcpyDeviceToHost, c.stream));
-    GPZ_CUDA_TRY(cudaStreamSynchronize(c.stream));
-    std::vector<int32_t> nb(c.nbrow);
-    for (int64_t I = 0; I < c.nbrow; I++) nb[I] = (int32_t)((ia[3 * I + 1] - ia[3 * I]) / 3);
-    const int64_t W = 2048;
-    std::vector<int32_t> perm(c.nbrow);
-    for (int64_t I = 0; I < c.nbrow; I++) perm[I] = (int32_t)I;
-    for (int64_t w0 = 0; w0 < c.nbrow; w0 += W) {
-      int64_t w1 = std::min<int64_t>(w0 + W, c.nbrow);
-      std::stable_sort(perm.begin() + w0, perm.begin() + w1, [&](int32_t x, int32_t y) { return nb[x] > nb[y]; });
-    }
-    c.nslice = (c.nbrow + 31) / 32;
-    perm.resize(c.nslice * 32, -1);
-    std::vector<int32_t> slen(c.nslice);
-    std::vector<int64_t> soff(c.nslice + 1, 0);
-    for (int64_t sl = 0; sl < c.nslice; sl++) {
-      int32_t m = 0;
-      for (int t = 0; t < 32; t++) {
-        int32_t I = perm[sl * 32 + t];
-        if (I >= 0) m = std::max(m, nb[I]);
-      }
-      slen[sl] = m;
-      soff[sl + 1] = soff[sl] + 32 * (int64_t)m;
-    }
-    c.sell_plane = soff[c.nslice];
-    c.d_sperm.upload(perm.data(), perm.size(), c.stream);
-    c.d_slen.upload(slen.data(), slen.size(), c.stream);
-    c.d_soff.upload(soff.data(), soff.size(), c.stream);
-    c.d_scol.alloc(std::max<int64_t>(c.sell_plane, 1));
-    c.d_sval.alloc((size_t)std::max<int64_t>(c.sell_plane, 1) * 9);
-    k_fill_sell3<<<grid_for(c.nslice * 32, 256), 256, 0, c.stream>>>(c.d_ia.p, c.d_ja.p, c.d_a.p, c.d_soff.p,
-                                                                     c.d_slen.p, c.d_sperm.p, c.nslice, c.sell_plane,
-                                                                     c.d_scol.p, c.d_sval.p, c.d_err.p);
+    // block CSR
+    c.d_bptr.alloc(c.nbrow + 1);
+    c.d_bcol.alloc(std::max<int64_t>(c.nnz / 9, 1));
+    c.d_bval.alloc(std::max<int64_t>(c.nnz, 1));
+    k_build_bsr3<<<grid_for(c.nbrow * 32, 256), 256, 0, c.stream>>>(c.d_ia.p, c.d_ja.p, c.d_a.p, c.nbrow, c.d_bptr.p,
+                                                                    c.d_bcol.p, c.d_bval.p, c.d_err.p);
     c.launches++;
     GPZ_CUDA_TRY(cudaGetLastError());
-    check_device_flag(c, "sliced ELL of 3x3 blocks");
-    c.d_a32.release();
+    check_device_flag(c, "3x3 block CSR");
     c.have_bsr3 = true;
+    c.d_a32.release();
+    tune_spmv32(c);
   } else {
     c.d_a32.alloc(std::max<int64_t>(c.nnz, 1));
     to_fp32(c);
@@ -803,7 +1069,7 @@ void build_block_jacobi(Ctx &c) {
   c.have_bjinv = true;
 }
 
-namespace {
+// ---- solver workspace and the iteration plan
 
 void alloc_work(Ctx &c, bool mixed) {
   SolverWork &w = c.sw;
@@ -850,9 +1116,8 @@ void launch_iteration(Ctx &c, const Plan &P) {
   const int padded = P.bsr ? 1 : 0;
   k_mx_p<<<wave(k_mx_p), kThreads, 0, c.stream>>>(w.r32.p, P.M32, w.pm.p, padded, P.nunits, R);
   if (P.bsr) {
-    k_mx_sell3<<<wave(k_mx_sell3), kThreads, 0, c.stream>>>(c.d_soff.p, c.d_slen.p, c.d_sperm.p, c.d_scol.p,
-                                                            c.d_sval.p, c.sell_plane, (const float4 *)w.pm.p, w.q32.p,
-                                                            c.nslice, R);
+    launch_spmv32(c, c.spmv32_variant, c.sell, R, c.stream);
+    c.launches--;
   } else {
     GPZ_TPR_SWITCH(P.tpr32, (k_mx_csr<T><<<wave(k_mx_csr<T>), kThreads, 0, c.stream>>>(c.d_ia.p, c.d_ja.p, c.d_a32.p,
                                                                                       w.pm.p, w.q32.p, c.neq, R)));
@@ -866,7 +1131,6 @@ void launch_iteration(Ctx &c, const Plan &P) {
   c.launches += 6;
 }
 
-}  // namespace
 
 int solve(Ctx &c, const gpz_solver_opts &o, gpz_solve_report &rep) {
   const bool mixed = o.solver == GPZ_SOLVER_MIXED_CG;
@@ -1002,8 +1266,8 @@ double time_spmv(Ctx &c, bool f32, int reps) {
   const int tpr = pick_tpr(c.nnz, c.neq);
   auto launch = [&]() {
     if (f32 && c.have_bsr3) {
-      k_mx_sell3<<<wave(k_mx_sell3), kThreads, 0, s>>>(c.d_soff.p, c.d_slen.p, c.d_sperm.p, c.d_scol.p, c.d_sval.p,
-                                                       c.sell_plane, (const float4 *)w.pm.p, w.q32.p, c.nslice, R);
+      launch_spmv32(c, c.spmv32_variant, c.sell, R, s);
+      c.launches--;
     } else if (f32) {
       GPZ_TPR_SWITCH(pick_tpr32(c.nnz, c.neq), (k_mx_csr<T><<<wave(k_mx_csr<T>), kThreads, 0, s>>>(c.d_ia.p, c.d_ja.p, c.d_a32.p, w.pm.p,
                                                                               w.q32.p, c.neq, R)));

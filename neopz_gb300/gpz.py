@@ -103,6 +103,7 @@ def lib():
         L.gpz_pattern_download.argtypes = [vp, vp, vp]
         L.gpz_pattern_info.argtypes = [vp, _P(i64), _P(i64)]
         L.gpz_time_kernel.argtypes = [vp, i32, i32, _P(dp)]
+        L.gpz_tuning_report.argtypes = [vp, ctypes.c_char_p, i64]
         L.gpz_assemble.argtypes = [vp, i32]
         L.gpz_matrix_download.argtypes = [vp, vp]
         L.gpz_rhs_download.argtypes = [vp, vp]
@@ -256,6 +257,12 @@ class Context:
         ms = ctypes.c_double()
         self._check(lib().gpz_time_kernel(self.h, which, reps, ctypes.byref(ms)))
         return ms.value
+
+    def tuning_report(self):
+        import json
+        buf = ctypes.create_string_buffer(4096)
+        self._check(lib().gpz_tuning_report(self.h, buf, 4096))
+        return json.loads(buf.value.decode())
 
     def pattern(self):
         ia = np.zeros(self.neq + 1, np.int64)
