@@ -143,7 +143,9 @@ struct Ctx {
   // FP32 3x3 blocks for the mixed CG (instead of d_a32), in the layout the
   // SpMV autotuner measured fastest on this matrix
   bool have_bsr3 = false;
-  int spmv32_variant = 0;                    // 0 block CSR, 1 block CSR two rows in flight, 2 sliced ELL
+  int spmv32_variant = 0;                    // 0 block CSR, 1 two rows in flight, 2 sliced ELL, 3 TMA-staged
+  uint32_t tma_vcap = 0, tma_ccap = 0;       // shared-memory stage capacities of the TMA-staged kernel
+  int tma_grid = 1;
   std::string tune_report;
   int64_t nbrow = 0;
   DBuf<int64_t> d_bptr;                      // block CSR: [nbrow+1]

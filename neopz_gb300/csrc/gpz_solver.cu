@@ -704,6 +704,167 @@ __global__ void __launch_bounds__(kThreads) k_mx_bsr3x2(const int64_t *__restric
   }
 }
 
+// ---- q = A32 p with the tile's value and column streams staged by TMA
+// Each CTA walks tiles of kTmaRows block rows.  Thread 0 issues two bulk
+// copies (cp.async.bulk, completion counted on an mbarrier) of the next tile's
+// contiguous values and columns into the other shared-memory stage while the
+// eight warps compute the current tile from shared memory; only the p gather
+// still reads global memory.  Bulk copies need 16-byte aligned addresses and
+// sizes, so each copy starts at the 16-byte boundary below the tile and the
+// kernel indexes from the remainder.  Every wait is bounded: on a timeout the
+// kernel records an error flag, waits (bounded) for its own copies and leaves.
+constexpr int kTmaRows = 16;
+
+__device__ __forceinline__ uint32_t smem_u32(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ void mbar_init(uint64_t *bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(uint64_t *bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes) : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+      : "=r"(ok)
+      : "r"(smem_u32(bar)), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+__device__ __forceinline__ bool mbar_wait_bounded(uint64_t *bar, uint32_t parity) {
+  for (int64_t i = 0; i < (1ll << 24); i++)
+    if (mbar_try_wait(bar, parity)) return true;
+  return false;
+}
+__device__ __forceinline__ void bulk_g2s(void *dst, const void *src, uint32_t bytes, uint64_t *bar) {
+  asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                   smem_u32(dst)),
+               "l"(src), "r"(bytes), "r"(smem_u32(bar))
+               : "memory");
+}
+
+struct TmaArgs {
+  const int64_t *bptr;
+  const int32_t *bcol;
+  const float *bval;
+  const float4 *p4;
+  float *q;
+  int64_t nbrow, ntiles;
+  uint32_t vcap, ccap;  // stage capacities in bytes
+  int *err;
+};
+
+__device__ __forceinline__ void tma_issue(const TmaArgs &A, int64_t tile, float *sv, int32_t *sc, uint64_t *bar) {
+  const int64_t I0 = tile * kTmaRows;
+  const int64_t I1 = min(I0 + kTmaRows, A.nbrow);
+  const int64_t b0 = A.bptr[I0], b1 = A.bptr[I1];
+  const uintptr_t v0 = (uintptr_t)(A.bval + 9 * b0), v1 = (uintptr_t)(A.bval + 9 * b1);
+  const uintptr_t c0 = (uintptr_t)(A.bcol + b0), c1 = (uintptr_t)(A.bcol + b1);
+  const uintptr_t va = v0 & ~(uintptr_t)15, ca = c0 & ~(uintptr_t)15;
+  uint32_t vb = (uint32_t)(((v1 - va) + 15) & ~(uintptr_t)15), cb = (uint32_t)(((c1 - ca) + 15) & ~(uintptr_t)15);
+  if (vb == 0) vb = 16;  // (a tile always holds a diagonal block; stay within the allocation slack anyway)
+  if (cb == 0) cb = 16;
+  if (vb > A.vcap || cb > A.ccap) {  // cannot happen with the host's capacity; never copy out of bounds
+    atomicOr(A.err, 1024);
+    vb = 16;
+    cb = 16;
+  }
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+  mbar_expect_tx(bar, vb + cb);
+  bulk_g2s(sv, (const void *)va, vb, bar);
+  bulk_g2s(sc, (const void *)ca, cb, bar);
+}
+
+__global__ void __launch_bounds__(kThreads) k_mx_bsr3_tma(TmaArgs A, Red R) {
+  extern __shared__ __align__(128) unsigned char smem[];
+  __shared__ bool s_ok;
+  if (!active(R.iscal)) return;
+  float *sv[2] = {(float *)smem, (float *)(smem + A.vcap)};
+  int32_t *sc[2] = {(int32_t *)(smem + 2 * A.vcap), (int32_t *)(smem + 2 * A.vcap + A.ccap)};
+  uint64_t *bar = (uint64_t *)(smem + 2 * A.vcap + 2 * A.ccap);
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarp = blockDim.x >> 5;
+  const int64_t first = blockIdx.x, step = gridDim.x;
+  if (threadIdx.x == 0) {
+    mbar_init(&bar[0], 1);
+    mbar_init(&bar[1], 1);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    if (first < A.ntiles) tma_issue(A, first, sv[0], sc[0], &bar[0]);
+  }
+  __syncthreads();
+  KSum pq;
+  bool ok = true;
+  int it = 0;
+  for (int64_t t = first; t < A.ntiles; t += step, it++) {
+    const int st = it & 1;
+    const uint32_t par = (uint32_t)((it >> 1) & 1);
+    if (threadIdx.x == 0) {
+      if (t + step < A.ntiles) tma_issue(A, t + step, sv[st ^ 1], sc[st ^ 1], &bar[st ^ 1]);
+      s_ok = mbar_wait_bounded(&bar[st], par);  // one thread decides, so the exit is uniform
+    }
+    __syncthreads();
+    if (!s_ok) {
+      ok = false;
+      break;
+    }
+    mbar_wait_bounded(&bar[st], par);  // already complete: gives every thread the acquire
+    const int64_t I0 = t * kTmaRows;
+    const int nrow = (int)min((int64_t)kTmaRows, A.nbrow - I0);
+    const int64_t bt = A.bptr[I0];
+    const int dv = (int)(((uintptr_t)(A.bval + 9 * bt) & 15) / 4);
+    const int dc = (int)(((uintptr_t)(A.bcol + bt) & 15) / 4);
+    for (int r = warp; r < nrow; r += nwarp) {
+      const int64_t I = I0 + r;
+      const int64_t b0 = A.bptr[I];
+      const int nb = (int)(A.bptr[I + 1] - b0);
+      const float *v = sv[st] + dv + 9 * (b0 - bt);
+      const int32_t *cc = sc[st] + dc + (b0 - bt);
+      float a0 = 0.f, a1 = 0.f, a2 = 0.f;
+      for (int j = lane; j < nb; j += 32) {
+        const float4 xv = __ldg(&A.p4[cc[j]]);
+        a0 = fmaf(v[0 * nb + j], xv.x, a0);
+        a0 = fmaf(v[1 * nb + j], xv.y, a0);
+        a0 = fmaf(v[2 * nb + j], xv.z, a0);
+        a1 = fmaf(v[3 * nb + j], xv.x, a1);
+        a1 = fmaf(v[4 * nb + j], xv.y, a1);
+        a1 = fmaf(v[5 * nb + j], xv.z, a1);
+        a2 = fmaf(v[6 * nb + j], xv.x, a2);
+        a2 = fmaf(v[7 * nb + j], xv.y, a2);
+        a2 = fmaf(v[8 * nb + j], xv.z, a2);
+      }
+      for (int o = 16; o > 0; o >>= 1) {
+        a0 += __shfl_xor_sync(0xffffffffu, a0, o);
+        a1 += __shfl_xor_sync(0xffffffffu, a1, o);
+        a2 += __shfl_xor_sync(0xffffffffu, a2, o);
+      }
+      if (lane == 0) {
+        A.q[3 * I] = a0;
+        A.q[3 * I + 1] = a1;
+        A.q[3 * I + 2] = a2;
+        const float4 pv = A.p4[I];
+        pq.add(pv.x * a0);
+        pq.add(pv.y * a1);
+        pq.add(pv.z * a2);
+      }
+    }
+    __syncthreads();  // the stage is free for the copy issued next iteration
+  }
+  if (!ok) {
+    // record, then let an outstanding copy of the other stage land before leaving
+    if (threadIdx.x == 0) {
+      atomicOr(A.err, 512);
+      mbar_wait_bounded(&bar[(it & 1) ^ 1], (uint32_t)(((it + 1) >> 1) & 1));
+    }
+    __syncthreads();
+  }
+  double vv[1] = {pq.get()}, tot[1];
+  if (grid_reduce<1>(vv, R, tot) && threadIdx.x == 0) {
+    R.scal[S_PQ] = tot[0];
+    R.scal[S_ALPHA] = R.scal[S_RHO] / tot[0];
+    R.iscal[I_SP32]++;
+  }
+}
+
 // q = A32 p for 3x3 blocks in sliced ELL: slices of 32 block rows (sorted by
 // length inside windows so a slice pads little), lane t owns row t of its
 // slice and walks the slice's block columns; entry k (0..8) of the blocks of a
@@ -961,6 +1122,11 @@ void launch_spmv32(Ctx &c, int v, const Ctx::Sell &S, Red R, cudaStream_t s) {
   } else if (v == 1) {
     k_mx_bsr3x2<<<wave(k_mx_bsr3x2), kThreads, 0, s>>>(c.d_bptr.p, c.d_bcol.p, c.d_bval.p, (const float4 *)w.pm.p,
                                                        w.q32.p, c.nbrow, R);
+  } else if (v == 3) {
+    TmaArgs A{c.d_bptr.p, c.d_bcol.p, c.d_bval.p, (const float4 *)w.pm.p, w.q32.p, c.nbrow,
+              (c.nbrow + kTmaRows - 1) / kTmaRows, c.tma_vcap, c.tma_ccap, c.d_err.p};
+    const size_t sh = 2 * (size_t)c.tma_vcap + 2 * (size_t)c.tma_ccap + 16;
+    k_mx_bsr3_tma<<<c.tma_grid, kThreads, sh, s>>>(A, R);
   } else {
     k_mx_sell3<<<wave(k_mx_sell3), kThreads, 0, s>>>(S.soff.p, S.slen.p, S.sperm.p, S.scol.p, S.sval.p, S.plane,
                                                      (const float4 *)w.pm.p, w.q32.p, S.nslice, R);
@@ -1001,6 +1167,28 @@ void tune_spmv32(Ctx &c) {
   };
   res.push_back({0, 0, time_it(0, cand[0])});
   res.push_back({1, 0, time_it(1, cand[0])});
+  {
+    // TMA-staged variant: per-stage capacity from the largest tile (+ alignment slack)
+    std::vector<int64_t> bp(c.nbrow + 1);
+    GPZ_CUDA_TRY(cudaMemcpyAsync(bp.data(), c.d_bptr.p, (c.nbrow + 1) * sizeof(int64_t), cudaMemcpyDeviceToHost, s));
+    GPZ_CUDA_TRY(cudaStreamSynchronize(s));
+    int64_t maxb = 0;
+    for (int64_t I0 = 0; I0 < c.nbrow; I0 += kTmaRows)
+      maxb = std::max(maxb, bp[std::min<int64_t>(I0 + kTmaRows, c.nbrow)] - bp[I0]);
+    c.tma_vcap = (uint32_t)(((36 * maxb + 32) + 127) & ~127ll);
+    c.tma_ccap = (uint32_t)(((4 * maxb + 32) + 127) & ~127ll);
+    const size_t sh = 2 * (size_t)c.tma_vcap + 2 * (size_t)c.tma_ccap + 16;
+    if (sh <= 200 * 1024) {
+      GPZ_CUDA_TRY(cudaFuncSetAttribute(k_mx_bsr3_tma, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sh));
+      int per = 0, nsm = 0, dev = 0;
+      GPZ_CUDA_TRY(cudaGetDevice(&dev));
+      GPZ_CUDA_TRY(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
+      GPZ_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_mx_bsr3_tma, kThreads, sh));
+      c.tma_grid = std::max(1, std::min(kGridBlocks, nsm * std::max(per, 1)));
+      res.push_back({3, 0, time_it(3, cand[0])});
+      check_device_flag(c, "TMA-staged block SpMV");
+    }
+  }
   for (int k = 0; k < 2; k++) {
     build_sell(c, cand[k], windows[k]);
     res.push_back({2, windows[k], time_it(2, cand[k])});
@@ -1013,11 +1201,20 @@ void tune_spmv32(Ctx &c) {
   c.spmv32_variant = res[best].v;
   std::string rep = "{";
   for (size_t i = 0; i < res.size(); i++) {
-    const char *nm = res[i].v == 0 ? "block_csr" : (res[i].v == 1 ? "block_csr_2rows" : "sliced_ell");
+    const char *nm = res[i].v == 0 ? "block_csr"
+                     : res[i].v == 1 ? "block_csr_2rows"
+                     : res[i].v == 3 ? "block_csr_tma_staged"
+                                     : "sliced_ell";
     rep += std::string(i ? ", " : "") + "\"" + nm + (res[i].v == 2 ? "_w" + std::to_string(res[i].window) : "") +
            "\": " + std::to_string(res[i].ms);
   }
   c.tune_report = rep + "}";
+  if (c.spmv32_variant != 2) {
+    for (int k = 0; k < 2; k++) {
+      cand[k].scol.release();
+      cand[k].sval.release();
+    }
+  }
   if (c.spmv32_variant == 2) {
     int k = res[best].window == windows[0] ? 0 : 1;
     Ctx::Sell &S = cand[k];
@@ -1041,8 +1238,8 @@ void make_fp32_copy(Ctx &c) {
     c.nbrow = c.neq / 3;
     // block CSR
     c.d_bptr.alloc(c.nbrow + 1);
-    c.d_bcol.alloc(std::max<int64_t>(c.nnz / 9, 1));
-    c.d_bval.alloc(std::max<int64_t>(c.nnz, 1));
+    c.d_bcol.alloc(std::max<int64_t>(c.nnz / 9, 1) + 16);  // slack for 16-byte rounded bulk copies
+    c.d_bval.alloc(std::max<int64_t>(c.nnz, 1) + 16);
     k_build_bsr3<<<grid_for(c.nbrow * 32, 256), 256, 0, c.stream>>>(c.d_ia.p, c.d_ja.p, c.d_a.p, c.nbrow, c.d_bptr.p,
                                                                     c.d_bcol.p, c.d_bval.p, c.d_err.p);
     c.launches++;
@@ -1230,6 +1427,7 @@ int solve(Ctx &c, const gpz_solver_opts &o, gpz_solve_report &rep) {
   cudaEventElapsedTime(&ms, ev0, ev1);
   cudaEventDestroy(ev0);
   cudaEventDestroy(ev1);
+  check_device_flag(c, "iterative solve");
   rep.iterations = hstate[I_IT];
   rep.resid = hs[S_RESID];
   rep.true_resid = std::sqrt(hs[S_TRUERR]) / hs[S_NORMB];
