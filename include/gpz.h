@@ -176,6 +176,8 @@ typedef struct {
   double reliable_delta;   /* mixed CG: true-residual update when ||r|| < delta * max||r|| */
   int32_t use_graph;       /* capture the iteration batch in a CUDA graph */
   int32_t from_current;    /* FromCurrent: start from x instead of zero */
+  int32_t spmv_variant;    /* mixed CG: -1 = autotuned; 0 block CSR, 1 two rows in flight, 2 sliced ELL,
+                              3 TMA-staged block CSR, 4 upper triangle with float4 atomics */
 } gpz_solver_opts;
 
 typedef struct {

@@ -143,12 +143,15 @@ struct Ctx {
   // FP32 3x3 blocks for the mixed CG (instead of d_a32), in the layout the
   // SpMV autotuner measured fastest on this matrix
   bool have_bsr3 = false;
-  int spmv32_variant = 0;                    // 0 block CSR, 1 two rows in flight, 2 sliced ELL, 3 TMA-staged
+  int spmv32_variant = 0;                    // 0 block CSR, 1 two rows in flight, 2 sliced ELL, 3 TMA-staged,
+                                             // 4 upper triangle with float4 atomics
   uint32_t tma_vcap = 0, tma_ccap = 0;       // shared-memory stage capacities of the TMA-staged kernel
   int tma_grid = 1;
   std::string tune_report;
   int64_t nbrow = 0;
-  DBuf<int64_t> d_bptr;                      // block CSR: [nbrow+1]
+  DBuf<int64_t> d_bptr, d_uptr;              // block CSR and its upper triangle: [nbrow+1]
+  DBuf<int32_t> d_ucol;
+  DBuf<float> d_uval;
   DBuf<int32_t> d_bcol;
   DBuf<float> d_bval;                        // per block row: 9 planes of its blocks
   struct Sell {
@@ -175,7 +178,7 @@ void build_element_offsets(Ctx &c);
 // assemble.cu
 void build_buckets(Ctx &c, const gpz_mesh_desc &d);
 void assemble_fp64(Ctx &c);
-void make_fp32_copy(Ctx &c);
+void make_fp32_copy(Ctx &c, int variant = -1);
 void to_fp32(Ctx &c);
 void build_block_jacobi(Ctx &c);
 // solver.cu

@@ -547,7 +547,7 @@ __device__ __forceinline__ void apply_prec32(const Prec32 &M, const float *__res
 
 // p = z + beta p (z = M r), or p = z at the first iteration / after a restart
 __global__ void __launch_bounds__(kThreads) k_mx_p(const float *__restrict__ r, Prec32 M, float *__restrict__ p,
-                                                   int padded, int64_t nunits, Red R) {
+                                                   int padded, float *__restrict__ qzero, int64_t nunits, Red R) {
   if (!active(R.iscal)) return;
   const bool first = R.iscal[I_IT] == 0 || R.iscal[I_RESTART] != 0;
   const float beta = first ? 0.f : (float)R.scal[S_BETA];
@@ -558,6 +558,7 @@ __global__ void __launch_bounds__(kThreads) k_mx_p(const float *__restrict__ r, 
     for (int k = 0; k < bs; k++) {
       const int64_t j = pidx(u * bs + k, padded);
       p[j] = first ? z[k] : fmaf(beta, p[j], z[k]);
+      if (qzero) qzero[j] = 0.f;  // the symmetric SpMV accumulates q with atomics
     }
   }
 }
@@ -865,6 +866,97 @@ __global__ void __launch_bounds__(kThreads) k_mx_bsr3_tma(TmaArgs A, Red R) {
   }
 }
 
+// ---- q = A32 p from the upper triangle of 3x3 blocks only (A symmetric)
+// Block row I stores its diagonal block and the blocks J > I (9 planes per
+// row, as the full block CSR).  y_I gets B p_J; the transposed products B^T p_I
+// go to block row J with one float4 atomic add each (q is padded to four floats
+// per block row and zeroed by the p-update kernel).  p.q is summed from the
+// symmetric form: p_I.B p_I on the diagonal, 2 p_I.B p_J off it.
+__global__ void __launch_bounds__(kThreads) k_mx_sym3(const int64_t *__restrict__ uptr, const int32_t *__restrict__ ucol,
+                                                      const float *__restrict__ uval, const float4 *__restrict__ p4,
+                                                      float4 *__restrict__ q4, int64_t nbrow, Red R) {
+  if (!active(R.iscal)) return;
+  const int lane = threadIdx.x & 31;
+  const int64_t warp_id = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) / 32;
+  const int64_t nwarps = (int64_t)gridDim.x * blockDim.x / 32;
+  KSum pq;
+  for (int64_t I = warp_id; I < nbrow; I += nwarps) {
+    const int64_t b0 = uptr[I];
+    const int nb = (int)(uptr[I + 1] - b0);
+    const float *v = uval + 9 * b0;
+    const float4 xi = __ldg(&p4[I]);
+    float a0 = 0.f, a1 = 0.f, a2 = 0.f;
+    for (int j = lane; j < nb; j += 32) {
+      const int J = __ldcs(&ucol[b0 + j]);
+      const float4 xj = __ldg(&p4[J]);
+      const float m00 = __ldcs(&v[0 * nb + j]), m01 = __ldcs(&v[1 * nb + j]), m02 = __ldcs(&v[2 * nb + j]);
+      const float m10 = __ldcs(&v[3 * nb + j]), m11 = __ldcs(&v[4 * nb + j]), m12 = __ldcs(&v[5 * nb + j]);
+      const float m20 = __ldcs(&v[6 * nb + j]), m21 = __ldcs(&v[7 * nb + j]), m22 = __ldcs(&v[8 * nb + j]);
+      const float y0 = fmaf(m00, xj.x, fmaf(m01, xj.y, m02 * xj.z));
+      const float y1 = fmaf(m10, xj.x, fmaf(m11, xj.y, m12 * xj.z));
+      const float y2 = fmaf(m20, xj.x, fmaf(m21, xj.y, m22 * xj.z));
+      a0 += y0;
+      a1 += y1;
+      a2 += y2;
+      const float d = fmaf(xi.x, y0, fmaf(xi.y, y1, xi.z * y2));
+      if (J != I) {
+        float4 t;
+        t.x = fmaf(m00, xi.x, fmaf(m10, xi.y, m20 * xi.z));
+        t.y = fmaf(m01, xi.x, fmaf(m11, xi.y, m21 * xi.z));
+        t.z = fmaf(m02, xi.x, fmaf(m12, xi.y, m22 * xi.z));
+        t.w = 0.f;
+        atomicAdd(&q4[J], t);
+        pq.add(2.f * d);
+      } else {
+        pq.add(d);
+      }
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+      a0 += __shfl_xor_sync(0xffffffffu, a0, o);
+      a1 += __shfl_xor_sync(0xffffffffu, a1, o);
+      a2 += __shfl_xor_sync(0xffffffffu, a2, o);
+    }
+    if (lane == 0) atomicAdd(&q4[I], make_float4(a0, a1, a2, 0.f));
+  }
+  double vv[1] = {pq.get()}, tot[1];
+  if (grid_reduce<1>(vv, R, tot) && threadIdx.x == 0) {
+    R.scal[S_PQ] = tot[0];
+    R.scal[S_ALPHA] = R.scal[S_RHO] / tot[0];
+    R.iscal[I_SP32]++;
+  }
+}
+
+// upper triangle of the block CSR: the suffix of every sorted block row from
+// its diagonal block (counts first, then the copy)
+__global__ void k_upper_count(const int64_t *__restrict__ bptr, const int32_t *__restrict__ bcol, int64_t nbrow,
+                              int64_t *__restrict__ ucount, int *__restrict__ err) {
+  const int64_t I = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (I >= nbrow) return;
+  int64_t lo = bptr[I], hi = bptr[I + 1];
+  while (lo < hi) {
+    int64_t mid = (lo + hi) >> 1;
+    if (bcol[mid] < I) lo = mid + 1;
+    else hi = mid;
+  }
+  if (lo >= bptr[I + 1] || bcol[lo] != I) atomicOr(err, 2048);
+  ucount[I] = bptr[I + 1] - lo;
+}
+
+__global__ void k_upper_fill(const int64_t *__restrict__ bptr, const int32_t *__restrict__ bcol,
+                             const float *__restrict__ bval, const int64_t *__restrict__ uptr, int64_t nbrow,
+                             int32_t *__restrict__ ucol, float *__restrict__ uval) {
+  const int lane = threadIdx.x & 31;
+  const int64_t I = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) / 32;
+  if (I >= nbrow) return;
+  const int64_t b0 = bptr[I], nb = bptr[I + 1] - b0, u0 = uptr[I], nu = uptr[I + 1] - u0, skip = nb - nu;
+  const float *v = bval + 9 * b0;
+  float *w = uval + 9 * u0;
+  for (int64_t j = lane; j < nu; j += 32) {
+    ucol[u0 + j] = bcol[b0 + skip + j];
+    for (int k = 0; k < 9; k++) w[k * nu + j] = v[k * nb + skip + j];
+  }
+}
+
 // q = A32 p for 3x3 blocks in sliced ELL: slices of 32 block rows (sorted by
 // length inside windows so a slice pads little), lane t owns row t of its
 // slice and walks the slice's block columns; entry k (0..8) of the blocks of a
@@ -946,7 +1038,7 @@ __global__ void __launch_bounds__(kThreads) k_mx_csr(const int64_t *__restrict__
 // alpha = rho / pq; dx += alpha p; r -= alpha q; rho' = r.(M r), rr = r.r
 __global__ void __launch_bounds__(kThreads) k_mx_update(float *__restrict__ dx, float *__restrict__ r,
                                                         const float *__restrict__ p, const float *__restrict__ q,
-                                                        Prec32 M, int padded, int64_t nunits, Red R) {
+                                                        Prec32 M, int padded, int qpad, int64_t nunits, Red R) {
   if (!active(R.iscal)) return;
   const double pq = R.scal[S_PQ];
   const float alpha = (float)R.scal[S_ALPHA];
@@ -957,7 +1049,7 @@ __global__ void __launch_bounds__(kThreads) k_mx_update(float *__restrict__ dx, 
       const int64_t i = u * bs + k;
       const float pi = p[pidx(i, padded)];
       dx[i] = fmaf(alpha, pi, dx[i]);
-      const float ri = fmaf(-alpha, q[i], r[i]);
+      const float ri = fmaf(-alpha, q[pidx(i, qpad)], r[i]);
       r[i] = ri;
       rr.add(ri * ri);
     }
@@ -1122,6 +1214,9 @@ void launch_spmv32(Ctx &c, int v, const Ctx::Sell &S, Red R, cudaStream_t s) {
   } else if (v == 1) {
     k_mx_bsr3x2<<<wave(k_mx_bsr3x2), kThreads, 0, s>>>(c.d_bptr.p, c.d_bcol.p, c.d_bval.p, (const float4 *)w.pm.p,
                                                        w.q32.p, c.nbrow, R);
+  } else if (v == 4) {
+    k_mx_sym3<<<wave(k_mx_sym3), kThreads, 0, s>>>(c.d_uptr.p, c.d_ucol.p, c.d_uval.p, (const float4 *)w.pm.p,
+                                                   (float4 *)w.q32.p, c.nbrow, R);
   } else if (v == 3) {
     TmaArgs A{c.d_bptr.p, c.d_bcol.p, c.d_bval.p, (const float4 *)w.pm.p, w.q32.p, c.nbrow,
               (c.nbrow + kTmaRows - 1) / kTmaRows, c.tma_vcap, c.tma_ccap, c.d_err.p};
@@ -1137,7 +1232,7 @@ void launch_spmv32(Ctx &c, int v, const Ctx::Sell &S, Red R, cudaStream_t s) {
 // Autotuner of the mixed CG's SpMV: every candidate layout / kernel is built
 // and timed (CUDA events, 5 launches after 2 warm-up launches) on this matrix;
 // the fastest is kept and the other layouts are released.
-void tune_spmv32(Ctx &c) {
+void tune_spmv32(Ctx &c, int only) {
   cudaStream_t s = c.stream;
   alloc_work(c, true);
   SolverWork &w = c.sw;
@@ -1165,9 +1260,10 @@ void tune_spmv32(Ctx &c) {
     cudaEventElapsedTime(&ms, e0, e1);
     return ms / 5;
   };
-  res.push_back({0, 0, time_it(0, cand[0])});
-  res.push_back({1, 0, time_it(1, cand[0])});
-  {
+  auto want = [&](int v) { return only < 0 || only == v; };
+  if (want(0)) res.push_back({0, 0, time_it(0, cand[0])});
+  if (want(1)) res.push_back({1, 0, time_it(1, cand[0])});
+  if (want(3)) {
     // TMA-staged variant: per-stage capacity from the largest tile (+ alignment slack)
     std::vector<int64_t> bp(c.nbrow + 1);
     GPZ_CUDA_TRY(cudaMemcpyAsync(bp.data(), c.d_bptr.p, (c.nbrow + 1) * sizeof(int64_t), cudaMemcpyDeviceToHost, s));
@@ -1189,10 +1285,33 @@ void tune_spmv32(Ctx &c) {
       check_device_flag(c, "TMA-staged block SpMV");
     }
   }
-  for (int k = 0; k < 2; k++) {
+  for (int k = 0; k < 2 && want(2); k++) {
+    if (only == 2 && k == 0) continue;
     build_sell(c, cand[k], windows[k]);
     res.push_back({2, windows[k], time_it(2, cand[k])});
   }
+  if (want(4)) {
+    DBuf<int64_t> ucount;
+    ucount.alloc(c.nbrow + 1);
+    ucount.zero(s);
+    k_upper_count<<<grid_for(c.nbrow, 256), 256, 0, s>>>(c.d_bptr.p, c.d_bcol.p, c.nbrow, ucount.p, c.d_err.p);
+    c.launches++;
+    GPZ_CUDA_TRY(cudaGetLastError());
+    check_device_flag(c, "upper block count");
+    c.d_uptr.alloc(c.nbrow + 1);
+    exclusive_scan_i64(ucount.p, c.d_uptr.p, c.nbrow + 1, s, c);
+    int64_t nu = 0;
+    GPZ_CUDA_TRY(cudaMemcpyAsync(&nu, c.d_uptr.p + c.nbrow, sizeof(int64_t), cudaMemcpyDeviceToHost, s));
+    GPZ_CUDA_TRY(cudaStreamSynchronize(s));
+    c.d_ucol.alloc(std::max<int64_t>(nu, 1));
+    c.d_uval.alloc((size_t)std::max<int64_t>(nu, 1) * 9);
+    k_upper_fill<<<grid_for(c.nbrow * 32, 256), 256, 0, s>>>(c.d_bptr.p, c.d_bcol.p, c.d_bval.p, c.d_uptr.p, c.nbrow,
+                                                             c.d_ucol.p, c.d_uval.p);
+    c.launches++;
+    GPZ_CUDA_TRY(cudaGetLastError());
+    res.push_back({4, 0, time_it(4, cand[0])});
+  }
+  if (res.empty()) res.push_back({0, 0, time_it(0, cand[0])});
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
   size_t best = 0;
@@ -1204,6 +1323,7 @@ void tune_spmv32(Ctx &c) {
     const char *nm = res[i].v == 0 ? "block_csr"
                      : res[i].v == 1 ? "block_csr_2rows"
                      : res[i].v == 3 ? "block_csr_tma_staged"
+                     : res[i].v == 4 ? "upper_blocks_float4_atomics"
                                      : "sliced_ell";
     rep += std::string(i ? ", " : "") + "\"" + nm + (res[i].v == 2 ? "_w" + std::to_string(res[i].window) : "") +
            "\": " + std::to_string(res[i].ms);
@@ -1214,6 +1334,14 @@ void tune_spmv32(Ctx &c) {
       cand[k].scol.release();
       cand[k].sval.release();
     }
+  }
+  if (c.spmv32_variant != 4) {
+    c.d_uptr.release();
+    c.d_ucol.release();
+    c.d_uval.release();
+  } else {
+    c.d_bcol.release();
+    c.d_bval.release();
   }
   if (c.spmv32_variant == 2) {
     int k = res[best].window == windows[0] ? 0 : 1;
@@ -1232,7 +1360,7 @@ void tune_spmv32(Ctx &c) {
   }
 }
 
-void make_fp32_copy(Ctx &c) {
+void make_fp32_copy(Ctx &c, int variant) {
   c.have_bsr3 = false;
   if (blocks_are_3(c)) {
     c.nbrow = c.neq / 3;
@@ -1247,7 +1375,7 @@ void make_fp32_copy(Ctx &c) {
     check_device_flag(c, "3x3 block CSR");
     c.have_bsr3 = true;
     c.d_a32.release();
-    tune_spmv32(c);
+    tune_spmv32(c, variant);
   } else {
     c.d_a32.alloc(std::max<int64_t>(c.nnz, 1));
     to_fp32(c);
@@ -1279,7 +1407,7 @@ void alloc_work(Ctx &c, bool mixed) {
   if (mixed) {
     w.pm.alloc(c.have_bsr3 ? (size_t)std::max<int64_t>(c.nbrow, 1) * 4 : (size_t)n);
     w.r32.alloc(n);
-    w.q32.alloc(n);
+    w.q32.alloc(c.have_bsr3 ? std::max<size_t>((size_t)n, (size_t)c.nbrow * 4) : (size_t)n);
     w.dx32.alloc(n);
   }
   w.partial.alloc((size_t)kGridBlocks * 4);
@@ -1311,7 +1439,9 @@ void launch_iteration(Ctx &c, const Plan &P) {
     return;
   }
   const int padded = P.bsr ? 1 : 0;
-  k_mx_p<<<wave(k_mx_p), kThreads, 0, c.stream>>>(w.r32.p, P.M32, w.pm.p, padded, P.nunits, R);
+  const bool sym = P.bsr && c.spmv32_variant == 4;
+  k_mx_p<<<wave(k_mx_p), kThreads, 0, c.stream>>>(w.r32.p, P.M32, w.pm.p, padded, sym ? w.q32.p : nullptr, P.nunits,
+                                                  R);
   if (P.bsr) {
     launch_spmv32(c, c.spmv32_variant, c.sell, R, c.stream);
     c.launches--;
@@ -1320,7 +1450,7 @@ void launch_iteration(Ctx &c, const Plan &P) {
                                                                                       w.pm.p, w.q32.p, c.neq, R)));
   }
   k_mx_update<<<wave(k_mx_update), kThreads, 0, c.stream>>>(w.dx32.p, w.r32.p, w.pm.p, w.q32.p, P.M32, padded,
-                                                            P.nunits, R);
+                                                            sym ? 1 : 0, P.nunits, R);
   k_mx_foldx<<<wave(k_mx_foldx), kThreads, 0, c.stream>>>(w.x.p, w.dx32.p, c.neq, 0, R);
   GPZ_TPR_SWITCH(P.tpr, (k_reliable<T><<<wave(k_reliable<T>), kThreads, 0, c.stream>>>(c.d_ia.p, c.d_ja.p, c.d_a.p,
                                                                                         w.x.p, w.b.p, w.r.p, c.neq, R)));
@@ -1335,7 +1465,8 @@ int solve(Ctx &c, const gpz_solver_opts &o, gpz_solve_report &rep) {
   GPZ_REQUIRE(o.precond == GPZ_PRECOND_JACOBI || o.precond == GPZ_PRECOND_BLOCK_JACOBI || o.precond == 0,
               GPZ_E_INVALID, "preconditioner not available");
   const bool block = o.precond == GPZ_PRECOND_BLOCK_JACOBI;
-  if (mixed && !c.have_a32) make_fp32_copy(c);
+  if (mixed && (!c.have_a32 || (o.spmv_variant >= 0 && c.have_bsr3 && o.spmv_variant != c.spmv32_variant)))
+    make_fp32_copy(c, o.spmv_variant);
   if (block && !c.have_bjinv) build_block_jacobi(c);
   alloc_work(c, mixed);
   SolverWork &w = c.sw;

@@ -53,7 +53,8 @@ class gpz_mesh_desc(ctypes.Structure):
 class gpz_solver_opts(ctypes.Structure):
     _fields_ = [("solver", ctypes.c_int32), ("precond", ctypes.c_int32), ("max_iter", ctypes.c_int64),
                 ("tol", ctypes.c_double), ("gmres_krylov", ctypes.c_int32), ("check_every", ctypes.c_int32),
-                ("reliable_delta", ctypes.c_double), ("use_graph", ctypes.c_int32), ("from_current", ctypes.c_int32)]
+                ("reliable_delta", ctypes.c_double), ("use_graph", ctypes.c_int32), ("from_current", ctypes.c_int32),
+                ("spmv_variant", ctypes.c_int32)]
 
 
 class gpz_solve_report(ctypes.Structure):
@@ -291,12 +292,14 @@ class Context:
         return z
 
     def solve(self, solver=GPZ_SOLVER_CG, precond=GPZ_PRECOND_JACOBI, max_iter=20000, tol=1e-8, b=None,
-              check_every=32, reliable_delta=1e-3, use_graph=True, x0=None, want_x=True, gmres_krylov=30):
+              check_every=32, reliable_delta=1e-3, use_graph=True, x0=None, want_x=True, gmres_krylov=30,
+              spmv_variant=-1):
         o = gpz_solver_opts()
         o.solver, o.precond, o.max_iter, o.tol = solver, precond, max_iter, tol
         o.gmres_krylov, o.check_every, o.reliable_delta, o.use_graph = gmres_krylov, check_every, reliable_delta, \
             int(use_graph)
         o.from_current = int(x0 is not None)
+        o.spmv_variant = spmv_variant
         rep = gpz_solve_report()
         x = None
         if want_x or x0 is not None:

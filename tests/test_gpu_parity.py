@@ -192,3 +192,24 @@ def test_mixed_block_jacobi_bsr3(built):
     ref = O.cg_jacobi(True, oia, oja, oa, of, 20000, 1e-12)
     assert np.linalg.norm(sol["x"] - ref["x"]) <= 1e-5 * np.linalg.norm(ref["x"])
     ctx.close()
+
+
+@pytest.mark.parametrize("variant", [0, 1, 2, 3, 4])
+def test_mixed_spmv_variants_converge(built, variant):
+    """Every layout / kernel the SpMV autotuner can pick gives the same converged solution."""
+    g = _gpz()
+    rng = np.random.default_rng(11)
+    E = np.exp(rng.standard_normal(5 ** 3))
+    om, grid = O.elasticity3d(5, 2, E=E), g.elasticity3d(5, 2, E=E)
+    ctx = g.Context(0)
+    ctx.upload_mesh(grid)
+    ctx.build_pattern(False)
+    ctx.assemble(g.GPZ_PREC_MIXED)
+    sol = ctx.solve(solver=g.GPZ_SOLVER_MIXED_CG, precond=g.GPZ_PRECOND_BLOCK_JACOBI, tol=1e-8, reliable_delta=1e-2,
+                    spmv_variant=variant)
+    assert sol["rc"] == 0 and sol["true_resid"] <= 1e-8
+    oia, oja = om.pattern(True)
+    oa, of = om.assemble(True, oia, oja)
+    ref = O.cg_jacobi(True, oia, oja, oa, of, 20000, 1e-12)
+    assert np.linalg.norm(sol["x"] - ref["x"]) <= 1e-5 * np.linalg.norm(ref["x"])
+    ctx.close()
