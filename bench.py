@@ -32,6 +32,9 @@ SEED = 5
 # algorithm, measured with the FP64 parity path); used to extrapolate the CPU
 # sample to the full solve.
 JACOBI_ITERS_64 = None
+# HBM bytes per stored block measured by ncu for the SpMV kernels (32^3 case):
+# k_mx_sym3 375.6 MB read + 3.3 MB written over 8,624,609 upper blocks
+NCU_TRAFFIC_PER_BLOCK = {"upper_blocks_float4_atomics": (375.615488e6 + 3.251968e6) / 8624609}
 
 
 def parse():
@@ -191,18 +194,33 @@ def run_gpu(args):
         t_step = float(t.item())
     last = reps[-1]
 
-    # roofline of the dominant kernel: the FP32-value CSR SpMV of the inner CG
+    # roofline of the dominant kernel: the FP32 3x3-block SpMV of the inner CG, in the
+    # layout the library's autotuner chose (HBM bytes that layout must stream per launch)
+    tune = ctx.tuning_report()
     ms32 = ctx.time_kernel(gpz.GPZ_KERNEL_SPMV_FP32, 20)
     ms64 = ctx.time_kernel(gpz.GPZ_KERNEL_SPMV_FP64, 10)
     neq = grid.neq
     nbrow = neq // 3
-    # 3x3 block CSR: 36 B values + 4 B column per block, block row pointers, p32 gather (16 B per block row,
-    # each read once ideally), q write and p read for p.q
-    bytes32 = (nnz // 9) * (36 + 4) + (nbrow + 1) * 8 + nbrow * 16 + neq * 8 + neq * 8
+    chosen = tune.get("chosen", "block_csr")
+    if chosen == "upper_blocks_float4_atomics":
+        nblk = tune["blocks_upper"]
+        kern = "k_mx_sym3: upper 3x3 blocks (36 B values + 4 B column), transposed products as float4 atomics in L2"
+        l2_atomics = nblk
+    else:
+        nblk = tune.get("blocks_full", nnz // 9)
+        kern = "k_mx_" + chosen + ": full 3x3 blocks (36 B values + 4 B column)"
+        l2_atomics = 0
+    # values + columns + block-row pointers + p (16 B per block row, read once) + q (written once)
+    bytes32 = nblk * (36 + 4) + (nbrow + 1) * 8 + nbrow * 16 + nbrow * 16
     bytes64 = nnz * (8 + 4) + (neq + 1) * 8 + neq * 8 + neq * 8 + neq * 8
     pk = peaks()
     hbm = pk.get("hbm_gbs", 6800.0)
     ach = bytes32 / (ms32 * 1e-3) / 1e9
+    # ncu capture of this kernel on the 32^3 case (dram__bytes_read.sum + dram__bytes_write.sum per launch),
+    # scaled by stored blocks to this size (traffic grows in proportion to the blocks streamed)
+    traffic = None
+    if chosen in NCU_TRAFFIC_PER_BLOCK:
+        traffic = int(NCU_TRAFFIC_PER_BLOCK[chosen] * nblk)
 
     # end to end through the C ABI from host buffers
     e2e_times = []
@@ -241,9 +259,9 @@ def run_gpu(args):
                      "pattern_build_s": t_pattern, "host_mesh_build_s": t_mesh},
         "e2e": {"value": round(t_e2e, 6) if t_e2e else None, "unit": "s", "h2d_bytes_per_step": int(b_in + neq * 0),
                 "d2h_bytes_per_step": int(neq * 8)},
-        "roofline": {"bound": "hbm", "kernel": "mixed-CG FP32 3x3-block SpMV (autotuned layout), q = A32 p32 with p.q",
-                     "achieved": round(ach, 1),
-                     "peak": hbm, "unit": "GB/s", "frac": round(ach / hbm, 4), "traffic": None,
+        "roofline": {"bound": "hbm", "kernel": kern, "achieved": round(ach, 1),
+                     "peak": hbm, "unit": "GB/s", "frac": round(ach / hbm, 4), "traffic": traffic,
+                     "l2_float4_atomics_per_launch": l2_atomics,
                      "algorithmic_bytes": int(bytes32), "ms_per_launch": ms32,
                      "fp64_spmv": {"ms_per_launch": ms64,
                                    "achieved_gbs": round(bytes64 / (ms64 * 1e-3) / 1e9, 1)},

@@ -1328,7 +1328,15 @@ void tune_spmv32(Ctx &c, int only) {
     rep += std::string(i ? ", " : "") + "\"" + nm + (res[i].v == 2 ? "_w" + std::to_string(res[i].window) : "") +
            "\": " + std::to_string(res[i].ms);
   }
-  c.tune_report = rep + "}";
+  int64_t nu = 0;
+  if (c.d_uptr.p) {
+    GPZ_CUDA_TRY(cudaMemcpy(&nu, c.d_uptr.p + c.nbrow, sizeof(int64_t), cudaMemcpyDeviceToHost));
+  }
+  const char *names[5] = {"block_csr", "block_csr_2rows", "sliced_ell", "block_csr_tma_staged",
+                          "upper_blocks_float4_atomics"};
+  c.tune_report = rep + ", \"chosen\": \"" + names[res[best].v] + "\", \"block_rows\": " + std::to_string(c.nbrow) +
+                  ", \"blocks_full\": " + std::to_string(c.nnz / 9) + ", \"blocks_upper\": " + std::to_string(nu) +
+                  "}";
   if (c.spmv32_variant != 2) {
     for (int k = 0; k < 2; k++) {
       cand[k].scol.release();
