@@ -35,6 +35,7 @@ extern "C" {
 #define GPZ_E_DEVICE_CHECK (-7)        /* a kernel's own bounds / invariant check failed */
 #define GPZ_E_NO_DEVICE (-8)           /* no CUDA device visible */
 #define GPZ_E_BREAKDOWN (-9)           /* NaN / non-positive curvature in the Krylov recurrence */
+#define GPZ_E_TOO_LARGE (-10)          /* problem exceeds the fixed scratch of gpz_cg_jacobi_noalloc */
 
 /* ---- element types (TPZShapeLinear / TPZShapeQuad / TPZShapeCube) -------- */
 #define GPZ_EL_LINE 1
@@ -210,6 +211,36 @@ int gpz_time_kernel(gpz_ctx *ctx, int which, int reps, double *ms_per_launch);
 /* JSON text of the SpMV autotuner's measurements (ms per launch of every
  * candidate layout / kernel of the mixed CG) for the assembled system. */
 int gpz_tuning_report(gpz_ctx *ctx, char *buf, int64_t len);
+
+/* ---- allocation-free solve -------------------------------------------------
+ * No counterpart in the reference (its CG allocates its work vectors on every
+ * call).  Jacobi-preconditioned FP64 CG with the algorithm of gpz_solve's
+ * GPZ_SOLVER_CG / GPZ_PRECOND_JACOBI (Solvers/LinearSolvers/cg.h:29-132), zero
+ * initial guess, on a caller-owned full CSR matrix (TPZFYsmpMatrix layout)
+ * already on the device, for callers that may not allocate device memory
+ * while they solve (an application that has handed all of HBM to its own
+ * pool, or a loop that must not touch the allocator after start-up).
+ *
+ * It allocates nothing: its work vectors live in one fixed static device
+ * array sized for GPZ_NOALLOC_MAX_EQ equations (about 8.4 MB per device);
+ * larger systems return GPZ_E_TOO_LARGE.  The first call on a device looks the
+ * array up (cudaGetSymbolAddress with that device current), which may make the
+ * CUDA runtime load the library's device code: make that first call during
+ * start-up, before any stream capture.  Every call on a device shares the
+ * array, so calls must not overlap in time on one device (one after the
+ * other, from any thread or stream, is fine).
+ *
+ * stream: cudaStream_t of the current device (NULL = legacy default stream);
+ * d_ia[neq+1] (int64), d_ja[nnz] (int32), d_a[nnz], d_b[neq], d_x[neq]: device
+ * pointers; x is overwritten with the solution.  The call returns when the
+ * solve has finished on `stream`; iterations / resid (host, may be NULL)
+ * receive fNumIterations and the final ||r||/||b||.  Bad row pointers or
+ * columns, or a missing / zero diagonal, return GPZ_E_INVALID before the first
+ * iteration. */
+#define GPZ_NOALLOC_MAX_EQ 262144
+int gpz_cg_jacobi_noalloc(void *stream, int64_t neq, int64_t nnz, const int64_t *d_ia, const int32_t *d_ja,
+                          const double *d_a, const double *d_b, double *d_x, int64_t max_iter, double tol,
+                          int64_t *iterations, double *resid);
 
 #ifdef __cplusplus
 }

@@ -59,6 +59,7 @@ const char *gpz_get_error_string(int code) {
     case GPZ_E_DEVICE_CHECK: return "a device-side bounds or invariant check failed";
     case GPZ_E_NO_DEVICE: return "no CUDA device";
     case GPZ_E_BREAKDOWN: return "Krylov breakdown (non-positive curvature or non-finite residual)";
+    case GPZ_E_TOO_LARGE: return "system larger than GPZ_NOALLOC_MAX_EQ equations (fixed scratch of the allocation-free CG)";
     default: return "unknown status";
   }
 }
