@@ -96,6 +96,9 @@ struct SolverWork {
   DBuf<double> scal;           // device scalars (see gpz_solver.cu)
   DBuf<unsigned int> counter;  // last-block counters
   DBuf<int64_t> iscal;         // device integer scalars
+  DBuf<double> gm_v;           // GMRES Krylov basis [m+1][neq]
+  DBuf<double> gm_d;           // GMRES Hessenberg, rotations, y, scalars
+  DBuf<int64_t> gm_i;          // GMRES state words
   size_t nblk = 0;
 };
 

@@ -1132,6 +1132,267 @@ int pick_tpr32(int64_t nnz, int64_t n) {  // FP32 rows: coalescing first
   return 4;
 }
 
+// ---------------------------------------------------------------- GMRES
+// Restarted, left-preconditioned GMRES(m) of Solvers/LinearSolvers/gmres.h:68-168
+// (SIAM Templates p. 20): modified Gram-Schmidt Arnoldi, Givens rotations,
+// back-substitution Update (gmres.h:20-35).  The Krylov basis is kept
+// unnormalised: column j of V holds v_j / vscale[j], so that normalising a new
+// vector costs no extra pass; every consumer multiplies by vscale[j].
+//
+// One Arnoldi step i is 2 + (i + 1) kernels: w = A v_i; w = M w with
+// h(0,i) = w.v_0; then for k = 0..i: w -= h(k,i) v_k fused with the next dot
+// (h(k+1,i) = w.v_{k+1}, or ||w|| when k = i).  The CTA that finishes ||w||
+// also applies the rotations and decides convergence.  A whole restart cycle
+// is captured once as a CUDA graph; a device state word, written only by the
+// last CTA of a reduction or by a one-thread kernel, lets every later kernel
+// of a finished solve return at entry.
+enum { GM_STATE = 0, GM_J, GM_K, GM_UPD, GM_MAXIT, GM_ITERS, GM_SP64, GM_NI };
+enum { GMS_RUN = 0, GMS_CONV_PENDING = 1, GMS_CONV = 2, GMS_MAXIT_PENDING = 3, GMS_MAXIT = 4, GMS_BREAK = 5 };
+enum { GMD_NORMB = 0, GMD_RESID, GMD_TOL, GMD_NS };
+
+struct Gm {
+  double *V;       // [m+1][n], column j scaled by vscale[j]
+  double *H;       // [(m+1) x (m+1)], column-major, H(i,j) = H[j*(m+1)+i]
+  double *s, *cs, *sn, *vscale, *y;
+  double *d;       // GMD_* scalars
+  int64_t *is;     // GM_* integers
+  int m;
+  int64_t n;
+};
+
+__device__ __forceinline__ double &gm_h(const Gm &G, int i, int j) { return G.H[(size_t)j * (G.m + 1) + i]; }
+__device__ __forceinline__ bool gm_running(const Gm &G) { return G.is[GM_STATE] == GMS_RUN; }
+
+__device__ __forceinline__ void gm_gen_rot(double dx, double dy, double &c, double &sv) {  // GeneratePlaneRotation
+  if (dy == 0.0) {
+    c = 1.0;
+    sv = 0.0;
+  } else if (fabs(dy) > fabs(dx)) {
+    const double t = dx / dy;
+    sv = 1.0 / sqrt(1.0 + t * t);
+    c = t * sv;
+  } else {
+    const double t = dy / dx;
+    c = 1.0 / sqrt(1.0 + t * t);
+    sv = t * c;
+  }
+}
+__device__ __forceinline__ void gm_app_rot(double &dx, double &dy, double c, double sv) {  // ApplyPlaneRotation
+  const double t = c * dx + sv * dy;
+  dy = -sv * dx + c * dy;
+  dx = t;
+}
+
+// ||M b|| (the GMRES normb), ||b|| (for the reported true residual), x = 0 unless from_current
+__global__ void __launch_bounds__(kThreads) k_gm_init(const double *__restrict__ b, double *__restrict__ x, Prec M,
+                                                      int64_t nunits, int from_current, Gm G, double *normb_true,
+                                                      Red R) {
+  const int bs = M.block ? 3 : 1;
+  double mbb = 0.0, bb = 0.0;
+  for (int64_t u = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; u < nunits; u += (int64_t)gridDim.x * blockDim.x) {
+    double z[3];
+    apply_prec(M, b, u, z);
+    for (int k = 0; k < bs; k++) {
+      const int64_t i = u * bs + k;
+      mbb += z[k] * z[k];
+      bb += b[i] * b[i];
+      if (!from_current) x[i] = 0.0;
+    }
+  }
+  double v[2] = {mbb, bb}, tot[2];
+  if (grid_reduce<2>(v, R, tot) && threadIdx.x == 0) {
+    const double nb = sqrt(tot[0]);
+    G.d[GMD_NORMB] = nb == 0.0 ? 1.0 : nb;
+    const double nt = sqrt(tot[1]);
+    *normb_true = nt == 0.0 ? 1.0 : nt;
+  }
+}
+
+// t = b - A x into V[0] (restart residual, before the preconditioner)
+template <int TPR>
+__global__ void __launch_bounds__(kThreads) k_gm_resid_spmv(const int64_t *__restrict__ ia,
+                                                            const int32_t *__restrict__ ja,
+                                                            const double *__restrict__ a,
+                                                            const double *__restrict__ x,
+                                                            const double *__restrict__ b, int initial, Gm G) {
+  if (!initial) {
+    const int64_t st = G.is[GM_STATE];
+    if (G.is[GM_UPD] != 1 || (st != GMS_RUN && st != GMS_MAXIT_PENDING)) return;
+  }
+  GPZ_ROW_LOOP(TPR, G.n) {
+    const int64_t i = r0 + (threadIdx.x & 31) / TPR;
+    const bool valid = i < G.n;
+    const double s = row_dot64<TPR>(ia, ja, a, x, i, sub, valid);
+    if (sub == 0 && valid) G.V[i] = b[i] - s;
+  }
+}
+
+// r = M t in place in V[0], beta = ||r||; starts the next cycle or ends the solve
+__global__ void __launch_bounds__(kThreads) k_gm_resid_prec(Prec M, int64_t nunits, int initial, Gm G, Red R) {
+  if (!initial) {
+    const int64_t st = G.is[GM_STATE];
+    if (G.is[GM_UPD] != 1 || (st != GMS_RUN && st != GMS_MAXIT_PENDING)) return;
+  }
+  const int bs = M.block ? 3 : 1;
+  double rr = 0.0;
+  for (int64_t u = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; u < nunits; u += (int64_t)gridDim.x * blockDim.x) {
+    double z[3];
+    apply_prec(M, G.V, u, z);
+    for (int k = 0; k < bs; k++) {
+      G.V[u * bs + k] = z[k];
+      rr += z[k] * z[k];
+    }
+  }
+  double v[1] = {rr}, tot[1];
+  if (grid_reduce<1>(v, R, tot) && threadIdx.x == 0) {
+    const double beta = sqrt(tot[0]);
+    const double resid = beta / G.d[GMD_NORMB];
+    int64_t *is = G.is;
+    G.vscale[0] = beta > 0.0 ? 1.0 / beta : 0.0;
+    for (int k = 0; k <= G.m; k++) G.s[k] = 0.0;
+    G.s[0] = beta;
+    G.d[GMD_RESID] = resid;
+    is[GM_SP64] += 1;
+    is[GM_UPD] = 0;
+    if (!isfinite(resid)) {
+      is[GM_STATE] = GMS_BREAK;
+    } else if (initial) {
+      // gmres.h:97-103: already converged -> x += r, max_iter = 0
+      is[GM_STATE] = resid <= G.d[GMD_TOL] ? GMS_CONV : GMS_RUN;
+      if (is[GM_STATE] == GMS_CONV) is[GM_ITERS] = 0;
+      else if (is[GM_MAXIT] < 1) is[GM_STATE] = GMS_MAXIT;
+    } else if (resid < G.d[GMD_TOL]) {
+      is[GM_STATE] = GMS_CONV;
+      is[GM_ITERS] = is[GM_J];
+    } else if (is[GM_STATE] == GMS_MAXIT_PENDING) {
+      is[GM_STATE] = GMS_MAXIT;
+    }
+  }
+}
+
+// w = vscale[i] A V[i] into V[i+1]
+template <int TPR>
+__global__ void __launch_bounds__(kThreads) k_gm_spmv(const int64_t *__restrict__ ia, const int32_t *__restrict__ ja,
+                                                      const double *__restrict__ a, int i, Gm G) {
+  if (!gm_running(G)) return;
+  const double *vi = G.V + (size_t)i * G.n;
+  double *w = G.V + (size_t)(i + 1) * G.n;
+  const double sc = G.vscale[i];
+  GPZ_ROW_LOOP(TPR, G.n) {
+    const int64_t r = r0 + (threadIdx.x & 31) / TPR;
+    const bool valid = r < G.n;
+    const double s = row_dot64<TPR>(ia, ja, a, vi, r, sub, valid);
+    if (sub == 0 && valid) w[r] = sc * s;
+  }
+}
+
+// w = M w, h(0,i) = w . v_0
+__global__ void __launch_bounds__(kThreads) k_gm_prec_dot(Prec M, int64_t nunits, int i, Gm G, Red R) {
+  if (!gm_running(G)) return;
+  double *w = G.V + (size_t)(i + 1) * G.n;
+  const double *v0 = G.V;
+  const int bs = M.block ? 3 : 1;
+  double d = 0.0;
+  for (int64_t u = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; u < nunits; u += (int64_t)gridDim.x * blockDim.x) {
+    double z[3];
+    apply_prec(M, w, u, z);
+    for (int k = 0; k < bs; k++) {
+      const int64_t q = u * bs + k;
+      w[q] = z[k];
+      d += z[k] * v0[q];
+    }
+  }
+  double v[1] = {d}, tot[1];
+  if (grid_reduce<1>(v, R, tot) && threadIdx.x == 0) gm_h(G, 0, i) = tot[0] * G.vscale[0];
+}
+
+// w -= h(k,i) v_k, then h(k+1,i) = w . v_{k+1} (k < i) or, for k = i, the step's end:
+// h(i+1,i) = ||w||, rotations, residual estimate |s(i+1)| / normb, convergence.
+__global__ void __launch_bounds__(kThreads) k_gm_mgs(int i, int k, Gm G, Red R) {
+  if (!gm_running(G)) return;
+  double *w = G.V + (size_t)(i + 1) * G.n;
+  const double *vk = G.V + (size_t)k * G.n;
+  const double c = gm_h(G, k, i) * G.vscale[k];
+  const bool last_k = k == i;
+  const double *vn = last_k ? w : G.V + (size_t)(k + 1) * G.n;
+  double d = 0.0;
+  for (int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; q < G.n; q += (int64_t)gridDim.x * blockDim.x) {
+    const double wq = w[q] - c * vk[q];
+    w[q] = wq;
+    d += wq * (last_k ? wq : vn[q]);
+  }
+  double v[1] = {d}, tot[1];
+  if (!grid_reduce<1>(v, R, tot) || threadIdx.x != 0) return;
+  if (!last_k) {
+    gm_h(G, k + 1, i) = tot[0] * G.vscale[k + 1];
+    return;
+  }
+  int64_t *is = G.is;
+  const double hn = sqrt(tot[0]);
+  gm_h(G, i + 1, i) = hn;
+  G.vscale[i + 1] = hn > 0.0 ? 1.0 / hn : 0.0;
+  for (int kk = 0; kk < i; kk++) gm_app_rot(gm_h(G, kk, i), gm_h(G, kk + 1, i), G.cs[kk], G.sn[kk]);
+  gm_gen_rot(gm_h(G, i, i), gm_h(G, i + 1, i), G.cs[i], G.sn[i]);
+  gm_app_rot(gm_h(G, i, i), gm_h(G, i + 1, i), G.cs[i], G.sn[i]);
+  gm_app_rot(G.s[i], G.s[i + 1], G.cs[i], G.sn[i]);
+  const double resid = fabs(G.s[i + 1]) / G.d[GMD_NORMB];
+  G.d[GMD_RESID] = resid;
+  is[GM_SP64] += 1;
+  if (!isfinite(resid)) {
+    is[GM_STATE] = GMS_BREAK;
+  } else if (resid < G.d[GMD_TOL]) {
+    is[GM_STATE] = GMS_CONV_PENDING;
+    is[GM_K] = i;
+    is[GM_ITERS] = is[GM_J];
+  } else {
+    is[GM_J] += 1;
+    if (is[GM_J] > is[GM_MAXIT]) {
+      is[GM_STATE] = GMS_MAXIT_PENDING;
+      is[GM_K] = i;
+    } else if (i == G.m - 1) {
+      is[GM_K] = i;
+    }
+  }
+}
+
+// Update (gmres.h:20-35): y = H(0:k,0:k)^-1 s(0:k), premultiplied by vscale;
+// one thread.  Also arms (GM_UPD = 1) or disarms the x update that follows.
+__global__ void k_gm_solve_y(Gm G) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  int64_t *is = G.is;
+  const int64_t st = is[GM_STATE];
+  if (st != GMS_RUN && st != GMS_CONV_PENDING && st != GMS_MAXIT_PENDING) {
+    is[GM_UPD] = 0;
+    return;
+  }
+  const int k = (int)is[GM_K];
+  for (int j = 0; j <= k; j++) G.y[j] = G.s[j];
+  for (int i = k; i >= 0; i--) {
+    G.y[i] /= gm_h(G, i, i);
+    for (int j = i - 1; j >= 0; j--) G.y[j] -= gm_h(G, j, i) * G.y[i];
+  }
+  for (int j = 0; j <= k; j++) G.y[j] *= G.vscale[j];
+  is[GM_UPD] = 1;
+  if (st == GMS_CONV_PENDING) is[GM_STATE] = GMS_CONV;
+}
+
+// x += sum_{j<=k} y_j v_j
+__global__ void __launch_bounds__(kThreads) k_gm_update_x(double *__restrict__ x, Gm G) {
+  if (G.is[GM_UPD] != 1) return;
+  const int k = (int)G.is[GM_K];
+  for (int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; q < G.n; q += (int64_t)gridDim.x * blockDim.x) {
+    double acc = x[q];
+    for (int j = 0; j <= k; j++) acc += G.y[j] * G.V[(size_t)j * G.n + q];
+    x[q] = acc;
+  }
+}
+
+// x += r (gmres.h:99-100) when the initial residual already meets the tolerance
+__global__ void __launch_bounds__(kThreads) k_gm_add_r(double *__restrict__ x, Gm G) {
+  for (int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; q < G.n; q += (int64_t)gridDim.x * blockDim.x)
+    x[q] += G.V[q];
+}
+
 #define GPZ_TPR_SWITCH(tpr, KERNEL_CALL) \
   switch (tpr) {                         \
     case 32: { constexpr int T = 32; KERNEL_CALL; } break; \
@@ -1467,7 +1728,143 @@ void launch_iteration(Ctx &c, const Plan &P) {
 }
 
 
+// Restarted GMRES(m) with Jacobi / block-Jacobi (TPZMatrix::SolveGMRES ->
+// GMRES, Matrix/pzmatrix.cpp:767-800, Solvers/LinearSolvers/gmres.h:68-168).
+// The reported iteration count and residual are the reference's: fNumIterations
+// is the Arnoldi step count j as the template returns it, and fTol the
+// preconditioned residual estimate ||M r|| / ||M b||.  One difference, on the
+// not-converged path only: when max_iter ends a cycle early the update uses
+// the columns that were built (the template's Update(x, m-1, ...) would also
+// read columns left over from the previous cycle).
+int solve_gmres(Ctx &c, const gpz_solver_opts &o, gpz_solve_report &rep) {
+  GPZ_REQUIRE(o.precond == GPZ_PRECOND_JACOBI || o.precond == GPZ_PRECOND_BLOCK_JACOBI || o.precond == 0,
+              GPZ_E_INVALID, "preconditioner not available");
+  const int m = o.gmres_krylov > 0 ? o.gmres_krylov : 30;
+  GPZ_REQUIRE(m <= 512, GPZ_E_INVALID, "gmres_krylov must be in 1..512");
+  const bool block = o.precond == GPZ_PRECOND_BLOCK_JACOBI;
+  if (block && !c.have_bjinv) build_block_jacobi(c);
+  alloc_work(c, false);
+  SolverWork &w = c.sw;
+  cudaStream_t s = c.stream;
+  const int64_t n = c.neq;
+  const size_t nh = (size_t)(m + 1) * (m + 1), nv = (size_t)m + 2;
+  w.gm_v.alloc((size_t)(m + 1) * (size_t)std::max<int64_t>(n, 1));
+  w.gm_d.alloc(nh + 5 * nv + GMD_NS);
+  w.gm_i.alloc(GM_NI);
+  Gm G;
+  G.V = w.gm_v.p;
+  G.H = w.gm_d.p;
+  G.s = G.H + nh;
+  G.cs = G.s + nv;
+  G.sn = G.cs + nv;
+  G.vscale = G.sn + nv;
+  G.y = G.vscale + nv;
+  G.d = G.y + nv;
+  G.is = w.gm_i.p;
+  G.m = m;
+  G.n = n;
+  const Prec M{c.d_dinv.p, block ? c.d_bjinv.p : nullptr, block ? 1 : 0};
+  const int64_t nunits = block ? n / 3 : n;
+  const int tpr = pick_tpr(c.nnz, c.neq);
+  Red R = red_of(c);
+
+  cudaEvent_t ev0, ev1;
+  GPZ_CUDA_TRY(cudaEventCreate(&ev0));
+  GPZ_CUDA_TRY(cudaEventCreate(&ev1));
+  GPZ_CUDA_TRY(cudaEventRecord(ev0, s));
+  w.gm_d.zero(s);
+  double hd[GMD_NS] = {0};
+  hd[GMD_TOL] = o.tol;
+  int64_t hi[GM_NI] = {0};
+  hi[GM_J] = 1;
+  hi[GM_MAXIT] = o.max_iter;
+  hi[GM_ITERS] = o.max_iter;
+  GPZ_CUDA_TRY(cudaMemcpyAsync(G.d, hd, sizeof(hd), cudaMemcpyHostToDevice, s));
+  GPZ_CUDA_TRY(cudaMemcpyAsync(G.is, hi, sizeof(hi), cudaMemcpyHostToDevice, s));
+  double hs[S_NSCAL] = {0};
+  GPZ_CUDA_TRY(cudaMemcpyAsync(w.scal.p, hs, sizeof(hs), cudaMemcpyHostToDevice, s));
+
+  k_gm_init<<<wave(k_gm_init), kThreads, 0, s>>>(w.b.p, w.x.p, M, nunits, o.from_current, G, w.scal.p + S_NORMB, R);
+  GPZ_TPR_SWITCH(tpr, (k_gm_resid_spmv<T><<<wave(k_gm_resid_spmv<T>), kThreads, 0, s>>>(c.d_ia.p, c.d_ja.p, c.d_a.p,
+                                                                                         w.x.p, w.b.p, 1, G)));
+  k_gm_resid_prec<<<wave(k_gm_resid_prec), kThreads, 0, s>>>(M, nunits, 1, G, R);
+  c.launches += 3;
+  GPZ_CUDA_TRY(cudaGetLastError());
+  GPZ_CUDA_TRY(cudaMemcpyAsync(hi, G.is, sizeof(hi), cudaMemcpyDeviceToHost, s));
+  GPZ_CUDA_TRY(cudaStreamSynchronize(s));
+  if (hi[GM_STATE] == GMS_CONV) {
+    k_gm_add_r<<<wave(k_gm_add_r), kThreads, 0, s>>>(w.x.p, G);
+    c.launches++;
+  }
+
+  auto launch_cycle = [&]() {
+    for (int i = 0; i < m; i++) {
+      GPZ_TPR_SWITCH(tpr, (k_gm_spmv<T><<<wave(k_gm_spmv<T>), kThreads, 0, s>>>(c.d_ia.p, c.d_ja.p, c.d_a.p, i, G)));
+      k_gm_prec_dot<<<wave(k_gm_prec_dot), kThreads, 0, s>>>(M, nunits, i, G, R);
+      for (int k = 0; k <= i; k++) k_gm_mgs<<<wave(k_gm_mgs), kThreads, 0, s>>>(i, k, G, R);
+    }
+    k_gm_solve_y<<<1, 32, 0, s>>>(G);
+    k_gm_update_x<<<wave(k_gm_update_x), kThreads, 0, s>>>(w.x.p, G);
+    GPZ_TPR_SWITCH(tpr, (k_gm_resid_spmv<T><<<wave(k_gm_resid_spmv<T>), kThreads, 0, s>>>(c.d_ia.p, c.d_ja.p,
+                                                                                           c.d_a.p, w.x.p, w.b.p, 0,
+                                                                                           G)));
+    k_gm_resid_prec<<<wave(k_gm_resid_prec), kThreads, 0, s>>>(M, nunits, 0, G, R);
+  };
+  const int64_t per_cycle = (int64_t)m * (m + 1) / 2 + 2 * (int64_t)m + 4;
+  const bool use_graph = o.use_graph && m <= 64;
+  cudaGraphExec_t exec = nullptr;
+  if (hi[GM_STATE] == GMS_RUN && use_graph) {
+    cudaGraph_t g;
+    GPZ_CUDA_TRY(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+    launch_cycle();
+    GPZ_CUDA_TRY(cudaStreamEndCapture(s, &g));
+    GPZ_CUDA_TRY(cudaGraphInstantiate(&exec, g, 0));
+    GPZ_CUDA_TRY(cudaGraphDestroy(g));
+  }
+  // the device ends the solve by itself after max_iter Arnoldi steps; the
+  // host bound only guards against a state machine that never finishes
+  const int64_t max_cycles = o.max_iter / m + 3;
+  int64_t cycles = 0;
+  while (hi[GM_STATE] == GMS_RUN && cycles < max_cycles) {
+    if (exec) GPZ_CUDA_TRY(cudaGraphLaunch(exec, s));
+    else launch_cycle();
+    c.launches += per_cycle;
+    cycles++;
+    GPZ_CUDA_TRY(cudaGetLastError());
+    GPZ_CUDA_TRY(cudaMemcpyAsync(hi, G.is, sizeof(hi), cudaMemcpyDeviceToHost, s));
+    GPZ_CUDA_TRY(cudaStreamSynchronize(s));
+  }
+  if (exec) cudaGraphExecDestroy(exec);
+  GPZ_TPR_SWITCH(tpr, (k_true_resid<T><<<wave(k_true_resid<T>), kThreads, 0, s>>>(c.d_ia.p, c.d_ja.p, c.d_a.p, w.x.p,
+                                                                                   w.b.p, c.neq, R)));
+  c.launches++;
+  GPZ_CUDA_TRY(cudaEventRecord(ev1, s));
+  GPZ_CUDA_TRY(cudaMemcpyAsync(hs, w.scal.p, sizeof(hs), cudaMemcpyDeviceToHost, s));
+  GPZ_CUDA_TRY(cudaMemcpyAsync(hd, G.d, sizeof(hd), cudaMemcpyDeviceToHost, s));
+  GPZ_CUDA_TRY(cudaMemcpyAsync(hi, G.is, sizeof(hi), cudaMemcpyDeviceToHost, s));
+  GPZ_CUDA_TRY(cudaStreamSynchronize(s));
+  float ms = 0.0f;
+  cudaEventElapsedTime(&ms, ev0, ev1);
+  cudaEventDestroy(ev0);
+  cudaEventDestroy(ev1);
+  check_device_flag(c, "GMRES");
+  GPZ_REQUIRE(hi[GM_STATE] != GMS_RUN && hi[GM_STATE] != GMS_CONV_PENDING && hi[GM_STATE] != GMS_MAXIT_PENDING,
+              GPZ_E_DEVICE_CHECK, "GMRES state machine did not finish");
+  rep.iterations = hi[GM_ITERS];
+  rep.resid = hd[GMD_RESID];
+  rep.true_resid = std::sqrt(hs[S_TRUERR]) / hs[S_NORMB];
+  rep.seconds = ms * 1e-3;
+  rep.spmv_fp64 = hi[GM_SP64] + 1;
+  rep.spmv_fp32 = 0;
+  rep.reliable_updates = 0;
+  rep.restarts = cycles;
+  c.have_solution = true;
+  if (hi[GM_STATE] == GMS_BREAK) return GPZ_E_BREAKDOWN;
+  return hi[GM_STATE] == GMS_CONV ? GPZ_OK : GPZ_NOT_CONVERGED;
+}
+
 int solve(Ctx &c, const gpz_solver_opts &o, gpz_solve_report &rep) {
+  if (o.solver == GPZ_SOLVER_GMRES) return solve_gmres(c, o, rep);
   const bool mixed = o.solver == GPZ_SOLVER_MIXED_CG;
   GPZ_REQUIRE(o.solver == GPZ_SOLVER_CG || mixed, GPZ_E_INVALID, "solver kind not available");
   GPZ_REQUIRE(o.precond == GPZ_PRECOND_JACOBI || o.precond == GPZ_PRECOND_BLOCK_JACOBI || o.precond == 0,

@@ -213,3 +213,51 @@ def test_mixed_spmv_variants_converge(built, variant):
     ref = O.cg_jacobi(True, oia, oja, oa, of, 20000, 1e-12)
     assert np.linalg.norm(sol["x"] - ref["x"]) <= 1e-5 * np.linalg.norm(ref["x"])
     ctx.close()
+
+
+@pytest.mark.parametrize("m", [30, 5])
+@pytest.mark.parametrize("case", ["poisson2d_p2", "darcy2d_p2", "elast3d_p2"])
+def test_gmres_jacobi_matches_oracle(built, case, m):
+    """Restarted Jacobi-GMRES(m) (gmres.h:68-168) against the oracle's restatement: same
+    stopping rule on the preconditioned residual; solution within 1e-8, Arnoldi step count
+    within max(3, 10%)."""
+    g = _gpz()
+    mk_o, mk_g = built[case]
+    om, grid = mk_o(), mk_g()
+    ctx = g.Context(0)
+    ctx.upload_mesh(grid)
+    ctx.build_pattern(False)
+    ctx.assemble()
+    tol = 1e-10
+    sol = ctx.solve(solver=g.GPZ_SOLVER_GMRES, tol=tol, max_iter=20000, gmres_krylov=m)
+    oia, oja = om.pattern(False)
+    oa, of = om.assemble(False, oia, oja)
+    ref = O.gmres_jacobi(False, oia, oja, oa, of, m, 20000, tol)
+    assert sol["rc"] == 0 and ref["rc"] == 0 and sol["resid"] < tol
+    assert np.linalg.norm(sol["x"] - ref["x"]) <= 1e-8 * np.linalg.norm(ref["x"])
+    assert abs(sol["iterations"] - ref["iters"]) <= max(3, 0.1 * ref["iters"]), (sol["iterations"], ref["iters"])
+    ctx.close()
+
+
+def test_gmres_graph_eager_budget_and_block_jacobi(built):
+    g = _gpz()
+    om, grid = built["elast3d_p2"][0](), built["elast3d_p2"][1]()
+    ctx = g.Context(0)
+    ctx.upload_mesh(grid)
+    ctx.build_pattern(False)
+    ctx.assemble()
+    s1 = ctx.solve(solver=g.GPZ_SOLVER_GMRES, tol=1e-10, gmres_krylov=20, use_graph=True)
+    s2 = ctx.solve(solver=g.GPZ_SOLVER_GMRES, tol=1e-10, gmres_krylov=20, use_graph=False)
+    assert s1["rc"] == 0 and s1["iterations"] == s2["iterations"] and np.array_equal(s1["x"], s2["x"])
+    # iteration budget: not converged, fNumIterations = max_iter
+    s3 = ctx.solve(solver=g.GPZ_SOLVER_GMRES, tol=1e-10, gmres_krylov=20, max_iter=7)
+    assert s3["rc"] == 1 and s3["iterations"] == 7 and s3["resid"] > 1e-10
+    # connect-block Jacobi: converges to the same solution, in fewer steps than point Jacobi
+    s4 = ctx.solve(solver=g.GPZ_SOLVER_GMRES, precond=g.GPZ_PRECOND_BLOCK_JACOBI, tol=1e-10, gmres_krylov=20)
+    assert s4["rc"] == 0
+    oia, oja = om.pattern(False)
+    oa, of = om.assemble(False, oia, oja)
+    ref = O.cg_jacobi(False, oia, oja, oa, of, 20000, 1e-12)
+    for s in (s1, s4):
+        assert np.linalg.norm(s["x"] - ref["x"]) <= 1e-8 * np.linalg.norm(ref["x"])
+    ctx.close()

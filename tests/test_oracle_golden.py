@@ -177,3 +177,19 @@ def test_shape_derivatives_match_finite_differences():
         e[d] = h
         fd = (O.shape(O.T_CUBE, ids, orders, x + e)[0] - O.shape(O.T_CUBE, ids, orders, x - e)[0]) / (2 * h)
         assert np.allclose(fd, dphi[d], atol=1e-7)
+
+
+@pytest.mark.parametrize("m", [30, 5])
+def test_oracle_gmres_matches_cg_solution(m):
+    """Restarted Jacobi-GMRES(m) (gmres.h) converges to the CG solution; a small m restarts many times."""
+    E = np.exp(np.random.default_rng(7).standard_normal(27))
+    om = O.elasticity3d(3, 2, E=E)
+    ia, ja = om.pattern(False)
+    a, f = om.assemble(False, ia, ja)
+    cg = O.cg_jacobi(False, ia, ja, a, f, 20000, 1e-12)
+    g = O.gmres_jacobi(False, ia, ja, a, f, m, 20000, 1e-10)
+    assert g["rc"] == 0 and g["resid"] < 1e-10 and g["iters"] > m
+    assert np.linalg.norm(g["x"] - cg["x"]) <= 1e-8 * np.linalg.norm(cg["x"])
+    # the iteration budget is honoured and reported as the reference does
+    g2 = O.gmres_jacobi(False, ia, ja, a, f, m, 7, 1e-10)
+    assert g2["rc"] == 1 and g2["iters"] == 7
