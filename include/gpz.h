@@ -212,6 +212,43 @@ int gpz_time_kernel(gpz_ctx *ctx, int which, int reps, double *ms_per_launch);
  * candidate layout / kernel of the mixed CG) for the assembled system. */
 int gpz_tuning_report(gpz_ctx *ctx, char *buf, int64_t len);
 
+/* ---- coefficient update -------------------------------------------------
+ * Replace the per-element coefficients (el_coef of gpz_mesh_desc) of the
+ * uploaded mesh, keeping its numbering and pattern: the reference's loop of
+ * re-assembling the same TPZCompMesh with new material data.  The matrix must
+ * be assembled again afterwards. */
+int gpz_mesh_set_coef(gpz_ctx *ctx, const double *el_coef);
+
+/* ---- learned preconditioner ----------------------------------------------
+ * No counterpart in the reference.  A symmetric positive definite
+ * preconditioner M r = S (u + m .* sum_e Q_e^T F_e F_e^T Q_e (m .* u)),
+ * u = S r, S = diag(A)^-1/2, m = 0 on penalty-Dirichlet equations, whose
+ * per-element factors F_e (equations x rank) come from an element-to-node
+ * message-passing network over log(el_coef) (3 layers, 32 channels), used by
+ * GPZ_SOLVER_LEARNED_FCG (flexible CG; an iteration whose correction is not a
+ * descent direction uses Jacobi).  The network is trained on the GPU on
+ * residual / error pairs of the Jacobi-PCG iterates of assembled systems.
+ * Needs one element type and one equation count for all volume elements. */
+/* Build the element incidence of the uploaded mesh and random initial
+ * parameters (rank 1..8 columns per element factor; seed of the init). */
+int gpz_learned_init(gpz_ctx *ctx, int rank, uint64_t seed);
+int gpz_learned_num_params(gpz_ctx *ctx, int64_t *n);
+int gpz_learned_get_params(gpz_ctx *ctx, float *out, int64_t n);
+int gpz_learned_set_params(gpz_ctx *ctx, const float *in, int64_t n);
+/* Training pairs of the assembled system: Jacobi-PCG to `tol` gives x*, an
+ * identical second run samples npairs (r_k, x* - x_k) spread over its
+ * iterations; cg_iterations receives the Jacobi-PCG iteration count. */
+int gpz_learned_collect(gpz_ctx *ctx, int npairs, double tol, int64_t max_iter, int64_t *cg_iterations);
+/* Training pairs given by the caller: r[npairs][neq], e[npairs][neq] (host). */
+int gpz_learned_set_pairs(gpz_ctx *ctx, int npairs, const double *r, const double *e);
+/* Loss mean_j (M r_j - e_j)^T A (M r_j - e_j) / e_j^T A e_j over the
+ * non-Dirichlet equations, and (grad != NULL) its gradient w.r.t. the n
+ * parameters. */
+int gpz_learned_loss_grad(gpz_ctx *ctx, double *loss, float *grad, int64_t n);
+/* `steps` Adam steps (learning rate lr) on the current pairs; the losses
+ * before the first and the last step. */
+int gpz_learned_train(gpz_ctx *ctx, int steps, double lr, double *loss_first, double *loss_last);
+
 /* ---- allocation-free solve -------------------------------------------------
  * No counterpart in the reference (its CG allocates its work vectors on every
  * call).  Jacobi-preconditioned FP64 CG with the algorithm of gpz_solve's

@@ -16,9 +16,6 @@ Ctx::~Ctx() {
 
 using namespace gpz;
 
-struct gpz_ctx {
-  Ctx c;
-};
 
 namespace {
 
@@ -165,6 +162,17 @@ int gpz_mesh_upload(gpz_ctx *ctx, const gpz_mesh_desc *d) {
     build_buckets(c, *d);
     c.have_mesh = true;
     c.have_pattern = c.have_matrix = c.have_solution = c.have_a32 = c.have_bjinv = false;
+    return GPZ_OK;
+  });
+}
+
+int gpz_mesh_set_coef(gpz_ctx *ctx, const double *el_coef) {
+  return guarded(ctx, [&](Ctx &c) {
+    GPZ_REQUIRE(c.have_mesh, GPZ_E_NOT_READY, "no mesh");
+    GPZ_REQUIRE(el_coef, GPZ_E_INVALID, "null coefficients");
+    c.d_coef.upload(el_coef, c.nel, c.stream);
+    c.have_matrix = c.have_solution = false;
+    GPZ_CUDA_TRY(cudaStreamSynchronize(c.stream));
     return GPZ_OK;
   });
 }

@@ -102,6 +102,34 @@ struct SolverWork {
   size_t nblk = 0;
 };
 
+// ---------------------------------------------------------------- learned preconditioner
+// Element-to-node message-passing network that produces per-element factors
+// F_e of the preconditioner in gpz_learned.cuh (gpz_learned.cu).
+struct Learned {
+  bool ready = false;                        // mesh incidence built
+  bool have_params = false;
+  int R = 4, NS = 0, nsides = 0;
+  int64_t E = 0, nconn = 0, nparams = 0, adam_t = 0;
+  std::vector<int64_t> h_vel;                // volume element -> element index
+  DBuf<int32_t> ec;                          // [E][nsides] connects of each volume element
+  DBuf<int64_t> ce_ptr;                      // connect -> volume elements
+  DBuf<int32_t> ce_idx;
+  DBuf<int32_t> dest;                        // [E][NS]
+  DBuf<int64_t> ne_ptr;                      // equation -> (element, local)
+  DBuf<int32_t> ne_idx;
+  DBuf<double> mask, dsq;                    // [neq]
+  DBuf<float> mdsq;                          // [neq] mask * dsq
+  DBuf<float> feat;                          // [E] log coefficient
+  DBuf<float> params, grad, m1, m2;
+  DBuf<float> F;                             // [E][NS][R]
+  DBuf<float> t;                             // [E][R]
+  DBuf<float> act, back, partial;            // activations, backward buffers, outer-product partials
+  DBuf<double> red;                          // dot-product partials
+  int npairs = 0;
+  DBuf<double> pr, pe, pz, pw, paw, pg;      // [P][neq] residuals, errors, M r, masked error of M r, A w, dL/dz
+  DBuf<double> pscal;                        // [P][2] e^T A e, loss
+};
+
 // ---------------------------------------------------------------- the context
 struct Ctx {
   int device = 0;
@@ -170,6 +198,7 @@ struct Ctx {
 
   SolverWork sw;
   bool have_solution = false;
+  Learned ln;
 
   ~Ctx();
 };
@@ -187,6 +216,10 @@ void build_block_jacobi(Ctx &c);
 // solver.cu
 void spmv_device(Ctx &c, const double *x, double *y, double alpha, double beta, const double *yin);
 int solve(Ctx &c, const gpz_solver_opts &o, gpz_solve_report &rep);
+int collect_cg_pairs(Ctx &c, int npairs, double tol, int64_t max_iter, double *R, double *X, double *xstar,
+                     int64_t *iters);
+// learned.cu
+void learned_prepare(Ctx &c);                // features, scaling and factors F for the assembled system
 // scan.cu
 void exclusive_scan_i64(const int64_t *in, int64_t *out, int64_t n, cudaStream_t s, Ctx &c);
 void check_device_flag(Ctx &c, const char *where);
@@ -199,3 +232,8 @@ inline int grid_for(int64_t n, int threads) {
 }
 
 }  // namespace gpz
+
+// the opaque handle of include/gpz.h
+struct gpz_ctx {
+  gpz::Ctx c;
+};

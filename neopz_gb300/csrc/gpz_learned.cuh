@@ -1,0 +1,71 @@
+// Device view of the learned preconditioner shared by the network kernels
+// (gpz_learned.cu) and the flexible CG (gpz_solver.cu).
+//
+// The preconditioner is linear and symmetric positive definite in the
+// residual by construction; what is learned is how it depends on the
+// coefficient field:
+//
+//   M r = S (u + m .* sum_e Q_e^T F_e F_e^T Q_e (m .* u)),   u = S r,
+//
+// with S = diag(a_ii)^-1/2 (the symmetric Jacobi scaling), m the mask that is 0
+// on penalty-Dirichlet equations (where Jacobi is already exact), Q_e the
+// gather of element e's equations (its destination indices, in the order of
+// TPZElementMatrix::ComputeDestinationIndices, Mesh/pzelmat.cpp:37-96) and
+// F_e an NS x R factor per element.  The factors come from an element-to-node
+// message-passing network over the element coefficients (see gpz_learned.cu),
+// evaluated once per solve; each application costs one gather, 2 NS R
+// multiply-adds per element and one gather back per equation.
+#pragma once
+#include <cstdint>
+
+namespace gpz {
+
+struct LnView {
+  const float *F;         // [E][NS][R] element factors
+  const int32_t *dest;    // [E][NS] element equations
+  const int64_t *ne_ptr;  // [neq+1] equation -> (element, local) incidences
+  const int32_t *ne_idx;  // e * NS + local
+  const float *mdsq;      // [neq] m_i S_i (0 on penalty-Dirichlet equations)
+  const double *dinv;     // [neq] 1 / a_ii
+  float *t;               // [E][R] F_e^T Q_e (m .* u)
+  int64_t E, n;
+  int NS, R;
+};
+
+// The correction runs in FP32 (this part's FP64 rate is a small fraction of
+// its FP32 rate); only the Jacobi part z = r / a_ii stays FP64.
+// One thread per (element, column k): t_e[k] = sum_loc F_e[loc][k] m S r[dest].
+template <class T>
+__device__ __forceinline__ void ln_elem_t(const LnView &L, const T *__restrict__ r, int64_t idx) {
+  const int32_t e = (int32_t)idx / L.R;  // E * R < 2^31 (checked at set-up)
+  const int k = (int)idx - e * L.R;
+  const int32_t *d = L.dest + e * L.NS;
+  const float *f = L.F + (size_t)e * L.NS * L.R + k;
+  float acc = 0.f;
+  for (int loc = 0; loc < L.NS; loc++) {
+    const int32_t q = d[loc];
+    acc += f[(size_t)loc * L.R] * (L.mdsq[q] * (float)r[q]);
+  }
+  L.t[idx] = acc;
+}
+
+// correction at equation i: m_i S_i sum_{(e,loc) at i} F_e[loc] . t_e
+__device__ __forceinline__ float ln_node_corr(const LnView &L, int64_t i) {
+  float c = 0.f;
+  for (int64_t k = L.ne_ptr[i]; k < L.ne_ptr[i + 1]; k++) {
+    const int32_t el = L.ne_idx[k];
+    const int32_t e = el / L.NS;
+    const float *f = L.F + (size_t)el * L.R;
+    const float *t = L.t + (size_t)e * L.R;
+    for (int j = 0; j < L.R; j++) c += f[j] * t[j];
+  }
+  return L.mdsq[i] * c;
+}
+
+// z_i = r_i / a_ii + correction
+template <class T>
+__device__ __forceinline__ double ln_node_z(const LnView &L, const T *__restrict__ r, int64_t i) {
+  return L.dinv[i] * (double)r[i] + (double)ln_node_corr(L, i);
+}
+
+}  // namespace gpz

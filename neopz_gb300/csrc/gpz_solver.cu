@@ -21,8 +21,11 @@
 #include <vector>
 
 #include "gpz_internal.h"
+#include "gpz_learned.cuh"
 
 namespace gpz {
+
+LnView learned_view(Ctx &c);
 
 namespace {
 
@@ -1393,6 +1396,93 @@ __global__ void __launch_bounds__(kThreads) k_gm_add_r(double *__restrict__ x, G
     x[q] += G.V[q];
 }
 
+// ---------------------------------------------------------------- flexible CG with the learned preconditioner
+// Notay's flexible CG (one stored direction): alpha = rho / (p.q),
+// beta = -(z_new . q) / (p.q), rho = z_new . r_new, with z = M r from
+// gpz_learned.cuh.  When the learned correction is not a descent direction
+// (z.r <= 0 or not finite) that iteration uses Jacobi (z = r / diag) instead;
+// I_RESTART carries that choice to the direction update and I_NRESTART counts it.
+__global__ void __launch_bounds__(kThreads) k_fcg_update(double *__restrict__ x, double *__restrict__ r,
+                                                         float *__restrict__ r32, const double *__restrict__ p,
+                                                         const double *__restrict__ q, int64_t n, Red R) {
+  if (!active(R.iscal)) return;
+  const double alpha = R.scal[S_ALPHA];
+  double rr = 0.0;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    x[i] += alpha * p[i];
+    const double ri = r[i] - alpha * q[i];
+    r[i] = ri;
+    r32[i] = (float)ri;
+    rr += ri * ri;
+  }
+  double v[1] = {rr}, tot[1];
+  if (grid_reduce<1>(v, R, tot) && threadIdx.x == 0) {
+    double *s = R.scal;
+    int64_t *is = R.iscal;
+    const double resid = sqrt(tot[0]) / s[S_NORMB];
+    s[S_RR] = tot[0];
+    s[S_RESID] = resid;
+    is[I_IT] += 1;
+    if (!(s[S_PQ] > 0.0) || !isfinite(resid)) {
+      is[I_BREAK] = 1;
+      is[I_CONV] = 2;
+    } else if (resid <= s[S_TOL]) {
+      is[I_CONV] = 1;
+    }
+  }
+}
+
+template <class T>
+__global__ void __launch_bounds__(kThreads) k_fcg_t(LnView L, const T *__restrict__ r, Red R) {
+  if (!active(R.iscal)) return;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < L.E * L.R; i += (int64_t)gridDim.x * blockDim.x)
+    ln_elem_t<T>(L, r, i);
+}
+
+__global__ void __launch_bounds__(kThreads) k_fcg_z(LnView L, const double *__restrict__ r,
+                                                    const double *__restrict__ q, const double *__restrict__ dinv,
+                                                    double *__restrict__ z, Red R) {
+  if (!active(R.iscal)) return;
+  const bool first = R.iscal[I_IT] == 0;
+  double zr = 0.0, zq = 0.0, jr = 0.0, jq = 0.0;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < L.n; i += (int64_t)gridDim.x * blockDim.x) {
+    const double zi = ln_node_z<double>(L, r, i);
+    const double ri = r[i];
+    const double ji = dinv[i] * ri;
+    z[i] = zi;
+    zr += zi * ri;
+    jr += ji * ri;
+    if (!first) {
+      const double qi = q[i];
+      zq += zi * qi;
+      jq += ji * qi;
+    }
+  }
+  double v[4] = {zr, zq, jr, jq}, tot[4];
+  if (grid_reduce<4>(v, R, tot) && threadIdx.x == 0) {
+    double *s = R.scal;
+    int64_t *is = R.iscal;
+    const bool ok = tot[0] > 0.0 && isfinite(tot[0]) && isfinite(tot[1]);
+    is[I_RESTART] = ok ? 0 : 1;
+    if (!ok) is[I_NRESTART] += 1;
+    s[S_RHO] = ok ? tot[0] : tot[2];
+    s[S_BETA] = first ? 0.0 : -(ok ? tot[1] : tot[3]) / s[S_PQ];
+  }
+}
+
+__global__ void __launch_bounds__(kThreads) k_fcg_p(const double *__restrict__ z, const double *__restrict__ r,
+                                                    const double *__restrict__ dinv, double *__restrict__ p, int64_t n,
+                                                    Red R) {
+  if (!active(R.iscal)) return;
+  const bool jac = R.iscal[I_RESTART] != 0;
+  const bool first = R.iscal[I_IT] == 0;
+  const double beta = R.scal[S_BETA];
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    const double zi = jac ? dinv[i] * r[i] : z[i];
+    p[i] = first ? zi : zi + beta * p[i];
+  }
+}
+
 #define GPZ_TPR_SWITCH(tpr, KERNEL_CALL) \
   switch (tpr) {                         \
     case 32: { constexpr int T = 32; KERNEL_CALL; } break; \
@@ -1863,8 +1953,182 @@ int solve_gmres(Ctx &c, const gpz_solver_opts &o, gpz_solve_report &rep) {
   return hi[GM_STATE] == GMS_CONV ? GPZ_OK : GPZ_NOT_CONVERGED;
 }
 
+// Flexible CG with the learned preconditioner (GPZ_SOLVER_LEARNED_FCG).  The
+// stopping rule is the reference's (recursive ||r||/||b|| <= tol, cg.h:100);
+// afterwards the true FP64 residual is recomputed and, if it misses the
+// tolerance, the solve restarts from the current x (at most three times).
+int solve_learned(Ctx &c, const gpz_solver_opts &o, gpz_solve_report &rep) {
+  learned_prepare(c);
+  alloc_work(c, false);
+  SolverWork &w = c.sw;
+  w.z.alloc(std::max<int64_t>(c.neq, 1));
+  w.r32.alloc(std::max<int64_t>(c.neq, 1));
+  cudaStream_t s = c.stream;
+  const int tpr = pick_tpr(c.nnz, c.neq);
+  const LnView L = learned_view(c);
+  Red R = red_of(c);
+  const int batch = o.check_every > 0 ? o.check_every : 32;
+  cudaEvent_t ev0, ev1;
+  GPZ_CUDA_TRY(cudaEventCreate(&ev0));
+  GPZ_CUDA_TRY(cudaEventCreate(&ev1));
+  GPZ_CUDA_TRY(cudaEventRecord(ev0, s));
+  auto iteration = [&]() {
+    GPZ_TPR_SWITCH(tpr, (k_cg_spmv<T, false><<<wave(k_cg_spmv<T, false>), kThreads, 0, s>>>(
+                            c.d_ia.p, c.d_ja.p, c.d_a.p, nullptr, w.p.p, nullptr, w.q.p, c.neq, R)));
+    k_fcg_update<<<wave(k_fcg_update), kThreads, 0, s>>>(w.x.p, w.r.p, w.r32.p, w.p.p, w.q.p, c.neq, R);
+    k_fcg_t<float><<<wave(k_fcg_t<float>), kThreads, 0, s>>>(L, w.r32.p, R);
+    k_fcg_z<<<wave(k_fcg_z), kThreads, 0, s>>>(L, w.r.p, w.q.p, c.d_dinv.p, w.z.p, R);
+    k_fcg_p<<<wave(k_fcg_p), kThreads, 0, s>>>(w.z.p, w.r.p, c.d_dinv.p, w.p.p, c.neq, R);
+    c.launches += 5;
+  };
+  cudaGraphExec_t exec = nullptr;
+  int64_t total_it = 0, nfallback = 0, hstate[I_NISCAL] = {0};
+  double hs[S_NSCAL] = {0};
+  int rc = GPZ_NOT_CONVERGED;
+  for (int pass = 0; pass < 4; pass++) {
+    for (int k = 0; k < S_NSCAL; k++) hs[k] = 0.0;
+    hs[S_TOL] = o.tol;
+    int64_t hi[I_NISCAL] = {0};
+    hi[I_MAXIT] = o.max_iter - total_it;
+    GPZ_CUDA_TRY(cudaMemcpyAsync(w.scal.p, hs, sizeof(hs), cudaMemcpyHostToDevice, s));
+    GPZ_CUDA_TRY(cudaMemcpyAsync(w.iscal.p, hi, sizeof(hi), cudaMemcpyHostToDevice, s));
+    const int from_current = pass > 0 ? 1 : o.from_current;
+    GPZ_TPR_SWITCH(tpr, (k_cg_init<T><<<wave(k_cg_init<T>), kThreads, 0, s>>>(c.d_ia.p, c.d_ja.p, c.d_a.p, w.x.p,
+                                                                               w.b.p, w.r.p, c.neq, from_current, R)));
+    k_fcg_t<double><<<wave(k_fcg_t<double>), kThreads, 0, s>>>(L, w.r.p, R);
+    k_fcg_z<<<wave(k_fcg_z), kThreads, 0, s>>>(L, w.r.p, w.q.p, c.d_dinv.p, w.z.p, R);
+    k_fcg_p<<<wave(k_fcg_p), kThreads, 0, s>>>(w.z.p, w.r.p, c.d_dinv.p, w.p.p, c.neq, R);
+    c.launches += 4;
+    GPZ_CUDA_TRY(cudaGetLastError());
+    if (o.use_graph && !exec) {
+      cudaGraph_t g;
+      GPZ_CUDA_TRY(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+      const int64_t l0 = c.launches;
+      for (int i = 0; i < batch; i++) iteration();
+      GPZ_CUDA_TRY(cudaStreamEndCapture(s, &g));
+      c.launches = l0;
+      GPZ_CUDA_TRY(cudaGraphInstantiate(&exec, g, 0));
+      GPZ_CUDA_TRY(cudaGraphDestroy(g));
+    }
+    for (;;) {
+      GPZ_CUDA_TRY(cudaMemcpyAsync(hstate, w.iscal.p, sizeof(hstate), cudaMemcpyDeviceToHost, s));
+      GPZ_CUDA_TRY(cudaStreamSynchronize(s));
+      if (hstate[I_CONV] != 0 || hstate[I_IT] >= hi[I_MAXIT]) break;
+      if (exec) {
+        GPZ_CUDA_TRY(cudaGraphLaunch(exec, s));
+        c.launches += (int64_t)batch * 5;
+      } else {
+        for (int i = 0; i < batch; i++) iteration();
+      }
+      GPZ_CUDA_TRY(cudaGetLastError());
+    }
+    GPZ_TPR_SWITCH(tpr, (k_true_resid<T><<<wave(k_true_resid<T>), kThreads, 0, s>>>(c.d_ia.p, c.d_ja.p, c.d_a.p,
+                                                                                     w.x.p, w.b.p, c.neq, R)));
+    c.launches++;
+    GPZ_CUDA_TRY(cudaMemcpyAsync(hs, w.scal.p, sizeof(hs), cudaMemcpyDeviceToHost, s));
+    GPZ_CUDA_TRY(cudaMemcpyAsync(hstate, w.iscal.p, sizeof(hstate), cudaMemcpyDeviceToHost, s));
+    GPZ_CUDA_TRY(cudaStreamSynchronize(s));
+    total_it += hstate[I_IT];
+    nfallback += hstate[I_NRESTART];
+    if (hstate[I_BREAK]) {
+      rc = GPZ_E_BREAKDOWN;
+      break;
+    }
+    const double true_resid = std::sqrt(hs[S_TRUERR]) / hs[S_NORMB];
+    if (hstate[I_CONV] == 1 && true_resid <= o.tol) {
+      rc = GPZ_OK;
+      break;
+    }
+    if (hstate[I_CONV] != 1 || total_it >= o.max_iter) break;  // budget spent
+  }
+  if (exec) cudaGraphExecDestroy(exec);
+  GPZ_CUDA_TRY(cudaEventRecord(ev1, s));
+  GPZ_CUDA_TRY(cudaStreamSynchronize(s));
+  float ms = 0.0f;
+  cudaEventElapsedTime(&ms, ev0, ev1);
+  cudaEventDestroy(ev0);
+  cudaEventDestroy(ev1);
+  check_device_flag(c, "learned flexible CG");
+  rep.iterations = total_it;
+  rep.resid = hs[S_RESID];
+  rep.true_resid = std::sqrt(hs[S_TRUERR]) / hs[S_NORMB];
+  rep.seconds = ms * 1e-3;
+  rep.spmv_fp64 = total_it + 1;
+  rep.spmv_fp32 = 0;
+  rep.reliable_updates = 0;
+  rep.restarts = nfallback;  // iterations that fell back to Jacobi
+  c.have_solution = true;
+  return rc;
+}
+
+// Training pairs from the Jacobi-PCG iterates of the assembled system
+// (cg.h:29-132): a first solve to `tol` gives x* and the iteration count K;
+// a second, identical (deterministic) run snapshots r_k and x_k at up to
+// `npairs` iterations spaced geometrically over 1..K.  Returns the number of pairs taken.
+int collect_cg_pairs(Ctx &c, int npairs, double tol, int64_t max_iter, double *R_out, double *X_out, double *xstar,
+                     int64_t *iters) {
+  alloc_work(c, false);
+  SolverWork &w = c.sw;
+  cudaStream_t s = c.stream;
+  GPZ_CUDA_TRY(cudaMemcpyAsync(w.b.p, c.d_f.p, c.neq * sizeof(double), cudaMemcpyDeviceToDevice, s));
+  gpz_solver_opts o{};
+  o.solver = GPZ_SOLVER_CG;
+  o.precond = GPZ_PRECOND_JACOBI;
+  o.max_iter = max_iter;
+  o.tol = tol;
+  o.check_every = 32;
+  o.use_graph = 1;
+  gpz_solve_report rep{};
+  solve(c, o, rep);
+  const int64_t K = rep.iterations;
+  *iters = K;
+  GPZ_CUDA_TRY(cudaMemcpyAsync(xstar, w.x.p, c.neq * sizeof(double), cudaMemcpyDeviceToDevice, s));
+  if (K < 1) return 0;
+  // geometric spacing over 1..K: the early, rough errors (which a local
+  // correction can remove) are as well represented as the late, smooth ones
+  std::vector<int64_t> snap;
+  for (int j = 0; j < npairs; j++) {
+    int64_t k = (int64_t)std::llround(std::pow((double)K, (double)(j + 1) / (double)(npairs + 1)));
+    k = std::max<int64_t>(1, std::min<int64_t>(K - 1, k));  // x_K = x*: no error left to learn from
+    if (k >= 1 && (snap.empty() || k > snap.back())) snap.push_back(k);
+  }
+  Plan P;
+  P.mixed = false;
+  P.block = false;
+  P.bsr = false;
+  P.tpr = pick_tpr(c.nnz, c.neq);
+  P.tpr32 = 0;
+  P.nunits = c.neq;
+  P.M = Prec{c.d_dinv.p, nullptr, 0};
+  double hs[S_NSCAL] = {0};
+  hs[S_TOL] = 0.0;  // run exactly K iterations
+  int64_t hi[I_NISCAL] = {0};
+  hi[I_MAXIT] = K;
+  GPZ_CUDA_TRY(cudaMemcpyAsync(w.scal.p, hs, sizeof(hs), cudaMemcpyHostToDevice, s));
+  GPZ_CUDA_TRY(cudaMemcpyAsync(w.iscal.p, hi, sizeof(hi), cudaMemcpyHostToDevice, s));
+  Red Rd = red_of(c);
+  GPZ_TPR_SWITCH(P.tpr, (k_cg_init<T><<<wave(k_cg_init<T>), kThreads, 0, s>>>(c.d_ia.p, c.d_ja.p, c.d_a.p, w.x.p,
+                                                                               w.b.p, w.r.p, c.neq, 0, Rd)));
+  k_precond_dot<<<wave(k_precond_dot), kThreads, 0, s>>>(w.r.p, P.M, P.nunits, Rd);
+  c.launches += 2;
+  size_t j = 0;
+  for (int64_t it = 1; it <= K && j < snap.size(); it++) {
+    launch_iteration(c, P);
+    if (it == snap[j]) {
+      GPZ_CUDA_TRY(cudaMemcpyAsync(R_out + j * c.neq, w.r.p, c.neq * sizeof(double), cudaMemcpyDeviceToDevice, s));
+      GPZ_CUDA_TRY(cudaMemcpyAsync(X_out + j * c.neq, w.x.p, c.neq * sizeof(double), cudaMemcpyDeviceToDevice, s));
+      j++;
+    }
+  }
+  GPZ_CUDA_TRY(cudaGetLastError());
+  GPZ_CUDA_TRY(cudaStreamSynchronize(s));
+  check_device_flag(c, "training pairs");
+  return (int)j;
+}
+
 int solve(Ctx &c, const gpz_solver_opts &o, gpz_solve_report &rep) {
   if (o.solver == GPZ_SOLVER_GMRES) return solve_gmres(c, o, rep);
+  if (o.solver == GPZ_SOLVER_LEARNED_FCG) return solve_learned(c, o, rep);
   const bool mixed = o.solver == GPZ_SOLVER_MIXED_CG;
   GPZ_REQUIRE(o.solver == GPZ_SOLVER_CG || mixed, GPZ_E_INVALID, "solver kind not available");
   GPZ_REQUIRE(o.precond == GPZ_PRECOND_JACOBI || o.precond == GPZ_PRECOND_BLOCK_JACOBI || o.precond == 0,

@@ -112,6 +112,15 @@ def lib():
         L.gpz_spmv.argtypes = [vp, dp, vp, dp, vp, vp]
         L.gpz_solve.argtypes = [vp, _P(gpz_solver_opts), vp, vp, _P(gpz_solve_report)]
         L.gpz_solution_download.argtypes = [vp, vp]
+        L.gpz_mesh_set_coef.argtypes = [vp, vp]
+        L.gpz_learned_init.argtypes = [vp, i32, ctypes.c_uint64]
+        L.gpz_learned_num_params.argtypes = [vp, _P(i64)]
+        L.gpz_learned_get_params.argtypes = [vp, vp, i64]
+        L.gpz_learned_set_params.argtypes = [vp, vp, i64]
+        L.gpz_learned_collect.argtypes = [vp, i32, dp, i64, _P(i64)]
+        L.gpz_learned_set_pairs.argtypes = [vp, i32, vp, vp]
+        L.gpz_learned_loss_grad.argtypes = [vp, _P(dp), vp, i64]
+        L.gpz_learned_train.argtypes = [vp, i32, dp, _P(dp), _P(dp)]
         _lib = L
     return _lib
 
@@ -133,6 +142,8 @@ def host():
             getattr(H, f).argtypes = [vp]
         H.gpzh_grid_dest.restype = ctypes.c_int
         H.gpzh_grid_dest.argtypes = [vp, i64, vp]
+        H.gpzh_grid_cells.restype = ctypes.c_int
+        H.gpzh_grid_cells.argtypes = [vp, vp]
         _host = H
     return _host
 
@@ -193,6 +204,19 @@ class Grid:
         self.nvol = H.gpzh_grid_nvol(self.h)
         self.desc = gpz_mesh_desc()
         H.gpzh_grid_desc(self.h, ctypes.byref(self.desc))
+
+    def cells(self):
+        """Grid cell of every element (-1 for boundary elements)."""
+        c = np.zeros(self.nel, np.int64)
+        host().gpzh_grid_cells(self.h, _p(c))
+        return c
+
+    def element_coef(self, cell_coef):
+        """Per-element coefficient array (the el_coef of the descriptor) from per-cell values."""
+        c = self.cells()
+        out = np.zeros(self.nel)
+        out[c >= 0] = np.asarray(cell_coef, np.float64)[c[c >= 0]]
+        return out
 
     def dest(self, e):
         d = np.zeros(64 * 3 * 27, np.int64)
@@ -291,6 +315,49 @@ class Context:
         self._check(lib().gpz_spmv(self.h, alpha, _p(x), beta, _p(yy), _p(z)))
         return z
 
+    def set_coef(self, grid, cell_coef):
+        """New per-cell coefficients for the uploaded mesh (same numbering and pattern)."""
+        self._coef_keep = np.ascontiguousarray(grid.element_coef(cell_coef))
+        self._check(lib().gpz_mesh_set_coef(self.h, _p(self._coef_keep)))
+
+    # ---- learned preconditioner
+    def learned_init(self, rank=4, seed=0):
+        self._check(lib().gpz_learned_init(self.h, rank, seed))
+        n = ctypes.c_int64()
+        self._check(lib().gpz_learned_num_params(self.h, ctypes.byref(n)))
+        self.learned_nparams = n.value
+        return n.value
+
+    def learned_params(self):
+        p = np.zeros(self.learned_nparams, np.float32)
+        self._check(lib().gpz_learned_get_params(self.h, _p(p), len(p)))
+        return p
+
+    def set_learned_params(self, p):
+        p = np.ascontiguousarray(p, np.float32)
+        self._check(lib().gpz_learned_set_params(self.h, _p(p), len(p)))
+
+    def learned_collect(self, npairs=16, tol=1e-12, max_iter=200000):
+        its = ctypes.c_int64()
+        self._check(lib().gpz_learned_collect(self.h, npairs, tol, max_iter, ctypes.byref(its)))
+        return its.value
+
+    def learned_set_pairs(self, R, E):
+        R = np.ascontiguousarray(R, np.float64)
+        E = np.ascontiguousarray(E, np.float64)
+        self._check(lib().gpz_learned_set_pairs(self.h, R.shape[0], _p(R), _p(E)))
+
+    def learned_loss_grad(self, want_grad=True):
+        loss = ctypes.c_double()
+        g = np.zeros(self.learned_nparams, np.float32) if want_grad else None
+        self._check(lib().gpz_learned_loss_grad(self.h, ctypes.byref(loss), _p(g), self.learned_nparams))
+        return loss.value, g
+
+    def learned_train(self, steps=8, lr=3e-3):
+        l0, l1 = ctypes.c_double(), ctypes.c_double()
+        self._check(lib().gpz_learned_train(self.h, steps, lr, ctypes.byref(l0), ctypes.byref(l1)))
+        return l0.value, l1.value
+
     def solve(self, solver=GPZ_SOLVER_CG, precond=GPZ_PRECOND_JACOBI, max_iter=20000, tol=1e-8, b=None,
               check_every=32, reliable_delta=1e-3, use_graph=True, x0=None, want_x=True, gmres_krylov=30,
               spmv_variant=-1):
@@ -338,6 +405,28 @@ def darcy(dim, n, p, perm, rhs=1.0):
     if dim == 2:
         return Grid(2, (n, n), (0, 0, 0), (1, 1, 0), [1, -1, -1, -1, -1], True, p, mats, bcs, elem_coef=perm)
     return Grid(3, (n, n, n), (0, 0, 0), (1, 1, 1), [1, -1, -1, -1, -1, -1, -1], True, p, mats, bcs, elem_coef=perm)
+
+
+def grf2d(n, sigma=1.5, ell=0.1, seed=0):
+    """exp(g) on the n x n cell centroids of the unit square, g a Gaussian random field with covariance
+    sigma^2 exp(-|x - y|^2 / (2 ell^2)), sampled by circulant embedding on the 2n x 2n periodic grid
+    (negative eigenvalues of the embedding clipped to zero) from a seeded PCG64 stream; cell index
+    ix + n iy, the element order of the grid."""
+    m, h = 2 * n, 1.0 / n
+    i = np.arange(m)
+    d = np.minimum(i, m - i) * h
+    c = sigma ** 2 * np.exp(-(d[:, None] ** 2 + d[None, :] ** 2) / (2 * ell ** 2))
+    lam = np.maximum(np.real(np.fft.fft2(c)), 0.0)
+    rng = np.random.default_rng(seed)
+    xi = rng.standard_normal((m, m)) + 1j * rng.standard_normal((m, m))
+    g = np.real(np.fft.fft2(np.sqrt(lam / (m * m)) * xi))[:n, :n]
+    return np.exp(g.reshape(-1))
+
+
+def darcy_grf(n, p=2, seed=0, sigma=1.5, ell=0.1):
+    """-div(k grad u) = 1 on the unit square, n x n quads of order p, k = grf2d(n, sigma, ell, seed), u = 0 on the
+    boundary (the learned-preconditioner workload)."""
+    return darcy(2, n, p, grf2d(n, sigma, ell, seed))
 
 
 def lognormal(ncells, sigma, seed):

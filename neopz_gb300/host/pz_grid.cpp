@@ -25,6 +25,7 @@ struct Grid {
   std::vector<int32_t> el_type, el_mat, el_order;
   std::vector<int64_t> el_nodes, el_conn;
   std::vector<double> el_coef;
+  std::vector<int64_t> el_cell;              // grid cell of each element (-1: boundary element)
   std::vector<int32_t> conn_order, block_size;
   std::vector<int64_t> block_pos;
   int64_t neq = 0;
@@ -287,6 +288,7 @@ void build_comp(Grid &g) {
       g.el_conn.push_back(ent2conn[ent]);
     }
     g.el_coef.push_back(s.elem_coef && e.cell >= 0 ? s.elem_coef[e.cell] : 0.0);
+    g.el_cell.push_back(e.cell >= 0 ? e.cell : -1);
   }
   // fix the padding: unused slots repeat connect 0 (never read)
   for (size_t e = 0; e < g.el_type.size(); e++)
@@ -352,6 +354,13 @@ int gpzh_grid_desc(void *grid, gpz_mesh_desc *d) {
 int64_t gpzh_grid_neq(void *grid) { return grid ? ((Grid *)grid)->neq : -1; }
 int64_t gpzh_grid_nel(void *grid) { return grid ? (int64_t)((Grid *)grid)->el_type.size() : -1; }
 int64_t gpzh_grid_nvol(void *grid) { return grid ? ((Grid *)grid)->nvol : -1; }
+
+int gpzh_grid_cells(void *grid, int64_t *cell) {
+  Grid *g = (Grid *)grid;
+  if (!g || !cell) return -1;
+  for (size_t e = 0; e < g->el_cell.size(); e++) cell[e] = g->el_cell[e];
+  return 0;
+}
 
 int gpzh_grid_dest(void *grid, int64_t e, int64_t *dest) {
   Grid *g = (Grid *)grid;

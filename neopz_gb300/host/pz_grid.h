@@ -42,6 +42,8 @@ int gpzh_grid_desc(void *grid, gpz_mesh_desc *out);
 int64_t gpzh_grid_neq(void *grid);
 int64_t gpzh_grid_nel(void *grid);
 int64_t gpzh_grid_nvol(void *grid);
+/* grid cell index of every element (-1 for boundary elements), nel entries */
+int gpzh_grid_cells(void *grid, int64_t *cell);
 /* destination equations of computational element e (TPZElementMatrix::ComputeDestinationIndices) */
 int gpzh_grid_dest(void *grid, int64_t e, int64_t *dest);
 

@@ -193,3 +193,30 @@ def test_oracle_gmres_matches_cg_solution(m):
     # the iteration budget is honoured and reported as the reference does
     g2 = O.gmres_jacobi(False, ia, ja, a, f, m, 7, 1e-10)
     assert g2["rc"] == 1 and g2["iters"] == 7
+
+
+def test_learned_oracle_gradient_matches_finite_differences():
+    """The numpy oracle of the learned preconditioner: analytic gradient = central differences (float64)."""
+    import scipy.sparse as sp
+    from oracle import learned_oracle as LO
+
+    rng = np.random.default_rng(3)
+    k = np.exp(rng.standard_normal(9))
+    om = O.darcy(2, 3, 2, k)
+    ia, ja = om.pattern(False)
+    a, f = om.assemble(False, ia, ja)
+    A = sp.csr_matrix((a, ja, ia), shape=(om.neq, om.neq))
+    mesh = LO.mesh_from_oracle(om, A, k)
+    R = 2
+    _, n = LO.layout(mesh.NS, R)
+    p = rng.standard_normal(n) * 0.3
+    Rs, Es = rng.standard_normal((2, om.neq)), rng.standard_normal((2, om.neq))
+    loss, g = LO.loss_and_grad(mesh, A, p, R, Rs, Es)
+    assert abs(loss - LO.loss_only(mesh, A, p, R, Rs, Es)) <= 1e-12 * abs(loss)
+    idx = rng.choice(n, 60, replace=False)
+    h = 1e-6
+    for i in idx:
+        e = np.zeros(n)
+        e[i] = h
+        fd = (LO.loss_only(mesh, A, p + e, R, Rs, Es) - LO.loss_only(mesh, A, p - e, R, Rs, Es)) / (2 * h)
+        assert abs(fd - g[i]) <= 1e-6 * max(1.0, np.abs(g).max()), (i, fd, g[i])
