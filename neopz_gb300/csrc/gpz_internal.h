@@ -128,6 +128,7 @@ struct Learned {
   int npairs = 0;
   DBuf<double> pr, pe, pz, pw, paw, pg;      // [P][neq] residuals, errors, M r, masked error of M r, A w, dL/dz
   DBuf<double> pscal;                        // [P][2] e^T A e, loss
+  DBuf<double> aterm;                        // [P] alpha-gradient terms
 };
 
 // ---------------------------------------------------------------- the context

@@ -15,7 +15,7 @@
 //     h_e  += tanh(W_l [h_e; nb_e] + b_l)
 //   F_e   = Wo h2_e + bo                       (NS x R factor, local equations x rank)
 // Parameters, in this order (floats): W0[H] b0[H] W1[H][2H] b1[H] W2[H][2H]
-// b2[H] Wo[NS*R][H] bo[NS*R].
+// b2[H] Wo[NS*R][H] bo[NS*R] a (the Jacobi part is scaled by exp(a)).
 //
 // Training data are residual / error pairs (r_k, e_k = x* - x_k) of the
 // Jacobi-PCG iterates of the system itself (collect_cg_pairs).  The loss is
@@ -41,7 +41,7 @@ constexpr int kMaxSeg = 64;
 constexpr int kRedBlocks = 256;
 
 struct Offs {
-  int64_t W0, b0, W1, b1, W2, b2, Wo, bo, total;
+  int64_t W0, b0, W1, b1, W2, b2, Wo, bo, a, total;
 };
 Offs offs_of(int NR) {
   Offs o;
@@ -53,7 +53,8 @@ Offs offs_of(int NR) {
   o.b2 = o.W2 + kH * 2 * kH;
   o.Wo = o.b2 + kH;
   o.bo = o.Wo + (int64_t)NR * kH;
-  o.total = o.bo + NR;
+  o.a = o.bo + NR;
+  o.total = o.a + 1;
   return o;
 }
 
@@ -328,7 +329,32 @@ __global__ void __launch_bounds__(kT) k_ln_apply_t(LnView L, const double *__res
   for (int64_t i = gthread(); i < L.E * L.R; i += nthread()) ln_elem_t<double>(L, r, i);
 }
 __global__ void __launch_bounds__(kT) k_ln_apply_z(LnView L, const double *__restrict__ r, double *__restrict__ z) {
-  for (int64_t i = gthread(); i < L.n; i += nthread()) z[i] = ln_node_z<double>(L, r, i);
+  const double alpha = exp((double)*L.loga);
+  for (int64_t i = gthread(); i < L.n; i += nthread()) z[i] = ln_node_z<double>(L, r, alpha, i);
+}
+// sum_i g_i (r_i / a_ii): the derivative of g^T z w.r.t. alpha, per pair
+__global__ void __launch_bounds__(kT) k_ln_dot3_part(int64_t n, const double *__restrict__ g,
+                                                     const double *__restrict__ dinv, const double *__restrict__ r,
+                                                     double *__restrict__ part) {
+  __shared__ double sh[kT / 32];
+  double s = 0.0;
+  for (int64_t i = gthread(); i < n; i += nthread()) s += g[i] * dinv[i] * r[i];
+  for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
+  if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = s;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double t = 0.0;
+    for (int w = 0; w < kT / 32; w++) t += sh[w];
+    part[blockIdx.x] = t;
+  }
+}
+// grad[a] = alpha * sum over pairs (terms[j] filled by k_ln_dot_fin)
+__global__ void k_ln_alpha_grad(int P, const double *__restrict__ terms, const float *__restrict__ params, int64_t oa,
+                                float *__restrict__ grad) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  double t = 0.0;
+  for (int j = 0; j < P; j++) t += terms[j];
+  grad[oa] = (float)(exp((double)params[oa]) * t);
 }
 __global__ void __launch_bounds__(kT) k_ln_masked_diff(int64_t n, const double *__restrict__ mask,
                                                        const double *__restrict__ a, const double *__restrict__ b,
@@ -512,6 +538,7 @@ LnView view_of(Ctx &c) {
   v.ne_idx = L.ne_idx.p;
   v.mdsq = L.mdsq.p;
   v.dinv = c.d_dinv.p;
+  v.loga = L.params.p + offs_of(L.NS * L.R).a;
   v.t = L.t.p;
   v.E = L.E;
   v.n = c.neq;
@@ -645,6 +672,7 @@ void alloc_pairs(Ctx &c, int P) {
   L.paw.alloc(sz);
   L.pg.alloc(sz);
   L.pscal.alloc((size_t)2 * P);
+  L.aterm.alloc(P);
   L.npairs = P;
 }
 
@@ -666,7 +694,17 @@ double loss_and_grad(Ctx &c, bool want_grad) {
                                                      L.pg.p + (size_t)j * n);
     c.launches += 3;
   }
-  if (want_grad) backward(c);
+  if (want_grad) {
+    backward(c);
+    const Offs o = offs_of(L.NS * L.R);
+    for (int j = 0; j < L.npairs; j++) {
+      k_ln_dot3_part<<<kRedBlocks, kT, 0, c.stream>>>(n, L.pg.p + (size_t)j * n, c.d_dinv.p, L.pr.p + (size_t)j * n,
+                                                      L.red.p);
+      k_ln_dot_fin<<<1, 32, 0, c.stream>>>(kRedBlocks, L.red.p, L.aterm.p + j);
+    }
+    k_ln_alpha_grad<<<1, 32, 0, c.stream>>>(L.npairs, L.aterm.p, L.params.p, o.a, L.grad.p);
+    c.launches += 2 * L.npairs + 1;
+  }
   std::vector<double> sc((size_t)2 * L.npairs);
   GPZ_CUDA_TRY(cudaMemcpyAsync(sc.data(), L.pscal.p, sc.size() * sizeof(double), cudaMemcpyDeviceToHost, c.stream));
   GPZ_CUDA_TRY(cudaStreamSynchronize(c.stream));

@@ -5,13 +5,14 @@
 // residual by construction; what is learned is how it depends on the
 // coefficient field:
 //
-//   M r = S (u + m .* sum_e Q_e^T F_e F_e^T Q_e (m .* u)),   u = S r,
+//   M r = S (alpha u + m .* sum_e Q_e^T F_e F_e^T Q_e (m .* u)),   u = S r,
 //
 // with S = diag(a_ii)^-1/2 (the symmetric Jacobi scaling), m the mask that is 0
 // on penalty-Dirichlet equations (where Jacobi is already exact), Q_e the
 // gather of element e's equations (its destination indices, in the order of
 // TPZElementMatrix::ComputeDestinationIndices, Mesh/pzelmat.cpp:37-96) and
-// F_e an NS x R factor per element.  The factors come from an element-to-node
+// F_e an NS x R factor per element; alpha = exp(a) > 0 a learned scale of the
+// Jacobi part.  The factors come from an element-to-node
 // message-passing network over the element coefficients (see gpz_learned.cu),
 // evaluated once per solve; each application costs one gather, 2 NS R
 // multiply-adds per element and one gather back per equation.
@@ -27,6 +28,7 @@ struct LnView {
   const int32_t *ne_idx;  // e * NS + local
   const float *mdsq;      // [neq] m_i S_i (0 on penalty-Dirichlet equations)
   const double *dinv;     // [neq] 1 / a_ii
+  const float *loga;      // log of the learned scale of the Jacobi part (one parameter)
   float *t;               // [E][R] F_e^T Q_e (m .* u)
   int64_t E, n;
   int NS, R;
@@ -62,10 +64,10 @@ __device__ __forceinline__ float ln_node_corr(const LnView &L, int64_t i) {
   return L.mdsq[i] * c;
 }
 
-// z_i = r_i / a_ii + correction
+// z_i = alpha r_i / a_ii + correction, alpha = exp(loga)
 template <class T>
-__device__ __forceinline__ double ln_node_z(const LnView &L, const T *__restrict__ r, int64_t i) {
-  return L.dinv[i] * (double)r[i] + (double)ln_node_corr(L, i);
+__device__ __forceinline__ double ln_node_z(const LnView &L, const T *__restrict__ r, double alpha, int64_t i) {
+  return alpha * L.dinv[i] * (double)r[i] + (double)ln_node_corr(L, i);
 }
 
 }  // namespace gpz

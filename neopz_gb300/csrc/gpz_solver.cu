@@ -1444,9 +1444,10 @@ __global__ void __launch_bounds__(kThreads) k_fcg_z(LnView L, const double *__re
                                                     double *__restrict__ z, Red R) {
   if (!active(R.iscal)) return;
   const bool first = R.iscal[I_IT] == 0;
+  const double alpha = exp((double)*L.loga);
   double zr = 0.0, zq = 0.0, jr = 0.0, jq = 0.0;
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < L.n; i += (int64_t)gridDim.x * blockDim.x) {
-    const double zi = ln_node_z<double>(L, r, i);
+    const double zi = ln_node_z<double>(L, r, alpha, i);
     const double ri = r[i];
     const double ji = dinv[i] * ri;
     z[i] = zi;

@@ -12,8 +12,8 @@ oracle's restatement of the reference's assembly.
 Network (H = 32): h0 = tanh(W0 x + b0), x = log(coefficient); for l = 1, 2:
 n_c = mean of h over the elements at connect c, nb_e = mean of n over the
 element's connects, h += tanh(W_l [h; nb] + b_l); F_e = Wo h2 + bo, reshaped
-NS x R.  M r = S (u + m * sum_e Q_e^T F_e F_e^T Q_e (m * u)), u = S r,
-S = diag(A)^-1/2, m = 0 on penalty-Dirichlet equations.
+NS x R.  M r = S (alpha u + m * sum_e Q_e^T F_e F_e^T Q_e (m * u)), u = S r,
+S = diag(A)^-1/2, m = 0 on penalty-Dirichlet equations, alpha = exp(a).
 Loss = mean_j (M r_j - e_j)^T A (M r_j - e_j) / e_j^T A e_j on masked vectors.
 """
 import numpy as np
@@ -25,7 +25,7 @@ def layout(NS, R):
     NR = NS * R
     o, off = 0, {}
     for name, size in (("W0", H), ("b0", H), ("W1", H * 2 * H), ("b1", H), ("W2", H * 2 * H), ("b2", H),
-                       ("Wo", NR * H), ("bo", NR)):
+                       ("Wo", NR * H), ("bo", NR), ("a", 1)):
         off[name] = (o, size)
         o += size
     return off, o
@@ -88,7 +88,7 @@ def forward(mesh, p, R):
     return F, act
 
 
-def apply_M(mesh, F, r):
+def apply_M(mesh, F, r, alpha=1.0):
     u = mesh.dsq * r
     um = mesh.mask * u
     ue = um[mesh.dest]                          # E x NS
@@ -96,24 +96,27 @@ def apply_M(mesh, F, r):
     ce = np.einsum("eir,er->ei", F, t)
     c = np.zeros_like(r)
     np.add.at(c, mesh.dest.reshape(-1), ce.reshape(-1))
-    return mesh.dsq * (u + mesh.mask * c)
+    return mesh.dsq * (alpha * u + mesh.mask * c)
 
 
 def loss_and_grad(mesh, A, p, R, Rs, Es):
     """A: scipy sparse matrix; Rs, Es: [P][n] residuals and errors."""
     F, act = forward(mesh, p, R)
     g = unpack(p, mesh.NS, R)
+    alpha = float(np.exp(g["a"][0]))
     P = len(Rs)
     loss = 0.0
+    da = 0.0
     dF = np.zeros_like(F)
     for r, e in zip(Rs, Es):
         em = mesh.mask * e
         eAe = em @ (A @ em)
-        z = apply_M(mesh, F, r)
+        z = apply_M(mesh, F, r, alpha)
         w = mesh.mask * (z - e)
         aw = A @ w
         loss += (w @ aw) / eAe / P
         gz = 2.0 / (P * eAe) * mesh.mask * aw
+        da += alpha * (gz @ (mesh.dsq ** 2 * r))
         ue = (mesh.mask * mesh.dsq * r)[mesh.dest]
         ge = (mesh.mask * mesh.dsq * gz)[mesh.dest]
         t = np.einsum("eir,ei->er", F, ue)
@@ -140,16 +143,18 @@ def loss_and_grad(mesh, A, p, R, Rs, Es):
     dpre0 = dh * (1 - h0 * h0)
     grad["W0"] = dpre0.T @ mesh.feat
     grad["b0"] = dpre0.sum(0)
+    grad["a"] = np.array([da])
     return loss, pack(grad, mesh.NS, R)
 
 
 def loss_only(mesh, A, p, R, Rs, Es):
     F, _ = forward(mesh, p, R)
+    alpha = float(np.exp(unpack(p, mesh.NS, R)["a"][0]))
     P = len(Rs)
     loss = 0.0
     for r, e in zip(Rs, Es):
         em = mesh.mask * e
-        z = apply_M(mesh, F, r)
+        z = apply_M(mesh, F, r, alpha)
         w = mesh.mask * (z - e)
         loss += (w @ (A @ w)) / (em @ (A @ em)) / P
     return loss

@@ -213,7 +213,7 @@ def test_learned_oracle_gradient_matches_finite_differences():
     Rs, Es = rng.standard_normal((2, om.neq)), rng.standard_normal((2, om.neq))
     loss, g = LO.loss_and_grad(mesh, A, p, R, Rs, Es)
     assert abs(loss - LO.loss_only(mesh, A, p, R, Rs, Es)) <= 1e-12 * abs(loss)
-    idx = rng.choice(n, 60, replace=False)
+    idx = np.append(rng.choice(n - 1, 60, replace=False), n - 1)  # the last parameter is the Jacobi scale
     h = 1e-6
     for i in idx:
         e = np.zeros(n)
