@@ -44,6 +44,7 @@ def parse():
     ap.add_argument("--no-fp64-baseline", action="store_true", help="skip the FP64 Jacobi-PCG reference solve")
     ap.add_argument("--no-e2e", action="store_true", help="skip the end-to-end C-ABI leg")
     ap.add_argument("--no-learned", action="store_true", help="skip the learned-preconditioner (2D Darcy) leg")
+    ap.add_argument("--no-hp", action="store_true", help="skip the hp (uneven-order) assembly leg")
     return ap.parse_args()
 
 
@@ -270,6 +271,8 @@ def run_gpu(args):
     }
     if rank == 0 and not args.no_learned:
         out["learned_darcy2d"] = learned_leg(gpz, dev)
+    if rank == 0 and not args.no_hp:
+        out["hp_elasticity"] = hp_leg(gpz, dev)
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         out["cpu_baseline"] = cpu_baseline(fp64["iterations"], n)
     if rank == 0:
@@ -277,6 +280,31 @@ def run_gpu(args):
     ctx.close()
     if world > 1:
         torch.distributed.destroy_process_group()
+
+
+def hp_leg(gpz, dev, n=40):
+    """Assembly of the uneven-order workload: 3D elasticity on 40^3 hexes, preferred order uniform in {1,2,3}
+    per element (seed 3), shared sides at the largest order, E lognormal(sigma=0.5), nu=0.3, body force
+    (0,0,-1), clamped base; plus its solve (mixed CG, block Jacobi) to the same true FP64 residual."""
+    orders = gpz.hp_orders(n ** 3, 3)
+    E = gpz.lognormal(n ** 3, 0.5, 3)
+    grid = gpz.elasticity3d_hp(n, orders, E=E)
+    ctx = gpz.Context(dev)
+    ctx.upload_mesh(grid)
+    nnz = ctx.build_pattern(True)
+    ctx.assemble()  # the first assembly runs the hp kernels' block-size autotuner
+    ms = ctx.time_kernel(gpz.GPZ_KERNEL_ASSEMBLE, 3)
+    rep = ctx.assembly_report()
+    ctx.assemble(gpz.GPZ_PREC_MIXED)
+    sol = ctx.solve(solver=gpz.GPZ_SOLVER_MIXED_CG, precond=gpz.GPZ_PRECOND_BLOCK_JACOBI, tol=TOL, max_iter=200000,
+                    reliable_delta=1e-2, check_every=64, want_x=False)
+    ctx.close()
+    return {"workload": f"3D elasticity {n}^3 hexes, p uniform in {{1,2,3}} per element (seed 3, max rule on shared "
+                        "sides), E lognormal(sigma=0.5) seed 3, nu=0.3, body force (0,0,-1), clamped z=0",
+            "neq": grid.neq, "nnz_upper": nnz, "elements": grid.nel, "assembly_fp64_s": ms / 1e3,
+            "elements_per_s": grid.nel / (ms / 1e3), "batching": rep,
+            "mixed_cg": {"iterations": sol["iterations"], "true_resid": sol["true_resid"], "seconds": sol["seconds"],
+                         "rc": sol["rc"]}}
 
 
 def learned_leg(gpz, dev, n=256, seeds=(10000, 10001, 10002)):
@@ -306,7 +334,7 @@ def learned_leg(gpz, dev, n=256, seeds=(10000, 10001, 10002)):
     tl = sum(r["learned_s"] for r in rows)
     return {"workload": f"2D Darcy {n}^2 Q2 quads, k = exp(GRF sigma 1.5, correlation 0.1), unseen seeds "
                         f"{seeds[0]}..{seeds[-1]}, tol {TOL} (true FP64 residual)",
-            "weights": "neopz_gb300/data/learned_darcy2d_q2.npy (trained on the GPU, 300 fields)",
+            "weights": "neopz_gb300/data/learned_darcy2d_q2.npy (trained on the GPU: 2000 fields, checkpoint selected on validation fields)",
             "fields": rows, "iterations_ratio": round(sum(r["learned_iterations"] for r in rows) /
                                                       sum(r["jacobi_iterations"] for r in rows), 3),
             "speedup_vs_fp64_jacobi_pcg": round(tj / tl, 3)}

@@ -147,6 +147,11 @@ int gpz_pattern_download(gpz_ctx *ctx, int64_t *IA, int64_t *JA);
 #define GPZ_PREC_MIXED 1
 int gpz_assemble(gpz_ctx *ctx, int precision);
 /* Download the assembled values (nnz doubles) and the load vector (neq). */
+/* Load vector only (TPZStructMatrix::Assemble(rhs, gui), StrMatrix/pzstrmatrixor.cpp:75-103;
+ * TPZLinearAnalysis::AssembleResidual): the same element kernels stopped
+ * before the element matrix; needs the mesh, not the pattern.  Read it with
+ * gpz_rhs_download. */
+int gpz_assemble_rhs(gpz_ctx *ctx);
 int gpz_matrix_download(gpz_ctx *ctx, double *A);
 int gpz_rhs_download(gpz_ctx *ctx, double *F);
 /* Overwrite the device load vector (a user right-hand side). */
@@ -211,6 +216,12 @@ int gpz_time_kernel(gpz_ctx *ctx, int which, int reps, double *ms_per_launch);
 /* JSON text of the SpMV autotuner's measurements (ms per launch of every
  * candidate layout / kernel of the mixed CG) for the assembled system. */
 int gpz_tuning_report(gpz_ctx *ctx, char *buf, int64_t len);
+/* JSON text of the element batching: uniform-order buckets (compile-time
+ * kernels), hp classes (elements of uneven side orders sharing the table of
+ * the full element of their largest order, one run-time kernel per class and
+ * colour), colours, and the hp kernels' block-size autotuner timings (ms of one
+ * assembly per candidate). */
+int gpz_assembly_report(gpz_ctx *ctx, char *buf, int64_t len);
 
 /* ---- coefficient update -------------------------------------------------
  * Replace the per-element coefficients (el_coef of gpz_mesh_desc) of the

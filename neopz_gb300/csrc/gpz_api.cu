@@ -161,7 +161,7 @@ int gpz_mesh_upload(gpz_ctx *ctx, const gpz_mesh_desc *d) {
     else c.d_coef.release();
     build_buckets(c, *d);
     c.have_mesh = true;
-    c.have_pattern = c.have_matrix = c.have_solution = c.have_a32 = c.have_bjinv = false;
+    c.have_pattern = c.have_matrix = c.have_solution = c.have_a32 = c.have_bjinv = c.have_rhs = false;
     return GPZ_OK;
   });
 }
@@ -171,7 +171,7 @@ int gpz_mesh_set_coef(gpz_ctx *ctx, const double *el_coef) {
     GPZ_REQUIRE(c.have_mesh, GPZ_E_NOT_READY, "no mesh");
     GPZ_REQUIRE(el_coef, GPZ_E_INVALID, "null coefficients");
     c.d_coef.upload(el_coef, c.nel, c.stream);
-    c.have_matrix = c.have_solution = false;
+    c.have_matrix = c.have_solution = c.have_rhs = false;
     GPZ_CUDA_TRY(cudaStreamSynchronize(c.stream));
     return GPZ_OK;
   });
@@ -185,6 +185,7 @@ int gpz_pattern_build(gpz_ctx *ctx, int sym, int64_t *nnz_out) {
     build_element_offsets(c);
     c.user_sym = sym ? 1 : 0;
     c.have_pattern = true;
+    c.spmv32_tuned = -1;  // a new pattern is tuned again at its first mixed assembly
     c.have_matrix = false;
     if (nnz_out) *nnz_out = sym ? c.nnz_upper : c.nnz;
     return GPZ_OK;
@@ -209,7 +210,32 @@ int gpz_pattern_upload(gpz_ctx *ctx, int sym, int64_t neq, const int64_t *IA, co
     build_element_offsets(c);
     c.user_sym = 0;
     c.have_pattern = true;
+    c.spmv32_tuned = -1;  // a new pattern is tuned again at its first mixed assembly
     c.have_matrix = false;
+    return GPZ_OK;
+  });
+}
+
+int gpz_assembly_report(gpz_ctx *ctx, char *buf, int64_t len) {
+  return guarded(ctx, [&](Ctx &c) {
+    GPZ_REQUIRE(c.have_mesh && buf && len > 0, GPZ_E_INVALID, "arguments");
+    int64_t nb = 0, nhp = 0, ehp = 0, eun = 0;
+    for (const Bucket *b : c.buckets) {
+      if (b->hp) {
+        nhp++;
+        ehp += (int64_t)b->elems.size();
+      } else {
+        nb++;
+        eun += (int64_t)b->elems.size();
+      }
+    }
+    std::string r = "{\"uniform_buckets\": " + std::to_string(nb) + ", \"uniform_elements\": " + std::to_string(eun) +
+                    ", \"hp_classes\": " + std::to_string(nhp) + ", \"hp_elements\": " + std::to_string(ehp) +
+                    ", \"colours\": " + std::to_string(c.ncolours) + ", \"hp_block_size_ms\": " +
+                    (c.asm_tune_report.empty() ? std::string("null") : c.asm_tune_report) + "}";
+    GPZ_REQUIRE((int64_t)r.size() < len, GPZ_E_INVALID, "buffer too small");
+    std::copy(r.begin(), r.end(), buf);
+    buf[r.size()] = 0;
     return GPZ_OK;
   });
 }
@@ -248,6 +274,18 @@ int gpz_assemble(gpz_ctx *ctx, int precision) {
     GPZ_CUDA_TRY(cudaStreamSynchronize(c.stream));
     check_device_flag(c, "assembly");
     c.have_matrix = true;
+    c.have_rhs = true;
+    return GPZ_OK;
+  });
+}
+
+int gpz_assemble_rhs(gpz_ctx *ctx) {
+  return guarded(ctx, [&](Ctx &c) {
+    GPZ_REQUIRE(c.have_mesh, GPZ_E_NOT_READY, "no mesh");
+    assemble_rhs(c);
+    GPZ_CUDA_TRY(cudaStreamSynchronize(c.stream));
+    check_device_flag(c, "load vector assembly");
+    c.have_rhs = true;
     return GPZ_OK;
   });
 }
@@ -288,7 +326,7 @@ int gpz_matrix_download(gpz_ctx *ctx, double *A) {
 
 int gpz_rhs_download(gpz_ctx *ctx, double *F) {
   return guarded(ctx, [&](Ctx &c) {
-    GPZ_REQUIRE(c.have_matrix, GPZ_E_NOT_READY, "not assembled");
+    GPZ_REQUIRE(c.have_matrix || c.have_rhs, GPZ_E_NOT_READY, "not assembled");
     GPZ_CUDA_TRY(cudaMemcpyAsync(F, c.d_f.p, c.neq * sizeof(double), cudaMemcpyDeviceToHost, c.stream));
     GPZ_CUDA_TRY(cudaStreamSynchronize(c.stream));
     return GPZ_OK;

@@ -25,6 +25,7 @@ bool BucketKey::operator<(const BucketKey &o) const {
   if (mat_kind != o.mat_kind) return mat_kind < o.mat_kind;
   if (mat_index != o.mat_index) return mat_index < o.mat_index;
   if (intorder != o.intorder) return intorder < o.intorder;
+  if (hp != o.hp) return hp < o.hp;
   for (int i = 0; i < 19; i++)
     if (orders[i] != o.orders[i]) return orders[i] < o.orders[i];
   for (int i = 0; i < 19; i++)
@@ -37,12 +38,13 @@ namespace {
 struct ElemArgs {
   const double *phi, *dphi, *w;
   const int *sside, *sk;
-  int nq, ncorner, nsides;
+  int nq, ncorner, nsides, nshape;
   const double *xyz;
   const int64_t *el_nodes, *el_conn, *bpos;
   const int32_t *el_mat;
   const double *coef;
   int kind, mdim, forcing, bc_type;
+  int rhs_only;  // load vector only (TPZStructMatrix::Assemble(rhs)): no matrix, no pattern needed
   double scale, E, nu, coef_const, big;
   double force[3], val2[3];
   const int64_t *ia, *offbase;
@@ -130,10 +132,27 @@ __device__ __forceinline__ void forcing_at(const ElemArgs &P, const double *x, d
   }
 }
 
-// NSH shapes, DIM element dimension, NST states per shape, BC boundary element
-template <int NSH, int DIM, int NST, bool BC>
-__global__ void __launch_bounds__(128) k_elem_fp64(ElemArgs P, const int64_t *__restrict__ elems, int64_t nelems) {
+// Active shapes of the elements of an hp class (one row of kMaxShapes per element).
+struct HpArgs {
+  const uint8_t *full;  // index into the class table
+  const uint8_t *k;     // index inside its side (the element's own enumeration)
+  const int32_t *n;     // number of shapes of the element
+};
+
+// NSH_T table shapes (0: read at run time), DIM element dimension, NST states
+// per shape, BC boundary element.  HP: the element uses a subset of the table's
+// shapes (hp element of uneven side orders; the H1 shapes of a side of order o
+// are among those of the same side at the class order, with the same values),
+// listed per element in H.  Any block size that is a multiple of 32 works; the
+// hp classes' block size is autotuned.
+template <int NSH_T, int DIM, int NST, bool BC, bool HP>
+__global__ void __launch_bounds__(256) k_elem_fp64(ElemArgs P, HpArgs H, const int64_t *__restrict__ elems,
+                                                   int64_t nelems) {
   extern __shared__ double sm[];
+  const int64_t ie = blockIdx.x;
+  if (ie >= nelems) return;
+  const int NT = NSH_T > 0 ? NSH_T : P.nshape;  // shapes of the table (its row stride)
+  const int NSH = HP ? H.n[ie] : NT;            // shapes of this element
   const int nq = P.nq;
   double *sG = sm;                                    // [nq][NSH][DIM] (volume)
   double *sW = sG + (BC ? 0 : nq * NSH * DIM);        // [nq]
@@ -141,11 +160,11 @@ __global__ void __launch_bounds__(128) k_elem_fp64(ElemArgs P, const int64_t *__
   double *sC = sX + nq * 3;                           // [8][3] corners
   int64_t *sRow = (int64_t *)(sC + 24);               // [NSH] first equation of each shape
   int *sSide = (int *)(sRow + NSH);                   // [NSH]
+  int *sIdx = sSide + NSH;                            // [NSH] table index of each shape
+  int *sK = sIdx + NSH;                               // [NSH] index of the shape inside its side
   __shared__ double sCoef;
   __shared__ int64_t sOffBase;
 
-  const int64_t ie = blockIdx.x;
-  if (ie >= nelems) return;
   const int64_t e = elems[ie];
   const int tid = threadIdx.x;
   const int nc = P.ncorner;
@@ -155,14 +174,18 @@ __global__ void __launch_bounds__(128) k_elem_fp64(ElemArgs P, const int64_t *__
     int64_t node = P.el_nodes[e * 8 + k];
     sC[k * 3 + j] = P.xyz[node * 3 + j];
   }
-  if (tid < NSH) {
-    int side = P.sside[tid];
-    int64_t cn = P.el_conn[e * 27 + side];
-    sRow[tid] = P.bpos[cn] + (int64_t)P.sk[tid] * NST;
-    sSide[tid] = side;
+  for (int a = tid; a < NSH; a += blockDim.x) {
+    const int fa = HP ? (int)H.full[ie * kMaxShapes + a] : a;
+    const int ka = HP ? (int)H.k[ie * kMaxShapes + a] : P.sk[a];
+    const int side = P.sside[fa];
+    const int64_t cn = P.el_conn[e * 27 + side];
+    sRow[a] = P.bpos[cn] + (int64_t)ka * NST;
+    sSide[a] = side;
+    sIdx[a] = fa;
+    sK[a] = ka;
   }
   if (tid == 0) {
-    sOffBase = P.offbase[e];
+    sOffBase = P.rhs_only ? 0 : P.offbase[e];
     double cf = P.kind == GPZ_MAT_ELAST3D ? P.E : P.coef_const;
     if (!BC && P.coef) cf = P.coef[e];
     sCoef = cf;
@@ -177,8 +200,8 @@ __global__ void __launch_bounds__(128) k_elem_fp64(ElemArgs P, const int64_t *__
     double phic[8], dc[3 * 8];
     // corner shapes are the first nc shapes of the table; their gradients give J
     for (int k = 0; k < nc; k++) {
-      phic[k] = P.phi[q * NSH + k];
-      for (int d = 0; d < DIM; d++) dc[d * 8 + k] = P.dphi[(q * DIM + d) * NSH + k];
+      phic[k] = P.phi[q * NT + k];  // the corner shapes are the table's first nc, active in every element
+      for (int d = 0; d < DIM; d++) dc[d * 8 + k] = P.dphi[(q * DIM + d) * NT + k];
     }
     (void)pt;
     double jinv[3][3];
@@ -191,12 +214,14 @@ __global__ void __launch_bounds__(128) k_elem_fp64(ElemArgs P, const int64_t *__
     }
     if (!BC) {
       // store jinv temporarily in sG is not possible; compute gradients directly
-      for (int a = 0; a < NSH; a++)
+      for (int a = 0; a < NSH; a++) {
+        const int fa = HP ? sIdx[a] : a;
         for (int d = 0; d < DIM; d++) {
           double g = 0.0;
-          for (int j = 0; j < DIM; j++) g += jinv[j][d] * P.dphi[(q * DIM + j) * NSH + a];
+          for (int j = 0; j < DIM; j++) g += jinv[j][d] * P.dphi[(q * DIM + j) * NT + fa];
           sG[(q * NSH + a) * DIM + d] = g;
         }
+      }
     }
   }
   __syncthreads();
@@ -205,19 +230,20 @@ __global__ void __launch_bounds__(128) k_elem_fp64(ElemArgs P, const int64_t *__
   // ---- load vector
   for (int idx = tid; idx < NSH * NST; idx += blockDim.x) {
     int a = idx / NST, s = idx % NST;
+    const int fa = HP ? sIdx[a] : a;
     double acc = 0.0;
     if (!BC) {
       for (int q = 0; q < nq; q++) {
         double fv[3];
         forcing_at(P, &sX[q * 3], fv);
-        double ph = P.phi[q * NSH + a];
+        double ph = P.phi[q * NT + fa];
         if (P.kind == GPZ_MAT_POISSON) acc += sW[q] * P.scale * ph * fv[0];
         else if (P.kind == GPZ_MAT_DARCY) acc += sW[q] * fv[0] * ph;
         else acc += sW[q] * (fv[s] * ph);
       }
     } else {
       double m = 0.0;
-      for (int q = 0; q < nq; q++) m += P.phi[q * NSH + a] * sW[q];
+      for (int q = 0; q < nq; q++) m += P.phi[q * NT + fa] * sW[q];
       if (P.bc_type == 0) acc = P.big * P.val2[s] * m;
       else if (P.bc_type == 1) acc = P.val2[s] * m * (P.kind == GPZ_MAT_POISSON ? P.scale : 1.0);
     }
@@ -228,7 +254,7 @@ __global__ void __launch_bounds__(128) k_elem_fp64(ElemArgs P, const int64_t *__
     }
     P.f[row] += acc;
   }
-  if (BC && P.bc_type != 0) return;
+  if ((BC && P.bc_type != 0) || P.rhs_only) return;
 
   // ---- matrix: pairs a <= b
   double C1 = 0, C2 = 0, C3 = 0;
@@ -244,8 +270,9 @@ __global__ void __launch_bounds__(128) k_elem_fp64(ElemArgs P, const int64_t *__
     if (a > b) continue;
     double K[NST][NST];
     if (BC) {
+      const int fa = HP ? sIdx[a] : a, fb = HP ? sIdx[b] : b;
       double m = 0.0;
-      for (int q = 0; q < nq; q++) m += sW[q] * P.phi[q * NSH + a] * P.phi[q * NSH + b];
+      for (int q = 0; q < nq; q++) m += sW[q] * P.phi[q * NT + fa] * P.phi[q * NT + fb];
       for (int s = 0; s < NST; s++)
         for (int t = 0; t < NST; t++) K[s][t] = (s == t) ? P.big * m : 0.0;
     } else if (NST == 1) {
@@ -280,7 +307,7 @@ __global__ void __launch_bounds__(128) k_elem_fp64(ElemArgs P, const int64_t *__
       atomicOr(P.err, 32);
       continue;
     }
-    const int ka = P.sk[a] * NST, kb = P.sk[b] * NST;
+    const int ka = sK[a] * NST, kb = sK[b] * NST;
     for (int s = 0; s < NST; s++) {
       const int64_t ra = sRow[a] + s;
       const int64_t base = P.ia[ra] + oab + kb;
@@ -316,16 +343,17 @@ __global__ void __launch_bounds__(128) k_elem_fp64(ElemArgs P, const int64_t *__
 
 size_t smem_bytes(int nsh, int dim, int nq, bool bc) {
   size_t d = (bc ? 0 : (size_t)nq * nsh * dim) + nq + (size_t)nq * 3 + 24;
-  return d * sizeof(double) + (size_t)nsh * (sizeof(int64_t) + sizeof(int)) + 16;
+  return d * sizeof(double) + (size_t)nsh * (sizeof(int64_t) + 3 * sizeof(int)) + 16;
 }
 
-typedef void (*ElemKernel)(ElemArgs, const int64_t *, int64_t);
+typedef void (*ElemKernel)(ElemArgs, HpArgs, const int64_t *, int64_t);
 
 template <int NSH, int DIM, int NST, bool BC>
 ElemKernel pick() {
-  return k_elem_fp64<NSH, DIM, NST, BC>;
+  return k_elem_fp64<NSH, DIM, NST, BC, false>;
 }
 
+// compile-time shape counts of the uniform-order elements; nullptr: use the batched run-time kernel
 ElemKernel select_kernel(int type, int nshape, int nstate, bool bc) {
   // volume hexes (3D) and quads (2D); boundary quads (3D faces) and lines (2D edges)
   if (type == GPZ_EL_HEX && !bc) {
@@ -363,6 +391,15 @@ ElemKernel select_kernel(int type, int nshape, int nstate, bool bc) {
   return nullptr;
 }
 
+// the run-time kernel of an hp class
+ElemKernel select_hp(int type, int nstate, bool bc) {
+  if (type == GPZ_EL_HEX && !bc) return nstate == 1 ? k_elem_fp64<0, 3, 1, false, true> : k_elem_fp64<0, 3, 3, false, true>;
+  if (type == GPZ_EL_QUAD && !bc && nstate == 1) return k_elem_fp64<0, 2, 1, false, true>;
+  if (type == GPZ_EL_QUAD && bc) return nstate == 1 ? k_elem_fp64<0, 2, 1, true, true> : k_elem_fp64<0, 2, 3, true, true>;
+  if (type == GPZ_EL_LINE && bc && nstate == 1) return k_elem_fp64<0, 1, 1, true, true>;
+  return nullptr;
+}
+
 __global__ void k_extract_diag(const double *__restrict__ a, const int64_t *__restrict__ diagpos, int64_t neq,
                                double *__restrict__ dinv) {
   int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -382,6 +419,8 @@ void build_buckets(Ctx &c, const gpz_mesh_desc &d) {
   c.buckets.clear();
   std::map<BucketKey, int> index;
   std::vector<int> el_bucket(c.nel, -1);
+  std::vector<uint8_t> act_full((size_t)c.nel * kMaxShapes, 0), act_k((size_t)c.nel * kMaxShapes, 0);
+  std::vector<int32_t> act_n(c.nel, 0);
   for (int64_t e = 0; e < c.nel; e++) {
     BucketKey k{};
     k.type = d.el_type[e];
@@ -405,14 +444,58 @@ void build_buckets(Ctx &c, const gpz_mesh_desc &d) {
     k.mat_index = d.el_mat[e];
     GPZ_REQUIRE(m->kind == GPZ_MAT_POISSON || m->kind == GPZ_MAT_DARCY || m->kind == GPZ_MAT_ELAST3D,
                 GPZ_E_UNSUPPORTED_MATERIAL, "material kind");
-    int p = d.el_order[e];
+    // IntegrationRuleOrder(MaxOrder): the largest order of the element's connects
+    // (hp sides set by SetSideOrder re-run AdjustIntegrationRule,
+    // Mesh/pzinterpolationspace.cpp:69-83); equal to the element's p when p is uniform
+    int p = 1;
+    for (int s = t.ncorner; s < t.nsides; s++) p = std::max(p, (int)d.conn_order[d.el_conn[e * 27 + s]]);
     if (k.is_bc || m->kind == GPZ_MAT_ELAST3D) k.intorder = 2 * p;
     else k.intorder = (p < m->forcing_porder) ? m->forcing_porder + p : 2 * p;
+    int eorder[19];
+    bool uniform = true;
     for (int s = t.ncorner; s < t.nsides; s++) {
       int64_t cn = d.el_conn[e * 27 + s];
-      int o = d.conn_order[cn];
+      eorder[s - t.ncorner] = d.conn_order[cn];
+      uniform &= eorder[s - t.ncorner] == p;
+    }
+    // uniform elements keep their own tables; an element of uneven side orders
+    // joins the hp class of its largest order, whose table is the full element
+    k.hp = uniform ? 0 : 1;
+    for (int s = t.ncorner; s < t.nsides; s++) {
+      int o = uniform ? eorder[s - t.ncorner] : p;
       k.orders[s - t.ncorner] = o;
       k.trans[s - t.ncorner] = side_nshape(k.type, s, o) > 1 ? side_orientation(k.type, s, &d.el_nodes[e * 8]) : 0;
+    }
+    if (!k.hp) {
+      int n = t.ncorner;
+      for (int s = t.ncorner; s < t.nsides; s++) n += side_nshape(k.type, s, k.orders[s - t.ncorner]);
+      if (!select_kernel(k.type, n, c.nstate, k.is_bc)) k.hp = 1;  // no compile-time kernel: same table, run-time path
+    }
+    if (k.hp) {
+      // active shapes of this element among the class table's: corners, then per
+      // side its order-o functions, found by their Chebyshev index tuple
+      int n = 0;
+      uint8_t *rf = &act_full[e * kMaxShapes], *rk = &act_k[e * kMaxShapes];
+      for (int a = 0; a < t.ncorner; a++, n++) {
+        rf[n] = (uint8_t)a;
+        rk[n] = 0;
+      }
+      int tstart = t.ncorner;
+      for (int s = t.ncorner; s < t.nsides; s++) {
+        const int o = eorder[s - t.ncorner], sd = t.side_dim[s];
+        const int ns = side_nshape(k.type, s, o), nsf = side_nshape(k.type, s, p);
+        const int m = o - 1, mf = p - 1;
+        for (int kk = 0; kk < ns; kk++, n++) {
+          int full;
+          if (sd == 1) full = kk;
+          else if (sd == 2) full = (kk / m) * mf + kk % m;
+          else full = ((kk / (m * m)) * mf + (kk / m) % m) * mf + kk % m;
+          rf[n] = (uint8_t)(tstart + full);
+          rk[n] = (uint8_t)kk;
+        }
+        tstart += nsf;
+      }
+      act_n[e] = n;
     }
     auto it = index.find(k);
     int bi;
@@ -446,8 +529,10 @@ void build_buckets(Ctx &c, const gpz_mesh_desc &d) {
         }
       }
       b->ndof = b->nshape * c.nstate;
-      GPZ_REQUIRE(select_kernel(k.type, b->nshape, c.nstate, k.is_bc) != nullptr, GPZ_E_UNSUPPORTED_ELEMENT,
-                  "no kernel for this element bucket");
+      b->hp = k.hp != 0;
+      GPZ_REQUIRE(b->hp ? select_hp(k.type, c.nstate, k.is_bc) != nullptr
+                        : select_kernel(k.type, b->nshape, c.nstate, k.is_bc) != nullptr,
+                  GPZ_E_UNSUPPORTED_ELEMENT, "no kernel for this element bucket");
       c.buckets.push_back(b);
     } else {
       bi = it->second;
@@ -489,6 +574,23 @@ void build_buckets(Ctx &c, const gpz_mesh_desc &d) {
     int bi = el_bucket[e];
     c.buckets[bi]->elems[fillpos[bi][colour[e]]++] = e;
   }
+  // per-element active shapes of the hp classes, in each class's element order
+  for (Bucket *b : c.buckets) {
+    if (!b->hp) continue;
+    const size_t ne = b->elems.size();
+    b->act_full.assign(ne * kMaxShapes, 0);
+    b->act_k.assign(ne * kMaxShapes, 0);
+    b->act_n.assign(ne, 0);
+    for (size_t i = 0; i < ne; i++) {
+      const int64_t e = b->elems[i];
+      std::copy(&act_full[e * kMaxShapes], &act_full[e * kMaxShapes] + kMaxShapes, &b->act_full[i * kMaxShapes]);
+      std::copy(&act_k[e * kMaxShapes], &act_k[e * kMaxShapes] + kMaxShapes, &b->act_k[i * kMaxShapes]);
+      b->act_n[i] = act_n[e];
+    }
+    b->d_act_full.upload(b->act_full.data(), b->act_full.size(), c.stream);
+    b->d_act_k.upload(b->act_k.data(), b->act_k.size(), c.stream);
+    b->d_act_n.upload(b->act_n.data(), b->act_n.size(), c.stream);
+  }
   for (Bucket *b : c.buckets) {
     b->d_phi.upload(b->phi.data(), b->phi.size(), c.stream);
     b->d_dphi.upload(b->dphi.data(), b->dphi.size(), c.stream);
@@ -500,73 +602,147 @@ void build_buckets(Ctx &c, const gpz_mesh_desc &d) {
   GPZ_CUDA_TRY(cudaStreamSynchronize(c.stream));
 }
 
-void assemble_fp64(Ctx &c) {
+namespace {
+
+ElemArgs args_of(Ctx &c, const Bucket *b) {
+  ElemArgs P{};
+  P.phi = b->d_phi.p;
+  P.dphi = b->d_dphi.p;
+  P.w = b->d_w.p;
+  P.sside = b->d_shape_side.p;
+  P.sk = b->d_shape_k.p;
+  P.nq = b->nq;
+  P.ncorner = b->ncorner;
+  P.nsides = b->nsides;
+  P.nshape = b->nshape;
+  P.xyz = c.d_xyz.p;
+  P.el_nodes = c.d_el_nodes.p;
+  P.el_conn = c.d_el_conn.p;
+  P.bpos = c.d_block_pos.p;
+  P.el_mat = c.d_el_mat.p;
+  P.coef = c.d_coef.p;
+  const int64_t e_any = b->elems[0];
+  const int mi = c.h_el_mat[e_any];
+  const gpz_material *m;
+  if (mi < 0) {
+    const gpz_bc &bc = c.bcs[-mi - 1];
+    m = &c.mats[bc.material];
+    P.bc_type = bc.type;
+    for (int k = 0; k < 3; k++) P.val2[k] = bc.val2[k];
+  } else {
+    m = &c.mats[mi];
+  }
+  P.kind = m->kind;
+  P.mdim = m->dim;
+  P.forcing = m->forcing;
+  P.scale = m->scale;
+  P.E = m->E;
+  P.nu = m->nu;
+  P.coef_const = m->coef_const;
+  P.big = m->kind == GPZ_MAT_ELAST3D ? 1.e12 : m->bignumber;  // TPZElasticity3D.cpp:632
+  for (int k = 0; k < 3; k++) P.force[k] = m->force[k];
+  P.ia = c.d_ia.p;
+  P.offbase = c.d_offbase.p;
+  P.off = c.d_off.p;
+  P.a = c.d_a.p;
+  P.f = c.d_f.p;
+  P.nnz = c.nnz;
+  P.neq = c.neq;
+  P.err = c.d_err.p;
+  return P;
+}
+
+// element integration + scatter of every bucket, colour by colour; the hp
+// classes run with `threads` (0: the class's tuned block size)
+void launch_elements(Ctx &c, int threads, bool rhs_only = false) {
   cudaStream_t s = c.stream;
-  c.d_a.alloc(std::max<int64_t>(c.nnz, 1));
-  c.d_f.alloc(std::max<int64_t>(c.neq, 1));
-  c.d_a.zero(s);
-  c.d_f.zero(s);
   for (int col = 0; col < c.ncolours; col++) {
     for (Bucket *b : c.buckets) {
       int64_t e0 = b->colour_begin[col], e1 = b->colour_begin[col + 1];
       if (e1 == e0) continue;
-      ElemArgs P{};
-      P.phi = b->d_phi.p;
-      P.dphi = b->d_dphi.p;
-      P.w = b->d_w.p;
-      P.sside = b->d_shape_side.p;
-      P.sk = b->d_shape_k.p;
-      P.nq = b->nq;
-      P.ncorner = b->ncorner;
-      P.nsides = b->nsides;
-      P.xyz = c.d_xyz.p;
-      P.el_nodes = c.d_el_nodes.p;
-      P.el_conn = c.d_el_conn.p;
-      P.bpos = c.d_block_pos.p;
-      P.el_mat = c.d_el_mat.p;
-      P.coef = c.d_coef.p;
-      int64_t e_any = b->elems[e0];
-      int mi = c.h_el_mat[e_any];
-      const gpz_material *m;
-      if (mi < 0) {
-        const gpz_bc &bc = c.bcs[-mi - 1];
-        m = &c.mats[bc.material];
-        P.bc_type = bc.type;
-        for (int k = 0; k < 3; k++) P.val2[k] = bc.val2[k];
-      } else {
-        m = &c.mats[mi];
-      }
-      P.kind = m->kind;
-      P.mdim = m->dim;
-      P.forcing = m->forcing;
-      P.scale = m->scale;
-      P.E = m->E;
-      P.nu = m->nu;
-      P.coef_const = m->coef_const;
-      P.big = m->kind == GPZ_MAT_ELAST3D ? 1.e12 : m->bignumber;  // TPZElasticity3D.cpp:632
-      for (int k = 0; k < 3; k++) P.force[k] = m->force[k];
-      P.ia = c.d_ia.p;
-      P.offbase = c.d_offbase.p;
-      P.off = c.d_off.p;
-      P.a = c.d_a.p;
-      P.f = c.d_f.p;
-      P.nnz = c.nnz;
-      P.neq = c.neq;
-      P.err = c.d_err.p;
-      ElemKernel k = select_kernel(b->key.type, b->nshape, c.nstate, b->key.is_bc);
+      ElemArgs P = args_of(c, b);
+      P.rhs_only = rhs_only ? 1 : 0;
       size_t sh = smem_bytes(b->nshape, b->dim, b->nq, b->key.is_bc);
+      ElemKernel k;
+      HpArgs H{nullptr, nullptr, nullptr};
+      int nt = 128;
+      if (b->hp) {
+        k = select_hp(b->key.type, c.nstate, b->key.is_bc);
+        H.full = b->d_act_full.p + e0 * kMaxShapes;
+        H.k = b->d_act_k.p + e0 * kMaxShapes;
+        H.n = b->d_act_n.p + e0;
+        nt = threads > 0 ? threads : b->threads;
+      } else {
+        k = select_kernel(b->key.type, b->nshape, c.nstate, b->key.is_bc);
+      }
       if (sh > 48 * 1024) GPZ_CUDA_TRY(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sh));
-      k<<<(unsigned)(e1 - e0), 128, sh, s>>>(P, b->d_elems.p + e0, e1 - e0);
+      k<<<(unsigned)(e1 - e0), nt, sh, s>>>(P, H, b->d_elems.p + e0, e1 - e0);
       c.launches++;
       GPZ_CUDA_TRY(cudaGetLastError());
     }
   }
+}
+
+}  // namespace
+
+void assemble_fp64(Ctx &c) {
+  cudaStream_t s = c.stream;
+  c.d_a.alloc(std::max<int64_t>(c.nnz, 1));
+  c.d_f.alloc(std::max<int64_t>(c.neq, 1));
+  // autotuner of the hp classes' run-time kernel: time one full assembly per
+  // block size (the values do not depend on it: one CTA per element, fixed
+  // summation order) and keep the fastest
+  bool tune = false;
+  for (Bucket *b : c.buckets) tune |= b->hp && !b->tuned;
+  if (tune) {
+    const int cand[3] = {64, 128, 256};
+    float best = 1e30f;
+    int best_t = 128;
+    std::string rep = "{";
+    cudaEvent_t e0, e1;
+    GPZ_CUDA_TRY(cudaEventCreate(&e0));
+    GPZ_CUDA_TRY(cudaEventCreate(&e1));
+    for (int i = 0; i < 3; i++) {
+      c.d_a.zero(s);
+      c.d_f.zero(s);
+      GPZ_CUDA_TRY(cudaEventRecord(e0, s));
+      launch_elements(c, cand[i]);
+      GPZ_CUDA_TRY(cudaEventRecord(e1, s));
+      GPZ_CUDA_TRY(cudaEventSynchronize(e1));
+      float ms = 0.f;
+      cudaEventElapsedTime(&ms, e0, e1);
+      rep += (i ? ", \"" : "\"") + std::to_string(cand[i]) + "\": " + std::to_string(ms);
+      if (ms < best) {
+        best = ms;
+        best_t = cand[i];
+      }
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    for (Bucket *b : c.buckets)
+      if (b->hp) {
+        b->threads = best_t;
+        b->tuned = true;
+      }
+    c.asm_tune_report = rep + ", \"chosen\": " + std::to_string(best_t) + "}";
+  }
+  c.d_a.zero(s);
+  c.d_f.zero(s);
+  launch_elements(c, 0);
   c.d_dinv.alloc(std::max<int64_t>(c.neq, 1));
   k_extract_diag<<<grid_for(c.neq, 256), 256, 0, s>>>(c.d_a.p, c.d_diagpos.p, c.neq, c.d_dinv.p);
   c.launches++;
   GPZ_CUDA_TRY(cudaGetLastError());
   c.have_a32 = false;
   c.have_bjinv = false;
+}
+
+// load vector alone (TPZStructMatrix::Assemble(rhs), StrMatrix/pzstrmatrixor.cpp:75-103):
+// the same element kernels, stopped before the element matrix
+void assemble_rhs(Ctx &c) {
+  c.d_f.alloc(std::max<int64_t>(c.neq, 1));
+  c.d_f.zero(c.stream);
+  launch_elements(c, 0, true);
 }
 
 void to_fp32(Ctx &c) {

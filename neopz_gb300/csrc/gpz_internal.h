@@ -68,6 +68,7 @@ constexpr int kMaxQp = 64;       // hex 4x4x4 Gauss points
 
 struct BucketKey {
   int type, is_bc, mat_kind, mat_index, intorder;  // mat_index: the element's el_mat value
+  int hp;              // 1: hp class (orders below are the class order; elements use subsets)
   int orders[19];      // order of each non-corner side
   int trans[19];       // orientation id of each non-corner side (0 when irrelevant)
   bool operator<(const BucketKey &o) const;
@@ -86,6 +87,16 @@ struct Bucket {
   std::vector<int64_t> elems;                // global element indices
   std::vector<int64_t> colour_begin;         // [ncolours+1]
   DBuf<int64_t> d_elems;
+  // hp class: elements of uneven side orders up to the class order share the
+  // tables of the full element of that order; per element (in elems order) the
+  // active shapes as indices into the table and as indices inside their side
+  bool hp = false;
+  std::vector<uint8_t> act_full, act_k;      // [elems][kMaxShapes]
+  std::vector<int32_t> act_n;                // [elems]
+  DBuf<uint8_t> d_act_full, d_act_k;
+  DBuf<int32_t> d_act_n;
+  int threads = 128;                         // block size (autotuned for hp classes)
+  bool tuned = false;
 };
 
 // ---------------------------------------------------------------- solver workspace
@@ -152,6 +163,7 @@ struct Ctx {
   DBuf<int64_t> d_el_nodes, d_el_conn, d_block_pos;
   DBuf<int32_t> d_el_type, d_el_mat, d_block_size, d_conn_order;
   std::vector<Bucket *> buckets;
+  std::string asm_tune_report;               // block-size timings of the hp element kernels
   int ncolours = 0;
   DBuf<int> d_err;                           // device-side check flag
 
@@ -169,12 +181,15 @@ struct Ctx {
 
   // values
   bool have_matrix = false;
+  bool have_rhs = false;                     // load vector assembled (with or without the matrix)
   DBuf<double> d_a, d_f, d_dinv;
   DBuf<float> d_a32;                         // FP32 CSR copy for the inner solves
   bool have_a32 = false;
   // FP32 3x3 blocks for the mixed CG (instead of d_a32), in the layout the
   // SpMV autotuner measured fastest on this matrix
   bool have_bsr3 = false;
+  int spmv32_tuned = -1;                     // variant the autotuner chose for the current pattern (-1: not yet)
+  int64_t sell_window_tuned = 2048;          // its sliced-ELL sort window
   int spmv32_variant = 0;                    // 0 block CSR, 1 two rows in flight, 2 sliced ELL, 3 TMA-staged,
                                              // 4 upper triangle with float4 atomics
   uint32_t tma_vcap = 0, tma_ccap = 0;       // shared-memory stage capacities of the TMA-staged kernel
@@ -211,6 +226,7 @@ void build_element_offsets(Ctx &c);
 // assemble.cu
 void build_buckets(Ctx &c, const gpz_mesh_desc &d);
 void assemble_fp64(Ctx &c);
+void assemble_rhs(Ctx &c);
 void make_fp32_copy(Ctx &c, int variant = -1);
 void to_fp32(Ctx &c);
 void build_block_jacobi(Ctx &c);

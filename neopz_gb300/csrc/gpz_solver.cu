@@ -1505,10 +1505,13 @@ void spmv_device(Ctx &c, const double *x, double *y, double alpha, double beta, 
 // uniform 3x3 connect blocks (elasticity with one shape per connect)?
 // (connects without shape functions hold no equations and are skipped, so the
 // equation blocks are then 3k .. 3k+2 for k < neq / 3)
+// Three states per shape, stored consecutively: the matrix is made of 3x3
+// blocks (one per pair of shapes) whenever every connect block holds whole
+// shapes, i.e. its size is a multiple of 3 (hp connects carry several shapes).
 bool blocks_are_3(const Ctx &c) {
   if (c.nstate != 3 || c.neq == 0) return false;
   for (int32_t s : c.h_block_size)
-    if (s != 3 && s != 0) return false;
+    if (s % 3 != 0) return false;
   return true;
 }
 
@@ -1584,7 +1587,9 @@ void launch_spmv32(Ctx &c, int v, const Ctx::Sell &S, Red R, cudaStream_t s) {
 // Autotuner of the mixed CG's SpMV: every candidate layout / kernel is built
 // and timed (CUDA events, 5 launches after 2 warm-up launches) on this matrix;
 // the fastest is kept and the other layouts are released.
-void tune_spmv32(Ctx &c, int only) {
+void finish_layout(Ctx &c, Ctx::Sell *cand, int k);
+
+void tune_spmv32(Ctx &c, int only, bool timing) {
   cudaStream_t s = c.stream;
   alloc_work(c, true);
   SolverWork &w = c.sw;
@@ -1602,6 +1607,7 @@ void tune_spmv32(Ctx &c, int only) {
   GPZ_CUDA_TRY(cudaEventCreate(&e0));
   GPZ_CUDA_TRY(cudaEventCreate(&e1));
   auto time_it = [&](int v, const Ctx::Sell &S) {
+    if (!timing) return 0.0f;  // layout rebuilt for a known choice
     for (int i = 0; i < 2; i++) launch_spmv32(c, v, S, R, s);
     GPZ_CUDA_TRY(cudaEventRecord(e0, s));
     for (int i = 0; i < 5; i++) launch_spmv32(c, v, S, R, s);
@@ -1638,7 +1644,7 @@ void tune_spmv32(Ctx &c, int only) {
     }
   }
   for (int k = 0; k < 2 && want(2); k++) {
-    if (only == 2 && k == 0) continue;
+    if (only == 2 && windows[k] != c.sell_window_tuned) continue;
     build_sell(c, cand[k], windows[k]);
     res.push_back({2, windows[k], time_it(2, cand[k])});
   }
@@ -1670,6 +1676,11 @@ void tune_spmv32(Ctx &c, int only) {
   for (size_t i = 1; i < res.size(); i++)
     if (res[i].ms < res[best].ms) best = i;
   c.spmv32_variant = res[best].v;
+  if (!timing) {
+    finish_layout(c, cand, res[best].window == windows[0] ? 0 : 1);
+    return;
+  }
+  c.sell_window_tuned = res[best].window ? res[best].window : c.sell_window_tuned;
   std::string rep = "{";
   for (size_t i = 0; i < res.size(); i++) {
     const char *nm = res[i].v == 0 ? "block_csr"
@@ -1689,22 +1700,24 @@ void tune_spmv32(Ctx &c, int only) {
   c.tune_report = rep + ", \"chosen\": \"" + names[res[best].v] + "\", \"block_rows\": " + std::to_string(c.nbrow) +
                   ", \"blocks_full\": " + std::to_string(c.nnz / 9) + ", \"blocks_upper\": " + std::to_string(nu) +
                   "}";
+  finish_layout(c, cand, res[best].window == windows[0] ? 0 : 1);
+}
+
+// keep the chosen layout's arrays, drop the other candidates' (the block CSR
+// stays allocated: the next assembly rebuilds the layout from it)
+void finish_layout(Ctx &c, Ctx::Sell *cand, int k) {
   if (c.spmv32_variant != 2) {
-    for (int k = 0; k < 2; k++) {
-      cand[k].scol.release();
-      cand[k].sval.release();
+    for (int i = 0; i < 2; i++) {
+      cand[i].scol.release();
+      cand[i].sval.release();
     }
   }
   if (c.spmv32_variant != 4) {
     c.d_uptr.release();
     c.d_ucol.release();
     c.d_uval.release();
-  } else {
-    c.d_bcol.release();
-    c.d_bval.release();
   }
   if (c.spmv32_variant == 2) {
-    int k = res[best].window == windows[0] ? 0 : 1;
     Ctx::Sell &S = cand[k];
     c.sell.nslice = S.nslice;
     c.sell.plane = S.plane;
@@ -1714,9 +1727,6 @@ void tune_spmv32(Ctx &c, int only) {
     std::swap(c.sell.sperm.p, S.sperm.p); std::swap(c.sell.sperm.n, S.sperm.n);
     std::swap(c.sell.scol.p, S.scol.p); std::swap(c.sell.scol.n, S.scol.n);
     std::swap(c.sell.sval.p, S.sval.p); std::swap(c.sell.sval.n, S.sval.n);
-    c.d_bptr.release();
-    c.d_bcol.release();
-    c.d_bval.release();
   }
 }
 
@@ -1735,7 +1745,12 @@ void make_fp32_copy(Ctx &c, int variant) {
     check_device_flag(c, "3x3 block CSR");
     c.have_bsr3 = true;
     c.d_a32.release();
-    tune_spmv32(c, variant);
+    if (variant < 0 && c.spmv32_tuned >= 0) {
+      tune_spmv32(c, c.spmv32_tuned, false);  // same pattern: rebuild the chosen layout only
+    } else {
+      tune_spmv32(c, variant, true);
+      if (variant < 0) c.spmv32_tuned = c.spmv32_variant;
+    }
   } else {
     c.d_a32.alloc(std::max<int64_t>(c.nnz, 1));
     to_fp32(c);
@@ -1744,7 +1759,8 @@ void make_fp32_copy(Ctx &c, int variant) {
 }
 
 void build_block_jacobi(Ctx &c) {
-  GPZ_REQUIRE(blocks_are_3(c), GPZ_E_INVALID, "block Jacobi needs uniform 3x3 connect blocks (nstate 3, one shape per connect)");
+  // per-shape 3x3 blocks: the connect blocks of TPZBlockDiagonal when every connect carries one shape
+  GPZ_REQUIRE(blocks_are_3(c), GPZ_E_INVALID, "block Jacobi needs 3 states per shape (nstate 3)");
   const int64_t nb = c.neq / 3;
   c.d_bjinv.alloc((size_t)nb * 9);
   k_block_inv3<<<grid_for(nb, 256), 256, 0, c.stream>>>(c.d_a.p, c.d_diagpos.p, nb, c.d_bjinv.p, c.d_err.p);

@@ -113,6 +113,8 @@ def lib():
         L.gpz_solve.argtypes = [vp, _P(gpz_solver_opts), vp, vp, _P(gpz_solve_report)]
         L.gpz_solution_download.argtypes = [vp, vp]
         L.gpz_mesh_set_coef.argtypes = [vp, vp]
+        L.gpz_assembly_report.argtypes = [vp, ctypes.c_char_p, i64]
+        L.gpz_assemble_rhs.argtypes = [vp]
         L.gpz_learned_init.argtypes = [vp, i32, ctypes.c_uint64]
         L.gpz_learned_num_params.argtypes = [vp, _P(i64)]
         L.gpz_learned_get_params.argtypes = [vp, vp, i64]
@@ -315,6 +317,16 @@ class Context:
         self._check(lib().gpz_spmv(self.h, alpha, _p(x), beta, _p(yy), _p(z)))
         return z
 
+    def assemble_rhs(self):
+        """Load vector alone (no matrix); read it with rhs()."""
+        self._check(lib().gpz_assemble_rhs(self.h))
+
+    def assembly_report(self):
+        import json
+        buf = ctypes.create_string_buffer(4096)
+        self._check(lib().gpz_assembly_report(self.h, buf, 4096))
+        return json.loads(buf.value.decode())
+
     def set_coef(self, grid, cell_coef):
         """New per-cell coefficients for the uploaded mesh (same numbering and pattern)."""
         self._coef_keep = np.ascontiguousarray(grid.element_coef(cell_coef))
@@ -396,6 +408,29 @@ def elasticity3d(n, p=2, E=None, nu=0.3, top_traction=True, body_force=(0.0, 0.0
     if top_traction:
         bcs.append((-3, bc(1, 0, (0, 0, -1.0))))
     return Grid(3, (n, n, n), (0, 0, 0), (1, 1, 1), [1, -1, -2, -2, -2, -2, -3], True, p, mats, bcs, elem_coef=E)
+
+
+def elasticity3d_hp(n, orders, E=None, nu=0.3, body_force=(0.0, 0.0, -1.0)):
+    """hp elasticity (the 40^3 uneven-p workload at n = 40): unit cube n^3 hexes, preferred order orders[e] per
+    element, every shared side at the largest order of its elements (SetSideOrder max rule), body force,
+    clamped z = 0 face."""
+    mats = [(1, material(GPZ_MAT_ELAST3D, 3, E=1.0, nu=nu, force=body_force, forcing=GPZ_F_CONST))]
+    bcs = [(-1, bc(0, 0))]
+    return Grid(3, (n, n, n), (0, 0, 0), (1, 1, 1), [1, -1, -2, -2, -2, -2, -2], True, 1, mats, bcs, elem_coef=E,
+                elem_order=orders)
+
+
+def darcy_hp(n, orders, perm, rhs=1.0):
+    """hp Darcy on the unit square: n x n quads of preferred orders orders[e], u = 0 on the boundary."""
+    mats = [(1, material(GPZ_MAT_DARCY, 2, forcing=GPZ_F_CONST, force=(rhs, 0, 0)))]
+    bcs = [(-1, bc(0, 0))]
+    return Grid(2, (n, n), (0, 0, 0), (1, 1, 0), [1, -1, -1, -1, -1], True, 1, mats, bcs, elem_coef=perm,
+                elem_order=orders)
+
+
+def hp_orders(ncells, seed, low=1, high=3):
+    """Preferred orders uniform in {low..high} per element from a seeded PCG64 stream."""
+    return np.random.default_rng(seed).integers(low, high + 1, ncells).astype(np.int32)
 
 
 def darcy(dim, n, p, perm, rhs=1.0):

@@ -53,14 +53,31 @@ def context_for(grid, rank=4, seed=0, params=None):
     return ctx
 
 
-def train(ctx, grid, coef_of_seed, seeds, steps=8, lr=3e-3, npairs=16, tol=1e-12, log_every=0, lr_final=None):
-    """Online training over the fields of `seeds` (learning rate decayed from lr to lr_final on a
-    cosine); returns (first loss, last loss, seconds)."""
+def validate(ctx, grid, coef_of_seed, seeds, tol=1e-8):
+    """Learned flexible-CG iterations summed over validation fields."""
+    its = 0
+    for s in seeds:
+        ctx.set_coef(grid, coef_of_seed(s))
+        ctx.assemble()
+        its += ctx.solve(solver=gpz.GPZ_SOLVER_LEARNED_FCG, tol=tol, want_x=False)["iterations"]
+    return its
+
+
+def train(ctx, grid, coef_of_seed, seeds, steps=8, lr=3e-3, npairs=16, tol=1e-12, log_every=0, lr_final=None,
+          val_seeds=(20000, 20001), val_every=50):
+    """Online training over the fields of `seeds` (learning rate decayed from lr to lr_final on a cosine).
+
+    The energy-norm loss flattens early while the parameters can keep drifting in directions that
+    lengthen the Krylov iteration, so every `val_every` fields the learned flexible CG is run on the
+    validation fields and the parameters with the fewest iterations are kept (restored at the end).
+    Returns (first loss, last loss, seconds, validation history)."""
     import math
     seeds = list(seeds)
     lr_final = lr / 10 if lr_final is None else lr_final
     t0 = time.time()
     first = last = None
+    history = []
+    best = None
     for i, s in enumerate(seeds):
         ctx.set_coef(grid, coef_of_seed(s))
         ctx.assemble()
@@ -69,9 +86,20 @@ def train(ctx, grid, coef_of_seed, seeds, steps=8, lr=3e-3, npairs=16, tol=1e-12
         l0, l1 = ctx.learned_train(steps=steps, lr=li)
         first = l0 if first is None else first
         last = l1
-        if log_every and (i + 1) % log_every == 0:
-            print(json.dumps({"fields": i + 1, "loss": l1, "seconds": round(time.time() - t0, 1)}), flush=True)
-    return first, last, time.time() - t0
+        done = i + 1
+        if val_seeds and (done % val_every == 0 or done == len(seeds)):
+            its = validate(ctx, grid, coef_of_seed, val_seeds)
+            history.append({"fields": done, "validation_iterations": its, "loss": l1})
+            if best is None or its < best[0]:
+                best = (its, ctx.learned_params(), done)
+        if log_every and done % log_every == 0:
+            print(json.dumps({"fields": done, "loss": l1, "seconds": round(time.time() - t0, 1),
+                              "validation": history[-1] if history else None}), flush=True)
+    if best is not None:
+        # set_learned_params also clears the Adam moments: a later train() call starts afresh from here
+        ctx.set_learned_params(best[1])
+        history.append({"kept_fields": best[2], "validation_iterations": best[0]})
+    return first, last, time.time() - t0, history
 
 
 def evaluate(ctx, grid, coef_of_seed, seeds, tol=1e-8, precond=gpz.GPZ_PRECOND_JACOBI):
@@ -103,18 +131,19 @@ def main(argv=None):
     ap.add_argument("--eval", type=int, default=5, help="evaluation fields (seeds 10000..)")
     ap.add_argument("--eval-n", type=int, default=0, help="evaluate on another grid size (0: the training size)")
     ap.add_argument("--block", action="store_true", help="also evaluate against block-Jacobi PCG")
+    ap.add_argument("--val-every", type=int, default=50, help="validation (checkpoint selection) interval in fields")
     ap.add_argument("--out", default="")
     a = ap.parse_args(argv)
     grid, coef = WORKLOADS[a.workload](a.n, a.p)
     ctx = context_for(grid, a.rank, a.init_seed)
-    first, last, secs = train(ctx, grid, coef, range(1, a.fields + 1), a.steps, a.lr, a.pairs,
-                              log_every=max(1, a.fields // 10))
+    first, last, secs, hist = train(ctx, grid, coef, range(1, a.fields + 1), a.steps, a.lr, a.pairs,
+                                    log_every=max(1, a.fields // 10), val_every=a.val_every)
     params = ctx.learned_params()
     if a.out:
         os.makedirs(os.path.dirname(os.path.abspath(a.out)), exist_ok=True)
         np.save(a.out, params)
     res = dict(workload=a.workload, n=a.n, p=a.p, fields=a.fields, steps=a.steps, lr=a.lr, pairs=a.pairs,
-               rank=a.rank, loss_first=first, loss_last=last, train_seconds=round(secs, 1))
+               rank=a.rank, loss_first=first, loss_last=last, train_seconds=round(secs, 1), validation=hist)
     if a.eval:
         if a.eval_n and a.eval_n != a.n:
             ctx.close()

@@ -280,6 +280,24 @@ def elasticity3d(n, p=2, E=None, nu=0.3, top_traction=True, side_bc=False):
     return OracleMesh(3, (n, n, n), (0, 0, 0), (1, 1, 1), matids, True, p, mats, bcs, elem_coef=E)
 
 
+def elasticity3d_hp(n, orders, E=None, nu=0.3):
+    """hp elasticity: unit cube n^3 hexes, preferred order orders[e] per element (shared sides take the
+    largest), body force (0,0,-1), clamped z=0 face; E per element (array) or 1."""
+    mats = [material(1, ORC_ELAST3D, 3, E=1.0, nu=nu, force=(0, 0, -1.0), forcing=ORC_F_CONST)]
+    bcs = [bc(-1, 1, 0)]
+    matids = [1, -1, -2, -2, -2, -2, -2]
+    return OracleMesh(3, (n, n, n), (0, 0, 0), (1, 1, 1), matids, True, 1, mats, bcs, elem_coef=E,
+                      elem_order=np.ascontiguousarray(orders, np.int32))
+
+
+def darcy_hp(n, orders, perm, rhs=1.0):
+    """hp Darcy on the unit square, n x n quads of preferred orders orders[e], u = 0 on the boundary."""
+    mats = [material(1, ORC_DARCY, 2, forcing=ORC_F_CONST, force=(rhs, 0, 0))]
+    bcs = [bc(-1, 1, 0)]
+    return OracleMesh(2, (n, n), (0, 0, 0), (1, 1, 0), [1, -1, -1, -1, -1], True, 1, mats, bcs, elem_coef=perm,
+                      elem_order=np.ascontiguousarray(orders, np.int32))
+
+
 def darcy(dim, n, p, perm, rhs=1.0):
     """-div(k grad u) = rhs on the unit square/cube with u = 0 penalty Dirichlet on every face."""
     mats = [material(1, ORC_DARCY, dim, forcing=ORC_F_CONST, force=(rhs, 0, 0))]

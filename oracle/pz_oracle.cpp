@@ -736,7 +736,29 @@ static void build_comp(Mesh &m) {
     }
     m.cels.push_back(c);
   }
+  // hp: the harness sets every shared side to the largest preferred order of the
+  // volume elements on it (TPZCompElH1::SetSideOrder, Mesh/TPZCompElH1.cpp:165-208,
+  // which resizes the connect's block)
+  if (!m.elorder.empty()) {
+    std::vector<int> mx(m.conn_order.size(), 0);
+    for (const CompEl &c : m.cels)
+      if (!c.is_bc)
+        for (int s = ncorner(c.type); s < nsides(c.type); s++) mx[c.conn[s]] = std::max(mx[c.conn[s]], c.order);
+    for (size_t i = 0; i < mx.size(); i++)
+      if (m.conn_dim[i] > 0 && mx[i] > 0) m.conn_order[i] = mx[i];
+    for (const CompEl &c : m.cels)
+      for (int s = 0; s < nsides(c.type); s++) {
+        int64_t ci = c.conn[s];
+        m.conn_nshape[ci] = nconnect_shape(c.type, s, m.conn_order[ci]);
+      }
+  }
 }
+
+// TPZInterpolatedElement::MaxOrder: the largest order of the element's connects.
+// SetSideOrder calls AdjustIntegrationRule (Mesh/pzinterpolationspace.cpp:69-83) on
+// every element at a side whose order changed, so the integration order of an hp
+// element is IntegrationRuleOrder(MaxOrder); for uniform p it is that of p.
+static int max_order(const Mesh &m, const CompEl &c);
 
 static void init_blocks(Mesh &m) {
   int64_t nb = (int64_t)m.conn_order.size();
@@ -759,6 +781,12 @@ static int element_dest(const Mesh &m, const CompEl &c, int64_t *dest) {
     for (int64_t k = 0; k < m.block_size[ci]; k++) dest[n++] = m.block_pos[ci] + k;
   }
   return n;
+}
+
+static int max_order(const Mesh &m, const CompEl &c) {
+  int mo = 1;
+  for (int s = 0; s < nsides(c.type); s++) mo = std::max(mo, m.conn_order[c.conn[s]]);
+  return mo;
 }
 
 static void side_orders_of(const Mesh &m, const CompEl &c, int *orders) {
@@ -839,8 +867,9 @@ static int calc_stiff(const Mesh &m, const CompEl &c, double *ek, double *ef) {
   double coords[8 * 3];
   for (int k = 0; k < NC; k++)
     for (int j = 0; j < 3; j++) coords[k * 3 + j] = m.nodes[g.nodes[k] * 3 + j];
-  // integration order (TPZIntelGen ctor, Mesh/pzelctemp.cpp:36-47; TPZMatSingleSpace.cpp:61-72)
-  int porder = c.order;
+  // integration order (TPZIntelGen ctor, Mesh/pzelctemp.cpp:36-47; TPZMatSingleSpace.cpp:61-72),
+  // of MaxOrder after the hp side orders are set
+  int porder = max_order(m, c);
   int intorder;
   const orc_material *vm = c.is_bc ? &m.spec.mats[find_mat(m, m.spec.bcs[c.mat].matid)] : &m.spec.mats[c.mat];
   if (!c.is_bc && vm->kind == ORC_ELAST3D) {

@@ -64,24 +64,14 @@ def test_learned_gradient_matches_oracle(g):
     ctx.close()
 
 
-def _train(g, ctx, grid, n, seeds, steps=8, lr=3e-3, npairs=16):
-    first = last = None
-    for s in seeds:
-        ctx.set_coef(grid, g.grf2d(n, seed=s))
-        ctx.assemble()
-        ctx.learned_collect(npairs=npairs, tol=1e-12)
-        l0, l1 = ctx.learned_train(steps=steps, lr=lr)
-        first = l0 if first is None else first
-        last = l1
-    return first, last
-
-
 def test_learned_training_gains_over_jacobi(g):
     n = 64
     grid = g.darcy(2, n, 2, g.grf2d(n, seed=0))
     ctx = _ctx(g, grid)
     ctx.learned_init(rank=4, seed=0)
-    first, last = _train(g, ctx, grid, n, range(1, 41))
+    from neopz_gb300 import learned
+    first, last, _, hist = learned.train(ctx, grid, lambda s: g.grf2d(n, seed=s), range(1, 41), val_every=10)
+    assert hist[-1]["kept_fields"] in (10, 20, 30, 40)
     assert last < 0.95 * first, (first, last)  # per-field losses differ; the iteration gain below is the test
     for s in (10000, 10001, 10002):
         k = g.grf2d(n, seed=s)

@@ -47,6 +47,9 @@ def _cases():
     k2 = np.exp(rng.standard_normal(16 * 16))
     k3 = np.exp(rng.standard_normal(4 ** 3))
     E3 = np.exp(rng.standard_normal(3 ** 3))
+    o3, o2 = g.hp_orders(27, 3), g.hp_orders(36, 5)
+    E3h = np.exp(0.5 * rng.standard_normal(27))
+    k2h = np.exp(rng.standard_normal(36))
     return {
         "poisson2d_p1": (lambda: O.poisson2d(16, 1), lambda: g.poisson2d(16, 1)),
         "poisson2d_p2": (lambda: O.poisson2d(16, 2), lambda: g.poisson2d(16, 2)),
@@ -56,11 +59,14 @@ def _cases():
         "elast3d_p1": (lambda: O.elasticity3d(3, 1, E=E3), lambda: g.elasticity3d(3, 1, E=E3)),
         "elast3d_p2": (lambda: O.elasticity3d(3, 2, E=E3), lambda: g.elasticity3d(3, 2, E=E3)),
         "elast3d_p3": (lambda: O.elasticity3d(2, 3), lambda: g.elasticity3d(2, 3)),
+        # hp: per-element orders in {1,2,3}, shared sides at the largest (batched run-time kernels)
+        "elast3d_hp": (lambda: O.elasticity3d_hp(3, o3, E=E3h), lambda: g.elasticity3d_hp(3, o3, E=E3h)),
+        "darcy2d_hp": (lambda: O.darcy_hp(6, o2, k2h), lambda: g.darcy_hp(6, o2, k2h)),
     }
 
 
 CASES = ["poisson2d_p1", "poisson2d_p2", "poisson2d_p3", "darcy2d_p2", "darcy3d_p2", "elast3d_p1", "elast3d_p2",
-         "elast3d_p3"]
+         "elast3d_p3", "elast3d_hp", "darcy2d_hp"]
 
 
 @pytest.fixture(scope="module")
@@ -96,7 +102,8 @@ def test_pattern_matrix_rhs(built, case, sym):
     ctx.close()
 
 
-@pytest.mark.parametrize("case", ["poisson2d_p2", "darcy2d_p2", "elast3d_p2", "elast3d_p3"])
+@pytest.mark.parametrize("case", ["poisson2d_p2", "darcy2d_p2", "elast3d_p2", "elast3d_p3", "elast3d_hp",
+                                  "darcy2d_hp"])
 def test_jacobi_pcg_matches_oracle(built, case):
     g = _gpz()
     mk_o, mk_g = built[case]
@@ -131,7 +138,7 @@ def test_jacobi_pcg_graph_and_eager_agree(built):
     ctx.close()
 
 
-@pytest.mark.parametrize("case", ["poisson2d_p2", "elast3d_p2", "darcy3d_p2"])
+@pytest.mark.parametrize("case", ["poisson2d_p2", "elast3d_p2", "darcy3d_p2", "elast3d_hp"])
 def test_mixed_cg_reaches_true_fp64_residual(built, case):
     g = _gpz()
     mk_o, mk_g = built[case]
@@ -155,7 +162,7 @@ def test_mixed_cg_reaches_true_fp64_residual(built, case):
     ctx.close()
 
 
-@pytest.mark.parametrize("case", ["elast3d_p1", "elast3d_p2"])
+@pytest.mark.parametrize("case", ["elast3d_p1", "elast3d_p2", "elast3d_hp"])
 def test_block_jacobi_pcg_matches_oracle(built, case):
     """Connect-block (3x3) Jacobi CG against the oracle's TPZBlockDiagonal-preconditioned CG."""
     g = _gpz()
@@ -260,4 +267,43 @@ def test_gmres_graph_eager_budget_and_block_jacobi(built):
     ref = O.cg_jacobi(False, oia, oja, oa, of, 20000, 1e-12)
     for s in (s1, s4):
         assert np.linalg.norm(s["x"] - ref["x"]) <= 1e-8 * np.linalg.norm(ref["x"])
+    ctx.close()
+
+
+def test_hp_batching_uses_classes_and_autotuner(built):
+    """Elements of uneven side orders are assembled by the hp classes (run-time kernel, block size
+    autotuned once), uniform ones by their compile-time buckets; the autotuned block size does not change
+    the assembled values."""
+    g = _gpz()
+    grid = built["elast3d_hp"][1]()
+    ctx = g.Context(0)
+    ctx.upload_mesh(grid)
+    ctx.build_pattern(False)
+    ctx.assemble()
+    rep = ctx.assembly_report()
+    assert rep["hp_classes"] >= 1 and rep["hp_elements"] >= 1
+    assert rep["hp_block_size_ms"]["chosen"] in (64, 128, 256)
+    a1 = ctx.matrix()
+    ctx.assemble()
+    assert np.array_equal(a1, ctx.matrix())
+    ctx.close()
+
+
+@pytest.mark.parametrize("case", ["poisson2d_p2", "elast3d_p2", "elast3d_hp"])
+def test_rhs_only_assembly(built, case):
+    """TPZStructMatrix::Assemble(rhs): the load vector without the matrix, identical to the full assembly's,
+    and to the oracle's within 1e-12; also before any pattern exists."""
+    g = _gpz()
+    mk_o, mk_g = built[case]
+    om, grid = mk_o(), mk_g()
+    ctx = g.Context(0)
+    ctx.upload_mesh(grid)
+    ctx.assemble_rhs()
+    f0 = ctx.rhs()
+    ctx.build_pattern(True)
+    ctx.assemble()
+    assert np.array_equal(f0, ctx.rhs())
+    oia, oja = om.pattern(True)
+    _, of = om.assemble(True, oia, oja)
+    assert np.max(np.abs(f0 - of)) <= 1e-12 * np.max(np.abs(of))
     ctx.close()

@@ -32,6 +32,16 @@ def _same_numbering(om, grid):
         assert np.array_equal(om.cel(e)["dest"], grid.dest(e)), e
 
 
+def test_numbering_hp(g):
+    """hp meshes (per-element orders, shared sides at the largest order): same equations per element."""
+    E = np.exp(0.5 * np.random.default_rng(4).standard_normal(27))
+    orders = g.hp_orders(27, 3)
+    _same_numbering(O.elasticity3d_hp(3, orders, E=E), g.elasticity3d_hp(3, orders, E=E))
+    o2 = g.hp_orders(36, 5)
+    k = np.exp(np.random.default_rng(1).standard_normal(36))
+    _same_numbering(O.darcy_hp(6, o2, k), g.darcy_hp(6, o2, k))
+
+
 @pytest.mark.parametrize("n,p", [(4, 1), (6, 2), (5, 3)])
 def test_numbering_2d(g, n, p):
     _same_numbering(O.poisson2d(n, p), g.poisson2d(n, p))
