@@ -45,6 +45,7 @@ def parse():
     ap.add_argument("--no-e2e", action="store_true", help="skip the end-to-end C-ABI leg")
     ap.add_argument("--no-learned", action="store_true", help="skip the learned-preconditioner (2D Darcy) leg")
     ap.add_argument("--no-hp", action="store_true", help="skip the hp (uneven-order) assembly leg")
+    ap.add_argument("--hp-n", type=int, default=40, help="hexes per direction of the hp leg")
     return ap.parse_args()
 
 
@@ -272,7 +273,7 @@ def run_gpu(args):
     if rank == 0 and not args.no_learned:
         out["learned_darcy2d"] = learned_leg(gpz, dev)
     if rank == 0 and not args.no_hp:
-        out["hp_elasticity"] = hp_leg(gpz, dev)
+        out["hp_elasticity"] = hp_leg(gpz, dev, args.hp_n)
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         out["cpu_baseline"] = cpu_baseline(fp64["iterations"], n)
     if rank == 0:
@@ -325,19 +326,26 @@ def learned_leg(gpz, dev, n=256, seeds=(10000, 10001, 10002)):
         for _ in range(2):  # the second of each is timed (graphs instantiated, caches warm)
             jac = ctx.solve(tol=TOL, max_iter=200000, want_x=False)
             lrn = ctx.solve(solver=gpz.GPZ_SOLVER_LEARNED_FCG, tol=TOL, max_iter=200000, want_x=False)
-        assert lrn["rc"] == 0 and lrn["true_resid"] <= TOL
+            lmx = ctx.solve(solver=gpz.GPZ_SOLVER_LEARNED_MIXED_FCG, tol=TOL, max_iter=200000, reliable_delta=1e-2,
+                            want_x=False)
+        assert lrn["rc"] == 0 and lrn["true_resid"] <= TOL and lmx["rc"] == 0 and lmx["true_resid"] <= TOL
         rows.append(dict(seed=s, jacobi_iterations=jac["iterations"], jacobi_s=round(jac["seconds"], 6),
                          learned_iterations=lrn["iterations"], learned_s=round(lrn["seconds"], 6),
-                         learned_true_resid=lrn["true_resid"], jacobi_fallbacks=lrn["restarts"]))
+                         learned_true_resid=lrn["true_resid"], jacobi_fallbacks=lrn["restarts"],
+                         learned_mixed_iterations=lmx["iterations"], learned_mixed_s=round(lmx["seconds"], 6),
+                         learned_mixed_true_resid=lmx["true_resid"],
+                         learned_mixed_reliable_updates=lmx["reliable_updates"]))
     ctx.close()
     tj = sum(r["jacobi_s"] for r in rows)
     tl = sum(r["learned_s"] for r in rows)
+    tm = sum(r["learned_mixed_s"] for r in rows)
     return {"workload": f"2D Darcy {n}^2 Q2 quads, k = exp(GRF sigma 1.5, correlation 0.1), unseen seeds "
                         f"{seeds[0]}..{seeds[-1]}, tol {TOL} (true FP64 residual)",
             "weights": "neopz_gb300/data/learned_darcy2d_q2.npy (trained on the GPU: 2000 fields, checkpoint selected on validation fields)",
             "fields": rows, "iterations_ratio": round(sum(r["learned_iterations"] for r in rows) /
                                                       sum(r["jacobi_iterations"] for r in rows), 3),
-            "speedup_vs_fp64_jacobi_pcg": round(tj / tl, 3)}
+            "speedup_vs_fp64_jacobi_pcg": round(tj / tl, 3),
+            "learned_mixed_speedup_vs_fp64_jacobi_pcg": round(tj / tm, 3)}
 
 
 def cpu_sample(n_sample, iters_full, n_full, threads, cg_iters=30):

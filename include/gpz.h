@@ -168,7 +168,9 @@ int gpz_spmv(gpz_ctx *ctx, double alpha, const double *x, double beta, const dou
 #define GPZ_SOLVER_CG 1            /* Solvers/LinearSolvers/cg.h:29-132 */
 #define GPZ_SOLVER_GMRES 2         /* Solvers/LinearSolvers/gmres.h:68-168 */
 #define GPZ_SOLVER_MIXED_CG 3      /* FP32-value SpMV CG, FP64 x/dots, reliable FP64 residual updates */
-#define GPZ_SOLVER_LEARNED_FCG 4   /* flexible CG with the learned correction + Jacobi, FP64 residual */
+#define GPZ_SOLVER_LEARNED_FCG 4   /* flexible CG with the learned preconditioner (gpz_learned_*), FP64 */
+#define GPZ_SOLVER_LEARNED_MIXED_FCG 5 /* the same with FP32-value SpMV, FP64 x/r/dots and true-residual
+                                          replacement (reliable_delta); scalar problems */
 #define GPZ_PRECOND_JACOBI 1       /* TPZMatrix::SolveJacobi, one sweep (Matrix/pzmatrix.cpp:643-667) */
 #define GPZ_PRECOND_BLOCK_JACOBI 2 /* connect blocks, TPZBlockDiagonal (Matrix/pzblockdiag.h:21) */
 

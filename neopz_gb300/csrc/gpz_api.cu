@@ -8,7 +8,13 @@ namespace gpz {
 void solver_prepare(Ctx &c, bool mixed);
 double time_spmv(Ctx &c, bool f32, int reps);
 
+void drop_assembly_graph(Ctx &c) {
+  if (c.asm_graph) cudaGraphExecDestroy(c.asm_graph);
+  c.asm_graph = nullptr;
+}
+
 Ctx::~Ctx() {
+  drop_assembly_graph(*this);
   for (Bucket *b : buckets) delete b;
   buckets.clear();
 }
@@ -162,6 +168,7 @@ int gpz_mesh_upload(gpz_ctx *ctx, const gpz_mesh_desc *d) {
     build_buckets(c, *d);
     c.have_mesh = true;
     c.have_pattern = c.have_matrix = c.have_solution = c.have_a32 = c.have_bjinv = c.have_rhs = false;
+    drop_assembly_graph(c);
     return GPZ_OK;
   });
 }
@@ -170,8 +177,10 @@ int gpz_mesh_set_coef(gpz_ctx *ctx, const double *el_coef) {
   return guarded(ctx, [&](Ctx &c) {
     GPZ_REQUIRE(c.have_mesh, GPZ_E_NOT_READY, "no mesh");
     GPZ_REQUIRE(el_coef, GPZ_E_INVALID, "null coefficients");
+    const double *before = c.d_coef.p;
     c.d_coef.upload(el_coef, c.nel, c.stream);
     c.have_matrix = c.have_solution = c.have_rhs = false;
+    if (c.d_coef.p != before) drop_assembly_graph(c);  // the captured kernels hold the coefficient pointer
     GPZ_CUDA_TRY(cudaStreamSynchronize(c.stream));
     return GPZ_OK;
   });
@@ -186,6 +195,7 @@ int gpz_pattern_build(gpz_ctx *ctx, int sym, int64_t *nnz_out) {
     c.user_sym = sym ? 1 : 0;
     c.have_pattern = true;
     c.spmv32_tuned = -1;  // a new pattern is tuned again at its first mixed assembly
+    drop_assembly_graph(c);
     c.have_matrix = false;
     if (nnz_out) *nnz_out = sym ? c.nnz_upper : c.nnz;
     return GPZ_OK;
@@ -211,6 +221,7 @@ int gpz_pattern_upload(gpz_ctx *ctx, int sym, int64_t neq, const int64_t *IA, co
     c.user_sym = 0;
     c.have_pattern = true;
     c.spmv32_tuned = -1;  // a new pattern is tuned again at its first mixed assembly
+    drop_assembly_graph(c);
     c.have_matrix = false;
     return GPZ_OK;
   });

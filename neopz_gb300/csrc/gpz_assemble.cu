@@ -654,7 +654,7 @@ ElemArgs args_of(Ctx &c, const Bucket *b) {
 
 // element integration + scatter of every bucket, colour by colour; the hp
 // classes run with `threads` (0: the class's tuned block size)
-void launch_elements(Ctx &c, int threads, bool rhs_only = false) {
+void launch_elements(Ctx &c, int threads, bool rhs_only = false, bool set_attrs = true) {
   cudaStream_t s = c.stream;
   for (int col = 0; col < c.ncolours; col++) {
     for (Bucket *b : c.buckets) {
@@ -675,7 +675,8 @@ void launch_elements(Ctx &c, int threads, bool rhs_only = false) {
       } else {
         k = select_kernel(b->key.type, b->nshape, c.nstate, b->key.is_bc);
       }
-      if (sh > 48 * 1024) GPZ_CUDA_TRY(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sh));
+      if (sh > 48 * 1024 && set_attrs)
+        GPZ_CUDA_TRY(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sh));
       k<<<(unsigned)(e1 - e0), nt, sh, s>>>(P, H, b->d_elems.p + e0, e1 - e0);
       c.launches++;
       GPZ_CUDA_TRY(cudaGetLastError());
@@ -726,12 +727,33 @@ void assemble_fp64(Ctx &c) {
       }
     c.asm_tune_report = rep + ", \"chosen\": " + std::to_string(best_t) + "}";
   }
-  c.d_a.zero(s);
-  c.d_f.zero(s);
-  launch_elements(c, 0);
   c.d_dinv.alloc(std::max<int64_t>(c.neq, 1));
-  k_extract_diag<<<grid_for(c.neq, 256), 256, 0, s>>>(c.d_a.p, c.d_diagpos.p, c.neq, c.d_dinv.p);
-  c.launches++;
+  auto body = [&](bool set_attrs) {
+    c.d_a.zero(s);
+    c.d_f.zero(s);
+    launch_elements(c, 0, false, set_attrs);
+    k_extract_diag<<<grid_for(c.neq, 256), 256, 0, s>>>(c.d_a.p, c.d_diagpos.p, c.neq, c.d_dinv.p);
+    c.launches++;
+    GPZ_CUDA_TRY(cudaGetLastError());
+  };
+  if (c.asm_graph) {
+    // same pattern and buffers: replay the captured assembly
+    GPZ_CUDA_TRY(cudaGraphLaunch(c.asm_graph, s));
+    c.launches += c.asm_graph_launches;
+  } else {
+    // first assembly of this pattern runs eagerly (kernel attributes set, hp
+    // block sizes tuned); its launch sequence is then captured for the next ones
+    body(true);
+    const int64_t l0 = c.launches;
+    cudaGraph_t g;
+    GPZ_CUDA_TRY(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+    body(false);
+    GPZ_CUDA_TRY(cudaStreamEndCapture(s, &g));
+    c.asm_graph_launches = c.launches - l0;
+    c.launches = l0;
+    GPZ_CUDA_TRY(cudaGraphInstantiate(&c.asm_graph, g, 0));
+    GPZ_CUDA_TRY(cudaGraphDestroy(g));
+  }
   GPZ_CUDA_TRY(cudaGetLastError());
   c.have_a32 = false;
   c.have_bjinv = false;

@@ -163,6 +163,8 @@ struct Ctx {
   DBuf<int64_t> d_el_nodes, d_el_conn, d_block_pos;
   DBuf<int32_t> d_el_type, d_el_mat, d_block_size, d_conn_order;
   std::vector<Bucket *> buckets;
+  cudaGraphExec_t asm_graph = nullptr;       // captured assembly of the current pattern (replayed)
+  int64_t asm_graph_launches = 0;
   std::string asm_tune_report;               // block-size timings of the hp element kernels
   int ncolours = 0;
   DBuf<int> d_err;                           // device-side check flag

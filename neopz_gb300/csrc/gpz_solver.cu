@@ -1404,7 +1404,7 @@ __global__ void __launch_bounds__(kThreads) k_gm_add_r(double *__restrict__ x, G
 // I_RESTART carries that choice to the direction update and I_NRESTART counts it.
 __global__ void __launch_bounds__(kThreads) k_fcg_update(double *__restrict__ x, double *__restrict__ r,
                                                          float *__restrict__ r32, const double *__restrict__ p,
-                                                         const double *__restrict__ q, int64_t n, Red R) {
+                                                         const double *__restrict__ q, int64_t n, int mixed, Red R) {
   if (!active(R.iscal)) return;
   const double alpha = R.scal[S_ALPHA];
   double rr = 0.0;
@@ -1423,20 +1423,54 @@ __global__ void __launch_bounds__(kThreads) k_fcg_update(double *__restrict__ x,
     s[S_RR] = tot[0];
     s[S_RESID] = resid;
     is[I_IT] += 1;
+    if (tot[0] > s[S_MAXRR]) s[S_MAXRR] = tot[0];
     if (!(s[S_PQ] > 0.0) || !isfinite(resid)) {
       is[I_BREAK] = 1;
       is[I_CONV] = 2;
-    } else if (resid <= s[S_TOL]) {
-      is[I_CONV] = 1;
+    } else if (!mixed) {
+      if (resid <= s[S_TOL]) is[I_CONV] = 1;
+    } else if (resid <= s[S_TOL] || tot[0] < s[S_DELTA2] * s[S_MAXRR]) {
+      is[I_UPDATE] = 1;  // the FP32-value q has drifted r: replace it by b - A64 x (k_reliable)
     }
   }
 }
 
-template <class T>
-__global__ void __launch_bounds__(kThreads) k_fcg_t(LnView L, const T *__restrict__ r, Red R) {
+// q = A32 p32 (FP32 values and accumulation, the mixed learned flexible CG), p.q in FP64
+template <int TPR>
+__global__ void __launch_bounds__(kThreads) k_lfcg_spmv(const int64_t *__restrict__ ia, const int32_t *__restrict__ ja,
+                                                        const float *__restrict__ a32, const float *__restrict__ p32,
+                                                        const double *__restrict__ p, double *__restrict__ q, int64_t n,
+                                                        Red R) {
   if (!active(R.iscal)) return;
-  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < L.E * L.R; i += (int64_t)gridDim.x * blockDim.x)
-    ln_elem_t<T>(L, r, i);
+  double pq = 0.0;
+  GPZ_ROW_LOOP(TPR, n) {
+    const int64_t i = r0 + (threadIdx.x & 31) / TPR;
+    const bool valid = i < n;
+    const float sv = row_dot32<TPR>(ia, ja, a32, p32, i, sub, valid);
+    if (sub == 0 && valid) {
+      const double qi = (double)sv;
+      q[i] = qi;
+      pq += p[i] * qi;
+    }
+  }
+  double v[1] = {pq}, tot[1];
+  if (grid_reduce<1>(v, R, tot) && threadIdx.x == 0) {
+    R.scal[S_PQ] = tot[0];
+    R.scal[S_ALPHA] = R.scal[S_RHO] / tot[0];
+    R.iscal[I_SP32]++;
+  }
+}
+
+// reads the FP32 copy of r written by the update, or the FP64 r when it was
+// just (re)computed (start, residual replacement: I_UPDATE == 2)
+__global__ void __launch_bounds__(kThreads) k_fcg_t(LnView L, const double *__restrict__ r64,
+                                                    const float *__restrict__ r32, Red R) {
+  if (!active(R.iscal)) return;
+  const bool fresh = R.iscal[I_UPDATE] == 2;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < L.E * L.R; i += (int64_t)gridDim.x * blockDim.x) {
+    if (fresh) ln_elem_t<double>(L, r64, i);
+    else ln_elem_t<float>(L, r32, i);
+  }
 }
 
 __global__ void __launch_bounds__(kThreads) k_fcg_z(LnView L, const double *__restrict__ r,
@@ -1445,7 +1479,7 @@ __global__ void __launch_bounds__(kThreads) k_fcg_z(LnView L, const double *__re
   if (!active(R.iscal)) return;
   const bool first = R.iscal[I_IT] == 0;
   const double alpha = exp((double)*L.loga);
-  double zr = 0.0, zq = 0.0, jr = 0.0, jq = 0.0;
+  double zr = 0.0, zq = 0.0, jr = 0.0, jq = 0.0;  // jr, jq: the Jacobi fallback's dots (FP64: its beta)
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < L.n; i += (int64_t)gridDim.x * blockDim.x) {
     const double zi = ln_node_z<double>(L, r, alpha, i);
     const double ri = r[i];
@@ -1468,19 +1502,22 @@ __global__ void __launch_bounds__(kThreads) k_fcg_z(LnView L, const double *__re
     if (!ok) is[I_NRESTART] += 1;
     s[S_RHO] = ok ? tot[0] : tot[2];
     s[S_BETA] = first ? 0.0 : -(ok ? tot[1] : tot[3]) / s[S_PQ];
+    if (is[I_UPDATE] == 2) is[I_UPDATE] = 0;
   }
 }
 
 __global__ void __launch_bounds__(kThreads) k_fcg_p(const double *__restrict__ z, const double *__restrict__ r,
-                                                    const double *__restrict__ dinv, double *__restrict__ p, int64_t n,
-                                                    Red R) {
+                                                    const double *__restrict__ dinv, double *__restrict__ p,
+                                                    float *__restrict__ p32, int64_t n, Red R) {
   if (!active(R.iscal)) return;
   const bool jac = R.iscal[I_RESTART] != 0;
   const bool first = R.iscal[I_IT] == 0;
   const double beta = R.scal[S_BETA];
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
     const double zi = jac ? dinv[i] * r[i] : z[i];
-    p[i] = first ? zi : zi + beta * p[i];
+    const double pi = first ? zi : zi + beta * p[i];
+    p[i] = pi;
+    if (p32) p32[i] = (float)pi;
   }
 }
 
@@ -1974,12 +2011,24 @@ int solve_gmres(Ctx &c, const gpz_solver_opts &o, gpz_solve_report &rep) {
 // stopping rule is the reference's (recursive ||r||/||b|| <= tol, cg.h:100);
 // afterwards the true FP64 residual is recomputed and, if it misses the
 // tolerance, the solve restarts from the current x (at most three times).
-int solve_learned(Ctx &c, const gpz_solver_opts &o, gpz_solve_report &rep) {
+// mixed: q = A32 p32 with FP32 values (scalar problems: the FP32 CSR copy),
+// FP64 x, r, z, dots and scalars; when ||r|| has dropped by reliable_delta (or
+// meets the tolerance) r is replaced by b - A64 x in FP64, and the solve stops
+// only on that true residual.
+int solve_learned(Ctx &c, const gpz_solver_opts &o, gpz_solve_report &rep, bool mixed) {
   learned_prepare(c);
-  alloc_work(c, false);
+  if (mixed) {
+    if (!c.have_a32) make_fp32_copy(c);
+    GPZ_REQUIRE(!c.have_bsr3, GPZ_E_INVALID,
+                "mixed learned flexible CG needs the FP32 CSR copy (scalar problems, nstate 1)");
+  }
+  alloc_work(c, mixed);
   SolverWork &w = c.sw;
   w.z.alloc(std::max<int64_t>(c.neq, 1));
   w.r32.alloc(std::max<int64_t>(c.neq, 1));
+  w.pm.alloc(std::max<int64_t>(c.neq, 1));
+  const int tpr32 = pick_tpr32(c.nnz, c.neq);
+  float *p32 = mixed ? w.pm.p : nullptr;
   cudaStream_t s = c.stream;
   const int tpr = pick_tpr(c.nnz, c.neq);
   const LnView L = learned_view(c);
@@ -1989,22 +2038,34 @@ int solve_learned(Ctx &c, const gpz_solver_opts &o, gpz_solve_report &rep) {
   GPZ_CUDA_TRY(cudaEventCreate(&ev0));
   GPZ_CUDA_TRY(cudaEventCreate(&ev1));
   GPZ_CUDA_TRY(cudaEventRecord(ev0, s));
+  const int per_iter = mixed ? 6 : 5;
   auto iteration = [&]() {
-    GPZ_TPR_SWITCH(tpr, (k_cg_spmv<T, false><<<wave(k_cg_spmv<T, false>), kThreads, 0, s>>>(
-                            c.d_ia.p, c.d_ja.p, c.d_a.p, nullptr, w.p.p, nullptr, w.q.p, c.neq, R)));
-    k_fcg_update<<<wave(k_fcg_update), kThreads, 0, s>>>(w.x.p, w.r.p, w.r32.p, w.p.p, w.q.p, c.neq, R);
-    k_fcg_t<float><<<wave(k_fcg_t<float>), kThreads, 0, s>>>(L, w.r32.p, R);
+    if (mixed) {
+      GPZ_TPR_SWITCH(tpr32, (k_lfcg_spmv<T><<<wave(k_lfcg_spmv<T>), kThreads, 0, s>>>(
+                                c.d_ia.p, c.d_ja.p, c.d_a32.p, p32, w.p.p, w.q.p, c.neq, R)));
+    } else {
+      GPZ_TPR_SWITCH(tpr, (k_cg_spmv<T, false><<<wave(k_cg_spmv<T, false>), kThreads, 0, s>>>(
+                              c.d_ia.p, c.d_ja.p, c.d_a.p, nullptr, w.p.p, nullptr, w.q.p, c.neq, R)));
+    }
+    k_fcg_update<<<wave(k_fcg_update), kThreads, 0, s>>>(w.x.p, w.r.p, w.r32.p, w.p.p, w.q.p, c.neq, mixed ? 1 : 0,
+                                                         R);
+    if (mixed)
+      GPZ_TPR_SWITCH(tpr, (k_reliable<T><<<wave(k_reliable<T>), kThreads, 0, s>>>(c.d_ia.p, c.d_ja.p, c.d_a.p,
+                                                                                    w.x.p, w.b.p, w.r.p, c.neq, R)));
+    k_fcg_t<<<wave(k_fcg_t), kThreads, 0, s>>>(L, w.r.p, w.r32.p, R);
     k_fcg_z<<<wave(k_fcg_z), kThreads, 0, s>>>(L, w.r.p, w.q.p, c.d_dinv.p, w.z.p, R);
-    k_fcg_p<<<wave(k_fcg_p), kThreads, 0, s>>>(w.z.p, w.r.p, c.d_dinv.p, w.p.p, c.neq, R);
-    c.launches += 5;
+    k_fcg_p<<<wave(k_fcg_p), kThreads, 0, s>>>(w.z.p, w.r.p, c.d_dinv.p, w.p.p, p32, c.neq, R);
+    c.launches += per_iter;
   };
   cudaGraphExec_t exec = nullptr;
-  int64_t total_it = 0, nfallback = 0, hstate[I_NISCAL] = {0};
+  int64_t total_it = 0, nfallback = 0, nupd = 0, nspmv64 = 0, hstate[I_NISCAL] = {0};
   double hs[S_NSCAL] = {0};
   int rc = GPZ_NOT_CONVERGED;
   for (int pass = 0; pass < 4; pass++) {
     for (int k = 0; k < S_NSCAL; k++) hs[k] = 0.0;
     hs[S_TOL] = o.tol;
+    hs[S_DELTA2] = (o.reliable_delta > 0 ? o.reliable_delta : 1e-2);
+    hs[S_DELTA2] *= hs[S_DELTA2];
     int64_t hi[I_NISCAL] = {0};
     hi[I_MAXIT] = o.max_iter - total_it;
     GPZ_CUDA_TRY(cudaMemcpyAsync(w.scal.p, hs, sizeof(hs), cudaMemcpyHostToDevice, s));
@@ -2012,9 +2073,9 @@ int solve_learned(Ctx &c, const gpz_solver_opts &o, gpz_solve_report &rep) {
     const int from_current = pass > 0 ? 1 : o.from_current;
     GPZ_TPR_SWITCH(tpr, (k_cg_init<T><<<wave(k_cg_init<T>), kThreads, 0, s>>>(c.d_ia.p, c.d_ja.p, c.d_a.p, w.x.p,
                                                                                w.b.p, w.r.p, c.neq, from_current, R)));
-    k_fcg_t<double><<<wave(k_fcg_t<double>), kThreads, 0, s>>>(L, w.r.p, R);
+    k_fcg_t<<<wave(k_fcg_t), kThreads, 0, s>>>(L, w.r.p, w.r32.p, R);  // k_cg_init leaves I_UPDATE = 2: FP64 r
     k_fcg_z<<<wave(k_fcg_z), kThreads, 0, s>>>(L, w.r.p, w.q.p, c.d_dinv.p, w.z.p, R);
-    k_fcg_p<<<wave(k_fcg_p), kThreads, 0, s>>>(w.z.p, w.r.p, c.d_dinv.p, w.p.p, c.neq, R);
+    k_fcg_p<<<wave(k_fcg_p), kThreads, 0, s>>>(w.z.p, w.r.p, c.d_dinv.p, w.p.p, p32, c.neq, R);
     c.launches += 4;
     GPZ_CUDA_TRY(cudaGetLastError());
     if (o.use_graph && !exec) {
@@ -2033,7 +2094,7 @@ int solve_learned(Ctx &c, const gpz_solver_opts &o, gpz_solve_report &rep) {
       if (hstate[I_CONV] != 0 || hstate[I_IT] >= hi[I_MAXIT]) break;
       if (exec) {
         GPZ_CUDA_TRY(cudaGraphLaunch(exec, s));
-        c.launches += (int64_t)batch * 5;
+        c.launches += (int64_t)batch * per_iter;
       } else {
         for (int i = 0; i < batch; i++) iteration();
       }
@@ -2047,6 +2108,8 @@ int solve_learned(Ctx &c, const gpz_solver_opts &o, gpz_solve_report &rep) {
     GPZ_CUDA_TRY(cudaStreamSynchronize(s));
     total_it += hstate[I_IT];
     nfallback += hstate[I_NRESTART];
+    nupd += hstate[I_NUPD];
+    nspmv64 += hstate[I_SP64];
     if (hstate[I_BREAK]) {
       rc = GPZ_E_BREAKDOWN;
       break;
@@ -2070,9 +2133,9 @@ int solve_learned(Ctx &c, const gpz_solver_opts &o, gpz_solve_report &rep) {
   rep.resid = hs[S_RESID];
   rep.true_resid = std::sqrt(hs[S_TRUERR]) / hs[S_NORMB];
   rep.seconds = ms * 1e-3;
-  rep.spmv_fp64 = total_it + 1;
-  rep.spmv_fp32 = 0;
-  rep.reliable_updates = 0;
+  rep.spmv_fp64 = mixed ? nspmv64 + 1 : total_it + 1;
+  rep.spmv_fp32 = mixed ? total_it : 0;
+  rep.reliable_updates = nupd;
   rep.restarts = nfallback;  // iterations that fell back to Jacobi
   c.have_solution = true;
   return rc;
@@ -2145,7 +2208,8 @@ int collect_cg_pairs(Ctx &c, int npairs, double tol, int64_t max_iter, double *R
 
 int solve(Ctx &c, const gpz_solver_opts &o, gpz_solve_report &rep) {
   if (o.solver == GPZ_SOLVER_GMRES) return solve_gmres(c, o, rep);
-  if (o.solver == GPZ_SOLVER_LEARNED_FCG) return solve_learned(c, o, rep);
+  if (o.solver == GPZ_SOLVER_LEARNED_FCG || o.solver == GPZ_SOLVER_LEARNED_MIXED_FCG)
+    return solve_learned(c, o, rep, o.solver == GPZ_SOLVER_LEARNED_MIXED_FCG);
   const bool mixed = o.solver == GPZ_SOLVER_MIXED_CG;
   GPZ_REQUIRE(o.solver == GPZ_SOLVER_CG || mixed, GPZ_E_INVALID, "solver kind not available");
   GPZ_REQUIRE(o.precond == GPZ_PRECOND_JACOBI || o.precond == GPZ_PRECOND_BLOCK_JACOBI || o.precond == 0,

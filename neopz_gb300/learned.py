@@ -110,7 +110,13 @@ def evaluate(ctx, grid, coef_of_seed, seeds, tol=1e-8, precond=gpz.GPZ_PRECOND_J
         ctx.assemble()
         base = ctx.solve(tol=tol, precond=precond, want_x=False)
         lrn = ctx.solve(solver=gpz.GPZ_SOLVER_LEARNED_FCG, tol=tol, want_x=False)
+        mixed = {}
+        if grid.desc.nstate == 1:  # learned + FP32-value SpMV (scalar problems)
+            m = ctx.solve(solver=gpz.GPZ_SOLVER_LEARNED_MIXED_FCG, tol=tol, reliable_delta=1e-2, want_x=False)
+            mixed = dict(learned_mixed_iterations=m["iterations"], learned_mixed_seconds=m["seconds"],
+                         learned_mixed_true_resid=m["true_resid"])
         out.append(dict(seed=s, base_precond="block_jacobi" if precond == gpz.GPZ_PRECOND_BLOCK_JACOBI else "jacobi",
+                        **mixed,
                         base_iterations=base["iterations"], base_seconds=base["seconds"],
                         learned_iterations=lrn["iterations"], learned_seconds=lrn["seconds"],
                         learned_true_resid=lrn["true_resid"], fallbacks=lrn["restarts"], rc=lrn["rc"]))
@@ -132,12 +138,16 @@ def main(argv=None):
     ap.add_argument("--eval-n", type=int, default=0, help="evaluate on another grid size (0: the training size)")
     ap.add_argument("--block", action="store_true", help="also evaluate against block-Jacobi PCG")
     ap.add_argument("--val-every", type=int, default=50, help="validation (checkpoint selection) interval in fields")
+    ap.add_argument("--weights", default="", help="start from these parameters (with --fields 0: evaluate only)")
     ap.add_argument("--out", default="")
     a = ap.parse_args(argv)
     grid, coef = WORKLOADS[a.workload](a.n, a.p)
-    ctx = context_for(grid, a.rank, a.init_seed)
-    first, last, secs, hist = train(ctx, grid, coef, range(1, a.fields + 1), a.steps, a.lr, a.pairs,
-                                    log_every=max(1, a.fields // 10), val_every=a.val_every)
+    ctx = context_for(grid, a.rank, a.init_seed, np.load(a.weights) if a.weights else None)
+    first = last = None
+    secs, hist = 0.0, []
+    if a.fields > 0:
+        first, last, secs, hist = train(ctx, grid, coef, range(1, a.fields + 1), a.steps, a.lr, a.pairs,
+                                        log_every=max(1, a.fields // 10), val_every=a.val_every)
     params = ctx.learned_params()
     if a.out:
         os.makedirs(os.path.dirname(os.path.abspath(a.out)), exist_ok=True)

@@ -6,7 +6,8 @@
 * training on the GPU lowers the loss, and the trained network gains over
   the method without it: flexible CG with the learned preconditioner needs at
   most 75% of the Jacobi-PCG iterations on unseen coefficient fields (64 x 64
-  Q2 Darcy, GRF permeability, 40 training fields), reaching
+  Q2 Darcy, GRF permeability, 40 training fields), also with the FP32-value
+  SpMV (learned + mixed), reaching
   the same true FP64 residual; at a tight tolerance its solution matches the
   oracle's CG solution within 1e-8;
 * Jacobi stays the fallback: with a broken network every iteration falls
@@ -82,12 +83,17 @@ def test_learned_training_gains_over_jacobi(g):
         assert jac["rc"] == 0 and lrn["rc"] == 0
         assert lrn["true_resid"] <= 1e-8 and lrn["restarts"] == 0
         assert lrn["iterations"] <= 0.75 * jac["iterations"], (s, lrn["iterations"], jac["iterations"])
+        # learned + mixed: FP32-value SpMV, FP64 true-residual replacement; same true tolerance
+        mx = ctx.solve(solver=g.GPZ_SOLVER_LEARNED_MIXED_FCG, tol=1e-8, reliable_delta=1e-2)
+        assert mx["rc"] == 0 and mx["true_resid"] <= 1e-8 and mx["spmv_fp32"] > 0 and mx["reliable_updates"] >= 1
+        assert mx["iterations"] <= 0.8 * jac["iterations"], (s, mx["iterations"], jac["iterations"])
         tight = ctx.solve(solver=g.GPZ_SOLVER_LEARNED_FCG, tol=1e-11)
         om = O.darcy(2, n, 2, k)
         oia, oja = om.pattern(True)
         oa, of = om.assemble(True, oia, oja)
         ref = O.cg_jacobi(True, oia, oja, oa, of, 20000, 1e-12)
         assert np.linalg.norm(tight["x"] - ref["x"]) <= 1e-8 * np.linalg.norm(ref["x"])
+        assert np.linalg.norm(mx["x"] - ref["x"]) <= 1e-5 * np.linalg.norm(ref["x"])  # true residual 1e-8
     ctx.close()
 
 

@@ -307,3 +307,30 @@ def test_rhs_only_assembly(built, case):
     _, of = om.assemble(True, oia, oja)
     assert np.max(np.abs(f0 - of)) <= 1e-12 * np.max(np.abs(of))
     ctx.close()
+
+
+def test_assembly_graph_replay(built):
+    """The second assembly of a pattern replays the captured CUDA graph: identical values; after new
+    coefficients, the replay equals a fresh context's eager assembly."""
+    g = _gpz()
+    n = 3
+    rng = np.random.default_rng(21)
+    E1, E2 = np.exp(rng.standard_normal(n ** 3)), np.exp(rng.standard_normal(n ** 3))
+    grid = g.elasticity3d(n, 2, E=E1)
+    ctx = g.Context(0)
+    ctx.upload_mesh(grid)
+    ctx.build_pattern(False)
+    ctx.assemble()
+    a1, f1 = ctx.matrix(), ctx.rhs()
+    ctx.assemble()
+    assert np.array_equal(a1, ctx.matrix()) and np.array_equal(f1, ctx.rhs())
+    ctx.set_coef(grid, E2)
+    ctx.assemble()
+    a2 = ctx.matrix()
+    fresh = g.Context(0)
+    fresh.upload_mesh(g.elasticity3d(n, 2, E=E2))
+    fresh.build_pattern(False)
+    fresh.assemble()
+    assert np.array_equal(a2, fresh.matrix())
+    fresh.close()
+    ctx.close()
