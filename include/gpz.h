@@ -162,6 +162,11 @@ int gpz_rhs_upload(gpz_ctx *ctx, const double *F);
  * Matrix/pzysmp.cpp:527-624):  z = alpha A x + beta y, host vectors. */
 int gpz_spmv(gpz_ctx *ctx, double alpha, const double *x, double beta, const double *y, double *z);
 
+/* y = A32 x with the FP32 operator of the mixed solvers (host FP64 vectors):
+ * the layout the SpMV autotuner chose, or `variant` (GPZ solver option
+ * spmv_variant, 0..5) for 3-state problems; the FP32 CSR copy otherwise. */
+int gpz_spmv_fp32(gpz_ctx *ctx, int variant, const double *x, double *y);
+
 /* ---- solve ----------------------------------------------------------------
  * TPZStepSolver::Solve (Solvers/pzstepsolver.cpp:64-169) with SetCG / SetGMRES
  * and a Jacobi (SetJacobi(1,0,0)) or block-Jacobi preconditioner. */
@@ -185,7 +190,8 @@ typedef struct {
   int32_t use_graph;       /* capture the iteration batch in a CUDA graph */
   int32_t from_current;    /* FromCurrent: start from x instead of zero */
   int32_t spmv_variant;    /* mixed CG: -1 = autotuned; 0 block CSR, 1 two rows in flight, 2 sliced ELL,
-                              3 TMA-staged block CSR, 4 upper triangle with float4 atomics */
+                              3 TMA-staged block CSR, 4 upper triangle with float4 atomics,
+                              5 matrix-free elements (uniform Q2 hex elasticity + penalty faces) */
 } gpz_solver_opts;
 
 typedef struct {

@@ -142,6 +142,21 @@ struct Learned {
   DBuf<double> aterm;                        // [P] alpha-gradient terms
 };
 
+// ---------------------------------------------------------------- matrix-free operator
+// Element records of the FP32 matrix-free elasticity operator (gpz_matfree.cu),
+// a candidate of the mixed CG's SpMV autotuner.
+struct MatFree {
+  bool ready = false;
+  int64_t nvol = 0, nface = 0;
+  DBuf<float> vxyz, vlm, vdphi, vw;          // volume: corners [n][8][3], (lambda, mu) [n][2], tables
+  DBuf<int32_t> vrows;                       // [n][27] block row of each shape
+  DBuf<float> fxyz, fphi, fdphi, fw;         // penalty faces
+  DBuf<int32_t> frows;
+  DBuf<double> energy;                       // the faces' share of p.q
+  float big = 0.f;
+  int grid_vol = 1, grid_face = 1;
+};
+
 // ---------------------------------------------------------------- the context
 struct Ctx {
   int device = 0;
@@ -217,6 +232,7 @@ struct Ctx {
   SolverWork sw;
   bool have_solution = false;
   Learned ln;
+  MatFree mf;
 
   ~Ctx();
 };
@@ -235,8 +251,12 @@ void build_block_jacobi(Ctx &c);
 // solver.cu
 void spmv_device(Ctx &c, const double *x, double *y, double alpha, double beta, const double *yin);
 int solve(Ctx &c, const gpz_solver_opts &o, gpz_solve_report &rep);
+void spmv32_apply(Ctx &c, int variant, const double *hx, double *hy);
 int collect_cg_pairs(Ctx &c, int npairs, double tol, int64_t max_iter, double *R, double *X, double *xstar,
                      int64_t *iters);
+// matfree.cu
+bool matfree_build(Ctx &c);
+void matfree_spmv(Ctx &c, cudaStream_t s);
 // learned.cu
 void learned_prepare(Ctx &c);                // features, scaling and factors F for the assembled system
 // scan.cu

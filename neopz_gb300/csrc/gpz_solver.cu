@@ -22,6 +22,7 @@
 
 #include "gpz_internal.h"
 #include "gpz_learned.cuh"
+#include "gpz_solver_common.cuh"
 
 namespace gpz {
 
@@ -29,93 +30,6 @@ LnView learned_view(Ctx &c);
 
 namespace {
 
-constexpr int kThreads = 256;
-constexpr int kGridBlocks = 152 * 8;  // upper bound of the grid-stride grids (partial-sum buffer size)
-
-// Grid-stride kernels run exactly one wave: SMs x resident CTAs of this kernel.
-template <class K>
-int wave(K kernel) {
-  static int nsm = 0;
-  if (!nsm) {
-    int dev = 0;
-    cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
-    if (nsm <= 0) nsm = 152;
-  }
-  int per = 0;
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, kernel, kThreads, 0);
-  if (per <= 0) per = 1;
-  int g = nsm * per;
-  return g > kGridBlocks ? kGridBlocks : g;
-}
-
-// device scalar slots
-// alpha and beta are formed once, by the CTA that finishes the reduction they depend on
-enum { S_RHO = 0, S_RHO1, S_PQ, S_RR, S_NORMB, S_TOL, S_MAXRR, S_DELTA2, S_RESID, S_TRUERR, S_ALPHA, S_BETA, S_NSCAL };
-enum { I_CONV = 0, I_IT, I_MAXIT, I_UPDATE, I_NUPD, I_SP64, I_SP32, I_BREAK, I_RESTART, I_NRESTART, I_NISCAL };
-
-struct Red {
-  double *partial;   // [grid][4]
-  unsigned *counter;
-  double *scal;
-  int64_t *iscal;
-};
-
-__device__ __forceinline__ double warp_sum(double v) {
-  for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
-  return v;
-}
-__device__ __forceinline__ float warp_sumf(float v) {
-  for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
-  return v;
-}
-
-// Block-reduce NV values, publish the block partial, and return true in the
-// last block to finish (after which tot[] holds the grid totals, summed in
-// block order).
-template <int NV>
-__device__ bool grid_reduce(double (&v)[NV], const Red &R, double (&tot)[NV]) {
-  __shared__ double sh[NV][kThreads / 32];
-  __shared__ bool last;
-  int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-  for (int k = 0; k < NV; k++) {
-    double s = warp_sum(v[k]);
-    if (lane == 0) sh[k][w] = s;
-  }
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    for (int k = 0; k < NV; k++) {
-      double s = 0.0;
-      for (int i = 0; i < kThreads / 32; i++) s += sh[k][i];
-      R.partial[(size_t)blockIdx.x * 4 + k] = s;
-    }
-    __threadfence();
-    unsigned t = atomicAdd(R.counter, 1u);
-    last = (t == gridDim.x - 1);
-  }
-  __syncthreads();
-  if (!last) return false;
-  __threadfence();
-  double acc[NV];
-  for (int k = 0; k < NV; k++) acc[k] = 0.0;
-  for (int i = threadIdx.x; i < (int)gridDim.x; i += blockDim.x)
-    for (int k = 0; k < NV; k++) acc[k] += ((volatile double *)R.partial)[(size_t)i * 4 + k];
-  __syncthreads();
-  for (int k = 0; k < NV; k++) {
-    double s = warp_sum(acc[k]);
-    if (lane == 0) sh[k][w] = s;
-  }
-  __syncthreads();
-  for (int k = 0; k < NV; k++) {
-    double s = 0.0;
-    for (int i = 0; i < kThreads / 32; i++) s += sh[k][i];
-    tot[k] = s;
-  }
-  if (threadIdx.x == 0) *R.counter = 0u;
-  return true;
-}
-
-__device__ __forceinline__ bool active(const int64_t *is) { return is[I_CONV] == 0 && is[I_IT] < is[I_MAXIT]; }
 
 // ---------------------------------------------------------------- SpMV
 // TPR threads cooperate on one row.
@@ -515,16 +429,6 @@ __global__ void k_block_inv3(const double *__restrict__ a, const int64_t *__rest
 // ======================================================================
 
 // compensated (Kahan) FP32 accumulation of one thread's terms
-struct KSum {
-  float s = 0.f, c = 0.f;
-  __device__ __forceinline__ void add(float v) {
-    float y = v - c;
-    float t = s + y;
-    c = (t - s) - y;
-    s = t;
-  }
-  __device__ __forceinline__ double get() const { return (double)s - (double)c; }
-};
 
 struct Prec32 {
   const float *dinv;  // [neq]
@@ -1600,6 +1504,10 @@ Red red_of(Ctx &c);
 // one launch of the FP32 3x3 SpMV variant v: q32 = A32 pm
 void launch_spmv32(Ctx &c, int v, const Ctx::Sell &S, Red R, cudaStream_t s) {
   SolverWork &w = c.sw;
+  if (v == 5) {
+    matfree_spmv(c, s);  // element by element (gpz_matfree.cu), counts its own launches
+    return;
+  }
   if (v == 0) {
     k_mx_bsr3<<<wave(k_mx_bsr3), kThreads, 0, s>>>(c.d_bptr.p, c.d_bcol.p, c.d_bval.p, (const float4 *)w.pm.p, w.q32.p,
                                                    c.nbrow, R);
@@ -1706,6 +1614,7 @@ void tune_spmv32(Ctx &c, int only, bool timing) {
     GPZ_CUDA_TRY(cudaGetLastError());
     res.push_back({4, 0, time_it(4, cand[0])});
   }
+  if (want(5) && matfree_build(c)) res.push_back({5, 0, time_it(5, cand[0])});
   if (res.empty()) res.push_back({0, 0, time_it(0, cand[0])});
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
@@ -1724,6 +1633,7 @@ void tune_spmv32(Ctx &c, int only, bool timing) {
                      : res[i].v == 1 ? "block_csr_2rows"
                      : res[i].v == 3 ? "block_csr_tma_staged"
                      : res[i].v == 4 ? "upper_blocks_float4_atomics"
+                     : res[i].v == 5 ? "matrix_free_elements"
                                      : "sliced_ell";
     rep += std::string(i ? ", " : "") + "\"" + nm + (res[i].v == 2 ? "_w" + std::to_string(res[i].window) : "") +
            "\": " + std::to_string(res[i].ms);
@@ -1732,8 +1642,8 @@ void tune_spmv32(Ctx &c, int only, bool timing) {
   if (c.d_uptr.p) {
     GPZ_CUDA_TRY(cudaMemcpy(&nu, c.d_uptr.p + c.nbrow, sizeof(int64_t), cudaMemcpyDeviceToHost));
   }
-  const char *names[5] = {"block_csr", "block_csr_2rows", "sliced_ell", "block_csr_tma_staged",
-                          "upper_blocks_float4_atomics"};
+  const char *names[6] = {"block_csr", "block_csr_2rows", "sliced_ell", "block_csr_tma_staged",
+                          "upper_blocks_float4_atomics", "matrix_free_elements"};
   c.tune_report = rep + ", \"chosen\": \"" + names[res[best].v] + "\", \"block_rows\": " + std::to_string(c.nbrow) +
                   ", \"blocks_full\": " + std::to_string(c.nnz / 9) + ", \"blocks_upper\": " + std::to_string(nu) +
                   "}";
@@ -1852,7 +1762,7 @@ void launch_iteration(Ctx &c, const Plan &P) {
     return;
   }
   const int padded = P.bsr ? 1 : 0;
-  const bool sym = P.bsr && c.spmv32_variant == 4;
+  const bool sym = P.bsr && (c.spmv32_variant == 4 || c.spmv32_variant == 5);  // q accumulated with atomics
   k_mx_p<<<wave(k_mx_p), kThreads, 0, c.stream>>>(w.r32.p, P.M32, w.pm.p, padded, sym ? w.q32.p : nullptr, P.nunits,
                                                   R);
   if (P.bsr) {
@@ -2320,6 +2230,41 @@ int solve(Ctx &c, const gpz_solver_opts &o, gpz_solve_report &rep) {
   c.have_solution = true;
   if (hstate[I_BREAK]) return GPZ_E_BREAKDOWN;
   return hstate[I_CONV] == 1 ? GPZ_OK : GPZ_NOT_CONVERGED;
+}
+
+// y = A32 x with the mixed CG's FP32 operator in its current layout (the
+// autotuned one, or `variant` >= 0), from and to host FP64 vectors
+void spmv32_apply(Ctx &c, int variant, const double *hx, double *hy) {
+  if (!c.have_a32 || (variant >= 0 && c.have_bsr3 && variant != c.spmv32_variant)) make_fp32_copy(c, variant);
+  alloc_work(c, true);
+  SolverWork &w = c.sw;
+  cudaStream_t s = c.stream;
+  const bool padded_in = c.have_bsr3;
+  const bool padded_out = c.have_bsr3 && (c.spmv32_variant == 4 || c.spmv32_variant == 5);
+  std::vector<float> xin(w.pm.n, 0.f);
+  for (int64_t i = 0; i < c.neq; i++) xin[padded_in ? 4 * (i / 3) + i % 3 : i] = (float)hx[i];
+  GPZ_CUDA_TRY(cudaMemcpyAsync(w.pm.p, xin.data(), xin.size() * sizeof(float), cudaMemcpyHostToDevice, s));
+  w.q32.zero(s);
+  double hs[S_NSCAL] = {0};
+  hs[S_RHO] = 1.0;
+  int64_t hi[I_NISCAL] = {0};
+  hi[I_MAXIT] = 1;
+  GPZ_CUDA_TRY(cudaMemcpyAsync(w.scal.p, hs, sizeof(hs), cudaMemcpyHostToDevice, s));
+  GPZ_CUDA_TRY(cudaMemcpyAsync(w.iscal.p, hi, sizeof(hi), cudaMemcpyHostToDevice, s));
+  Red R = red_of(c);
+  if (c.have_bsr3) {
+    launch_spmv32(c, c.spmv32_variant, c.sell, R, s);
+  } else {
+    GPZ_TPR_SWITCH(pick_tpr32(c.nnz, c.neq), (k_mx_csr<T><<<wave(k_mx_csr<T>), kThreads, 0, s>>>(
+                                                 c.d_ia.p, c.d_ja.p, c.d_a32.p, w.pm.p, w.q32.p, c.neq, R)));
+    c.launches++;
+  }
+  GPZ_CUDA_TRY(cudaGetLastError());
+  std::vector<float> yout(w.q32.n);
+  GPZ_CUDA_TRY(cudaMemcpyAsync(yout.data(), w.q32.p, yout.size() * sizeof(float), cudaMemcpyDeviceToHost, s));
+  GPZ_CUDA_TRY(cudaStreamSynchronize(s));
+  check_device_flag(c, "FP32 SpMV");
+  for (int64_t i = 0; i < c.neq; i++) hy[i] = yout[padded_out ? 4 * (i / 3) + i % 3 : i];
 }
 
 void solver_prepare(Ctx &c, bool mixed) {

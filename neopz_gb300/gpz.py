@@ -115,6 +115,7 @@ def lib():
         L.gpz_mesh_set_coef.argtypes = [vp, vp]
         L.gpz_assembly_report.argtypes = [vp, ctypes.c_char_p, i64]
         L.gpz_assemble_rhs.argtypes = [vp]
+        L.gpz_spmv_fp32.argtypes = [vp, i32, vp, vp]
         L.gpz_learned_init.argtypes = [vp, i32, ctypes.c_uint64]
         L.gpz_learned_num_params.argtypes = [vp, _P(i64)]
         L.gpz_learned_get_params.argtypes = [vp, vp, i64]
@@ -316,6 +317,13 @@ class Context:
         yy = None if y is None else np.ascontiguousarray(y, np.float64)
         self._check(lib().gpz_spmv(self.h, alpha, _p(x), beta, _p(yy), _p(z)))
         return z
+
+    def spmv_fp32(self, x, variant=-1):
+        """y = A32 x with the mixed solvers' FP32 operator (autotuned layout, or `variant`)."""
+        x = np.ascontiguousarray(x, np.float64)
+        y = np.zeros(self.neq)
+        self._check(lib().gpz_spmv_fp32(self.h, variant, _p(x), _p(y)))
+        return y
 
     def assemble_rhs(self):
         """Load vector alone (no matrix); read it with rhs()."""

@@ -201,7 +201,7 @@ def test_mixed_block_jacobi_bsr3(built):
     ctx.close()
 
 
-@pytest.mark.parametrize("variant", [0, 1, 2, 3, 4])
+@pytest.mark.parametrize("variant", [0, 1, 2, 3, 4, 5])
 def test_mixed_spmv_variants_converge(built, variant):
     """Every layout / kernel the SpMV autotuner can pick gives the same converged solution."""
     g = _gpz()
@@ -333,4 +333,30 @@ def test_assembly_graph_replay(built):
     fresh.assemble()
     assert np.array_equal(a2, fresh.matrix())
     fresh.close()
+    ctx.close()
+
+
+@pytest.mark.parametrize("variant", [0, 1, 2, 3, 4, 5])
+def test_fp32_operator_layouts_match_fp64_spmv(built, variant):
+    """Every FP32 operator layout of the mixed CG (block CSR, two rows, sliced ELL, TMA-staged, upper blocks
+    with atomics, matrix-free elements) applies the assembled operator: within 1e-5 of the FP64 CSR SpMV,
+    normwise and on the non-penalty rows alone."""
+    g = _gpz()
+    rng = np.random.default_rng(12)
+    n = 5
+    E = np.exp(rng.standard_normal(n ** 3))
+    grid = g.elasticity3d(n, 2, E=E)
+    ctx = g.Context(0)
+    ctx.upload_mesh(grid)
+    ctx.build_pattern(False)
+    ctx.assemble(g.GPZ_PREC_MIXED)
+    x = rng.standard_normal(grid.neq)
+    y64 = ctx.spmv(x)
+    y32 = ctx.spmv_fp32(x, variant)
+    assert np.linalg.norm(y32 - y64) <= 1e-5 * np.linalg.norm(y64)
+    ia, ja = ctx.pattern()
+    a = ctx.matrix()
+    diag = np.array([a[ia[i]:ia[i + 1]][ja[ia[i]:ia[i + 1]] == i][0] for i in range(grid.neq)])
+    inner = diag < 1e6 * np.median(diag)  # rows without the 1e12 penalty
+    assert np.linalg.norm((y32 - y64)[inner]) <= 1e-5 * np.linalg.norm(y64[inner])
     ctx.close()
