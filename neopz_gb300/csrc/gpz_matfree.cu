@@ -14,9 +14,9 @@
 // scatters the nodal vectors, instead of streaming ~2.7 GB of blocks at 64^3.
 //
 // Q2 hexes (27 shapes, 27 points): one warp per element; lane q keeps its
-// point's reference gradients (81 floats) and lane a its shape's (81 floats)
-// in registers, loaded once per CTA; per element only the nodal values and
-// the per-point stress pass through shared memory (as broadcasts).  p^T q is
+// point's reference gradients (81 floats) in registers and the shapes'
+// gradients sit in shared memory, both loaded once per CTA; per element the
+// nodal values and the per-point stress pass through shared memory.  p^T q is
 // the sum of the element energies u_e^T K_e u_e.
 #include <cmath>
 #include <vector>
@@ -124,42 +124,72 @@ __global__ void __launch_bounds__(kThreads) k_mf_faces(int64_t n, const float *_
   if (grid_reduce<1>(v, R, tot) && threadIdx.x == 0) *energy = tot[0];
 }
 
-// volume elements (Q2 hexes); pq = element energies + the faces' (*face_energy)
-__global__ void __launch_bounds__(kThreads, 1) k_mf_hex27(int64_t n, const float *__restrict__ rxyz,
-                                                          const int32_t *__restrict__ rows,
-                                                          const float *__restrict__ rlm,
-                                                          const float *__restrict__ dphi /*[q][3][a]*/,
-                                                          const float *__restrict__ w, const float4 *__restrict__ p4,
-                                                          float4 *__restrict__ q4,
-                                                          const double *__restrict__ face_energy, Red R) {
+// volume elements (Q2 hexes); pq = element energies + the faces' (*face_energy).
+// 128-thread CTAs, 3 per SM: lane q keeps its point's reference gradients in
+// registers (81 floats); the shapes' gradients sit in shared memory as
+// [point][shape] float4 rows (conflict-free 16-byte loads); the next
+// element's records are loaded while the current one is computed.
+constexpr int kMfThreads = 128;
+constexpr int kMfWarps = kMfThreads / 32;
+__global__ void __launch_bounds__(kMfThreads, 3) k_mf_hex27(int64_t n, const float *__restrict__ rxyz,
+                                                            const int32_t *__restrict__ rows,
+                                                            const float *__restrict__ rlm,
+                                                            const float *__restrict__ dphi /*[q][3][a]*/,
+                                                            const float *__restrict__ w,
+                                                            const float4 *__restrict__ p4, float4 *__restrict__ q4,
+                                                            const double *__restrict__ face_energy, Red R) {
   if (!active(R.iscal)) return;
-  __shared__ float4 su[kWarps][kNS];
-  __shared__ float sc[kWarps][24];
-  __shared__ float4 st[kWarps][kNQ][3];  // per point: the 3 x 3 stress-times-Jinv^T rows (x, y, z; w unused)
+  __shared__ float4 sdt[kNQ][32];            // [q][a] = (d0, d1, d2, 0) of shape a at point q
+  __shared__ float4 su[kMfWarps][kNS];
+  __shared__ float sc[kMfWarps][24];
+  __shared__ float4 st[kMfWarps][kNQ][3];
   const int lane = threadIdx.x & 31, wp = threadIdx.x >> 5;
-  // lane q: its point's reference gradients D[j][b]; lane a: its shape's Dt[q][j]
-  float D[3][kNS], Dt[kNQ][3], wq = 0.f;
+  for (int k = threadIdx.x; k < kNQ * 32; k += blockDim.x) {
+    const int q = k / 32, a = k % 32;
+    float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
+    if (a < kNS) {
+      v.x = dphi[(q * 3 + 0) * kNS + a];
+      v.y = dphi[(q * 3 + 1) * kNS + a];
+      v.z = dphi[(q * 3 + 2) * kNS + a];
+    }
+    sdt[q][a] = v;
+  }
+  float D[3][kNS], wq = 0.f;
 #pragma unroll
   for (int j = 0; j < 3; j++)
 #pragma unroll
     for (int b = 0; b < kNS; b++) D[j][b] = lane < kNQ ? dphi[(lane * 3 + j) * kNS + b] : 0.f;
-#pragma unroll
-  for (int q = 0; q < kNQ; q++)
-#pragma unroll
-    for (int j = 0; j < 3; j++) Dt[q][j] = lane < kNS ? dphi[(q * 3 + j) * kNS + lane] : 0.f;
   if (lane < kNQ) wq = w[lane];
+  __syncthreads();
   KSum en;
-  for (int64_t i = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; i < n;
-       i += ((int64_t)gridDim.x * blockDim.x) >> 5) {
-    int32_t row = 0;
+  const int64_t step = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  int64_t i = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  // records of the first element
+  int32_t row = 0;
+  float cxv = 0.f, lam = 0.f, mu = 0.f;
+  if (i < n) {
+    if (lane < kNS) row = rows[i * kNS + lane];
+    if (lane < 24) cxv = rxyz[i * 24 + lane];
+    lam = rlm[2 * i];
+    mu = rlm[2 * i + 1];
+  }
+  for (; i < n; i += step) {
     float4 u = make_float4(0.f, 0.f, 0.f, 0.f);
     if (lane < kNS) {
-      row = rows[i * kNS + lane];
       u = p4[row];
       su[wp][lane] = u;
     }
-    if (lane < 24) sc[wp][lane] = rxyz[i * 24 + lane];
-    const float lam = rlm[2 * i], mu = rlm[2 * i + 1];
+    if (lane < 24) sc[wp][lane] = cxv;
+    const float lam_i = lam, mu_i = mu;
+    const int32_t row_i = row;
+    // prefetch the next element's records
+    const int64_t nx = i + step;
+    if (nx < n) {
+      if (lane < kNS) row = rows[nx * kNS + lane];
+      if (lane < 24) cxv = rxyz[nx * 24 + lane];
+      lam = rlm[2 * nx];
+      mu = rlm[2 * nx + 1];
+    }
     __syncwarp();
     if (lane < kNQ) {
       // Jacobian from the corner shapes (the first 8 of the table), as TPZGeoEl::Jacobian
@@ -197,25 +227,25 @@ __global__ void __launch_bounds__(kThreads, 1) k_mf_hex27(int64_t n, const float
       }
       float H[3][3];
 #pragma unroll
-      for (int s = 0; s < 3; s++)
+      for (int s2 = 0; s2 < 3; s2++)
 #pragma unroll
-        for (int d = 0; d < 3; d++) H[s][d] = hh[s][0] * ji[0][d] + hh[s][1] * ji[1][d] + hh[s][2] * ji[2][d];
+        for (int d = 0; d < 3; d++) H[s2][d] = hh[s2][0] * ji[0][d] + hh[s2][1] * ji[1][d] + hh[s2][2] * ji[2][d];
       const float wd = wq * fabsf(det);
-      const float lt = lam * (H[0][0] + H[1][1] + H[2][2]);
+      const float lt = lam_i * (H[0][0] + H[1][1] + H[2][2]);
       float T[3][3];
 #pragma unroll
-      for (int s = 0; s < 3; s++)
+      for (int s2 = 0; s2 < 3; s2++)
 #pragma unroll
-        for (int d = 0; d < 3; d++) T[s][d] = wd * (mu * (H[s][d] + H[d][s]) + (s == d ? lt : 0.f));
+        for (int d = 0; d < 3; d++) T[s2][d] = wd * (mu_i * (H[s2][d] + H[d][s2]) + (s2 == d ? lt : 0.f));
       // back to reference derivatives: Th[s][j] = sum_d T[s][d] ji[j][d]
 #pragma unroll
-      for (int s = 0; s < 3; s++) {
+      for (int s2 = 0; s2 < 3; s2++) {
         float4 t;
-        t.x = T[s][0] * ji[0][0] + T[s][1] * ji[0][1] + T[s][2] * ji[0][2];
-        t.y = T[s][0] * ji[1][0] + T[s][1] * ji[1][1] + T[s][2] * ji[1][2];
-        t.z = T[s][0] * ji[2][0] + T[s][1] * ji[2][1] + T[s][2] * ji[2][2];
+        t.x = T[s2][0] * ji[0][0] + T[s2][1] * ji[0][1] + T[s2][2] * ji[0][2];
+        t.y = T[s2][0] * ji[1][0] + T[s2][1] * ji[1][1] + T[s2][2] * ji[1][2];
+        t.z = T[s2][0] * ji[2][0] + T[s2][1] * ji[2][1] + T[s2][2] * ji[2][2];
         t.w = 0.f;
-        st[wp][lane][s] = t;
+        st[wp][lane][s2] = t;
       }
     }
     __syncwarp();
@@ -224,12 +254,13 @@ __global__ void __launch_bounds__(kThreads, 1) k_mf_hex27(int64_t n, const float
 #pragma unroll
       for (int q = 0; q < kNQ; q++) {
         const float4 t0 = st[wp][q][0], t1 = st[wp][q][1], t2 = st[wp][q][2];
-        y0 += t0.x * Dt[q][0] + t0.y * Dt[q][1] + t0.z * Dt[q][2];
-        y1 += t1.x * Dt[q][0] + t1.y * Dt[q][1] + t1.z * Dt[q][2];
-        y2 += t2.x * Dt[q][0] + t2.y * Dt[q][1] + t2.z * Dt[q][2];
+        const float4 g = sdt[q][lane];
+        y0 += t0.x * g.x + t0.y * g.y + t0.z * g.z;
+        y1 += t1.x * g.x + t1.y * g.y + t1.z * g.z;
+        y2 += t2.x * g.x + t2.y * g.y + t2.z * g.z;
       }
       en.add(y0 * u.x + y1 * u.y + y2 * u.z);
-      atomicAdd(&q4[row], make_float4(y0, y1, y2, 0.f));
+      atomicAdd(&q4[row_i], make_float4(y0, y1, y2, 0.f));
     }
     __syncwarp();
   }
@@ -243,11 +274,12 @@ __global__ void __launch_bounds__(kThreads, 1) k_mf_hex27(int64_t n, const float
 }
 
 template <class K>
-int mf_grid(K kernel) {
+int mf_grid(K kernel, int threads) {
   int dev = 0, nsm = 0, per = 0;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, kernel, kThreads, 0);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, kernel, threads, 0);
+  // grid_reduce's partial-sum buffer holds kGridBlocks CTAs
   return std::max(1, std::min(kGridBlocks, nsm * std::max(per, 1)));
 }
 
@@ -312,8 +344,8 @@ bool matfree_build(Ctx &c) {
   M.energy.alloc(1);
   GPZ_CUDA_TRY(cudaGetLastError());
   check_device_flag(c, "matrix-free records");
-  M.grid_vol = mf_grid(k_mf_hex27);
-  M.grid_face = mf_grid(k_mf_faces);
+  M.grid_vol = mf_grid(k_mf_hex27, kMfThreads);
+  M.grid_face = mf_grid(k_mf_faces, kThreads);
   M.ready = true;
   return true;
 }
@@ -330,7 +362,7 @@ void matfree_spmv(Ctx &c, cudaStream_t s) {
                                                 q4, M.energy.p, R);
     c.launches++;
   }
-  k_mf_hex27<<<M.grid_vol, kThreads, 0, s>>>(M.nvol, M.vxyz.p, M.vrows.p, M.vlm.p, M.vdphi.p, M.vw.p, p4, q4,
+  k_mf_hex27<<<M.grid_vol, kMfThreads, 0, s>>>(M.nvol, M.vxyz.p, M.vrows.p, M.vlm.p, M.vdphi.p, M.vw.p, p4, q4,
                                              M.nface ? M.energy.p : nullptr, R);
   c.launches++;
 }

@@ -66,7 +66,7 @@ __device__ bool grid_reduce(double (&v)[NV], const Red &R, double (&tot)[NV]) {
   if (threadIdx.x == 0) {
     for (int k = 0; k < NV; k++) {
       double s = 0.0;
-      for (int i = 0; i < kThreads / 32; i++) s += sh[k][i];
+      for (int i = 0; i < (int)(blockDim.x >> 5); i++) s += sh[k][i];  // CTAs of up to kThreads
       R.partial[(size_t)blockIdx.x * 4 + k] = s;
     }
     __threadfence();
@@ -88,7 +88,7 @@ __device__ bool grid_reduce(double (&v)[NV], const Red &R, double (&tot)[NV]) {
   __syncthreads();
   for (int k = 0; k < NV; k++) {
     double s = 0.0;
-    for (int i = 0; i < kThreads / 32; i++) s += sh[k][i];
+    for (int i = 0; i < (int)(blockDim.x >> 5); i++) s += sh[k][i];  // CTAs of up to kThreads
     tot[k] = s;
   }
   if (threadIdx.x == 0) *R.counter = 0u;
