@@ -201,7 +201,19 @@ def run_gpu(args):
     neq = grid.neq
     nbrow = neq // 3
     chosen = tune.get("chosen", "block_csr")
-    if chosen == "upper_blocks_float4_atomics":
+    mf_flops = None
+    if chosen == "matrix_free_elements":
+        # element records (corners 96 B, block rows 108 B, lambda/mu 8 B), penalty-face records (48 + 36 B),
+        # p read once and q accumulated once (16 B per block row each)
+        nface = (n + 0) * (n + 0)
+        nblk = 0
+        kern = ("k_mf_hex27: matrix-free Q2 elasticity, one warp per element (CUDA-core FP32; records + one "
+                "pass of p and q are its HBM bytes)")
+        l2_atomics = 27 * nvol + 9 * nface
+        # FLOPs per element: per point, grad(u) from 27 shapes (2 x 243), geometry ~110, stress and the two
+        # Jacobian products ~60 + 2 x 27; per shape, the 27-point back-projection (2 x 27 x 9)
+        mf_flops = nvol * (27 * (2 * 243 + 110 + 60 + 2 * 27) + 27 * 2 * 27 * 9) + nface * 2 * 9 * 9 * 6
+    elif chosen == "upper_blocks_float4_atomics":
         nblk = tune["blocks_upper"]
         kern = "k_mx_sym3: upper 3x3 blocks (36 B values + 4 B column), transposed products as float4 atomics in L2"
         l2_atomics = nblk
@@ -211,6 +223,8 @@ def run_gpu(args):
         l2_atomics = 0
     # values + columns + block-row pointers + p (16 B per block row, read once) + q (written once)
     bytes32 = nblk * (36 + 4) + (nbrow + 1) * 8 + nbrow * 16 + nbrow * 16
+    if chosen == "matrix_free_elements":
+        bytes32 = nvol * (96 + 108 + 8) + nface * (48 + 36) + nbrow * 16 + nbrow * 16
     bytes64 = nnz * (8 + 4) + (neq + 1) * 8 + neq * 8 + neq * 8 + neq * 8
     pk = peaks()
     hbm = pk.get("hbm_gbs", 6800.0)
@@ -246,7 +260,7 @@ def run_gpu(args):
         "config": {"workload": f"3D linear elasticity {n}^3 hex Q2 (TPZElasticity3D), E lognormal(sigma=1) seed {SEED}, "
                                "nu=0.3, clamped z=0 (penalty), traction (0,0,-1) on z=1",
                    "neq": neq, "nnz_full": nnz, "nnz_upper": nnz_upper, "elements": nel, "volume_elements": nvol,
-                   "path": "FP64 assembly + FP32 3x3 block-CSR copy; CG with FP32-value block SpMV, FP64 x/r/dots, "
+                   "path": f"FP64 assembly; CG with the FP32 inner operator chosen by the autotuner ({chosen}), FP64 x/r/dots, "
                            "reliable FP64 true-residual updates; connect-block (3x3) Jacobi", "l2": "inputs larger than L2 (matrix > 129 MB)",
                    "parallelism": f"replicas x{world}"},
         "solve": {"iterations": last["iterations"], "true_resid": last["true_resid"],
@@ -262,6 +276,8 @@ def run_gpu(args):
                      "peak": hbm, "unit": "GB/s", "frac": round(ach / hbm, 4), "traffic": traffic,
                      "l2_float4_atomics_per_launch": l2_atomics,
                      "algorithmic_bytes": int(bytes32), "ms_per_launch": ms32,
+                     "fp32_tflops": (round(mf_flops / (ms32 * 1e-3) / 1e12, 2) if mf_flops else None),
+                     "fp32_peak_tflops_nominal": (round(152 * 128 * 2 * 2.07e9 / 1e12, 1) if mf_flops else None),
                      "fp64_spmv": {"ms_per_launch": ms64,
                                    "achieved_gbs": round(bytes64 / (ms64 * 1e-3) / 1e9, 1)},
                      "peak_source": "MEASURED_PEAKS.json hbm_gbs (burst copy)" if "fallback" not in pk else
