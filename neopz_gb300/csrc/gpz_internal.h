@@ -154,7 +154,7 @@ struct MatFree {
   DBuf<int32_t> frows;
   DBuf<double> energy;                       // the faces' share of p.q
   float big = 0.f;
-  int grid_vol = 1, grid_face = 1;
+  int grid_vol = 1, grid_face = 1, grid_tc = 1;
 };
 
 // ---------------------------------------------------------------- the context
@@ -256,7 +256,7 @@ int collect_cg_pairs(Ctx &c, int npairs, double tol, int64_t max_iter, double *R
                      int64_t *iters);
 // matfree.cu
 bool matfree_build(Ctx &c);
-void matfree_spmv(Ctx &c, cudaStream_t s);
+void matfree_spmv(Ctx &c, cudaStream_t s, bool tensor);
 // learned.cu
 void learned_prepare(Ctx &c);                // features, scaling and factors F for the assembled system
 // scan.cu

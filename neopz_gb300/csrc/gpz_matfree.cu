@@ -273,6 +273,353 @@ __global__ void __launch_bounds__(kMfThreads, 3) k_mf_hex27(int64_t n, const flo
   }
 }
 
+
+// ---------------------------------------------------------------- tensor-core variant
+// The same operator with the two element contractions on the 5th-generation
+// tensor cores (tcgen05.mma kind::tf32, operands in shared memory, FP32
+// accumulators in TMEM), as split 3xTF32 products (hi.hi + hi.lo + lo.hi, about
+// FP32 accuracy).  A CTA of 4 warps takes tiles of 40 elements; matrix row
+// r = 32 w + 3 e + s holds component s of element e of warp w (rows 30 and 31 of
+// each warp are padding), so an element's three rows stay in one warp.
+//   phase 1:  Hh[r][(q,j)] = sum_b U[r][b] D[b][(q,j)]       M 128, N 96 (81), K 32 (27)
+//   pointwise: per (element, point) the Jacobian from the corners, the stress,
+//              and back to reference derivatives TH; the element energy sum TH.Hh
+//   phase 2:  Y[r][a] = sum_(q,j) TH[r][(q,j)] D[(q,j)][a]   M 128, N 32 (27), K 96 (81)
+// Operands are K-major without swizzle: 8-row x 16-byte core matrices, K
+// direction fastest (LBO 128 B, SBO = K/4 x 128 B).
+constexpr int kTcThreads = 256;  // 8 warps: warps w and w + 4 share TMEM lane quarter w
+constexpr int kTcEl = 40;   // elements per tile
+constexpr int kTcElW = 10;  // per warp
+constexpr uint32_t kB1 = 96 * 32 * 4, kB2 = 32 * 96 * 4, kA1 = 128 * 32 * 4, kA2 = 128 * 96 * 4;
+constexpr uint32_t OFF_B1H = 0, OFF_B1L = OFF_B1H + kB1, OFF_B2H = OFF_B1L + kB1, OFF_B2L = OFF_B2H + kB2;
+constexpr uint32_t OFF_A1H = OFF_B2L + kB2, OFF_A1L = OFF_A1H + kA1, OFF_A2H = OFF_A1L + kA1, OFF_A2L = OFF_A2H + kA2;
+constexpr uint32_t OFF_CG = OFF_A2L + kA2, OFF_W = OFF_CG + 27 * 3 * 8 * 4, OFF_CX = OFF_W + 32 * 4;
+constexpr uint32_t OFF_LM = OFF_CX + kTcEl * 24 * 4, OFF_ST1 = OFF_LM + kTcEl * 2 * 4;
+constexpr uint32_t OFF_TC_END = OFF_ST1 + 128 * 32 * 4;  // results staging (phase-2 rows)
+constexpr int kTcGather = kTcEl * 32 / kTcThreads;        // (element, shape) items per thread
+constexpr int kTcItems = (kTcEl * 27 + kTcThreads - 1) / kTcThreads;  // (element, point) items per thread
+constexpr int kTcWaitTries = 1 << 22;
+
+__device__ __forceinline__ uint32_t tc_smem(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
+__device__ __forceinline__ uint32_t kmaj(int r, int k, int kcols) {
+  return ((uint32_t)(r >> 3) * (uint32_t)(kcols >> 2) + (uint32_t)(k >> 2)) * 128u + (uint32_t)(r & 7) * 16u +
+         (uint32_t)(k & 3) * 4u;
+}
+__device__ __forceinline__ uint64_t tc_desc(uint32_t saddr, uint32_t sbo) {
+  return (uint64_t)((saddr >> 4) & 0x3FFF) | ((uint64_t)((128u >> 4) & 0x3FFF) << 16) |
+         ((uint64_t)((sbo >> 4) & 0x3FFF) << 32) | ((uint64_t)1 << 46);
+}
+__device__ __forceinline__ float tf32_rna(float x) {
+  uint32_t r;
+  asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(r) : "f"(x));
+  return __uint_as_float(r);
+}
+__device__ __forceinline__ void st_split(unsigned char *hi, unsigned char *lo, uint32_t off, float v) {
+  const float h = tf32_rna(v);
+  *(float *)(hi + off) = h;
+  *(float *)(lo + off) = tf32_rna(v - h);
+}
+__device__ __forceinline__ void tc_mma(uint32_t tm, uint64_t a, uint64_t b, uint32_t idesc, uint32_t acc) {
+  asm volatile("{\n.reg .pred p;\nsetp.ne.b32 p, %4, 0;\ntcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n}\n" ::"r"(tm),
+               "l"(a), "l"(b), "r"(idesc), "r"(acc));
+}
+__device__ __forceinline__ void tc_commit(uint64_t *mb) {
+  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(tc_smem(mb)));
+}
+__device__ __forceinline__ bool tc_wait(uint64_t *mb, uint32_t parity) {
+  uint32_t done = 0;
+  for (int it = 0; it < kTcWaitTries && !done; it++)
+    asm volatile("{\n.reg .pred p;\nmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\nselp.u32 %0, 1, 0, p;\n}\n"
+                 : "=r"(done)
+                 : "r"(tc_smem(mb)), "r"(parity));
+  return done != 0;
+}
+__device__ __forceinline__ void tc_ld16(uint32_t taddr, float *v) {
+  uint32_t r[16];
+  asm volatile("tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
+               : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+                 "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+               : "r"(taddr));
+  asm volatile("tcgen05.wait::ld.sync.aligned;");
+#pragma unroll
+  for (int j = 0; j < 16; j++) v[j] = __uint_as_float(r[j]);
+}
+
+// U rows of a tile (the nodal values, split hi / lo), its corners and (lambda, mu);
+// every load is issued before the first store
+__device__ __forceinline__ void tc_gather(unsigned char *sm, int64_t e0, int64_t n, const int32_t *__restrict__ rows,
+                                          const float4 *__restrict__ p4, const float *__restrict__ rxyz,
+                                          const float *__restrict__ rlm, int tid) {
+  int32_t ri[kTcGather];
+  float4 pv[kTcGather];
+#pragma unroll
+  for (int k = 0; k < kTcGather; k++) {
+    const int t = tid + k * kTcThreads, le = t / 32, b = t % 32;
+    const int64_t e = e0 + le;
+    ri[k] = (b < 27 && e < n) ? rows[e * 27 + b] : -1;
+  }
+#pragma unroll
+  for (int k = 0; k < kTcGather; k++) pv[k] = ri[k] >= 0 ? p4[ri[k]] : make_float4(0.f, 0.f, 0.f, 0.f);
+  float cv[4];
+  float lv[2] = {0.f, 0.f};
+#pragma unroll
+  for (int k = 0; k < 4; k++) {
+    const int t = tid + k * kTcThreads;
+    const int64_t e = e0 + t / 24;
+    cv[k] = (t < kTcEl * 24 && e < n) ? rxyz[e * 24 + t % 24] : 0.f;
+  }
+  if (tid < kTcEl && e0 + tid < n) {
+    lv[0] = rlm[2 * (e0 + tid)];
+    lv[1] = rlm[2 * (e0 + tid) + 1];
+  }
+#pragma unroll
+  for (int k = 0; k < kTcGather; k++) {
+    const int t = tid + k * kTcThreads, le = t / 32, b = t % 32;
+    const int r0 = (le / kTcElW) * 32 + 3 * (le % kTcElW);
+    st_split(sm + OFF_A1H, sm + OFF_A1L, kmaj(r0, b, 32), pv[k].x);
+    st_split(sm + OFF_A1H, sm + OFF_A1L, kmaj(r0 + 1, b, 32), pv[k].y);
+    st_split(sm + OFF_A1H, sm + OFF_A1L, kmaj(r0 + 2, b, 32), pv[k].z);
+  }
+  float *cx = (float *)(sm + OFF_CX), *lm = (float *)(sm + OFF_LM);
+#pragma unroll
+  for (int k = 0; k < 4; k++) {
+    const int t = tid + k * kTcThreads;
+    if (t < kTcEl * 24) cx[t] = cv[k];
+  }
+  if (tid < kTcEl) {
+    lm[2 * tid] = lv[0];
+    lm[2 * tid + 1] = lv[1];
+  }
+}
+
+__global__ void __launch_bounds__(kTcThreads, 1) k_mf_hex27_tc(int64_t n, const float *__restrict__ rxyz,
+                                                               const int32_t *__restrict__ rows,
+                                                               const float *__restrict__ rlm,
+                                                               const float *__restrict__ dphi /*[q][3][a]*/,
+                                                               const float *__restrict__ w,
+                                                               const float4 *__restrict__ p4, float4 *__restrict__ q4,
+                                                               const double *__restrict__ face_energy,
+                                                               int *__restrict__ err, Red R) {
+  if (!active(R.iscal)) return;
+  extern __shared__ __align__(1024) unsigned char sm[];
+  __shared__ uint32_t s_tmem;
+  __shared__ __align__(8) uint64_t s_mb[2];
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  float *cg = (float *)(sm + OFF_CG), *sw = (float *)(sm + OFF_W), *cx = (float *)(sm + OFF_CX);
+  float *lm = (float *)(sm + OFF_LM);
+  // constant operands: B1[n][b] = D(b at point q, direction j), n = 3q + j; B2[a][n] = the same transposed
+  for (int i = tid; i < 96 * 32; i += blockDim.x) {
+    const int nn = i / 32, b = i % 32;
+    st_split(sm + OFF_B1H, sm + OFF_B1L, kmaj(nn, b, 32), (nn < 81 && b < 27) ? dphi[nn * 27 + b] : 0.f);
+  }
+  for (int i = tid; i < 32 * 96; i += blockDim.x) {
+    const int a = i / 96, nn = i % 96;
+    st_split(sm + OFF_B2H, sm + OFF_B2L, kmaj(a, nn, 96), (a < 27 && nn < 81) ? dphi[nn * 27 + a] : 0.f);
+  }
+  for (int i = tid; i < 27 * 3 * 8; i += blockDim.x) cg[i] = dphi[(i / 8) * 27 + i % 8];  // corner gradients
+  if (tid < 27) sw[tid] = w[tid];
+  for (uint32_t i = tid; i < (kA1 + kA1 + kA2 + kA2) / 4; i += blockDim.x) ((float *)(sm + OFF_A1H))[i] = 0.f;
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(tc_smem(&s_tmem)), "r"(256));
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+  }
+  if (tid == 0) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(tc_smem(&s_mb[0])));
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(tc_smem(&s_mb[1])));
+    asm volatile("fence.mbarrier_init.release.cluster;");
+  }
+  asm volatile("fence.proxy.async.shared::cta;");
+  asm volatile("tcgen05.fence::before_thread_sync;");
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;");
+  const uint32_t tm = s_tmem;
+  const uint32_t id1 = (1u << 4) | (2u << 7) | (2u << 10) | ((96u >> 3) << 17) | ((128u >> 4) << 24);
+  const uint32_t id2 = (1u << 4) | (2u << 7) | (2u << 10) | ((32u >> 3) << 17) | ((128u >> 4) << 24);
+  const uint32_t a1h = tc_smem(sm + OFF_A1H), a1l = tc_smem(sm + OFF_A1L), a2h = tc_smem(sm + OFF_A2H),
+                 a2l = tc_smem(sm + OFF_A2L);
+  const uint32_t b1h = tc_smem(sm + OFF_B1H), b1l = tc_smem(sm + OFF_B1L), b2h = tc_smem(sm + OFF_B2H),
+                 b2l = tc_smem(sm + OFF_B2L);
+  KSum en;
+  uint32_t parity = 0;
+  bool failed = false;
+  if ((int64_t)blockIdx.x * kTcEl < n) tc_gather(sm, (int64_t)blockIdx.x * kTcEl, n, rows, p4, rxyz, rlm, tid);
+  for (int64_t tile = blockIdx.x; tile * kTcEl < n && !failed; tile += gridDim.x) {
+    const int64_t e0 = tile * kTcEl;
+    asm volatile("fence.proxy.async.shared::cta;");
+    asm volatile("tcgen05.fence::before_thread_sync;");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;");
+    if (tid == 0) {
+      for (int k = 0; k < 4; k++) {
+        const uint64_t ah = tc_desc(a1h + k * 256, 1024), al = tc_desc(a1l + k * 256, 1024);
+        const uint64_t bh = tc_desc(b1h + k * 256, 1024), bl = tc_desc(b1l + k * 256, 1024);
+        tc_mma(tm, ah, bh, id1, k > 0);
+        tc_mma(tm, ah, bl, id1, 1u);
+        tc_mma(tm, al, bh, id1, 1u);
+      }
+      tc_commit(&s_mb[0]);
+    }
+    bool ok = tc_wait(&s_mb[0], parity);
+    if (__syncthreads_or(!ok)) {
+      failed = true;
+      break;
+    }
+    asm volatile("tcgen05.fence::after_thread_sync;");
+    // phase-1 rows -> row-major staging (row r at A2H + (r / 32) * 12288 + (r % 32) * 324): warp w reads
+    // TMEM lanes 32 (w % 4) .. + 31, columns 48 (w / 4) .. + 47
+    const int quarter = warp & 3, half = warp >> 2;
+    {
+      float *stg = (float *)(sm + OFF_A2H + quarter * 4 * 24 * 128);
+      float h[16];
+      for (int c0 = 48 * half; c0 < 48 * half + 48; c0 += 16) {
+        tc_ld16(tm + ((uint32_t)(quarter * 32) << 16) + c0, h);
+#pragma unroll
+        for (int j = 0; j < 16; j++)
+          if (c0 + j < 81) stg[lane * 81 + c0 + j] = h[j];
+      }
+    }
+    __syncthreads();
+    // pointwise, item (element le, point q): Jacobian, stress, TH; the element energy TH . Hh
+    float th[kTcItems][9];
+#pragma unroll
+    for (int k = 0; k < kTcItems; k++) {
+#pragma unroll
+      for (int m = 0; m < 9; m++) th[k][m] = 0.f;
+      const int it = tid + k * kTcThreads;
+      if (it >= kTcEl * 27) continue;
+      const int le = it / 27, q = it % 27;
+      if (e0 + le >= n) continue;
+      const int rq = le / kTcElW, rl = 3 * (le % kTcElW);
+      const float *srow = (const float *)(sm + OFF_A2H + rq * 4 * 24 * 128);
+      float hh[3][3];
+#pragma unroll
+      for (int s2 = 0; s2 < 3; s2++)
+#pragma unroll
+        for (int j = 0; j < 3; j++) hh[s2][j] = srow[(rl + s2) * 81 + q * 3 + j];
+      const float lam = lm[2 * le], mu = lm[2 * le + 1];
+      const float *ce = cx + le * 24;
+      float a[3][3] = {{0.f, 0.f, 0.f}, {0.f, 0.f, 0.f}, {0.f, 0.f, 0.f}};
+#pragma unroll
+      for (int c = 0; c < 8; c++)
+#pragma unroll
+        for (int j = 0; j < 3; j++)
+#pragma unroll
+          for (int d = 0; d < 3; d++) a[j][d] += ce[c * 3 + j] * cg[(q * 3 + d) * 8 + c];
+      const float det = -a[0][2] * a[1][1] * a[2][0] + a[0][1] * a[1][2] * a[2][0] + a[0][2] * a[1][0] * a[2][1] -
+                        a[0][0] * a[1][2] * a[2][1] - a[0][1] * a[1][0] * a[2][2] + a[0][0] * a[1][1] * a[2][2];
+      const float id = 1.f / det;
+      float ji[3][3];
+      ji[0][0] = (-a[1][2] * a[2][1] + a[1][1] * a[2][2]) * id;
+      ji[0][1] = (a[0][2] * a[2][1] - a[0][1] * a[2][2]) * id;
+      ji[0][2] = (-a[0][2] * a[1][1] + a[0][1] * a[1][2]) * id;
+      ji[1][0] = (a[1][2] * a[2][0] - a[1][0] * a[2][2]) * id;
+      ji[1][1] = (-a[0][2] * a[2][0] + a[0][0] * a[2][2]) * id;
+      ji[1][2] = (a[0][2] * a[1][0] - a[0][0] * a[1][2]) * id;
+      ji[2][0] = (-a[1][1] * a[2][0] + a[1][0] * a[2][1]) * id;
+      ji[2][1] = (a[0][1] * a[2][0] - a[0][0] * a[2][1]) * id;
+      ji[2][2] = (-a[0][1] * a[1][0] + a[0][0] * a[1][1]) * id;
+      float H[3][3];
+#pragma unroll
+      for (int s2 = 0; s2 < 3; s2++)
+#pragma unroll
+        for (int d = 0; d < 3; d++) H[s2][d] = hh[s2][0] * ji[0][d] + hh[s2][1] * ji[1][d] + hh[s2][2] * ji[2][d];
+      const float wd = sw[q] * fabsf(det);
+      const float lt = lam * (H[0][0] + H[1][1] + H[2][2]);
+      float e_q = 0.f;
+#pragma unroll
+      for (int s2 = 0; s2 < 3; s2++) {
+        float T[3];
+#pragma unroll
+        for (int d = 0; d < 3; d++) T[d] = wd * (mu * (H[s2][d] + H[d][s2]) + (s2 == d ? lt : 0.f));
+#pragma unroll
+        for (int j = 0; j < 3; j++) {
+          const float t = T[0] * ji[j][0] + T[1] * ji[j][1] + T[2] * ji[j][2];
+          th[k][s2 * 3 + j] = t;
+          e_q += t * hh[s2][j];
+        }
+      }
+      en.add(e_q);
+    }
+    __syncthreads();  // all staging reads done before A2 is overwritten
+#pragma unroll
+    for (int k = 0; k < kTcItems; k++) {
+      const int it = tid + k * kTcThreads;
+      if (it >= kTcEl * 27) continue;
+      const int le = it / 27, q = it % 27;
+      const int r0 = (le / kTcElW) * 32 + 3 * (le % kTcElW);
+#pragma unroll
+      for (int s2 = 0; s2 < 3; s2++)
+#pragma unroll
+        for (int j = 0; j < 3; j++) st_split(sm + OFF_A2H, sm + OFF_A2L, kmaj(r0 + s2, q * 3 + j, 96), th[k][s2 * 3 + j]);
+    }
+    // K padding (columns 81..95) of the element rows, and the two padding rows of each quarter, are zero
+    for (int t = tid; t < 128 * 15; t += kTcThreads) {
+      const int r = t / 15, c = 81 + t % 15;
+      st_split(sm + OFF_A2H, sm + OFF_A2L, kmaj(r, c, 96), 0.f);
+    }
+    for (int t = tid; t < 4 * 2 * 81; t += kTcThreads) {
+      const int r = (t / 162) * 32 + 30 + (t / 81) % 2, c = t % 81;
+      st_split(sm + OFF_A2H, sm + OFF_A2L, kmaj(r, c, 96), 0.f);
+    }
+    asm volatile("fence.proxy.async.shared::cta;");
+    asm volatile("tcgen05.fence::before_thread_sync;");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;");
+    if (tid == 0) {
+      for (int k = 0; k < 12; k++) {
+        const uint64_t ah = tc_desc(a2h + k * 256, 3072), al = tc_desc(a2l + k * 256, 3072);
+        const uint64_t bh = tc_desc(b2h + k * 256, 3072), bl = tc_desc(b2l + k * 256, 3072);
+        tc_mma(tm + 128, ah, bh, id2, k > 0);
+        tc_mma(tm + 128, ah, bl, id2, 1u);
+        tc_mma(tm + 128, al, bh, id2, 1u);
+      }
+      tc_commit(&s_mb[1]);
+    }
+    // the next tile's nodal values go into U while the phase-2 MMAs run (they read A2 / B2 only)
+    if ((tile + gridDim.x) * kTcEl < n) tc_gather(sm, (tile + gridDim.x) * kTcEl, n, rows, p4, rxyz, rlm, tid);
+    ok = tc_wait(&s_mb[1], parity);
+    if (__syncthreads_or(!ok)) {
+      failed = true;
+      break;
+    }
+    asm volatile("tcgen05.fence::after_thread_sync;");
+    // results: rows -> staging -> one float4 atomic per (element, shape)
+    float *st1 = (float *)(sm + OFF_ST1);
+    {
+      float y[16];
+      tc_ld16(tm + ((uint32_t)(quarter * 32) << 16) + 128 + 16 * half, y);
+#pragma unroll
+      for (int j = 0; j < 16; j++) st1[(quarter * 32 + lane) * 32 + 16 * half + j] = y[j];
+    }
+    __syncthreads();
+    for (int t = tid; t < kTcEl * 27; t += kTcThreads) {
+      const int le = t / 27, a = t % 27;
+      const int64_t e = e0 + le;
+      if (e >= n) continue;
+      const int r0 = (le / kTcElW) * 32 + 3 * (le % kTcElW);
+      const float4 v = make_float4(st1[(r0 + 0) * 32 + a], st1[(r0 + 1) * 32 + a], st1[(r0 + 2) * 32 + a], 0.f);
+      atomicAdd(&q4[rows[e * 27 + a]], v);
+    }
+    parity ^= 1u;
+  }
+  if (failed) {
+    if (tid == 0) atomicOr(err, 8192);
+    // let the MMAs in flight finish (bounded) before the accumulators are released
+    tc_wait(&s_mb[0], parity);
+    tc_wait(&s_mb[1], parity);
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;");
+  __syncthreads();
+  if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tm), "r"(256));
+  double v[1] = {failed ? 0.0 : en.get()}, tot[1];
+  if (grid_reduce<1>(v, R, tot) && threadIdx.x == 0) {
+    const double pq = tot[0] + (face_energy ? *face_energy : 0.0);
+    R.scal[S_PQ] = pq;
+    R.scal[S_ALPHA] = R.scal[S_RHO] / pq;
+    R.iscal[I_SP32]++;
+  }
+}
+
 template <class K>
 int mf_grid(K kernel, int threads) {
   int dev = 0, nsm = 0, per = 0;
@@ -346,12 +693,20 @@ bool matfree_build(Ctx &c) {
   check_device_flag(c, "matrix-free records");
   M.grid_vol = mf_grid(k_mf_hex27, kMfThreads);
   M.grid_face = mf_grid(k_mf_faces, kThreads);
+  GPZ_CUDA_TRY(cudaFuncSetAttribute(k_mf_hex27_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)OFF_TC_END));
+  {
+    int dev = 0, nsm = 0;
+    GPZ_CUDA_TRY(cudaGetDevice(&dev));
+    GPZ_CUDA_TRY(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
+    M.grid_tc = std::max(1, std::min(kGridBlocks, nsm));  // one 187 KB CTA per SM, persistent over tiles
+  }
   M.ready = true;
   return true;
 }
 
-// q4 = A p4 (q4 zeroed by the caller), p.q and alpha as the block SpMV kernels
-void matfree_spmv(Ctx &c, cudaStream_t s) {
+// q4 = A p4 (q4 zeroed by the caller), p.q and alpha as the block SpMV kernels;
+// tensor: the tcgen05 3xTF32 volume kernel instead of the CUDA-core one
+void matfree_spmv(Ctx &c, cudaStream_t s, bool tensor) {
   MatFree &M = c.mf;
   SolverWork &w = c.sw;
   Red R{w.partial.p, w.counter.p, w.scal.p, w.iscal.p};
@@ -362,8 +717,12 @@ void matfree_spmv(Ctx &c, cudaStream_t s) {
                                                 q4, M.energy.p, R);
     c.launches++;
   }
-  k_mf_hex27<<<M.grid_vol, kMfThreads, 0, s>>>(M.nvol, M.vxyz.p, M.vrows.p, M.vlm.p, M.vdphi.p, M.vw.p, p4, q4,
-                                             M.nface ? M.energy.p : nullptr, R);
+  if (tensor)
+    k_mf_hex27_tc<<<M.grid_tc, kTcThreads, OFF_TC_END, s>>>(M.nvol, M.vxyz.p, M.vrows.p, M.vlm.p, M.vdphi.p, M.vw.p,
+                                                            p4, q4, M.nface ? M.energy.p : nullptr, c.d_err.p, R);
+  else
+    k_mf_hex27<<<M.grid_vol, kMfThreads, 0, s>>>(M.nvol, M.vxyz.p, M.vrows.p, M.vlm.p, M.vdphi.p, M.vw.p, p4, q4,
+                                                 M.nface ? M.energy.p : nullptr, R);
   c.launches++;
 }
 

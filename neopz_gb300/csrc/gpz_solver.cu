@@ -1504,8 +1504,8 @@ Red red_of(Ctx &c);
 // one launch of the FP32 3x3 SpMV variant v: q32 = A32 pm
 void launch_spmv32(Ctx &c, int v, const Ctx::Sell &S, Red R, cudaStream_t s) {
   SolverWork &w = c.sw;
-  if (v == 5) {
-    matfree_spmv(c, s);  // element by element (gpz_matfree.cu), counts its own launches
+  if (v == 5 || v == 6) {
+    matfree_spmv(c, s, v == 6);  // element by element (gpz_matfree.cu), counts its own launches
     return;
   }
   if (v == 0) {
@@ -1614,7 +1614,13 @@ void tune_spmv32(Ctx &c, int only, bool timing) {
     GPZ_CUDA_TRY(cudaGetLastError());
     res.push_back({4, 0, time_it(4, cand[0])});
   }
-  if (want(5) && matfree_build(c)) res.push_back({5, 0, time_it(5, cand[0])});
+  if ((want(5) || want(6)) && matfree_build(c)) {
+    if (want(5)) res.push_back({5, 0, time_it(5, cand[0])});
+    if (want(6)) {
+      res.push_back({6, 0, time_it(6, cand[0])});
+      check_device_flag(c, "tensor-core matrix-free operator");
+    }
+  }
   if (res.empty()) res.push_back({0, 0, time_it(0, cand[0])});
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
@@ -1634,6 +1640,7 @@ void tune_spmv32(Ctx &c, int only, bool timing) {
                      : res[i].v == 3 ? "block_csr_tma_staged"
                      : res[i].v == 4 ? "upper_blocks_float4_atomics"
                      : res[i].v == 5 ? "matrix_free_elements"
+                     : res[i].v == 6 ? "matrix_free_tcgen05_3xtf32"
                                      : "sliced_ell";
     rep += std::string(i ? ", " : "") + "\"" + nm + (res[i].v == 2 ? "_w" + std::to_string(res[i].window) : "") +
            "\": " + std::to_string(res[i].ms);
@@ -1642,8 +1649,8 @@ void tune_spmv32(Ctx &c, int only, bool timing) {
   if (c.d_uptr.p) {
     GPZ_CUDA_TRY(cudaMemcpy(&nu, c.d_uptr.p + c.nbrow, sizeof(int64_t), cudaMemcpyDeviceToHost));
   }
-  const char *names[6] = {"block_csr", "block_csr_2rows", "sliced_ell", "block_csr_tma_staged",
-                          "upper_blocks_float4_atomics", "matrix_free_elements"};
+  const char *names[7] = {"block_csr", "block_csr_2rows", "sliced_ell", "block_csr_tma_staged",
+                          "upper_blocks_float4_atomics", "matrix_free_elements", "matrix_free_tcgen05_3xtf32"};
   c.tune_report = rep + ", \"chosen\": \"" + names[res[best].v] + "\", \"block_rows\": " + std::to_string(c.nbrow) +
                   ", \"blocks_full\": " + std::to_string(c.nnz / 9) + ", \"blocks_upper\": " + std::to_string(nu) +
                   "}";
@@ -1762,7 +1769,7 @@ void launch_iteration(Ctx &c, const Plan &P) {
     return;
   }
   const int padded = P.bsr ? 1 : 0;
-  const bool sym = P.bsr && (c.spmv32_variant == 4 || c.spmv32_variant == 5);  // q accumulated with atomics
+  const bool sym = P.bsr && c.spmv32_variant >= 4;  // 4, 5, 6: q accumulated with atomics
   k_mx_p<<<wave(k_mx_p), kThreads, 0, c.stream>>>(w.r32.p, P.M32, w.pm.p, padded, sym ? w.q32.p : nullptr, P.nunits,
                                                   R);
   if (P.bsr) {
@@ -2240,7 +2247,7 @@ void spmv32_apply(Ctx &c, int variant, const double *hx, double *hy) {
   SolverWork &w = c.sw;
   cudaStream_t s = c.stream;
   const bool padded_in = c.have_bsr3;
-  const bool padded_out = c.have_bsr3 && (c.spmv32_variant == 4 || c.spmv32_variant == 5);
+  const bool padded_out = c.have_bsr3 && c.spmv32_variant >= 4;
   std::vector<float> xin(w.pm.n, 0.f);
   for (int64_t i = 0; i < c.neq; i++) xin[padded_in ? 4 * (i / 3) + i % 3 : i] = (float)hx[i];
   GPZ_CUDA_TRY(cudaMemcpyAsync(w.pm.p, xin.data(), xin.size() * sizeof(float), cudaMemcpyHostToDevice, s));
