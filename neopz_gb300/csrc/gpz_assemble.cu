@@ -37,6 +37,7 @@ namespace {
 
 struct ElemArgs {
   const double *phi, *dphi, *w;
+  const double *ghat;  // reference Gram [NT][NT][3][3] of a volume hex bucket, or null
   const int *sside, *sk;
   int nq, ncorner, nsides, nshape;
   const double *xyz;
@@ -184,13 +185,51 @@ __global__ void __launch_bounds__(256) k_elem_fp64(ElemArgs P, HpArgs H, const i
     sIdx[a] = fa;
     sK[a] = ka;
   }
+  __shared__ int sAff;
+  __shared__ double sJi[3][3], sDet;
   if (tid == 0) {
     sOffBase = P.rhs_only ? 0 : P.offbase[e];
     double cf = P.kind == GPZ_MAT_ELAST3D ? P.E : P.coef_const;
     if (!BC && P.coef) cf = P.coef[e];
     sCoef = cf;
+    sAff = 0;
   }
   __syncthreads();
+  if (!BC && DIM == 3 && P.ghat != nullptr && tid == 0) {
+    // affine hex: the trilinear map's xi.eta, xi.zeta, eta.zeta and xi.eta.zeta
+    // coefficients vanish, the Jacobian is constant and the element Gram is
+    // |J| Jinv^T G Jinv with the bucket's reference Gram G
+    const signed char c4[8] = {1, -1, 1, -1, 1, -1, 1, -1}, c5[8] = {1, -1, -1, 1, -1, 1, 1, -1},
+                      c6[8] = {1, 1, -1, -1, -1, -1, 1, 1}, c7[8] = {-1, 1, -1, 1, 1, -1, 1, -1};
+    double big = 0.0, hi = 0.0;
+    for (int j = 0; j < 3; j++) {
+      double t4 = 0, t5 = 0, t6 = 0, t7 = 0, mn = sC[j], mx = sC[j];
+      for (int k = 0; k < 8; k++) {
+        const double x = sC[k * 3 + j];
+        t4 += c4[k] * x;
+        t5 += c5[k] * x;
+        t6 += c6[k] * x;
+        t7 += c7[k] * x;
+        mn = fmin(mn, x);
+        mx = fmax(mx, x);
+      }
+      hi = fmax(hi, fmax(fmax(fabs(t4), fabs(t5)), fmax(fabs(t6), fabs(t7))));
+      big = fmax(big, mx - mn);
+    }
+    if (hi <= 1e-12 * big) {
+      // the Jacobian from the corner gradients at the first point (as at every point)
+      double dc[3 * 8];
+      for (int k = 0; k < nc; k++)
+        for (int d = 0; d < DIM; d++) dc[d * 8 + k] = P.dphi[(0 * DIM + d) * NT + k];
+      double ji[3][3];
+      sDet = jacobian_at<DIM>(sC, dc, nc, ji);
+      for (int i = 0; i < 3; i++)
+        for (int j = 0; j < 3; j++) sJi[i][j] = ji[i][j];
+      sAff = 1;
+    }
+  }
+  __syncthreads();
+  const bool aff = sAff != 0;
 
   // per-point geometry
   for (int q = tid; q < nq; q += blockDim.x) {
@@ -205,14 +244,14 @@ __global__ void __launch_bounds__(256) k_elem_fp64(ElemArgs P, HpArgs H, const i
     }
     (void)pt;
     double jinv[3][3];
-    double det = jacobian_at<DIM>(sC, dc, nc, jinv);
+    const double det = aff ? sDet : jacobian_at<DIM>(sC, dc, nc, jinv);
     sW[q] = P.w[q] * det;
     for (int j = 0; j < 3; j++) {
       double x = 0.0;
       for (int k = 0; k < nc; k++) x += phic[k] * sC[k * 3 + j];
       sX[q * 3 + j] = x;
     }
-    if (!BC) {
+    if (!BC && !aff) {
       // store jinv temporarily in sG is not possible; compute gradients directly
       for (int a = 0; a < NSH; a++) {
         const int fa = HP ? sIdx[a] : a;
@@ -275,6 +314,24 @@ __global__ void __launch_bounds__(256) k_elem_fp64(ElemArgs P, HpArgs H, const i
       for (int q = 0; q < nq; q++) m += sW[q] * P.phi[q * NT + fa] * P.phi[q * NT + fb];
       for (int s = 0; s < NST; s++)
         for (int t = 0; t < NST; t++) K[s][t] = (s == t) ? P.big * m : 0.0;
+    } else if (aff) {
+      // S = |J| Jinv^T G_ab Jinv (S[d][e] = sum_q w |J| g_a,d g_b,e as below)
+      const int fa = HP ? sIdx[a] : a, fb = HP ? sIdx[b] : b;
+      const double *G = P.ghat + ((size_t)fa * NT + fb) * 9;
+      double M1[3][3], S[3][3];
+      for (int i = 0; i < 3; i++)
+        for (int e2 = 0; e2 < 3; e2++) M1[i][e2] = G[i * 3 + 0] * sJi[0][e2] + G[i * 3 + 1] * sJi[1][e2] + G[i * 3 + 2] * sJi[2][e2];
+      for (int d = 0; d < 3; d++)
+        for (int e2 = 0; e2 < 3; e2++)
+          S[d][e2] = sDet * (sJi[0][d] * M1[0][e2] + sJi[1][d] * M1[1][e2] + sJi[2][d] * M1[2][e2]);
+      if (NST == 1) {
+        K[0][0] = (P.kind == GPZ_MAT_POISSON ? P.scale : coef) * (S[0][0] + S[1][1] + S[2][2]);
+      } else {
+        double tr = S[0][0] + S[1][1] + S[2][2];
+        for (int s = 0; s < NST; s++)
+          for (int t = 0; t < NST; t++)
+            K[s][t] = (s == t) ? (tr - S[s][s]) * C1 + S[s][s] * C3 : S[t][s] * C1 - S[s][t] * C2;
+      }
     } else if (NST == 1) {
       double acc = 0.0;
       for (int q = 0; q < nq; q++) {
@@ -529,6 +586,19 @@ void build_buckets(Ctx &c, const gpz_mesh_desc &d) {
         }
       }
       b->ndof = b->nshape * c.nstate;
+      if (k.type == GPZ_EL_HEX && !k.is_bc) {
+        const int nt = b->nshape;
+        b->ghat.assign((size_t)nt * nt * 9, 0.0);
+        for (int a = 0; a < nt; a++)
+          for (int bb = 0; bb < nt; bb++)
+            for (int i = 0; i < 3; i++)
+              for (int j = 0; j < 3; j++) {
+                long double acc = 0.0L;
+                for (int q = 0; q < b->nq; q++)
+                  acc += (long double)b->w[q] * b->dphi[(q * 3 + i) * nt + a] * b->dphi[(q * 3 + j) * nt + bb];
+                b->ghat[((size_t)a * nt + bb) * 9 + i * 3 + j] = (double)acc;
+              }
+      }
       b->hp = k.hp != 0;
       GPZ_REQUIRE(b->hp ? select_hp(k.type, c.nstate, k.is_bc) != nullptr
                         : select_kernel(k.type, b->nshape, c.nstate, k.is_bc) != nullptr,
@@ -595,6 +665,7 @@ void build_buckets(Ctx &c, const gpz_mesh_desc &d) {
     b->d_phi.upload(b->phi.data(), b->phi.size(), c.stream);
     b->d_dphi.upload(b->dphi.data(), b->dphi.size(), c.stream);
     b->d_w.upload(b->w.data(), b->w.size(), c.stream);
+    if (!b->ghat.empty()) b->d_ghat.upload(b->ghat.data(), b->ghat.size(), c.stream);
     b->d_shape_side.upload(b->shape_side.data(), b->shape_side.size(), c.stream);
     b->d_shape_k.upload(b->shape_k.data(), b->shape_k.size(), c.stream);
     b->d_elems.upload(b->elems.data(), b->elems.size(), c.stream);
@@ -609,6 +680,7 @@ ElemArgs args_of(Ctx &c, const Bucket *b) {
   P.phi = b->d_phi.p;
   P.dphi = b->d_dphi.p;
   P.w = b->d_w.p;
+  P.ghat = b->d_ghat.p;
   P.sside = b->d_shape_side.p;
   P.sk = b->d_shape_k.p;
   P.nq = b->nq;

@@ -82,6 +82,9 @@ struct Bucket {
   std::vector<int> shape_side, shape_k;      // shape -> side, index inside the side
   // device tables
   DBuf<double> d_phi, d_dphi, d_w;
+  // reference Gram of the volume hex tables: G[a][b][i][j] = sum_q w_q dphi_i(a) dphi_j(b) (affine elements)
+  std::vector<double> ghat;
+  DBuf<double> d_ghat;
   DBuf<int> d_shape_side, d_shape_k;
   // elements of this bucket grouped by colour
   std::vector<int64_t> elems;                // global element indices

@@ -208,6 +208,10 @@ class Grid:
         self.desc = gpz_mesh_desc()
         H.gpzh_grid_desc(self.h, ctypes.byref(self.desc))
 
+    def nodes(self):
+        """Node coordinates [nnodes][3] of the descriptor (a writable view: edit before upload_mesh)."""
+        return np.ctypeslib.as_array(self.desc.node_xyz, shape=(self.desc.nnodes, 3))
+
     def cells(self):
         """Grid cell of every element (-1 for boundary elements)."""
         c = np.zeros(self.nel, np.int64)

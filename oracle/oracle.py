@@ -75,6 +75,7 @@ def lib():
         L.orc_cel_info.argtypes = [vp, i64, P(i32), P(i32), P(i64), vp, vp]
         L.orc_block_info.argtypes = [vp, vp, vp]
         L.orc_nodes.argtypes = [vp, vp]
+        L.orc_set_nodes.argtypes = [vp, vp]
         L.orc_calc_stiff.restype = i32
         L.orc_calc_stiff.argtypes = [vp, i64, vp, vp]
         L.orc_shape.restype = i32
@@ -174,6 +175,10 @@ class OracleMesh:
         xyz = np.zeros((n, 3))
         lib().orc_nodes(self.h, _p(xyz))
         return xyz
+
+    def set_nodes(self, xyz):
+        xyz = np.ascontiguousarray(xyz, np.float64)
+        lib().orc_set_nodes(self.h, _p(xyz))
 
     def cel(self, ic):
         t, b, g = ctypes.c_int(), ctypes.c_int(), ctypes.c_int64()

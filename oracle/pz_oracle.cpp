@@ -1092,6 +1092,13 @@ void orc_nodes(void *h, double *xyz) {
   std::copy(m->nodes.begin(), m->nodes.end(), xyz);
 }
 
+// Move the mesh nodes (the same numbering): a distorted, non-affine mesh
+// for the tests, as a user program editing TPZGeoNode coordinates would.
+void orc_set_nodes(void *h, const double *xyz) {
+  Mesh *m = (Mesh *)h;
+  std::copy(xyz, xyz + m->nodes.size(), m->nodes.begin());
+}
+
 int orc_calc_stiff(void *h, int64_t ic, double *ek, double *ef) {
   Mesh *m = (Mesh *)h;
   return calc_stiff(*m, m->cels[ic], ek, ef);
