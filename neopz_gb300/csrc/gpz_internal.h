@@ -152,6 +152,7 @@ struct MatFree {
   bool ready = false;
   int64_t nvol = 0, nface = 0;
   DBuf<float> vxyz, vlm, vdphi, vw;          // volume: corners [n][8][3], (lambda, mu) [n][2], tables
+  DBuf<float> vgeo;                          // [n][10] affine elements: Jinv (row-major), |det J| (0: not affine)
   DBuf<int32_t> vrows;                       // [n][27] block row of each shape
   DBuf<float> fxyz, fphi, fdphi, fw;         // penalty faces
   DBuf<int32_t> frows;

@@ -34,19 +34,70 @@ constexpr int kFS = 9;   // Q2 face shapes
 constexpr int kFQ = 9;   // 3 x 3 face points
 constexpr int kWarps = kThreads / 32;
 
-// element records: corner coordinates, block rows of the shapes, (lambda, mu)
+__device__ __forceinline__ double x_of(const double (&cx)[8][3], int k, int j) { return cx[k][j]; }
+
+// element records: corner coordinates, block rows of the shapes, (lambda, mu),
+// and for affine hexes the constant inverse Jacobian and |det J|
 __global__ void k_mf_records(int64_t n, const int64_t *__restrict__ elems, const int64_t *__restrict__ el_nodes,
                              const double *__restrict__ xyz, const int64_t *__restrict__ el_conn,
                              const int64_t *__restrict__ bpos, const int *__restrict__ sside,
                              const int *__restrict__ sk, int nsh, int nc, const double *__restrict__ coef, double E0,
                              double nu, float *__restrict__ rxyz, int32_t *__restrict__ rrows, float *__restrict__ rlm,
-                             int *__restrict__ err) {
+                             float *__restrict__ rgeo, int *__restrict__ err) {
   const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
   const int64_t e = elems[i];
+  double cx[8][3];
   for (int k = 0; k < nc; k++) {
     const int64_t node = el_nodes[e * 8 + k];
-    for (int j = 0; j < 3; j++) rxyz[(i * nc + k) * 3 + j] = (float)xyz[node * 3 + j];
+    for (int j = 0; j < 3; j++) {
+      cx[k][j] = xyz[node * 3 + j];
+      rxyz[(i * nc + k) * 3 + j] = (float)cx[k][j];
+    }
+  }
+  if (rgeo) {
+    // affine hex (vanishing xi.eta, xi.zeta, eta.zeta, xi.eta.zeta coefficients):
+    // constant Jacobian; (Jinv, |det J|), det 0 marks a non-affine element
+    const signed char sg[8][3] = {{-1, -1, -1}, {1, -1, -1}, {1, 1, -1}, {-1, 1, -1},
+                                  {-1, -1, 1},  {1, -1, 1},  {1, 1, 1},  {-1, 1, 1}};
+    double hi = 0.0, big = 0.0, a[3][3];
+    for (int j = 0; j < 3; j++) {
+      double t4 = 0, t5 = 0, t6 = 0, t7 = 0, mn = cx[0][j], mx = cx[0][j];
+      for (int k = 0; k < 8; k++) {
+        const double x = cx[k][j];
+        t4 += sg[k][0] * sg[k][1] * x;
+        t5 += sg[k][0] * sg[k][2] * x;
+        t6 += sg[k][1] * sg[k][2] * x;
+        t7 += sg[k][0] * sg[k][1] * sg[k][2] * x;
+        mn = fmin(mn, x);
+        mx = fmax(mx, x);
+      }
+      hi = fmax(hi, fmax(fmax(fabs(t4), fabs(t5)), fmax(fabs(t6), fabs(t7))));
+      big = fmax(big, mx - mn);
+      for (int d = 0; d < 3; d++) {
+        double t = 0.0;
+        for (int k = 0; k < 8; k++) t += sg[k][d] * x_of(cx, k, j);
+        a[j][d] = t / 8.0;
+      }
+    }
+    float *g = rgeo + i * 10;
+    if (hi <= 1e-12 * big) {
+      const double det = -a[0][2] * a[1][1] * a[2][0] + a[0][1] * a[1][2] * a[2][0] + a[0][2] * a[1][0] * a[2][1] -
+                         a[0][0] * a[1][2] * a[2][1] - a[0][1] * a[1][0] * a[2][2] + a[0][0] * a[1][1] * a[2][2];
+      const double id = 1.0 / det;
+      g[0] = (float)((-a[1][2] * a[2][1] + a[1][1] * a[2][2]) * id);
+      g[1] = (float)((a[0][2] * a[2][1] - a[0][1] * a[2][2]) * id);
+      g[2] = (float)((-a[0][2] * a[1][1] + a[0][1] * a[1][2]) * id);
+      g[3] = (float)((a[1][2] * a[2][0] - a[1][0] * a[2][2]) * id);
+      g[4] = (float)((-a[0][2] * a[2][0] + a[0][0] * a[2][2]) * id);
+      g[5] = (float)((a[0][2] * a[1][0] - a[0][0] * a[1][2]) * id);
+      g[6] = (float)((-a[1][1] * a[2][0] + a[1][0] * a[2][1]) * id);
+      g[7] = (float)((a[0][1] * a[2][0] - a[0][0] * a[2][1]) * id);
+      g[8] = (float)((-a[0][1] * a[1][0] + a[0][0] * a[1][1]) * id);
+      g[9] = (float)fabs(det);
+    } else {
+      for (int k = 0; k < 10; k++) g[k] = 0.f;
+    }
   }
   for (int a = 0; a < nsh; a++) {
     const int64_t eq = bpos[el_conn[e * 27 + sside[a]]] + (int64_t)sk[a] * 3;
@@ -134,6 +185,7 @@ constexpr int kMfWarps = kMfThreads / 32;
 __global__ void __launch_bounds__(kMfThreads, 3) k_mf_hex27(int64_t n, const float *__restrict__ rxyz,
                                                             const int32_t *__restrict__ rows,
                                                             const float *__restrict__ rlm,
+                                                            const float *__restrict__ rgeo,
                                                             const float *__restrict__ dphi /*[q][3][a]*/,
                                                             const float *__restrict__ w,
                                                             const float4 *__restrict__ p4, float4 *__restrict__ q4,
@@ -141,7 +193,7 @@ __global__ void __launch_bounds__(kMfThreads, 3) k_mf_hex27(int64_t n, const flo
   if (!active(R.iscal)) return;
   __shared__ float4 sdt[kNQ][32];            // [q][a] = (d0, d1, d2, 0) of shape a at point q
   __shared__ float4 su[kMfWarps][kNS];
-  __shared__ float sc[kMfWarps][24];
+  __shared__ float sc[kMfWarps][24 + 10];  // corners, then the affine geometry (Jinv, |det|)
   __shared__ float4 st[kMfWarps][kNQ][3];
   const int lane = threadIdx.x & 31, wp = threadIdx.x >> 5;
   for (int k = threadIdx.x; k < kNQ * 32; k += blockDim.x) {
@@ -166,10 +218,11 @@ __global__ void __launch_bounds__(kMfThreads, 3) k_mf_hex27(int64_t n, const flo
   int64_t i = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   // records of the first element
   int32_t row = 0;
-  float cxv = 0.f, lam = 0.f, mu = 0.f;
+  float cxv = 0.f, gv = 0.f, lam = 0.f, mu = 0.f;
   if (i < n) {
     if (lane < kNS) row = rows[i * kNS + lane];
     if (lane < 24) cxv = rxyz[i * 24 + lane];
+    if (lane < 10) gv = rgeo[i * 10 + lane];
     lam = rlm[2 * i];
     mu = rlm[2 * i + 1];
   }
@@ -180,6 +233,7 @@ __global__ void __launch_bounds__(kMfThreads, 3) k_mf_hex27(int64_t n, const flo
       su[wp][lane] = u;
     }
     if (lane < 24) sc[wp][lane] = cxv;
+    if (lane < 10) sc[wp][24 + lane] = gv;
     const float lam_i = lam, mu_i = mu;
     const int32_t row_i = row;
     // prefetch the next element's records
@@ -187,32 +241,40 @@ __global__ void __launch_bounds__(kMfThreads, 3) k_mf_hex27(int64_t n, const flo
     if (nx < n) {
       if (lane < kNS) row = rows[nx * kNS + lane];
       if (lane < 24) cxv = rxyz[nx * 24 + lane];
+      if (lane < 10) gv = rgeo[nx * 10 + lane];
       lam = rlm[2 * nx];
       mu = rlm[2 * nx + 1];
     }
     __syncwarp();
     if (lane < kNQ) {
-      // Jacobian from the corner shapes (the first 8 of the table), as TPZGeoEl::Jacobian
-      float a[3][3] = {{0.f, 0.f, 0.f}, {0.f, 0.f, 0.f}, {0.f, 0.f, 0.f}};
+      float ji[3][3], det;
+      if (sc[wp][24 + 9] > 0.f) {
+        // affine element: the constant Jacobian of the records
 #pragma unroll
-      for (int k = 0; k < 8; k++)
+        for (int k = 0; k < 9; k++) ji[k / 3][k % 3] = sc[wp][24 + k];
+        det = sc[wp][24 + 9];
+      } else {
+        // Jacobian from the corner shapes (the first 8 of the table), as TPZGeoEl::Jacobian
+        float a[3][3] = {{0.f, 0.f, 0.f}, {0.f, 0.f, 0.f}, {0.f, 0.f, 0.f}};
 #pragma unroll
-        for (int j = 0; j < 3; j++)
+        for (int k = 0; k < 8; k++)
 #pragma unroll
-          for (int d = 0; d < 3; d++) a[j][d] += sc[wp][k * 3 + j] * D[d][k];
-      const float det = -a[0][2] * a[1][1] * a[2][0] + a[0][1] * a[1][2] * a[2][0] + a[0][2] * a[1][0] * a[2][1] -
-                        a[0][0] * a[1][2] * a[2][1] - a[0][1] * a[1][0] * a[2][2] + a[0][0] * a[1][1] * a[2][2];
-      const float id = 1.f / det;
-      float ji[3][3];
-      ji[0][0] = (-a[1][2] * a[2][1] + a[1][1] * a[2][2]) * id;
-      ji[0][1] = (a[0][2] * a[2][1] - a[0][1] * a[2][2]) * id;
-      ji[0][2] = (-a[0][2] * a[1][1] + a[0][1] * a[1][2]) * id;
-      ji[1][0] = (a[1][2] * a[2][0] - a[1][0] * a[2][2]) * id;
-      ji[1][1] = (-a[0][2] * a[2][0] + a[0][0] * a[2][2]) * id;
-      ji[1][2] = (a[0][2] * a[1][0] - a[0][0] * a[1][2]) * id;
-      ji[2][0] = (-a[1][1] * a[2][0] + a[1][0] * a[2][1]) * id;
-      ji[2][1] = (a[0][1] * a[2][0] - a[0][0] * a[2][1]) * id;
-      ji[2][2] = (-a[0][1] * a[1][0] + a[0][0] * a[1][1]) * id;
+          for (int j = 0; j < 3; j++)
+#pragma unroll
+            for (int d = 0; d < 3; d++) a[j][d] += sc[wp][k * 3 + j] * D[d][k];
+        det = -a[0][2] * a[1][1] * a[2][0] + a[0][1] * a[1][2] * a[2][0] + a[0][2] * a[1][0] * a[2][1] -
+              a[0][0] * a[1][2] * a[2][1] - a[0][1] * a[1][0] * a[2][2] + a[0][0] * a[1][1] * a[2][2];
+        const float id = 1.f / det;
+        ji[0][0] = (-a[1][2] * a[2][1] + a[1][1] * a[2][2]) * id;
+        ji[0][1] = (a[0][2] * a[2][1] - a[0][1] * a[2][2]) * id;
+        ji[0][2] = (-a[0][2] * a[1][1] + a[0][1] * a[1][2]) * id;
+        ji[1][0] = (a[1][2] * a[2][0] - a[1][0] * a[2][2]) * id;
+        ji[1][1] = (-a[0][2] * a[2][0] + a[0][0] * a[2][2]) * id;
+        ji[1][2] = (a[0][2] * a[1][0] - a[0][0] * a[1][2]) * id;
+        ji[2][0] = (-a[1][1] * a[2][0] + a[1][0] * a[2][1]) * id;
+        ji[2][1] = (a[0][1] * a[2][0] - a[0][0] * a[2][1]) * id;
+        ji[2][2] = (-a[0][1] * a[1][0] + a[0][0] * a[1][1]) * id;
+      }
       // reference gradient of u at the point, then physical H[s][d] = sum_j Hh[s][j] ji[j][d]
       float hh[3][3] = {{0.f, 0.f, 0.f}, {0.f, 0.f, 0.f}, {0.f, 0.f, 0.f}};
 #pragma unroll
@@ -294,7 +356,8 @@ constexpr uint32_t kB1 = 96 * 32 * 4, kB2 = 32 * 96 * 4, kA1 = 128 * 32 * 4, kA2
 constexpr uint32_t OFF_B1H = 0, OFF_B1L = OFF_B1H + kB1, OFF_B2H = OFF_B1L + kB1, OFF_B2L = OFF_B2H + kB2;
 constexpr uint32_t OFF_A1H = OFF_B2L + kB2, OFF_A1L = OFF_A1H + kA1, OFF_A2H = OFF_A1L + kA1, OFF_A2L = OFF_A2H + kA2;
 constexpr uint32_t OFF_CG = OFF_A2L + kA2, OFF_W = OFF_CG + 27 * 3 * 8 * 4, OFF_CX = OFF_W + 32 * 4;
-constexpr uint32_t OFF_LM = OFF_CX + kTcEl * 24 * 4, OFF_ST1 = OFF_LM + kTcEl * 2 * 4;
+constexpr uint32_t OFF_LM = OFF_CX + kTcEl * 24 * 4, OFF_GEO = OFF_LM + kTcEl * 2 * 4;
+constexpr uint32_t OFF_ST1 = OFF_GEO + kTcEl * 10 * 4;
 constexpr uint32_t OFF_TC_END = OFF_ST1 + 128 * 32 * 4;  // results staging (phase-2 rows)
 constexpr int kTcGather = kTcEl * 32 / kTcThreads;        // (element, shape) items per thread
 constexpr int kTcItems = (kTcEl * 27 + kTcThreads - 1) / kTcThreads;  // (element, point) items per thread
@@ -349,7 +412,7 @@ __device__ __forceinline__ void tc_ld16(uint32_t taddr, float *v) {
 // every load is issued before the first store
 __device__ __forceinline__ void tc_gather(unsigned char *sm, int64_t e0, int64_t n, const int32_t *__restrict__ rows,
                                           const float4 *__restrict__ p4, const float *__restrict__ rxyz,
-                                          const float *__restrict__ rlm, int tid) {
+                                          const float *__restrict__ rlm, const float *__restrict__ rgeo, int tid) {
   int32_t ri[kTcGather];
   float4 pv[kTcGather];
 #pragma unroll
@@ -372,6 +435,12 @@ __device__ __forceinline__ void tc_gather(unsigned char *sm, int64_t e0, int64_t
     lv[0] = rlm[2 * (e0 + tid)];
     lv[1] = rlm[2 * (e0 + tid) + 1];
   }
+  float gv[2];
+#pragma unroll
+  for (int k = 0; k < 2; k++) {
+    const int t = tid + k * kTcThreads;
+    gv[k] = (t < kTcEl * 10 && e0 + t / 10 < n) ? rgeo[(e0 + t / 10) * 10 + t % 10] : 0.f;
+  }
 #pragma unroll
   for (int k = 0; k < kTcGather; k++) {
     const int t = tid + k * kTcThreads, le = t / 32, b = t % 32;
@@ -390,11 +459,18 @@ __device__ __forceinline__ void tc_gather(unsigned char *sm, int64_t e0, int64_t
     lm[2 * tid] = lv[0];
     lm[2 * tid + 1] = lv[1];
   }
+  float *geo = (float *)(sm + OFF_GEO);
+#pragma unroll
+  for (int k = 0; k < 2; k++) {
+    const int t = tid + k * kTcThreads;
+    if (t < kTcEl * 10) geo[t] = gv[k];
+  }
 }
 
 __global__ void __launch_bounds__(kTcThreads, 1) k_mf_hex27_tc(int64_t n, const float *__restrict__ rxyz,
                                                                const int32_t *__restrict__ rows,
                                                                const float *__restrict__ rlm,
+                                                               const float *__restrict__ rgeo,
                                                                const float *__restrict__ dphi /*[q][3][a]*/,
                                                                const float *__restrict__ w,
                                                                const float4 *__restrict__ p4, float4 *__restrict__ q4,
@@ -442,7 +518,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_mf_hex27_tc(int64_t n, const 
   KSum en;
   uint32_t parity = 0;
   bool failed = false;
-  if ((int64_t)blockIdx.x * kTcEl < n) tc_gather(sm, (int64_t)blockIdx.x * kTcEl, n, rows, p4, rxyz, rlm, tid);
+  if ((int64_t)blockIdx.x * kTcEl < n) tc_gather(sm, (int64_t)blockIdx.x * kTcEl, n, rows, p4, rxyz, rlm, rgeo, tid);
   for (int64_t tile = blockIdx.x; tile * kTcEl < n && !failed; tile += gridDim.x) {
     const int64_t e0 = tile * kTcEl;
     asm volatile("fence.proxy.async.shared::cta;");
@@ -498,26 +574,33 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_mf_hex27_tc(int64_t n, const 
         for (int j = 0; j < 3; j++) hh[s2][j] = srow[(rl + s2) * 81 + q * 3 + j];
       const float lam = lm[2 * le], mu = lm[2 * le + 1];
       const float *ce = cx + le * 24;
-      float a[3][3] = {{0.f, 0.f, 0.f}, {0.f, 0.f, 0.f}, {0.f, 0.f, 0.f}};
+      const float *ge = (const float *)(sm + OFF_GEO) + le * 10;
+      float ji[3][3], det;
+      if (ge[9] > 0.f) {  // affine element: the constant Jacobian of the records
 #pragma unroll
-      for (int c = 0; c < 8; c++)
+        for (int m = 0; m < 9; m++) ji[m / 3][m % 3] = ge[m];
+        det = ge[9];
+      } else {
+        float a[3][3] = {{0.f, 0.f, 0.f}, {0.f, 0.f, 0.f}, {0.f, 0.f, 0.f}};
 #pragma unroll
-        for (int j = 0; j < 3; j++)
+        for (int c = 0; c < 8; c++)
 #pragma unroll
-          for (int d = 0; d < 3; d++) a[j][d] += ce[c * 3 + j] * cg[(q * 3 + d) * 8 + c];
-      const float det = -a[0][2] * a[1][1] * a[2][0] + a[0][1] * a[1][2] * a[2][0] + a[0][2] * a[1][0] * a[2][1] -
-                        a[0][0] * a[1][2] * a[2][1] - a[0][1] * a[1][0] * a[2][2] + a[0][0] * a[1][1] * a[2][2];
-      const float id = 1.f / det;
-      float ji[3][3];
-      ji[0][0] = (-a[1][2] * a[2][1] + a[1][1] * a[2][2]) * id;
-      ji[0][1] = (a[0][2] * a[2][1] - a[0][1] * a[2][2]) * id;
-      ji[0][2] = (-a[0][2] * a[1][1] + a[0][1] * a[1][2]) * id;
-      ji[1][0] = (a[1][2] * a[2][0] - a[1][0] * a[2][2]) * id;
-      ji[1][1] = (-a[0][2] * a[2][0] + a[0][0] * a[2][2]) * id;
-      ji[1][2] = (a[0][2] * a[1][0] - a[0][0] * a[1][2]) * id;
-      ji[2][0] = (-a[1][1] * a[2][0] + a[1][0] * a[2][1]) * id;
-      ji[2][1] = (a[0][1] * a[2][0] - a[0][0] * a[2][1]) * id;
-      ji[2][2] = (-a[0][1] * a[1][0] + a[0][0] * a[1][1]) * id;
+          for (int j = 0; j < 3; j++)
+#pragma unroll
+            for (int d = 0; d < 3; d++) a[j][d] += ce[c * 3 + j] * cg[(q * 3 + d) * 8 + c];
+        det = -a[0][2] * a[1][1] * a[2][0] + a[0][1] * a[1][2] * a[2][0] + a[0][2] * a[1][0] * a[2][1] -
+              a[0][0] * a[1][2] * a[2][1] - a[0][1] * a[1][0] * a[2][2] + a[0][0] * a[1][1] * a[2][2];
+        const float id = 1.f / det;
+        ji[0][0] = (-a[1][2] * a[2][1] + a[1][1] * a[2][2]) * id;
+        ji[0][1] = (a[0][2] * a[2][1] - a[0][1] * a[2][2]) * id;
+        ji[0][2] = (-a[0][2] * a[1][1] + a[0][1] * a[1][2]) * id;
+        ji[1][0] = (a[1][2] * a[2][0] - a[1][0] * a[2][2]) * id;
+        ji[1][1] = (-a[0][2] * a[2][0] + a[0][0] * a[2][2]) * id;
+        ji[1][2] = (a[0][2] * a[1][0] - a[0][0] * a[1][2]) * id;
+        ji[2][0] = (-a[1][1] * a[2][0] + a[1][0] * a[2][1]) * id;
+        ji[2][1] = (a[0][1] * a[2][0] - a[0][0] * a[2][1]) * id;
+        ji[2][2] = (-a[0][1] * a[1][0] + a[0][0] * a[1][1]) * id;
+      }
       float H[3][3];
 #pragma unroll
       for (int s2 = 0; s2 < 3; s2++)
@@ -576,7 +659,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_mf_hex27_tc(int64_t n, const 
       tc_commit(&s_mb[1]);
     }
     // the next tile's nodal values go into U while the phase-2 MMAs run (they read A2 / B2 only)
-    if ((tile + gridDim.x) * kTcEl < n) tc_gather(sm, (tile + gridDim.x) * kTcEl, n, rows, p4, rxyz, rlm, tid);
+    if ((tile + gridDim.x) * kTcEl < n) tc_gather(sm, (tile + gridDim.x) * kTcEl, n, rows, p4, rxyz, rlm, rgeo, tid);
     ok = tc_wait(&s_mb[1], parity);
     if (__syncthreads_or(!ok)) {
       failed = true;
@@ -666,11 +749,13 @@ bool matfree_build(Ctx &c) {
   M.vxyz.alloc((size_t)M.nvol * 24);
   M.vrows.alloc((size_t)M.nvol * kNS);
   M.vlm.alloc((size_t)M.nvol * 2);
+  M.vgeo.alloc((size_t)M.nvol * 10);
   f32(vol->dphi, M.vdphi);
   f32(vol->w, M.vw);
   k_mf_records<<<grid_for(M.nvol, 256), 256, 0, s>>>(M.nvol, vol->d_elems.p, c.d_el_nodes.p, c.d_xyz.p, c.d_el_conn.p,
                                                      c.d_block_pos.p, vol->d_shape_side.p, vol->d_shape_k.p, kNS, 8,
-                                                     c.d_coef.p, m.E, m.nu, M.vxyz.p, M.vrows.p, M.vlm.p, c.d_err.p);
+                                                     c.d_coef.p, m.E, m.nu, M.vxyz.p, M.vrows.p, M.vlm.p, M.vgeo.p,
+                                                     c.d_err.p);
   c.launches++;
   M.nface = 0;
   if (!faces.empty()) {
@@ -685,7 +770,7 @@ bool matfree_build(Ctx &c) {
     k_mf_records<<<grid_for(M.nface, 256), 256, 0, s>>>(M.nface, f->d_elems.p, c.d_el_nodes.p, c.d_xyz.p,
                                                         c.d_el_conn.p, c.d_block_pos.p, f->d_shape_side.p,
                                                         f->d_shape_k.p, kFS, 4, nullptr, 0.0, 0.0, M.fxyz.p,
-                                                        M.frows.p, nullptr, c.d_err.p);
+                                                        M.frows.p, nullptr, nullptr, c.d_err.p);
     c.launches++;
   }
   M.energy.alloc(1);
@@ -718,10 +803,11 @@ void matfree_spmv(Ctx &c, cudaStream_t s, bool tensor) {
     c.launches++;
   }
   if (tensor)
-    k_mf_hex27_tc<<<M.grid_tc, kTcThreads, OFF_TC_END, s>>>(M.nvol, M.vxyz.p, M.vrows.p, M.vlm.p, M.vdphi.p, M.vw.p,
+    k_mf_hex27_tc<<<M.grid_tc, kTcThreads, OFF_TC_END, s>>>(M.nvol, M.vxyz.p, M.vrows.p, M.vlm.p, M.vgeo.p, M.vdphi.p,
+                                                            M.vw.p,
                                                             p4, q4, M.nface ? M.energy.p : nullptr, c.d_err.p, R);
   else
-    k_mf_hex27<<<M.grid_vol, kMfThreads, 0, s>>>(M.nvol, M.vxyz.p, M.vrows.p, M.vlm.p, M.vdphi.p, M.vw.p, p4, q4,
+    k_mf_hex27<<<M.grid_vol, kMfThreads, 0, s>>>(M.nvol, M.vxyz.p, M.vrows.p, M.vlm.p, M.vgeo.p, M.vdphi.p, M.vw.p, p4, q4,
                                                  M.nface ? M.energy.p : nullptr, R);
   c.launches++;
 }
