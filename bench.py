@@ -235,6 +235,23 @@ def run_gpu(args):
     if chosen in NCU_TRAFFIC_PER_BLOCK:
         traffic = int(NCU_TRAFFIC_PER_BLOCK[chosen] * nblk)
 
+    # exact-solution error norms (TPZAnalysis::PostProcessError) of the last solution kept on the device,
+    # against u = 0: the norms (energy, L2, H1 semi) of the solution itself, the load having no closed-form
+    # solution; the evaluation call includes the upload of the exact values (zeros) at every point
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    exyz = ctx.error_points(2)
+    t1 = time.perf_counter()
+    ue, due = np.zeros((len(exyz), 3)), np.zeros((len(exyz), 3, 3))
+    t2 = time.perf_counter()
+    enorm, _ = ctx.error_norms(2, ue, due)
+    t3 = time.perf_counter()
+    err_leg = {"exact_order": 2, "points": int(len(exyz)), "solution_norms": [float(v) for v in enorm],
+               "points_s": round(t1 - t0, 4), "evaluate_s": round(t3 - t2, 4),
+               "volume_elements_per_s": round(nvol / (t3 - t2), 1),
+               "h2d_bytes": int(ue.nbytes + due.nbytes)}
+    del exyz, ue, due
+
     # end to end through the C ABI from host buffers
     e2e_times = []
     b_in = mesh_bytes(grid)
@@ -283,6 +300,7 @@ def run_gpu(args):
                      "peak_source": "MEASURED_PEAKS.json hbm_gbs (burst copy)" if "fallback" not in pk else
                      "fallback 6.8 TB/s"},
         "spmv_autotune_ms": ctx.tuning_report(),
+        "error_norms": err_leg,
         "clocks": clk,
         "gpu_launches": int(launches),
     }

@@ -51,6 +51,7 @@ extern "C" {
 #define GPZ_F_NONE 0
 #define GPZ_F_CONST 1       /* force[0..2] */
 #define GPZ_F_SINPROD 2     /* force[0] * d pi^2 prod_k sin(pi x_k) */
+#define GPZ_F_QUADRATIC 3   /* force[0] + force[1] |x|^2 (4 - 2x^2 - 2y^2 of UnitTest_PZ/TestMesh/TestError.cpp:62-68) */
 
 typedef struct {
   int32_t kind;           /* GPZ_MAT_* */
@@ -222,6 +223,32 @@ int gpz_solution_download(gpz_ctx *ctx, double *x);
 #define GPZ_KERNEL_SPMV_FP32 2
 #define GPZ_KERNEL_ASSEMBLE 3
 int gpz_time_kernel(gpz_ctx *ctx, int which, int reps, double *ms_per_launch);
+/* ---- exact-solution error norms -----------------------------------------
+ * Replace TPZAnalysis::PostProcessError (Analysis/TPZAnalysis.cpp:625-650) ->
+ * TPZCompMesh::EvaluateError (Mesh/pzcmesh.cpp:1497-1551) ->
+ * TPZInterpolationSpace::EvaluateError (Mesh/pzinterpolationspace.cpp:1108-1200).
+ * The reference calls the exact-solution function set by SetExact(f, order)
+ * at every integration point; across this ABI the exact solution is data:
+ *
+ *   gpz_error_points(ctx, order, &n, NULL);   -> n, the number of points
+ *   gpz_error_points(ctx, order, &n, xyz);    -> xyz[n][3], TPZGeoEl::X of each
+ *       point of every volume element's error rule (element order, rule order)
+ *   ... the caller evaluates u[n][nstate] and du[n][3][nstate] there
+ *       (du[p][d][s] = d u_s / d x_d, the TPZFMatrix dsol layout) ...
+ *   gpz_error_evaluate(ctx, order, sol, u, du, &nerr, errors, el_errors);
+ *
+ * order is the exact solution's polynomial order (SetExactSol's pOrder): the
+ * element rule is raised to it as EvaluateError does.  sol: host solution
+ * [neq], or NULL for the last gpz_solve solution kept on the device.
+ * errors[nerr] receives the mesh norms sqrt(sum_e err_e^2) (nerr = 3:
+ * TPZMatPoisson / TPZElasticity3D [energy or H1, L2, H1 semi-norm]; 6 with a
+ * TPZDarcyFlow material, which adds the flux components), el_errors
+ * [nel][nerr] (may be NULL) the per-element errors EvaluateError stores
+ * (zero rows for boundary elements). */
+int gpz_error_points(gpz_ctx *ctx, int32_t exact_order, int64_t *npoints, double *xyz);
+int gpz_error_evaluate(gpz_ctx *ctx, int32_t exact_order, const double *sol, const double *u_exact,
+                       const double *du_exact, int32_t *nerrors, double *errors, double *el_errors);
+
 /* JSON text of the SpMV autotuner's measurements (ms per launch of every
  * candidate layout / kernel of the mixed CG) for the assembled system. */
 int gpz_tuning_report(gpz_ctx *ctx, char *buf, int64_t len);

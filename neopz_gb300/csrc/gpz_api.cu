@@ -166,6 +166,7 @@ int gpz_mesh_upload(gpz_ctx *ctx, const gpz_mesh_desc *d) {
     if (d->el_coef) c.d_coef.upload(d->el_coef, d->nel, s);
     else c.d_coef.release();
     build_buckets(c, *d);
+    c.er.reset();
     c.have_mesh = true;
     c.have_pattern = c.have_matrix = c.have_solution = c.have_a32 = c.have_bjinv = c.have_rhs = false;
     drop_assembly_graph(c);
@@ -297,6 +298,41 @@ int gpz_assemble_rhs(gpz_ctx *ctx) {
     GPZ_CUDA_TRY(cudaStreamSynchronize(c.stream));
     check_device_flag(c, "load vector assembly");
     c.have_rhs = true;
+    return GPZ_OK;
+  });
+}
+
+int gpz_error_points(gpz_ctx *ctx, int32_t exact_order, int64_t *npoints, double *xyz) {
+  return guarded(ctx, [&](Ctx &c) {
+    GPZ_REQUIRE(c.have_mesh, GPZ_E_NOT_READY, "no mesh");
+    GPZ_REQUIRE(npoints, GPZ_E_INVALID, "null npoints");
+    error_prepare(c, exact_order);
+    *npoints = c.er.npts;
+    if (xyz) {
+      error_points(c, xyz);
+      check_device_flag(c, "error points");
+    }
+    return GPZ_OK;
+  });
+}
+
+int gpz_error_evaluate(gpz_ctx *ctx, int32_t exact_order, const double *sol, const double *u_exact,
+                       const double *du_exact, int32_t *nerrors, double *errors, double *el_errors) {
+  return guarded(ctx, [&](Ctx &c) {
+    GPZ_REQUIRE(c.have_mesh, GPZ_E_NOT_READY, "no mesh");
+    GPZ_REQUIRE(errors, GPZ_E_INVALID, "null errors");
+    error_prepare(c, exact_order);
+    GPZ_REQUIRE(c.er.npts == 0 || (u_exact && du_exact), GPZ_E_INVALID, "null exact solution");
+    const double *sol_dev = c.sw.x.p;
+    if (sol) {
+      c.er.sol.upload(sol, c.neq, c.stream);
+      sol_dev = c.er.sol.p;
+    } else {
+      GPZ_REQUIRE(c.have_solution && c.sw.x.p, GPZ_E_NOT_READY, "no solution on the device");
+    }
+    error_evaluate(c, sol_dev, u_exact, du_exact, errors, el_errors);
+    check_device_flag(c, "error norms");
+    if (nerrors) *nerrors = c.er.nerr;
     return GPZ_OK;
   });
 }

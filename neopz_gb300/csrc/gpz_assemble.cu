@@ -130,6 +130,10 @@ __device__ __forceinline__ void forcing_at(const ElemArgs &P, const double *x, d
     double v = P.force[0] * (P.mdim == 2 ? 2.0 * pi * pi : 3.0 * pi * pi) * sin(pi * x[0]) * sin(pi * x[1]);
     if (P.mdim == 3) v *= sin(pi * x[2]);
     fv[0] = v;
+  } else if (P.forcing == GPZ_F_QUADRATIC) {
+    double r2 = x[0] * x[0] + x[1] * x[1];
+    if (P.mdim == 3) r2 += x[2] * x[2];
+    fv[0] = P.force[0] + P.force[1] * r2;
   }
 }
 

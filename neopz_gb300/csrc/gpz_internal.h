@@ -162,6 +162,28 @@ struct MatFree {
 };
 
 // ---------------------------------------------------------------- the context
+// ---------------------------------------------------------------- exact-solution errors
+// Error-rule tables of the volume buckets and the layout of the error points
+// (gpz_error.cu); rebuilt when the exact-solution order or the mesh changes.
+struct ErrorEval {
+  struct Tab {
+    int bucket = 0, nq = 0;
+    DBuf<double> phi, dphi, w;               // [nq][nshape], [nq][dim][nshape], [nq]
+  };
+  int exact_order = -1;                      // -1: not prepared
+  int nerr = 0;                              // norms per element (3; 6 with a Darcy material)
+  int64_t npts = 0;
+  std::vector<Tab *> tabs;
+  std::vector<int64_t> h_pt_off;             // [nel+1] first error point of each element
+  DBuf<int64_t> pt_off;
+  DBuf<double> xyz, uex, duex, sol, el;      // points, exact values [npts][nstate], gradients [npts][3][nstate]
+  ErrorEval() = default;
+  ErrorEval(const ErrorEval &) = delete;
+  ErrorEval &operator=(const ErrorEval &) = delete;
+  ~ErrorEval();
+  void reset();
+};
+
 struct Ctx {
   int device = 0;
   cudaStream_t stream = nullptr;
@@ -237,10 +259,16 @@ struct Ctx {
   bool have_solution = false;
   Learned ln;
   MatFree mf;
+  ErrorEval er;
 
   ~Ctx();
 };
 
+// error.cu
+void error_prepare(Ctx &c, int exact_order);
+void error_points(Ctx &c, double *xyz_host);
+void error_evaluate(Ctx &c, const double *sol_dev, const double *uex_host, const double *duex_host, double *errors,
+                    double *el_host);
 // pattern.cu
 void build_pattern(Ctx &c);
 void build_upper(Ctx &c);

@@ -17,7 +17,7 @@ LIBHOST = os.path.join(_HERE, "_build", "libgpzhost.so")
 GPZ_OK, GPZ_NOT_CONVERGED = 0, 1
 GPZ_EL_LINE, GPZ_EL_QUAD, GPZ_EL_HEX = 1, 2, 3
 GPZ_MAT_POISSON, GPZ_MAT_DARCY, GPZ_MAT_ELAST3D = 1, 2, 3
-GPZ_F_NONE, GPZ_F_CONST, GPZ_F_SINPROD = 0, 1, 2
+GPZ_F_NONE, GPZ_F_CONST, GPZ_F_SINPROD, GPZ_F_QUADRATIC = 0, 1, 2, 3
 GPZ_PREC_FP64, GPZ_PREC_MIXED = 0, 1
 GPZ_SOLVER_CG, GPZ_SOLVER_GMRES, GPZ_SOLVER_MIXED_CG, GPZ_SOLVER_LEARNED_FCG, GPZ_SOLVER_LEARNED_MIXED_FCG = 1, 2, 3, 4, 5
 GPZ_PRECOND_JACOBI, GPZ_PRECOND_BLOCK_JACOBI = 1, 2
@@ -116,6 +116,8 @@ def lib():
         L.gpz_assembly_report.argtypes = [vp, ctypes.c_char_p, i64]
         L.gpz_assemble_rhs.argtypes = [vp]
         L.gpz_spmv_fp32.argtypes = [vp, i32, vp, vp]
+        L.gpz_error_points.argtypes = [vp, i32, _P(i64), vp]
+        L.gpz_error_evaluate.argtypes = [vp, i32, vp, vp, vp, _P(i32), vp, vp]
         L.gpz_learned_init.argtypes = [vp, i32, ctypes.c_uint64]
         L.gpz_learned_num_params.argtypes = [vp, _P(i64)]
         L.gpz_learned_get_params.argtypes = [vp, vp, i64]
@@ -273,6 +275,7 @@ class Context:
         self._grid = grid
         self._check(lib().gpz_mesh_upload(self.h, ctypes.byref(grid.desc)))
         self.neq = grid.neq
+        self.nel = grid.nel
 
     def build_pattern(self, sym):
         nnz = ctypes.c_int64()
@@ -328,6 +331,35 @@ class Context:
         y = np.zeros(self.neq)
         self._check(lib().gpz_spmv_fp32(self.h, variant, _p(x), _p(y)))
         return y
+
+    def error_points(self, exact_order):
+        """Coordinates [npts][3] of the error-rule points of every volume element (element order)."""
+        n = ctypes.c_int64()
+        self._check(lib().gpz_error_points(self.h, int(exact_order), ctypes.byref(n), None))
+        xyz = np.zeros((n.value, 3))
+        self._check(lib().gpz_error_points(self.h, int(exact_order), ctypes.byref(n), _p(xyz)))
+        return xyz
+
+    def error_norms(self, exact_order, u_exact, du_exact, sol=None):
+        """Error norms against the exact solution values u_exact [npts][nstate] and gradients
+        du_exact [npts][3][nstate] at error_points(exact_order); sol: host solution, or None for the last
+        solve's device solution.  Returns (mesh norms [nerr], per-element errors [nel][nerr])."""
+        ue = np.ascontiguousarray(u_exact, np.float64)
+        due = np.ascontiguousarray(du_exact, np.float64)
+        x = None if sol is None else np.ascontiguousarray(sol, np.float64)
+        tot = np.zeros(6)
+        el = np.zeros(self.nel * 6)
+        ne = ctypes.c_int32()
+        self._check(lib().gpz_error_evaluate(self.h, int(exact_order), _p(x), _p(ue), _p(due), ctypes.byref(ne),
+                                             _p(tot), _p(el)))
+        k = ne.value
+        return tot[:k].copy(), el[: self.nel * k].reshape(self.nel, k).copy()
+
+    def evaluate_error(self, exact, exact_order, sol=None):
+        """TPZAnalysis::PostProcessError with a vectorised exact solution: exact(xyz [n][3]) ->
+        (u [n][nstate], du [n][3][nstate])."""
+        u, du = exact(self.error_points(exact_order))
+        return self.error_norms(exact_order, u, du, sol)
 
     def assemble_rhs(self):
         """Load vector alone (no matrix); read it with rhs()."""
@@ -406,6 +438,15 @@ class Context:
 # ---------------------------------------------------------------------------
 # Synthetic workloads (the user programs of the reference's configurations).
 # ---------------------------------------------------------------------------
+def poisson_square_quadratic(n, p):
+    """[-1, 1]^2 in n x n quads of order p, -lap u = 4 - 2x^2 - 2y^2 (pOrder 2), u = 0 penalty Dirichlet: the
+    error known-answer problem of UnitTest_PZ/TestMesh/TestError.cpp:43-160 (there on triangles), whose exact
+    solution (x^2 - 1)(y^2 - 1) lies in the order-2 space of quadrilaterals."""
+    mats = [(1, material(GPZ_MAT_POISSON, 2, forcing=GPZ_F_QUADRATIC, force=(4.0, -2.0, 0), forcing_porder=2))]
+    bcs = [(-1, bc(0, 0))]
+    return Grid(2, (n, n), (-1, -1, 0), (1, 1, 0), [1, -1, -1, -1, -1], True, p, mats, bcs)
+
+
 def poisson2d(n=64, p=2):
     """Unit square, n x n quads, H1 p, f = 2 pi^2 sin(pi x) sin(pi y) (pOrder 2), u = 0 penalty Dirichlet."""
     mats = [(1, material(GPZ_MAT_POISSON, 2, forcing=GPZ_F_SINPROD, force=(1.0, 0, 0), forcing_porder=2))]

@@ -16,7 +16,7 @@ _SRC = os.path.join(_HERE, "pz_oracle.cpp")
 _LIB = os.path.join(_HERE, "_build", "liborc.so")
 
 ORC_POISSON, ORC_DARCY, ORC_ELAST3D, ORC_MOCK = 1, 2, 3, 4
-ORC_F_NONE, ORC_F_CONST, ORC_F_SINPROD = 0, 1, 2
+ORC_F_NONE, ORC_F_CONST, ORC_F_SINPROD, ORC_F_QUADRATIC = 0, 1, 2, 3
 T_LINE, T_QUAD, T_CUBE = 1, 2, 3
 BIGNUMBER = 10.0 ** 17 * 2 / 3  # TPZMaterial::fBigNumber default for double
 
@@ -92,6 +92,10 @@ def lib():
         L.orc_cg_jacobi.argtypes = [i64, i32, vp, vp, vp, vp, vp, i64, dp, i32, P(i64), P(dp), vp]
         L.orc_cg_block_jacobi.restype = i32
         L.orc_cg_block_jacobi.argtypes = [i64, i32, vp, vp, vp, vp, vp, i32, i64, dp, P(i64), P(dp)]
+        L.orc_error_points.restype = i64
+        L.orc_error_points.argtypes = [vp, i32, vp]
+        L.orc_error_eval.restype = i32
+        L.orc_error_eval.argtypes = [vp, i32, vp, vp, vp, vp, vp]
         L.orc_gmres_jacobi.restype = i32
         L.orc_gmres_jacobi.argtypes = [i64, i32, vp, vp, vp, vp, vp, i32, i64, dp, P(i64), P(dp)]
         _lib = L
@@ -196,6 +200,24 @@ class OracleMesh:
         flat = ek.reshape(-1)[: n * n].reshape(n, n).T.copy()
         return flat, ef[:n].copy()
 
+    def error_points(self, exact_order):
+        """Coordinates [npts][3] of the error-rule points, element after element (volume elements)."""
+        n = lib().orc_error_points(self.h, int(exact_order), None)
+        xyz = np.zeros((n, 3))
+        lib().orc_error_points(self.h, int(exact_order), _p(xyz))
+        return xyz
+
+    def error_eval(self, exact_order, sol, u_exact, du_exact):
+        """Error norms of sol against the exact solution values u_exact [npts][nstate] and gradients
+        du_exact [npts][3][nstate] at error_points(): (mesh totals, per-element errors [ncel][nerr])."""
+        sol = np.ascontiguousarray(sol, np.float64)
+        ue = np.ascontiguousarray(u_exact, np.float64)
+        due = np.ascontiguousarray(du_exact, np.float64)
+        tot = np.zeros(6)
+        el = np.zeros((self.ncel, 6))
+        ne = lib().orc_error_eval(self.h, int(exact_order), _p(sol), _p(ue), _p(due), _p(tot), _p(el))
+        return tot[:ne].copy(), el.reshape(-1)[: self.ncel * ne].reshape(self.ncel, ne).copy()
+
     def pattern(self, sym):
         nnz = lib().orc_pattern(self.h, int(sym), None, None)
         ia = np.zeros(self.neq + 1, np.int64)
@@ -267,6 +289,15 @@ def shape(type, ids, orders, pt):
 # ---------------------------------------------------------------------------
 # The synthetic workloads, as the reference user programs would build them.
 # ---------------------------------------------------------------------------
+def poisson_square_quadratic(n, p):
+    """The error known-answer mesh of UnitTest_PZ/TestMesh/TestError.cpp:43-160 on quadrilaterals:
+    [-1, 1]^2 in n x n quads of order p, -lap u = 4 - 2x^2 - 2y^2 (pOrder 2), u = 0 penalty Dirichlet;
+    exact solution (x^2 - 1)(y^2 - 1) (in the order-2 space of quads)."""
+    mats = [material(1, ORC_POISSON, 2, forcing=ORC_F_QUADRATIC, force=(4.0, -2.0, 0), forcing_porder=2)]
+    bcs = [bc(-1, 1, 0)]
+    return OracleMesh(2, (n, n), (-1, -1, 0), (1, 1, 0), [1, -1, -1, -1, -1], True, p, mats, bcs)
+
+
 def poisson2d(n=64, p=2):
     """64x64 quads, H1 p, f = 2 pi^2 sin(pi x) sin(pi y) (pOrder 2), u = 0 penalty Dirichlet."""
     mats = [material(1, ORC_POISSON, 2, forcing=ORC_F_SINPROD, force=(1.0, 0, 0), forcing_porder=2)]

@@ -510,8 +510,9 @@ extern "C" {
 // TPZDarcyFlow (Material/DarcyFlow/TPZDarcyFlow.cpp:19-47),
 // TPZElasticity3D CODE3 (Material/Elasticity/TPZElasticity3D.cpp:269-400).
 enum { ORC_POISSON = 1, ORC_DARCY = 2, ORC_ELAST3D = 3, ORC_MOCK = 4 };
-// Forcing kinds: none, constant vector, 2 pi^2 sin(pi x) sin(pi y) [sin(pi z)] scaled by force[0].
-enum { ORC_F_NONE = 0, ORC_F_CONST = 1, ORC_F_SINPROD = 2 };
+// Forcing kinds: none, constant vector, 2 pi^2 sin(pi x) sin(pi y) [sin(pi z)] scaled by force[0],
+// force[0] + force[1] |x|^2 (the TestError.cpp right-hand side 4 - 2x^2 - 2y^2 with force = (4, -2)).
+enum { ORC_F_NONE = 0, ORC_F_CONST = 1, ORC_F_SINPROD = 2, ORC_F_QUADRATIC = 3 };
 
 typedef struct {
   int id;
@@ -802,6 +803,10 @@ static void forcing_value(const orc_material &mat, const double *x, double *f) {
     double v = mat.force[0] * (mat.dim == 2 ? 2 * pi * pi : 3 * pi * pi) * std::sin(pi * x[0]) * std::sin(pi * x[1]);
     if (mat.dim == 3) v *= std::sin(pi * x[2]);
     f[0] = v;
+  } else if (mat.forcing == ORC_F_QUADRATIC) {
+    double r2 = x[0] * x[0] + x[1] * x[1];
+    if (mat.dim == 3) r2 += x[2] * x[2];
+    f[0] = mat.force[0] + mat.force[1] * r2;
   }
 }
 
@@ -940,6 +945,214 @@ static int calc_stiff(const Mesh &m, const CompEl &c, double *ek, double *ef) {
     }
   }
   return n;
+}
+
+// ---------------------------------------------------------------------------
+// Exact-solution error norms: TPZCompMesh::EvaluateError (Mesh/pzcmesh.cpp:1497-1551)
+// over the elements in element order, TPZInterpolationSpace::EvaluateError
+// (Mesh/pzinterpolationspace.cpp:1108-1200) per element and the materials'
+// Errors() at each point.  The exact solution is data here: the points of every
+// element's error rule are listed first (error_points), the caller evaluates
+// its exact solution u[s] and gradient du[d][s] (direction d, state s, the
+// TPZFMatrix dsol layout) at them, and error_eval integrates.
+// ---------------------------------------------------------------------------
+// Error rule order: the element rule's order raised to the exact solution's
+// polynomial order, unless that exceeds the rule's maximum
+// (Mesh/pzinterpolationspace.cpp:1140-1156).  GetMaxOrder is 36 for
+// TPZIntQuad and 20 for TPZIntCube3D (Integral/pzquad.h:217,299);
+// TPZIntQuad::GetOrder returns the requested order, TPZIntCube3D::GetOrder
+// the rule's own, 2 (npoints - 1) (Integral/pzquad.cpp:176-194,289-305,
+// Integral/tpzgaussrule.cpp:170-181).
+static int error_order(int t, int intorder, int exact_order) {
+  int maxo = t == T_CUBE ? 20 : 36;
+  int prev = t == T_CUBE ? 2 * (gauss_npoints(intorder) - 1) : intorder;
+  if (maxo > exact_order) return prev > exact_order ? prev : exact_order;
+  return maxo;
+}
+
+static int element_intorder(const Mesh &m, const CompEl &c) {
+  int porder = max_order(m, c);
+  const orc_material &vm = m.spec.mats[c.mat];
+  if (vm.kind == ORC_ELAST3D) return 2 * porder;
+  if (porder < vm.forcing_porder) return vm.forcing_porder + porder;
+  return 2 * porder;
+}
+
+static int nerrors_of(int kind) { return kind == ORC_DARCY ? 6 : 3; }
+
+// Errors() at one point: TPZMatPoisson (Material/Poisson/TPZMatPoisson.cpp:173-218),
+// TPZDarcyFlow (Material/DarcyFlow/TPZDarcyFlow.cpp:268-327), TPZElasticity3D
+// (Material/Elasticity/TPZElasticity3D.cpp:1081-1133 with ComputeStressVector,
+// :1178-1192, and ComputeStressTensor, :1152-1166; no prestress).  gradu and due
+// are [3][ns] in xyz; coef is the element's permeability or Young modulus.
+static void material_errors(const orc_material &mat, double coef, int ns, const double *u, const double *gradu,
+                            const double *ue, const double *due, double *v) {
+  for (int k = 0; k < 6; k++) v[k] = 0.0;
+  if (mat.kind == ORC_POISSON) {
+    double diff = u[0] - ue[0];
+    v[1] = diff * diff;
+    v[2] = 0.0;
+    for (int id = 0; id < mat.dim; id++) {
+      diff = gradu[id] - due[id];
+      v[2] += diff * diff;
+    }
+    v[0] = v[1] + v[2];
+  } else if (mat.kind == ORC_DARCY) {
+    double diff = std::fabs(u[0] - ue[0]);
+    v[1] = diff * diff;
+    double gd[3] = {0.0, 0.0, 0.0};
+    for (int id = 0; id < mat.dim; id++) gd[id] += std::fabs(gradu[id] - due[id]);
+    diff = 0.0;
+    for (int id = 0; id < mat.dim; id++) diff += coef * gd[id];
+    v[2] += std::fabs(diff * diff);
+    v[0] = v[1] + v[2];
+    for (int id = 0; id < mat.dim; id++) {
+      double flux = -coef * gradu[id];
+      diff = std::fabs(due[id] - flux);
+      v[3 + id] = diff * diff;
+    }
+  } else if (mat.kind == ORC_ELAST3D) {
+    double L2 = 0.0;
+    for (int i = 0; i < 3; i++) L2 += (u[i] - ue[i]) * (u[i] - ue[i]);
+    double semi = 0.0, D[3][3];
+    for (int i = 0; i < 3; i++)
+      for (int j = 0; j < 3; j++) {
+        D[i][j] = gradu[i * ns + j] - due[i * ns + j];
+        semi += D[i][j] * D[i][j];
+      }
+    const double E = coef, ni = mat.nu;
+    const double const1 = -1. + ni, const2 = -1. + ni + 2. * ni * ni, const3 = 2. * (1. + ni);
+    double sv[6];
+    sv[0] = E * (D[0][0] * const1 - (D[1][1] + D[2][2]) * ni) / const2;
+    sv[1] = E * (D[1][1] * const1 - (D[0][0] + D[2][2]) * ni) / const2;
+    sv[2] = E * (D[2][2] * const1 - (D[0][0] + D[1][1]) * ni) / const2;
+    sv[3] = E * (D[1][0] + D[0][1]) / const3;
+    sv[4] = E * (D[2][0] + D[0][2]) / const3;
+    sv[5] = E * (D[2][1] + D[1][2]) / const3;
+    const double S[3][3] = {{sv[0], sv[3], sv[4]}, {sv[3], sv[1], sv[5]}, {sv[4], sv[5], sv[2]}};
+    double energy = 0.0;
+    for (int i = 0; i < 3; i++)
+      for (int j = 0; j < 3; j++) energy += D[i][j] * S[i][j];
+    v[1] = L2;
+    v[2] = semi;
+    v[0] = energy;
+  }
+}
+
+static bool has_error(const Mesh &m, const CompEl &c) { return !c.is_bc && tdim(c.type) == m.spec.dim; }
+
+// Physical coordinates (TPZGeoEl::X) of every error-rule point, element after element.
+static int64_t error_points(const Mesh &m, int exact_order, double *xyz) {
+  int64_t np = 0;
+  for (const CompEl &c : m.cels) {
+    if (!has_error(m, c)) continue;
+    const GeoEl &g = m.gels[c.gel];
+    double coords[8 * 3];
+    for (int k = 0; k < ncorner(c.type); k++)
+      for (int j = 0; j < 3; j++) coords[k * 3 + j] = m.nodes[g.nodes[k] * 3 + j];
+    IntRule rule = make_rule(c.type, error_order(c.type, element_intorder(m, c), exact_order));
+    for (size_t ip = 0; ip < rule.wts.size(); ip++, np++) {
+      if (!xyz) continue;
+      Jac J = jacobian(c.type, coords, &rule.pts[ip * rule.dim]);
+      for (int j = 0; j < 3; j++) xyz[np * 3 + j] = J.x[j];
+    }
+  }
+  return np;
+}
+
+// Per-element errors (sqrt of the integrated values, as EvaluateError leaves
+// them; zero rows for boundary elements) and the mesh totals sqrt(sum_e err_e^2).
+static int error_eval(const Mesh &m, int exact_order, const double *sol, const double *uex, const double *duex,
+                      double *errors, double *el) {
+  const int ns = m.nstate;
+  int nerr = 0;
+  for (int i = 0; i < m.spec.nmat; i++) nerr = std::max(nerr, nerrors_of(m.spec.mats[i].kind));
+  std::vector<double> tot(nerr, 0.0);
+  int64_t np = 0;
+  for (size_t ic = 0; ic < m.cels.size(); ic++) {
+    const CompEl &c = m.cels[ic];
+    double ee[6] = {0, 0, 0, 0, 0, 0};
+    if (has_error(m, c)) {
+      const GeoEl &g = m.gels[c.gel];
+      const orc_material &vm = m.spec.mats[c.mat];
+      int t = c.type, NC = ncorner(t), D = tdim(t);
+      int orders[26];
+      side_orders_of(m, c, orders);
+      int nshape = NC;
+      for (int s = NC; s < nsides(t); s++) nshape += nconnect_shape(t, s, orders[s - NC]);
+      std::vector<int64_t> dest(nshape * ns);
+      element_dest(m, c, dest.data());
+      double coords[8 * 3];
+      for (int k = 0; k < NC; k++)
+        for (int j = 0; j < 3; j++) coords[k * 3 + j] = m.nodes[g.nodes[k] * 3 + j];
+      double coef = vm.kind == ORC_ELAST3D ? vm.E : vm.coef_const;
+      if (!m.coef.empty() && c.gel < m.nvol) coef = m.coef[c.gel];
+      IntRule rule = make_rule(t, error_order(t, element_intorder(m, c), exact_order));
+      std::vector<double> phi(nshape), dphi(3 * nshape), dx(3 * nshape);
+      for (size_t ip = 0; ip < rule.wts.size(); ip++, np++) {
+        const double *pt = &rule.pts[ip * rule.dim];
+        double weight = rule.wts[ip];
+        Jac J = jacobian(t, coords, pt);
+        shape_h1(t, g.nodes, orders, pt, phi.data(), dphi.data(), nshape);
+        for (int i = 0; i < D; i++)
+          for (int k = 0; k < nshape; k++) {
+            double acc = 0.0;
+            for (int j = 0; j < D; j++) acc += J.jinv[j][i] * dphi[j * nshape + k];
+            dx[i * nshape + k] = acc;
+          }
+        // TPZInterpolationSpace::ReallyComputeSolutionT (Mesh/pzinterpolationspace.cpp:135-178)
+        double u[3] = {0, 0, 0}, dsol[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
+        for (int iv = 0; iv < nshape * ns; iv++) {
+          const double xv = sol[dest[iv]];
+          u[iv % ns] += phi[iv / ns] * xv;
+          for (int d = 0; d < D; d++) dsol[d][iv % ns] += dx[d * nshape + iv / ns] * xv;
+        }
+        // TPZAxesTools::Axes2XYZ (Util/pzaxestools.h:61-86) with the axes of
+        // TPZGeoEl::Jacobian (Mesh/pzgeoel.cpp:1228-1292; the identity in 3D)
+        double axes[3][3] = {{1, 0, 0}, {0, 1, 0}, {0, 0, 1}};
+        if (D == 2) {
+          double cp[27], cd[3 * 27], v1[3] = {0, 0, 0}, v2[3] = {0, 0, 0};
+          corner_shapes(t, pt, cp, cd);
+          for (int k = 0; k < NC; k++)
+            for (int i = 0; i < 3; i++) {
+              v1[i] += coords[k * 3 + i] * cd[0 * 27 + k];
+              v2[i] += coords[k * 3 + i] * cd[1 * 27 + k];
+            }
+          double n1 = 0.0, d12 = 0.0, n2 = 0.0, v1t[3], v2t[3];
+          for (int i = 0; i < 3; i++) { n1 += v1[i] * v1[i]; d12 += v1[i] * v2[i]; }
+          n1 = std::sqrt(n1);
+          for (int i = 0; i < 3; i++) {
+            v1t[i] = v1[i] / n1;
+            v2t[i] = v2[i] - d12 * v1t[i] / n1;
+            n2 += v2t[i] * v2t[i];
+          }
+          n2 = std::sqrt(n2);
+          for (int i = 0; i < 3; i++) {
+            axes[0][i] = v1t[i];
+            axes[1][i] = v2t[i] / n2;
+          }
+        }
+        double gradu[3 * 3] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+        for (int i = 0; i < 3; i++)
+          for (int s2 = 0; s2 < ns; s2++) {
+            double acc = 0.0;
+            for (int d = 0; d < D; d++) acc += axes[d][i] * dsol[d][s2];
+            gradu[i * ns + s2] = acc;
+          }
+        double v[6];
+        material_errors(vm, coef, ns, u, gradu, &uex[np * ns], &duex[np * 3 * ns], v);
+        weight *= std::fabs(J.detjac);
+        for (int k = 0; k < nerr; k++) ee[k] += weight * v[k];
+      }
+      for (int k = 0; k < nerr; k++) ee[k] = std::sqrt(ee[k]);
+    }
+    for (int k = 0; k < nerr; k++) {
+      if (el) el[ic * nerr + k] = ee[k];
+      tot[k] += ee[k] * ee[k];
+    }
+  }
+  for (int k = 0; k < nerr; k++) errors[k] = std::sqrt(tot[k]);
+  return nerr;
 }
 
 // ---------------------------------------------------------------------------
@@ -1102,6 +1315,17 @@ void orc_set_nodes(void *h, const double *xyz) {
 int orc_calc_stiff(void *h, int64_t ic, double *ek, double *ef) {
   Mesh *m = (Mesh *)h;
   return calc_stiff(*m, m->cels[ic], ek, ef);
+}
+
+// Error norms against an exact solution given at the error-rule points
+// (TPZAnalysis::PostProcessError, Analysis/TPZAnalysis.cpp:625-650):
+// orc_error_points returns the number of points and, with xyz, their
+// coordinates; orc_error_eval returns the number of norms.
+int64_t orc_error_points(void *h, int exact_order, double *xyz) { return error_points(*(Mesh *)h, exact_order, xyz); }
+
+int orc_error_eval(void *h, int exact_order, const double *sol, const double *uex, const double *duex, double *errors,
+                   double *el) {
+  return error_eval(*(Mesh *)h, exact_order, sol, uex, duex, errors, el);
 }
 
 // H1 shape functions of one element type at one point (for the shape-table tests).

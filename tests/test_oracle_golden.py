@@ -220,3 +220,69 @@ def test_learned_oracle_gradient_matches_finite_differences():
         e[i] = h
         fd = (LO.loss_only(mesh, A, p + e, R, Rs, Es) - LO.loss_only(mesh, A, p - e, R, Rs, Es)) / (2 * h)
         assert abs(fd - g[i]) <= 1e-6 * max(1.0, np.abs(g).max()), (i, fd, g[i])
+
+
+def _dense(ia, ja, a, n):
+    A = np.zeros((n, n))
+    for r in range(n):
+        A[r, ja[ia[r]:ia[r + 1]]] = a[ia[r]:ia[r + 1]]
+    return A
+
+
+def _quadratic_exact(xyz):
+    """(x^2 - 1)(y^2 - 1) and its gradient, the exact solution of UnitTest_PZ/TestMesh/TestError.cpp:50-59."""
+    x, y = xyz[:, 0], xyz[:, 1]
+    u = ((x * x - 1) * (y * y - 1))[:, None]
+    du = np.zeros((len(x), 3, 1))
+    du[:, 0, 0] = 2 * x * (y * y - 1)
+    du[:, 1, 0] = 2 * y * (x * x - 1)
+    return u, du
+
+
+def test_error_known_answer_poisson():
+    """The error test of UnitTest_PZ/TestMesh/TestError.cpp:20-41 (TPZAnalysis::PostProcessError after a direct
+    solve, exact order 4), on quadrilaterals: the exact solution is in the order-2 space of quads, so the three
+    norms (H1, L2, H1 semi-norm) drop from O(1) at p = 1 to the reference's bound of 10 machine epsilons for
+    p = 2, 3, 4 (the triangles of the reference reach it at p = 4)."""
+    eps = np.finfo(float).eps
+    prev = None
+    for p in range(1, 5):
+        om = O.poisson_square_quadratic(2, p)
+        ia, ja = om.pattern(False)
+        a, f = om.assemble(False, ia, ja)
+        x = np.linalg.solve(_dense(ia, ja, a, om.neq), f)
+        u, du = _quadratic_exact(om.error_points(4))
+        tot, el = om.error_eval(4, x, u, du)
+        assert tot.shape == (3,) and el.shape == (om.ncel, 3)
+        assert np.allclose(np.sqrt((el ** 2).sum(0)), tot, rtol=1e-14)
+        if p == 1:
+            assert np.all(tot > 0.1)
+        else:
+            # at the rounding floor the norms are no longer ordered in p
+            assert np.all(tot <= 10 * eps), (p, tot)
+            assert np.all(tot <= prev) or p > 2
+        prev = tot
+
+
+def test_error_norms_of_known_fields():
+    """Norms of an exact field against the zero solution, integrated by the error rule: the L2 and H1
+    semi-norms of (x^2 - 1)(y^2 - 1) on [-1, 1]^2 are 16/15 and sqrt(256/45); the uniform strain u = (x, 0, 0)
+    on the unit cube gives L2^2 = 1/3, semi-norm 1 and energy E (1 - nu) / ((1 + nu)(1 - 2 nu))."""
+    om = O.poisson_square_quadratic(3, 2)
+    u, du = _quadratic_exact(om.error_points(4))
+    tot, _ = om.error_eval(4, np.zeros(om.neq), u, du)
+    assert abs(tot[1] - 16 / 15) <= 1e-13
+    assert abs(tot[2] - np.sqrt(256 / 45)) <= 1e-13
+    assert abs(tot[0] ** 2 - (tot[1] ** 2 + tot[2] ** 2)) <= 1e-13
+    nu = 0.3
+    om = O.elasticity3d(2, 2, nu=nu)
+    xyz = om.error_points(2)
+    u = np.zeros((len(xyz), 3))
+    u[:, 0] = xyz[:, 0]
+    du = np.zeros((len(xyz), 3, 3))
+    du[:, 0, 0] = 1.0
+    tot, el = om.error_eval(2, np.zeros(om.neq), u, du)
+    assert abs(tot[1] ** 2 - 1 / 3) <= 1e-13
+    assert abs(tot[2] - 1.0) <= 1e-13
+    assert abs(tot[0] ** 2 - (1 - nu) / ((1 + nu) * (1 - 2 * nu))) <= 1e-13
+    assert np.all(el[8:] == 0.0)  # boundary elements carry no error
