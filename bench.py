@@ -1,13 +1,17 @@
 """Benchmark: time to ||r||/||b|| < 1e-8 on 3D Q2 linear elasticity (64^3 hexes) on one GB300.
 
 One step = the hot path over the synthetic system: global assembly into the
-CSR (FP64 parity assembly + FP32 copy for the inner solves) and the iterative
-solve to a TRUE FP64 residual below 1e-8.  `value` is device time with the
-mesh and pattern resident in HBM (CUDA events on the library's stream);
-`e2e` is the same pipeline through the public C ABI from host buffers
-(mesh upload, pattern build, assembly, solve, solution download).  The plain
-FP64 Jacobi-PCG of the reference (same algorithm, on the GPU) is timed once
-beside it as the path's own baseline.
+CSR (FP64 parity assembly + the FP32 operator of the inner solves) and the
+iterative solve to a TRUE FP64 residual below 1e-8 with the learned + mixed
+flexible PCG (the committed elasticity weights, FP32 operator and recurrence,
+FP64 true-residual replacement).  `value` is device time with the mesh and
+pattern resident in HBM (CUDA events on the library's stream); `e2e` is the
+same pipeline through the public C ABI from host buffers (mesh upload, pattern
+build, assembly, weights, solve, solution download).  The plain FP64
+Jacobi-PCG of the reference (same algorithm, on the GPU) is timed once beside
+it as the path's own baseline, and the mixed block-Jacobi CG without the
+learned correction (`--path mixed` times it as the step) once as the other
+comparison.
 
 Usage: python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference] [--n 64]
 """
@@ -26,6 +30,8 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 METRIC = "s to ||r||/||b||<1e-8: learned+mixed PCG vs FP64 Jacobi-PCG (GB300); elem/s"
+LEARNED_WEIGHTS = os.path.join(ROOT, "neopz_gb300", "data", "learned_elasticity3d_q2.npy")
+LEARNED_RANK = 8
 TOL = 1e-8
 SEED = 5
 # HBM bytes per stored block measured by ncu for the SpMV kernels (32^3 case):
@@ -46,6 +52,8 @@ def parse():
     ap.add_argument("--no-learned", action="store_true", help="skip the learned-preconditioner (2D Darcy) leg")
     ap.add_argument("--no-hp", action="store_true", help="skip the hp (uneven-order) assembly leg")
     ap.add_argument("--hp-n", type=int, default=40, help="hexes per direction of the hp leg")
+    ap.add_argument("--path", default="learned", choices=["learned", "mixed"],
+                    help="solver of the timed step: learned + mixed flexible PCG, or mixed block-Jacobi CG")
     return ap.parse_args()
 
 
@@ -147,12 +155,31 @@ def run_gpu(args):
     nel = grid.nel
     nvol = grid.nvol
 
-    def step(mixed=True):
+    weights = np.load(LEARNED_WEIGHTS)
+    ctx.assemble(gpz.GPZ_PREC_FP64)
+    ctx.learned_init(rank=LEARNED_RANK, seed=0)
+    ctx.set_learned_params(weights)
+
+    def step(mixed=True, learned=None):
+        learned = args.path == "learned" if learned is None else learned
         ctx.assemble(gpz.GPZ_PREC_MIXED if mixed else gpz.GPZ_PREC_FP64)
+        if mixed and learned:
+            return ctx.solve(solver=gpz.GPZ_SOLVER_LEARNED_MIXED_FCG, tol=TOL, max_iter=200000, reliable_delta=1e-2,
+                             check_every=64, want_x=False)
         if mixed:
             return ctx.solve(solver=gpz.GPZ_SOLVER_MIXED_CG, precond=gpz.GPZ_PRECOND_BLOCK_JACOBI, tol=TOL,
                              max_iter=200000, reliable_delta=1e-2, check_every=64, want_x=False)
         return ctx.solve(solver=gpz.GPZ_SOLVER_CG, tol=TOL, max_iter=200000, check_every=64, want_x=False)
+
+    def timed(fn):
+        torch.cuda.synchronize()
+        with torch.cuda.stream(stream):
+            e0.record(stream)
+        r = fn()
+        with torch.cuda.stream(stream):
+            e1.record(stream)
+        torch.cuda.synchronize()
+        return r, e0.elapsed_time(e1) / 1e3
 
     # the reference's plain FP64 Jacobi-PCG on the GPU (the 3x target's denominator)
     e0 = torch.cuda.Event(enable_timing=True)
@@ -192,6 +219,9 @@ def run_gpu(args):
         torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
         t_step = float(t.item())
     last = reps[-1]
+    # the other mixed path, once: block-Jacobi CG without the learned correction (or the learned one
+    # when the step is the block-Jacobi CG)
+    other, t_other = timed(lambda: step(learned=args.path != "learned"))
 
     # roofline of the dominant kernel: the FP32 3x3-block SpMV of the inner CG, in the
     # layout the library's autotuner chose (HBM bytes that layout must stream per launch)
@@ -262,8 +292,14 @@ def run_gpu(args):
         c2.upload_mesh(grid)
         c2.build_pattern(True)
         c2.assemble(gpz.GPZ_PREC_MIXED)
-        r2 = c2.solve(solver=gpz.GPZ_SOLVER_MIXED_CG, precond=gpz.GPZ_PRECOND_BLOCK_JACOBI, tol=TOL,
-                      max_iter=200000, reliable_delta=1e-2, check_every=64, want_x=True)
+        if args.path == "learned":
+            c2.learned_init(rank=LEARNED_RANK, seed=0)
+            c2.set_learned_params(weights)
+            r2 = c2.solve(solver=gpz.GPZ_SOLVER_LEARNED_MIXED_FCG, tol=TOL, max_iter=200000, reliable_delta=1e-2,
+                          check_every=64, want_x=True)
+        else:
+            r2 = c2.solve(solver=gpz.GPZ_SOLVER_MIXED_CG, precond=gpz.GPZ_PRECOND_BLOCK_JACOBI, tol=TOL,
+                          max_iter=200000, reliable_delta=1e-2, check_every=64, want_x=True)
         torch.cuda.synchronize()
         e2e_times.append(time.perf_counter() - t0)
         assert r2["true_resid"] <= TOL
@@ -277,17 +313,26 @@ def run_gpu(args):
         "config": {"workload": f"3D linear elasticity {n}^3 hex Q2 (TPZElasticity3D), E lognormal(sigma=1) seed {SEED}, "
                                "nu=0.3, clamped z=0 (penalty), traction (0,0,-1) on z=1",
                    "neq": neq, "nnz_full": nnz, "nnz_upper": nnz_upper, "elements": nel, "volume_elements": nvol,
-                   "path": f"FP64 assembly; CG with the FP32 inner operator chosen by the autotuner ({chosen}), FP64 x/r/dots, "
-                           "reliable FP64 true-residual updates; connect-block (3x3) Jacobi", "l2": "inputs larger than L2 (matrix > 129 MB)",
+                   "path": (f"FP64 assembly; learned + mixed flexible PCG: learned element-to-node correction (rank "
+                            f"{LEARNED_RANK}, weights {os.path.relpath(LEARNED_WEIGHTS, ROOT)}, trained on the GPU) "
+                            f"on Jacobi, FP32 operator chosen by the autotuner ({chosen}), FP32 recurrence, FP64 "
+                            "x/dots/alpha/beta, reliable FP64 true-residual updates" if args.path == "learned" else
+                            f"FP64 assembly; CG with the FP32 inner operator chosen by the autotuner ({chosen}), "
+                            "FP64 x/dots, reliable FP64 true-residual updates; connect-block (3x3) Jacobi"),
+                   "l2": "inputs larger than L2 (matrix > 129 MB)",
                    "parallelism": f"replicas x{world}"},
         "solve": {"iterations": last["iterations"], "true_resid": last["true_resid"],
                   "reliable_updates": last["reliable_updates"], "spmv_fp32": last["spmv_fp32"],
                   "spmv_fp64": last["spmv_fp64"], "restarts": last["restarts"], "solve_s": last["seconds"]},
         "fp64_jacobi_pcg": {"seconds": t_fp64, "iterations": fp64["iterations"], "true_resid": fp64["true_resid"],
                             "speedup_of_value": (t_fp64 / t_step) if t_fp64 else None},
+        ("mixed_block_jacobi_cg" if args.path == "learned" else "learned_mixed_fcg"): {
+            "seconds": round(t_other, 6), "iterations": other["iterations"], "true_resid": other["true_resid"],
+            "solve_s": other["seconds"], "speedup_vs_fp64_jacobi_pcg": (t_fp64 / t_other) if t_fp64 else None,
+            "note": "one step (assembly + solve), timed once after the timed steps"},
         "assembly": {"fp64_seconds": t_asm, "elements_per_s": nel / t_asm, "volume_elements_per_s": nvol / t_asm,
                      "pattern_build_s": t_pattern, "host_mesh_build_s": t_mesh},
-        "e2e": {"value": round(t_e2e, 6) if t_e2e else None, "unit": "s", "h2d_bytes_per_step": int(b_in + neq * 0),
+        "e2e": {"value": round(t_e2e, 6) if t_e2e else None, "unit": "s", "h2d_bytes_per_step": int(b_in + (weights.nbytes if args.path == "learned" else 0)),
                 "d2h_bytes_per_step": int(neq * 8)},
         "roofline": {"bound": "hbm", "kernel": kern, "achieved": round(ach, 1),
                      "peak": hbm, "unit": "GB/s", "frac": round(ach / hbm, 4), "traffic": traffic,

@@ -106,6 +106,7 @@ struct Bucket {
 struct SolverWork {
   DBuf<double> r, z, p, q, x, b, t;
   DBuf<float> pm, r32, q32, dx32;  // mixed CG inner vectors (pm padded x4 for the block SpMV)
+  DBuf<float> z32;                 // learned flexible CG over the FP32 operator: z = M r
   DBuf<double> partial;        // per-CTA partial sums
   DBuf<double> scal;           // device scalars (see gpz_solver.cu)
   DBuf<unsigned int> counter;  // last-block counters

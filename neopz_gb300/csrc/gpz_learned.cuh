@@ -51,6 +51,40 @@ __device__ __forceinline__ void ln_elem_t(const LnView &L, const T *__restrict__
   L.t[idx] = acc;
 }
 
+constexpr int kLnMaxR = 8;  // largest rank R of the factors
+
+// t_e = F_e^T Q_e (m .* S r) with one warp per element: lanes over the element's
+// equations (coalesced rows of F, float4 loads for R = 8), then a warp sum per
+// column; lane k writes t_e[k].
+template <class T>
+__device__ __forceinline__ void ln_elem_t_warp(const LnView &L, const T *__restrict__ r, int64_t e, int lane) {
+  float acc[kLnMaxR];
+#pragma unroll
+  for (int k = 0; k < kLnMaxR; k++) acc[k] = 0.f;
+  const int32_t *d = L.dest + e * L.NS;
+  for (int loc = lane; loc < L.NS; loc += 32) {
+    const int32_t q = d[loc];
+    const float v = L.mdsq[q] * (float)r[q];
+    const float *f = L.F + ((size_t)e * L.NS + loc) * L.R;
+    if (L.R == 8) {
+      const float4 a = *(const float4 *)f, b = *(const float4 *)(f + 4);
+      acc[0] += a.x * v; acc[1] += a.y * v; acc[2] += a.z * v; acc[3] += a.w * v;
+      acc[4] += b.x * v; acc[5] += b.y * v; acc[6] += b.z * v; acc[7] += b.w * v;
+    } else {
+#pragma unroll
+      for (int k = 0; k < kLnMaxR; k++)
+        if (k < L.R) acc[k] += f[k] * v;
+    }
+  }
+#pragma unroll
+  for (int k = 0; k < kLnMaxR; k++) {
+    if (k >= L.R) break;
+    float s = acc[k];
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+    if (lane == k) L.t[e * L.R + k] = s;
+  }
+}
+
 // correction at equation i: m_i S_i sum_{(e,loc) at i} F_e[loc] . t_e
 __device__ __forceinline__ float ln_node_corr(const LnView &L, int64_t i) {
   float c = 0.f;
@@ -59,7 +93,14 @@ __device__ __forceinline__ float ln_node_corr(const LnView &L, int64_t i) {
     const int32_t e = el / L.NS;
     const float *f = L.F + (size_t)el * L.R;
     const float *t = L.t + (size_t)e * L.R;
-    for (int j = 0; j < L.R; j++) c += f[j] * t[j];
+    if (L.R == 8) {
+      const float4 f0 = *(const float4 *)f, f1 = *(const float4 *)(f + 4);
+      const float4 t0 = *(const float4 *)t, t1 = *(const float4 *)(t + 4);
+      c += f0.x * t0.x + f0.y * t0.y + f0.z * t0.z + f0.w * t0.w + f1.x * t1.x + f1.y * t1.y + f1.z * t1.z +
+           f1.w * t1.w;
+    } else {
+      for (int j = 0; j < L.R; j++) c += f[j] * t[j];
+    }
   }
   return L.mdsq[i] * c;
 }

@@ -1371,9 +1371,105 @@ __global__ void __launch_bounds__(kThreads) k_fcg_t(LnView L, const double *__re
                                                     const float *__restrict__ r32, Red R) {
   if (!active(R.iscal)) return;
   const bool fresh = R.iscal[I_UPDATE] == 2;
-  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < L.E * L.R; i += (int64_t)gridDim.x * blockDim.x) {
-    if (fresh) ln_elem_t<double>(L, r64, i);
-    else ln_elem_t<float>(L, r32, i);
+  const int lane = threadIdx.x & 31;
+  const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  for (int64_t e = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; e < L.E; e += nw) {
+    if (fresh) ln_elem_t_warp<double>(L, r64, e, lane);
+    else ln_elem_t_warp<float>(L, r32, e, lane);
+  }
+}
+
+// ---- learned flexible CG over the mixed CG's FP32 operator (3 states: 3x3
+// blocks or matrix-free elements).  As in the mixed CG, r, p, z and the
+// solution increment dx are FP32 (x += dx and r = b - A64 x at reliable
+// updates, k_mx_foldx / k_reliable); dots, alpha and beta are FP64.  p32 is in
+// the operator's padded input layout, q32 in its output layout (qpad), and
+// k_lfb_p clears q32 for the next accumulating launch (qzero).
+__global__ void __launch_bounds__(kThreads) k_lfb_update(float *__restrict__ dx, float *__restrict__ r32,
+                                                         const float *__restrict__ p32, const float *__restrict__ q32,
+                                                         int qpad, int64_t n, Red R) {
+  if (!active(R.iscal)) return;
+  const float alpha = (float)R.scal[S_ALPHA];
+  double rr = 0.0;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    dx[i] = fmaf(alpha, p32[pidx(i, 1)], dx[i]);
+    const float ri = fmaf(-alpha, q32[pidx(i, qpad)], r32[i]);
+    r32[i] = ri;
+    rr += (double)ri * ri;
+  }
+  double v[1] = {rr}, tot[1];
+  if (grid_reduce<1>(v, R, tot) && threadIdx.x == 0) {
+    double *s = R.scal;
+    int64_t *is = R.iscal;
+    const double resid = sqrt(tot[0]) / s[S_NORMB];
+    s[S_RR] = tot[0];
+    s[S_RESID] = resid;
+    is[I_IT] += 1;
+    if (tot[0] > s[S_MAXRR]) s[S_MAXRR] = tot[0];
+    if (!(s[S_PQ] > 0.0) || !isfinite(resid)) {
+      is[I_BREAK] = 1;
+      is[I_CONV] = 2;
+    } else if (resid <= s[S_TOL] || tot[0] < s[S_DELTA2] * s[S_MAXRR]) {
+      is[I_UPDATE] = 1;  // replace r by b - A64 x (k_mx_foldx, k_reliable)
+    }
+  }
+}
+
+// z = M r (FP32 out), the dots of the flexible recurrence and of the Jacobi
+// fallback; after a replacement (I_UPDATE == 2) r is the fresh FP64 residual
+// and r32 is refreshed from it
+__global__ void __launch_bounds__(kThreads) k_lfb_z(LnView L, const double *__restrict__ r64, float *__restrict__ r32,
+                                                    const float *__restrict__ q32, int qpad,
+                                                    const double *__restrict__ dinv, float *__restrict__ z32, Red R) {
+  if (!active(R.iscal)) return;
+  const bool first = R.iscal[I_IT] == 0;
+  const bool fresh = R.iscal[I_UPDATE] == 2;
+  const double alpha = exp((double)*L.loga);
+  double zr = 0.0, zq = 0.0, jr = 0.0, jq = 0.0;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < L.n; i += (int64_t)gridDim.x * blockDim.x) {
+    double ri;
+    if (fresh) {
+      ri = r64[i];
+      r32[i] = (float)ri;
+    } else {
+      ri = (double)r32[i];
+    }
+    const double zi = (double)(float)(alpha * dinv[i] * ri + (double)ln_node_corr(L, i));
+    const double ji = dinv[i] * ri;
+    z32[i] = (float)zi;
+    zr += zi * ri;
+    jr += ji * ri;
+    if (!first) {
+      const double qi = (double)q32[pidx(i, qpad)];
+      zq += zi * qi;
+      jq += ji * qi;
+    }
+  }
+  double v[4] = {zr, zq, jr, jq}, tot[4];
+  if (grid_reduce<4>(v, R, tot) && threadIdx.x == 0) {
+    double *s = R.scal;
+    int64_t *is = R.iscal;
+    const bool ok = tot[0] > 0.0 && isfinite(tot[0]) && isfinite(tot[1]);
+    is[I_RESTART] = ok ? 0 : 1;
+    if (!ok) is[I_NRESTART] += 1;
+    s[S_RHO] = ok ? tot[0] : tot[2];
+    s[S_BETA] = first ? 0.0 : -(ok ? tot[1] : tot[3]) / s[S_PQ];
+    if (is[I_UPDATE] == 2) is[I_UPDATE] = 0;
+  }
+}
+
+__global__ void __launch_bounds__(kThreads) k_lfb_p(const float *__restrict__ z32, const float *__restrict__ r32,
+                                                    const double *__restrict__ dinv, float *__restrict__ p32,
+                                                    float *__restrict__ q32, int qpad, int qzero, int64_t n, Red R) {
+  if (!active(R.iscal)) return;
+  const bool jac = R.iscal[I_RESTART] != 0;
+  const bool first = R.iscal[I_IT] == 0;
+  const float beta = (float)R.scal[S_BETA];
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    const float zi = jac ? (float)(dinv[i] * (double)r32[i]) : z32[i];
+    const int64_t k = pidx(i, 1);
+    p32[k] = first ? zi : fmaf(beta, p32[k], zi);
+    if (qzero) q32[pidx(i, qpad)] = 0.f;
   }
 }
 
@@ -1934,19 +2030,27 @@ int solve_gmres(Ctx &c, const gpz_solver_opts &o, gpz_solve_report &rep) {
 // only on that true residual.
 int solve_learned(Ctx &c, const gpz_solver_opts &o, gpz_solve_report &rep, bool mixed) {
   learned_prepare(c);
-  if (mixed) {
-    if (!c.have_a32) make_fp32_copy(c);
-    GPZ_REQUIRE(!c.have_bsr3, GPZ_E_INVALID,
-                "mixed learned flexible CG needs the FP32 CSR copy (scalar problems, nstate 1)");
-  }
+  if (mixed && (!c.have_a32 || (o.spmv_variant >= 0 && c.have_bsr3 && o.spmv_variant != c.spmv32_variant)))
+    make_fp32_copy(c, o.spmv_variant);
+  // scalar problems: FP32 CSR (k_lfcg_spmv); 3 states: the mixed CG's FP32
+  // operator in the layout the autotuner chose (3x3 blocks or matrix-free)
+  const bool blk = mixed && c.have_bsr3;
+  const int v32 = c.spmv32_variant;
+  const int qpad = blk && v32 >= 4 ? 1 : 0;  // padded, accumulated with atomics
   alloc_work(c, mixed);
   SolverWork &w = c.sw;
   w.z.alloc(std::max<int64_t>(c.neq, 1));
   w.r32.alloc(std::max<int64_t>(c.neq, 1));
-  w.pm.alloc(std::max<int64_t>(c.neq, 1));
+  if (!blk) w.pm.alloc(std::max<int64_t>(c.neq, 1));
   const int tpr32 = pick_tpr32(c.nnz, c.neq);
   float *p32 = mixed ? w.pm.p : nullptr;
   cudaStream_t s = c.stream;
+  if (blk) {
+    w.z32.alloc(std::max<int64_t>(c.neq, 1));
+    w.pm.zero(s);
+    w.q32.zero(s);
+    w.dx32.zero(s);
+  }
   const int tpr = pick_tpr(c.nnz, c.neq);
   const LnView L = learned_view(c);
   Red R = red_of(c);
@@ -1955,14 +2059,29 @@ int solve_learned(Ctx &c, const gpz_solver_opts &o, gpz_solve_report &rep, bool 
   GPZ_CUDA_TRY(cudaEventCreate(&ev0));
   GPZ_CUDA_TRY(cudaEventCreate(&ev1));
   GPZ_CUDA_TRY(cudaEventRecord(ev0, s));
-  const int per_iter = mixed ? 6 : 5;
+  int64_t per_iter = mixed ? 6 : 5;  // the FP32 operator counts its own launches (measured at capture)
   auto iteration = [&]() {
+    if (blk) {
+      launch_spmv32(c, v32, c.sell, R, s);
+      k_lfb_update<<<wave(k_lfb_update), kThreads, 0, s>>>(w.dx32.p, w.r32.p, w.pm.p, w.q32.p, qpad, c.neq, R);
+      k_mx_foldx<<<wave(k_mx_foldx), kThreads, 0, s>>>(w.x.p, w.dx32.p, c.neq, 0, R);
+      GPZ_TPR_SWITCH(tpr, (k_reliable<T><<<wave(k_reliable<T>), kThreads, 0, s>>>(c.d_ia.p, c.d_ja.p, c.d_a.p,
+                                                                                    w.x.p, w.b.p, w.r.p, c.neq, R)));
+      k_fcg_t<<<wave(k_fcg_t), kThreads, 0, s>>>(L, w.r.p, w.r32.p, R);
+      k_lfb_z<<<wave(k_lfb_z), kThreads, 0, s>>>(L, w.r.p, w.r32.p, w.q32.p, qpad, c.d_dinv.p, w.z32.p, R);
+      k_lfb_p<<<wave(k_lfb_p), kThreads, 0, s>>>(w.z32.p, w.r32.p, c.d_dinv.p, w.pm.p, w.q32.p, qpad, qpad, c.neq,
+                                                 R);
+      c.launches += 6;
+      return;
+    }
     if (mixed) {
       GPZ_TPR_SWITCH(tpr32, (k_lfcg_spmv<T><<<wave(k_lfcg_spmv<T>), kThreads, 0, s>>>(
                                 c.d_ia.p, c.d_ja.p, c.d_a32.p, p32, w.p.p, w.q.p, c.neq, R)));
+      c.launches++;
     } else {
       GPZ_TPR_SWITCH(tpr, (k_cg_spmv<T, false><<<wave(k_cg_spmv<T, false>), kThreads, 0, s>>>(
                               c.d_ia.p, c.d_ja.p, c.d_a.p, nullptr, w.p.p, nullptr, w.q.p, c.neq, R)));
+      c.launches++;
     }
     k_fcg_update<<<wave(k_fcg_update), kThreads, 0, s>>>(w.x.p, w.r.p, w.r32.p, w.p.p, w.q.p, c.neq, mixed ? 1 : 0,
                                                          R);
@@ -1972,7 +2091,7 @@ int solve_learned(Ctx &c, const gpz_solver_opts &o, gpz_solve_report &rep, bool 
     k_fcg_t<<<wave(k_fcg_t), kThreads, 0, s>>>(L, w.r.p, w.r32.p, R);
     k_fcg_z<<<wave(k_fcg_z), kThreads, 0, s>>>(L, w.r.p, w.q.p, c.d_dinv.p, w.z.p, R);
     k_fcg_p<<<wave(k_fcg_p), kThreads, 0, s>>>(w.z.p, w.r.p, c.d_dinv.p, w.p.p, p32, c.neq, R);
-    c.launches += per_iter;
+    c.launches += mixed ? 5 : 4;
   };
   cudaGraphExec_t exec = nullptr;
   int64_t total_it = 0, nfallback = 0, nupd = 0, nspmv64 = 0, hstate[I_NISCAL] = {0};
@@ -1991,8 +2110,14 @@ int solve_learned(Ctx &c, const gpz_solver_opts &o, gpz_solve_report &rep, bool 
     GPZ_TPR_SWITCH(tpr, (k_cg_init<T><<<wave(k_cg_init<T>), kThreads, 0, s>>>(c.d_ia.p, c.d_ja.p, c.d_a.p, w.x.p,
                                                                                w.b.p, w.r.p, c.neq, from_current, R)));
     k_fcg_t<<<wave(k_fcg_t), kThreads, 0, s>>>(L, w.r.p, w.r32.p, R);  // k_cg_init leaves I_UPDATE = 2: FP64 r
-    k_fcg_z<<<wave(k_fcg_z), kThreads, 0, s>>>(L, w.r.p, w.q.p, c.d_dinv.p, w.z.p, R);
-    k_fcg_p<<<wave(k_fcg_p), kThreads, 0, s>>>(w.z.p, w.r.p, c.d_dinv.p, w.p.p, p32, c.neq, R);
+    if (blk) {
+      k_lfb_z<<<wave(k_lfb_z), kThreads, 0, s>>>(L, w.r.p, w.r32.p, w.q32.p, qpad, c.d_dinv.p, w.z32.p, R);
+      k_lfb_p<<<wave(k_lfb_p), kThreads, 0, s>>>(w.z32.p, w.r32.p, c.d_dinv.p, w.pm.p, w.q32.p, qpad, qpad, c.neq,
+                                                 R);
+    } else {
+      k_fcg_z<<<wave(k_fcg_z), kThreads, 0, s>>>(L, w.r.p, w.q.p, c.d_dinv.p, w.z.p, R);
+      k_fcg_p<<<wave(k_fcg_p), kThreads, 0, s>>>(w.z.p, w.r.p, c.d_dinv.p, w.p.p, p32, c.neq, R);
+    }
     c.launches += 4;
     GPZ_CUDA_TRY(cudaGetLastError());
     if (o.use_graph && !exec) {
@@ -2001,6 +2126,7 @@ int solve_learned(Ctx &c, const gpz_solver_opts &o, gpz_solve_report &rep, bool 
       const int64_t l0 = c.launches;
       for (int i = 0; i < batch; i++) iteration();
       GPZ_CUDA_TRY(cudaStreamEndCapture(s, &g));
+      per_iter = (c.launches - l0) / batch;
       c.launches = l0;
       GPZ_CUDA_TRY(cudaGraphInstantiate(&exec, g, 0));
       GPZ_CUDA_TRY(cudaGraphDestroy(g));
@@ -2016,6 +2142,10 @@ int solve_learned(Ctx &c, const gpz_solver_opts &o, gpz_solve_report &rep, bool 
         for (int i = 0; i < batch; i++) iteration();
       }
       GPZ_CUDA_TRY(cudaGetLastError());
+    }
+    if (blk) {
+      k_mx_foldx<<<wave(k_mx_foldx), kThreads, 0, s>>>(w.x.p, w.dx32.p, c.neq, 1, R);
+      c.launches++;
     }
     GPZ_TPR_SWITCH(tpr, (k_true_resid<T><<<wave(k_true_resid<T>), kThreads, 0, s>>>(c.d_ia.p, c.d_ja.p, c.d_a.p,
                                                                                      w.x.p, w.b.p, c.neq, R)));

@@ -110,11 +110,13 @@ def evaluate(ctx, grid, coef_of_seed, seeds, tol=1e-8, precond=gpz.GPZ_PRECOND_J
         ctx.assemble()
         base = ctx.solve(tol=tol, precond=precond, want_x=False)
         lrn = ctx.solve(solver=gpz.GPZ_SOLVER_LEARNED_FCG, tol=tol, want_x=False)
-        mixed = {}
-        if grid.desc.nstate == 1:  # learned + FP32-value SpMV (scalar problems)
-            m = ctx.solve(solver=gpz.GPZ_SOLVER_LEARNED_MIXED_FCG, tol=tol, reliable_delta=1e-2, want_x=False)
-            mixed = dict(learned_mixed_iterations=m["iterations"], learned_mixed_seconds=m["seconds"],
-                         learned_mixed_true_resid=m["true_resid"])
+        # learned + the FP32 operator (FP32 CSR for scalar problems; the autotuned 3x3-block or
+        # matrix-free operator for elasticity, which needs a mixed assembly)
+        if grid.desc.nstate == 3:
+            ctx.assemble(gpz.GPZ_PREC_MIXED)
+        m = ctx.solve(solver=gpz.GPZ_SOLVER_LEARNED_MIXED_FCG, tol=tol, reliable_delta=1e-2, want_x=False)
+        mixed = dict(learned_mixed_iterations=m["iterations"], learned_mixed_seconds=m["seconds"],
+                     learned_mixed_true_resid=m["true_resid"], learned_mixed_rc=m["rc"])
         out.append(dict(seed=s, base_precond="block_jacobi" if precond == gpz.GPZ_PRECOND_BLOCK_JACOBI else "jacobi",
                         **mixed,
                         base_iterations=base["iterations"], base_seconds=base["seconds"],

@@ -109,3 +109,59 @@ def test_learned_falls_back_to_jacobi(g):
     assert lrn["restarts"] >= lrn["iterations"]  # every application fell back
     assert abs(lrn["iterations"] - jac["iterations"]) <= max(3, 0.1 * jac["iterations"])
     ctx.close()
+
+
+def test_learned_gradient_matches_oracle_elasticity(g):
+    """The same check on 3D Q2 elasticity (81 equations per element, rank 8): every kernel of the 3-state,
+    rank-8 path (element gathers, dF outer products, the output layer) against the numpy oracle."""
+    n, R = 2, 8
+    rng = np.random.default_rng(3)
+    E = np.exp(rng.standard_normal(n ** 3))
+    grid = g.elasticity3d(n, 2, E=E, top_traction=False)  # penalty-Dirichlet base only: the mask of both sides
+    ctx = _ctx(g, grid)
+    npar = ctx.learned_init(rank=R, seed=2)
+    p = (0.2 * rng.standard_normal(npar)).astype(np.float32)
+    ctx.set_learned_params(p)
+    P = 2
+    Rs, Es = rng.standard_normal((P, grid.neq)), rng.standard_normal((P, grid.neq))
+    ctx.learned_set_pairs(Rs, Es)
+    loss, grad = ctx.learned_loss_grad()
+    ia, ja = ctx.pattern()
+    A = sp.csr_matrix((ctx.matrix(), ja, ia), shape=(grid.neq, grid.neq))
+    om = O.elasticity3d(n, 2, E=E, top_traction=False)
+    mesh = LO.mesh_from_oracle(om, A, E)
+    lref, gref = LO.loss_and_grad(mesh, A, p.astype(np.float64), R, Rs, Es)
+    assert abs(loss - lref) <= 1e-4 * abs(lref), (loss, lref)
+    off, _ = LO.layout(mesh.NS, R)
+    for name, (a, m) in off.items():
+        d = np.linalg.norm(grad[a:a + m] - gref[a:a + m])
+        assert d <= 1e-3 * max(np.linalg.norm(gref[a:a + m]), 1e-6 * np.linalg.norm(gref)), name
+    ctx.close()
+
+
+def test_learned_elasticity_weights_gain_and_mixed_path(g):
+    """The committed elasticity weights (trained on the GPU on 12^3 fields, neopz_gb300/data) on unseen 16^3
+    fields: the learned flexible CG needs at most 85% of the Jacobi-PCG iterations; the learned + mixed
+    path (the mixed CG's FP32 operator chosen by the autotuner, FP32 recurrence, FP64 true-residual
+    replacement) reaches the same true residual 1e-8 in about as many iterations, and its solution is
+    within 1e-5 of a tight FP64 solve."""
+    import os
+    from neopz_gb300 import learned
+    w = np.load(os.path.join(learned.DATA, "learned_elasticity3d_q2.npy"))
+    n = 16
+    grid, coef = learned.elasticity3d(n)
+    ctx = learned.context_for(grid, rank=8, seed=0, params=w)
+    for s in (10000, 10001):
+        ctx.set_coef(grid, coef(s))
+        ctx.assemble()
+        jac = ctx.solve(tol=1e-8, want_x=False)
+        lrn = ctx.solve(solver=g.GPZ_SOLVER_LEARNED_FCG, tol=1e-8, want_x=False)
+        assert jac["rc"] == 0 and lrn["rc"] == 0 and lrn["restarts"] == 0
+        assert lrn["iterations"] <= 0.85 * jac["iterations"], (s, lrn["iterations"], jac["iterations"])
+        ref = ctx.solve(tol=1e-11, max_iter=50000)
+        ctx.assemble(g.GPZ_PREC_MIXED)
+        mx = ctx.solve(solver=g.GPZ_SOLVER_LEARNED_MIXED_FCG, tol=1e-8, reliable_delta=1e-2)
+        assert mx["rc"] == 0 and mx["true_resid"] <= 1e-8 and mx["spmv_fp32"] > 0 and mx["reliable_updates"] >= 1
+        assert mx["iterations"] <= 1.1 * lrn["iterations"], (s, mx["iterations"], lrn["iterations"])
+        assert np.linalg.norm(mx["x"] - ref["x"]) <= 1e-5 * np.linalg.norm(ref["x"])
+    ctx.close()
