@@ -137,6 +137,7 @@ struct Learned {
   DBuf<float> feat;                          // [E] log coefficient
   DBuf<float> params, grad, m1, m2;
   DBuf<float> F;                             // [E][NS][R]
+  DBuf<uint16_t> F16;                        // F in bfloat16, read by the solves
   DBuf<float> t;                             // [E][R]
   DBuf<float> act, back, partial;            // activations, backward buffers, outer-product partials
   DBuf<double> red;                          // dot-product partials

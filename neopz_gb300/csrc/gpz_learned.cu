@@ -27,6 +27,8 @@
 #include <vector>
 
 #include "gpz_internal.h"
+#include <cuda_bf16.h>
+
 #include "gpz_learned.cuh"
 
 namespace gpz {
@@ -529,10 +531,16 @@ void init_params(Ctx &c, uint64_t seed) {
   L.have_params = true;
 }
 
+// the solves' copy of the factors, rounded to nearest bfloat16
+__global__ void __launch_bounds__(kT) k_ln_to_bf16(int64_t n, const float *__restrict__ F, uint16_t *__restrict__ h) {
+  for (int64_t i = gthread(); i < n; i += nthread()) h[i] = __bfloat16_as_ushort(__float2bfloat16_rn(F[i]));
+}
+
 LnView view_of(Ctx &c) {
   Learned &L = c.ln;
   LnView v;
   v.F = L.F.p;
+  v.F16 = L.F16.p;
   v.dest = L.dest.p;
   v.ne_ptr = L.ne_ptr.p;
   v.ne_idx = L.ne_idx.p;
@@ -724,6 +732,11 @@ void learned_prepare(Ctx &c) {
   k_ln_dsq<<<grid_t(c.neq), kT, 0, c.stream>>>(c.neq, c.d_dinv.p, L.mask.p, L.dsq.p, L.mdsq.p);
   c.launches++;
   forward(c);
+  const int64_t nf = L.E * L.NS * L.R;
+  L.F16.alloc(std::max<int64_t>(nf, 1));
+  k_ln_to_bf16<<<grid_t(nf), kT, 0, c.stream>>>(nf, L.F.p, L.F16.p);
+  c.launches++;
+  GPZ_CUDA_TRY(cudaGetLastError());
 }
 
 LnView learned_view(Ctx &c) { return view_of(c); }

@@ -23,6 +23,7 @@ namespace gpz {
 
 struct LnView {
   const float *F;         // [E][NS][R] element factors
+  const uint16_t *F16;    // the same rounded to bfloat16 for the solves (half the bytes per application)
   const int32_t *dest;    // [E][NS] element equations
   const int64_t *ne_ptr;  // [neq+1] equation -> (element, local) incidences
   const int32_t *ne_idx;  // e * NS + local
@@ -53,10 +54,40 @@ __device__ __forceinline__ void ln_elem_t(const LnView &L, const T *__restrict__
 
 constexpr int kLnMaxR = 8;  // largest rank R of the factors
 
-// t_e = F_e^T Q_e (m .* S r) with one warp per element: lanes over the element's
-// equations (coalesced rows of F, float4 loads for R = 8), then a warp sum per
-// column; lane k writes t_e[k].
-template <class T>
+// one factor row F_e[loc][0..R) (el = e * NS + loc) as floats; B16: from the
+// bfloat16 copy (one 16-byte load for R = 8)
+template <bool B16>
+__device__ __forceinline__ void ln_row(const LnView &L, size_t el, float (&f)[kLnMaxR]) {
+  if (B16) {
+    const uint16_t *h = L.F16 + el * L.R;
+    if (L.R == 8) {
+      const uint4 v = *(const uint4 *)h;
+      const uint32_t w[4] = {v.x, v.y, v.z, v.w};
+#pragma unroll
+      for (int k = 0; k < 4; k++) {
+        f[2 * k] = __uint_as_float(w[k] << 16);
+        f[2 * k + 1] = __uint_as_float(w[k] & 0xffff0000u);
+      }
+    } else {
+#pragma unroll
+      for (int k = 0; k < kLnMaxR; k++) f[k] = k < L.R ? __uint_as_float((uint32_t)h[k] << 16) : 0.f;
+    }
+  } else {
+    const float *g = L.F + el * L.R;
+    if (L.R == 8) {
+      const float4 a = *(const float4 *)g, b = *(const float4 *)(g + 4);
+      f[0] = a.x; f[1] = a.y; f[2] = a.z; f[3] = a.w; f[4] = b.x; f[5] = b.y; f[6] = b.z; f[7] = b.w;
+    } else {
+#pragma unroll
+      for (int k = 0; k < kLnMaxR; k++) f[k] = k < L.R ? g[k] : 0.f;
+    }
+  }
+}
+
+// t_e = F_e^T Q_e (m .* S r) with one warp per element (elements of 32 or more
+// equations): lanes over the element's equations, then a warp sum per column;
+// lane k writes t_e[k].
+template <class T, bool B16>
 __device__ __forceinline__ void ln_elem_t_warp(const LnView &L, const T *__restrict__ r, int64_t e, int lane) {
   float acc[kLnMaxR];
 #pragma unroll
@@ -65,16 +96,10 @@ __device__ __forceinline__ void ln_elem_t_warp(const LnView &L, const T *__restr
   for (int loc = lane; loc < L.NS; loc += 32) {
     const int32_t q = d[loc];
     const float v = L.mdsq[q] * (float)r[q];
-    const float *f = L.F + ((size_t)e * L.NS + loc) * L.R;
-    if (L.R == 8) {
-      const float4 a = *(const float4 *)f, b = *(const float4 *)(f + 4);
-      acc[0] += a.x * v; acc[1] += a.y * v; acc[2] += a.z * v; acc[3] += a.w * v;
-      acc[4] += b.x * v; acc[5] += b.y * v; acc[6] += b.z * v; acc[7] += b.w * v;
-    } else {
+    float f[kLnMaxR];
+    ln_row<B16>(L, (size_t)e * L.NS + loc, f);
 #pragma unroll
-      for (int k = 0; k < kLnMaxR; k++)
-        if (k < L.R) acc[k] += f[k] * v;
-    }
+    for (int k = 0; k < kLnMaxR; k++) acc[k] += f[k] * v;
   }
 #pragma unroll
   for (int k = 0; k < kLnMaxR; k++) {
@@ -85,25 +110,42 @@ __device__ __forceinline__ void ln_elem_t_warp(const LnView &L, const T *__restr
   }
 }
 
+// the same with one thread per (element, column k), for small elements
+template <class T>
+__device__ __forceinline__ void ln_elem_t16(const LnView &L, const T *__restrict__ r, int64_t idx) {
+  const int32_t e = (int32_t)idx / L.R;
+  const int k = (int)idx - e * L.R;
+  const int32_t *d = L.dest + e * L.NS;
+  const uint16_t *h = L.F16 + (size_t)e * L.NS * L.R + k;
+  float acc = 0.f;
+  for (int loc = 0; loc < L.NS; loc++) {
+    const int32_t q = d[loc];
+    acc += __uint_as_float((uint32_t)h[(size_t)loc * L.R] << 16) * (L.mdsq[q] * (float)r[q]);
+  }
+  L.t[idx] = acc;
+}
+
 // correction at equation i: m_i S_i sum_{(e,loc) at i} F_e[loc] . t_e
-__device__ __forceinline__ float ln_node_corr(const LnView &L, int64_t i) {
+template <bool B16>
+__device__ __forceinline__ float ln_node_corr_t(const LnView &L, int64_t i) {
   float c = 0.f;
   for (int64_t k = L.ne_ptr[i]; k < L.ne_ptr[i + 1]; k++) {
     const int32_t el = L.ne_idx[k];
     const int32_t e = el / L.NS;
-    const float *f = L.F + (size_t)el * L.R;
+    float f[kLnMaxR];
+    ln_row<B16>(L, (size_t)el, f);
     const float *t = L.t + (size_t)e * L.R;
     if (L.R == 8) {
-      const float4 f0 = *(const float4 *)f, f1 = *(const float4 *)(f + 4);
       const float4 t0 = *(const float4 *)t, t1 = *(const float4 *)(t + 4);
-      c += f0.x * t0.x + f0.y * t0.y + f0.z * t0.z + f0.w * t0.w + f1.x * t1.x + f1.y * t1.y + f1.z * t1.z +
-           f1.w * t1.w;
+      c += f[0] * t0.x + f[1] * t0.y + f[2] * t0.z + f[3] * t0.w + f[4] * t1.x + f[5] * t1.y + f[6] * t1.z +
+           f[7] * t1.w;
     } else {
       for (int j = 0; j < L.R; j++) c += f[j] * t[j];
     }
   }
   return L.mdsq[i] * c;
 }
+__device__ __forceinline__ float ln_node_corr(const LnView &L, int64_t i) { return ln_node_corr_t<false>(L, i); }
 
 // z_i = alpha r_i / a_ii + correction, alpha = exp(loga)
 template <class T>

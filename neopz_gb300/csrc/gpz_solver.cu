@@ -1371,11 +1371,18 @@ __global__ void __launch_bounds__(kThreads) k_fcg_t(LnView L, const double *__re
                                                     const float *__restrict__ r32, Red R) {
   if (!active(R.iscal)) return;
   const bool fresh = R.iscal[I_UPDATE] == 2;
-  const int lane = threadIdx.x & 31;
-  const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
-  for (int64_t e = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; e < L.E; e += nw) {
-    if (fresh) ln_elem_t_warp<double>(L, r64, e, lane);
-    else ln_elem_t_warp<float>(L, r32, e, lane);
+  if (L.NS >= 32) {  // a warp per element (3D elasticity: 81 equations)
+    const int lane = threadIdx.x & 31;
+    const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    for (int64_t e = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; e < L.E; e += nw) {
+      if (fresh) ln_elem_t_warp<double, true>(L, r64, e, lane);
+      else ln_elem_t_warp<float, true>(L, r32, e, lane);
+    }
+  } else {  // a thread per (element, column)
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < L.E * L.R; i += (int64_t)gridDim.x * blockDim.x) {
+      if (fresh) ln_elem_t16<double>(L, r64, i);
+      else ln_elem_t16<float>(L, r32, i);
+    }
   }
 }
 
@@ -1434,7 +1441,7 @@ __global__ void __launch_bounds__(kThreads) k_lfb_z(LnView L, const double *__re
     } else {
       ri = (double)r32[i];
     }
-    const double zi = (double)(float)(alpha * dinv[i] * ri + (double)ln_node_corr(L, i));
+    const double zi = (double)(float)(alpha * dinv[i] * ri + (double)ln_node_corr_t<true>(L, i));
     const double ji = dinv[i] * ri;
     z32[i] = (float)zi;
     zr += zi * ri;
@@ -1481,7 +1488,7 @@ __global__ void __launch_bounds__(kThreads) k_fcg_z(LnView L, const double *__re
   const double alpha = exp((double)*L.loga);
   double zr = 0.0, zq = 0.0, jr = 0.0, jq = 0.0;  // jr, jq: the Jacobi fallback's dots (FP64: its beta)
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < L.n; i += (int64_t)gridDim.x * blockDim.x) {
-    const double zi = ln_node_z<double>(L, r, alpha, i);
+    const double zi = alpha * L.dinv[i] * r[i] + (double)ln_node_corr_t<true>(L, i);
     const double ri = r[i];
     const double ji = dinv[i] * ri;
     z[i] = zi;
