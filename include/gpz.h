@@ -165,7 +165,7 @@ int gpz_spmv(gpz_ctx *ctx, double alpha, const double *x, double beta, const dou
 
 /* y = A32 x with the FP32 operator of the mixed solvers (host FP64 vectors):
  * the layout the SpMV autotuner chose, or `variant` (GPZ solver option
- * spmv_variant, 0..6) for 3-state problems; the FP32 CSR copy otherwise. */
+ * spmv_variant, 0..7) for 3-state problems; the FP32 CSR copy otherwise. */
 int gpz_spmv_fp32(gpz_ctx *ctx, int variant, const double *x, double *y);
 
 /* ---- solve ----------------------------------------------------------------
@@ -193,7 +193,8 @@ typedef struct {
   int32_t spmv_variant;    /* mixed CG: -1 = autotuned; 0 block CSR, 1 two rows in flight, 2 sliced ELL,
                               3 TMA-staged block CSR, 4 upper triangle with float4 atomics,
                               5 matrix-free elements (uniform Q2 hex elasticity + penalty faces),
-                              6 the same on the tensor cores (tcgen05, 3xTF32) */
+                              6 the same on the tensor cores (tcgen05, 3xTF32),
+                              7 the same sum-factorised on Lagrange nodal values */
 } gpz_solver_opts;
 
 typedef struct {

@@ -160,7 +160,10 @@ struct MatFree {
   DBuf<int32_t> frows;
   DBuf<double> energy;                       // the faces' share of p.q
   float big = 0.f;
-  int grid_vol = 1, grid_face = 1, grid_tc = 1;
+  int grid_vol = 1, grid_face = 1, grid_tc = 1, grid_sf = 1;
+  bool sf_ready = false;                     // the sum-factorised tables of the volume bucket were built
+  DBuf<float> sf_tab;                        // 1D Lagrange values / derivatives, weights, corner gradients, Phi
+  DBuf<int> sf_idx;
 };
 
 // ---------------------------------------------------------------- the context
@@ -290,7 +293,7 @@ int collect_cg_pairs(Ctx &c, int npairs, double tol, int64_t max_iter, double *R
                      int64_t *iters);
 // matfree.cu
 bool matfree_build(Ctx &c);
-void matfree_spmv(Ctx &c, cudaStream_t s, bool tensor);
+void matfree_spmv(Ctx &c, cudaStream_t s, int mode);  // 0 CUDA cores, 1 tcgen05, 2 sum-factorised
 // learned.cu
 void learned_prepare(Ctx &c);                // features, scaling and factors F for the assembled system
 // scan.cu

@@ -22,6 +22,7 @@
 #include <vector>
 
 #include "gpz_internal.h"
+#include "gpz_shapes.h"
 #include "gpz_solver_common.cuh"
 
 namespace gpz {
@@ -335,6 +336,311 @@ __global__ void __launch_bounds__(kMfThreads, 3) k_mf_hex27(int64_t n, const flo
   }
 }
 
+
+// ---------------------------------------------------------------- sum-factorised variant
+// The 27 Q2 functions of the hex span the tensor space Q2, so each element's
+// field is also given by its values v at the 27 Lagrange nodes (-1, 0, 1)^3:
+// v = Phi c with Phi[j][a] = phi_a(node j) (125 nonzeros; one long row, the
+// interior node).  On nodal values the reference gradients at the 3 x 3 x 3
+// Gauss points factor into 1D contractions with the 3 x 3 Lagrange value and
+// derivative matrices B, D: 8 x 81 multiply-adds per component instead of
+// 27 x 81, and the transposed contractions and Phi^T bring the stresses back.
+// One warp per element; the 27 active lanes are (component, pencil) in the
+// tensor stages and points in the pointwise stage, exchanging through shared
+// memory.  The arithmetic is the element operator of k_mf_hex27 with another
+// summation order.
+constexpr int kSfThreads = 128;
+constexpr int kSfWarps = kSfThreads / 32;
+constexpr int kSfMaxNz = 160;  // stored nonzeros of Phi (rows of <= 9, plus the long row)
+// table layout (floats): B[3][3], D[3][3], w[27], corner gradients [27][3][8],
+// long row [27], row values, column values
+constexpr int SF_B = 0, SF_D = 9, SF_W = 18, SF_DC = 45, SF_LONG = SF_DC + 27 * 24, SF_RV = SF_LONG + 27,
+              SF_CV = SF_RV + kSfMaxNz, SF_NF = SF_CV + kSfMaxNz;
+// index layout (ints): row pointers [28], column pointers [28], row columns, column rows, long row index
+constexpr int SFI_RP = 0, SFI_CP = 28, SFI_RC = 56, SFI_CR = SFI_RC + kSfMaxNz, SFI_LONG = SFI_CR + kSfMaxNz,
+              SFI_NI = SFI_LONG + 1;
+
+// 1D Lagrange values B[q][j] and derivatives D[q][j] at the 3 Gauss points:
+// warp-uniform operands, read through the constant cache
+__constant__ float c_sfB[9], c_sfD[9];
+
+struct SfWarp {
+  float4 su[27];   // element coefficients (3 components per shape)
+  float v[81];     // [s][j] nodal values, later the adjoint's nodal output
+  float t1[2][81]; // zeta contractions (B, D): [s][j1 + 3 j2 + 9 q3]
+  float t2[3][81]; // eta contractions (BB, DB, BD): [s][j1 + 3 q2 + 9 q3]
+  float h[9][27];  // [s * 3 + d][q] reference gradients, then the pulled-back stresses
+  float geo[34];   // corners, then the affine geometry (Jinv, |det J|)
+};
+
+__global__ void __launch_bounds__(kSfThreads, 5) k_mf_hex27_sf(int64_t n, const float *__restrict__ rxyz,
+                                                               const int32_t *__restrict__ rows,
+                                                               const float *__restrict__ rlm,
+                                                               const float *__restrict__ rgeo,
+                                                               const float *__restrict__ tabf,
+                                                               const int *__restrict__ tabi,
+                                                               const float4 *__restrict__ p4, float4 *__restrict__ q4,
+                                                               const double *__restrict__ face_energy, Red R) {
+  if (!active(R.iscal)) return;
+  __shared__ float sf[SF_NF];
+  __shared__ int si[SFI_NI];
+  __shared__ SfWarp sw[kSfWarps];
+  for (int k = threadIdx.x; k < SF_NF; k += blockDim.x) sf[k] = tabf[k];
+  for (int k = threadIdx.x; k < SFI_NI; k += blockDim.x) si[k] = tabi[k];
+  __syncthreads();
+  const int lane = threadIdx.x & 31, wp = threadIdx.x >> 5;
+  SfWarp &W = sw[wp];
+  const float *B = c_sfB, *D = c_sfD;
+  const int jl = si[SFI_LONG];
+  // this lane's row (node j = lane) and column (shape a = lane) of Phi, in registers
+  constexpr int kRow = 9, kCol = 8;
+  float rv[kRow], cv[kCol];
+  uint32_t rc[3] = {0u, 0u, 0u}, cr[2] = {0u, 0u};  // indices (< 27), four per word
+  int nrow = 0, ncol = 0;
+  if (lane < kNS) {
+    const int r0 = si[SFI_RP + lane], c0 = si[SFI_CP + lane];
+    nrow = lane == jl ? 0 : min(kRow, si[SFI_RP + lane + 1] - r0);
+    ncol = min(kCol, si[SFI_CP + lane + 1] - c0);
+#pragma unroll
+    for (int k = 0; k < kRow; k++) {
+      rv[k] = k < nrow ? sf[SF_RV + r0 + k] : 0.f;
+      rc[k / 4] |= (uint32_t)(k < nrow ? si[SFI_RC + r0 + k] : 0) << (8 * (k % 4));
+    }
+#pragma unroll
+    for (int k = 0; k < kCol; k++) {
+      cv[k] = k < ncol ? sf[SF_CV + c0 + k] : 0.f;
+      cr[k / 4] |= (uint32_t)(k < ncol ? si[SFI_CR + c0 + k] : 0) << (8 * (k % 4));
+    }
+  }
+  const float flong = lane < kNS ? sf[SF_LONG + lane] : 0.f;
+  // stage lanes: component s and pencil p (two tensor indices of 0..2)
+  const bool act = lane < 27;
+  const int s = act ? lane / 9 : 0, p = lane % 9;
+  const int pa = p % 3, pb = p / 3;
+  KSum en;
+  const int64_t step = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  int64_t i = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  int32_t row = 0;
+  float cxv = 0.f, gv = 0.f, lam = 0.f, mu = 0.f;
+  if (i < n) {
+    if (lane < kNS) row = rows[i * kNS + lane];
+    if (lane < 24) cxv = rxyz[i * 24 + lane];
+    if (lane < 10) gv = rgeo[i * 10 + lane];
+    lam = rlm[2 * i];
+    mu = rlm[2 * i + 1];
+  }
+  for (; i < n; i += step) {
+    float4 u = make_float4(0.f, 0.f, 0.f, 0.f);
+    if (lane < kNS) {
+      u = p4[row];
+      W.su[lane] = u;
+    }
+    if (lane < 24) W.geo[lane] = cxv;
+    if (lane < 10) W.geo[24 + lane] = gv;
+    const float lam_i = lam, mu_i = mu;
+    const int32_t row_i = row;
+    const int64_t nx = i + step;
+    if (nx < n) {
+      if (lane < kNS) row = rows[nx * kNS + lane];
+      if (lane < 24) cxv = rxyz[nx * 24 + lane];
+      if (lane < 10) gv = rgeo[nx * 10 + lane];
+      lam = rlm[2 * nx];
+      mu = rlm[2 * nx + 1];
+    }
+    __syncwarp();
+    // v = Phi c: short rows by their lane, the long row as a warp sum
+    {
+      float a0 = 0.f, a1 = 0.f, a2 = 0.f;
+      if (lane < kNS && lane != jl) {
+#pragma unroll
+        for (int k = 0; k < kRow; k++) {
+          if (k >= nrow) break;
+          const float4 c = W.su[(rc[k / 4] >> (8 * (k % 4))) & 0xffu];
+          a0 = fmaf(rv[k], c.x, a0);
+          a1 = fmaf(rv[k], c.y, a1);
+          a2 = fmaf(rv[k], c.z, a2);
+        }
+        W.v[lane] = a0;
+        W.v[27 + lane] = a1;
+        W.v[54 + lane] = a2;
+      }
+      float b0 = flong * u.x, b1 = flong * u.y, b2 = flong * u.z;
+      for (int o = 16; o > 0; o >>= 1) {
+        b0 += __shfl_xor_sync(0xffffffffu, b0, o);
+        b1 += __shfl_xor_sync(0xffffffffu, b1, o);
+        b2 += __shfl_xor_sync(0xffffffffu, b2, o);
+      }
+      if (lane == 0) {
+        W.v[jl] = b0;
+        W.v[27 + jl] = b1;
+        W.v[54 + jl] = b2;
+      }
+    }
+    __syncwarp();
+    // zeta: lane (s, j1 = pa, j2 = pb)
+    if (act) {
+      const float x0 = W.v[s * 27 + p], x1 = W.v[s * 27 + p + 9], x2 = W.v[s * 27 + p + 18];
+#pragma unroll
+      for (int q3 = 0; q3 < 3; q3++) {
+        W.t1[0][s * 27 + p + 9 * q3] = B[q3 * 3] * x0 + B[q3 * 3 + 1] * x1 + B[q3 * 3 + 2] * x2;
+        W.t1[1][s * 27 + p + 9 * q3] = D[q3 * 3] * x0 + D[q3 * 3 + 1] * x1 + D[q3 * 3 + 2] * x2;
+      }
+    }
+    __syncwarp();
+    // eta: lane (s, j1 = pa, q3 = pb)
+    if (act) {
+      const int b = s * 27 + pa + 9 * pb;
+      const float y0 = W.t1[0][b], y1 = W.t1[0][b + 3], y2 = W.t1[0][b + 6];
+      const float z0 = W.t1[1][b], z1 = W.t1[1][b + 3], z2 = W.t1[1][b + 6];
+#pragma unroll
+      for (int q2 = 0; q2 < 3; q2++) {
+        W.t2[0][b + 3 * q2] = B[q2 * 3] * y0 + B[q2 * 3 + 1] * y1 + B[q2 * 3 + 2] * y2;
+        W.t2[1][b + 3 * q2] = D[q2 * 3] * y0 + D[q2 * 3 + 1] * y1 + D[q2 * 3 + 2] * y2;
+        W.t2[2][b + 3 * q2] = B[q2 * 3] * z0 + B[q2 * 3 + 1] * z1 + B[q2 * 3 + 2] * z2;
+      }
+    }
+    __syncwarp();
+    // xi: lane (s, q2 = pa, q3 = pb) -> reference gradients at q = q1 + 3 p
+    if (act) {
+      const int b = s * 27 + 3 * p;
+      const float g0 = W.t2[0][b], g1 = W.t2[0][b + 1], g2 = W.t2[0][b + 2];
+      const float e0 = W.t2[1][b], e1 = W.t2[1][b + 1], e2 = W.t2[1][b + 2];
+      const float f0 = W.t2[2][b], f1 = W.t2[2][b + 1], f2 = W.t2[2][b + 2];
+#pragma unroll
+      for (int q1 = 0; q1 < 3; q1++) {
+        const int q = q1 + 3 * p;
+        W.h[s * 3 + 0][q] = D[q1 * 3] * g0 + D[q1 * 3 + 1] * g1 + D[q1 * 3 + 2] * g2;
+        W.h[s * 3 + 1][q] = B[q1 * 3] * e0 + B[q1 * 3 + 1] * e1 + B[q1 * 3 + 2] * e2;
+        W.h[s * 3 + 2][q] = B[q1 * 3] * f0 + B[q1 * 3 + 1] * f1 + B[q1 * 3 + 2] * f2;
+      }
+    }
+    __syncwarp();
+    // pointwise: lane q
+    if (lane < kNQ) {
+      const int q = lane;
+      float ji[3][3], det;
+      if (W.geo[24 + 9] > 0.f) {
+#pragma unroll
+        for (int k = 0; k < 9; k++) ji[k / 3][k % 3] = W.geo[24 + k];
+        det = W.geo[24 + 9];
+      } else {
+        float a[3][3] = {{0.f, 0.f, 0.f}, {0.f, 0.f, 0.f}, {0.f, 0.f, 0.f}};
+        const float *dc = sf + SF_DC + q * 24;
+#pragma unroll
+        for (int k = 0; k < 8; k++)
+#pragma unroll
+          for (int j = 0; j < 3; j++)
+#pragma unroll
+            for (int d = 0; d < 3; d++) a[j][d] += W.geo[k * 3 + j] * dc[d * 8 + k];
+        det = -a[0][2] * a[1][1] * a[2][0] + a[0][1] * a[1][2] * a[2][0] + a[0][2] * a[1][0] * a[2][1] -
+              a[0][0] * a[1][2] * a[2][1] - a[0][1] * a[1][0] * a[2][2] + a[0][0] * a[1][1] * a[2][2];
+        const float id = 1.f / det;
+        ji[0][0] = (-a[1][2] * a[2][1] + a[1][1] * a[2][2]) * id;
+        ji[0][1] = (a[0][2] * a[2][1] - a[0][1] * a[2][2]) * id;
+        ji[0][2] = (-a[0][2] * a[1][1] + a[0][1] * a[1][2]) * id;
+        ji[1][0] = (a[1][2] * a[2][0] - a[1][0] * a[2][2]) * id;
+        ji[1][1] = (-a[0][2] * a[2][0] + a[0][0] * a[2][2]) * id;
+        ji[1][2] = (a[0][2] * a[1][0] - a[0][0] * a[1][2]) * id;
+        ji[2][0] = (-a[1][1] * a[2][0] + a[1][0] * a[2][1]) * id;
+        ji[2][1] = (a[0][1] * a[2][0] - a[0][0] * a[2][1]) * id;
+        ji[2][2] = (-a[0][1] * a[1][0] + a[0][0] * a[1][1]) * id;
+      }
+      float hh[3][3], H[3][3], T[3][3];
+#pragma unroll
+      for (int s2 = 0; s2 < 3; s2++)
+#pragma unroll
+        for (int j = 0; j < 3; j++) hh[s2][j] = W.h[s2 * 3 + j][q];
+#pragma unroll
+      for (int s2 = 0; s2 < 3; s2++)
+#pragma unroll
+        for (int d = 0; d < 3; d++) H[s2][d] = hh[s2][0] * ji[0][d] + hh[s2][1] * ji[1][d] + hh[s2][2] * ji[2][d];
+      const float wd = sf[SF_W + q] * fabsf(det);
+      const float lt = lam_i * (H[0][0] + H[1][1] + H[2][2]);
+#pragma unroll
+      for (int s2 = 0; s2 < 3; s2++)
+#pragma unroll
+        for (int d = 0; d < 3; d++) T[s2][d] = wd * (mu_i * (H[s2][d] + H[d][s2]) + (s2 == d ? lt : 0.f));
+#pragma unroll
+      for (int s2 = 0; s2 < 3; s2++)
+#pragma unroll
+        for (int j = 0; j < 3; j++)
+          W.h[s2 * 3 + j][q] = T[s2][0] * ji[j][0] + T[s2][1] * ji[j][1] + T[s2][2] * ji[j][2];
+    }
+    __syncwarp();
+    // transposed xi: lane (s, q2 = pa, q3 = pb)
+    if (act) {
+      const int b = s * 27 + 3 * p;
+      float g[3], e[3], f[3];
+#pragma unroll
+      for (int q1 = 0; q1 < 3; q1++) {
+        g[q1] = W.h[s * 3 + 0][q1 + 3 * p];
+        e[q1] = W.h[s * 3 + 1][q1 + 3 * p];
+        f[q1] = W.h[s * 3 + 2][q1 + 3 * p];
+      }
+#pragma unroll
+      for (int j1 = 0; j1 < 3; j1++) {
+        W.t2[0][b + j1] = D[j1] * g[0] + D[3 + j1] * g[1] + D[6 + j1] * g[2];
+        W.t2[1][b + j1] = B[j1] * e[0] + B[3 + j1] * e[1] + B[6 + j1] * e[2];
+        W.t2[2][b + j1] = B[j1] * f[0] + B[3 + j1] * f[1] + B[6 + j1] * f[2];
+      }
+    }
+    __syncwarp();
+    // transposed eta: lane (s, j1 = pa, q3 = pb)
+    if (act) {
+      const int b = s * 27 + pa + 9 * pb;
+      float g[3], e[3], f[3];
+#pragma unroll
+      for (int q2 = 0; q2 < 3; q2++) {
+        g[q2] = W.t2[0][b + 3 * q2];
+        e[q2] = W.t2[1][b + 3 * q2];
+        f[q2] = W.t2[2][b + 3 * q2];
+      }
+#pragma unroll
+      for (int j2 = 0; j2 < 3; j2++) {
+        W.t1[0][b + 3 * j2] = B[j2] * g[0] + B[3 + j2] * g[1] + B[6 + j2] * g[2] + D[j2] * e[0] + D[3 + j2] * e[1] +
+                              D[6 + j2] * e[2];
+        W.t1[1][b + 3 * j2] = B[j2] * f[0] + B[3 + j2] * f[1] + B[6 + j2] * f[2];
+      }
+    }
+    __syncwarp();
+    // transposed zeta: lane (s, j1 = pa, j2 = pb) -> nodal output
+    if (act) {
+      float g[3], f[3];
+#pragma unroll
+      for (int q3 = 0; q3 < 3; q3++) {
+        g[q3] = W.t1[0][s * 27 + p + 9 * q3];
+        f[q3] = W.t1[1][s * 27 + p + 9 * q3];
+      }
+#pragma unroll
+      for (int j3 = 0; j3 < 3; j3++)
+        W.v[s * 27 + p + 9 * j3] = B[j3] * g[0] + B[3 + j3] * g[1] + B[6 + j3] * g[2] + D[j3] * f[0] +
+                                   D[3 + j3] * f[1] + D[6 + j3] * f[2];
+    }
+    __syncwarp();
+    // y = Phi^T v: lane a, its column (<= 8 nodes)
+    if (lane < kNS) {
+      float y0 = 0.f, y1 = 0.f, y2 = 0.f;
+#pragma unroll
+      for (int k = 0; k < kCol; k++) {
+        if (k >= ncol) break;
+        const int j = (cr[k / 4] >> (8 * (k % 4))) & 0xffu;
+        y0 = fmaf(cv[k], W.v[j], y0);
+        y1 = fmaf(cv[k], W.v[27 + j], y1);
+        y2 = fmaf(cv[k], W.v[54 + j], y2);
+      }
+      en.add(y0 * u.x + y1 * u.y + y2 * u.z);
+      atomicAdd(&q4[row_i], make_float4(y0, y1, y2, 0.f));
+    }
+    __syncwarp();
+  }
+  double v[1] = {en.get()}, tot[1];
+  if (grid_reduce<1>(v, R, tot) && threadIdx.x == 0) {
+    const double pq = tot[0] + (face_energy ? *face_energy : 0.0);
+    R.scal[S_PQ] = pq;
+    R.scal[S_ALPHA] = R.scal[S_RHO] / pq;
+    R.iscal[I_SP32]++;
+  }
+}
 
 // ---------------------------------------------------------------- tensor-core variant
 // The same operator with the two element contractions on the 5th-generation
@@ -715,6 +1021,117 @@ int mf_grid(K kernel, int threads) {
 
 }  // namespace
 
+// Tables of the sum-factorised operator for the volume bucket: Phi at the
+// Lagrange nodes (-1, 0, 1)^3 from the bucket's own shape functions, the 1D
+// Lagrange values and derivatives at the rule's 1D Gauss points, the weights
+// and the corner-shape gradients.  Built in FP64 and checked: the factorised
+// gradients must reproduce the bucket's table at every point (1e-10), else
+// the variant is not offered.
+bool sf_tables(Ctx &c, const Bucket &vol) {
+  const BucketKey &k = vol.key;
+  std::vector<double> g1, w1;
+  gauss_rule(GPZ_EL_LINE, k.intorder, g1, w1);
+  if ((int)g1.size() != 3) return false;
+  const double node[3] = {-1.0, 0.0, 1.0};
+  auto lag = [&](int j, double x) {
+    return j == 0 ? 0.5 * x * (x - 1.0) : j == 1 ? 1.0 - x * x : 0.5 * x * (x + 1.0);
+  };
+  auto dlag = [&](int j, double x) { return j == 0 ? x - 0.5 : j == 1 ? -2.0 * x : x + 0.5; };
+  double Bd[3][3], Dd[3][3];
+  for (int q = 0; q < 3; q++)
+    for (int j = 0; j < 3; j++) {
+      Bd[q][j] = lag(j, g1[q]);
+      Dd[q][j] = dlag(j, g1[q]);
+    }
+  double phi[kMaxShapes], dph[3 * kMaxShapes];
+  std::vector<double> P((size_t)kNQ * kNS);
+  for (int j = 0; j < kNQ; j++) {
+    const double pt[3] = {node[j % 3], node[(j / 3) % 3], node[j / 9]};
+    if (eval_shapes(k.type, k.orders, k.trans, pt, phi, dph, kMaxShapes) != kNS) return false;
+    for (int a = 0; a < kNS; a++) P[j * kNS + a] = std::fabs(phi[a]) > 1e-13 ? phi[a] : 0.0;
+  }
+  // the factorised reference gradients reproduce the table
+  double worst = 0.0, scale = 0.0;
+  for (int q = 0; q < kNQ; q++) {
+    const int q1 = q % 3, q2 = (q / 3) % 3, q3 = q / 9;
+    for (int a = 0; a < kNS; a++) {
+      double g[3] = {0.0, 0.0, 0.0};
+      for (int j = 0; j < kNQ; j++) {
+        const int j1 = j % 3, j2 = (j / 3) % 3, j3 = j / 9;
+        const double pa = P[j * kNS + a];
+        if (pa == 0.0) continue;
+        g[0] += pa * Dd[q1][j1] * Bd[q2][j2] * Bd[q3][j3];
+        g[1] += pa * Bd[q1][j1] * Dd[q2][j2] * Bd[q3][j3];
+        g[2] += pa * Bd[q1][j1] * Bd[q2][j2] * Dd[q3][j3];
+      }
+      for (int d = 0; d < 3; d++) {
+        const double t = vol.dphi[((size_t)q * 3 + d) * kNS + a];
+        worst = std::max(worst, std::fabs(g[d] - t));
+        scale = std::max(scale, std::fabs(t));
+      }
+    }
+  }
+  if (!(worst <= 1e-10 * scale)) return false;
+  std::vector<float> tf(SF_NF, 0.f);
+  std::vector<int> ti(SFI_NI, 0);
+  for (int q = 0; q < 3; q++)
+    for (int j = 0; j < 3; j++) {
+      tf[SF_B + q * 3 + j] = (float)Bd[q][j];
+      tf[SF_D + q * 3 + j] = (float)Dd[q][j];
+    }
+  for (int q = 0; q < kNQ; q++) {
+    tf[SF_W + q] = (float)vol.w[q];
+    for (int d = 0; d < 3; d++)
+      for (int kk = 0; kk < 8; kk++) tf[SF_DC + q * 24 + d * 8 + kk] = (float)vol.dphi[((size_t)q * 3 + d) * kNS + kk];
+  }
+  // rows of <= 9 nonzeros by their lane; at most one longer row, summed across the warp
+  int jl = -1, nr = 0, nc = 0;
+  for (int j = 0; j < kNQ; j++) {
+    int len = 0;
+    for (int a = 0; a < kNS; a++) len += P[j * kNS + a] != 0.0;
+    if (len > 9) {
+      if (jl >= 0) return false;
+      jl = j;
+    }
+  }
+  if (jl < 0) jl = 0;  // every row short: row 0 goes the warp-sum way
+  for (int a = 0; a < kNS; a++) {
+    int len = 0;
+    for (int j = 0; j < kNQ; j++) len += P[j * kNS + a] != 0.0;
+    if (len > 8) return false;  // the kernel keeps <= 8 entries of a column in registers
+  }
+  for (int j = 0; j < kNQ; j++) {
+    ti[SFI_RP + j] = nr;
+    if (j == jl) continue;
+    for (int a = 0; a < kNS; a++)
+      if (P[j * kNS + a] != 0.0) {
+        if (nr >= kSfMaxNz) return false;
+        ti[SFI_RC + nr] = a;
+        tf[SF_RV + nr++] = (float)P[j * kNS + a];
+      }
+  }
+  ti[SFI_RP + kNQ] = nr;
+  for (int a = 0; a < kNS; a++) tf[SF_LONG + a] = (float)P[jl * kNS + a];
+  for (int a = 0; a < kNS; a++) {
+    ti[SFI_CP + a] = nc;
+    for (int j = 0; j < kNQ; j++)
+      if (P[j * kNS + a] != 0.0) {
+        if (nc >= kSfMaxNz) return false;
+        ti[SFI_CR + nc] = j;
+        tf[SF_CV + nc++] = (float)P[j * kNS + a];
+      }
+  }
+  ti[SFI_CP + kNS] = nc;
+  ti[SFI_LONG] = jl;
+  c.mf.sf_tab.upload(tf.data(), tf.size(), c.stream);
+  c.mf.sf_idx.upload(ti.data(), ti.size(), c.stream);
+  // B and D depend only on the 3-point rule: the same values for every context
+  GPZ_CUDA_TRY(cudaMemcpyToSymbolAsync(c_sfB, tf.data() + SF_B, 9 * sizeof(float), 0, cudaMemcpyHostToDevice, c.stream));
+  GPZ_CUDA_TRY(cudaMemcpyToSymbolAsync(c_sfD, tf.data() + SF_D, 9 * sizeof(float), 0, cudaMemcpyHostToDevice, c.stream));
+  GPZ_CUDA_TRY(cudaStreamSynchronize(c.stream));
+  return true;
+}
+
 // Build the element records of the matrix-free operator; false when the mesh
 // is not made of uniform Q2 hex elasticity elements plus penalty / traction faces.
 bool matfree_build(Ctx &c) {
@@ -776,6 +1193,7 @@ bool matfree_build(Ctx &c) {
   M.energy.alloc(1);
   GPZ_CUDA_TRY(cudaGetLastError());
   check_device_flag(c, "matrix-free records");
+  M.sf_ready = sf_tables(c, *vol);
   M.grid_vol = mf_grid(k_mf_hex27, kMfThreads);
   M.grid_face = mf_grid(k_mf_faces, kThreads);
   GPZ_CUDA_TRY(cudaFuncSetAttribute(k_mf_hex27_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)OFF_TC_END));
@@ -785,13 +1203,14 @@ bool matfree_build(Ctx &c) {
     GPZ_CUDA_TRY(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
     M.grid_tc = std::max(1, std::min(kGridBlocks, nsm));  // one 187 KB CTA per SM, persistent over tiles
   }
+  M.grid_sf = mf_grid(k_mf_hex27_sf, kSfThreads);
   M.ready = true;
   return true;
 }
 
 // q4 = A p4 (q4 zeroed by the caller), p.q and alpha as the block SpMV kernels;
 // tensor: the tcgen05 3xTF32 volume kernel instead of the CUDA-core one
-void matfree_spmv(Ctx &c, cudaStream_t s, bool tensor) {
+void matfree_spmv(Ctx &c, cudaStream_t s, int mode) {
   MatFree &M = c.mf;
   SolverWork &w = c.sw;
   Red R{w.partial.p, w.counter.p, w.scal.p, w.iscal.p};
@@ -802,13 +1221,16 @@ void matfree_spmv(Ctx &c, cudaStream_t s, bool tensor) {
                                                 q4, M.energy.p, R);
     c.launches++;
   }
-  if (tensor)
+  const double *fe = M.nface ? M.energy.p : nullptr;
+  if (mode == 1)
     k_mf_hex27_tc<<<M.grid_tc, kTcThreads, OFF_TC_END, s>>>(M.nvol, M.vxyz.p, M.vrows.p, M.vlm.p, M.vgeo.p, M.vdphi.p,
-                                                            M.vw.p,
-                                                            p4, q4, M.nface ? M.energy.p : nullptr, c.d_err.p, R);
+                                                            M.vw.p, p4, q4, fe, c.d_err.p, R);
+  else if (mode == 2)
+    k_mf_hex27_sf<<<M.grid_sf, kSfThreads, 0, s>>>(M.nvol, M.vxyz.p, M.vrows.p, M.vlm.p, M.vgeo.p, M.sf_tab.p,
+                                                   M.sf_idx.p, p4, q4, fe, R);
   else
     k_mf_hex27<<<M.grid_vol, kMfThreads, 0, s>>>(M.nvol, M.vxyz.p, M.vrows.p, M.vlm.p, M.vgeo.p, M.vdphi.p, M.vw.p, p4, q4,
-                                                 M.nface ? M.energy.p : nullptr, R);
+                                                 fe, R);
   c.launches++;
 }
 

@@ -1607,8 +1607,8 @@ Red red_of(Ctx &c);
 // one launch of the FP32 3x3 SpMV variant v: q32 = A32 pm
 void launch_spmv32(Ctx &c, int v, const Ctx::Sell &S, Red R, cudaStream_t s) {
   SolverWork &w = c.sw;
-  if (v == 5 || v == 6) {
-    matfree_spmv(c, s, v == 6);  // element by element (gpz_matfree.cu), counts its own launches
+  if (v == 5 || v == 6 || v == 7) {
+    matfree_spmv(c, s, v - 5);  // element by element (gpz_matfree.cu), counts its own launches
     return;
   }
   if (v == 0) {
@@ -1717,8 +1717,9 @@ void tune_spmv32(Ctx &c, int only, bool timing) {
     GPZ_CUDA_TRY(cudaGetLastError());
     res.push_back({4, 0, time_it(4, cand[0])});
   }
-  if ((want(5) || want(6)) && matfree_build(c)) {
+  if ((want(5) || want(6) || want(7)) && matfree_build(c)) {
     if (want(5)) res.push_back({5, 0, time_it(5, cand[0])});
+    if (want(7) && c.mf.sf_ready) res.push_back({7, 0, time_it(7, cand[0])});
     if (want(6)) {
       res.push_back({6, 0, time_it(6, cand[0])});
       check_device_flag(c, "tensor-core matrix-free operator");
@@ -1744,6 +1745,7 @@ void tune_spmv32(Ctx &c, int only, bool timing) {
                      : res[i].v == 4 ? "upper_blocks_float4_atomics"
                      : res[i].v == 5 ? "matrix_free_elements"
                      : res[i].v == 6 ? "matrix_free_tcgen05_3xtf32"
+                     : res[i].v == 7 ? "matrix_free_sum_factorised"
                                      : "sliced_ell";
     rep += std::string(i ? ", " : "") + "\"" + nm + (res[i].v == 2 ? "_w" + std::to_string(res[i].window) : "") +
            "\": " + std::to_string(res[i].ms);
@@ -1752,8 +1754,9 @@ void tune_spmv32(Ctx &c, int only, bool timing) {
   if (c.d_uptr.p) {
     GPZ_CUDA_TRY(cudaMemcpy(&nu, c.d_uptr.p + c.nbrow, sizeof(int64_t), cudaMemcpyDeviceToHost));
   }
-  const char *names[7] = {"block_csr", "block_csr_2rows", "sliced_ell", "block_csr_tma_staged",
-                          "upper_blocks_float4_atomics", "matrix_free_elements", "matrix_free_tcgen05_3xtf32"};
+  const char *names[8] = {"block_csr", "block_csr_2rows", "sliced_ell", "block_csr_tma_staged",
+                          "upper_blocks_float4_atomics", "matrix_free_elements", "matrix_free_tcgen05_3xtf32",
+                          "matrix_free_sum_factorised"};
   c.tune_report = rep + ", \"chosen\": \"" + names[res[best].v] + "\", \"block_rows\": " + std::to_string(c.nbrow) +
                   ", \"blocks_full\": " + std::to_string(c.nnz / 9) + ", \"blocks_upper\": " + std::to_string(nu) +
                   "}";
@@ -1872,7 +1875,7 @@ void launch_iteration(Ctx &c, const Plan &P) {
     return;
   }
   const int padded = P.bsr ? 1 : 0;
-  const bool sym = P.bsr && c.spmv32_variant >= 4;  // 4, 5, 6: q accumulated with atomics
+  const bool sym = P.bsr && c.spmv32_variant >= 4;  // 4..7: q accumulated with atomics
   k_mx_p<<<wave(k_mx_p), kThreads, 0, c.stream>>>(w.r32.p, P.M32, w.pm.p, padded, sym ? w.q32.p : nullptr, P.nunits,
                                                   R);
   if (P.bsr) {

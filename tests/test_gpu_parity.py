@@ -201,7 +201,7 @@ def test_mixed_block_jacobi_bsr3(built):
     ctx.close()
 
 
-@pytest.mark.parametrize("variant", [0, 1, 2, 3, 4, 5, 6])
+@pytest.mark.parametrize("variant", [0, 1, 2, 3, 4, 5, 6, 7])
 def test_mixed_spmv_variants_converge(built, variant):
     """Every layout / kernel the SpMV autotuner can pick gives the same converged solution."""
     g = _gpz()
@@ -336,10 +336,11 @@ def test_assembly_graph_replay(built):
     ctx.close()
 
 
-@pytest.mark.parametrize("variant", [0, 1, 2, 3, 4, 5, 6])
+@pytest.mark.parametrize("variant", [0, 1, 2, 3, 4, 5, 6, 7])
 def test_fp32_operator_layouts_match_fp64_spmv(built, variant):
     """Every FP32 operator layout of the mixed CG (block CSR, two rows, sliced ELL, TMA-staged, upper blocks
-    with atomics, matrix-free elements on CUDA cores and on the tensor cores in 3xTF32) applies the assembled
+    with atomics, matrix-free elements on CUDA cores, on the tensor cores in 3xTF32 and sum-factorised on
+    Lagrange nodal values) applies the assembled
     operator: within 1e-5 of the FP64 CSR SpMV,
     normwise and on the non-penalty rows alone."""
     g = _gpz()
@@ -391,6 +392,6 @@ def test_distorted_mesh_general_quadrature_path(built):
     assert np.max(np.abs(f - of)) <= 1e-12 * np.max(np.abs(of))
     x = rng.standard_normal(grid.neq)
     y64 = ctx.spmv(x)
-    for v in (0, 4, 5, 6):
+    for v in (0, 4, 5, 6, 7):
         assert np.linalg.norm(ctx.spmv_fp32(x, v) - y64) <= 1e-5 * np.linalg.norm(y64), v
     ctx.close()
