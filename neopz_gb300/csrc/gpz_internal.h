@@ -134,6 +134,7 @@ struct Learned {
   DBuf<int32_t> ne_idx;
   DBuf<double> mask, dsq;                    // [neq]
   DBuf<float> mdsq;                          // [neq] mask * dsq
+  DBuf<float> dinv32;                        // [neq] 1 / a_ii in FP32 (the FP32 recurrence of the mixed path)
   DBuf<float> feat;                          // [E] log coefficient
   DBuf<float> params, grad, m1, m2;
   DBuf<float> F;                             // [E][NS][R]

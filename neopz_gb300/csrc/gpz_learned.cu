@@ -394,12 +394,13 @@ __global__ void __launch_bounds__(kT) k_ln_pair_grad(int64_t n, int P, const dou
 }
 __global__ void __launch_bounds__(kT) k_ln_dsq(int64_t n, const double *__restrict__ dinv,
                                                const double *__restrict__ mask, double *__restrict__ dsq,
-                                               float *__restrict__ mdsq) {
+                                               float *__restrict__ mdsq, float *__restrict__ dinv32) {
   for (int64_t i = gthread(); i < n; i += nthread()) {
     const double d = dinv[i];
     const double s = d > 0.0 ? sqrt(d) : 0.0;
     dsq[i] = s;
     mdsq[i] = (float)(mask[i] * s);
+    dinv32[i] = (float)d;
   }
 }
 __global__ void __launch_bounds__(kT) k_ln_axpy(int64_t n, double a, const double *__restrict__ x,
@@ -546,6 +547,7 @@ LnView view_of(Ctx &c) {
   v.ne_idx = L.ne_idx.p;
   v.mdsq = L.mdsq.p;
   v.dinv = c.d_dinv.p;
+  v.dinv32 = L.dinv32.p;
   v.loga = L.params.p + offs_of(L.NS * L.R).a;
   v.t = L.t.p;
   v.E = L.E;
@@ -724,13 +726,20 @@ double loss_and_grad(Ctx &c, bool want_grad) {
 
 }  // namespace
 
+// S = diag^-1/2, m S and the FP32 1 / a_ii of the assembled matrix
+void scaling(Ctx &c) {
+  Learned &L = c.ln;
+  L.dinv32.alloc(std::max<int64_t>(c.neq, 1));
+  k_ln_dsq<<<grid_t(c.neq), kT, 0, c.stream>>>(c.neq, c.d_dinv.p, L.mask.p, L.dsq.p, L.mdsq.p, L.dinv32.p);
+  c.launches++;
+}
+
 void learned_prepare(Ctx &c) {
   Learned &L = c.ln;
   GPZ_REQUIRE(L.ready && L.have_params, GPZ_E_NOT_READY, "learned preconditioner not initialised");
   GPZ_REQUIRE(c.have_matrix, GPZ_E_NOT_READY, "not assembled");
   refresh_features(c);
-  k_ln_dsq<<<grid_t(c.neq), kT, 0, c.stream>>>(c.neq, c.d_dinv.p, L.mask.p, L.dsq.p, L.mdsq.p);
-  c.launches++;
+  scaling(c);
   forward(c);
   const int64_t nf = L.E * L.NS * L.R;
   L.F16.alloc(std::max<int64_t>(nf, 1));
@@ -826,7 +835,7 @@ int gpz_learned_collect(gpz_ctx *ctx, int npairs, double tol, int64_t max_iter, 
                                                                     L.pe.p + (size_t)j * c.neq);
     GPZ_CUDA_TRY(cudaGetLastError());
     gpz::refresh_features(c);
-    gpz::k_ln_dsq<<<gpz::grid_t(c.neq), gpz::kT, 0, c.stream>>>(c.neq, c.d_dinv.p, L.mask.p, L.dsq.p, L.mdsq.p);
+    gpz::scaling(c);
     gpz::pair_norms(c);
     GPZ_CUDA_TRY(cudaStreamSynchronize(c.stream));
     if (cg_iterations) *cg_iterations = its;
@@ -845,7 +854,7 @@ int gpz_learned_set_pairs(gpz_ctx *ctx, int npairs, const double *r, const doubl
     GPZ_CUDA_TRY(cudaMemcpyAsync(L.pr.p, r, bytes, cudaMemcpyHostToDevice, c.stream));
     GPZ_CUDA_TRY(cudaMemcpyAsync(L.pe.p, e, bytes, cudaMemcpyHostToDevice, c.stream));
     gpz::refresh_features(c);
-    gpz::k_ln_dsq<<<gpz::grid_t(c.neq), gpz::kT, 0, c.stream>>>(c.neq, c.d_dinv.p, L.mask.p, L.dsq.p, L.mdsq.p);
+    gpz::scaling(c);
     gpz::pair_norms(c);
     GPZ_CUDA_TRY(cudaStreamSynchronize(c.stream));
     return GPZ_OK;

@@ -29,6 +29,7 @@ struct LnView {
   const int32_t *ne_idx;  // e * NS + local
   const float *mdsq;      // [neq] m_i S_i (0 on penalty-Dirichlet equations)
   const double *dinv;     // [neq] 1 / a_ii
+  const float *dinv32;    // the same in FP32
   const float *loga;      // log of the learned scale of the Jacobi part (one parameter)
   float *t;               // [E][R] F_e^T Q_e (m .* u)
   int64_t E, n;

@@ -1397,14 +1397,14 @@ __global__ void __launch_bounds__(kThreads) k_lfb_update(float *__restrict__ dx,
                                                          int qpad, int64_t n, Red R) {
   if (!active(R.iscal)) return;
   const float alpha = (float)R.scal[S_ALPHA];
-  double rr = 0.0;
+  KSum rr;  // compensated FP32 partial sums: GB300's FP64 rate would bound this kernel
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
     dx[i] = fmaf(alpha, p32[pidx(i, 1)], dx[i]);
     const float ri = fmaf(-alpha, q32[pidx(i, qpad)], r32[i]);
     r32[i] = ri;
-    rr += (double)ri * ri;
+    rr.add(ri * ri);
   }
-  double v[1] = {rr}, tot[1];
+  double v[1] = {rr.get()}, tot[1];
   if (grid_reduce<1>(v, R, tot) && threadIdx.x == 0) {
     double *s = R.scal;
     int64_t *is = R.iscal;
@@ -1426,33 +1426,35 @@ __global__ void __launch_bounds__(kThreads) k_lfb_update(float *__restrict__ dx,
 // fallback; after a replacement (I_UPDATE == 2) r is the fresh FP64 residual
 // and r32 is refreshed from it
 __global__ void __launch_bounds__(kThreads) k_lfb_z(LnView L, const double *__restrict__ r64, float *__restrict__ r32,
-                                                    const float *__restrict__ q32, int qpad,
-                                                    const double *__restrict__ dinv, float *__restrict__ z32, Red R) {
+                                                    const float *__restrict__ q32, int qpad, float *__restrict__ z32,
+                                                    Red R) {
   if (!active(R.iscal)) return;
   const bool first = R.iscal[I_IT] == 0;
   const bool fresh = R.iscal[I_UPDATE] == 2;
-  const double alpha = exp((double)*L.loga);
-  double zr = 0.0, zq = 0.0, jr = 0.0, jq = 0.0;
+  const float alpha = expf(*L.loga);
+  // FP32 arithmetic, compensated FP32 partial dots (FP64 across threads and CTAs)
+  KSum zr, zq, jr, jq;
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < L.n; i += (int64_t)gridDim.x * blockDim.x) {
-    double ri;
+    float ri;
     if (fresh) {
-      ri = r64[i];
-      r32[i] = (float)ri;
+      ri = (float)r64[i];
+      r32[i] = ri;
     } else {
-      ri = (double)r32[i];
+      ri = r32[i];
     }
-    const double zi = (double)(float)(alpha * dinv[i] * ri + (double)ln_node_corr_t<true>(L, i));
-    const double ji = dinv[i] * ri;
-    z32[i] = (float)zi;
-    zr += zi * ri;
-    jr += ji * ri;
+    const float di = L.dinv32[i];
+    const float zi = fmaf(alpha * di, ri, ln_node_corr_t<true>(L, i));
+    const float ji = di * ri;
+    z32[i] = zi;
+    zr.add(zi * ri);
+    jr.add(ji * ri);
     if (!first) {
-      const double qi = (double)q32[pidx(i, qpad)];
-      zq += zi * qi;
-      jq += ji * qi;
+      const float qi = q32[pidx(i, qpad)];
+      zq.add(zi * qi);
+      jq.add(ji * qi);
     }
   }
-  double v[4] = {zr, zq, jr, jq}, tot[4];
+  double v[4] = {zr.get(), zq.get(), jr.get(), jq.get()}, tot[4];
   if (grid_reduce<4>(v, R, tot) && threadIdx.x == 0) {
     double *s = R.scal;
     int64_t *is = R.iscal;
@@ -1466,14 +1468,14 @@ __global__ void __launch_bounds__(kThreads) k_lfb_z(LnView L, const double *__re
 }
 
 __global__ void __launch_bounds__(kThreads) k_lfb_p(const float *__restrict__ z32, const float *__restrict__ r32,
-                                                    const double *__restrict__ dinv, float *__restrict__ p32,
+                                                    const float *__restrict__ dinv32, float *__restrict__ p32,
                                                     float *__restrict__ q32, int qpad, int qzero, int64_t n, Red R) {
   if (!active(R.iscal)) return;
   const bool jac = R.iscal[I_RESTART] != 0;
   const bool first = R.iscal[I_IT] == 0;
   const float beta = (float)R.scal[S_BETA];
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
-    const float zi = jac ? (float)(dinv[i] * (double)r32[i]) : z32[i];
+    const float zi = jac ? dinv32[i] * r32[i] : z32[i];
     const int64_t k = pidx(i, 1);
     p32[k] = first ? zi : fmaf(beta, p32[k], zi);
     if (qzero) q32[pidx(i, qpad)] = 0.f;
@@ -2078,8 +2080,8 @@ int solve_learned(Ctx &c, const gpz_solver_opts &o, gpz_solve_report &rep, bool 
       GPZ_TPR_SWITCH(tpr, (k_reliable<T><<<wave(k_reliable<T>), kThreads, 0, s>>>(c.d_ia.p, c.d_ja.p, c.d_a.p,
                                                                                     w.x.p, w.b.p, w.r.p, c.neq, R)));
       k_fcg_t<<<wave(k_fcg_t), kThreads, 0, s>>>(L, w.r.p, w.r32.p, R);
-      k_lfb_z<<<wave(k_lfb_z), kThreads, 0, s>>>(L, w.r.p, w.r32.p, w.q32.p, qpad, c.d_dinv.p, w.z32.p, R);
-      k_lfb_p<<<wave(k_lfb_p), kThreads, 0, s>>>(w.z32.p, w.r32.p, c.d_dinv.p, w.pm.p, w.q32.p, qpad, qpad, c.neq,
+      k_lfb_z<<<wave(k_lfb_z), kThreads, 0, s>>>(L, w.r.p, w.r32.p, w.q32.p, qpad, w.z32.p, R);
+      k_lfb_p<<<wave(k_lfb_p), kThreads, 0, s>>>(w.z32.p, w.r32.p, L.dinv32, w.pm.p, w.q32.p, qpad, qpad, c.neq,
                                                  R);
       c.launches += 6;
       return;
@@ -2121,8 +2123,8 @@ int solve_learned(Ctx &c, const gpz_solver_opts &o, gpz_solve_report &rep, bool 
                                                                                w.b.p, w.r.p, c.neq, from_current, R)));
     k_fcg_t<<<wave(k_fcg_t), kThreads, 0, s>>>(L, w.r.p, w.r32.p, R);  // k_cg_init leaves I_UPDATE = 2: FP64 r
     if (blk) {
-      k_lfb_z<<<wave(k_lfb_z), kThreads, 0, s>>>(L, w.r.p, w.r32.p, w.q32.p, qpad, c.d_dinv.p, w.z32.p, R);
-      k_lfb_p<<<wave(k_lfb_p), kThreads, 0, s>>>(w.z32.p, w.r32.p, c.d_dinv.p, w.pm.p, w.q32.p, qpad, qpad, c.neq,
+      k_lfb_z<<<wave(k_lfb_z), kThreads, 0, s>>>(L, w.r.p, w.r32.p, w.q32.p, qpad, w.z32.p, R);
+      k_lfb_p<<<wave(k_lfb_p), kThreads, 0, s>>>(w.z32.p, w.r32.p, L.dinv32, w.pm.p, w.q32.p, qpad, qpad, c.neq,
                                                  R);
     } else {
       k_fcg_z<<<wave(k_fcg_z), kThreads, 0, s>>>(L, w.r.p, w.q.p, c.d_dinv.p, w.z.p, R);
