@@ -232,17 +232,26 @@ def run_gpu(args):
     nbrow = neq // 3
     chosen = tune.get("chosen", "block_csr")
     mf_flops = None
-    if chosen == "matrix_free_elements":
-        # element records (corners 96 B, block rows 108 B, lambda/mu 8 B), penalty-face records (48 + 36 B),
+    matfree = chosen in ("matrix_free_elements", "matrix_free_sum_factorised", "matrix_free_tcgen05_3xtf32")
+    if matfree:
+        # element records (corners 96 B, block rows 108 B, lambda/mu 8 B, affine geometry 40 B), penalty-face
+        # records (48 + 36 B),
         # p read once and q accumulated once (16 B per block row each)
         nface = (n + 0) * (n + 0)
         nblk = 0
-        kern = ("k_mf_hex27: matrix-free Q2 elasticity, one warp per element (CUDA-core FP32; records + one "
-                "pass of p and q are its HBM bytes)")
         l2_atomics = 27 * nvol + 9 * nface
-        # FLOPs per element: per point, grad(u) from 27 shapes (2 x 243), geometry ~110, stress and the two
-        # Jacobian products ~60 + 2 x 27; per shape, the 27-point back-projection (2 x 27 x 9)
-        mf_flops = nvol * (27 * (2 * 243 + 110 + 60 + 2 * 27) + 27 * 2 * 27 * 9) + nface * 2 * 9 * 9 * 6
+        if chosen == "matrix_free_sum_factorised":
+            kern = ("k_mf_hex27_sf: matrix-free Q2 elasticity, sum-factorised on Lagrange nodal values, one warp per "
+                    "element (CUDA-core FP32; records + one pass of p and q are its HBM bytes)")
+            # FLOPs per element: Phi and Phi^T (2 x 2 x 125 x 3), the 1D contractions forward and back
+            # (2 x 2 x 8 x 81 x 3), per point the Jacobian products and the stress (27 x (2 x 2 x 27 + 30))
+            mf_flops = nvol * (2 * 2 * 125 * 3 + 2 * 2 * 8 * 81 * 3 + 27 * (2 * 2 * 27 + 30)) + nface * 2 * 9 * 9 * 6
+        else:
+            kern = ("k_mf_hex27" + ("_tc" if chosen.endswith("3xtf32") else "") + ": matrix-free Q2 elasticity, one "
+                    "warp per element (records + one pass of p and q are its HBM bytes)")
+            # FLOPs per element: per point, grad(u) from 27 shapes (2 x 243), geometry ~110, stress and the two
+            # Jacobian products ~60 + 2 x 27; per shape, the 27-point back-projection (2 x 27 x 9)
+            mf_flops = nvol * (27 * (2 * 243 + 110 + 60 + 2 * 27) + 27 * 2 * 27 * 9) + nface * 2 * 9 * 9 * 6
     elif chosen == "upper_blocks_float4_atomics":
         nblk = tune["blocks_upper"]
         kern = "k_mx_sym3: upper 3x3 blocks (36 B values + 4 B column), transposed products as float4 atomics in L2"
@@ -253,8 +262,8 @@ def run_gpu(args):
         l2_atomics = 0
     # values + columns + block-row pointers + p (16 B per block row, read once) + q (written once)
     bytes32 = nblk * (36 + 4) + (nbrow + 1) * 8 + nbrow * 16 + nbrow * 16
-    if chosen == "matrix_free_elements":
-        bytes32 = nvol * (96 + 108 + 8) + nface * (48 + 36) + nbrow * 16 + nbrow * 16
+    if matfree:
+        bytes32 = nvol * (96 + 108 + 8 + 40) + nface * (48 + 36) + nbrow * 16 + nbrow * 16
     bytes64 = nnz * (8 + 4) + (neq + 1) * 8 + neq * 8 + neq * 8 + neq * 8
     pk = peaks()
     hbm = pk.get("hbm_gbs", 6800.0)
