@@ -52,6 +52,7 @@ def parse():
     ap.add_argument("--no-learned", action="store_true", help="skip the learned-preconditioner (2D Darcy) leg")
     ap.add_argument("--no-hp", action="store_true", help="skip the hp (uneven-order) assembly leg")
     ap.add_argument("--hp-n", type=int, default=40, help="hexes per direction of the hp leg")
+    ap.add_argument("--no-poisson3d", action="store_true", help="skip the 3D scalar (64^3 Q2 Darcy) leg")
     ap.add_argument("--path", default="learned", choices=["learned", "mixed"],
                     help="solver of the timed step: learned + mixed flexible PCG, or mixed block-Jacobi CG")
     return ap.parse_args()
@@ -362,6 +363,8 @@ def run_gpu(args):
         out["learned_darcy2d"] = learned_leg(gpz, dev)
     if rank == 0 and not args.no_hp:
         out["hp_elasticity"] = hp_leg(gpz, dev, args.hp_n)
+    if rank == 0 and not args.no_poisson3d:
+        out["poisson3d"] = poisson3d_leg(gpz, dev)
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         out["cpu_baseline"] = cpu_baseline(fp64["iterations"], n)
     if rank == 0:
@@ -394,6 +397,30 @@ def hp_leg(gpz, dev, n=40):
             "elements_per_s": grid.nel / (ms / 1e3), "batching": rep,
             "mixed_cg": {"iterations": sol["iterations"], "true_resid": sol["true_resid"], "seconds": sol["seconds"],
                          "rc": sol["rc"]}}
+
+
+def poisson3d_leg(gpz, dev, n=64):
+    """The 3D scalar workload: -div(k grad u) = 1 on the unit cube, 64^3 Q2 hexes (2,146,689 equations),
+    k lognormal(sigma=1) per element (seed 1), u = 0 on the boundary: FP64 assembly, then the mixed CG (FP32
+    CSR values, Jacobi) and the FP64 Jacobi-PCG, both to a true FP64 residual 1e-8."""
+    k = gpz.lognormal(n ** 3, 1.0, 1)
+    grid = gpz.darcy(3, n, 2, k)
+    ctx = gpz.Context(dev)
+    ctx.upload_mesh(grid)
+    nnz = ctx.build_pattern(True)
+    ctx.assemble()
+    ms = ctx.time_kernel(gpz.GPZ_KERNEL_ASSEMBLE, 3)
+    f64 = ctx.solve(tol=TOL, max_iter=200000, check_every=64, want_x=False)
+    ctx.assemble(gpz.GPZ_PREC_MIXED)
+    mx = ctx.solve(solver=gpz.GPZ_SOLVER_MIXED_CG, tol=TOL, max_iter=200000, reliable_delta=1e-2, check_every=64,
+                   want_x=False)
+    ctx.close()
+    return {"workload": f"3D Darcy/Poisson {n}^3 hex Q2, k lognormal(sigma=1) seed 1, u = 0 on the boundary (penalty)",
+            "neq": grid.neq, "nnz_upper": nnz, "assembly_fp64_s": ms / 1e3, "volume_elements_per_s": n ** 3 / (ms / 1e3),
+            "fp64_jacobi_pcg": {"iterations": f64["iterations"], "seconds": f64["seconds"],
+                                "true_resid": f64["true_resid"]},
+            "mixed_cg": {"iterations": mx["iterations"], "seconds": mx["seconds"], "true_resid": mx["true_resid"],
+                         "speedup_vs_fp64_jacobi_pcg": f64["seconds"] / mx["seconds"] if mx["seconds"] else None}}
 
 
 def learned_leg(gpz, dev, n=256, seeds=(10000, 10001, 10002)):

@@ -165,3 +165,20 @@ def test_learned_elasticity_weights_gain_and_mixed_path(g):
         assert mx["iterations"] <= 1.1 * lrn["iterations"], (s, mx["iterations"], lrn["iterations"])
         assert np.linalg.norm(mx["x"] - ref["x"]) <= 1e-5 * np.linalg.norm(ref["x"])
     ctx.close()
+
+
+def test_learned_mixed_elasticity_falls_back(g):
+    """The FP32 learned + mixed path of 3-state problems keeps the Jacobi fallback: with a broken network every
+    iteration falls back and the solve still reaches the true residual."""
+    n = 6
+    grid = g.elasticity3d(n, 2, E=np.exp(np.random.default_rng(4).standard_normal(n ** 3)))
+    ctx = _ctx(g, grid)
+    npar = ctx.learned_init(rank=8, seed=0)
+    ctx.set_learned_params(np.full(npar, np.nan, np.float32))
+    ctx.assemble(g.GPZ_PREC_MIXED)
+    jac = ctx.solve(tol=1e-8)
+    mx = ctx.solve(solver=g.GPZ_SOLVER_LEARNED_MIXED_FCG, tol=1e-8, reliable_delta=1e-2)
+    assert mx["rc"] == 0 and mx["true_resid"] <= 1e-8
+    assert mx["restarts"] >= mx["iterations"] - 1  # every application fell back
+    assert np.linalg.norm(mx["x"] - jac["x"]) <= 1e-5 * np.linalg.norm(jac["x"])
+    ctx.close()
