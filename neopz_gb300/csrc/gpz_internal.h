@@ -130,8 +130,9 @@ struct Learned {
   DBuf<int64_t> ce_ptr;                      // connect -> volume elements
   DBuf<int32_t> ce_idx;
   DBuf<int32_t> dest;                        // [E][NS]
-  DBuf<int64_t> ne_ptr;                      // equation -> (element, local)
+  DBuf<int64_t> ne_ptr;                      // equation -> (element, local), built when first needed
   DBuf<int32_t> ne_idx;
+  bool have_ne = false;
   DBuf<double> mask, dsq;                    // [neq]
   DBuf<float> mdsq;                          // [neq] mask * dsq
   DBuf<float> dinv32;                        // [neq] 1 / a_ii in FP32 (the FP32 recurrence of the mixed path)
@@ -296,7 +297,8 @@ int collect_cg_pairs(Ctx &c, int npairs, double tol, int64_t max_iter, double *R
 bool matfree_build(Ctx &c);
 void matfree_spmv(Ctx &c, cudaStream_t s, int mode);  // 0 CUDA cores, 1 tcgen05, 2 sum-factorised
 // learned.cu
-void learned_prepare(Ctx &c);                // features, scaling and factors F for the assembled system
+void learned_prepare(Ctx &c);
+void ensure_node_incidence(Ctx &c);                // features, scaling and factors F for the assembled system
 // scan.cu
 void exclusive_scan_i64(const int64_t *in, int64_t *out, int64_t n, cudaStream_t s, Ctx &c);
 void check_device_flag(Ctx &c, const char *where);

@@ -440,6 +440,7 @@ void setup_mesh(Ctx &c, int R) {
   const int ns = sides_of(vtype);
   const int64_t E = (int64_t)L.h_vel.size();
   std::vector<int32_t> ec((size_t)E * ns), dest;
+  dest.reserve((size_t)E * 3 * ns);
   int NS = -1;
   for (int64_t k = 0; k < E; k++) {
     const int64_t e = L.h_vel[k];
@@ -470,26 +471,22 @@ void setup_mesh(Ctx &c, int R) {
       for (int j = 0; j < c.h_block_size[cn]; j++) mask[c.h_block_pos[cn] + j] = 0.0;
     }
   }
-  // connect -> volume elements, equation -> (element, local)
-  std::vector<int64_t> ce_ptr(c.nconnects + 1, 0), ne_ptr(c.neq + 1, 0);
+  // connect -> volume elements
+  std::vector<int64_t> ce_ptr(c.nconnects + 1, 0);
   for (int64_t k = 0; k < E * ns; k++) ce_ptr[ec[k] + 1]++;
-  for (int64_t k = 0; k < E * NS; k++) ne_ptr[dest[k] + 1]++;
   for (int64_t i = 0; i < c.nconnects; i++) ce_ptr[i + 1] += ce_ptr[i];
-  for (int64_t i = 0; i < c.neq; i++) ne_ptr[i + 1] += ne_ptr[i];
-  std::vector<int32_t> ce_idx(ce_ptr.back()), ne_idx(ne_ptr.back());
+  std::vector<int32_t> ce_idx(ce_ptr.back());
   {
-    std::vector<int64_t> f(ce_ptr.begin(), ce_ptr.end() - 1), g(ne_ptr.begin(), ne_ptr.end() - 1);
+    std::vector<int64_t> f(ce_ptr.begin(), ce_ptr.end() - 1);
     for (int64_t k = 0; k < E; k++)
       for (int s = 0; s < ns; s++) ce_idx[f[ec[k * ns + s]]++] = (int32_t)k;
-    for (int64_t k = 0; k < E * NS; k++) ne_idx[g[dest[k]]++] = (int32_t)k;
   }
   cudaStream_t st = c.stream;
   L.ec.upload(ec.data(), ec.size(), st);
   L.ce_ptr.upload(ce_ptr.data(), ce_ptr.size(), st);
   L.ce_idx.upload(ce_idx.data(), std::max<size_t>(ce_idx.size(), 1), st);
   L.dest.upload(dest.data(), dest.size(), st);
-  L.ne_ptr.upload(ne_ptr.data(), ne_ptr.size(), st);
-  L.ne_idx.upload(ne_idx.data(), std::max<size_t>(ne_idx.size(), 1), st);
+  L.have_ne = false;
   L.mask.upload(mask.data(), mask.size(), st);
   L.dsq.alloc(std::max<int64_t>(c.neq, 1));
   L.mdsq.alloc(std::max<int64_t>(c.neq, 1));
@@ -510,6 +507,7 @@ void setup_mesh(Ctx &c, int R) {
   L.nparams = o.total;
   L.ready = true;
   GPZ_CUDA_TRY(cudaStreamSynchronize(st));
+  ensure_node_incidence(c);
 }
 
 void init_params(Ctx &c, uint64_t seed) {
@@ -726,6 +724,67 @@ double loss_and_grad(Ctx &c, bool want_grad) {
 
 }  // namespace
 
+// equation -> (element, local) lists of the gather form of the correction,
+// built on the device from the connect -> element lists: the m elements of a
+// connect's list (in element order) give each of its equations m incidences,
+// in the same order.
+namespace {
+__global__ void k_ln_ne_count(int64_t nconn, const int64_t *__restrict__ ce_ptr, const int32_t *__restrict__ bsize,
+                              int64_t *__restrict__ cnt) {
+  const int64_t cn = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (cn < nconn) cnt[cn] = (ce_ptr[cn + 1] - ce_ptr[cn]) * (int64_t)bsize[cn];
+}
+__global__ void k_ln_ne_fill(int64_t nconn, int ns, int NS, const int64_t *__restrict__ ce_ptr,
+                             const int32_t *__restrict__ ce_idx, const int32_t *__restrict__ ec,
+                             const int64_t *__restrict__ bpos, const int32_t *__restrict__ bsize,
+                             const int64_t *__restrict__ base, int64_t *__restrict__ ne_ptr,
+                             int32_t *__restrict__ ne_idx, int *__restrict__ err) {
+  const int64_t cn = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (cn >= nconn) return;
+  const int64_t m = ce_ptr[cn + 1] - ce_ptr[cn];
+  const int bs = bsize[cn];
+  for (int j = 0; j < bs; j++) ne_ptr[bpos[cn] + j] = base[cn] + j * m;
+  for (int64_t r = 0; r < m; r++) {
+    const int32_t k = ce_idx[ce_ptr[cn] + r];
+    int off = 0, s = 0;
+    for (; s < ns; s++) {
+      const int32_t cs = ec[(int64_t)k * ns + s];
+      if (cs == cn) break;
+      off += bsize[cs];
+    }
+    if (s == ns || off + bs > NS) {
+      atomicOr(err, 64);
+      continue;
+    }
+    for (int j = 0; j < bs; j++) ne_idx[base[cn] + j * m + r] = (int32_t)((int64_t)k * NS + off + j);
+  }
+}
+}  // namespace
+
+void ensure_node_incidence(Ctx &c) {
+  Learned &L = c.ln;
+  if (L.have_ne) return;
+  cudaStream_t st = c.stream;
+  DBuf<int64_t> cnt, base;
+  cnt.alloc(c.nconnects + 1);
+  cnt.zero(st);
+  base.alloc(c.nconnects + 1);
+  k_ln_ne_count<<<grid_for(c.nconnects, 256), 256, 0, st>>>(c.nconnects, L.ce_ptr.p, c.d_block_size.p, cnt.p);
+  exclusive_scan_i64(cnt.p, base.p, c.nconnects + 1, st, c);
+  L.ne_ptr.alloc(c.neq + 1);
+  L.ne_idx.alloc(std::max<int64_t>(L.E * L.NS, 1));
+  k_ln_ne_fill<<<grid_for(c.nconnects, 256), 256, 0, st>>>(c.nconnects, L.nsides, L.NS, L.ce_ptr.p, L.ce_idx.p,
+                                                           L.ec.p, c.d_block_pos.p, c.d_block_size.p, base.p,
+                                                           L.ne_ptr.p, L.ne_idx.p, c.d_err.p);
+  c.launches += 2;
+  GPZ_CUDA_TRY(cudaGetLastError());
+  // ne_ptr[neq] = the total number of incidences
+  GPZ_CUDA_TRY(cudaMemcpyAsync(L.ne_ptr.p + c.neq, base.p + c.nconnects, sizeof(int64_t), cudaMemcpyDeviceToDevice, st));
+  GPZ_CUDA_TRY(cudaStreamSynchronize(st));
+  check_device_flag(c, "learned node incidence");
+  L.have_ne = true;
+}
+
 // S = diag^-1/2, m S and the FP32 1 / a_ii of the assembled matrix
 void scaling(Ctx &c) {
   Learned &L = c.ln;
@@ -822,6 +881,7 @@ int gpz_learned_collect(gpz_ctx *ctx, int npairs, double tol, int64_t max_iter, 
   return guarded_ln(ctx, [&](Ctx &c) {
     gpz::Learned &L = c.ln;
     GPZ_REQUIRE(L.ready, GPZ_E_NOT_READY, "learned preconditioner not initialised");
+    gpz::ensure_node_incidence(c);
     GPZ_REQUIRE(c.have_matrix, GPZ_E_NOT_READY, "not assembled");
     GPZ_REQUIRE(npairs >= 1 && npairs <= 256 && tol > 0 && max_iter > 0, GPZ_E_INVALID, "arguments");
     gpz::alloc_pairs(c, npairs);
@@ -847,6 +907,7 @@ int gpz_learned_set_pairs(gpz_ctx *ctx, int npairs, const double *r, const doubl
   return guarded_ln(ctx, [&](Ctx &c) {
     gpz::Learned &L = c.ln;
     GPZ_REQUIRE(L.ready, GPZ_E_NOT_READY, "learned preconditioner not initialised");
+    gpz::ensure_node_incidence(c);
     GPZ_REQUIRE(c.have_matrix, GPZ_E_NOT_READY, "not assembled");
     GPZ_REQUIRE(npairs >= 1 && npairs <= 256 && r && e, GPZ_E_INVALID, "arguments");
     gpz::alloc_pairs(c, npairs);
@@ -865,6 +926,7 @@ int gpz_learned_loss_grad(gpz_ctx *ctx, double *loss, float *grad, int64_t n) {
   return guarded_ln(ctx, [&](Ctx &c) {
     GPZ_REQUIRE(c.ln.have_params, GPZ_E_NOT_READY, "learned preconditioner not initialised");
     GPZ_REQUIRE(!grad || n == c.ln.nparams, GPZ_E_INVALID, "parameter count");
+    gpz::ensure_node_incidence(c);
     const double l = gpz::loss_and_grad(c, grad != nullptr);
     if (grad) {
       GPZ_CUDA_TRY(cudaMemcpyAsync(grad, c.ln.grad.p, n * sizeof(float), cudaMemcpyDeviceToHost, c.stream));
@@ -880,6 +942,7 @@ int gpz_learned_train(gpz_ctx *ctx, int steps, double lr, double *loss_first, do
     gpz::Learned &L = c.ln;
     GPZ_REQUIRE(L.have_params, GPZ_E_NOT_READY, "learned preconditioner not initialised");
     GPZ_REQUIRE(steps >= 1 && lr > 0, GPZ_E_INVALID, "arguments");
+    gpz::ensure_node_incidence(c);
     double l0 = 0, l1 = 0;
     const float b1 = 0.9f, b2 = 0.999f;
     for (int s = 0; s < steps; s++) {

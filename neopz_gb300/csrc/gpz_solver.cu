@@ -1668,7 +1668,44 @@ void tune_spmv32(Ctx &c, int only, bool timing) {
     cudaEventElapsedTime(&ms, e0, e1);
     return ms / 5;
   };
-  auto want = [&](int v) { return only < 0 || only == v; };
+  auto want0 = [&](int v) { return only < 0 || only == v; };
+  // The matrix-free operators are timed first (their records are cheap to
+  // build); an assembled layout whose HBM bytes alone, at the device's
+  // theoretical bandwidth, take longer than the best time measured so far
+  // cannot win and is neither built nor timed.
+  double peak_gbs = 0.0;
+  {
+    int dev = 0, clk_khz = 0, bus_bits = 0;
+    GPZ_CUDA_TRY(cudaGetDevice(&dev));
+    cudaDeviceGetAttribute(&clk_khz, cudaDevAttrMemoryClockRate, dev);
+    cudaDeviceGetAttribute(&bus_bits, cudaDevAttrGlobalMemoryBusWidth, dev);
+    peak_gbs = 2.0 * clk_khz * 1e3 * bus_bits / 8.0 / 1e9;
+  }
+  const double nb_full = (double)c.nnz / 9.0, nb_upper = (nb_full + (double)c.nbrow) / 2.0;
+  auto floor_ms = [&](int v) {
+    const double blocks = v == 4 ? nb_upper : nb_full;
+    const double bytes = blocks * 40.0 + (double)(c.nbrow + 1) * 8.0 + (double)c.nbrow * 32.0;
+    return peak_gbs > 0.0 ? bytes / (peak_gbs * 1e9) * 1e3 : 0.0;
+  };
+  float best_mf = -1.f;
+  std::string pruned;
+  if (timing && only < 0 && (want0(5) || want0(6) || want0(7)) && matfree_build(c)) {
+    res.push_back({5, 0, time_it(5, cand[0])});
+    if (c.mf.sf_ready) res.push_back({7, 0, time_it(7, cand[0])});
+    res.push_back({6, 0, time_it(6, cand[0])});
+    check_device_flag(c, "tensor-core matrix-free operator");
+    for (const Res &r : res) best_mf = best_mf < 0.f ? r.ms : std::min(best_mf, r.ms);
+  }
+  auto want = [&](int v) {
+    if (!want0(v)) return false;
+    if (timing && best_mf > 0.f && floor_ms(v) >= best_mf) {
+      const char *nm[5] = {"block_csr", "block_csr_2rows", "sliced_ell", "block_csr_tma_staged",
+                           "upper_blocks_float4_atomics"};
+      pruned += std::string(pruned.empty() ? "" : ", ") + "\"" + nm[v] + "\": " + std::to_string(floor_ms(v));
+      return false;
+    }
+    return true;
+  };
   if (want(0)) res.push_back({0, 0, time_it(0, cand[0])});
   if (want(1)) res.push_back({1, 0, time_it(1, cand[0])});
   if (want(3)) {
@@ -1719,10 +1756,10 @@ void tune_spmv32(Ctx &c, int only, bool timing) {
     GPZ_CUDA_TRY(cudaGetLastError());
     res.push_back({4, 0, time_it(4, cand[0])});
   }
-  if ((want(5) || want(6) || want(7)) && matfree_build(c)) {
-    if (want(5)) res.push_back({5, 0, time_it(5, cand[0])});
-    if (want(7) && c.mf.sf_ready) res.push_back({7, 0, time_it(7, cand[0])});
-    if (want(6)) {
+  if (best_mf < 0.f && (want0(5) || want0(6) || want0(7)) && matfree_build(c)) {
+    if (want0(5)) res.push_back({5, 0, time_it(5, cand[0])});
+    if (want0(7) && c.mf.sf_ready) res.push_back({7, 0, time_it(7, cand[0])});
+    if (want0(6)) {
       res.push_back({6, 0, time_it(6, cand[0])});
       check_device_flag(c, "tensor-core matrix-free operator");
     }
@@ -1759,6 +1796,7 @@ void tune_spmv32(Ctx &c, int only, bool timing) {
   const char *names[8] = {"block_csr", "block_csr_2rows", "sliced_ell", "block_csr_tma_staged",
                           "upper_blocks_float4_atomics", "matrix_free_elements", "matrix_free_tcgen05_3xtf32",
                           "matrix_free_sum_factorised"};
+  if (!pruned.empty()) rep += ", \"pruned_by_byte_floor_ms\": {" + pruned + "}";
   c.tune_report = rep + ", \"chosen\": \"" + names[res[best].v] + "\", \"block_rows\": " + std::to_string(c.nbrow) +
                   ", \"blocks_full\": " + std::to_string(c.nnz / 9) + ", \"blocks_upper\": " + std::to_string(nu) +
                   "}";
@@ -2041,9 +2079,9 @@ int solve_gmres(Ctx &c, const gpz_solver_opts &o, gpz_solve_report &rep) {
 // meets the tolerance) r is replaced by b - A64 x in FP64, and the solve stops
 // only on that true residual.
 int solve_learned(Ctx &c, const gpz_solver_opts &o, gpz_solve_report &rep, bool mixed) {
-  learned_prepare(c);
   if (mixed && (!c.have_a32 || (o.spmv_variant >= 0 && c.have_bsr3 && o.spmv_variant != c.spmv32_variant)))
     make_fp32_copy(c, o.spmv_variant);
+  learned_prepare(c);
   // scalar problems: FP32 CSR (k_lfcg_spmv); 3 states: the mixed CG's FP32
   // operator in the layout the autotuner chose (3x3 blocks or matrix-free)
   const bool blk = mixed && c.have_bsr3;
@@ -2072,6 +2110,10 @@ int solve_learned(Ctx &c, const gpz_solver_opts &o, gpz_solve_report &rep, bool 
   GPZ_CUDA_TRY(cudaEventCreate(&ev1));
   GPZ_CUDA_TRY(cudaEventRecord(ev0, s));
   int64_t per_iter = mixed ? 6 : 5;  // the FP32 operator counts its own launches (measured at capture)
+  auto apply_z32 = [&]() {
+    k_lfb_z<<<wave(k_lfb_z), kThreads, 0, s>>>(L, w.r.p, w.r32.p, w.q32.p, qpad, w.z32.p, R);
+    c.launches++;
+  };
   auto iteration = [&]() {
     if (blk) {
       launch_spmv32(c, v32, c.sell, R, s);
@@ -2080,10 +2122,10 @@ int solve_learned(Ctx &c, const gpz_solver_opts &o, gpz_solve_report &rep, bool 
       GPZ_TPR_SWITCH(tpr, (k_reliable<T><<<wave(k_reliable<T>), kThreads, 0, s>>>(c.d_ia.p, c.d_ja.p, c.d_a.p,
                                                                                     w.x.p, w.b.p, w.r.p, c.neq, R)));
       k_fcg_t<<<wave(k_fcg_t), kThreads, 0, s>>>(L, w.r.p, w.r32.p, R);
-      k_lfb_z<<<wave(k_lfb_z), kThreads, 0, s>>>(L, w.r.p, w.r32.p, w.q32.p, qpad, w.z32.p, R);
+      apply_z32();
       k_lfb_p<<<wave(k_lfb_p), kThreads, 0, s>>>(w.z32.p, w.r32.p, L.dinv32, w.pm.p, w.q32.p, qpad, qpad, c.neq,
                                                  R);
-      c.launches += 6;
+      c.launches += 5;
       return;
     }
     if (mixed) {
@@ -2123,9 +2165,10 @@ int solve_learned(Ctx &c, const gpz_solver_opts &o, gpz_solve_report &rep, bool 
                                                                                w.b.p, w.r.p, c.neq, from_current, R)));
     k_fcg_t<<<wave(k_fcg_t), kThreads, 0, s>>>(L, w.r.p, w.r32.p, R);  // k_cg_init leaves I_UPDATE = 2: FP64 r
     if (blk) {
-      k_lfb_z<<<wave(k_lfb_z), kThreads, 0, s>>>(L, w.r.p, w.r32.p, w.q32.p, qpad, w.z32.p, R);
+      apply_z32();
       k_lfb_p<<<wave(k_lfb_p), kThreads, 0, s>>>(w.z32.p, w.r32.p, L.dinv32, w.pm.p, w.q32.p, qpad, qpad, c.neq,
                                                  R);
+      c.launches -= 1;
     } else {
       k_fcg_z<<<wave(k_fcg_z), kThreads, 0, s>>>(L, w.r.p, w.q.p, c.d_dinv.p, w.z.p, R);
       k_fcg_p<<<wave(k_fcg_p), kThreads, 0, s>>>(w.z.p, w.r.p, c.d_dinv.p, w.p.p, p32, c.neq, R);
