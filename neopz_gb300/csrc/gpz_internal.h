@@ -140,6 +140,7 @@ struct Learned {
   DBuf<float> params, grad, m1, m2;
   DBuf<float> F;                             // [E][NS][R]
   DBuf<uint16_t> F16;                        // F in bfloat16, read by the solves
+  DBuf<uint16_t> F16ne;                      // its rows in incidence (ne_idx) order
   DBuf<float> t;                             // [E][R]
   DBuf<float> act, back, partial;            // activations, backward buffers, outer-product partials
   DBuf<double> red;                          // dot-product partials

@@ -535,11 +535,18 @@ __global__ void __launch_bounds__(kT) k_ln_to_bf16(int64_t n, const float *__res
   for (int64_t i = gthread(); i < n; i += nthread()) h[i] = __bfloat16_as_ushort(__float2bfloat16_rn(F[i]));
 }
 
+// the same rows in incidence order: row k = row ne_idx[k] of the element-ordered copy
+__global__ void __launch_bounds__(kT) k_ln_rows_by_incidence(int64_t n, int R, const int32_t *__restrict__ ne_idx,
+                                                             const uint16_t *__restrict__ h, uint16_t *__restrict__ hne) {
+  for (int64_t k = gthread(); k < n * R; k += nthread()) hne[k] = h[(int64_t)ne_idx[k / R] * R + k % R];
+}
+
 LnView view_of(Ctx &c) {
   Learned &L = c.ln;
   LnView v;
   v.F = L.F.p;
   v.F16 = L.F16.p;
+  v.F16ne = L.F16ne.p;
   v.dest = L.dest.p;
   v.ne_ptr = L.ne_ptr.p;
   v.ne_idx = L.ne_idx.p;
@@ -803,7 +810,10 @@ void learned_prepare(Ctx &c) {
   const int64_t nf = L.E * L.NS * L.R;
   L.F16.alloc(std::max<int64_t>(nf, 1));
   k_ln_to_bf16<<<grid_t(nf), kT, 0, c.stream>>>(nf, L.F.p, L.F16.p);
-  c.launches++;
+  ensure_node_incidence(c);
+  L.F16ne.alloc(std::max<int64_t>(nf, 1));
+  k_ln_rows_by_incidence<<<grid_t(nf), kT, 0, c.stream>>>(L.E * L.NS, L.R, L.ne_idx.p, L.F16.p, L.F16ne.p);
+  c.launches += 2;
   GPZ_CUDA_TRY(cudaGetLastError());
 }
 

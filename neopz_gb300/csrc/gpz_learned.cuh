@@ -24,6 +24,7 @@ namespace gpz {
 struct LnView {
   const float *F;         // [E][NS][R] element factors
   const uint16_t *F16;    // the same rounded to bfloat16 for the solves (half the bytes per application)
+  const uint16_t *F16ne;  // bfloat16 rows in incidence order (row k belongs to incidence k of ne_idx)
   const int32_t *dest;    // [E][NS] element equations
   const int64_t *ne_ptr;  // [neq+1] equation -> (element, local) incidences
   const int32_t *ne_idx;  // e * NS + local
@@ -147,6 +148,28 @@ __device__ __forceinline__ float ln_node_corr_t(const LnView &L, int64_t i) {
   return L.mdsq[i] * c;
 }
 __device__ __forceinline__ float ln_node_corr(const LnView &L, int64_t i) { return ln_node_corr_t<false>(L, i); }
+
+// the same for the solves, from the incidence-ordered bfloat16 rows: the rows of
+// consecutive equations are contiguous, so a warp streams them
+__device__ __forceinline__ float ln_node_corr_ne(const LnView &L, int64_t i) {
+  float c = 0.f;
+  for (int64_t k = L.ne_ptr[i]; k < L.ne_ptr[i + 1]; k++) {
+    const int32_t e = L.ne_idx[k] / L.NS;
+    const uint16_t *h = L.F16ne + (size_t)k * L.R;
+    const float *t = L.t + (size_t)e * L.R;
+    if (L.R == 8) {
+      const uint4 v = *(const uint4 *)h;
+      const float4 t0 = *(const float4 *)t, t1 = *(const float4 *)(t + 4);
+      c += __uint_as_float(v.x << 16) * t0.x + __uint_as_float(v.x & 0xffff0000u) * t0.y +
+           __uint_as_float(v.y << 16) * t0.z + __uint_as_float(v.y & 0xffff0000u) * t0.w +
+           __uint_as_float(v.z << 16) * t1.x + __uint_as_float(v.z & 0xffff0000u) * t1.y +
+           __uint_as_float(v.w << 16) * t1.z + __uint_as_float(v.w & 0xffff0000u) * t1.w;
+    } else {
+      for (int j = 0; j < L.R; j++) c += __uint_as_float((uint32_t)h[j] << 16) * t[j];
+    }
+  }
+  return L.mdsq[i] * c;
+}
 
 // z_i = alpha r_i / a_ii + correction, alpha = exp(loga)
 template <class T>

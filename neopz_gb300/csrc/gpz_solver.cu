@@ -1443,7 +1443,7 @@ __global__ void __launch_bounds__(kThreads) k_lfb_z(LnView L, const double *__re
       ri = r32[i];
     }
     const float di = L.dinv32[i];
-    const float zi = fmaf(alpha * di, ri, ln_node_corr_t<true>(L, i));
+    const float zi = fmaf(alpha * di, ri, ln_node_corr_ne(L, i));
     const float ji = di * ri;
     z32[i] = zi;
     zr.add(zi * ri);
@@ -1452,6 +1452,77 @@ __global__ void __launch_bounds__(kThreads) k_lfb_z(LnView L, const double *__re
       const float qi = q32[pidx(i, qpad)];
       zq.add(zi * qi);
       jq.add(ji * qi);
+    }
+  }
+  double v[4] = {zr.get(), zq.get(), jr.get(), jq.get()}, tot[4];
+  if (grid_reduce<4>(v, R, tot) && threadIdx.x == 0) {
+    double *s = R.scal;
+    int64_t *is = R.iscal;
+    const bool ok = tot[0] > 0.0 && isfinite(tot[0]) && isfinite(tot[1]);
+    is[I_RESTART] = ok ? 0 : 1;
+    if (!ok) is[I_NRESTART] += 1;
+    s[S_RHO] = ok ? tot[0] : tot[2];
+    s[S_BETA] = first ? 0.0 : -(ok ? tot[1] : tot[3]) / s[S_PQ];
+    if (is[I_UPDATE] == 2) is[I_UPDATE] = 0;
+  }
+}
+
+// The same for meshes whose connects all carry 3 equations (Q2 elasticity):
+// one thread per connect; its elements (the connect -> element list, in the
+// order of the incidence lists) and their t_e are loaded once for the three
+// equations, whose incidence-ordered rows sit at ne_ptr[eq] + r.
+__global__ void __launch_bounds__(kThreads) k_lfb_z3(LnView L, const int64_t *__restrict__ ce_ptr,
+                                                     const int32_t *__restrict__ ce_idx,
+                                                     const int64_t *__restrict__ bpos,
+                                                     const int32_t *__restrict__ bsize, int64_t nconn,
+                                                     const double *__restrict__ r64, float *__restrict__ r32,
+                                                     const float *__restrict__ q32, int qpad, float *__restrict__ z32,
+                                                     Red R) {
+  if (!active(R.iscal)) return;
+  const bool first = R.iscal[I_IT] == 0;
+  const bool fresh = R.iscal[I_UPDATE] == 2;
+  const float alpha = expf(*L.loga);
+  KSum zr, zq, jr, jq;
+  for (int64_t cn = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; cn < nconn; cn += (int64_t)gridDim.x * blockDim.x) {
+    if (bsize[cn] != 3) continue;
+    const int64_t eq0 = bpos[cn];
+    const int64_t c0 = ce_ptr[cn], m = ce_ptr[cn + 1] - c0;
+    const int64_t p0 = L.ne_ptr[eq0], p1 = L.ne_ptr[eq0 + 1], p2 = L.ne_ptr[eq0 + 2];
+    float a[3] = {0.f, 0.f, 0.f};
+    for (int64_t r = 0; r < m; r++) {
+      const int32_t e = ce_idx[c0 + r];
+      const float4 t0 = *(const float4 *)(L.t + (size_t)e * 8), t1 = *(const float4 *)(L.t + (size_t)e * 8 + 4);
+      const int64_t pr[3] = {p0 + r, p1 + r, p2 + r};
+#pragma unroll
+      for (int j = 0; j < 3; j++) {
+        const uint4 v = *(const uint4 *)(L.F16ne + (size_t)pr[j] * 8);
+        a[j] += __uint_as_float(v.x << 16) * t0.x + __uint_as_float(v.x & 0xffff0000u) * t0.y +
+                __uint_as_float(v.y << 16) * t0.z + __uint_as_float(v.y & 0xffff0000u) * t0.w +
+                __uint_as_float(v.z << 16) * t1.x + __uint_as_float(v.z & 0xffff0000u) * t1.y +
+                __uint_as_float(v.w << 16) * t1.z + __uint_as_float(v.w & 0xffff0000u) * t1.w;
+      }
+    }
+#pragma unroll
+    for (int j = 0; j < 3; j++) {
+      const int64_t i = eq0 + j;
+      float ri;
+      if (fresh) {
+        ri = (float)r64[i];
+        r32[i] = ri;
+      } else {
+        ri = r32[i];
+      }
+      const float di = L.dinv32[i];
+      const float zi = fmaf(alpha * di, ri, L.mdsq[i] * a[j]);
+      const float ji = di * ri;
+      z32[i] = zi;
+      zr.add(zi * ri);
+      jr.add(ji * ri);
+      if (!first) {
+        const float qi = q32[pidx(i, qpad)];
+        zq.add(zi * qi);
+        jq.add(ji * qi);
+      }
     }
   }
   double v[4] = {zr.get(), zq.get(), jr.get(), jq.get()}, tot[4];
@@ -1490,7 +1561,7 @@ __global__ void __launch_bounds__(kThreads) k_fcg_z(LnView L, const double *__re
   const double alpha = exp((double)*L.loga);
   double zr = 0.0, zq = 0.0, jr = 0.0, jq = 0.0;  // jr, jq: the Jacobi fallback's dots (FP64: its beta)
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < L.n; i += (int64_t)gridDim.x * blockDim.x) {
-    const double zi = alpha * L.dinv[i] * r[i] + (double)ln_node_corr_t<true>(L, i);
+    const double zi = alpha * L.dinv[i] * r[i] + (double)ln_node_corr_ne(L, i);
     const double ri = r[i];
     const double ji = dinv[i] * ri;
     z[i] = zi;
@@ -2110,8 +2181,17 @@ int solve_learned(Ctx &c, const gpz_solver_opts &o, gpz_solve_report &rep, bool 
   GPZ_CUDA_TRY(cudaEventCreate(&ev1));
   GPZ_CUDA_TRY(cudaEventRecord(ev0, s));
   int64_t per_iter = mixed ? 6 : 5;  // the FP32 operator counts its own launches (measured at capture)
+  // connects of 0 or 3 equations and rank 8: the connect-wise z kernel
+  bool by_connect = blk && c.ln.R == 8;
+  for (int64_t cn = 0; cn < c.nconnects && by_connect; cn++)
+    by_connect = c.h_block_size[cn] == 0 || c.h_block_size[cn] == 3;
   auto apply_z32 = [&]() {
-    k_lfb_z<<<wave(k_lfb_z), kThreads, 0, s>>>(L, w.r.p, w.r32.p, w.q32.p, qpad, w.z32.p, R);
+    if (by_connect)
+      k_lfb_z3<<<wave(k_lfb_z3), kThreads, 0, s>>>(L, c.ln.ce_ptr.p, c.ln.ce_idx.p, c.d_block_pos.p,
+                                                   c.d_block_size.p, c.nconnects, w.r.p, w.r32.p, w.q32.p, qpad,
+                                                   w.z32.p, R);
+    else
+      k_lfb_z<<<wave(k_lfb_z), kThreads, 0, s>>>(L, w.r.p, w.r32.p, w.q32.p, qpad, w.z32.p, R);
     c.launches++;
   };
   auto iteration = [&]() {
