@@ -1860,7 +1860,7 @@ void tune_spmv32(Ctx &c, int only, bool timing) {
     rep += std::string(i ? ", " : "") + "\"" + nm + (res[i].v == 2 ? "_w" + std::to_string(res[i].window) : "") +
            "\": " + std::to_string(res[i].ms);
   }
-  int64_t nu = 0;
+  int64_t nu = (c.nnz / 9 + c.nbrow) / 2;  // the block pattern is symmetric with every diagonal block stored
   if (c.d_uptr.p) {
     GPZ_CUDA_TRY(cudaMemcpy(&nu, c.d_uptr.p + c.nbrow, sizeof(int64_t), cudaMemcpyDeviceToHost));
   }
