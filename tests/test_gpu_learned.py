@@ -182,3 +182,22 @@ def test_learned_mixed_elasticity_falls_back(g):
     assert mx["restarts"] >= mx["iterations"] - 1  # every application fell back
     assert np.linalg.norm(mx["x"] - jac["x"]) <= 1e-5 * np.linalg.norm(jac["x"])
     ctx.close()
+
+
+def test_learned_mixed_elasticity_equation_wise_path(g):
+    """Rank 4 (not the connect-wise kernel's rank 8): the equation-wise node correction of the FP32 learned +
+    mixed path reaches the same true residual as the FP64 learned flexible CG with the same network, in at most
+    1.5x its iterations (the FP32 recurrence on the 1e12-penalty rows costs iterations on small meshes), and the
+    solutions agree within 1e-5."""
+    n = 6
+    grid = g.elasticity3d(n, 2, E=np.exp(np.random.default_rng(9).standard_normal(n ** 3)))
+    ctx = _ctx(g, grid)
+    npar = ctx.learned_init(rank=4, seed=3)
+    ctx.set_learned_params((0.05 * np.random.default_rng(1).standard_normal(npar)).astype(np.float32))
+    f64 = ctx.solve(solver=g.GPZ_SOLVER_LEARNED_FCG, tol=1e-8)
+    ctx.assemble(g.GPZ_PREC_MIXED)
+    mx = ctx.solve(solver=g.GPZ_SOLVER_LEARNED_MIXED_FCG, tol=1e-8, reliable_delta=1e-2)
+    assert f64["rc"] == 0 and mx["rc"] == 0 and mx["true_resid"] <= 1e-8
+    assert mx["iterations"] <= 1.5 * f64["iterations"], (mx["iterations"], f64["iterations"])
+    assert np.linalg.norm(mx["x"] - f64["x"]) <= 1e-5 * np.linalg.norm(f64["x"])
+    ctx.close()
