@@ -364,12 +364,21 @@ constexpr int SFI_RP = 0, SFI_CP = 28, SFI_RC = 56, SFI_CR = SFI_RC + kSfMaxNz, 
 // warp-uniform operands, read through the constant cache
 __constant__ float c_sfB[9], c_sfD[9];
 
+// Shared-memory layouts (component s, tensor indices a, b, c of 0..2): each is
+// a position map under which the warp's 27 addresses fall in 27 distinct
+// banks in both stages that access the buffer (the writer's and the reader's
+// lane patterns differ), so no tensor stage has bank conflicts.
+__device__ __forceinline__ int sf_v(int s, int a, int b, int c) { return 3 * s + a + 9 * b + 29 * c; }   // nodal
+__device__ __forceinline__ int sf_t1(int s, int a, int b, int c) { return 9 * s + a + 3 * b + 29 * c; }  // (j1, j2, q3)
+__device__ __forceinline__ int sf_t2(int s, int a, int b, int c) { return 3 * s + a + 27 * b + 9 * c; }  // (j1, q2, q3)
+__device__ __forceinline__ int sf_h(int s, int d, int q) { return 27 * s + 81 * d + q; }
+
 struct SfWarp {
   float4 su[27];   // element coefficients (3 components per shape)
-  float v[81];     // [s][j] nodal values, later the adjoint's nodal output
-  float t1[2][81]; // zeta contractions (B, D): [s][j1 + 3 j2 + 9 q3]
-  float t2[3][81]; // eta contractions (BB, DB, BD): [s][j1 + 3 q2 + 9 q3]
-  float h[9][27];  // [s * 3 + d][q] reference gradients, then the pulled-back stresses
+  float v[85];     // nodal values sf_v, later the adjoint's nodal output
+  float t1[2][85]; // zeta contractions (B, D) sf_t1
+  float t2[3][81]; // eta contractions (BB, DB, BD) sf_t2
+  float h[243];    // reference gradients sf_h(s, d, q), then the pulled-back stresses
   float geo[34];   // corners, then the affine geometry (Jinv, |det J|)
 };
 
@@ -409,10 +418,12 @@ __global__ void __launch_bounds__(kSfThreads, 5) k_mf_hex27_sf(int64_t n, const 
 #pragma unroll
     for (int k = 0; k < kCol; k++) {
       cv[k] = k < ncol ? sf[SF_CV + c0 + k] : 0.f;
-      cr[k / 4] |= (uint32_t)(k < ncol ? si[SFI_CR + c0 + k] : 0) << (8 * (k % 4));
+      const int jn = k < ncol ? si[SFI_CR + c0 + k] : 0;  // node -> its sf_v offset (component 0)
+      cr[k / 4] |= (uint32_t)sf_v(0, jn % 3, (jn / 3) % 3, jn / 9) << (8 * (k % 4));
     }
   }
   const float flong = lane < kNS ? sf[SF_LONG + lane] : 0.f;
+  const int vlane = sf_v(0, lane % 3, (lane / 3) % 3, lane / 9), vlong = sf_v(0, jl % 3, (jl / 3) % 3, jl / 9);
   // stage lanes: component s and pencil p (two tensor indices of 0..2)
   const bool act = lane < 27;
   const int s = act ? lane / 9 : 0, p = lane % 9;
@@ -460,9 +471,9 @@ __global__ void __launch_bounds__(kSfThreads, 5) k_mf_hex27_sf(int64_t n, const 
           a1 = fmaf(rv[k], c.y, a1);
           a2 = fmaf(rv[k], c.z, a2);
         }
-        W.v[lane] = a0;
-        W.v[27 + lane] = a1;
-        W.v[54 + lane] = a2;
+        W.v[vlane] = a0;
+        W.v[vlane + 3] = a1;
+        W.v[vlane + 6] = a2;
       }
       float b0 = flong * u.x, b1 = flong * u.y, b2 = flong * u.z;
       for (int o = 16; o > 0; o >>= 1) {
@@ -471,47 +482,49 @@ __global__ void __launch_bounds__(kSfThreads, 5) k_mf_hex27_sf(int64_t n, const 
         b2 += __shfl_xor_sync(0xffffffffu, b2, o);
       }
       if (lane == 0) {
-        W.v[jl] = b0;
-        W.v[27 + jl] = b1;
-        W.v[54 + jl] = b2;
+        W.v[vlong] = b0;
+        W.v[vlong + 3] = b1;
+        W.v[vlong + 6] = b2;
       }
     }
     __syncwarp();
     // zeta: lane (s, j1 = pa, j2 = pb)
     if (act) {
-      const float x0 = W.v[s * 27 + p], x1 = W.v[s * 27 + p + 9], x2 = W.v[s * 27 + p + 18];
+      const float x0 = W.v[sf_v(s, pa, pb, 0)], x1 = W.v[sf_v(s, pa, pb, 1)], x2 = W.v[sf_v(s, pa, pb, 2)];
 #pragma unroll
       for (int q3 = 0; q3 < 3; q3++) {
-        W.t1[0][s * 27 + p + 9 * q3] = B[q3 * 3] * x0 + B[q3 * 3 + 1] * x1 + B[q3 * 3 + 2] * x2;
-        W.t1[1][s * 27 + p + 9 * q3] = D[q3 * 3] * x0 + D[q3 * 3 + 1] * x1 + D[q3 * 3 + 2] * x2;
+        W.t1[0][sf_t1(s, pa, pb, q3)] = B[q3 * 3] * x0 + B[q3 * 3 + 1] * x1 + B[q3 * 3 + 2] * x2;
+        W.t1[1][sf_t1(s, pa, pb, q3)] = D[q3 * 3] * x0 + D[q3 * 3 + 1] * x1 + D[q3 * 3 + 2] * x2;
       }
     }
     __syncwarp();
     // eta: lane (s, j1 = pa, q3 = pb)
     if (act) {
-      const int b = s * 27 + pa + 9 * pb;
-      const float y0 = W.t1[0][b], y1 = W.t1[0][b + 3], y2 = W.t1[0][b + 6];
-      const float z0 = W.t1[1][b], z1 = W.t1[1][b + 3], z2 = W.t1[1][b + 6];
+      const float y0 = W.t1[0][sf_t1(s, pa, 0, pb)], y1 = W.t1[0][sf_t1(s, pa, 1, pb)],
+                  y2 = W.t1[0][sf_t1(s, pa, 2, pb)];
+      const float z0 = W.t1[1][sf_t1(s, pa, 0, pb)], z1 = W.t1[1][sf_t1(s, pa, 1, pb)],
+                  z2 = W.t1[1][sf_t1(s, pa, 2, pb)];
 #pragma unroll
       for (int q2 = 0; q2 < 3; q2++) {
-        W.t2[0][b + 3 * q2] = B[q2 * 3] * y0 + B[q2 * 3 + 1] * y1 + B[q2 * 3 + 2] * y2;
-        W.t2[1][b + 3 * q2] = D[q2 * 3] * y0 + D[q2 * 3 + 1] * y1 + D[q2 * 3 + 2] * y2;
-        W.t2[2][b + 3 * q2] = B[q2 * 3] * z0 + B[q2 * 3 + 1] * z1 + B[q2 * 3 + 2] * z2;
+        const int o = sf_t2(s, pa, q2, pb);
+        W.t2[0][o] = B[q2 * 3] * y0 + B[q2 * 3 + 1] * y1 + B[q2 * 3 + 2] * y2;
+        W.t2[1][o] = D[q2 * 3] * y0 + D[q2 * 3 + 1] * y1 + D[q2 * 3 + 2] * y2;
+        W.t2[2][o] = B[q2 * 3] * z0 + B[q2 * 3 + 1] * z1 + B[q2 * 3 + 2] * z2;
       }
     }
     __syncwarp();
     // xi: lane (s, q2 = pa, q3 = pb) -> reference gradients at q = q1 + 3 p
     if (act) {
-      const int b = s * 27 + 3 * p;
+      const int b = sf_t2(s, 0, pa, pb);  // + j1
       const float g0 = W.t2[0][b], g1 = W.t2[0][b + 1], g2 = W.t2[0][b + 2];
       const float e0 = W.t2[1][b], e1 = W.t2[1][b + 1], e2 = W.t2[1][b + 2];
       const float f0 = W.t2[2][b], f1 = W.t2[2][b + 1], f2 = W.t2[2][b + 2];
 #pragma unroll
       for (int q1 = 0; q1 < 3; q1++) {
         const int q = q1 + 3 * p;
-        W.h[s * 3 + 0][q] = D[q1 * 3] * g0 + D[q1 * 3 + 1] * g1 + D[q1 * 3 + 2] * g2;
-        W.h[s * 3 + 1][q] = B[q1 * 3] * e0 + B[q1 * 3 + 1] * e1 + B[q1 * 3 + 2] * e2;
-        W.h[s * 3 + 2][q] = B[q1 * 3] * f0 + B[q1 * 3 + 1] * f1 + B[q1 * 3 + 2] * f2;
+        W.h[sf_h(s, 0, q)] = D[q1 * 3] * g0 + D[q1 * 3 + 1] * g1 + D[q1 * 3 + 2] * g2;
+        W.h[sf_h(s, 1, q)] = B[q1 * 3] * e0 + B[q1 * 3 + 1] * e1 + B[q1 * 3 + 2] * e2;
+        W.h[sf_h(s, 2, q)] = B[q1 * 3] * f0 + B[q1 * 3 + 1] * f1 + B[q1 * 3 + 2] * f2;
       }
     }
     __syncwarp();
@@ -549,7 +562,7 @@ __global__ void __launch_bounds__(kSfThreads, 5) k_mf_hex27_sf(int64_t n, const 
 #pragma unroll
       for (int s2 = 0; s2 < 3; s2++)
 #pragma unroll
-        for (int j = 0; j < 3; j++) hh[s2][j] = W.h[s2 * 3 + j][q];
+        for (int j = 0; j < 3; j++) hh[s2][j] = W.h[sf_h(s2, j, q)];
 #pragma unroll
       for (int s2 = 0; s2 < 3; s2++)
 #pragma unroll
@@ -564,18 +577,18 @@ __global__ void __launch_bounds__(kSfThreads, 5) k_mf_hex27_sf(int64_t n, const 
       for (int s2 = 0; s2 < 3; s2++)
 #pragma unroll
         for (int j = 0; j < 3; j++)
-          W.h[s2 * 3 + j][q] = T[s2][0] * ji[j][0] + T[s2][1] * ji[j][1] + T[s2][2] * ji[j][2];
+          W.h[sf_h(s2, j, q)] = T[s2][0] * ji[j][0] + T[s2][1] * ji[j][1] + T[s2][2] * ji[j][2];
     }
     __syncwarp();
     // transposed xi: lane (s, q2 = pa, q3 = pb)
     if (act) {
-      const int b = s * 27 + 3 * p;
+      const int b = sf_t2(s, 0, pa, pb);  // + j1
       float g[3], e[3], f[3];
 #pragma unroll
       for (int q1 = 0; q1 < 3; q1++) {
-        g[q1] = W.h[s * 3 + 0][q1 + 3 * p];
-        e[q1] = W.h[s * 3 + 1][q1 + 3 * p];
-        f[q1] = W.h[s * 3 + 2][q1 + 3 * p];
+        g[q1] = W.h[sf_h(s, 0, q1 + 3 * p)];
+        e[q1] = W.h[sf_h(s, 1, q1 + 3 * p)];
+        f[q1] = W.h[sf_h(s, 2, q1 + 3 * p)];
       }
 #pragma unroll
       for (int j1 = 0; j1 < 3; j1++) {
@@ -587,19 +600,20 @@ __global__ void __launch_bounds__(kSfThreads, 5) k_mf_hex27_sf(int64_t n, const 
     __syncwarp();
     // transposed eta: lane (s, j1 = pa, q3 = pb)
     if (act) {
-      const int b = s * 27 + pa + 9 * pb;
       float g[3], e[3], f[3];
 #pragma unroll
       for (int q2 = 0; q2 < 3; q2++) {
-        g[q2] = W.t2[0][b + 3 * q2];
-        e[q2] = W.t2[1][b + 3 * q2];
-        f[q2] = W.t2[2][b + 3 * q2];
+        const int o = sf_t2(s, pa, q2, pb);
+        g[q2] = W.t2[0][o];
+        e[q2] = W.t2[1][o];
+        f[q2] = W.t2[2][o];
       }
 #pragma unroll
       for (int j2 = 0; j2 < 3; j2++) {
-        W.t1[0][b + 3 * j2] = B[j2] * g[0] + B[3 + j2] * g[1] + B[6 + j2] * g[2] + D[j2] * e[0] + D[3 + j2] * e[1] +
-                              D[6 + j2] * e[2];
-        W.t1[1][b + 3 * j2] = B[j2] * f[0] + B[3 + j2] * f[1] + B[6 + j2] * f[2];
+        const int o = sf_t1(s, pa, j2, pb);
+        W.t1[0][o] = B[j2] * g[0] + B[3 + j2] * g[1] + B[6 + j2] * g[2] + D[j2] * e[0] + D[3 + j2] * e[1] +
+                     D[6 + j2] * e[2];
+        W.t1[1][o] = B[j2] * f[0] + B[3 + j2] * f[1] + B[6 + j2] * f[2];
       }
     }
     __syncwarp();
@@ -608,12 +622,12 @@ __global__ void __launch_bounds__(kSfThreads, 5) k_mf_hex27_sf(int64_t n, const 
       float g[3], f[3];
 #pragma unroll
       for (int q3 = 0; q3 < 3; q3++) {
-        g[q3] = W.t1[0][s * 27 + p + 9 * q3];
-        f[q3] = W.t1[1][s * 27 + p + 9 * q3];
+        g[q3] = W.t1[0][sf_t1(s, pa, pb, q3)];
+        f[q3] = W.t1[1][sf_t1(s, pa, pb, q3)];
       }
 #pragma unroll
       for (int j3 = 0; j3 < 3; j3++)
-        W.v[s * 27 + p + 9 * j3] = B[j3] * g[0] + B[3 + j3] * g[1] + B[6 + j3] * g[2] + D[j3] * f[0] +
+        W.v[sf_v(s, pa, pb, j3)] = B[j3] * g[0] + B[3 + j3] * g[1] + B[6 + j3] * g[2] + D[j3] * f[0] +
                                    D[3 + j3] * f[1] + D[6 + j3] * f[2];
     }
     __syncwarp();
@@ -623,10 +637,10 @@ __global__ void __launch_bounds__(kSfThreads, 5) k_mf_hex27_sf(int64_t n, const 
 #pragma unroll
       for (int k = 0; k < kCol; k++) {
         if (k >= ncol) break;
-        const int j = (cr[k / 4] >> (8 * (k % 4))) & 0xffu;
-        y0 = fmaf(cv[k], W.v[j], y0);
-        y1 = fmaf(cv[k], W.v[27 + j], y1);
-        y2 = fmaf(cv[k], W.v[54 + j], y2);
+        const int o = (cr[k / 4] >> (8 * (k % 4))) & 0xffu;  // sf_v offset of the node, component 0
+        y0 = fmaf(cv[k], W.v[o], y0);
+        y1 = fmaf(cv[k], W.v[o + 3], y1);
+        y2 = fmaf(cv[k], W.v[o + 6], y2);
       }
       en.add(y0 * u.x + y1 * u.y + y2 * u.z);
       atomicAdd(&q4[row_i], make_float4(y0, y1, y2, 0.f));
