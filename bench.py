@@ -53,6 +53,8 @@ def parse():
     ap.add_argument("--no-hp", action="store_true", help="skip the hp (uneven-order) assembly leg")
     ap.add_argument("--hp-n", type=int, default=40, help="hexes per direction of the hp leg")
     ap.add_argument("--no-poisson3d", action="store_true", help="skip the 3D scalar (64^3 Q2 Darcy) leg")
+    ap.add_argument("--spmv-variant", type=int, default=-1,
+                    help="FP32 operator of the mixed solves: -1 autotuned, else the gpz_solver_opts spmv_variant")
     ap.add_argument("--path", default="learned", choices=["learned", "mixed"],
                     help="solver of the timed step: learned + mixed flexible PCG, or mixed block-Jacobi CG")
     return ap.parse_args()
@@ -166,10 +168,11 @@ def run_gpu(args):
         ctx.assemble(gpz.GPZ_PREC_MIXED if mixed else gpz.GPZ_PREC_FP64)
         if mixed and learned:
             return ctx.solve(solver=gpz.GPZ_SOLVER_LEARNED_MIXED_FCG, tol=TOL, max_iter=200000, reliable_delta=1e-2,
-                             check_every=64, want_x=False)
+                             check_every=64, want_x=False, spmv_variant=args.spmv_variant)
         if mixed:
             return ctx.solve(solver=gpz.GPZ_SOLVER_MIXED_CG, precond=gpz.GPZ_PRECOND_BLOCK_JACOBI, tol=TOL,
-                             max_iter=200000, reliable_delta=1e-2, check_every=64, want_x=False)
+                             max_iter=200000, reliable_delta=1e-2, check_every=64, want_x=False,
+                             spmv_variant=args.spmv_variant)
         return ctx.solve(solver=gpz.GPZ_SOLVER_CG, tol=TOL, max_iter=200000, check_every=64, want_x=False)
 
     def timed(fn):
