@@ -177,6 +177,12 @@ int gpz_spmv_fp32(gpz_ctx *ctx, int variant, const double *x, double *y);
 #define GPZ_SOLVER_LEARNED_FCG 4   /* flexible CG with the learned preconditioner (gpz_learned_*), FP64 */
 #define GPZ_SOLVER_LEARNED_MIXED_FCG 5 /* the same with FP32-value SpMV, FP64 x/r/dots and true-residual
                                           replacement (reliable_delta); scalar problems */
+#define GPZ_SOLVER_JACOBI 6        /* the stationary Jacobi iteration, SetJacobi as the solver
+                                      (Solvers/pzstepsolver.cpp:94-98): TPZMatrix::SolveJacobi
+                                      (Matrix/pzmatrix.cpp:643-667) for a symmetric pattern, the
+                                      TPZFYsmpMatrix override (Matrix/pzysmp.cpp:725-781, first sweep
+                                      always made) for a full one; tol is on the ABSOLUTE ||b - A x||,
+                                      iterations = sweeps performed; precond must be 0 or JACOBI */
 #define GPZ_PRECOND_JACOBI 1       /* TPZMatrix::SolveJacobi, one sweep (Matrix/pzmatrix.cpp:643-667) */
 #define GPZ_PRECOND_BLOCK_JACOBI 2 /* connect blocks, TPZBlockDiagonal (Matrix/pzblockdiag.h:21) */
 
@@ -184,7 +190,8 @@ typedef struct {
   int32_t solver;          /* GPZ_SOLVER_* */
   int32_t precond;         /* GPZ_PRECOND_* */
   int64_t max_iter;
-  double tol;              /* stop when ||r||/||b|| <= tol (recursive r, as cg.h:100) */
+  double tol;              /* stop when ||r||/||b|| <= tol (recursive r, as cg.h:100);
+                              GPZ_SOLVER_JACOBI: when ||b - A x|| <= tol */
   int32_t gmres_krylov;    /* GMRES restart length (SetGMRES numvectors) */
   int32_t check_every;     /* iterations per graph launch between convergence checks */
   double reliable_delta;   /* mixed CG: true-residual update when ||r|| < delta * max||r|| */

@@ -329,6 +329,61 @@ __global__ void __launch_bounds__(kThreads) k_true_resid(const int64_t *__restri
   if (grid_reduce<1>(v, R, tot) && threadIdx.x == 0) R.scal[S_TRUERR] = tot[0];
 }
 
+// ---- stationary Jacobi: TPZStepSolver::SetJacobi as the solver
+// (TPZMatrix::SolveJacobi, Matrix/pzmatrix.cpp:643-667, and the TPZFYsmpMatrix
+// override, Matrix/pzysmp.cpp:725-781).  A sweep is x += r / a_ii (a division,
+// as the reference) and then r = b - A x with ||r|| against the absolute
+// tolerance in S_TOL; sweeps of a batch after convergence (or a NaN norm)
+// return at entry.  The first sweep of a full (TPZFYsmpMatrix) pattern is unconditional: the
+// start kernel clears I_CONV for it.
+__global__ void k_jac_start(Red R, int first_sweep_always) {
+  double *s = R.scal;
+  int64_t *is = R.iscal;
+  is[I_IT] = 0;
+  const double res = sqrt(s[S_RR]);
+  is[I_CONV] = first_sweep_always ? 0 : res <= s[S_TOL] ? 1 : res > s[S_TOL] ? 0 : 2;
+}
+
+__global__ void __launch_bounds__(kThreads) k_jac_x(const double *__restrict__ a, const int64_t *__restrict__ diagpos,
+                                                    const double *__restrict__ r, double *__restrict__ x, int64_t n,
+                                                    const int64_t *__restrict__ is) {
+  if (!active(is)) return;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    x[i] += r[i] / a[diagpos[i]];
+}
+
+template <int TPR>
+__global__ void __launch_bounds__(kThreads) k_jac_resid(const int64_t *__restrict__ ia, const int32_t *__restrict__ ja,
+                                                        const double *__restrict__ a, const double *__restrict__ x,
+                                                        const double *__restrict__ b, double *__restrict__ r, int64_t n,
+                                                        Red R) {
+  if (!active(R.iscal)) return;
+  double rr = 0.0;
+  GPZ_ROW_LOOP(TPR, n) {
+    const int64_t i = r0 + (threadIdx.x & 31) / TPR;
+    const bool valid = i < n;
+    const double s = row_dot64<TPR>(ia, ja, a, x, i, sub, valid);
+    if (sub == 0 && valid) {
+      const double ri = b[i] - s;
+      r[i] = ri;
+      rr += ri * ri;
+    }
+  }
+  double v[1] = {rr}, tot[1];
+  if (grid_reduce<1>(v, R, tot) && threadIdx.x == 0) {
+    double *s = R.scal;
+    int64_t *is = R.iscal;
+    const double res = sqrt(tot[0]);
+    s[S_RR] = tot[0];
+    s[S_RESID] = res / s[S_NORMB];
+    is[I_SP64]++;
+    is[I_IT]++;
+    // the reference's loop runs while ||r|| > tol: a NaN norm ends it too (I_CONV = 2, not converged)
+    if (res <= s[S_TOL]) is[I_CONV] = 1;
+    else if (!(res > s[S_TOL])) is[I_CONV] = 2;
+  }
+}
+
 // ---- setup kernels for the mixed path and the block preconditioner
 __global__ void k_build_bsr3(const int64_t *__restrict__ ia, const int32_t *__restrict__ ja,
                              const double *__restrict__ a, int64_t nbrow, int64_t *__restrict__ bptr,
@@ -2388,7 +2443,94 @@ int collect_cg_pairs(Ctx &c, int npairs, double tol, int64_t max_iter, double *R
   return (int)j;
 }
 
+// Stationary Jacobi iteration (kernels k_jac_*): two launches per sweep, a
+// batch of sweeps captured once as a CUDA graph, convergence read back per
+// batch.  rep.iterations is the number of sweeps performed.
+int solve_jacobi(Ctx &c, const gpz_solver_opts &o, gpz_solve_report &rep) {
+  GPZ_REQUIRE(o.precond == GPZ_PRECOND_JACOBI || o.precond == 0, GPZ_E_INVALID,
+              "the Jacobi iteration takes no preconditioner");
+  alloc_work(c, false);
+  SolverWork &w = c.sw;
+  cudaStream_t s = c.stream;
+  const int tpr = pick_tpr(c.nnz, c.neq);
+  const int full = c.user_sym ? 0 : 1;
+  const int64_t maxit = full ? std::max<int64_t>(o.max_iter, 1) : o.max_iter;
+  const int batch = o.check_every > 0 ? o.check_every : 32;
+  cudaEvent_t ev0, ev1;
+  GPZ_CUDA_TRY(cudaEventCreate(&ev0));
+  GPZ_CUDA_TRY(cudaEventCreate(&ev1));
+  GPZ_CUDA_TRY(cudaEventRecord(ev0, s));
+  double hs[S_NSCAL] = {0};
+  hs[S_TOL] = o.tol;
+  int64_t hi[I_NISCAL] = {0};
+  hi[I_MAXIT] = maxit;
+  GPZ_CUDA_TRY(cudaMemcpyAsync(w.scal.p, hs, sizeof(hs), cudaMemcpyHostToDevice, s));
+  GPZ_CUDA_TRY(cudaMemcpyAsync(w.iscal.p, hi, sizeof(hi), cudaMemcpyHostToDevice, s));
+  Red R = red_of(c);
+  GPZ_TPR_SWITCH(tpr, (k_cg_init<T><<<wave(k_cg_init<T>), kThreads, 0, s>>>(c.d_ia.p, c.d_ja.p, c.d_a.p, w.x.p,
+                                                                             w.b.p, w.r.p, c.neq, o.from_current, R)));
+  k_jac_start<<<1, 1, 0, s>>>(R, full);
+  c.launches += 2;
+  GPZ_CUDA_TRY(cudaGetLastError());
+  auto sweeps = [&](int k) {
+    for (int i = 0; i < k; i++) {
+      k_jac_x<<<wave(k_jac_x), kThreads, 0, s>>>(c.d_a.p, c.d_diagpos.p, w.r.p, w.x.p, c.neq, w.iscal.p);
+      GPZ_TPR_SWITCH(tpr, (k_jac_resid<T><<<wave(k_jac_resid<T>), kThreads, 0, s>>>(c.d_ia.p, c.d_ja.p, c.d_a.p,
+                                                                                     w.x.p, w.b.p, w.r.p, c.neq, R)));
+      c.launches += 2;
+    }
+  };
+  cudaGraphExec_t exec = nullptr;
+  if (o.use_graph) {
+    cudaGraph_t g;
+    GPZ_CUDA_TRY(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+    const int64_t l0 = c.launches;
+    sweeps(batch);
+    GPZ_CUDA_TRY(cudaStreamEndCapture(s, &g));
+    c.launches = l0;
+    GPZ_CUDA_TRY(cudaGraphInstantiate(&exec, g, 0));
+    GPZ_CUDA_TRY(cudaGraphDestroy(g));
+  }
+  int64_t hstate[I_NISCAL];
+  for (;;) {
+    GPZ_CUDA_TRY(cudaMemcpyAsync(hstate, w.iscal.p, sizeof(hstate), cudaMemcpyDeviceToHost, s));
+    GPZ_CUDA_TRY(cudaStreamSynchronize(s));
+    if (hstate[I_CONV] != 0 || hstate[I_IT] >= maxit) break;
+    if (exec) {
+      GPZ_CUDA_TRY(cudaGraphLaunch(exec, s));
+      c.launches += 2 * (int64_t)batch;
+    } else {
+      sweeps(batch);
+    }
+    GPZ_CUDA_TRY(cudaGetLastError());
+  }
+  if (exec) cudaGraphExecDestroy(exec);
+  GPZ_TPR_SWITCH(tpr, (k_true_resid<T><<<wave(k_true_resid<T>), kThreads, 0, s>>>(c.d_ia.p, c.d_ja.p, c.d_a.p, w.x.p,
+                                                                                   w.b.p, c.neq, R)));
+  c.launches++;
+  GPZ_CUDA_TRY(cudaEventRecord(ev1, s));
+  GPZ_CUDA_TRY(cudaMemcpyAsync(hs, w.scal.p, sizeof(hs), cudaMemcpyDeviceToHost, s));
+  GPZ_CUDA_TRY(cudaMemcpyAsync(hstate, w.iscal.p, sizeof(hstate), cudaMemcpyDeviceToHost, s));
+  GPZ_CUDA_TRY(cudaStreamSynchronize(s));
+  float ms = 0.0f;
+  cudaEventElapsedTime(&ms, ev0, ev1);
+  cudaEventDestroy(ev0);
+  cudaEventDestroy(ev1);
+  check_device_flag(c, "Jacobi iteration");
+  rep.iterations = hstate[I_IT];
+  rep.resid = hs[S_RESID];
+  rep.true_resid = std::sqrt(hs[S_TRUERR]) / hs[S_NORMB];
+  rep.seconds = ms * 1e-3;
+  rep.spmv_fp64 = hstate[I_SP64] + (o.from_current ? 1 : 0) + 1;  // + the final true residual
+  rep.spmv_fp32 = 0;
+  rep.reliable_updates = 0;
+  rep.restarts = 0;
+  c.have_solution = true;
+  return hstate[I_CONV] == 1 ? GPZ_OK : GPZ_NOT_CONVERGED;
+}
+
 int solve(Ctx &c, const gpz_solver_opts &o, gpz_solve_report &rep) {
+  if (o.solver == GPZ_SOLVER_JACOBI) return solve_jacobi(c, o, rep);
   if (o.solver == GPZ_SOLVER_GMRES) return solve_gmres(c, o, rep);
   if (o.solver == GPZ_SOLVER_LEARNED_FCG || o.solver == GPZ_SOLVER_LEARNED_MIXED_FCG)
     return solve_learned(c, o, rep, o.solver == GPZ_SOLVER_LEARNED_MIXED_FCG);

@@ -20,6 +20,7 @@ GPZ_MAT_POISSON, GPZ_MAT_DARCY, GPZ_MAT_ELAST3D = 1, 2, 3
 GPZ_F_NONE, GPZ_F_CONST, GPZ_F_SINPROD, GPZ_F_QUADRATIC = 0, 1, 2, 3
 GPZ_PREC_FP64, GPZ_PREC_MIXED = 0, 1
 GPZ_SOLVER_CG, GPZ_SOLVER_GMRES, GPZ_SOLVER_MIXED_CG, GPZ_SOLVER_LEARNED_FCG, GPZ_SOLVER_LEARNED_MIXED_FCG = 1, 2, 3, 4, 5
+GPZ_SOLVER_JACOBI = 6
 GPZ_PRECOND_JACOBI, GPZ_PRECOND_BLOCK_JACOBI = 1, 2
 GPZ_KERNEL_SPMV_FP64, GPZ_KERNEL_SPMV_FP32, GPZ_KERNEL_ASSEMBLE = 1, 2, 3
 BIGNUMBER = 10.0 ** 17 * 2 / 3  # TPZMaterial::fBigNumber default for double

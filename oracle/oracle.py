@@ -90,6 +90,8 @@ def lib():
         L.orc_spmv.argtypes = [i64, i32, vp, vp, vp, vp, vp]
         L.orc_cg_jacobi.restype = i32
         L.orc_cg_jacobi.argtypes = [i64, i32, vp, vp, vp, vp, vp, i64, dp, i32, P(i64), P(dp), vp]
+        L.orc_jacobi.restype = i32
+        L.orc_jacobi.argtypes = [i64, i32, vp, vp, vp, vp, vp, i64, dp, i32, P(i64), P(dp)]
         L.orc_cg_block_jacobi.restype = i32
         L.orc_cg_block_jacobi.argtypes = [i64, i32, vp, vp, vp, vp, vp, i32, i64, dp, P(i64), P(dp)]
         L.orc_error_points.restype = i64
@@ -249,6 +251,17 @@ def cg_jacobi(sym, ia, ja, a, b, maxit, tol, jacobi_residual=False, history=Fals
     if history:
         out["hist"] = hist[: it.value].copy()
     return out
+
+
+def jacobi(sym, ia, ja, a, b, maxit, tol, x0=None):
+    """Stationary Jacobi (TPZStepSolver::SetJacobi as the solver); tol on the absolute ||b - A x||; x0 = the
+    FromCurrent initial guess."""
+    n = len(ia) - 1
+    x = np.zeros(n) if x0 is None else np.array(x0, np.float64)
+    it, res = ctypes.c_int64(), ctypes.c_double()
+    rc = lib().orc_jacobi(n, int(sym), _p(ia), _p(ja), _p(a), _p(np.ascontiguousarray(b)), _p(x), maxit, tol,
+                          int(x0 is not None), ctypes.byref(it), ctypes.byref(res))
+    return dict(x=x, iters=it.value, resid=res.value, rc=rc)
 
 
 def cg_block_jacobi(sym, ia, ja, a, b, bs, maxit, tol):

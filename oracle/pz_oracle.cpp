@@ -1478,6 +1478,52 @@ int orc_cg_jacobi(int64_t n, int sym, const int64_t *IA, const int64_t *JA, cons
   return 1;
 }
 
+// Stationary Jacobi iteration, TPZStepSolver::SetJacobi as the solver
+// (Solvers/pzstepsolver.cpp:94-98).  sym != 0: TPZSYsmpMatrix inherits
+// TPZMatrix::SolveJacobi (Matrix/pzmatrix.cpp:643-667): r = b - A x (from
+// current) or r = b, x = 0; while it < maxit and ||r|| > tol: x += r / a_ii,
+// r = b - A x.  sym == 0: the TPZFYsmpMatrix override (Matrix/pzysmp.cpp:
+// 725-781) always makes the first sweep (x = b / a_ii from zero) and then
+// continues as above for at most maxit sweeps in all.  The tolerance is on
+// the absolute residual norm.  iters_out receives the sweeps performed (the
+// reference leaves numiterations at its input value), resid_out the final
+// ||b - A x||.
+int orc_jacobi(int64_t n, int sym, const int64_t *IA, const int64_t *JA, const double *A, const double *b, double *x,
+               int64_t maxit, double tol, int from_current, int64_t *iters_out, double *resid_out) {
+  std::vector<double> diag(n), r(n), ax(n);
+  for (int64_t i = 0; i < n; i++) {
+    double d = 0.0;
+    for (int64_t k = IA[i]; k < IA[i + 1]; k++)
+      if (JA[k] == i) { d = A[k]; break; }
+    diag[i] = d;
+  }
+  auto residual = [&]() {
+    orc_spmv(n, sym, IA, JA, A, x, ax.data());
+    for (int64_t i = 0; i < n; i++) r[i] = b[i] - ax[i];
+    return std::sqrt(dot(n, r.data(), r.data()));
+  };
+  int64_t it = 0;
+  double res;
+  if (from_current) {
+    res = residual();
+  } else {
+    for (int64_t i = 0; i < n; i++) { x[i] = 0.0; r[i] = b[i]; }
+    res = std::sqrt(dot(n, r.data(), r.data()));
+  }
+  if (!sym) {
+    for (int64_t i = 0; i < n; i++) x[i] += r[i] / diag[i];
+    it = 1;
+    res = residual();
+  }
+  for (; it < maxit && res > tol; it++) {
+    for (int64_t i = 0; i < n; i++) x[i] += r[i] / diag[i];
+    res = residual();
+  }
+  *iters_out = it;
+  *resid_out = res;
+  return res <= tol ? 0 : 1;
+}
+
 // CG with a block-Jacobi preconditioner over consecutive equation blocks of
 // size bs (TPZBlockDiagonal, Matrix/pzblockdiag.h:21, built over the mesh's
 // connect blocks as TPZAnalysis::BuildPreconditioner(EBlockJacobi) does for

@@ -286,3 +286,54 @@ def test_error_norms_of_known_fields():
     assert abs(tot[2] - 1.0) <= 1e-13
     assert abs(tot[0] ** 2 - (1 - nu) / ((1 + nu) * (1 - 2 * nu))) <= 1e-13
     assert np.all(el[8:] == 0.0)  # boundary elements carry no error
+
+
+def _dense(ia, ja, a, n):
+    A = np.zeros((n, n))
+    for r in range(n):
+        A[r, ja[ia[r]:ia[r + 1]]] = a[ia[r]:ia[r + 1]]
+    return A
+
+
+def test_oracle_jacobi_iteration():
+    """The stationary Jacobi solver (SetJacobi as the solver): the oracle's sweeps against a numpy restatement of
+    TPZMatrix::SolveJacobi (Matrix/pzmatrix.cpp:643-667) on a dense copy, the TPZFYsmpMatrix override's first
+    sweep (Matrix/pzysmp.cpp:725-781), FromCurrent restarts and convergence on the absolute residual norm."""
+    om = O.poisson2d(8, 1)
+    ia, ja = om.pattern(False)
+    a, f = om.assemble(False, ia, ja)
+    sa, sj = om.pattern(True)
+    sv, sf = om.assemble(True, sa, sj)
+    n = om.neq
+    A = _dense(ia, ja, a, n)
+    d = np.diag(A).copy()
+    x = np.zeros(n)
+    r = f.copy()
+    for _ in range(5):
+        x = x + r / d
+        r = f - A @ x
+    for sym, (pi, pj, pv) in ((True, (sa, sj, sv)), (False, (ia, ja, a))):
+        out = O.jacobi(sym, pi, pj, pv, f, 5, 0.0)
+        assert out["iters"] == 5 and out["rc"] == 1
+        assert np.max(np.abs(out["x"] - x)) <= 1e-12 * np.max(np.abs(x))
+        assert abs(out["resid"] - np.linalg.norm(r)) <= 1e-9 * np.linalg.norm(r)
+        # FromCurrent: 2 + 3 sweeps are the 5 sweeps
+        x2 = O.jacobi(sym, pi, pj, pv, f, 2, 0.0)["x"]
+        out3 = O.jacobi(sym, pi, pj, pv, f, 3, 0.0, x0=x2)
+        assert out3["iters"] == 3
+        assert np.max(np.abs(out3["x"] - out["x"])) <= 1e-14 * np.max(np.abs(x))
+    # numiterations = 0, or a tolerance the initial residual meets: no sweep for TPZMatrix::SolveJacobi, one
+    # sweep (x = b / diag) for the TPZFYsmpMatrix override
+    big = 2 * np.linalg.norm(f)
+    for maxit, tol in ((0, 0.0), (10, big)):
+        s0 = O.jacobi(True, sa, sj, sv, f, maxit, tol)
+        f0 = O.jacobi(False, ia, ja, a, f, maxit, tol)
+        assert s0["iters"] == 0 and np.all(s0["x"] == 0.0)
+        assert f0["iters"] == 1 and np.array_equal(f0["x"], f / d)
+    # convergence on the absolute ||b - A x||, to the direct solution
+    tol = 1e-9 * np.linalg.norm(f)
+    conv = O.jacobi(True, sa, sj, sv, f, 100000, tol)
+    assert conv["rc"] == 0 and 10 < conv["iters"] < 100000 and conv["resid"] <= tol
+    xs = np.linalg.solve(A, f)
+    assert np.linalg.norm(conv["x"] - xs) <= 1e-6 * np.linalg.norm(xs)
+    assert np.linalg.norm(f - A @ conv["x"]) <= 1.01 * tol
