@@ -26,6 +26,7 @@ extern "C" {
  * plugin classes map negative codes back to DebugStop(). */
 #define GPZ_OK 0
 #define GPZ_NOT_CONVERGED 1            /* CG/GMRES hit max_iter (cg.h:129-131 returns 1) */
+#define GPZ_CANCELLED 2                /* gpz_set_killed(ctx, 1) was set: the call stopped (see gpz_set_killed) */
 #define GPZ_E_INVALID (-1)             /* bad argument / inconsistent descriptor */
 #define GPZ_E_CUDA (-2)                /* CUDA runtime error */
 #define GPZ_E_NOMEM (-3)               /* device allocation failed */
@@ -167,6 +168,19 @@ int gpz_spmv(gpz_ctx *ctx, double alpha, const double *x, double beta, const dou
  * the layout the SpMV autotuner chose, or `variant` (GPZ solver option
  * spmv_variant, 0..7) for 3-state problems; the FP32 CSR copy otherwise. */
 int gpz_spmv_fp32(gpz_ctx *ctx, int variant, const double *x, double *y);
+
+/* ---- cancellation ---------------------------------------------------------
+ * Replaces TPZGuiInterface::SetKilled / AmIKilled (Common/TPZGuiInterface.cpp:
+ * 80-87).  The reference polls AmIKilled before it starts the assembly threads
+ * and after each CalcStiff (StrMatrix/pzstrmatrixor.cpp:182,490) and returns
+ * silently.  Here gpz_assemble / gpz_assemble_rhs return GPZ_CANCELLED without
+ * assembling while the flag is set, and every iterative solve polls it between
+ * batches of iterations (CUDA-graph launches) and returns GPZ_CANCELLED with the
+ * last completed batch's iterate and report.  The flag stays set until cleared
+ * with gpz_set_killed(ctx, 0).  This is the one entry point that may be called
+ * from another thread while a call on the same context runs: it only stores
+ * the flag (no CUDA call). */
+int gpz_set_killed(gpz_ctx *ctx, int killed);
 
 /* ---- solve ----------------------------------------------------------------
  * TPZStepSolver::Solve (Solvers/pzstepsolver.cpp:64-169) with SetCG / SetGMRES

@@ -53,6 +53,7 @@ const char *gpz_get_error_string(int code) {
   switch (code) {
     case GPZ_OK: return "ok";
     case GPZ_NOT_CONVERGED: return "iterative solver did not converge within max_iter";
+    case GPZ_CANCELLED: return "cancelled by gpz_set_killed";
     case GPZ_E_INVALID: return "invalid argument";
     case GPZ_E_CUDA: return "CUDA runtime error";
     case GPZ_E_NOMEM: return "device memory allocation failed";
@@ -277,9 +278,16 @@ int gpz_pattern_download(gpz_ctx *ctx, int64_t *IA, int64_t *JA) {
   });
 }
 
+int gpz_set_killed(gpz_ctx *ctx, int killed) {
+  if (!ctx) return GPZ_E_INVALID;
+  ctx->c.killed.store(killed ? 1 : 0);
+  return GPZ_OK;
+}
+
 int gpz_assemble(gpz_ctx *ctx, int precision) {
   return guarded(ctx, [&](Ctx &c) {
     GPZ_REQUIRE(c.have_pattern, GPZ_E_NOT_READY, "no pattern");
+    if (c.killed.load()) return GPZ_CANCELLED;  // StrMatrix/pzstrmatrixor.cpp:490
     GPZ_REQUIRE(precision == GPZ_PREC_FP64 || precision == GPZ_PREC_MIXED, GPZ_E_INVALID, "precision");
     assemble_fp64(c);
     if (precision == GPZ_PREC_MIXED) make_fp32_copy(c);
@@ -294,6 +302,7 @@ int gpz_assemble(gpz_ctx *ctx, int precision) {
 int gpz_assemble_rhs(gpz_ctx *ctx) {
   return guarded(ctx, [&](Ctx &c) {
     GPZ_REQUIRE(c.have_mesh, GPZ_E_NOT_READY, "no mesh");
+    if (c.killed.load()) return GPZ_CANCELLED;
     assemble_rhs(c);
     GPZ_CUDA_TRY(cudaStreamSynchronize(c.stream));
     check_device_flag(c, "load vector assembly");

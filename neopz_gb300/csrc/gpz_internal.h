@@ -3,6 +3,7 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <atomic>
 #include <string>
 #include <vector>
 
@@ -194,6 +195,7 @@ struct ErrorEval {
 
 struct Ctx {
   int device = 0;
+  std::atomic<int> killed{0};  // gpz_set_killed; read between batches of device work
   cudaStream_t stream = nullptr;
   std::string last_error;
   int64_t launches = 0;

@@ -2158,7 +2158,12 @@ int solve_gmres(Ctx &c, const gpz_solver_opts &o, gpz_solve_report &rep) {
   // host bound only guards against a state machine that never finishes
   const int64_t max_cycles = o.max_iter / m + 3;
   int64_t cycles = 0;
+  bool cancelled = false;
   while (hi[GM_STATE] == GMS_RUN && cycles < max_cycles) {
+    if (c.killed.load()) {
+      cancelled = true;
+      break;
+    }
     if (exec) GPZ_CUDA_TRY(cudaGraphLaunch(exec, s));
     else launch_cycle();
     c.launches += per_cycle;
@@ -2181,9 +2186,10 @@ int solve_gmres(Ctx &c, const gpz_solver_opts &o, gpz_solve_report &rep) {
   cudaEventDestroy(ev0);
   cudaEventDestroy(ev1);
   check_device_flag(c, "GMRES");
-  GPZ_REQUIRE(hi[GM_STATE] != GMS_RUN && hi[GM_STATE] != GMS_CONV_PENDING && hi[GM_STATE] != GMS_MAXIT_PENDING,
+  GPZ_REQUIRE(cancelled ||
+                  (hi[GM_STATE] != GMS_RUN && hi[GM_STATE] != GMS_CONV_PENDING && hi[GM_STATE] != GMS_MAXIT_PENDING),
               GPZ_E_DEVICE_CHECK, "GMRES state machine did not finish");
-  rep.iterations = hi[GM_ITERS];
+  rep.iterations = cancelled ? hi[GM_J] - 1 : hi[GM_ITERS];  // GM_J counts from 1 (gmres.h's j)
   rep.resid = hd[GMD_RESID];
   rep.true_resid = std::sqrt(hs[S_TRUERR]) / hs[S_NORMB];
   rep.seconds = ms * 1e-3;
@@ -2193,6 +2199,7 @@ int solve_gmres(Ctx &c, const gpz_solver_opts &o, gpz_solve_report &rep) {
   rep.restarts = cycles;
   c.have_solution = true;
   if (hi[GM_STATE] == GMS_BREAK) return GPZ_E_BREAKDOWN;
+  if (cancelled) return GPZ_CANCELLED;
   return hi[GM_STATE] == GMS_CONV ? GPZ_OK : GPZ_NOT_CONVERGED;
 }
 
@@ -2321,10 +2328,15 @@ int solve_learned(Ctx &c, const gpz_solver_opts &o, gpz_solve_report &rep, bool 
       GPZ_CUDA_TRY(cudaGraphInstantiate(&exec, g, 0));
       GPZ_CUDA_TRY(cudaGraphDestroy(g));
     }
+    bool cancelled = false;
     for (;;) {
       GPZ_CUDA_TRY(cudaMemcpyAsync(hstate, w.iscal.p, sizeof(hstate), cudaMemcpyDeviceToHost, s));
       GPZ_CUDA_TRY(cudaStreamSynchronize(s));
       if (hstate[I_CONV] != 0 || hstate[I_IT] >= hi[I_MAXIT]) break;
+      if (c.killed.load()) {
+        cancelled = true;
+        break;
+      }
       if (exec) {
         GPZ_CUDA_TRY(cudaGraphLaunch(exec, s));
         c.launches += (int64_t)batch * per_iter;
@@ -2349,6 +2361,10 @@ int solve_learned(Ctx &c, const gpz_solver_opts &o, gpz_solve_report &rep, bool 
     nspmv64 += hstate[I_SP64];
     if (hstate[I_BREAK]) {
       rc = GPZ_E_BREAKDOWN;
+      break;
+    }
+    if (cancelled) {
+      rc = GPZ_CANCELLED;
       break;
     }
     const double true_resid = std::sqrt(hs[S_TRUERR]) / hs[S_NORMB];
@@ -2492,10 +2508,15 @@ int solve_jacobi(Ctx &c, const gpz_solver_opts &o, gpz_solve_report &rep) {
     GPZ_CUDA_TRY(cudaGraphDestroy(g));
   }
   int64_t hstate[I_NISCAL];
+  bool cancelled = false;
   for (;;) {
     GPZ_CUDA_TRY(cudaMemcpyAsync(hstate, w.iscal.p, sizeof(hstate), cudaMemcpyDeviceToHost, s));
     GPZ_CUDA_TRY(cudaStreamSynchronize(s));
     if (hstate[I_CONV] != 0 || hstate[I_IT] >= maxit) break;
+    if (c.killed.load()) {
+      cancelled = true;
+      break;
+    }
     if (exec) {
       GPZ_CUDA_TRY(cudaGraphLaunch(exec, s));
       c.launches += 2 * (int64_t)batch;
@@ -2526,6 +2547,7 @@ int solve_jacobi(Ctx &c, const gpz_solver_opts &o, gpz_solve_report &rep) {
   rep.reliable_updates = 0;
   rep.restarts = 0;
   c.have_solution = true;
+  if (cancelled) return GPZ_CANCELLED;
   return hstate[I_CONV] == 1 ? GPZ_OK : GPZ_NOT_CONVERGED;
 }
 
@@ -2604,7 +2626,12 @@ int solve(Ctx &c, const gpz_solver_opts &o, gpz_solve_report &rep) {
     GPZ_CUDA_TRY(cudaGraphDestroy(g));
   }
   int64_t hstate[I_NISCAL];
+  bool cancelled = false;
   for (;;) {
+    if (c.killed.load()) {
+      cancelled = true;
+      break;
+    }
     if (exec) {
       GPZ_CUDA_TRY(cudaGraphLaunch(exec, s));
       c.launches += (int64_t)batch * per_iter;
@@ -2643,6 +2670,7 @@ int solve(Ctx &c, const gpz_solver_opts &o, gpz_solve_report &rep) {
   rep.restarts = hstate[I_NRESTART];
   c.have_solution = true;
   if (hstate[I_BREAK]) return GPZ_E_BREAKDOWN;
+  if (cancelled && hstate[I_CONV] == 0) return GPZ_CANCELLED;
   return hstate[I_CONV] == 1 ? GPZ_OK : GPZ_NOT_CONVERGED;
 }
 

@@ -14,7 +14,7 @@ _HERE = os.path.dirname(os.path.abspath(__file__))
 LIBGPZ = os.path.join(_HERE, "_build", "libgpz.so")
 LIBHOST = os.path.join(_HERE, "_build", "libgpzhost.so")
 
-GPZ_OK, GPZ_NOT_CONVERGED = 0, 1
+GPZ_OK, GPZ_NOT_CONVERGED, GPZ_CANCELLED = 0, 1, 2
 GPZ_EL_LINE, GPZ_EL_QUAD, GPZ_EL_HEX = 1, 2, 3
 GPZ_MAT_POISSON, GPZ_MAT_DARCY, GPZ_MAT_ELAST3D = 1, 2, 3
 GPZ_F_NONE, GPZ_F_CONST, GPZ_F_SINPROD, GPZ_F_QUADRATIC = 0, 1, 2, 3
@@ -107,6 +107,7 @@ def lib():
         L.gpz_time_kernel.argtypes = [vp, i32, i32, _P(dp)]
         L.gpz_tuning_report.argtypes = [vp, ctypes.c_char_p, i64]
         L.gpz_assemble.argtypes = [vp, i32]
+        L.gpz_set_killed.argtypes = [vp, i32]
         L.gpz_matrix_download.argtypes = [vp, vp]
         L.gpz_rhs_download.argtypes = [vp, vp]
         L.gpz_rhs_upload.argtypes = [vp, vp]
@@ -307,7 +308,13 @@ class Context:
         return ia, ja
 
     def assemble(self, precision=GPZ_PREC_FP64):
-        self._check(lib().gpz_assemble(self.h, precision))
+        """GPZ_OK, or GPZ_CANCELLED (nothing assembled) while set_killed(True) holds."""
+        return self._check(lib().gpz_assemble(self.h, precision), allow=(GPZ_CANCELLED,))
+
+    def set_killed(self, killed=True):
+        """TPZGuiInterface::SetKilled: assemblies return GPZ_CANCELLED, solves stop at their next batch boundary;
+        callable from another thread while a call on this context runs."""
+        self._check(lib().gpz_set_killed(self.h, int(bool(killed))))
 
     def matrix(self):
         a = np.zeros(self.nnz)
@@ -364,7 +371,7 @@ class Context:
 
     def assemble_rhs(self):
         """Load vector alone (no matrix); read it with rhs()."""
-        self._check(lib().gpz_assemble_rhs(self.h))
+        return self._check(lib().gpz_assemble_rhs(self.h), allow=(GPZ_CANCELLED,))
 
     def assembly_report(self):
         import json
@@ -430,7 +437,7 @@ class Context:
             x = np.zeros(self.neq) if x0 is None else np.array(x0, np.float64)
         bb = None if b is None else np.ascontiguousarray(b, np.float64)
         rc = self._check(lib().gpz_solve(self.h, ctypes.byref(o), _p(bb), _p(x), ctypes.byref(rep)),
-                         allow=(GPZ_NOT_CONVERGED,))
+                         allow=(GPZ_NOT_CONVERGED, GPZ_CANCELLED))
         return dict(rc=rc, x=x, iterations=rep.iterations, resid=rep.resid, true_resid=rep.true_resid,
                     seconds=rep.seconds, spmv_fp64=rep.spmv_fp64, spmv_fp32=rep.spmv_fp32,
                     reliable_updates=rep.reliable_updates, restarts=rep.restarts)
