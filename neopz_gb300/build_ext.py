@@ -43,7 +43,8 @@ def _run(cmd):
 
 def build(verbose=False, jobs=None):
     os.makedirs(BUILD, exist_ok=True)
-    headers = glob.glob(os.path.join(CSRC, "*.h")) + glob.glob(os.path.join(ROOT, "include", "*.h"))
+    headers = (glob.glob(os.path.join(CSRC, "*.h")) + glob.glob(os.path.join(CSRC, "*.cuh")) +
+               glob.glob(os.path.join(ROOT, "include", "*.h")))
     srcs = sorted(glob.glob(os.path.join(CSRC, "*.cu")) + glob.glob(os.path.join(CSRC, "*.cpp")))
     objs, jobs_l = [], []
     for s in srcs:
