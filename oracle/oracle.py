@@ -1,7 +1,7 @@
 """TEST INFRASTRUCTURE ONLY: ctypes front end of the CPU oracle (pz_oracle.cpp).
 
-The oracle is the checker for the GPU library and the CPU baseline of the
-benchmark.  It is imported by tests/, by ``__graft_entry__.smoke()`` and by the
+The tests compare the GPU library against the oracle, and the oracle is the CPU
+baseline of the benchmark.  It is imported by tests/, by ``__graft_entry__.smoke()`` and by the
 CPU-baseline leg of ``bench.py`` only; the product (``neopz_gb300``) never
 imports it.
 """

@@ -8,8 +8,8 @@
 //  and  TPZLinearAnalysis::Solve -> TPZStepSolver -> CG / GMRES / Jacobi.
 //  Every function cites the reference file:line it follows.
 //
-//  It is the CHECKER for the GPU library (libgpz.so) and the CPU baseline
-//  timed beside it.  The product never links, loads or calls it; only the
+//  The tests compare the GPU library (libgpz.so) against it, and it is the CPU
+//  baseline timed beside it.  The product never links, loads or calls it; only the
 //  tests, the smoke check and the CPU-baseline leg of the benchmark do.
 //
 //  Parity pins (see tests/test_oracle_golden.py): the reference's own unit
