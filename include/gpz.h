@@ -122,6 +122,32 @@ int64_t gpz_kernel_launches(gpz_ctx *ctx);
  * (TPZStructMatrix::ComputeElementColors, StrMatrix/TPZStructMatrix.cpp:104-161). */
 int gpz_mesh_upload(gpz_ctx *ctx, const gpz_mesh_desc *desc);
 
+/* ---- equation filter ----------------------------------------------------
+ * Replaces TPZEquationFilter::SetActiveEquations / Reset
+ * (StrMatrix/TPZEquationFilter.h) on the structural matrix.  Call after
+ * gpz_mesh_upload and before gpz_pattern_build (a new filter drops the
+ * pattern and the values).  active: mesh equation numbers, any order,
+ * duplicates removed; nactive < 0 resets the filter (all equations active).
+ * Under an active set of n equations, as the reference does:
+ *   - the pattern, matrix, gpz_spmv and gpz_solve are over the n active
+ *     equations, renumbered in increasing mesh order (the mesh-level pattern
+ *     restricted to active rows and columns, StrMatrix/TPZSSpStructMatrix.cpp:
+ *     49-193 / TPZSpStructMatrix.cpp:53-190; element contributions to an
+ *     inactive row or column are dropped, TPZEquationFilter::Filter);
+ *   - the load vector (gpz_rhs_download) keeps the mesh's size with zeros at
+ *     the inactive equations (TPZEquationFilter::Scatter after the condensed
+ *     assembly, StrMatrix/pzstrmatrixor.cpp:43-71); gpz_solve with b = NULL
+ *     gathers its active entries (TPZLinearAnalysis::SolveT,
+ *     Analysis/TPZLinearAnalysis.cpp:194);
+ *   - gpz_error_evaluate with sol = NULL scatters the device solution to the
+ *     mesh equations with zeros elsewhere (TPZLinearAnalysis.cpp:197); a host
+ *     sol has the mesh's size.
+ * The 3x3-block FP32 layouts, the matrix-free operators, block Jacobi and the
+ * learned preconditioner need whole connect blocks: under a filter the mixed
+ * CG uses the FP32 CSR copy, and block Jacobi and gpz_learned_* return
+ * GPZ_E_INVALID.  gpz_pattern_upload is not available under a filter. */
+int gpz_equation_filter(gpz_ctx *ctx, int64_t nactive, const int64_t *active);
+
 /* ---- sparsity pattern ----------------------------------------------------
  * Replaces TPZSSpStructMatrix::Create / SetupMatrixData (sym = 1, upper
  * triangle; StrMatrix/TPZSSpStructMatrix.cpp:31-193) and

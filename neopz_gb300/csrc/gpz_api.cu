@@ -1,4 +1,5 @@
 // C ABI entry points (include/gpz.h).  No exception crosses this boundary.
+#include <algorithm>
 #include <cstring>
 
 #include "gpz_internal.h"
@@ -148,6 +149,9 @@ int gpz_mesh_upload(gpz_ctx *ctx, const gpz_mesh_desc *d) {
     c.nnodes = d->nnodes;
     c.nconnects = d->nconnects;
     c.neq = d->neq;
+    c.neq_mesh = d->neq;
+    c.flt.active = false;  // a new mesh starts without an equation filter
+    c.flt.h_act.clear();
     c.mats.assign(d->mats, d->mats + d->nmat);
     c.bcs.assign(d->bcs, d->bcs + d->nbc);
     c.h_el_type.assign(d->el_type, d->el_type + d->nel);
@@ -188,12 +192,41 @@ int gpz_mesh_set_coef(gpz_ctx *ctx, const double *el_coef) {
   });
 }
 
+int gpz_equation_filter(gpz_ctx *ctx, int64_t nactive, const int64_t *active) {
+  return guarded(ctx, [&](Ctx &c) {
+    GPZ_REQUIRE(c.have_mesh, GPZ_E_NOT_READY, "no mesh");
+    std::vector<int64_t> v;
+    if (nactive >= 0) {
+      GPZ_REQUIRE(nactive > 0 && active, GPZ_E_INVALID, "active equations");
+      v.assign(active, active + nactive);
+      for (int64_t q : v) GPZ_REQUIRE(q >= 0 && q < c.neq_mesh, GPZ_E_INVALID, "active equation out of range");
+      std::sort(v.begin(), v.end());  // SetActiveEquations: duplicates removed, increasing order
+      v.erase(std::unique(v.begin(), v.end()), v.end());
+    }
+    c.flt.active = nactive >= 0;
+    c.flt.h_act.swap(v);
+    // another system: its pattern and values are built again
+    c.neq = c.neq_mesh;
+    c.have_pattern = false;
+    c.have_matrix = false;
+    c.have_solution = false;
+    c.have_a32 = false;
+    c.have_bsr3 = false;
+    c.have_bjinv = false;
+    c.spmv32_tuned = -1;
+    drop_assembly_graph(c);
+    return GPZ_OK;
+  });
+}
+
 int gpz_pattern_build(gpz_ctx *ctx, int sym, int64_t *nnz_out) {
   return guarded(ctx, [&](Ctx &c) {
     GPZ_REQUIRE(c.have_mesh, GPZ_E_NOT_READY, "no mesh");
+    c.neq = c.neq_mesh;
     build_pattern(c);
     build_upper(c);
     build_element_offsets(c);
+    if (c.flt.active) condense_pattern(c);
     c.user_sym = sym ? 1 : 0;
     c.have_pattern = true;
     c.spmv32_tuned = -1;  // a new pattern is tuned again at its first mixed assembly
@@ -207,7 +240,8 @@ int gpz_pattern_build(gpz_ctx *ctx, int sym, int64_t *nnz_out) {
 int gpz_pattern_upload(gpz_ctx *ctx, int sym, int64_t neq, const int64_t *IA, const int64_t *JA) {
   return guarded(ctx, [&](Ctx &c) {
     GPZ_REQUIRE(c.have_mesh, GPZ_E_NOT_READY, "no mesh");
-    GPZ_REQUIRE(neq == c.neq && IA && JA, GPZ_E_INVALID, "pattern size");
+    GPZ_REQUIRE(!c.flt.active, GPZ_E_INVALID, "under an equation filter the pattern is built on the device");
+    GPZ_REQUIRE(neq == c.neq_mesh && IA && JA, GPZ_E_INVALID, "pattern size");
     GPZ_REQUIRE(!sym, GPZ_E_INVALID, "upload the full pattern (TPZFYsmpMatrix layout); the upper one is derived");
     int64_t nnz = IA[neq];
     std::vector<int32_t> ja32(nnz);
@@ -334,10 +368,15 @@ int gpz_error_evaluate(gpz_ctx *ctx, int32_t exact_order, const double *sol, con
     GPZ_REQUIRE(c.er.npts == 0 || (u_exact && du_exact), GPZ_E_INVALID, "null exact solution");
     const double *sol_dev = c.sw.x.p;
     if (sol) {
-      c.er.sol.upload(sol, c.neq, c.stream);
+      c.er.sol.upload(sol, c.neq_mesh, c.stream);
       sol_dev = c.er.sol.p;
     } else {
       GPZ_REQUIRE(c.have_solution && c.sw.x.p, GPZ_E_NOT_READY, "no solution on the device");
+      if (c.flt.active) {  // TPZEquationFilter::Scatter of the condensed solution (Analysis/TPZLinearAnalysis.cpp:197)
+        c.flt.xfull.alloc(std::max<int64_t>(c.neq_mesh, 1));
+        filter_scatter(c, c.sw.x.p, c.flt.xfull.p);
+        sol_dev = c.flt.xfull.p;
+      }
     }
     error_evaluate(c, sol_dev, u_exact, du_exact, errors, el_errors);
     check_device_flag(c, "error norms");
@@ -383,7 +422,7 @@ int gpz_matrix_download(gpz_ctx *ctx, double *A) {
 int gpz_rhs_download(gpz_ctx *ctx, double *F) {
   return guarded(ctx, [&](Ctx &c) {
     GPZ_REQUIRE(c.have_matrix || c.have_rhs, GPZ_E_NOT_READY, "not assembled");
-    GPZ_CUDA_TRY(cudaMemcpyAsync(F, c.d_f.p, c.neq * sizeof(double), cudaMemcpyDeviceToHost, c.stream));
+    GPZ_CUDA_TRY(cudaMemcpyAsync(F, c.d_f.p, c.neq_mesh * sizeof(double), cudaMemcpyDeviceToHost, c.stream));
     GPZ_CUDA_TRY(cudaStreamSynchronize(c.stream));
     return GPZ_OK;
   });
@@ -393,7 +432,7 @@ int gpz_rhs_upload(gpz_ctx *ctx, const double *F) {
   return guarded(ctx, [&](Ctx &c) {
     GPZ_REQUIRE(c.have_matrix, GPZ_E_NOT_READY, "not assembled");
     GPZ_REQUIRE(F, GPZ_E_INVALID, "null input");
-    GPZ_CUDA_TRY(cudaMemcpyAsync(c.d_f.p, F, c.neq * sizeof(double), cudaMemcpyHostToDevice, c.stream));
+    GPZ_CUDA_TRY(cudaMemcpyAsync(c.d_f.p, F, c.neq_mesh * sizeof(double), cudaMemcpyHostToDevice, c.stream));
     GPZ_CUDA_TRY(cudaStreamSynchronize(c.stream));
     return GPZ_OK;
   });
@@ -431,6 +470,7 @@ int gpz_solve(gpz_ctx *ctx, const gpz_solver_opts *opts, const double *b, double
     solver_prepare(c, mixed);
     cudaStream_t s = c.stream;
     if (b) GPZ_CUDA_TRY(cudaMemcpyAsync(c.sw.b.p, b, c.neq * sizeof(double), cudaMemcpyHostToDevice, s));
+    else if (c.flt.active) filter_gather(c, c.d_f.p, c.sw.b.p);  // TPZEquationFilter::Gather (TPZLinearAnalysis.cpp:194)
     else GPZ_CUDA_TRY(cudaMemcpyAsync(c.sw.b.p, c.d_f.p, c.neq * sizeof(double), cudaMemcpyDeviceToDevice, s));
     if (opts->from_current) {
       GPZ_REQUIRE(x, GPZ_E_INVALID, "from_current needs x");

@@ -717,13 +717,14 @@ ElemArgs args_of(Ctx &c, const Bucket *b) {
   P.coef_const = m->coef_const;
   P.big = m->kind == GPZ_MAT_ELAST3D ? 1.e12 : m->bignumber;  // TPZElasticity3D.cpp:632
   for (int k = 0; k < 3; k++) P.force[k] = m->force[k];
-  P.ia = c.d_ia.p;
+  const bool flt = c.flt.active;  // the element kernels fill the mesh-level CSR under a filter
+  P.ia = flt ? c.flt.m_ia.p : c.d_ia.p;
   P.offbase = c.d_offbase.p;
   P.off = c.d_off.p;
-  P.a = c.d_a.p;
+  P.a = flt ? c.flt.m_a.p : c.d_a.p;
   P.f = c.d_f.p;
-  P.nnz = c.nnz;
-  P.neq = c.neq;
+  P.nnz = flt ? c.flt.m_nnz : c.nnz;
+  P.neq = c.neq_mesh;
   P.err = c.d_err.p;
   return P;
 }
@@ -764,8 +765,11 @@ void launch_elements(Ctx &c, int threads, bool rhs_only = false, bool set_attrs 
 
 void assemble_fp64(Ctx &c) {
   cudaStream_t s = c.stream;
+  const bool flt = c.flt.active;
   c.d_a.alloc(std::max<int64_t>(c.nnz, 1));
-  c.d_f.alloc(std::max<int64_t>(c.neq, 1));
+  if (flt) c.flt.m_a.alloc(std::max<int64_t>(c.flt.m_nnz, 1));
+  DBuf<double> &target = flt ? c.flt.m_a : c.d_a;
+  c.d_f.alloc(std::max<int64_t>(c.neq_mesh, 1));
   // autotuner of the hp classes' run-time kernel: time one full assembly per
   // block size (the values do not depend on it: one CTA per element, fixed
   // summation order) and keep the fastest
@@ -780,7 +784,7 @@ void assemble_fp64(Ctx &c) {
     GPZ_CUDA_TRY(cudaEventCreate(&e0));
     GPZ_CUDA_TRY(cudaEventCreate(&e1));
     for (int i = 0; i < 3; i++) {
-      c.d_a.zero(s);
+      target.zero(s);
       c.d_f.zero(s);
       GPZ_CUDA_TRY(cudaEventRecord(e0, s));
       launch_elements(c, cand[i]);
@@ -805,9 +809,13 @@ void assemble_fp64(Ctx &c) {
   }
   c.d_dinv.alloc(std::max<int64_t>(c.neq, 1));
   auto body = [&](bool set_attrs) {
-    c.d_a.zero(s);
+    target.zero(s);
     c.d_f.zero(s);
     launch_elements(c, 0, false, set_attrs);
+    if (flt) {
+      filter_values(c);
+      filter_zero_inactive(c, c.d_f.p);
+    }
     k_extract_diag<<<grid_for(c.neq, 256), 256, 0, s>>>(c.d_a.p, c.d_diagpos.p, c.neq, c.d_dinv.p);
     c.launches++;
     GPZ_CUDA_TRY(cudaGetLastError());
@@ -838,9 +846,10 @@ void assemble_fp64(Ctx &c) {
 // load vector alone (TPZStructMatrix::Assemble(rhs), StrMatrix/pzstrmatrixor.cpp:75-103):
 // the same element kernels, stopped before the element matrix
 void assemble_rhs(Ctx &c) {
-  c.d_f.alloc(std::max<int64_t>(c.neq, 1));
+  c.d_f.alloc(std::max<int64_t>(c.neq_mesh, 1));
   c.d_f.zero(c.stream);
   launch_elements(c, 0, true);
+  if (c.flt.active) filter_zero_inactive(c, c.d_f.p);
 }
 
 void to_fp32(Ctx &c) {

@@ -375,7 +375,7 @@ static ErrArgs err_args(Ctx &c, const ErrorEval::Tab &t, int points_only) {
   P.coef_const = m.kind == GPZ_MAT_ELAST3D ? m.E : m.coef_const;
   P.nu = m.nu;
   P.pt_off = c.er.pt_off.p;
-  P.neq = c.neq;
+  P.neq = c.neq_mesh;
   P.err = c.d_err.p;
   return P;
 }

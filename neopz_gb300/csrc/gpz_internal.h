@@ -203,7 +203,8 @@ struct Ctx {
   // mesh
   bool have_mesh = false;
   int dim = 0, nstate = 1;
-  int64_t nel = 0, nnodes = 0, nconnects = 0, neq = 0;
+  int64_t nel = 0, nnodes = 0, nconnects = 0, neq = 0;  // neq: equations of the system (the solves' size)
+  int64_t neq_mesh = 0;                      // equations of the mesh (larger than neq under an equation filter)
   std::vector<gpz_material> mats;
   std::vector<gpz_bc> bcs;
   std::vector<int32_t> h_el_type, h_el_mat;
@@ -231,6 +232,23 @@ struct Ctx {
   DBuf<int64_t> d_diagpos;                   // [neq] slot of the diagonal entry
   DBuf<int64_t> d_offbase;                   // [nel] start of the element's offset table
   DBuf<int32_t> d_off;                       // element side-pair offsets inside a block row
+
+  // TPZEquationFilter (StrMatrix/TPZEquationFilter.h): with an active set the
+  // system is the mesh-level CSR restricted to the active rows and columns,
+  // renumbered in increasing order; the element kernels assemble into the
+  // mesh-level arrays, which a gather condenses
+  struct EqFilter {
+    bool active = false;
+    std::vector<int64_t> h_act;              // sorted, unique (mesh numbering)
+    DBuf<int64_t> act;                       // [neq] active equations
+    DBuf<int64_t> dest;                      // [neq_mesh] condensed index, or -1
+    DBuf<int64_t> keep;                      // [nnz] mesh-level slot of each condensed entry
+    DBuf<int64_t> m_ia, m_diagpos;           // mesh-level full CSR, the assembly's target
+    DBuf<int32_t> m_ja;
+    DBuf<double> m_a;
+    int64_t m_nnz = 0;
+    DBuf<double> xfull;                      // a solution expanded to the mesh equations
+  } flt;
 
   // values
   bool have_matrix = false;
@@ -283,6 +301,11 @@ void error_evaluate(Ctx &c, const double *sol_dev, const double *uex_host, const
 void build_pattern(Ctx &c);
 void build_upper(Ctx &c);
 void build_element_offsets(Ctx &c);
+void condense_pattern(Ctx &c);  // restrict the system to the equation filter's active set
+void filter_gather(Ctx &c, const double *v_mesh, double *v_sys);
+void filter_scatter(Ctx &c, const double *v_sys, double *v_mesh);
+void filter_zero_inactive(Ctx &c, double *f_mesh);
+void filter_values(Ctx &c);     // condensed values from the mesh-level ones (c.flt.keep)
 // assemble.cu
 void build_buckets(Ctx &c, const gpz_mesh_desc &d);
 void assemble_fp64(Ctx &c);

@@ -426,6 +426,7 @@ int sides_of(int type) { return type == GPZ_EL_HEX ? 27 : (type == GPZ_EL_QUAD ?
 void setup_mesh(Ctx &c, int R) {
   Learned &L = c.ln;
   GPZ_REQUIRE(c.have_mesh, GPZ_E_NOT_READY, "no mesh");
+  GPZ_REQUIRE(!c.flt.active, GPZ_E_INVALID, "learned preconditioner: not available under an equation filter");
   GPZ_REQUIRE(R >= 1 && R <= kMaxR, GPZ_E_INVALID, "rank must be in 1..8");
   L.h_vel.clear();
   int vtype = -1;
@@ -830,6 +831,7 @@ int guarded_ln(gpz_ctx *ctx, F &&f) {
   Ctx &c = ctx->c;
   try {
     GPZ_CUDA_TRY(cudaSetDevice(c.device));
+    GPZ_REQUIRE(!c.flt.active, GPZ_E_INVALID, "learned preconditioner: not available under an equation filter");
     return f(c);
   } catch (const gpz::Error &e) {
     c.last_error = e.msg;

@@ -167,6 +167,62 @@ __global__ void k_fill_ja(const int32_t *__restrict__ nbr, const int64_t *__rest
   }
 }
 
+// ---- equation filter (TPZEquationFilter::SetActiveEquations / Filter,
+// StrMatrix/TPZEquationFilter.h; applied to the pattern as
+// TPZSSpStructMatrix::SetupMatrixData, StrMatrix/TPZSSpStructMatrix.cpp:49-193,
+// and TPZSpStructMatrix::SetupMatrixData, StrMatrix/TPZSpStructMatrix.cpp:53-190,
+// apply it: rows and columns of inactive equations are dropped and the active
+// ones renumbered in increasing order, which keeps every row sorted)
+__global__ void k_flt_dest(const int64_t *__restrict__ act, int64_t n, int64_t *__restrict__ dest) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) dest[act[i]] = i;
+}
+
+__global__ void k_flt_gather(const double *__restrict__ v, const int64_t *__restrict__ idx, int64_t n,
+                             double *__restrict__ out) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) out[i] = v[idx[i]];
+}
+
+__global__ void k_flt_scatter(const double *__restrict__ v, const int64_t *__restrict__ idx, int64_t n,
+                              double *__restrict__ out) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) out[idx[i]] = v[i];
+}
+
+__global__ void k_flt_zero_inactive(const int64_t *__restrict__ dest, int64_t n, double *__restrict__ f) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n && dest[i] < 0) f[i] = 0.0;
+}
+
+__global__ void k_flt_count(const int64_t *__restrict__ m_ia, const int32_t *__restrict__ m_ja,
+                            const int64_t *__restrict__ act, const int64_t *__restrict__ dest, int64_t n,
+                            int64_t *__restrict__ rowlen) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const int64_t r = act[i];
+  int64_t cnt = 0;
+  for (int64_t k = m_ia[r]; k < m_ia[r + 1]; k++) cnt += dest[m_ja[k]] >= 0 ? 1 : 0;
+  rowlen[i] = cnt;
+}
+
+__global__ void k_flt_fill(const int64_t *__restrict__ m_ia, const int32_t *__restrict__ m_ja,
+                           const int64_t *__restrict__ act, const int64_t *__restrict__ dest, int64_t n,
+                           const int64_t *__restrict__ ia, int32_t *__restrict__ ja, int64_t *__restrict__ keep) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const int64_t r = act[i];
+  int64_t p = ia[i];
+  for (int64_t k = m_ia[r]; k < m_ia[r + 1]; k++) {
+    const int64_t d = dest[m_ja[k]];
+    if (d >= 0) {
+      ja[p] = (int32_t)d;
+      keep[p] = k;
+      p++;
+    }
+  }
+}
+
 __device__ __forceinline__ int64_t find_col(const int32_t *__restrict__ ja, int64_t lo, int64_t hi, int64_t col) {
   while (lo < hi) {
     int64_t mid = (lo + hi) >> 1;
@@ -314,6 +370,72 @@ void build_upper(Ctx &c) {
     GPZ_CUDA_TRY(cudaGetLastError());
   }
   GPZ_CUDA_TRY(cudaStreamSynchronize(s));
+}
+
+template <class T>
+static void swap_buf(DBuf<T> &a, DBuf<T> &b) {
+  std::swap(a.p, b.p);
+  std::swap(a.n, b.n);
+}
+
+// The mesh-level full CSR in c.d_ia / c.d_ja (after build_pattern, build_upper
+// and build_element_offsets) becomes the assembly's target (c.flt.m_*), and the
+// system arrays are rebuilt over the active equations.
+void condense_pattern(Ctx &c) {
+  cudaStream_t s = c.stream;
+  auto &F = c.flt;
+  const int64_t n = (int64_t)F.h_act.size();
+  swap_buf(c.d_ia, F.m_ia);
+  swap_buf(c.d_ja, F.m_ja);
+  swap_buf(c.d_diagpos, F.m_diagpos);
+  F.m_nnz = c.nnz;
+  F.act.upload(F.h_act.data(), n, s);
+  F.dest.alloc(c.neq_mesh);
+  GPZ_CUDA_TRY(cudaMemsetAsync(F.dest.p, 0xff, c.neq_mesh * sizeof(int64_t), s));  // -1
+  k_flt_dest<<<grid_for(n, 256), 256, 0, s>>>(F.act.p, n, F.dest.p);
+  DBuf<int64_t> rowlen;
+  rowlen.alloc(n + 1);
+  rowlen.zero(s);
+  k_flt_count<<<grid_for(n, 256), 256, 0, s>>>(F.m_ia.p, F.m_ja.p, F.act.p, F.dest.p, n, rowlen.p);
+  c.launches += 2;
+  GPZ_CUDA_TRY(cudaGetLastError());
+  c.d_ia.alloc(n + 1);
+  exclusive_scan_i64(rowlen.p, c.d_ia.p, n + 1, s, c);
+  GPZ_CUDA_TRY(cudaMemcpyAsync(&c.nnz, c.d_ia.p + n, sizeof(int64_t), cudaMemcpyDeviceToHost, s));
+  GPZ_CUDA_TRY(cudaStreamSynchronize(s));
+  c.d_ja.alloc(std::max<int64_t>(c.nnz, 1));
+  F.keep.alloc(std::max<int64_t>(c.nnz, 1));
+  k_flt_fill<<<grid_for(n, 256), 256, 0, s>>>(F.m_ia.p, F.m_ja.p, F.act.p, F.dest.p, n, c.d_ia.p, c.d_ja.p,
+                                              F.keep.p);
+  c.launches++;
+  GPZ_CUDA_TRY(cudaGetLastError());
+  c.neq = n;
+  build_upper(c);  // the system's diagonal slots and upper triangle
+}
+
+// TPZEquationFilter::Gather (mesh -> active equations), ::Scatter (active
+// equations -> mesh, zeros elsewhere), and the zeros the reference's filtered
+// rhs assembly leaves at inactive equations (StrMatrix/pzstrmatrixor.cpp:43-71)
+void filter_gather(Ctx &c, const double *v_mesh, double *v_sys) {
+  k_flt_gather<<<grid_for(c.neq, 256), 256, 0, c.stream>>>(v_mesh, c.flt.act.p, c.neq, v_sys);
+  c.launches++;
+  GPZ_CUDA_TRY(cudaGetLastError());
+}
+void filter_scatter(Ctx &c, const double *v_sys, double *v_mesh) {
+  GPZ_CUDA_TRY(cudaMemsetAsync(v_mesh, 0, c.neq_mesh * sizeof(double), c.stream));
+  k_flt_scatter<<<grid_for(c.neq, 256), 256, 0, c.stream>>>(v_sys, c.flt.act.p, c.neq, v_mesh);
+  c.launches++;
+  GPZ_CUDA_TRY(cudaGetLastError());
+}
+void filter_zero_inactive(Ctx &c, double *f_mesh) {
+  k_flt_zero_inactive<<<grid_for(c.neq_mesh, 256), 256, 0, c.stream>>>(c.flt.dest.p, c.neq_mesh, f_mesh);
+  c.launches++;
+  GPZ_CUDA_TRY(cudaGetLastError());
+}
+void filter_values(Ctx &c) {
+  k_flt_gather<<<grid_for(c.nnz, 256), 256, 0, c.stream>>>(c.flt.m_a.p, c.flt.keep.p, c.nnz, c.d_a.p);
+  c.launches++;
+  GPZ_CUDA_TRY(cudaGetLastError());
 }
 
 void build_element_offsets(Ctx &c) {

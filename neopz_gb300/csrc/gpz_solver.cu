@@ -1681,7 +1681,7 @@ void spmv_device(Ctx &c, const double *x, double *y, double alpha, double beta, 
 // blocks (one per pair of shapes) whenever every connect block holds whole
 // shapes, i.e. its size is a multiple of 3 (hp connects carry several shapes).
 bool blocks_are_3(const Ctx &c) {
-  if (c.nstate != 3 || c.neq == 0) return false;
+  if (c.nstate != 3 || c.neq == 0 || c.flt.active) return false;  // a filter may split the connect blocks
   for (int32_t s : c.h_block_size)
     if (s % 3 != 0) return false;
   return true;
@@ -1986,7 +1986,8 @@ void make_fp32_copy(Ctx &c, int variant) {
 
 void build_block_jacobi(Ctx &c) {
   // per-shape 3x3 blocks: the connect blocks of TPZBlockDiagonal when every connect carries one shape
-  GPZ_REQUIRE(blocks_are_3(c), GPZ_E_INVALID, "block Jacobi needs 3 states per shape (nstate 3)");
+  GPZ_REQUIRE(blocks_are_3(c), GPZ_E_INVALID,
+              "block Jacobi needs 3 states per shape (nstate 3) and no equation filter");
   const int64_t nb = c.neq / 3;
   c.d_bjinv.alloc((size_t)nb * 9);
   k_block_inv3<<<grid_for(nb, 256), 256, 0, c.stream>>>(c.d_a.p, c.d_diagpos.p, nb, c.d_bjinv.p, c.d_err.p);
@@ -2212,6 +2213,7 @@ int solve_gmres(Ctx &c, const gpz_solver_opts &o, gpz_solve_report &rep) {
 // meets the tolerance) r is replaced by b - A64 x in FP64, and the solve stops
 // only on that true residual.
 int solve_learned(Ctx &c, const gpz_solver_opts &o, gpz_solve_report &rep, bool mixed) {
+  GPZ_REQUIRE(!c.flt.active, GPZ_E_INVALID, "learned preconditioner: not available under an equation filter");
   if (mixed && (!c.have_a32 || (o.spmv_variant >= 0 && c.have_bsr3 && o.spmv_variant != c.spmv32_variant)))
     make_fp32_copy(c, o.spmv_variant);
   learned_prepare(c);

@@ -108,6 +108,7 @@ def lib():
         L.gpz_tuning_report.argtypes = [vp, ctypes.c_char_p, i64]
         L.gpz_assemble.argtypes = [vp, i32]
         L.gpz_set_killed.argtypes = [vp, i32]
+        L.gpz_equation_filter.argtypes = [vp, i64, vp]
         L.gpz_matrix_download.argtypes = [vp, vp]
         L.gpz_rhs_download.argtypes = [vp, vp]
         L.gpz_rhs_upload.argtypes = [vp, vp]
@@ -276,7 +277,8 @@ class Context:
     def upload_mesh(self, grid):
         self._grid = grid
         self._check(lib().gpz_mesh_upload(self.h, ctypes.byref(grid.desc)))
-        self.neq = grid.neq
+        self.neq = grid.neq       # equations of the system (the active ones under an equation filter)
+        self.neq_mesh = grid.neq  # equations of the mesh
         self.nel = grid.nel
 
     def build_pattern(self, sym):
@@ -321,8 +323,20 @@ class Context:
         self._check(lib().gpz_matrix_download(self.h, _p(a)))
         return a
 
+    def equation_filter(self, active=None):
+        """TPZEquationFilter::SetActiveEquations (active: mesh equation numbers) or Reset (None); call before
+        build_pattern.  The system then has the active equations in increasing order."""
+        if active is None:
+            self._check(lib().gpz_equation_filter(self.h, -1, None))
+            self.neq = self.neq_mesh
+            return
+        a = np.ascontiguousarray(active, np.int64)
+        self._check(lib().gpz_equation_filter(self.h, len(a), _p(a)))
+        self.neq = len(np.unique(a))
+
     def rhs(self):
-        f = np.zeros(self.neq)
+        """The load vector over the mesh equations (zeros at inactive ones under an equation filter)."""
+        f = np.zeros(self.neq_mesh)
         self._check(lib().gpz_rhs_download(self.h, _p(f)))
         return f
 

@@ -253,6 +253,33 @@ def cg_jacobi(sym, ia, ja, a, b, maxit, tol, jacobi_residual=False, history=Fals
     return out
 
 
+def filter_system(sym, ia, ja, a, f, active):
+    """An equation filter (TPZEquationFilter::SetActiveEquations, StrMatrix/TPZEquationFilter.h) applied as the
+    reference applies it to an assembled system: TPZSSpStructMatrix / TPZSpStructMatrix::SetupMatrixData
+    (StrMatrix/TPZSSpStructMatrix.cpp:49-193, StrMatrix/TPZSpStructMatrix.cpp:53-190) keep the rows and
+    columns of active equations, renumbered in increasing order (fDestIndices); the filtered AddKel drops every
+    element entry with an inactive row or column (TPZEquationFilter::Filter), so the condensed values are the
+    mesh-level ones at the kept positions; the load vector assembled over the active equations is scattered
+    back to the mesh's size with zeros elsewhere (StrMatrix/pzstrmatrixor.cpp:43-71), and the solve takes its
+    gathered entries (Analysis/TPZLinearAnalysis.cpp:194).  Returns (ia, ja, a) of the condensed system, the
+    mesh-size load vector and the condensed one."""
+    n = len(ia) - 1
+    act = np.unique(np.asarray(active, np.int64))
+    dest = np.full(n, -1, np.int64)
+    dest[act] = np.arange(len(act))
+    ic, jc, vc = [0], [], []
+    for r in act:
+        cols = np.asarray(ja[ia[r]:ia[r + 1]])
+        keep = dest[cols] >= 0
+        jc.append(dest[cols[keep]])
+        vc.append(np.asarray(a[ia[r]:ia[r + 1]])[keep])
+        ic.append(ic[-1] + int(keep.sum()))
+    fm = np.array(f, np.float64)
+    fm[dest < 0] = 0.0
+    return (np.array(ic, np.int64), np.concatenate(jc).astype(np.int64), np.concatenate(vc), fm,
+            np.asarray(f, np.float64)[act])
+
+
 def jacobi(sym, ia, ja, a, b, maxit, tol, x0=None):
     """Stationary Jacobi (TPZStepSolver::SetJacobi as the solver); tol on the absolute ||b - A x||; x0 = the
     FromCurrent initial guess."""

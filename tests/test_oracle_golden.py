@@ -337,3 +337,26 @@ def test_oracle_jacobi_iteration():
     xs = np.linalg.solve(A, f)
     assert np.linalg.norm(conv["x"] - xs) <= 1e-6 * np.linalg.norm(xs)
     assert np.linalg.norm(f - A @ conv["x"]) <= 1.01 * tol
+
+
+def test_oracle_equation_filter():
+    """The oracle's equation filter against dense restrictions: the condensed full matrix is A[act][:, act], the
+    condensed upper pattern its upper triangle (rows still start at the diagonal), and the load vector keeps the
+    mesh's size with zeros at the inactive equations."""
+    om = O.poisson2d(4, 2)
+    rng = np.random.default_rng(8)
+    active = rng.choice(om.neq, size=om.neq - 11, replace=False)
+    act = np.sort(active)
+    for sym in (False, True):
+        ia, ja = om.pattern(sym)
+        a, f = om.assemble(sym, ia, ja)
+        ic, jc, vc, fm, fc = O.filter_system(sym, ia, ja, a, f, np.concatenate([active, active[:5]]))
+        n = len(act)
+        D = _dense(ia, ja, a, om.neq)
+        C = _dense(ic, jc, vc, n)
+        assert np.array_equal(C, D[np.ix_(act, act)])
+        for r in range(n):
+            row = jc[ic[r]:ic[r + 1]]
+            assert np.all(np.diff(row) > 0) and (not sym or row[0] == r)
+        assert np.array_equal(fc, f[act]) and np.all(fm[np.setdiff1d(np.arange(om.neq), act)] == 0.0)
+        assert np.array_equal(fm[act], f[act])
