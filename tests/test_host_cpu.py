@@ -85,3 +85,36 @@ def test_no_gpu_no_context(g):
     with pytest.raises(g.GpzError) as ei:
         g.Context(0)
     assert ei.value.code == -8  # GPZ_E_NO_DEVICE
+
+
+def _replica_rank(rank, world, port, q):
+    os.environ.update(MASTER_ADDR="127.0.0.1", MASTER_PORT=str(port), RANK=str(rank), WORLD_SIZE=str(world),
+                      LOCAL_RANK=str(rank))
+    import torch.distributed as dist
+    dist.init_process_group("gloo", rank=rank, world_size=world)
+    import bench
+    r, w, _ = bench.dist_info()
+    t = bench.max_over_ranks(1.0 + 0.5 * rank, w, "cpu")
+    dist.barrier()
+    dist.destroy_process_group()
+    q.put((r, w, t))
+
+
+def test_replica_timing_takes_the_slowest_rank():
+    """bench.py's N > 1 path (replicas, one system per rank, no data-path collective): the ranks read their
+    place from the torchrun environment and the job's step time is the slowest rank's; world size 2 over gloo."""
+    import socket
+    import torch.multiprocessing as mp
+    with socket.socket() as s:
+        s.bind(("127.0.0.1", 0))
+        port = s.getsockname()[1]
+    ctx = mp.get_context("spawn")
+    q = ctx.Queue()
+    ps = [ctx.Process(target=_replica_rank, args=(r, 2, port, q)) for r in range(2)]
+    for p in ps:
+        p.start()
+    out = sorted(q.get(timeout=120) for _ in ps)
+    for p in ps:
+        p.join(timeout=60)
+        assert p.exitcode == 0
+    assert out == [(0, 2, 1.5), (1, 2, 1.5)]
