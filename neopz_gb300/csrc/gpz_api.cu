@@ -205,6 +205,7 @@ int gpz_equation_filter(gpz_ctx *ctx, int64_t nactive, const int64_t *active) {
     }
     c.flt.active = nactive >= 0;
     c.flt.h_act.swap(v);
+    if (c.flt.active) filter_prepare(c);
     // another system: its pattern and values are built again
     c.neq = c.neq_mesh;
     c.have_pattern = false;

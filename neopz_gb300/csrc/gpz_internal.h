@@ -302,6 +302,7 @@ void build_pattern(Ctx &c);
 void build_upper(Ctx &c);
 void build_element_offsets(Ctx &c);
 void condense_pattern(Ctx &c);  // restrict the system to the equation filter's active set
+void filter_prepare(Ctx &c);    // the active set and the mesh -> condensed map on the device
 void filter_gather(Ctx &c, const double *v_mesh, double *v_sys);
 void filter_scatter(Ctx &c, const double *v_sys, double *v_mesh);
 void filter_zero_inactive(Ctx &c, double *f_mesh);

@@ -372,6 +372,20 @@ void build_upper(Ctx &c) {
   GPZ_CUDA_TRY(cudaStreamSynchronize(s));
 }
 
+// the active set and the mesh -> condensed map on the device (set when the
+// filter is given, so that a load-vector-only assembly can use them too)
+void filter_prepare(Ctx &c) {
+  auto &F = c.flt;
+  const int64_t n = (int64_t)F.h_act.size();
+  cudaStream_t s = c.stream;
+  F.act.upload(F.h_act.data(), n, s);
+  F.dest.alloc(c.neq_mesh);
+  GPZ_CUDA_TRY(cudaMemsetAsync(F.dest.p, 0xff, c.neq_mesh * sizeof(int64_t), s));  // -1
+  k_flt_dest<<<grid_for(n, 256), 256, 0, s>>>(F.act.p, n, F.dest.p);
+  c.launches++;
+  GPZ_CUDA_TRY(cudaGetLastError());
+}
+
 template <class T>
 static void swap_buf(DBuf<T> &a, DBuf<T> &b) {
   std::swap(a.p, b.p);
@@ -389,15 +403,12 @@ void condense_pattern(Ctx &c) {
   swap_buf(c.d_ja, F.m_ja);
   swap_buf(c.d_diagpos, F.m_diagpos);
   F.m_nnz = c.nnz;
-  F.act.upload(F.h_act.data(), n, s);
-  F.dest.alloc(c.neq_mesh);
-  GPZ_CUDA_TRY(cudaMemsetAsync(F.dest.p, 0xff, c.neq_mesh * sizeof(int64_t), s));  // -1
-  k_flt_dest<<<grid_for(n, 256), 256, 0, s>>>(F.act.p, n, F.dest.p);
+  filter_prepare(c);
   DBuf<int64_t> rowlen;
   rowlen.alloc(n + 1);
   rowlen.zero(s);
   k_flt_count<<<grid_for(n, 256), 256, 0, s>>>(F.m_ia.p, F.m_ja.p, F.act.p, F.dest.p, n, rowlen.p);
-  c.launches += 2;
+  c.launches++;
   GPZ_CUDA_TRY(cudaGetLastError());
   c.d_ia.alloc(n + 1);
   exclusive_scan_i64(rowlen.p, c.d_ia.p, n + 1, s, c);

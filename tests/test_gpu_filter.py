@@ -83,6 +83,14 @@ def test_filter_error_norms_reset_and_refusals(built):
     ctx.upload_mesh(grid)
     active = np.arange(0, om.neq, 2)
     ctx.equation_filter(active)
+    # the load vector alone, before any pattern: zeros at the inactive equations
+    assert ctx.assemble_rhs() == g.GPZ_OK
+    oia, oja = om.pattern(True)
+    _, of = om.assemble(True, oia, oja)
+    fm = of.copy()
+    fm[1::2] = 0.0
+    f0 = ctx.rhs()
+    assert np.all(f0[1::2] == 0.0) and np.max(np.abs(f0 - fm)) <= 1e-12 * np.max(np.abs(fm))
     ctx.build_pattern(True)
     ctx.assemble()
     x = ctx.solve(tol=1e-10, max_iter=20000)["x"]
@@ -104,7 +112,6 @@ def test_filter_error_norms_reset_and_refusals(built):
     ctx.equation_filter(None)
     ctx.build_pattern(True)
     ia, ja = ctx.pattern()
-    oia, oja = om.pattern(True)
     assert np.array_equal(ia, oia) and np.array_equal(ja, oja) and ctx.neq == om.neq
     ctx.assemble()
     r = ctx.solve(tol=1e-10, max_iter=20000)
