@@ -122,6 +122,21 @@ int64_t gpz_kernel_launches(gpz_ctx *ctx);
  * (TPZStructMatrix::ComputeElementColors, StrMatrix/TPZStructMatrix.cpp:104-161). */
 int gpz_mesh_upload(gpz_ctx *ctx, const gpz_mesh_desc *desc);
 
+/* ---- bandwidth / profile reduction ------------------------------------------
+ * Replaces TPZSloanRenumbering::Resequence (External/TPZSloanRenumbering.cpp:
+ * 23-175), the renumbering TPZAnalysis::OptimizeBandwidth applies before
+ * assembling (Analysis/TPZAnalysis.cpp:228-300), with the same permutation.
+ * Host code: the algorithm is one sequential greedy front; it needs no context
+ * and no GPU.  Inputs are TPZCompMesh::ComputeElGraph's lists
+ * (Mesh/pzcmesh.cpp:1214-1262): elgraphindex[nel+1] offsets into elgraph, the
+ * independent connect sequence numbers of each element, nnodes of them.
+ * Outputs: perm_gather[old sequence number] = new one (the vector
+ * TPZCompMesh::Permute takes) and perm_scatter[k] = the connect numbered k.
+ * GPZ_E_INVALID for an index out of range or a graph that is not connected
+ * (the reference stops there as well); nnodes = 0 returns GPZ_OK untouched. */
+int gpz_sloan_resequence(int64_t nnodes, int64_t nel, const int64_t *elgraphindex, const int64_t *elgraph,
+                         int64_t *perm_gather, int64_t *perm_scatter);
+
 /* ---- equation filter ----------------------------------------------------
  * Replaces TPZEquationFilter::SetActiveEquations / Reset
  * (StrMatrix/TPZEquationFilter.h) on the structural matrix.  Call after

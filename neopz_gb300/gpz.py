@@ -109,6 +109,7 @@ def lib():
         L.gpz_assemble.argtypes = [vp, i32]
         L.gpz_set_killed.argtypes = [vp, i32]
         L.gpz_equation_filter.argtypes = [vp, i64, vp]
+        L.gpz_sloan_resequence.argtypes = [i64, i64, vp, vp, vp, vp]
         L.gpz_matrix_download.argtypes = [vp, vp]
         L.gpz_rhs_download.argtypes = [vp, vp]
         L.gpz_rhs_upload.argtypes = [vp, vp]
@@ -216,6 +217,43 @@ class Grid:
     def nodes(self):
         """Node coordinates [nnodes][3] of the descriptor (a writable view: edit before upload_mesh)."""
         return np.ctypeslib.as_array(self.desc.node_xyz, shape=(self.desc.nnodes, 3))
+
+    def element_graph(self):
+        """TPZCompMesh::ComputeElGraph of the descriptor: (elgraphindex [nel+1], elgraph), the connects of every
+        element (boundary elements included)."""
+        d = self.desc
+        types = np.ctypeslib.as_array(d.el_type, shape=(d.nel,))
+        conn = np.ctypeslib.as_array(d.el_conn, shape=(d.nel * 27,))
+        ns = np.array([0, 3, 9, 27])[types]
+        idx = np.concatenate([[0], np.cumsum(ns)]).astype(np.int64)
+        g = np.concatenate([conn[e * 27:e * 27 + ns[e]] for e in range(d.nel)]) if d.nel else np.zeros(0)
+        return idx, g.astype(np.int64)
+
+    def permute_connects(self, perm_gather):
+        """TPZCompMesh::Permute (Mesh/pzcmesh.cpp:1399-1460) on the descriptor: connect s gets sequence number
+        perm_gather[s]; block sizes, orders and positions follow.  Returns old -> new equation map."""
+        d = self.desc
+        nc, nel = d.nconnects, d.nel
+        perm = np.asarray(perm_gather, np.int64)
+        size = np.ctypeslib.as_array(d.block_size, shape=(nc,)).copy()
+        order = np.ctypeslib.as_array(d.conn_order, shape=(nc,)).copy()
+        pos = np.ctypeslib.as_array(d.block_pos, shape=(nc,)).copy()
+        new_size, new_order = np.empty_like(size), np.empty_like(order)
+        new_size[perm] = size
+        new_order[perm] = order
+        new_pos = np.concatenate([[0], np.cumsum(new_size)[:-1]]).astype(np.int64)
+        np.ctypeslib.as_array(d.block_size, shape=(nc,))[:] = new_size
+        np.ctypeslib.as_array(d.conn_order, shape=(nc,))[:] = new_order
+        np.ctypeslib.as_array(d.block_pos, shape=(nc,))[:] = new_pos
+        conn = np.ctypeslib.as_array(d.el_conn, shape=(nel * 27,))
+        types = np.ctypeslib.as_array(d.el_type, shape=(nel,))
+        for e in range(nel):
+            ns = (0, 3, 9, 27)[int(types[e])]
+            conn[e * 27:e * 27 + ns] = perm[conn[e * 27:e * 27 + ns]]
+        eqmap = np.empty(d.neq, np.int64)
+        for c in range(nc):
+            eqmap[pos[c]:pos[c] + size[c]] = new_pos[perm[c]] + np.arange(size[c])
+        return eqmap
 
     def cells(self):
         """Grid cell of every element (-1 for boundary elements)."""
@@ -460,6 +498,18 @@ class Context:
 # ---------------------------------------------------------------------------
 # Synthetic workloads (the user programs of the reference's configurations).
 # ---------------------------------------------------------------------------
+def sloan_resequence(nnodes, elgraphindex, elgraph):
+    """TPZSloanRenumbering::Resequence on the host (gpz_sloan_resequence): (perm_gather, perm_scatter)."""
+    ei = np.ascontiguousarray(elgraphindex, np.int64)
+    eg = np.ascontiguousarray(elgraph, np.int64)
+    g = np.zeros(nnodes, np.int64)
+    s = np.zeros(nnodes, np.int64)
+    rc = lib().gpz_sloan_resequence(nnodes, len(ei) - 1, _p(ei), _p(eg), _p(g), _p(s))
+    if rc != GPZ_OK:
+        raise GpzError(rc, lib().gpz_get_error_string(rc).decode())
+    return g, s
+
+
 def poisson_square_quadratic(n, p):
     """[-1, 1]^2 in n x n quads of order p, -lap u = 4 - 2x^2 - 2y^2 (pOrder 2), u = 0 penalty Dirichlet: the
     error known-answer problem of UnitTest_PZ/TestMesh/TestError.cpp:43-160 (there on triangles), whose exact

@@ -92,6 +92,8 @@ def lib():
         L.orc_cg_jacobi.argtypes = [i64, i32, vp, vp, vp, vp, vp, i64, dp, i32, P(i64), P(dp), vp]
         L.orc_jacobi.restype = i32
         L.orc_jacobi.argtypes = [i64, i32, vp, vp, vp, vp, vp, i64, dp, i32, P(i64), P(dp)]
+        L.orc_sloan.restype = i32
+        L.orc_sloan.argtypes = [i64, i64, vp, vp, vp, vp]
         L.orc_cg_block_jacobi.restype = i32
         L.orc_cg_block_jacobi.argtypes = [i64, i32, vp, vp, vp, vp, vp, i32, i64, dp, P(i64), P(dp)]
         L.orc_error_points.restype = i64
@@ -251,6 +253,16 @@ def cg_jacobi(sym, ia, ja, a, b, maxit, tol, jacobi_residual=False, history=Fals
     if history:
         out["hist"] = hist[: it.value].copy()
     return out
+
+
+def sloan(nnodes, elgraphindex, elgraph):
+    """TPZSloanRenumbering::Resequence as the reference runs it: (rc, perm_gather, perm_scatter)."""
+    ei = np.ascontiguousarray(elgraphindex, np.int64)
+    eg = np.ascontiguousarray(elgraph, np.int64)
+    g = np.zeros(nnodes, np.int64)
+    sc = np.zeros(nnodes, np.int64)
+    rc = lib().orc_sloan(nnodes, len(ei) - 1, _p(ei), _p(eg), _p(g), _p(sc))
+    return rc, g, sc
 
 
 def filter_system(sym, ia, ja, a, f, active):

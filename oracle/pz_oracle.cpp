@@ -1524,6 +1524,155 @@ int orc_jacobi(int64_t n, int sym, const int64_t *IA, const int64_t *JA, const d
   return res <= tol ? 0 : 1;
 }
 
+// Sloan renumbering as the reference runs it: TPZSloanRenumbering::Resequence
+// (External/TPZSloanRenumbering.cpp:23-175) over the node graph of
+// TPZRenumbering::ConvertGraph (External/TPZRenumbering.cpp:76-105), with the
+// pseudo-peripheral pair of TPZCutHillMcKee::SGraph (External/TPZCutHillMcKee.cpp:
+// 16-30, 93-119, 121-260), the SList queue (External/TPZSloanRenumbering.h:20-86:
+// append once ever, remove by moving the last entry into the hole) and
+// FindHighestPriority's scan for the first entry of largest priority
+// (TPZSloanRenumbering.cpp:177-192).  Weights W1 = 1, W2 = 2.  Returns 0, or 1
+// when not every node is reached (the reference stops there).
+int orc_sloan(int64_t nnodes, int64_t nel, const int64_t *eptr, const int64_t *eg, int64_t *perm_gather,
+              int64_t *perm_scatter) {
+  // node graph: std::set of the element lists through each node, self erased
+  std::vector<std::vector<int64_t>> n2e(nnodes);
+  for (int64_t e = 0; e < nel; e++)
+    for (int64_t k = eptr[e]; k < eptr[e + 1]; k++) n2e[eg[k]].push_back(e);
+  std::vector<int64_t> gptr(nnodes + 1, 0), gadj;
+  for (int64_t v = 0; v < nnodes; v++) {
+    std::set<int64_t> con;
+    for (int64_t e : n2e[v]) con.insert(eg + eptr[e], eg + eptr[e + 1]);
+    con.erase(v);
+    gadj.insert(gadj.end(), con.begin(), con.end());
+    gptr[v + 1] = (int64_t)gadj.size();
+  }
+  auto degree = [&](int64_t v) { return gptr[v + 1] - gptr[v]; };
+  // RootedLevelStructure: each level from GetAdjacentNodes(previous level, processed)
+  auto levels = [&](int64_t root) {
+    std::vector<std::vector<int64_t>> L;
+    std::vector<int64_t> processed(nnodes, 0), level{root};
+    for (int64_t il = 0; il < nnodes && !level.empty(); il++) {
+      for (int64_t v : level) processed[v] = 1;
+      L.push_back(level);
+      std::vector<int64_t> next, history(nnodes, 0);
+      for (int64_t p : L.back())
+        for (int64_t k = gptr[p]; k < gptr[p + 1]; k++) {
+          const int64_t v = gadj[k];
+          if (processed[v] == 0 && history[v] == 0) {
+            next.push_back(v);
+            history[v] = 1;
+          }
+        }
+      level = next;
+    }
+    return L;
+  };
+  // PseudoPeripheralNodes
+  int64_t mindeg = 1000000, start = -1, end = -1;
+  for (int64_t v = 0; v < nnodes; v++)
+    if (degree(v) < mindeg) {
+      mindeg = degree(v);
+      start = v;
+    }
+  if (start < 0) return 1;
+  std::vector<std::vector<int64_t>> LS = levels(start);
+  int64_t count = 0;
+  while (count < 10 || end == -1) {
+    count++;
+    const int64_t cps = start, cpe = end;
+    const int64_t nlev = (int64_t)LS.size();
+    if (!nlev) break;
+    std::vector<int64_t> last = LS[nlev - 1];
+    const int64_t nelsOrig = (int64_t)last.size();
+    std::multimap<int64_t, int64_t> bydeg;  // SortNodes
+    for (int64_t v : last) bydeg.insert(std::make_pair(degree(v), v));
+    last.clear();
+    for (auto &kv : bydeg) last.push_back(kv.second);
+    std::map<int64_t, int64_t> shrink;  // ShrinkLastLevel
+    for (int64_t v : last) shrink[degree(v)] = v;
+    last.clear();
+    for (auto &kv : shrink) last.push_back(kv.second);
+    const int64_t newsize = (nelsOrig + 2) / 2;
+    if (newsize < (int64_t)last.size()) last.resize(newsize);
+    int64_t we = 1000000000L, hs = nlev;
+    for (int64_t q : last) {
+      std::vector<std::vector<int64_t>> loc = levels(q);
+      const int64_t h = (int64_t)loc.size();
+      int64_t w = 0;
+      for (auto &l : loc) w = std::max<int64_t>(w, (int64_t)l.size());
+      if (h > hs && w < we) {
+        start = q;
+        LS = loc;
+        break;
+      } else if (w < we) {
+        end = q;
+        we = w;
+      }
+    }
+    if (cps == start && cpe == end) break;
+  }
+  if (start < 0 || end < 0) return 1;
+  std::vector<int64_t> dist(nnodes, -1);
+  std::vector<std::vector<int64_t>> LE = levels(end);
+  for (int64_t l = 0; l < (int64_t)LE.size(); l++)
+    for (int64_t v : LE[l]) dist[v] = l;
+  for (int64_t v = 0; v < nnodes; v++)
+    if (dist[v] < 0) return 1;
+  const int64_t W1 = 1, W2 = 2;
+  std::vector<int64_t> priority(nnodes);
+  for (int64_t i = 0; i < nnodes; i++) priority[i] = W1 * dist[i] - W2 * (degree(i) + 1);
+  enum { EInactive = 0, EPreActive = 1, EActive = 2, EPostActive = 3 };
+  std::vector<int> status(nnodes, EInactive);
+  std::vector<int64_t> qlist(nnodes), hist(nnodes, 0);
+  int64_t qsize = 0, nr = 0;
+  auto push_back = [&](int64_t v) {
+    if (hist[v]) return false;
+    hist[v] = 1;
+    qlist[qsize++] = v;
+    return true;
+  };
+  status[start] = EPreActive;
+  push_back(start);
+  while (qsize) {
+    int64_t index = 0, cur = qlist[0], np = priority[cur];
+    for (int64_t i = 1; i < qsize; i++)
+      if (priority[qlist[i]] > np) {
+        cur = qlist[i];
+        np = priority[cur];
+        index = i;
+      }
+    qlist[index] = qlist[qsize - 1];
+    qsize--;
+    if (status[cur] == EPreActive) {
+      for (int64_t k = gptr[cur]; k < gptr[cur + 1]; k++) {
+        const int64_t a = gadj[k];
+        priority[a] += W2;
+        if (push_back(a) == true && status[a] == EInactive) status[a] = EPreActive;
+      }
+    }
+    perm_scatter[nr++] = cur;
+    status[cur] = EPostActive;
+    for (int64_t k = gptr[cur]; k < gptr[cur + 1]; k++) {
+      const int64_t a = gadj[k];
+      if (status[a] != EPreActive) continue;
+      status[a] = EActive;
+      priority[a] += W2;
+      for (int64_t j = gptr[a]; j < gptr[a + 1]; j++) {
+        const int64_t q = gadj[j];
+        if (status[q] != EPostActive) {
+          const int pr = (int)priority[q];
+          priority[q] = pr + W2;
+        }
+        if (push_back(q) == true && status[q] == EInactive) status[q] = EPreActive;
+      }
+    }
+  }
+  if (nr != nnodes) return 1;
+  for (int64_t i = 0; i < nnodes; i++) perm_gather[perm_scatter[i]] = i;
+  return 0;
+}
+
 // CG with a block-Jacobi preconditioner over consecutive equation blocks of
 // size bs (TPZBlockDiagonal, Matrix/pzblockdiag.h:21, built over the mesh's
 // connect blocks as TPZAnalysis::BuildPreconditioner(EBlockJacobi) does for

@@ -1,6 +1,6 @@
 """The GPU path consumes whatever connect numbering the host mesh holds (the reference renumbers connects with
 TPZAnalysis::OptimizeBandwidth / TPZSloanRenumbering before it assembles, Analysis/TPZAnalysis.cpp:228-300):
-with the connects of the same mesh renumbered at random, the pattern, matrix, load vector and solution are those
+with the connects of the same mesh renumbered at random or by gpz_sloan_resequence, the pattern, matrix, load vector and solution are those
 of the original numbering permuted -- the pattern exactly, values and load vector within 1e-12, solutions within
 1e-8.  The original numbering is pinned to the oracle by the parity tests.
 """
@@ -28,14 +28,14 @@ def _arr(ptr, n):
     return np.ctypeslib.as_array(ptr, shape=(n,))
 
 
-def _renumber(grid, rng):
-    """Renumber the connects of grid's descriptor in place; returns old -> new equation map."""
+def _renumber(grid, perm):
+    """Renumber the connects of grid's descriptor in place (connect c gets number perm[c]); returns old -> new
+    equation map."""
     d = grid.desc
     nc, nel = d.nconnects, d.nel
     size = _arr(d.block_size, nc).copy()
     order = _arr(d.conn_order, nc).copy()
     pos = _arr(d.block_pos, nc).copy()
-    perm = rng.permutation(nc)  # old connect -> new connect
     new_size = np.empty_like(size)
     new_order = np.empty_like(order)
     new_size[perm] = size
@@ -74,8 +74,10 @@ def _system(g, grid, sym):
     return ia, ja, a, f, x
 
 
+@pytest.mark.parametrize("kind", ["random", "sloan"])
 @pytest.mark.parametrize("case", ["elast3d_p2", "elast3d_hp", "darcy2d_p3"])
-def test_renumbered_connects_give_the_permuted_system(built, case):
+def test_renumbered_connects_give_the_permuted_system(built, case, kind):
+    """kind "sloan": the permutation TPZAnalysis::OptimizeBandwidth applies (gpz_sloan_resequence)."""
     g = _gpz()
     rng = np.random.default_rng(21)
     E = np.exp(rng.standard_normal(27))
@@ -84,7 +86,16 @@ def test_renumbered_connects_give_the_permuted_system(built, case):
             "elast3d_hp": lambda: g.elasticity3d_hp(3, g.hp_orders(27, 3), E=E),
             "darcy2d_p3": lambda: g.darcy(2, 6, 3, k)}[case]
     base, moved = make(), make()
-    eqmap = _renumber(moved, np.random.default_rng(5))
+    nc = moved.desc.nconnects
+    if kind == "random":
+        perm = np.random.default_rng(5).permutation(nc)
+    else:
+        ei, eg = moved.element_graph()
+        perm = g.sloan_resequence(nc, ei, eg)[0]
+        eqmap_helper = make().permute_connects(perm)  # the Python helper gives the same equation map
+    eqmap = _renumber(moved, perm)
+    if kind == "sloan":
+        assert np.array_equal(eqmap, eqmap_helper)
     n = base.neq
     for sym in (False, True):
         ia, ja, a, f, x = _system(g, base, sym)
