@@ -53,6 +53,7 @@ def parse():
     ap.add_argument("--no-hp", action="store_true", help="skip the hp (uneven-order) assembly leg")
     ap.add_argument("--hp-n", type=int, default=40, help="hexes per direction of the hp leg")
     ap.add_argument("--no-poisson3d", action="store_true", help="skip the 3D scalar (64^3 Q2 Darcy) leg")
+    ap.add_argument("--no-sloan", action="store_true", help="skip the host Sloan renumbering leg")
     ap.add_argument("--spmv-variant", type=int, default=-1,
                     help="FP32 operator of the mixed solves: -1 autotuned, else the gpz_solver_opts spmv_variant")
     ap.add_argument("--path", default="learned", choices=["learned", "mixed"],
@@ -391,6 +392,8 @@ def run_gpu(args):
         out["learned_darcy2d"] = learned_leg(gpz, dev)
     if rank == 0 and not args.no_hp:
         out["hp_elasticity"] = hp_leg(gpz, dev, args.hp_n)
+    if rank == 0 and not args.no_sloan:
+        out["sloan_renumbering"] = sloan_leg(gpz, n)
     if rank == 0 and not args.no_poisson3d:
         out["poisson3d"] = poisson3d_leg(gpz, dev)
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
@@ -425,6 +428,31 @@ def hp_leg(gpz, dev, n=40):
             "elements_per_s": grid.nel / (ms / 1e3), "batching": rep,
             "mixed_cg": {"iterations": sol["iterations"], "true_resid": sol["true_resid"], "seconds": sol["seconds"],
                          "rc": sol["rc"]}}
+
+
+def sloan_leg(gpz, n):
+    """TPZAnalysis::OptimizeBandwidth's Sloan renumbering (gpz_sloan_resequence, host code) of the benchmark
+    mesh's connect graph; the profile of the connect graph before and after."""
+    try:
+        grid = gpz.elasticity3d(n, 2)
+        ei, eg = grid.element_graph()
+        nn = grid.desc.nconnects
+        t0 = time.perf_counter()
+        pg, _ = gpz.sloan_resequence(nn, ei, eg)
+        dt = time.perf_counter() - t0
+
+        def envelope(perm):
+            low = np.arange(nn)
+            for e in range(len(ei) - 1):
+                p = perm[eg[ei[e]:ei[e + 1]]]
+                low[p] = np.minimum(low[p], p.min())
+            return int(np.sum(np.arange(nn) - low))
+
+        return {"workload": f"connect graph of the {n}^3 Q2 hex mesh (boundary elements included)", "connects": nn,
+                "seconds": round(dt, 3), "threads": 1, "envelope_creation_order": envelope(np.arange(nn)),
+                "envelope_sloan": envelope(pg)}
+    except Exception as exc:  # a host-side leg: report, do not stop the benchmark
+        return {"error": repr(exc)}
 
 
 def poisson3d_leg(gpz, dev, n=64):
