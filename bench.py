@@ -449,7 +449,8 @@ def sloan_leg(gpz, n):
             return int(np.sum(np.arange(nn) - low))
 
         return {"workload": f"connect graph of the {n}^3 Q2 hex mesh (boundary elements included)", "connects": nn,
-                "seconds": round(dt, 3), "threads": 1, "envelope_creation_order": envelope(np.arange(nn)),
+                "seconds": round(dt, 3), "graph_build_threads": min(16, os.cpu_count() or 1),
+                "numbering_threads": 1, "envelope_creation_order": envelope(np.arange(nn)),
                 "envelope_sloan": envelope(pg)}
     except Exception as exc:  # a host-side leg: report, do not stop the benchmark
         return {"error": repr(exc)}

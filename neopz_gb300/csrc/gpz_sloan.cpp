@@ -16,6 +16,7 @@
 #include <climits>
 #include <cstdint>
 #include <map>
+#include <thread>
 #include <vector>
 
 #include "../../include/gpz.h"
@@ -28,7 +29,9 @@ struct Graph {
   int64_t degree(int64_t v) const { return ptr[v + 1] - ptr[v]; }
 };
 
-// TPZRenumbering::ConvertGraph (External/TPZRenumbering.cpp:76-105)
+// TPZRenumbering::ConvertGraph (External/TPZRenumbering.cpp:76-105): every
+// node's list is built on its own (a count pass and a fill pass over node
+// ranges on the host threads), so the result does not depend on the threads
 bool convert_graph(int64_t nnodes, int64_t nel, const int64_t *eptr, const int64_t *eg, Graph &g) {
   std::vector<int64_t> cnt(nnodes + 1, 0);
   for (int64_t e = 0; e < nel; e++)
@@ -42,11 +45,13 @@ bool convert_graph(int64_t nnodes, int64_t nel, const int64_t *eptr, const int64
     for (int64_t k = eptr[e]; k < eptr[e + 1]; k++) n2e[fill[eg[k]]++] = e;
   g.n = nnodes;
   g.ptr.assign(nnodes + 1, 0);
-  g.adj.clear();
-  std::vector<int64_t> mark(nnodes, -1), nb;
-  for (int64_t v = 0; v < nnodes; v++) {
+  unsigned nt = std::thread::hardware_concurrency();
+  nt = std::max(1u, std::min(nt, 16u));
+  if (nnodes < 65536) nt = 1;
+  // one node's neighbours (self removed), unsorted, with a per-thread marker
+  auto neighbours = [&](int64_t v, std::vector<int64_t> &mark, std::vector<int64_t> &nb) {
     nb.clear();
-    mark[v] = v;  // self removed
+    mark[v] = v;
     for (int64_t k = cnt[v]; k < cnt[v + 1]; k++) {
       const int64_t e = n2e[k];
       for (int64_t j = eptr[e]; j < eptr[e + 1]; j++)
@@ -55,10 +60,28 @@ bool convert_graph(int64_t nnodes, int64_t nel, const int64_t *eptr, const int64
           nb.push_back(eg[j]);
         }
     }
+  };
+  auto run = [&](auto &&body) {
+    std::vector<std::thread> th;
+    for (unsigned t = 0; t < nt; t++)
+      th.emplace_back([&, t]() {
+        std::vector<int64_t> mark(nnodes, -1), nb;
+        const int64_t b = nnodes * t / nt, e = nnodes * (t + 1) / nt;
+        for (int64_t v = b; v < e; v++) body(v, mark, nb);
+      });
+    for (auto &x : th) x.join();
+  };
+  run([&](int64_t v, std::vector<int64_t> &mark, std::vector<int64_t> &nb) {
+    neighbours(v, mark, nb);
+    g.ptr[v + 1] = (int64_t)nb.size();
+  });
+  for (int64_t v = 0; v < nnodes; v++) g.ptr[v + 1] += g.ptr[v];
+  g.adj.assign(g.ptr[nnodes], 0);
+  run([&](int64_t v, std::vector<int64_t> &mark, std::vector<int64_t> &nb) {
+    neighbours(v, mark, nb);
     std::sort(nb.begin(), nb.end());
-    g.adj.insert(g.adj.end(), nb.begin(), nb.end());
-    g.ptr[v + 1] = (int64_t)g.adj.size();
-  }
+    std::copy(nb.begin(), nb.end(), g.adj.begin() + g.ptr[v]);
+  });
   return true;
 }
 
@@ -160,6 +183,19 @@ struct LeftMax {
       arg[i] = arg[l];
     }
   }
+  // an increase of one slot's value: walk up only while this slot wins
+  void raise(int64_t slot, int64_t v) {
+    int64_t i = size + slot;
+    val[i] = v;
+    for (i >>= 1; i >= 1; i >>= 1) {
+      if (arg[i] == slot || v > val[i] || (v == val[i] && slot < arg[i])) {
+        val[i] = v;
+        arg[i] = slot;
+      } else {
+        break;  // this subtree's winner is unchanged, so is everything above it
+      }
+    }
+  }
   void set(int64_t slot, int64_t v) {
     int64_t i = size + slot;
     val[i] = v;
@@ -204,13 +240,13 @@ extern "C" int gpz_sloan_resequence(int64_t nnodes, int64_t nel, const int64_t *
       hist[v] = 1;
       slot_node[qsize] = v;
       slot_of[v] = qsize;
-      tree.set(qsize, prio[v]);
+      tree.raise(qsize, prio[v]);  // from the empty value
       qsize++;
       return true;
     };
     auto bump = [&](int64_t v, int64_t by) {
       prio[v] += by;
-      if (slot_of[v] >= 0) tree.set(slot_of[v], prio[v]);
+      if (slot_of[v] >= 0) tree.raise(slot_of[v], prio[v]);  // priorities only grow
     };
     status[start] = kPreActive;
     push(start);
