@@ -239,7 +239,10 @@ int gpz_set_killed(gpz_ctx *ctx, int killed);
                                       always made) for a full one; tol is on the ABSOLUTE ||b - A x||,
                                       iterations = sweeps performed; precond must be 0 or JACOBI */
 #define GPZ_PRECOND_JACOBI 1       /* TPZMatrix::SolveJacobi, one sweep (Matrix/pzmatrix.cpp:643-667) */
-#define GPZ_PRECOND_BLOCK_JACOBI 2 /* connect blocks, TPZBlockDiagonal (Matrix/pzblockdiag.h:21) */
+#define GPZ_PRECOND_BLOCK_JACOBI 2 /* connect blocks, TPZBlockDiagonal (Matrix/pzblockdiag.h:21):
+                                      TPZAnalysis::BuildPreconditioner(EBlockJacobi, overlap = true)
+                                      (Analysis/TPZAnalysis.cpp:1073-1080) with its
+                                      TPZBlockDiagonalStructMatrix connect blocks */
 
 typedef struct {
   int32_t solver;          /* GPZ_SOLVER_* */
