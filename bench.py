@@ -53,7 +53,7 @@ def parse():
     ap.add_argument("--no-hp", action="store_true", help="skip the hp (uneven-order) assembly leg")
     ap.add_argument("--hp-n", type=int, default=40, help="hexes per direction of the hp leg")
     ap.add_argument("--no-poisson3d", action="store_true", help="skip the 3D scalar (64^3 Q2 Darcy) leg")
-    ap.add_argument("--no-sloan", action="store_true", help="skip the host Sloan renumbering leg")
+    ap.add_argument("--no-sloan", action="store_true", help="skip the host graph legs (Sloan renumbering, node-set blocks)")
     ap.add_argument("--spmv-variant", type=int, default=-1,
                     help="FP32 operator of the mixed solves: -1 autotuned, else the gpz_solver_opts spmv_variant")
     ap.add_argument("--path", default="learned", choices=["learned", "mixed"],
@@ -393,7 +393,7 @@ def run_gpu(args):
     if rank == 0 and not args.no_hp:
         out["hp_elasticity"] = hp_leg(gpz, dev, args.hp_n)
     if rank == 0 and not args.no_sloan:
-        out["sloan_renumbering"] = sloan_leg(gpz, n)
+        out["sloan_renumbering"], out["nodeset_blocks"] = sloan_leg(gpz, n)
     if rank == 0 and not args.no_poisson3d:
         out["poisson3d"] = poisson3d_leg(gpz, dev)
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
@@ -431,12 +431,17 @@ def hp_leg(gpz, dev, n=40):
 
 
 def sloan_leg(gpz, n):
-    """TPZAnalysis::OptimizeBandwidth's Sloan renumbering (gpz_sloan_resequence, host code) of the benchmark
-    mesh's connect graph; the profile of the connect graph before and after."""
+    """Host graph work on the benchmark mesh's connect graph: TPZAnalysis::OptimizeBandwidth's Sloan
+    renumbering (gpz_sloan_resequence) with the graph's profile before and after, and the node-set blocks of
+    BuildPreconditioner(EBlockJacobi, overlap = false) (gpz_nodeset_blocks) with their size histogram."""
     try:
         grid = gpz.elasticity3d(n, 2)
         ei, eg = grid.element_graph()
         nn = grid.desc.nconnects
+    except Exception as exc:  # a host-side leg: report, do not stop the benchmark
+        return {"error": repr(exc)}, {"error": repr(exc)}
+    workload = f"connect graph of the {n}^3 Q2 hex mesh (boundary elements included)"
+    try:
         t0 = time.perf_counter()
         pg, _ = gpz.sloan_resequence(nn, ei, eg)
         dt = time.perf_counter() - t0
@@ -448,12 +453,26 @@ def sloan_leg(gpz, n):
                 low[p] = np.minimum(low[p], p.min())
             return int(np.sum(np.arange(nn) - low))
 
-        return {"workload": f"connect graph of the {n}^3 Q2 hex mesh (boundary elements included)", "connects": nn,
-                "seconds": round(dt, 3), "graph_build_threads": min(16, os.cpu_count() or 1),
-                "numbering_threads": 1, "envelope_creation_order": envelope(np.arange(nn)),
-                "envelope_sloan": envelope(pg)}
-    except Exception as exc:  # a host-side leg: report, do not stop the benchmark
-        return {"error": repr(exc)}
+        sloan = {"workload": workload, "connects": nn,
+                 "seconds": round(dt, 3), "graph_build_threads": min(16, os.cpu_count() or 1),
+                 "numbering_threads": 1, "envelope_creation_order": envelope(np.arange(nn)),
+                 "envelope_sloan": envelope(pg)}
+    except Exception as exc:
+        sloan = {"error": repr(exc)}
+    try:
+        bp = np.ctypeslib.as_array(grid.desc.block_pos, shape=(nn,)).copy()
+        bs = np.ctypeslib.as_array(grid.desc.block_size, shape=(nn,)).copy()
+        t0 = time.perf_counter()
+        r = gpz.nodeset_blocks(nn, ei, eg, bp, bs, grid.neq)
+        dt = time.perf_counter() - t0
+        sizes, counts = np.unique(np.diff(r["blockindex"]), return_counts=True)
+        nodeset = {"workload": workload, "connects": nn, "equations": grid.neq, "seconds": round(dt, 3),
+                   "relation_threads": min(16, os.cpu_count() or 1), "numbering_threads": 1,
+                   "blocks": int(len(r["blockindex"]) - 1), "colors": r["ncolors"],
+                   "block_sizes": {str(int(k)): int(v) for k, v in zip(sizes, counts)}}
+    except Exception as exc:
+        nodeset = {"error": repr(exc)}
+    return sloan, nodeset
 
 
 def poisson3d_leg(gpz, dev, n=64):

@@ -137,6 +137,25 @@ int gpz_mesh_upload(gpz_ctx *ctx, const gpz_mesh_desc *desc);
 int gpz_sloan_resequence(int64_t nnodes, int64_t nel, const int64_t *elgraphindex, const int64_t *elgraph,
                          int64_t *perm_gather, int64_t *perm_scatter);
 
+/* ---- node-set blocks of the block-Jacobi preconditioner ----------------------
+ * Replaces the block construction of TPZAnalysis::BuildPreconditioner(
+ * EBlockJacobi, overlap = false) (Analysis/TPZAnalysis.cpp:1008-1085):
+ * TPZNodesetCompute::AnalyseGraph + BuildNodeGraph + ExpandGraph + ColorGraph
+ * (External/tpznodesetcompute.cpp:47-209, 528-607) over the node graph of
+ * TPZRenumbering::ConvertGraph.  Host code, no context and no GPU.  Inputs:
+ * ComputeElGraph's lists as for gpz_sloan_resequence (nnodes connects), and the
+ * mesh's TPZBlock: block_position / block_size of every connect, neq equations.
+ * Outputs, in the reference's order: nblocks equation blocks,
+ * blockindex[nblocks+1] offsets into blockeqs (capacities: nnodes + 1 and the
+ * sum of block_size), the blocks' colours (colors[nblocks], ncolors; blocks of
+ * disjoint connects never clash, so ncolors = 1), and, if non-NULL, every
+ * connect's sequence number and level (fSeqNumber / fLevel, nnodes each).
+ * GPZ_E_INVALID for an index or block out of range. */
+int gpz_nodeset_blocks(int64_t nnodes, int64_t nel, const int64_t *elgraphindex, const int64_t *elgraph,
+                       const int64_t *block_position, const int64_t *block_size, int64_t neq,
+                       int64_t *blockindex, int64_t *blockeqs, int64_t *nblocks, int *colors, int *ncolors,
+                       int64_t *seqnum, int *level);
+
 /* ---- equation filter ----------------------------------------------------
  * Replaces TPZEquationFilter::SetActiveEquations / Reset
  * (StrMatrix/TPZEquationFilter.h) on the structural matrix.  Call after

@@ -110,6 +110,7 @@ def lib():
         L.gpz_set_killed.argtypes = [vp, i32]
         L.gpz_equation_filter.argtypes = [vp, i64, vp]
         L.gpz_sloan_resequence.argtypes = [i64, i64, vp, vp, vp, vp]
+        L.gpz_nodeset_blocks.argtypes = [i64, i64, vp, vp, vp, vp, i64, vp, vp, _P(i64), vp, _P(i32), vp, vp]
         L.gpz_matrix_download.argtypes = [vp, vp]
         L.gpz_rhs_download.argtypes = [vp, vp]
         L.gpz_rhs_upload.argtypes = [vp, vp]
@@ -508,6 +509,29 @@ def sloan_resequence(nnodes, elgraphindex, elgraph):
     if rc != GPZ_OK:
         raise GpzError(rc, lib().gpz_get_error_string(rc).decode())
     return g, s
+
+
+def nodeset_blocks(nnodes, elgraphindex, elgraph, block_pos, block_size, neq):
+    """The node-set blocks of BuildPreconditioner(EBlockJacobi, overlap = false) on the host
+    (gpz_nodeset_blocks): dict of blockindex, blockeqs (the equations of each block), colors, ncolors and the
+    connects' seqnum / level."""
+    ei = np.ascontiguousarray(elgraphindex, np.int64)
+    eg = np.ascontiguousarray(elgraph, np.int64)
+    bp = np.ascontiguousarray(block_pos, np.int64)
+    bs = np.ascontiguousarray(block_size, np.int64)
+    bidx = np.zeros(nnodes + 1, np.int64)
+    beqs = np.zeros(max(int(bs.sum()), 1), np.int64)
+    cols = np.zeros(max(nnodes, 1), np.int32)
+    seq = np.zeros(max(nnodes, 1), np.int64)
+    lev = np.zeros(max(nnodes, 1), np.int32)
+    nb, nc = ctypes.c_int64(0), ctypes.c_int32(0)
+    rc = lib().gpz_nodeset_blocks(nnodes, len(ei) - 1, _p(ei), _p(eg), _p(bp), _p(bs), neq, _p(bidx), _p(beqs),
+                                  ctypes.byref(nb), _p(cols), ctypes.byref(nc), _p(seq), _p(lev))
+    if rc != GPZ_OK:
+        raise GpzError(rc, lib().gpz_get_error_string(rc).decode())
+    nb = nb.value
+    return dict(blockindex=bidx[:nb + 1], blockeqs=beqs[:bidx[nb]], colors=cols[:nb], ncolors=nc.value,
+                seqnum=seq[:nnodes], level=lev[:nnodes])
 
 
 def poisson_square_quadratic(n, p):

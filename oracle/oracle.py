@@ -95,6 +95,10 @@ def lib():
         L.orc_sloan.restype = i32
         L.orc_sloan.argtypes = [i64, i64, vp, vp, vp, vp]
         L.orc_cg_block_jacobi.restype = i32
+        L.orc_nodeset.restype = i32
+        L.orc_nodeset.argtypes = [i64, i64, vp, vp, vp, vp, i64, vp, vp, P(i64), vp, P(i32), vp, vp]
+        L.orc_cg_sparse_block_jacobi.restype = i32
+        L.orc_cg_sparse_block_jacobi.argtypes = [i64, i32, vp, vp, vp, vp, vp, i64, vp, vp, i64, dp, P(i64), P(dp)]
         L.orc_cg_block_jacobi.argtypes = [i64, i32, vp, vp, vp, vp, vp, i32, i64, dp, P(i64), P(dp)]
         L.orc_error_points.restype = i64
         L.orc_error_points.argtypes = [vp, i32, vp]
@@ -263,6 +267,39 @@ def sloan(nnodes, elgraphindex, elgraph):
     sc = np.zeros(nnodes, np.int64)
     rc = lib().orc_sloan(nnodes, len(ei) - 1, _p(ei), _p(eg), _p(g), _p(sc))
     return rc, g, sc
+
+
+def nodeset(nnodes, elgraphindex, elgraph, block_pos, block_size, neq):
+    """TPZNodesetCompute's blocks as BuildPreconditioner(EBlockJacobi, overlap = false) computes them:
+    (rc, dict of blockindex, blockeqs, colors, ncolors, seqnum, level)."""
+    ei = np.ascontiguousarray(elgraphindex, np.int64)
+    eg = np.ascontiguousarray(elgraph, np.int64)
+    bp = np.ascontiguousarray(block_pos, np.int64)
+    bs = np.ascontiguousarray(block_size, np.int64)
+    bidx = np.zeros(nnodes + 1, np.int64)
+    beqs = np.zeros(max(int(bs.sum()), 1), np.int64)
+    cols = np.zeros(max(nnodes, 1), np.int32)
+    seq = np.zeros(max(nnodes, 1), np.int64)
+    lev = np.zeros(max(nnodes, 1), np.int32)
+    nb, nc = ctypes.c_int64(0), ctypes.c_int32(0)
+    rc = lib().orc_nodeset(nnodes, len(ei) - 1, _p(ei), _p(eg), _p(bp), _p(bs), neq, _p(bidx), _p(beqs),
+                           ctypes.byref(nb), _p(cols), ctypes.byref(nc), _p(seq), _p(lev))
+    nb = nb.value
+    return rc, dict(blockindex=bidx[:nb + 1], blockeqs=beqs[:bidx[nb]], colors=cols[:nb], ncolors=nc.value,
+                    seqnum=seq[:nnodes], level=lev[:nnodes])
+
+
+def cg_sparse_block_jacobi(sym, ia, ja, a, b, blockindex, blockeqs, maxit, tol):
+    """CG preconditioned by LU solves of the given equation blocks (the TPZSparseBlockDiagonal step solver)."""
+    n = len(ia) - 1
+    x = np.zeros(n)
+    bi = np.ascontiguousarray(blockindex, np.int64)
+    be = np.ascontiguousarray(blockeqs, np.int64)
+    it, res = ctypes.c_int64(), ctypes.c_double()
+    rc = lib().orc_cg_sparse_block_jacobi(n, int(sym), _p(ia), _p(ja), _p(a), _p(np.ascontiguousarray(b)), _p(x),
+                                          len(bi) - 1, _p(bi), _p(be), maxit, tol, ctypes.byref(it),
+                                          ctypes.byref(res))
+    return dict(x=x, iters=it.value, resid=res.value, rc=rc)
 
 
 def filter_system(sym, ia, ja, a, f, active):

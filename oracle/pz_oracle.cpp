@@ -1826,4 +1826,242 @@ int orc_gmres_jacobi(int64_t n, int sym, const int64_t *IA, const int64_t *JA, c
   return 1;
 }
 
+// Node-set blocks as TPZAnalysis::BuildPreconditioner(EBlockJacobi, overlap =
+// false) computes them (Analysis/TPZAnalysis.cpp:1008-1085), restated as the
+// reference writes them: TPZNodesetCompute::AnalyseGraph / AnalyseNode
+// (External/tpznodesetcompute.cpp:47-188) on std::set copies of the closed
+// neighbourhoods, recomputed when cleared, includes() and operator!= per
+// neighbour, recursion into proper subsets, identical sets sharing the
+// sequence number; BuildNodeGraph (:190-209), ExpandGraph over the TPZBlock
+// (:528-562) and ColorGraph (:567-607).  The node graph is ConvertGraph's
+// (External/TPZRenumbering.cpp:76-105).  Returns 0, or 1 at the reference's
+// DebugStop (an identical set numbered apart).
+namespace orc {
+struct Nodeset {
+  const std::vector<int64_t> &ng, &ngi;
+  std::vector<int64_t> seq;
+  std::vector<int> level;
+  std::vector<char> included;
+  std::vector<int64_t> card;
+  int64_t maxseq = -1;
+  int maxlevel = -1;
+  bool ok = true;
+  Nodeset(const std::vector<int64_t> &g, const std::vector<int64_t> &gi)
+      : ng(g), ngi(gi), seq(gi.size() - 1, -1), level(gi.size() - 1, 0), included(gi.size() - 1, 0) {}
+  void fill(int64_t v, std::vector<std::set<int64_t>> &ns) {
+    if (ns[v].size()) return;
+    ns[v].insert(ng.begin() + ngi[v], ng.begin() + ngi[v + 1]);
+    ns[v].insert(v);
+  }
+  void analyse(int64_t node, std::vector<std::set<int64_t>> &ns) {
+    if (seq[node] != -1) return;
+    fill(node, ns);
+    int minlevel = 0;
+    std::vector<int64_t> equalnodes;
+    for (auto it = ns[node].begin(); it != ns[node].end(); ++it) {
+      const int64_t other = *it;
+      if (other == node) continue;
+      fill(other, ns);
+      const bool inc = std::includes(ns[node].begin(), ns[node].end(), ns[other].begin(), ns[other].end());
+      const bool diff = ns[node] != ns[other];
+      if (inc && diff) {
+        included[other] = 1;
+        analyse(other, ns);
+        minlevel = std::max(minlevel, level[other] + 1);
+      } else if (!diff) {
+        if (included[node]) included[other] = 1;
+        equalnodes.push_back(other);
+      }
+      if (inc && diff && seq[other] != -1) {
+        included[other] = 1;
+        minlevel = std::max(minlevel, level[other] + 1);
+      } else if (!diff && seq[other] != -1) {
+        minlevel = std::max(minlevel, level[other]);
+        ok = false;
+      }
+    }
+    maxseq++;
+    seq[node] = maxseq;
+    card.push_back(1);
+    maxlevel = std::max(maxlevel, minlevel);
+    level[node] = minlevel;
+    ns[node].erase(node);
+    for (auto it = ns[node].begin(); it != ns[node].end(); ++it) {
+      const int64_t other = *it;
+      if (seq[other] != -1 && level[other] <= minlevel) {
+        ns[other].clear();
+        if (other == node) { ok = false; break; }
+      }
+    }
+    ns[node].clear();
+    for (int64_t o : equalnodes) {
+      seq[o] = maxseq;
+      level[o] = minlevel;
+      ns[o].clear();
+      card[maxseq]++;
+    }
+  }
+};
+}  // namespace orc
+
+int orc_nodeset(int64_t nnodes, int64_t nel, const int64_t *eptr, const int64_t *eg, const int64_t *block_pos,
+                const int64_t *block_size, int64_t neq, int64_t *blockindex, int64_t *blockeqs, int64_t *nblocks,
+                int *colors, int *ncolors, int64_t *seqnum, int *level) {
+  std::vector<std::vector<int64_t>> n2e(nnodes);
+  for (int64_t e = 0; e < nel; e++)
+    for (int64_t k = eptr[e]; k < eptr[e + 1]; k++) n2e[eg[k]].push_back(e);
+  std::vector<int64_t> ngi(nnodes + 1, 0), ng;
+  for (int64_t v = 0; v < nnodes; v++) {
+    std::set<int64_t> con;
+    for (int64_t e : n2e[v]) con.insert(eg + eptr[e], eg + eptr[e + 1]);
+    con.erase(v);
+    ng.insert(ng.end(), con.begin(), con.end());
+    ngi[v + 1] = (int64_t)ng.size();
+  }
+  orc::Nodeset an(ng, ngi);
+  {
+    std::vector<std::set<int64_t>> ns(nnodes);
+    for (int64_t in = 0; in < nnodes; in++) an.analyse(in, ns);
+  }
+  if (!an.ok) return 1;
+  // BuildNodeGraph
+  const int64_t nseq = (int64_t)an.card.size();
+  std::vector<int64_t> bgi(nseq + 1, 0), bg(nnodes);
+  if (nseq >= 1) bgi[1] = 0;
+  for (int64_t s = 2; s <= nseq; s++) bgi[s] = bgi[s - 1] + an.card[s - 2];
+  for (int64_t in = 0; in < nnodes; in++) {
+    const int64_t sn = an.seq[in];
+    bg[bgi[sn + 1]] = in;
+    bgi[sn + 1]++;
+  }
+  // ExpandGraph
+  int64_t counter = 0, blcounter = 0;
+  std::vector<int64_t> egi(nseq + 1, 0);
+  std::vector<int64_t> expg;
+  for (int64_t ibl = 0; ibl < nseq; ibl++) {
+    for (int64_t ieq = bgi[ibl]; ieq < bgi[ibl + 1]; ieq++) {
+      const int64_t bsz = block_size[bg[ieq]], pos = block_pos[bg[ieq]];
+      for (int64_t b = 0; b < bsz; b++) { expg.push_back(pos + b); counter++; }
+    }
+    if (egi[blcounter] != counter) egi[++blcounter] = counter;
+  }
+  // ColorGraph
+  std::vector<int> eqcolor(neq), col(blcounter, -1);
+  int color = 0;
+  bool hasuncolored = true;
+  while (hasuncolored) {
+    hasuncolored = false;
+    std::fill(eqcolor.begin(), eqcolor.end(), -1);
+    for (int64_t ibl = 0; ibl < blcounter; ibl++) {
+      if (col[ibl] != -1) continue;
+      int64_t ieq;
+      for (ieq = egi[ibl]; ieq < egi[ibl + 1]; ieq++)
+        if (eqcolor[expg[ieq]] == color) break;
+      if (ieq != egi[ibl + 1]) {
+        hasuncolored = true;
+      } else {
+        col[ibl] = color;
+        for (ieq = egi[ibl]; ieq < egi[ibl + 1]; ieq++) eqcolor[expg[ieq]] = color;
+      }
+    }
+    color++;
+  }
+  *nblocks = blcounter;
+  std::copy(egi.begin(), egi.begin() + blcounter + 1, blockindex);
+  std::copy(expg.begin(), expg.end(), blockeqs);
+  if (colors) std::copy(col.begin(), col.end(), colors);
+  if (ncolors) *ncolors = color;
+  if (seqnum) std::copy(an.seq.begin(), an.seq.end(), seqnum);
+  if (level) std::copy(an.level.begin(), an.level.end(), level);
+  return 0;
+}
+
+// CG with the node-set block preconditioner that BuildSequenceSolver returns for
+// one colour (Analysis/TPZAnalysis.cpp:1093-1107): a TPZStepSolver(ELU) over a
+// TPZSparseBlockDiagonal (Matrix/tpzsparseblockdiagonal.cpp) whose blocks
+// UpdateFrom copies out of the matrix (GetSub, :300-322), factored by
+// TPZFMatrix::Decompose_LU without pivoting, a zero pivot (IsZero, |a| <
+// 1e-12) replaced by 1 (Matrix/pzfmatrix.cpp:1285-1320), and solved by
+// TPZFMatrix::Substitution (:1354-1385) on the gathered residual; equations in
+// no block get zero (Substitution zeroes B before the scatter, :148-156).  The
+// CG loop is that of orc_cg_block_jacobi (Solvers/LinearSolvers/cg.h:29-132).
+int orc_cg_sparse_block_jacobi(int64_t n, int sym, const int64_t *IA, const int64_t *JA, const double *A,
+                               const double *b, double *x, int64_t nblocks, const int64_t *blockindex,
+                               const int64_t *blockeqs, int64_t maxit, double tol, int64_t *iters_out,
+                               double *resid_out) {
+  std::vector<int64_t> local(n, -1), lupos(nblocks + 1, 0);
+  for (int64_t B = 0; B < nblocks; B++) {
+    const int64_t bs = blockindex[B + 1] - blockindex[B];
+    lupos[B + 1] = lupos[B] + bs * bs;
+  }
+  std::vector<double> lu(lupos[nblocks], 0.0);
+  for (int64_t B = 0; B < nblocks; B++) {
+    const int64_t b0 = blockindex[B], bs = blockindex[B + 1] - b0;
+    double *m = lu.data() + lupos[B];  // column-major bs x bs, as TPZFMatrix
+    for (int64_t s = 0; s < bs; s++) local[blockeqs[b0 + s]] = s;
+    for (int64_t s = 0; s < bs; s++) {
+      const int64_t r = blockeqs[b0 + s];
+      for (int64_t k = IA[r]; k < IA[r + 1]; k++) {
+        const int64_t t = local[JA[k]];
+        if (t < 0) continue;
+        m[t * bs + s] = A[k];
+        if (sym) m[s * bs + t] = A[k];
+      }
+    }
+    for (int64_t s = 0; s < bs; s++) local[blockeqs[b0 + s]] = -1;
+    for (int64_t k = 0; k < bs; k++) {
+      double pivot = m[k * bs + k];
+      if (std::fabs(pivot) < 1.e-12) { m[k * bs + k] = 1.0; pivot = 1.0; }
+      for (int64_t i = k + 1; i < bs; i++) m[k * bs + i] /= pivot;
+      for (int64_t j = k + 1; j < bs; j++) {
+        const double kj = m[j * bs + k];
+        for (int64_t i = k + 1; i < bs; i++) m[j * bs + i] -= m[k * bs + i] * kj;
+      }
+    }
+  }
+  auto M = [&](const double *r, double *z) {
+    for (int64_t i = 0; i < n; i++) z[i] = 0.0;
+    std::vector<double> y;
+    for (int64_t B = 0; B < nblocks; B++) {
+      const int64_t b0 = blockindex[B], bs = blockindex[B + 1] - b0;
+      const double *m = lu.data() + lupos[B];
+      y.assign(bs, 0.0);
+      for (int64_t s = 0; s < bs; s++) y[s] = r[blockeqs[b0 + s]];
+      for (int64_t i = 0; i < bs; i++)
+        for (int64_t j = 0; j < i; j++) y[i] -= m[j * bs + i] * y[j];
+      for (int64_t i = bs - 1; i >= 0; i--) {
+        for (int64_t j = i + 1; j < bs; j++) y[i] -= m[j * bs + i] * y[j];
+        y[i] /= m[i * bs + i];
+      }
+      for (int64_t s = 0; s < bs; s++) z[blockeqs[b0 + s]] += y[s];
+    }
+  };
+  std::vector<double> r(n), z(n), p(n), q(n);
+  double normb = std::sqrt(dot(n, b, b));
+  for (int64_t i = 0; i < n; i++) { x[i] = 0.0; r[i] = b[i]; }
+  if (normb == 0.0) normb = 1.0;
+  double resid = std::sqrt(dot(n, r.data(), r.data())) / normb;
+  if (resid <= tol) { *iters_out = 0; *resid_out = resid; return 0; }
+  double rho = 0, rho_1 = 0;
+  for (int64_t it = 1; it <= maxit; it++) {
+    M(r.data(), z.data());
+    rho = dot(n, r.data(), z.data());
+    if (it == 1) p = z;
+    else {
+      double beta = rho / rho_1;
+      for (int64_t i = 0; i < n; i++) p[i] = z[i] + beta * p[i];
+    }
+    orc_spmv(n, sym, IA, JA, A, p.data(), q.data());
+    double alpha = rho / dot(n, p.data(), q.data());
+    for (int64_t i = 0; i < n; i++) { x[i] += alpha * p[i]; r[i] -= alpha * q[i]; }
+    resid = std::sqrt(dot(n, r.data(), r.data())) / normb;
+    if (resid <= tol) { *iters_out = it; *resid_out = resid; return 0; }
+    rho_1 = rho;
+  }
+  *iters_out = maxit;
+  *resid_out = resid;
+  return 1;
+}
+
 }  // extern "C"
+
