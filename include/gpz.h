@@ -261,7 +261,11 @@ int gpz_set_killed(gpz_ctx *ctx, int killed);
 #define GPZ_PRECOND_BLOCK_JACOBI 2 /* connect blocks, TPZBlockDiagonal (Matrix/pzblockdiag.h:21):
                                       TPZAnalysis::BuildPreconditioner(EBlockJacobi, overlap = true)
                                       (Analysis/TPZAnalysis.cpp:1073-1080) with its
-                                      TPZBlockDiagonalStructMatrix connect blocks */
+                                      TPZBlockDiagonalStructMatrix connect blocks.  The device
+                                      inverts 3x3 blocks, one per shape function: exactly the
+                                      connect blocks when every connect carries one shape (p <= 2);
+                                      a connect of order 3 (2, 4 or 8 shapes) is split into its
+                                      shapes' 3x3 blocks instead of one block of 6, 12 or 24 */
 
 typedef struct {
   int32_t solver;          /* GPZ_SOLVER_* */
