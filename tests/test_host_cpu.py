@@ -299,3 +299,20 @@ def test_hp_block_jacobi_variants_in_the_oracle(g):
     assert ns["iters"] < 0.85 * conn["iters"], (ns["iters"], conn["iters"])
     for s in (shape3, ns):
         assert np.linalg.norm(s["x"] - conn["x"]) <= 1e-6 * np.linalg.norm(conn["x"])
+
+
+def test_cxx_program_uses_the_c_abi(g, tmp_path):
+    """A C++ translation unit that includes only include/gpz.h compiles with g++, links libgpz.so and runs: the
+    host-only entry points give the node-set blocks and the Sloan order of a three-connect chain, and a context
+    is refused with GPZ_E_NO_DEVICE when no GPU is visible (no CPU fallback behind the ABI)."""
+    import subprocess
+    import torch
+    build = os.path.join(ROOT, "neopz_gb300", "_build")
+    exe = str(tmp_path / "abi_consumer")
+    subprocess.run(["g++", "-std=c++17", "-O1", "-I" + os.path.join(ROOT, "include"),
+                    os.path.join(ROOT, "tests", "abi_consumer.cpp"), "-L" + build, "-lgpz", "-Wl,-rpath," + build,
+                    "-o", exe], check=True)
+    out = subprocess.run([exe], check=True, stdout=subprocess.PIPE, text=True).stdout.splitlines()
+    assert out[0] == "nodeset 0 3 1 0 2 1"
+    assert out[1].startswith("sloan 0 ") and sorted(map(int, out[1].split()[2:])) == [0, 1, 2]
+    assert out[2] == ("context 0" if torch.cuda.is_available() else "context -8")  # -8: GPZ_E_NO_DEVICE
