@@ -213,22 +213,26 @@ def test_nodeset_blocks_match_the_reference_algorithm(g, case):
     assert np.array_equal(r2["blockeqs"], r["blockeqs"]) and np.array_equal(r2["blockindex"], r["blockindex"])
 
 
-@pytest.mark.parametrize("n", [4, 8, 16])
-def test_nodeset_blocks_of_a_q2_elasticity_cube(g, n):
-    """Known structure on n^3 Q2 hexes (3 equations per connect): a connect's node set is the union of the
+@pytest.mark.parametrize("kind,n", [("elast3d", 4), ("elast3d", 8), ("elast3d", 16), ("darcy3d", 5),
+                                    ("poisson2d", 3), ("poisson2d", 9)])
+def test_nodeset_blocks_of_q2_grids(g, kind, n):
+    """Known structure on n^d Q2 grids (nstate equations per connect): a connect's node set is the union of the
     elements around it, so two connects share a block only when every element of one is an element of the
-    other and back.  Away from the outer layer of elements no two connects have the same set ((2n - 3)^3
-    blocks of 3 equations); in the outer layer a boundary connect merges with the connects of the one, two or
-    four elements it touches: (2n - 3)^2 blocks of 6 per face, 2n - 3 blocks of 12 per edge and 8 corner
-    blocks of 24 (the corner vertex, three edges, three faces and the interior of a corner element)."""
-    grid = g.elasticity3d(n, 2)
+    other and back.  Away from the outer layer of elements no two connects have the same set (m^d one-connect
+    blocks, m = 2n - 3); in the outer layer a boundary connect merges with the connects of the one, two or four
+    elements it touches.  3D: 6 m^2 blocks of 2 connects, 12 m of 4 and 8 corner blocks of 8 (the corner
+    vertex, three edges, three faces and the interior of a corner element); 2D: 4 m of 2 and 4 of 4."""
+    grid = {"elast3d": lambda: g.elasticity3d(n, 2), "darcy3d": lambda: g.darcy(3, n, 2, np.ones(n ** 3)),
+            "poisson2d": lambda: g.poisson2d(n, 2)}[kind]()
+    ns = 3 if kind == "elast3d" else 1
     ei, eg = grid.element_graph()
     nn, bp, bs = _blocks_of(grid)
     r = g.nodeset_blocks(nn, ei, eg, bp, bs, grid.neq)
     sizes, counts = np.unique(np.diff(r["blockindex"]), return_counts=True)
     m = 2 * n - 3
-    assert dict(zip(sizes.tolist(), counts.tolist())) == {3: m ** 3, 6: 6 * m ** 2, 12: 12 * m, 24: 8}
-    assert r["level"].max() == 3
+    want = {1: m ** 3, 2: 6 * m ** 2, 4: 12 * m, 8: 8} if kind != "poisson2d" else {1: m ** 2, 2: 4 * m, 4: 4}
+    assert dict(zip(sizes.tolist(), counts.tolist())) == {ns * k: v for k, v in want.items()}
+    assert r["level"].max() == (2 if kind == "poisson2d" else 3)
 
 
 def test_nodeset_block_preconditioner_in_the_oracle(g):
