@@ -403,13 +403,15 @@ int gpz_learned_train(gpz_ctx *ctx, int steps, double lr, double *loss_first, do
  * array, so calls must not overlap in time on one device (one after the
  * other, from any thread or stream, is fine).
  *
- * stream: cudaStream_t of the current device (NULL = legacy default stream);
- * d_ia[neq+1] (int64), d_ja[nnz] (int32), d_a[nnz], d_b[neq], d_x[neq]: device
- * pointers; x is overwritten with the solution.  The call returns when the
- * solve has finished on `stream`; iterations / resid (host, may be NULL)
- * receive fNumIterations and the final ||r||/||b||.  Bad row pointers or
- * columns, or a missing / zero diagonal, return GPZ_E_INVALID before the first
- * iteration. */
+ * stream: cudaStream_t of the current device (NULL = legacy default stream;
+ * a stream of another device returns GPZ_E_INVALID); d_ia[neq+1] (int64),
+ * d_ja[nnz] (int32), d_a[nnz], d_b[neq], d_x[neq]: device pointers; x is
+ * overwritten with the solution.  Every call blocks the calling host thread
+ * until the solve has finished on `stream` (it reads the device's stop flag
+ * every 32 iterations); iterations / resid (host, may be NULL) receive
+ * fNumIterations and the final ||r||/||b||.  Bad row pointers or columns, or
+ * a missing / zero diagonal, return GPZ_E_INVALID before the first iteration
+ * and leave x unchanged. */
 #define GPZ_NOALLOC_MAX_EQ 262144
 int gpz_cg_jacobi_noalloc(void *stream, int64_t neq, int64_t nnz, const int64_t *d_ia, const int32_t *d_ja,
                           const double *d_a, const double *d_b, double *d_x, int64_t max_iter, double tol,

@@ -4,6 +4,7 @@
 #pragma once
 #include <algorithm>
 #include <cstdint>
+#include <exception>
 #include <thread>
 #include <vector>
 
@@ -17,7 +18,8 @@ struct Graph {
 
 // TPZRenumbering::ConvertGraph (External/TPZRenumbering.cpp:76-105): every
 // node's list is built on its own (a count pass and a fill pass over node
-// ranges on the host threads), so the result does not depend on the threads
+// ranges on the host threads), so the result does not depend on the threads.
+// Allocation failures throw std::bad_alloc into the caller's thread.
 inline bool convert_graph(int64_t nnodes, int64_t nel, const int64_t *eptr, const int64_t *eg, Graph &g) {
   std::vector<int64_t> cnt(nnodes + 1, 0);
   for (int64_t e = 0; e < nel; e++)
@@ -47,15 +49,27 @@ inline bool convert_graph(int64_t nnodes, int64_t nel, const int64_t *eptr, cons
         }
     }
   };
+  // the per-thread markers are allocated here, in the calling thread, so an
+  // allocation failure reaches the caller's handler; anything a worker still
+  // throws (its neighbour list growing) is carried out and rethrown after join
+  std::vector<std::vector<int64_t>> marks(nt, std::vector<int64_t>(nnodes, -1));
   auto run = [&](auto &&body) {
+    for (auto &m : marks) std::fill(m.begin(), m.end(), -1);
+    std::vector<std::exception_ptr> err(nt);
     std::vector<std::thread> th;
     for (unsigned t = 0; t < nt; t++)
       th.emplace_back([&, t]() {
-        std::vector<int64_t> mark(nnodes, -1), nb;
-        const int64_t b = nnodes * t / nt, e = nnodes * (t + 1) / nt;
-        for (int64_t v = b; v < e; v++) body(v, mark, nb);
+        try {
+          std::vector<int64_t> nb;
+          const int64_t b = nnodes * t / nt, e = nnodes * (t + 1) / nt;
+          for (int64_t v = b; v < e; v++) body(v, marks[t], nb);
+        } catch (...) {
+          err[t] = std::current_exception();
+        }
       });
     for (auto &x : th) x.join();
+    for (auto &x : err)
+      if (x) std::rethrow_exception(x);
   };
   run([&](int64_t v, std::vector<int64_t> &mark, std::vector<int64_t> &nb) {
     neighbours(v, mark, nb);

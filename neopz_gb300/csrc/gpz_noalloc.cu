@@ -16,7 +16,8 @@
 // during start-up, before any stream capture and before the region that must
 // not allocate.  After that a call only launches kernels, sets the flag block
 // with cudaMemsetAsync and reads the flag block back with cudaMemcpyAsync into
-// host stack memory.
+// host stack memory.  The host waits on the stream every 32 iterations to read
+// that block, so each call blocks the calling thread until the solve ends.
 //
 // Sharing: every call on a device uses the same array.  The reduction counter
 // and the flags must start at zero; each call clears them itself before its
@@ -142,14 +143,15 @@ __device__ inline bool grid_sum(const View &s, double (&v)[NV]) {
   return true;
 }
 
-// x = 0, r = b, 1/diag, ||b||, rho = r . (D^-1 r).  Also checks the CSR
-// arrays (row pointers inside [0, nnz] and non-decreasing, columns inside
-// [0, n)) and that every row has a finite, non-zero diagonal; any failure
-// stops the solve before the first iteration.
+// r = b, 1/diag, ||b||, rho = r . (D^-1 r).  Also checks the CSR arrays
+// (row pointers inside [0, nnz] and non-decreasing, columns inside [0, n))
+// and that every row has a finite, non-zero diagonal; any failure stops the
+// solve before the first iteration.  x is not written here: k_na_zero_x
+// clears it once the checks have passed, so bad input leaves x as it was.
 __global__ void __launch_bounds__(kThreads) k_na_start(int64_t n, int64_t nnz, const int64_t *__restrict__ ia,
                                                        const int32_t *__restrict__ ja, const double *__restrict__ a,
-                                                       const double *__restrict__ b, double *__restrict__ x,
-                                                       double tol, int64_t maxit, View s) {
+                                                       const double *__restrict__ b, double tol, int64_t maxit,
+                                                       View s) {
   double v[3] = {0.0, 0.0, 0.0};  // b.b, b.(D^-1 b), bad rows
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
     const double bi = b[i];
@@ -168,7 +170,6 @@ __global__ void __launch_bounds__(kThreads) k_na_start(int64_t n, int64_t nnz, c
       }
     ok = ok && found && d != 0.0 && isfinite(d);
     const double di = ok ? 1.0 / d : 0.0;
-    x[i] = 0.0;
     s.r[i] = bi;
     s.p[i] = 0.0;
     s.dinv[i] = di;
@@ -194,6 +195,13 @@ __global__ void __launch_bounds__(kThreads) k_na_start(int64_t n, int64_t nnz, c
     else if (maxit <= 0) stop = STOP_MAXIT;
     s.flag[FL_STOP] = stop;
   }
+}
+
+// x = 0 (the zero initial guess of cg.h), unless the input checks failed
+__global__ void __launch_bounds__(kThreads) k_na_zero_x(int64_t n, double *__restrict__ x, View s) {
+  if (*reinterpret_cast<volatile unsigned long long *>(&s.flag[FL_STOP]) == STOP_BAD_INPUT) return;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    x[i] = 0.0;
 }
 
 // p = D^-1 r + beta p  (beta = 0 in the first iteration, p = 0 from the start kernel)
@@ -305,6 +313,14 @@ extern "C" int gpz_cg_jacobi_noalloc(void *stream, int64_t neq, int64_t nnz, con
   if (rc != GPZ_OK) return rc;
   const View s = view_of(base);
   cudaStream_t st = static_cast<cudaStream_t>(stream);
+  if (st) {  // a stream of another device would launch against the wrong device's scratch
+    int sdev = -1, cur = -1;
+    if (cudaStreamGetDevice(st, &sdev) != cudaSuccess || cudaGetDevice(&cur) != cudaSuccess) {
+      cudaGetLastError();
+      return GPZ_E_INVALID;
+    }
+    if (sdev != cur) return GPZ_E_INVALID;
+  }
 
   // the counter and the flags start at zero on every call
   if (cudaMemsetAsync(s.flag, 0, kNumFlag * sizeof(unsigned long long), st) != cudaSuccess) {
@@ -313,7 +329,8 @@ extern "C" int gpz_cg_jacobi_noalloc(void *stream, int64_t neq, int64_t nnz, con
   }
   const int gv = grid_for(neq);
   const int gs = grid_for(neq * 32);
-  k_na_start<<<gv, kThreads, 0, st>>>(neq, nnz, ia, ja, a, b, x, tol, max_iter, s);
+  k_na_start<<<gv, kThreads, 0, st>>>(neq, nnz, ia, ja, a, b, tol, max_iter, s);
+  k_na_zero_x<<<gv, kThreads, 0, st>>>(neq, x, s);
   unsigned long long hflag[kNumFlag] = {};
   double hscal[kNumScal] = {};
   const int64_t nbatch = max_iter / kBatch + 2;  // the device stops itself at max_iter

@@ -45,10 +45,12 @@ void relations(const Graph &g, std::vector<char> &rel) {
   unsigned nt = std::thread::hardware_concurrency();
   nt = std::max(1u, std::min(nt, 16u));
   if (n < 65536) nt = 1;
+  // markers allocated in the calling thread: an allocation failure reaches the caller's handler
+  std::vector<std::vector<int64_t>> marks(nt, std::vector<int64_t>(n, -1));
   std::vector<std::thread> th;
   for (unsigned t = 0; t < nt; t++)
     th.emplace_back([&, t]() {
-      std::vector<int64_t> mark(n, -1);
+      std::vector<int64_t> &mark = marks[t];
       const int64_t b = n * t / nt, e = n * (t + 1) / nt;
       for (int64_t v = b; v < e; v++) {
         mark[v] = v;

@@ -756,13 +756,14 @@ __global__ void __launch_bounds__(kThreads) k_mx_bsr3_tma(TmaArgs A, Red R) {
   }
   __syncthreads();
   KSum pq;
-  bool ok = true;
+  bool ok = true, next_issued = false;
   int it = 0;
   for (int64_t t = first; t < A.ntiles; t += step, it++) {
     const int st = it & 1;
     const uint32_t par = (uint32_t)((it >> 1) & 1);
     if (threadIdx.x == 0) {
-      if (t + step < A.ntiles) tma_issue(A, t + step, sv[st ^ 1], sc[st ^ 1], &bar[st ^ 1]);
+      next_issued = t + step < A.ntiles;
+      if (next_issued) tma_issue(A, t + step, sv[st ^ 1], sc[st ^ 1], &bar[st ^ 1]);
       s_ok = mbar_wait_bounded(&bar[st], par);  // one thread decides, so the exit is uniform
     }
     __syncthreads();
@@ -813,10 +814,13 @@ __global__ void __launch_bounds__(kThreads) k_mx_bsr3_tma(TmaArgs A, Red R) {
     __syncthreads();  // the stage is free for the copy issued next iteration
   }
   if (!ok) {
-    // record, then let an outstanding copy of the other stage land before leaving
+    // record, then give both copies still in flight -- the stage whose wait
+    // timed out and the next tile's, issued just before -- another bounded
+    // wait, so that no bulk copy lands in this CTA's shared memory after it leaves
     if (threadIdx.x == 0) {
       atomicOr(A.err, 512);
-      mbar_wait_bounded(&bar[(it & 1) ^ 1], (uint32_t)(((it + 1) >> 1) & 1));
+      mbar_wait_bounded(&bar[it & 1], (uint32_t)((it >> 1) & 1));
+      if (next_issued) mbar_wait_bounded(&bar[(it & 1) ^ 1], (uint32_t)(((it + 1) >> 1) & 1));
     }
     __syncthreads();
   }

@@ -394,10 +394,10 @@ def poisson2d(n=64, p=2):
     return OracleMesh(2, (n, n), (0, 0, 0), (1, 1, 0), [1, -1, -1, -1, -1], True, p, mats, bcs)
 
 
-def elasticity3d(n, p=2, E=None, nu=0.3, top_traction=True, side_bc=False):
+def elasticity3d(n, p=2, E=None, nu=0.3, top_traction=True, side_bc=False, body_force=(0.0, 0.0, -1.0)):
     """Unit cube n^3 hexes, clamped z=0 face (type 0), traction (0,0,-1) on top (type 1),
-    body force (0,0,-1); E per element (array) or 1."""
-    mats = [material(1, ORC_ELAST3D, 3, E=1.0, nu=nu, force=(0, 0, -1.0), forcing=ORC_F_CONST)]
+    body force body_force; E per element (array) or 1."""
+    mats = [material(1, ORC_ELAST3D, 3, E=1.0, nu=nu, force=tuple(body_force), forcing=ORC_F_CONST)]
     bcs = [bc(-1, 1, 0)]
     if top_traction:
         bcs.append(bc(-3, 1, 1, val2=(0, 0, -1.0)))

@@ -16,7 +16,7 @@ library itself printed for the synthetic grids of the benchmark (a run of the
 reference's TPZSSpStructMatrix / TPZSpStructMatrix + TPZStepSolver CG with
 Jacobi on the configurations below).
 
-Usage:  python tests/golden/make_golden.py [REFERENCE_ROOT]
+Usage:  python tests/golden/make_golden.py REFERENCE_ROOT   (the NeoPZ source tree; required)
 The fixture is committed; the tests never read the reference tree.
 """
 import json
@@ -76,4 +76,6 @@ def main(ref):
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    if len(sys.argv) != 2:
+        sys.exit("usage: python tests/golden/make_golden.py <path of the NeoPZ source tree>")
+    main(sys.argv[1])

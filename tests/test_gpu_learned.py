@@ -140,7 +140,7 @@ def test_learned_gradient_matches_oracle_elasticity(g):
 
 
 def test_learned_elasticity_weights_gain_and_mixed_path(g):
-    """The committed elasticity weights (trained on the GPU on 12^3 fields, neopz_gb300/data) on unseen 16^3
+    """The committed elasticity weights (trained on the GPU on 200 seeded 16^3 fields, neopz_gb300/data) on unseen 16^3
     fields: the learned flexible CG needs at most 85% of the Jacobi-PCG iterations; the learned + mixed
     path (the mixed CG's FP32 operator chosen by the autotuner, FP32 recurrence, FP64 true-residual
     replacement) reaches the same true residual 1e-8 in about as many iterations, and its solution is

@@ -87,6 +87,7 @@ def test_noalloc_matches_context_jacobi_pcg(g, case):
     f = _entry(g)
     neq, nnz = len(b), len(ja)
     xs = []
+    free_before = None
     for _ in range(2):
         rc, its, res = _call(f, stream, neq, nnz, d_ia.data_ptr(), d_ja.data_ptr(), d_a.data_ptr(), d_b.data_ptr(),
                              d_x.data_ptr(), max_iter, tol)
@@ -98,7 +99,15 @@ def test_noalloc_matches_context_jacobi_pcg(g, case):
         xs.append((its, res, x))
         d_x.copy_(torch.from_numpy(np.full(neq, np.nan)))
         torch.cuda.synchronize()
+        if free_before is None:  # after the first call (which looks the scratch up) nothing is allocated
+            free_before = torch.cuda.mem_get_info(dev)[0]
     assert xs[0][0] == xs[1][0] and xs[0][1] == xs[1][1] and np.array_equal(xs[0][2], xs[1][2])
+    assert torch.cuda.mem_get_info(dev)[0] == free_before, "device free memory changed across calls"
+
+    # a stream of the current device is accepted; the legacy default stream (NULL) too
+    rc, its, _ = _call(f, None, neq, nnz, d_ia.data_ptr(), d_ja.data_ptr(), d_a.data_ptr(), d_b.data_ptr(),
+                       d_x.data_ptr(), max_iter, tol)
+    assert rc == 0 and its == xs[0][0]
 
     # a budget of a few iterations: not converged, iteration count = max_iter
     rc, its, res = _call(f, stream, neq, nnz, d_ia.data_ptr(), d_ja.data_ptr(), d_a.data_ptr(), d_b.data_ptr(),
@@ -117,9 +126,12 @@ def test_noalloc_matches_context_jacobi_pcg(g, case):
     d_jabad = torch.from_numpy(ja_bad).to(dev)
     torch.cuda.synchronize()
     for jj, aa in ((d_ja, d_abad), (d_jabad, d_a)):
+        d_x.fill_(7.0)
+        torch.cuda.synchronize()
         rc, its, _ = _call(f, stream, neq, nnz, d_ia.data_ptr(), jj.data_ptr(), aa.data_ptr(), d_b.data_ptr(),
                            d_x.data_ptr(), max_iter, tol)
         assert rc == GPZ_E_INVALID and its == 0
+        assert bool(torch.all(d_x == 7.0)), "bad input must leave x unchanged"
     # and a good call right after still solves
     rc, its, res = _call(f, stream, neq, nnz, d_ia.data_ptr(), d_ja.data_ptr(), d_a.data_ptr(), d_b.data_ptr(),
                          d_x.data_ptr(), max_iter, tol)
