@@ -33,6 +33,7 @@ METRIC = "s to ||r||/||b||<1e-8: learned+mixed PCG vs FP64 Jacobi-PCG (GB300); e
 LEARNED_WEIGHTS = os.path.join(ROOT, "neopz_gb300", "data", "learned_elasticity3d_q2.npy")
 LEARNED_RANK = 8
 TOL = 1e-8
+ERR_REF_TOL = 1e-12  # true residual of the FP64 solve the solution errors are measured against
 SEED = 5
 # HBM bytes per stored block measured by ncu for the SpMV kernels (32^3 case):
 # k_mx_sym3 375.6 MB read + 3.3 MB written over 8,624,609 upper blocks
@@ -202,7 +203,7 @@ def run_gpu(args):
     e0 = torch.cuda.Event(enable_timing=True)
     e1 = torch.cuda.Event(enable_timing=True)
     torch.cuda.synchronize()
-    fp64, t_fp64 = {"iterations": None, "true_resid": None}, None
+    fp64, t_fp64, x_fp64 = {"iterations": None, "true_resid": None}, None, None
     if not args.no_fp64_baseline:
         with torch.cuda.stream(stream):
             e0.record(stream)
@@ -211,6 +212,7 @@ def run_gpu(args):
             e1.record(stream)
         torch.cuda.synchronize()
         t_fp64 = e0.elapsed_time(e1) / 1e3
+        x_fp64 = ctx.solution()
     for _ in range(args.warmup):
         step()
     # element matrices + scatter alone (FP64), for elements/s
@@ -233,9 +235,30 @@ def run_gpu(args):
     t_step = ms_step / 1e3
     t_step = max_over_ranks(t_step, world, "cuda")
     last = reps[-1]
+    x_step = ctx.solution()  # the last timed step's solution (outside the timed region)
     # the other mixed path, once: block-Jacobi CG without the learned correction (or the learned one
     # when the step is the block-Jacobi CG)
     other, t_other = timed(lambda: step(learned=args.path != "learned"))
+    x_other = ctx.solution()
+    # solution error against the FP64 solution: the FP64 Jacobi-PCG (the parity-tested path, the same algorithm
+    # as the reference's CG) run to a true residual of 1e-12, well below the 1e-8 stop of the compared solves
+    accuracy = {}
+    if not args.no_fp64_baseline:
+        ctx.assemble(gpz.GPZ_PREC_FP64)
+        tight = ctx.solve(solver=gpz.GPZ_SOLVER_CG, tol=ERR_REF_TOL, max_iter=400000, check_every=64)
+        xr = tight["x"]
+        nr = float(np.linalg.norm(xr))
+        accuracy = {
+            "reference_solution": (f"FP64 Jacobi-PCG (GPU, parity-tested against the oracle and the reference's "
+                                   f"fixtures) to a true residual {ERR_REF_TOL:g}: {tight['iterations']} iterations, "
+                                   f"true residual {tight['true_resid']:.3g}"),
+            "value_path": float(np.linalg.norm(x_step - xr) / nr),
+            ("mixed_block_jacobi_cg" if args.path == "learned" else "learned_mixed_fcg"):
+                float(np.linalg.norm(x_other - xr) / nr),
+            "fp64_jacobi_pcg": float(np.linalg.norm(x_fp64 - xr) / nr) if x_fp64 is not None else None,
+            "bar": 1e-8}
+        del xr, tight
+        ctx.assemble(gpz.GPZ_PREC_MIXED)  # back to the timed path's operator for the kernel timings below
 
     # roofline of the dominant kernel: the FP32 3x3-block SpMV of the inner CG, in the
     # layout the library's autotuner chose (HBM bytes that layout must stream per launch)
@@ -360,6 +383,8 @@ def run_gpu(args):
                             "FP64 x/dots, reliable FP64 true-residual updates; connect-block (3x3) Jacobi"),
                    "l2": "inputs larger than L2 (matrix > 129 MB)",
                    "parallelism": f"replicas x{world}"},
+        "solution_rel_err_vs_fp64": accuracy.get("value_path"),
+        "solution_error": accuracy,
         "solve": {"iterations": last["iterations"], "true_resid": last["true_resid"],
                   "reliable_updates": last["reliable_updates"], "spmv_fp32": last["spmv_fp32"],
                   "spmv_fp64": last["spmv_fp64"], "restarts": last["restarts"], "solve_s": last["seconds"]},

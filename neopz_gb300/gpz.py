@@ -476,6 +476,12 @@ class Context:
         self._check(lib().gpz_learned_train(self.h, steps, lr, ctypes.byref(l0), ctypes.byref(l1)))
         return l0.value, l1.value
 
+    def solution(self):
+        """The device solution of the last solve (gpz_solution_download)."""
+        x = np.zeros(self.neq)
+        self._check(lib().gpz_solution_download(self.h, _p(x)))
+        return x
+
     def solve(self, solver=GPZ_SOLVER_CG, precond=GPZ_PRECOND_JACOBI, max_iter=20000, tol=1e-8, b=None,
               check_every=32, reliable_delta=1e-3, use_graph=True, x0=None, want_x=True, gmres_krylov=30,
               spmv_variant=-1):

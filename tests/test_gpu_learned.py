@@ -93,7 +93,8 @@ def test_learned_training_gains_over_jacobi(g):
         oa, of = om.assemble(True, oia, oja)
         ref = O.cg_jacobi(True, oia, oja, oa, of, 20000, 1e-12)
         assert np.linalg.norm(tight["x"] - ref["x"]) <= 1e-8 * np.linalg.norm(ref["x"])
-        assert np.linalg.norm(mx["x"] - ref["x"]) <= 1e-5 * np.linalg.norm(ref["x"])  # true residual 1e-8
+        # true residual 1e-8; the solution error against the FP64 oracle's tight solve is held to 1e-8
+        assert np.linalg.norm(mx["x"] - ref["x"]) <= 1e-8 * np.linalg.norm(ref["x"])
     ctx.close()
 
 
@@ -144,7 +145,7 @@ def test_learned_elasticity_weights_gain_and_mixed_path(g):
     fields: the learned flexible CG needs at most 85% of the Jacobi-PCG iterations; the learned + mixed
     path (the mixed CG's FP32 operator chosen by the autotuner, FP32 recurrence, FP64 true-residual
     replacement) reaches the same true residual 1e-8 in about as many iterations, and its solution is
-    within 1e-5 of a tight FP64 solve."""
+    within 1e-8 of a tight FP64 solve."""
     import os
     from neopz_gb300 import learned
     w = np.load(os.path.join(learned.DATA, "learned_elasticity3d_q2.npy"))
@@ -158,12 +159,12 @@ def test_learned_elasticity_weights_gain_and_mixed_path(g):
         lrn = ctx.solve(solver=g.GPZ_SOLVER_LEARNED_FCG, tol=1e-8, want_x=False)
         assert jac["rc"] == 0 and lrn["rc"] == 0 and lrn["restarts"] == 0
         assert lrn["iterations"] <= 0.85 * jac["iterations"], (s, lrn["iterations"], jac["iterations"])
-        ref = ctx.solve(tol=1e-11, max_iter=50000)
+        ref = ctx.solve(tol=1e-12, max_iter=50000)
         ctx.assemble(g.GPZ_PREC_MIXED)
         mx = ctx.solve(solver=g.GPZ_SOLVER_LEARNED_MIXED_FCG, tol=1e-8, reliable_delta=1e-2)
         assert mx["rc"] == 0 and mx["true_resid"] <= 1e-8 and mx["spmv_fp32"] > 0 and mx["reliable_updates"] >= 1
         assert mx["iterations"] <= 1.1 * lrn["iterations"], (s, mx["iterations"], lrn["iterations"])
-        assert np.linalg.norm(mx["x"] - ref["x"]) <= 1e-5 * np.linalg.norm(ref["x"])
+        assert np.linalg.norm(mx["x"] - ref["x"]) <= 1e-8 * np.linalg.norm(ref["x"])
     ctx.close()
 
 
@@ -180,7 +181,8 @@ def test_learned_mixed_elasticity_falls_back(g):
     mx = ctx.solve(solver=g.GPZ_SOLVER_LEARNED_MIXED_FCG, tol=1e-8, reliable_delta=1e-2)
     assert mx["rc"] == 0 and mx["true_resid"] <= 1e-8
     assert mx["restarts"] >= mx["iterations"] - 1  # every application fell back
-    assert np.linalg.norm(mx["x"] - jac["x"]) <= 1e-5 * np.linalg.norm(jac["x"])
+    tight = ctx.solve(tol=1e-12)
+    assert np.linalg.norm(mx["x"] - tight["x"]) <= 1e-8 * np.linalg.norm(tight["x"])
     ctx.close()
 
 
@@ -188,7 +190,7 @@ def test_learned_mixed_elasticity_equation_wise_path(g):
     """Rank 4 (not the connect-wise kernel's rank 8): the equation-wise node correction of the FP32 learned +
     mixed path reaches the same true residual as the FP64 learned flexible CG with the same network, in at most
     1.5x its iterations (the FP32 recurrence on the 1e12-penalty rows costs iterations on small meshes), and the
-    solutions agree within 1e-5."""
+    solution is within 1e-8 of a tight FP64 solve."""
     n = 6
     grid = g.elasticity3d(n, 2, E=np.exp(np.random.default_rng(9).standard_normal(n ** 3)))
     ctx = _ctx(g, grid)
@@ -199,5 +201,6 @@ def test_learned_mixed_elasticity_equation_wise_path(g):
     mx = ctx.solve(solver=g.GPZ_SOLVER_LEARNED_MIXED_FCG, tol=1e-8, reliable_delta=1e-2)
     assert f64["rc"] == 0 and mx["rc"] == 0 and mx["true_resid"] <= 1e-8
     assert mx["iterations"] <= 1.5 * f64["iterations"], (mx["iterations"], f64["iterations"])
-    assert np.linalg.norm(mx["x"] - f64["x"]) <= 1e-5 * np.linalg.norm(f64["x"])
+    tight = ctx.solve(tol=1e-12)
+    assert np.linalg.norm(mx["x"] - tight["x"]) <= 1e-8 * np.linalg.norm(tight["x"])
     ctx.close()

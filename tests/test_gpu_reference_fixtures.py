@@ -1,0 +1,104 @@
+"""The GPU path against fixtures the NeoPZ reference library itself wrote
+(tests/golden/ref_*.npz, made by tests/golden/make_ref_fixtures.py; what
+they hold and the value tolerances are in tests/refcases.py).
+
+Per fixture, through the C ABI:
+* the device pattern build gives the reference's CSR bit for bit (SHA-256 of
+  row pointers and columns, upper TPZSSpStructMatrix and full
+  TPZSpStructMatrix), the FP64 assembly its values and load vector within
+  1e-12 at each row's scale;
+* the FP64 Jacobi-PCG needs the reference's iteration count within
+  max(3, 10%) -- 30% for the 6.7e16-penalty Poisson system, whose count
+  depends on the summation order -- and its solution is within 1e-8 of the
+  reference's tight (1e-13) solve;
+* the mixed-precision CG (FP32 operator and recurrence, FP64 true-residual
+  replacement; block Jacobi for elasticity) and, where trained weights exist,
+  the learned + mixed flexible CG stop on a true FP64 residual at the
+  workload's tolerance with a solution error at most 1e-8 relative to the
+  reference's FP64 solution: the error bar of the mixed-precision design.
+"""
+import os
+
+import numpy as np
+import pytest
+
+import refcases as RC
+
+pytestmark = pytest.mark.gpu
+
+MIXED_ERR = 1e-8
+
+
+@pytest.fixture(scope="module")
+def g():
+    import __graft_entry__
+    __graft_entry__.build()
+    from neopz_gb300 import gpz
+    return gpz
+
+
+def _system(g, fx):
+    grid = RC.problem(g, fx)
+    ctx = g.Context(0)
+    ctx.upload_mesh(grid)
+    ctx.build_pattern(bool(int(fx["sym"])))
+    return ctx, grid
+
+
+@pytest.mark.parametrize("name", RC.names())
+def test_gpu_system_and_fp64_cg_match_reference(g, name):
+    fx = RC.load(name)
+    ctx, grid = _system(g, fx)
+    ia, ja = ctx.pattern()
+    ctx.assemble(g.GPZ_PREC_FP64)
+    RC.check_system(fx, ia, ja, ctx.matrix(), ctx.rhs())
+    if "x" in fx:
+        tol = float(fx["tol"])
+        sol = ctx.solve(tol=tol, max_iter=200000, check_every=64)
+        assert sol["rc"] == 0
+        ref_it = int(fx["cg_iterations"])
+        margin = 0.3 if str(fx["case"]) == "poisson2d" else 0.1
+        assert abs(sol["iterations"] - ref_it) <= max(3, margin * ref_it), (sol["iterations"], ref_it)
+        assert RC.rel_err(sol["x"], fx) <= 1e-8
+    ctx.close()
+
+
+MIXED = [n for n in RC.names() if not n.endswith("_full")]
+
+
+@pytest.mark.parametrize("name", MIXED)
+def test_gpu_mixed_cg_error_against_reference(g, name):
+    fx = RC.load(name)
+    ctx, grid = _system(g, fx)
+    ctx.assemble(g.GPZ_PREC_MIXED)
+    elast = str(fx["case"]).startswith("elast")
+    tol = float(fx["tol"])
+    sol = ctx.solve(solver=g.GPZ_SOLVER_MIXED_CG, precond=g.GPZ_PRECOND_BLOCK_JACOBI if elast else
+                    g.GPZ_PRECOND_JACOBI, tol=tol, max_iter=200000, reliable_delta=1e-2, check_every=64)
+    assert sol["rc"] == 0 and sol["true_resid"] <= tol and sol["spmv_fp32"] > 0
+    err = RC.rel_err(sol["x"], fx)
+    assert err <= MIXED_ERR, err
+    ctx.close()
+
+
+LEARNED = {"c5_elast3d_16_q2": ("learned_elasticity3d_q2.npy", 8),
+           "c5_elast3d_8_q2": ("learned_elasticity3d_q2.npy", 8),
+           "c4_darcy2d_grf_32_q2": ("learned_darcy2d_q2.npy", 4)}
+
+
+@pytest.mark.parametrize("name", sorted(LEARNED))
+def test_gpu_learned_mixed_error_against_reference(g, name):
+    from neopz_gb300 import learned
+    fx = RC.load(name)
+    wfile, rank = LEARNED[name]
+    ctx, grid = _system(g, fx)
+    ctx.assemble(g.GPZ_PREC_MIXED)
+    ctx.learned_init(rank=rank, seed=0)
+    ctx.set_learned_params(np.load(os.path.join(learned.DATA, wfile)))
+    tol = float(fx["tol"])
+    sol = ctx.solve(solver=g.GPZ_SOLVER_LEARNED_MIXED_FCG, tol=tol, max_iter=200000, reliable_delta=1e-2,
+                    check_every=64)
+    assert sol["rc"] == 0 and sol["true_resid"] <= tol
+    err = RC.rel_err(sol["x"], fx)
+    assert err <= MIXED_ERR, err
+    ctx.close()
