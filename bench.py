@@ -269,7 +269,9 @@ def run_gpu(args):
     nbrow = neq // 3
     chosen = tune.get("chosen", "block_csr")
     mf_flops = None
-    matfree = chosen in ("matrix_free_elements", "matrix_free_sum_factorised", "matrix_free_tcgen05_3xtf32")
+    matfree = chosen in ("matrix_free_elements", "matrix_free_sum_factorised", "matrix_free_tcgen05_3xtf32",
+                         "matrix_free_shared_matrix_tcgen05")
+    mma_flops = None
     if matfree:
         # element records (corners 96 B, block rows 108 B, lambda/mu 8 B, affine geometry 40 B), penalty-face
         # records (48 + 36 B),
@@ -277,7 +279,14 @@ def run_gpu(args):
         nface = (n + 0) * (n + 0)
         nblk = 0
         l2_atomics = 27 * nvol + 9 * nface
-        if chosen == "matrix_free_sum_factorised":
+        if chosen == "matrix_free_shared_matrix_tcgen05":
+            kern = ("k_mf_hex27_gm: matrix-free Q2 elasticity on a uniform grid, K_e = mu_e Khat as one tcgen05 "
+                    "kind::tf32 3xTF32 GEMM per tile of 128 elements (M 128, N 96, K 88), float4 atomics (block rows "
+                    "+ mu per element and one pass of p and q are its HBM bytes)")
+            # algorithmic FLOPs: the 81 x 81 product per element; the MMAs execute 3 products of the padded tile
+            mf_flops = nvol * 2 * 81 * 81 + nface * 2 * 9 * 9 * 6
+            mma_flops = -(-nvol // 128) * 3 * 2 * 128 * 96 * 88
+        elif chosen == "matrix_free_sum_factorised":
             kern = ("k_mf_hex27_sf: matrix-free Q2 elasticity, sum-factorised on Lagrange nodal values, one warp per "
                     "element (CUDA-core FP32; records + one pass of p and q are its HBM bytes)")
             # FLOPs per element: Phi and Phi^T (2 x 2 x 125 x 3), the 1D contractions forward and back
@@ -300,7 +309,8 @@ def run_gpu(args):
     # values + columns + block-row pointers + p (16 B per block row, read once) + q (written once)
     bytes32 = nblk * (36 + 4) + (nbrow + 1) * 8 + nbrow * 16 + nbrow * 16
     if matfree:
-        bytes32 = nvol * (96 + 108 + 8 + 40) + nface * (48 + 36) + nbrow * 16 + nbrow * 16
+        rec = 108 + 8 if chosen == "matrix_free_shared_matrix_tcgen05" else 96 + 108 + 8 + 40
+        bytes32 = nvol * rec + nface * (48 + 36) + nbrow * 16 + nbrow * 16
     bytes64 = nnz * (8 + 4) + (neq + 1) * 8 + neq * 8 + neq * 8 + neq * 8
     pk = peaks()
     hbm = pk.get("hbm_gbs", 6800.0)
@@ -403,6 +413,7 @@ def run_gpu(args):
                      "l2_float4_atomics_per_launch": l2_atomics,
                      "algorithmic_bytes": int(bytes32), "ms_per_launch": ms32,
                      "fp32_tflops": (round(mf_flops / (ms32 * 1e-3) / 1e12, 2) if mf_flops else None),
+                     "tensor_mma_tflops": (round(mma_flops / (ms32 * 1e-3) / 1e12, 2) if mma_flops else None),
                      "fp32_peak_tflops_nominal": (round(152 * 128 * 2 * 2.07e9 / 1e12, 1) if mf_flops else None),
                      "fp64_spmv": {"ms_per_launch": ms64,
                                    "achieved_gbs": round(bytes64 / (ms64 * 1e-3) / 1e9, 1)},

@@ -226,7 +226,7 @@ int gpz_spmv(gpz_ctx *ctx, double alpha, const double *x, double beta, const dou
 
 /* y = A32 x with the FP32 operator of the mixed solvers (host FP64 vectors):
  * the layout the SpMV autotuner chose, or `variant` (GPZ solver option
- * spmv_variant, 0..7) for 3-state problems; the FP32 CSR copy otherwise. */
+ * spmv_variant, 0..8) for 3-state problems; the FP32 CSR copy otherwise. */
 int gpz_spmv_fp32(gpz_ctx *ctx, int variant, const double *x, double *y);
 
 /* ---- cancellation ---------------------------------------------------------
@@ -261,11 +261,30 @@ int gpz_set_killed(gpz_ctx *ctx, int killed);
 #define GPZ_PRECOND_BLOCK_JACOBI 2 /* connect blocks, TPZBlockDiagonal (Matrix/pzblockdiag.h:21):
                                       TPZAnalysis::BuildPreconditioner(EBlockJacobi, overlap = true)
                                       (Analysis/TPZAnalysis.cpp:1073-1080) with its
-                                      TPZBlockDiagonalStructMatrix connect blocks.  The device
-                                      inverts 3x3 blocks, one per shape function: exactly the
-                                      connect blocks when every connect carries one shape (p <= 2);
-                                      a connect of order 3 (2, 4 or 8 shapes) is split into its
-                                      shapes' 3x3 blocks instead of one block of 6, 12 or 24 */
+                                      TPZBlockDiagonalStructMatrix connect blocks, one block of
+                                      NShape x NState equations per connect.  CG and the mixed CG
+                                      invert each whole connect block (3x3 blocks when every
+                                      connect carries one shape, p <= 2; blocks of 6, 12, 24 ...
+                                      for the connects of order 3).  GMRES splits a larger connect
+                                      block into its shapes' 3x3 blocks */
+#define GPZ_PRECOND_NODESET_JACOBI 3 /* node-set blocks: TPZAnalysis::BuildPreconditioner(EBlockJacobi,
+                                      overlap = false) (Analysis/TPZAnalysis.cpp:1008-1085,1093-1107):
+                                      the blocks of gpz_nodeset_blocks (TPZNodesetCompute) of the
+                                      mesh's element graph, each inverted on the device (Gauss-Jordan
+                                      without pivoting, the TPZSparseBlockDiagonal LU without
+                                      pivoting up to rounding); CG and the mixed CG only */
+
+#define GPZ_PRECOND_TWO_LEVEL 4    /* mixed CG only; no counterpart among BuildPreconditioner's options (the
+                                      reference's multigrid is TPZMGSolver, Solvers/Multigrid/pzmgsolver.cpp,
+                                      over a TPZTransfer between meshes).  Additive two-level block Jacobi:
+                                      M = B^-1 + P Ac^-1 P^T with B the 3x3 connect blocks of
+                                      GPZ_PRECOND_BLOCK_JACOBI, P the trilinear interpolation from a coarse
+                                      grid of boxes (each s^3 fine elements; gpz_two_level_config) to the
+                                      vertex connects, Ac = P^T A P the Galerkin coarse matrix (coarse
+                                      nodes touching a penalty-Dirichlet equation removed), inverted on
+                                      the device.  Needs one uniform grid of axis-aligned Q2 hex
+                                      elasticity elements (every element a translate of one box) and at
+                                      most 3000 coarse equations; GPZ_E_INVALID otherwise. */
 
 typedef struct {
   int32_t solver;          /* GPZ_SOLVER_* */
@@ -282,7 +301,9 @@ typedef struct {
                               3 TMA-staged block CSR, 4 upper triangle with float4 atomics,
                               5 matrix-free elements (uniform Q2 hex elasticity + penalty faces),
                               6 the same on the tensor cores (tcgen05, 3xTF32),
-                              7 the same sum-factorised on Lagrange nodal values */
+                              7 the same sum-factorised on Lagrange nodal values,
+                              8 the same when every element has one affine Jacobian (uniform grid):
+                                K_e = mu_e Khat as one tcgen05 3xTF32 GEMM per tile of elements */
 } gpz_solver_opts;
 
 typedef struct {
@@ -295,6 +316,21 @@ typedef struct {
   int64_t reliable_updates;
   int64_t restarts;        /* mixed CG: direction restarts at residual replacement */
 } gpz_solve_report;
+
+/* z = M r for one preconditioner of the assembled system, as the solvers apply
+ * it: TPZStepSolver::Solve on the preconditioner step solver
+ * (Solvers/pzstepsolver.cpp:64-169; Jacobi, the connect / node-set block
+ * Jacobi of BuildPreconditioner, FP64) or the mixed CG's two-level
+ * preconditioner (FP32).  Host vectors of the system's size. */
+int gpz_precond_apply(gpz_ctx *ctx, int precond, const double *r, double *z);
+
+/* Two-level preconditioner: coarse boxes per direction asked for (default 8;
+ * the grid takes the divisor s of its cell counts that comes closest), and
+ * after a two-level solve its shape: info[9] = fine cells per direction (3),
+ * s, coarse boxes per direction (3), coarse equations, removed coarse nodes.
+ * No counterpart in the reference. */
+int gpz_two_level_config(gpz_ctx *ctx, int coarse_boxes);
+int gpz_two_level_info(gpz_ctx *ctx, int64_t *info);
 
 /* b: host load vector (NULL = use the assembled device rhs); x: host solution
  * (in: initial guess if from_current, out: solution; may be NULL to keep the

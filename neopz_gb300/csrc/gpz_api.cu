@@ -174,6 +174,9 @@ int gpz_mesh_upload(gpz_ctx *ctx, const gpz_mesh_desc *d) {
     c.er.reset();
     c.have_mesh = true;
     c.have_pattern = c.have_matrix = c.have_solution = c.have_a32 = c.have_bjinv = c.have_rhs = false;
+    c.have_vbinv = false;
+    c.vb_kind = 0;
+    c.tl.ready = c.tl.have_inv = false;
     drop_assembly_graph(c);
     return GPZ_OK;
   });
@@ -188,6 +191,36 @@ int gpz_mesh_set_coef(gpz_ctx *ctx, const double *el_coef) {
     c.have_matrix = c.have_solution = c.have_rhs = false;
     if (c.d_coef.p != before) drop_assembly_graph(c);  // the captured kernels hold the coefficient pointer
     GPZ_CUDA_TRY(cudaStreamSynchronize(c.stream));
+    return GPZ_OK;
+  });
+}
+
+int gpz_precond_apply(gpz_ctx *ctx, int precond, const double *r, double *z) {
+  return guarded(ctx, [&](Ctx &c) {
+    GPZ_REQUIRE(c.have_matrix, GPZ_E_NOT_READY, "no assembled matrix");
+    GPZ_REQUIRE(r && z, GPZ_E_INVALID, "null vector");
+    precond_apply(c, precond, r, z);
+    return GPZ_OK;
+  });
+}
+
+int gpz_two_level_config(gpz_ctx *ctx, int coarse_boxes) {
+  return guarded(ctx, [&](Ctx &c) {
+    GPZ_REQUIRE(coarse_boxes >= 1 && coarse_boxes <= 64, GPZ_E_INVALID, "coarse boxes per direction: 1..64");
+    c.tl.target = coarse_boxes;
+    c.tl.ready = c.tl.have_inv = false;
+    return GPZ_OK;
+  });
+}
+
+int gpz_two_level_info(gpz_ctx *ctx, int64_t *info) {
+  return guarded(ctx, [&](Ctx &c) {
+    GPZ_REQUIRE(info, GPZ_E_INVALID, "null info");
+    GPZ_REQUIRE(c.tl.ready, GPZ_E_NOT_READY, "no two-level solve on this mesh yet");
+    const TwoLevel &T = c.tl;
+    const int64_t v[8] = {T.lx[0], T.lx[1], T.lx[2], T.s, T.m[0], T.m[1], T.m[2], T.nc};
+    for (int k = 0; k < 8; k++) info[k] = v[k];
+    info[8] = T.nfixed;
     return GPZ_OK;
   });
 }
@@ -214,6 +247,9 @@ int gpz_equation_filter(gpz_ctx *ctx, int64_t nactive, const int64_t *active) {
     c.have_a32 = false;
     c.have_bsr3 = false;
     c.have_bjinv = false;
+    c.have_vbinv = false;
+    c.vb_kind = 0;
+    c.tl.ready = c.tl.have_inv = false;
     c.spmv32_tuned = -1;
     drop_assembly_graph(c);
     return GPZ_OK;
@@ -457,7 +493,7 @@ int gpz_spmv(gpz_ctx *ctx, double alpha, const double *x, double beta, const dou
 int gpz_spmv_fp32(gpz_ctx *ctx, int variant, const double *x, double *y) {
   return guarded(ctx, [&](Ctx &c) {
     GPZ_REQUIRE(c.have_matrix, GPZ_E_NOT_READY, "not assembled");
-    GPZ_REQUIRE(x && y && variant >= -1 && variant <= 7, GPZ_E_INVALID, "arguments");
+    GPZ_REQUIRE(x && y && variant >= -1 && variant <= 8, GPZ_E_INVALID, "arguments");
     spmv32_apply(c, variant, x, y);
     return GPZ_OK;
   });

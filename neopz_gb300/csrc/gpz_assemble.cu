@@ -841,6 +841,8 @@ void assemble_fp64(Ctx &c) {
   GPZ_CUDA_TRY(cudaGetLastError());
   c.have_a32 = false;
   c.have_bjinv = false;
+  c.have_vbinv = false;
+  c.tl.have_inv = false;
 }
 
 // load vector alone (TPZStructMatrix::Assemble(rhs), StrMatrix/pzstrmatrixor.cpp:75-103):

@@ -168,6 +168,41 @@ struct MatFree {
   bool sf_ready = false;                     // the sum-factorised tables of the volume bucket were built
   DBuf<float> sf_tab;                        // 1D Lagrange values / derivatives, weights, corner gradients, Phi
   DBuf<int> sf_idx;
+  // shared element matrix: every volume element has the same affine Jacobian,
+  // so K_e = mu_e Khat; Khat (81 x 81, for mu = 1) split into TF32 hi / lo in
+  // the tensor-core operand layout
+  bool gm_ready = false;
+  int grid_gm = 1;
+  DBuf<float> gm_b;                          // [2][96 x 88] hi, lo (K-major core matrices)
+  DBuf<double> gm_ref;                       // element 0's Jinv (9) and |det J|
+  DBuf<int> gm_flag;
+};
+
+// ---------------------------------------------------------------- two-level preconditioner
+// Additive two-level block Jacobi for uniform Q2 hex grids (every volume
+// element a translate of one axis-aligned box): M = B^-1 + P Ac^-1 P^T with B
+// the 3x3 connect blocks, P the trilinear interpolation from a coarse grid of
+// m^3 boxes (s^3 fine elements each) to the vertex connects, Ac = P^T A P the
+// Galerkin coarse matrix (from the vertex block of the element matrix, exact for
+// the hierarchical basis: its vertex functions are the trilinear ones), coarse
+// nodes whose functions touch a penalty-Dirichlet equation removed.
+struct TwoLevel {
+  bool ready = false;                        // geometry part built for the current mesh
+  bool have_inv = false;                     // coarse inverse of the current assembly
+  int target = 8;                            // coarse boxes per direction asked for
+  int64_t lx[3] = {0, 0, 0};                 // fine lattice cells per direction
+  int s = 0;                                 // fine cells per coarse box (every direction)
+  int m[3] = {0, 0, 0};                      // coarse boxes per direction
+  int64_t nnode = 0, nc = 0, ncell = 0, nfixed = 0;
+  double mufac = 0.0, E0 = 1.0;              // mu_e = coef_e * mufac (E0 without coefficients)
+  DBuf<int32_t> vtx_eq;                      // [(lx+1)(ly+1)(lz+1)] first equation of the vertex, -1 none
+  DBuf<int32_t> brow_vtx;                    // [nbrow] lattice vertex of a vertex block row, -1 otherwise
+  DBuf<int32_t> cell_off, cell_el, el_sub;   // volume elements grouped by coarse box; sub position
+  DBuf<double> tsub;                         // [s^3][24][24] P^T Khat_vv P for mu = 1
+  DBuf<int32_t> cfix;                        // [nnode] 1: removed (touches a penalty equation)
+  DBuf<double> ac, piv;                      // [nc][nc] coarse matrix, then its inverse; pivot row / column
+  DBuf<float> acinv32;                       // [nc][nc]
+  DBuf<float> rc, zc, z32;                   // coarse residual / correction, preconditioned residual
 };
 
 // ---------------------------------------------------------------- the context
@@ -281,6 +316,18 @@ struct Ctx {
   DBuf<double> d_bjinv;                      // block-Jacobi inverses [neq/3][9]
   DBuf<float> d_bjinv32, d_dinv32;           // FP32 preconditioners of the mixed CG
   bool have_bjinv = false;
+  // variable-size block Jacobi (whole connect blocks of any size, or the
+  // node-set blocks): block b holds equations vb_eq[vb_off[b] .. vb_off[b+1])
+  // and its inverse (row-major) at vb_inv[vb_ioff[b]]
+  int vb_kind = 0;                           // 0 none, GPZ_PRECOND_BLOCK_JACOBI or GPZ_PRECOND_NODESET_JACOBI
+  int64_t vb_nb = 0;
+  int vb_maxn = 0;
+  DBuf<int64_t> d_vb_off, d_vb_eq, d_vb_ioff;
+  DBuf<int32_t> d_vb_eqblk, d_vb_eqloc;      // equation -> block, position inside it
+  DBuf<double> d_vb_inv;
+  DBuf<float> d_vb_inv32;
+  bool have_vbinv = false;
+  TwoLevel tl;
   int bj_bs = 0;
 
   SolverWork sw;
@@ -318,11 +365,14 @@ void build_block_jacobi(Ctx &c);
 void spmv_device(Ctx &c, const double *x, double *y, double alpha, double beta, const double *yin);
 int solve(Ctx &c, const gpz_solver_opts &o, gpz_solve_report &rep);
 void spmv32_apply(Ctx &c, int variant, const double *hx, double *hy);
+void precond_apply(Ctx &c, int precond, const double *hr, double *hz);
 int collect_cg_pairs(Ctx &c, int npairs, double tol, int64_t max_iter, double *R, double *X, double *xstar,
                      int64_t *iters);
 // matfree.cu
 bool matfree_build(Ctx &c);
-void matfree_spmv(Ctx &c, cudaStream_t s, int mode);  // 0 CUDA cores, 1 tcgen05, 2 sum-factorised
+int two_level_build(Ctx &c);     // geometry part (once per mesh); GPZ_OK or GPZ_E_INVALID when not a uniform grid
+void two_level_assemble(Ctx &c); // coarse matrix and its inverse for the current assembly
+void matfree_spmv(Ctx &c, cudaStream_t s, int mode);  // 0 CUDA cores, 1 tcgen05, 2 sum-factorised, 3 shared matrix
 // learned.cu
 void learned_prepare(Ctx &c);
 void ensure_node_incidence(Ctx &c);                // features, scaling and factors F for the assembled system

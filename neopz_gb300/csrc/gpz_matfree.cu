@@ -18,7 +18,9 @@
 // gradients sit in shared memory, both loaded once per CTA; per element the
 // nodal values and the per-point stress pass through shared memory.  p^T q is
 // the sum of the element energies u_e^T K_e u_e.
+#include <algorithm>
 #include <cmath>
+#include <cstring>
 #include <vector>
 
 #include "gpz_internal.h"
@@ -684,7 +686,7 @@ constexpr int kTcItems = (kTcEl * 27 + kTcThreads - 1) / kTcThreads;  // (elemen
 constexpr int kTcWaitTries = 1 << 22;
 
 __device__ __forceinline__ uint32_t tc_smem(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
-__device__ __forceinline__ uint32_t kmaj(int r, int k, int kcols) {
+__host__ __device__ __forceinline__ uint32_t kmaj(int r, int k, int kcols) {
   return ((uint32_t)(r >> 3) * (uint32_t)(kcols >> 2) + (uint32_t)(k >> 2)) * 128u + (uint32_t)(r & 7) * 16u +
          (uint32_t)(k & 3) * 4u;
 }
@@ -1023,6 +1025,417 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_mf_hex27_tc(int64_t n, const 
   }
 }
 
+
+// ---------------------------------------------------------------- shared element matrix on the tensor cores
+// When every volume element has the same affine Jacobian (a uniform grid: the
+// elements differ by a translation) and one Poisson ratio, every element
+// matrix is one matrix scaled by the element's shear modulus, K_e = mu_e Khat
+// (TPZElasticity3D's C1, C2, C3 are all proportional to E).  The operator over
+// a tile of 128 elements is then one product
+//   Y[e][n] = sum_k U[e][k] Khat[n][k],   k, n = 3 a + s (shape a, component s),
+// with U the elements' gathered coefficients: tcgen05.mma kind::tf32 with the
+// 3xTF32 split (hi.hi + hi.lo + lo.hi, FP32 accumulation in TMEM), M = 128
+// elements, N = 96 (81 rows), K = 88 (81 columns), both operands K-major
+// without swizzle.  Thread t gathers half of element (t mod 128)'s row (shapes
+// [0, 12) or [12, 27)) and later scatters half of its results (TMEM columns
+// [0, 48) or [48, 96)) with float4 atomics, scaled by mu_e; the element energy
+// mu_e Y[e] . U[e] gives p.q.  Two TMEM accumulator pairs (hi.hi and the
+// correction products, 4 x 128 of the 512 columns: one CTA per SM) let the
+// MMAs of the next tile run while the current tile's results are scattered.  Every wait is
+// bounded: on a timeout the kernel records an error flag, waits (bounded) for
+// the MMAs in flight, frees its TMEM and leaves.
+constexpr int kGmThreads = 256;
+constexpr int kGmEl = 128;                  // elements per tile (MMA M)
+constexpr int kGmK = 88, kGmN = 96;         // padded K (81) and N (81)
+constexpr int kGmSplit = 12;                // gather: shapes [0, 12) by threads 0..127, [12, 27) by 128..255
+constexpr uint32_t kGmSmall = 128;          // TMEM column offset of the correction accumulator
+constexpr int64_t kTlMaxNc = 3000;          // largest coarse system of the two-level preconditioner
+constexpr uint32_t kGmB = kGmN * kGmK * 4, kGmA = kGmEl * kGmK * 4;
+constexpr uint32_t GM_BH = 0, GM_BL = kGmB, GM_AH = 2 * kGmB, GM_AL = 2 * kGmB + kGmA, GM_END = 2 * kGmB + 2 * kGmA;
+static_assert(GM_AH % 1024 == 0 && GM_AL % 1024 == 0 && GM_END % 1024 == 0, "operand alignment");
+
+__device__ __forceinline__ float4 tf32_split4(float4 v, float4 &lo) {
+  float4 h;
+  h.x = tf32_rna(v.x);
+  h.y = tf32_rna(v.y);
+  h.z = tf32_rna(v.z);
+  h.w = tf32_rna(v.w);
+  lo.x = tf32_rna(v.x - h.x);
+  lo.y = tf32_rna(v.y - h.y);
+  lo.z = tf32_rna(v.z - h.z);
+  lo.w = tf32_rna(v.w - h.w);
+  return h;
+}
+
+// Half of one element's row of U: shapes [A0, A1) -> columns [3 A0, 3 A1),
+// the last half also writes the zero padding up to K.  Rows of elements past
+// the end are zero.
+template <int A0, int A1>
+__device__ __forceinline__ void gm_gather(unsigned char *sm, int64_t e, bool valid, int le,
+                                          const int32_t *__restrict__ rows, const float4 *__restrict__ p4) {
+  constexpr int NA = A1 - A0, K0 = 3 * A0, K1 = A1 == kNS ? kGmK : 3 * A1, NV = K1 - K0;
+  static_assert(K0 % 4 == 0 && NV % 4 == 0, "16-byte chunks");
+  int32_t r[NA];
+#pragma unroll
+  for (int a = 0; a < NA; a++) r[a] = valid ? rows[e * kNS + A0 + a] : -1;
+  float v[NV];
+#pragma unroll
+  for (int k = 0; k < NV; k++) v[k] = 0.f;
+#pragma unroll
+  for (int a = 0; a < NA; a++) {
+    const float4 pv = r[a] >= 0 ? p4[r[a]] : make_float4(0.f, 0.f, 0.f, 0.f);
+    v[3 * a] = pv.x;
+    v[3 * a + 1] = pv.y;
+    v[3 * a + 2] = pv.z;
+  }
+#pragma unroll
+  for (int c = 0; c < NV / 4; c++) {
+    float4 lo;
+    const float4 hi = tf32_split4(make_float4(v[4 * c], v[4 * c + 1], v[4 * c + 2], v[4 * c + 3]), lo);
+    const uint32_t off = kmaj(le, K0 + 4 * c, kGmK);
+    *(float4 *)(sm + GM_AH + off) = hi;
+    *(float4 *)(sm + GM_AL + off) = lo;
+  }
+}
+
+// Half of one element's results: TMEM columns [C0, C0 + 48) of the warp's
+// lane quarter (lane = element), shapes [A0, A1).
+template <int C0, int A0, int A1>
+__device__ __forceinline__ void gm_scatter(uint32_t taddr, int64_t e, bool valid, const int32_t *__restrict__ rows,
+                                           const float *__restrict__ rlm, const float4 *__restrict__ p4,
+                                           float4 *__restrict__ q4, KSum &en) {
+  float y[48], ys[16];
+#pragma unroll
+  for (int c = 0; c < 48; c += 16) {
+    tc_ld16(taddr + C0 + c, y + c);
+    tc_ld16(taddr + kGmSmall + C0 + c, ys);
+#pragma unroll
+    for (int j = 0; j < 16; j++) y[c + j] += ys[j];
+  }
+  if (!valid) return;
+  const float mu = rlm[2 * e + 1];
+#pragma unroll
+  for (int a = A0; a < A1; a++) {
+    const int j = 3 * a - C0;
+    const int32_t r = rows[e * kNS + a];
+    const float4 pv = p4[r];
+    const float4 yv = make_float4(mu * y[j], mu * y[j + 1], mu * y[j + 2], 0.f);
+    en.add(yv.x * pv.x + yv.y * pv.y + yv.z * pv.z);
+    atomicAdd(&q4[r], yv);
+  }
+}
+
+// hi.hi into the accumulator at column tm, the correction products hi.lo + lo.hi
+// into their own accumulator at tm + kGmSmall: summed at their own scale, they
+// are not rounded against the large hi.hi sums (the epilogue adds the two)
+__device__ __forceinline__ void gm_mma(uint32_t tm, uint32_t ah, uint32_t al, uint32_t bh, uint32_t bl) {
+  const uint32_t id = (1u << 4) | (2u << 7) | (2u << 10) | ((uint32_t)(kGmN >> 3) << 17) | ((uint32_t)(kGmEl >> 4) << 24);
+  constexpr uint32_t sbo = (kGmK / 4) * 128;
+#pragma unroll 1
+  for (int k = 0; k < kGmK / 8; k++) {
+    const uint64_t dah = tc_desc(ah + k * 256, sbo), dal = tc_desc(al + k * 256, sbo);
+    const uint64_t dbh = tc_desc(bh + k * 256, sbo), dbl = tc_desc(bl + k * 256, sbo);
+    tc_mma(tm + kGmSmall, dal, dbh, id, k > 0);
+    tc_mma(tm + kGmSmall, dah, dbl, id, 1u);
+    tc_mma(tm, dah, dbh, id, k > 0);
+  }
+}
+
+__global__ void __launch_bounds__(kGmThreads, 1) k_mf_hex27_gm(int64_t n, const int32_t *__restrict__ rows,
+                                                               const float *__restrict__ rlm,
+                                                               const float4 *__restrict__ bsplit,
+                                                               const float4 *__restrict__ p4, float4 *__restrict__ q4,
+                                                               const double *__restrict__ face_energy,
+                                                               int *__restrict__ err, Red R) {
+  if (!active(R.iscal)) return;
+  extern __shared__ __align__(1024) unsigned char sm[];
+  __shared__ uint32_t s_tmem;
+  __shared__ __align__(8) uint64_t s_mb[2];
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const int le = tid & (kGmEl - 1), half = tid >> 7;
+  // Khat hi / lo, already in the operand layout
+  for (uint32_t i = tid; i < 2 * kGmB / 16; i += kGmThreads) ((float4 *)(sm + GM_BH))[i] = bsplit[i];
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(tc_smem(&s_tmem)), "r"(512));
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+  }
+  if (tid == 0) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(tc_smem(&s_mb[0])));
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(tc_smem(&s_mb[1])));
+    asm volatile("fence.mbarrier_init.release.cluster;");
+  }
+  const uint32_t ah = tc_smem(sm + GM_AH), al = tc_smem(sm + GM_AL), bh = tc_smem(sm + GM_BH),
+                 bl = tc_smem(sm + GM_BL);
+  int64_t tile = blockIdx.x;
+  const int64_t ntile = (n + kGmEl - 1) / kGmEl;
+  if (tile < ntile) {
+    const int64_t e = tile * kGmEl + le;
+    if (half == 0) gm_gather<0, kGmSplit>(sm, e, e < n, le, rows, p4);
+    else gm_gather<kGmSplit, kNS>(sm, e, e < n, le, rows, p4);
+  }
+  asm volatile("fence.proxy.async.shared::cta;");
+  asm volatile("tcgen05.fence::before_thread_sync;");
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;");
+  const uint32_t tm = s_tmem;
+  if (tile < ntile && tid == 0) {
+    gm_mma(tm, ah, al, bh, bl);
+    tc_commit(&s_mb[0]);
+  }
+  KSum en;
+  uint32_t phase[2] = {0u, 0u};
+  int it = 0;
+  bool failed = false;
+  for (; tile < ntile; tile += gridDim.x, it++) {
+    const int b = it & 1;
+    const bool ok = tc_wait(&s_mb[b], phase[b]);
+    if (__syncthreads_or(!ok)) {
+      failed = true;
+      break;
+    }
+    phase[b] ^= 1u;
+    asm volatile("tcgen05.fence::after_thread_sync;");
+    // the operand U is free: the next tile's gather, then its MMAs into the other accumulator
+    const int64_t next = tile + gridDim.x;
+    if (next < ntile) {
+      const int64_t e = next * kGmEl + le;
+      if (half == 0) gm_gather<0, kGmSplit>(sm, e, e < n, le, rows, p4);
+      else gm_gather<kGmSplit, kNS>(sm, e, e < n, le, rows, p4);
+    }
+    asm volatile("fence.proxy.async.shared::cta;");
+    asm volatile("tcgen05.fence::before_thread_sync;");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;");
+    if (next < ntile && tid == 0) {
+      gm_mma(tm + (uint32_t)(b ^ 1) * 256u, ah, al, bh, bl);
+      tc_commit(&s_mb[b ^ 1]);
+    }
+    // this tile's results: warp w reads TMEM lanes 32 (w mod 4) .. + 31 (its elements)
+    const int64_t e = tile * kGmEl + le;
+    const uint32_t taddr = tm + ((uint32_t)((warp & 3) * 32) << 16) + (uint32_t)b * 256u;
+    if (half == 0) gm_scatter<0, 0, 16>(taddr, e, e < n, rows, rlm, p4, q4, en);
+    else gm_scatter<48, 16, kNS>(taddr, e, e < n, rows, rlm, p4, q4, en);
+    asm volatile("tcgen05.fence::before_thread_sync;");
+  }
+  if (failed) {
+    if (tid == 0) atomicOr(err, 16384);
+    // the MMAs in flight write the accumulators: let them finish (bounded) before the TMEM is released
+    tc_wait(&s_mb[it & 1], phase[it & 1]);
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;");
+  __syncthreads();
+  if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tm), "r"(512));
+  double v[1] = {failed ? 0.0 : en.get()}, tot[1];
+  if (grid_reduce<1>(v, R, tot) && threadIdx.x == 0) {
+    const double pq = tot[0] + (face_energy ? *face_energy : 0.0);
+    R.scal[S_PQ] = pq;
+    R.scal[S_ALPHA] = R.scal[S_RHO] / pq;
+    R.iscal[I_SP32]++;
+  }
+}
+
+// The FP64 affine Jacobian of every volume element against element 0's: flag 1
+// when one is not affine or differs (the shared element matrix does not apply);
+// element 0's Jinv (row-major, Jinv[j][d] = d xi_j / d x_d) and |det J| to ref.
+__device__ bool gm_affine(const int64_t *__restrict__ el_nodes, const double *__restrict__ xyz, int64_t e,
+                          double (&a)[3][3], double &scale) {
+  const signed char sg[8][3] = {{-1, -1, -1}, {1, -1, -1}, {1, 1, -1}, {-1, 1, -1},
+                                {-1, -1, 1},  {1, -1, 1},  {1, 1, 1},  {-1, 1, 1}};
+  double cx[8][3];
+  for (int k = 0; k < 8; k++)
+    for (int j = 0; j < 3; j++) cx[k][j] = xyz[el_nodes[e * 8 + k] * 3 + j];
+  double hi = 0.0, big = 0.0;
+  for (int j = 0; j < 3; j++) {
+    double t4 = 0, t5 = 0, t6 = 0, t7 = 0, mn = cx[0][j], mx = cx[0][j];
+    for (int k = 0; k < 8; k++) {
+      const double x = cx[k][j];
+      t4 += sg[k][0] * sg[k][1] * x;
+      t5 += sg[k][0] * sg[k][2] * x;
+      t6 += sg[k][1] * sg[k][2] * x;
+      t7 += sg[k][0] * sg[k][1] * sg[k][2] * x;
+      mn = fmin(mn, x);
+      mx = fmax(mx, x);
+    }
+    hi = fmax(hi, fmax(fmax(fabs(t4), fabs(t5)), fmax(fabs(t6), fabs(t7))));
+    big = fmax(big, mx - mn);
+    for (int d = 0; d < 3; d++) {
+      double t = 0.0;
+      for (int k = 0; k < 8; k++) t += sg[k][d] * cx[k][j];
+      a[j][d] = t / 8.0;
+    }
+  }
+  scale = big;
+  return hi <= 1e-12 * big;
+}
+
+__global__ void k_mf_uniform(int64_t n, const int64_t *__restrict__ elems, const int64_t *__restrict__ el_nodes,
+                             const double *__restrict__ xyz, double *__restrict__ ref, int *__restrict__ flag) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  double a0[3][3], a[3][3], s0, s;
+  const bool aff0 = gm_affine(el_nodes, xyz, elems[0], a0, s0);
+  const bool aff = gm_affine(el_nodes, xyz, elems[i], a, s);
+  bool same = aff0 && aff;
+  for (int j = 0; j < 3; j++)
+    for (int d = 0; d < 3; d++) same = same && fabs(a[j][d] - a0[j][d]) <= 1e-12 * s0;
+  if (!same) atomicOr(flag, 1);
+  if (i == 0 && aff0) {
+    const double det = -a0[0][2] * a0[1][1] * a0[2][0] + a0[0][1] * a0[1][2] * a0[2][0] +
+                       a0[0][2] * a0[1][0] * a0[2][1] - a0[0][0] * a0[1][2] * a0[2][1] -
+                       a0[0][1] * a0[1][0] * a0[2][2] + a0[0][0] * a0[1][1] * a0[2][2];
+    const double id = 1.0 / det;
+    ref[0] = (-a0[1][2] * a0[2][1] + a0[1][1] * a0[2][2]) * id;
+    ref[1] = (a0[0][2] * a0[2][1] - a0[0][1] * a0[2][2]) * id;
+    ref[2] = (-a0[0][2] * a0[1][1] + a0[0][1] * a0[1][2]) * id;
+    ref[3] = (a0[1][2] * a0[2][0] - a0[1][0] * a0[2][2]) * id;
+    ref[4] = (-a0[0][2] * a0[2][0] + a0[0][0] * a0[2][2]) * id;
+    ref[5] = (a0[0][2] * a0[1][0] - a0[0][0] * a0[1][2]) * id;
+    ref[6] = (-a0[1][1] * a0[2][0] + a0[1][0] * a0[2][1]) * id;
+    ref[7] = (a0[0][1] * a0[2][0] - a0[0][0] * a0[2][1]) * id;
+    ref[8] = (-a0[0][1] * a0[1][0] + a0[0][0] * a0[1][1]) * id;
+    ref[9] = fabs(det);
+  }
+}
+
+
+// ---------------------------------------------------------------- two-level preconditioner: set-up kernels
+// hex corner k at lattice offset (kOffX[k], kOffY[k], kOffZ[k]) from corner 0
+__constant__ int c_tlOff[8][3] = {{0, 0, 0}, {1, 0, 0}, {1, 1, 0}, {0, 1, 0}, {0, 0, 1}, {1, 0, 1}, {1, 1, 1}, {0, 1, 1}};
+
+// lattice coordinates of every volume element's corner 0 relative to element
+// 0's (box size h); lmm[0..2] min, lmm[3..5] max over all corners; err bit
+// 1 << 17 when a corner is off the lattice
+__global__ void k_tl_lattice(int64_t n, const int64_t *__restrict__ elems, const int64_t *__restrict__ el_nodes,
+                             const double *__restrict__ xyz, double x0, double y0, double z0, double hx, double hy,
+                             double hz, int32_t *__restrict__ lat, int *__restrict__ lmm, int *__restrict__ err) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const int64_t e = elems[i];
+  const double o[3] = {x0, y0, z0}, h[3] = {hx, hy, hz};
+  int l0[3] = {0, 0, 0};
+  for (int k = 0; k < 8; k++) {
+    const int64_t node = el_nodes[e * 8 + k];
+    for (int d = 0; d < 3; d++) {
+      const double t = (xyz[node * 3 + d] - o[d]) / h[d];
+      const long long li = llround(t);
+      if (fabs(t - (double)li) > 1e-6 || li < -(1ll << 30) || li > (1ll << 30)) atomicOr(err, 1 << 17);
+      if (k == 0) l0[d] = (int)li;
+      else if ((int)li - l0[d] != c_tlOff[k][d]) atomicOr(err, 1 << 17);
+      atomicMin(&lmm[d], (int)li);
+      atomicMax(&lmm[3 + d], (int)li);
+    }
+  }
+  for (int d = 0; d < 3; d++) lat[i * 3 + d] = l0[d];
+}
+
+// vertex map, coarse box and sub position of every volume element
+__global__ void k_tl_vertices(int64_t n, const int64_t *__restrict__ elems, const int64_t *__restrict__ el_conn,
+                              const int64_t *__restrict__ bpos, const int32_t *__restrict__ lat, int mx, int my, int mz,
+                              int lx0, int ly0, int lz0, int nvx, int nvy, int s, int mcx, int mcy,
+                              int32_t *__restrict__ vtx_eq, int32_t *__restrict__ el_cell, int32_t *__restrict__ el_sub) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const int64_t e = elems[i];
+  const int a = lat[i * 3] - mx, b = lat[i * 3 + 1] - my, c = lat[i * 3 + 2] - mz;
+  for (int k = 0; k < 8; k++) {
+    const int64_t v = (int64_t)(a + c_tlOff[k][0]) + (int64_t)nvx * ((b + c_tlOff[k][1]) + (int64_t)nvy * (c + c_tlOff[k][2]));
+    vtx_eq[v] = (int32_t)bpos[el_conn[e * 27 + k]];
+  }
+  const int I = a / s, J = b / s, K = c / s;
+  el_cell[i] = I + mcx * (J + mcy * K);
+  el_sub[i] = (a - I * s) + s * ((b - J * s) + s * (c - K * s));
+  (void)lx0; (void)ly0; (void)lz0;
+}
+
+__global__ void k_tl_browvtx(int64_t nv, const int32_t *__restrict__ vtx_eq, int32_t *__restrict__ brow_vtx) {
+  const int64_t v = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (v >= nv) return;
+  const int32_t eq = vtx_eq[v];
+  if (eq >= 0) brow_vtx[eq / 3] = (int32_t)v;
+}
+
+// coarse nodes whose trilinear function is nonzero at a vertex of a penalty face
+__global__ void k_tl_fixnodes(int64_t n, const int64_t *__restrict__ elems, const int64_t *__restrict__ el_conn,
+                              const int64_t *__restrict__ bpos, const int32_t *__restrict__ brow_vtx, int nvx, int nvy,
+                              int s, int mcx, int mcy, int mcz, int32_t *__restrict__ cfix) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const int64_t e = elems[i];
+  for (int k = 0; k < 4; k++) {
+    const int32_t v = brow_vtx[bpos[el_conn[e * 27 + k]] / 3];
+    if (v < 0) continue;
+    const int vi = v % nvx, vj = (v / nvx) % nvy, vk = v / (nvx * nvy);
+    const int I = min(vi / s, mcx - 1), J = min(vj / s, mcy - 1), K = min(vk / s, mcz - 1);
+    const int ri = vi - I * s, rj = vj - J * s, rk = vk - K * s;
+    for (int cn = 0; cn < 8; cn++) {
+      const int bx = c_tlOff[cn][0], by = c_tlOff[cn][1], bz = c_tlOff[cn][2];
+      const bool nz = (bx ? ri > 0 : ri < s) && (by ? rj > 0 : rj < s) && (bz ? rk > 0 : rk < s);
+      if (nz) cfix[(I + bx) + (mcx + 1) * ((J + by) + (mcy + 1) * (K + bz))] = 1;
+    }
+  }
+}
+
+// coarse box matrices sum_e mu_e T[sub_e], scattered into the dense coarse matrix
+__global__ void __launch_bounds__(256) k_tl_cells(const int32_t *__restrict__ cell_off,
+                                                  const int32_t *__restrict__ cell_el,
+                                                  const int32_t *__restrict__ el_sub, const int64_t *__restrict__ elems,
+                                                  const double *__restrict__ coef, double E0, double mufac,
+                                                  const double *__restrict__ tsub, int mcx, int mcy, int64_t nc,
+                                                  double *__restrict__ ac) {
+  const int cell = blockIdx.x;
+  const int I = cell % mcx, J = (cell / mcx) % mcy, K = cell / (mcx * mcy);
+  for (int t = threadIdx.x; t < 576; t += blockDim.x) {
+    double acc = 0.0;
+    for (int32_t k = cell_off[cell]; k < cell_off[cell + 1]; k++) {
+      const int32_t i = cell_el[k];
+      const double mu = (coef ? coef[elems[i]] : E0) * mufac;
+      acc += mu * tsub[(size_t)el_sub[i] * 576 + t];
+    }
+    const int r = t / 24, c = t % 24;  // (coarse corner, component)
+    const int rn = r / 3, rs = r % 3, cn = c / 3, cs = c % 3;
+    const int64_t nr = (I + c_tlOff[rn][0]) + (int64_t)(mcx + 1) * ((J + c_tlOff[rn][1]) + (int64_t)(mcy + 1) * (K + c_tlOff[rn][2]));
+    const int64_t ncn = (I + c_tlOff[cn][0]) + (int64_t)(mcx + 1) * ((J + c_tlOff[cn][1]) + (int64_t)(mcy + 1) * (K + c_tlOff[cn][2]));
+    atomicAdd(&ac[(3 * nr + rs) * nc + 3 * ncn + cs], acc);
+  }
+}
+
+// removed coarse nodes: zero row and column, unit diagonal
+__global__ void k_tl_fixrows(int64_t nc, const int32_t *__restrict__ cfix, double *__restrict__ ac) {
+  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= nc * nc) return;
+  const int64_t i = t / nc, j = t % nc;
+  if (cfix[i / 3] || cfix[j / 3]) ac[t] = i == j ? 1.0 : 0.0;
+}
+
+// in-place Gauss-Jordan inversion of the SPD coarse matrix, no pivoting: step k
+// in two launches, the pivot row and column saved first
+__global__ void k_tl_gj_save(int64_t n, int64_t k, const double *__restrict__ A, double *__restrict__ piv) {
+  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t < n) piv[t] = A[k * n + t];
+  else if (t < 2 * n) piv[t] = A[(t - n) * n + k];
+}
+__global__ void k_tl_gj_step(int64_t n, int64_t k, double *__restrict__ A, const double *__restrict__ piv,
+                             int *__restrict__ err) {
+  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= n * n) return;
+  const int64_t i = t / n, j = t % n;
+  const double p = piv[k];
+  if (t == 0 && !(p > 0.0)) atomicOr(err, 1 << 18);
+  const double ip = 1.0 / p;
+  double v;
+  if (i == k && j == k) v = ip;
+  else if (i == k) v = piv[j] * ip;
+  else if (j == k) v = -piv[n + i] * ip;
+  else v = A[t] - piv[n + i] * piv[j] * ip;
+  A[t] = v;
+}
+__global__ void k_tl_to32(int64_t n, const double *__restrict__ A, float *__restrict__ B) {
+  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= n * n) return;
+  const int64_t i = t / n, j = t % n;
+  B[t] = (float)(0.5 * (A[t] + A[j * n + i]));
+}
+
 template <class K>
 int mf_grid(K kernel, int threads) {
   int dev = 0, nsm = 0, per = 0;
@@ -1146,11 +1559,306 @@ bool sf_tables(Ctx &c, const Bucket &vol) {
   return true;
 }
 
+// TF32 (10-bit mantissa) rounding to nearest, ties away from zero: the value
+// cvt.rna.tf32.f32 gives, on the host
+static float tf32_round_host(float x) {
+  uint32_t b;
+  std::memcpy(&b, &x, 4);
+  if ((b & 0x7f800000u) != 0x7f800000u) b = (b + 0x1000u) & ~0x1fffu;
+  float r;
+  std::memcpy(&r, &b, 4);
+  return r;
+}
+
+// The element matrix of a Q2 hex elasticity element for mu = 1 (E = 2 + 2 nu,
+// TPZElasticity3D's CODE3 coefficients C1 = 1, C2, C3), from the bucket's
+// reference Gram and the element's constant Jinv / |det J| (ref[0..9]): the
+// formula of the FP64 affine assembly.  K[(3 a + s) * 81 + 3 b + t].
+static void khat_elasticity(const Bucket &vol, const double *ref, double nu, std::vector<double> &K) {
+  const double E = 2.0 + 2.0 * nu;
+  const double C1 = E / (2. + 2. * nu), C2 = E * nu / (-1. + nu + 2. * nu * nu),
+               C3 = E * (nu - 1.) / (-1. + nu + 2. * nu * nu);
+  double ji[3][3];
+  for (int k = 0; k < 9; k++) ji[k / 3][k % 3] = ref[k];
+  const double det = ref[9];
+  K.assign((size_t)81 * 81, 0.0);
+  for (int a = 0; a < kNS; a++)
+    for (int b = 0; b < kNS; b++) {
+      const double *G = vol.ghat.data() + ((size_t)a * kNS + b) * 9;
+      double M1[3][3], S[3][3];
+      for (int i = 0; i < 3; i++)
+        for (int e2 = 0; e2 < 3; e2++) M1[i][e2] = G[i * 3 + 0] * ji[0][e2] + G[i * 3 + 1] * ji[1][e2] + G[i * 3 + 2] * ji[2][e2];
+      for (int d = 0; d < 3; d++)
+        for (int e2 = 0; e2 < 3; e2++) S[d][e2] = det * (ji[0][d] * M1[0][e2] + ji[1][d] * M1[1][e2] + ji[2][d] * M1[2][e2]);
+      const double tr = S[0][0] + S[1][1] + S[2][2];
+      for (int si = 0; si < 3; si++)
+        for (int t = 0; t < 3; t++)
+          K[(size_t)(3 * a + si) * 81 + 3 * b + t] =
+              si == t ? (tr - S[si][si]) * C1 + S[si][si] * C3 : S[t][si] * C1 - S[si][t] * C2;
+    }
+}
+
+// The shared element matrix of a uniform volume bucket: every element's FP64
+// affine Jacobian is checked against element 0's on the device; when they all
+// agree, Khat (the element matrix for mu = 1, i.e. E = 2 + 2 nu) is formed in
+// FP64 from the bucket's reference Gram with TPZElasticity3D's CODE3
+// coefficients, as the FP64 assembly forms affine element matrices, and
+// uploaded split into TF32 hi / lo in the K-major operand layout.
+static bool gm_tables(Ctx &c, const Bucket &vol, double nu) {
+  MatFree &M = c.mf;
+  if (vol.ghat.empty() || vol.nshape != kNS) return false;
+  cudaStream_t s = c.stream;
+  M.gm_ref.alloc(10);
+  M.gm_flag.alloc(1);
+  M.gm_flag.zero(s);
+  M.gm_ref.zero(s);
+  k_mf_uniform<<<grid_for(M.nvol, 256), 256, 0, s>>>(M.nvol, vol.d_elems.p, c.d_el_nodes.p, c.d_xyz.p, M.gm_ref.p,
+                                                      M.gm_flag.p);
+  c.launches++;
+  GPZ_CUDA_TRY(cudaGetLastError());
+  int flag = 0;
+  double ref[10];
+  GPZ_CUDA_TRY(cudaMemcpyAsync(&flag, M.gm_flag.p, sizeof(int), cudaMemcpyDeviceToHost, s));
+  GPZ_CUDA_TRY(cudaMemcpyAsync(ref, M.gm_ref.p, sizeof(ref), cudaMemcpyDeviceToHost, s));
+  GPZ_CUDA_TRY(cudaStreamSynchronize(s));
+  if (flag != 0 || !(ref[9] > 0.0)) return false;
+  std::vector<double> K;
+  khat_elasticity(vol, ref, nu, K);
+  std::vector<float> hl(2 * kGmB / 4, 0.f);
+  for (int nn = 0; nn < 81; nn++)
+    for (int k = 0; k < 81; k++) {
+      const double v = K[(size_t)nn * 81 + k];
+      const float hi = tf32_round_host((float)v);
+      const float lo = tf32_round_host((float)(v - (double)hi));
+      const uint32_t off = kmaj(nn, k, kGmK) / 4;
+      hl[off] = hi;
+      hl[kGmB / 4 + off] = lo;
+    }
+  M.gm_b.upload(hl.data(), hl.size(), s);
+  GPZ_CUDA_TRY(cudaFuncSetAttribute(k_mf_hex27_gm, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)GM_END));
+  int dev = 0, nsm = 0;
+  GPZ_CUDA_TRY(cudaGetDevice(&dev));
+  GPZ_CUDA_TRY(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
+  M.grid_gm = std::max(1, std::min(kGridBlocks, nsm));  // one CTA per SM, persistent over tiles
+  GPZ_CUDA_TRY(cudaStreamSynchronize(s));
+  return true;
+}
+
+// ---------------------------------------------------------------- two-level preconditioner set-up
+// Geometry part, once per mesh: the fine lattice of the uniform grid, the
+// coarse boxes (s^3 elements each, about `target` boxes per direction), the
+// vertex map, the coarse nodes touching penalty-Dirichlet equations, and the
+// tables T[sub] = P_sub^T Khat_vv P_sub (mu = 1) of a fine element at each of
+// the s^3 positions inside its coarse box.
+int two_level_build(Ctx &c) {
+  TwoLevel &T = c.tl;
+  T.ready = false;
+  T.have_inv = false;
+  if (c.nstate != 3 || c.flt.active) return GPZ_E_INVALID;
+  for (int32_t b : c.h_block_size)
+    if (b != 0 && b != 3) return GPZ_E_INVALID;
+  Bucket *vol = nullptr;
+  std::vector<Bucket *> fixb;
+  for (Bucket *b : c.buckets) {
+    if (b->hp) return GPZ_E_INVALID;
+    const int mi = c.h_el_mat[b->elems[0]];
+    if (!b->key.is_bc) {
+      if (vol || b->key.type != GPZ_EL_HEX || b->nshape != kNS || b->key.mat_kind != GPZ_MAT_ELAST3D ||
+          b->ghat.empty())
+        return GPZ_E_INVALID;
+      vol = b;
+    } else if (c.bcs[-mi - 1].type == 0) {
+      if (b->key.type != GPZ_EL_QUAD) return GPZ_E_INVALID;
+      fixb.push_back(b);
+    }
+  }
+  if (!vol) return GPZ_E_INVALID;
+  for (int k = 0; k < 8; k++)
+    if (vol->shape_side[k] != k) return GPZ_E_INVALID;  // corner shapes first
+  cudaStream_t s = c.stream;
+  const int64_t n = (int64_t)vol->elems.size();
+  // every element the same axis-aligned box
+  DBuf<double> ref;
+  DBuf<int> flag;
+  ref.alloc(10);
+  flag.alloc(1);
+  ref.zero(s);
+  flag.zero(s);
+  k_mf_uniform<<<grid_for(n, 256), 256, 0, s>>>(n, vol->d_elems.p, c.d_el_nodes.p, c.d_xyz.p, ref.p, flag.p);
+  c.launches++;
+  double hr[10];
+  int hf = 0;
+  int64_t node0 = 0;
+  GPZ_CUDA_TRY(cudaMemcpyAsync(hr, ref.p, sizeof(hr), cudaMemcpyDeviceToHost, s));
+  GPZ_CUDA_TRY(cudaMemcpyAsync(&hf, flag.p, sizeof(int), cudaMemcpyDeviceToHost, s));
+  GPZ_CUDA_TRY(cudaMemcpyAsync(&node0, c.d_el_nodes.p + vol->elems[0] * 8, sizeof(int64_t), cudaMemcpyDeviceToHost, s));
+  GPZ_CUDA_TRY(cudaStreamSynchronize(s));
+  if (hf != 0 || !(hr[9] > 0.0)) return GPZ_E_INVALID;
+  double jmax = 0.0;
+  for (int k = 0; k < 9; k++) jmax = std::max(jmax, std::fabs(hr[k]));
+  for (int i = 0; i < 3; i++)
+    for (int j = 0; j < 3; j++)
+      if ((i != j && std::fabs(hr[i * 3 + j]) > 1e-12 * jmax) || (i == j && !(hr[i * 3 + j] > 0.0)))
+        return GPZ_E_INVALID;
+  double x0[3];
+  GPZ_CUDA_TRY(cudaMemcpy(x0, c.d_xyz.p + node0 * 3, sizeof(x0), cudaMemcpyDeviceToHost));
+  const double h[3] = {2.0 / hr[0], 2.0 / hr[4], 2.0 / hr[8]};  // J = h / 2 on the diagonal
+  // lattice
+  DBuf<int32_t> lat, cell;
+  DBuf<int> lmm;
+  lat.alloc((size_t)n * 3);
+  cell.alloc((size_t)n);
+  lmm.alloc(6);
+  const int init[6] = {1 << 30, 1 << 30, 1 << 30, -(1 << 30), -(1 << 30), -(1 << 30)};
+  GPZ_CUDA_TRY(cudaMemcpyAsync(lmm.p, init, sizeof(init), cudaMemcpyHostToDevice, s));
+  k_tl_lattice<<<grid_for(n, 256), 256, 0, s>>>(n, vol->d_elems.p, c.d_el_nodes.p, c.d_xyz.p, x0[0], x0[1], x0[2],
+                                                h[0], h[1], h[2], lat.p, lmm.p, c.d_err.p);
+  c.launches++;
+  int hm[6];
+  GPZ_CUDA_TRY(cudaMemcpyAsync(hm, lmm.p, sizeof(hm), cudaMemcpyDeviceToHost, s));
+  GPZ_CUDA_TRY(cudaStreamSynchronize(s));
+  check_device_flag(c, "two-level lattice");
+  int64_t g = 0;
+  for (int d = 0; d < 3; d++) {
+    T.lx[d] = hm[3 + d] - hm[d];
+    if (T.lx[d] < 2) return GPZ_E_INVALID;
+    g = std::__gcd<int64_t>(g, T.lx[d]);
+  }
+  // s divides every lx; pick the one whose smallest box count is closest to the target
+  int best = -1;
+  for (int64_t cand = 1; cand <= g; cand++) {
+    if (g % cand) continue;
+    const int64_t mmin = std::min(T.lx[0], std::min(T.lx[1], T.lx[2])) / cand;
+    const int64_t nn = (T.lx[0] / cand + 1) * (T.lx[1] / cand + 1) * (T.lx[2] / cand + 1);
+    if (mmin < 1 || 3 * nn > kTlMaxNc) continue;
+    if (best < 0 || std::llabs(mmin - T.target) < std::llabs(std::min(T.lx[0], std::min(T.lx[1], T.lx[2])) / best - T.target))
+      best = (int)cand;
+  }
+  if (best < 0) return GPZ_E_INVALID;
+  T.s = best;
+  for (int d = 0; d < 3; d++) T.m[d] = (int)(T.lx[d] / T.s);
+  T.nnode = (int64_t)(T.m[0] + 1) * (T.m[1] + 1) * (T.m[2] + 1);
+  T.nc = 3 * T.nnode;
+  T.ncell = (int64_t)T.m[0] * T.m[1] * T.m[2];
+  const int nvx = (int)T.lx[0] + 1, nvy = (int)T.lx[1] + 1;
+  const int64_t nv = (int64_t)nvx * nvy * (T.lx[2] + 1);
+  T.vtx_eq.alloc(nv);
+  GPZ_CUDA_TRY(cudaMemsetAsync(T.vtx_eq.p, 0xff, nv * sizeof(int32_t), s));
+  T.el_sub.alloc(n);
+  k_tl_vertices<<<grid_for(n, 256), 256, 0, s>>>(n, vol->d_elems.p, c.d_el_conn.p, c.d_block_pos.p, lat.p, hm[0],
+                                                 hm[1], hm[2], 0, 0, 0, nvx, nvy, T.s, T.m[0], T.m[1], T.vtx_eq.p,
+                                                 cell.p, T.el_sub.p);
+  c.launches++;
+  const int64_t nbrow = c.neq / 3;
+  T.brow_vtx.alloc(std::max<int64_t>(nbrow, 1));
+  GPZ_CUDA_TRY(cudaMemsetAsync(T.brow_vtx.p, 0xff, T.brow_vtx.n * sizeof(int32_t), s));
+  k_tl_browvtx<<<grid_for(nv, 256), 256, 0, s>>>(nv, T.vtx_eq.p, T.brow_vtx.p);
+  c.launches++;
+  T.cfix.alloc(T.nnode);
+  T.cfix.zero(s);
+  for (Bucket *b : fixb) {
+    const int64_t nb = (int64_t)b->elems.size();
+    k_tl_fixnodes<<<grid_for(nb, 256), 256, 0, s>>>(nb, b->d_elems.p, c.d_el_conn.p, c.d_block_pos.p, T.brow_vtx.p,
+                                                    nvx, nvy, T.s, T.m[0], T.m[1], T.m[2], T.cfix.p);
+    c.launches++;
+  }
+  // elements grouped by coarse box (counting sort on the host)
+  std::vector<int32_t> hc(n), fixed(T.nnode);
+  GPZ_CUDA_TRY(cudaMemcpyAsync(hc.data(), cell.p, n * sizeof(int32_t), cudaMemcpyDeviceToHost, s));
+  GPZ_CUDA_TRY(cudaMemcpyAsync(fixed.data(), T.cfix.p, T.nnode * sizeof(int32_t), cudaMemcpyDeviceToHost, s));
+  GPZ_CUDA_TRY(cudaStreamSynchronize(s));
+  GPZ_CUDA_TRY(cudaGetLastError());
+  std::vector<int32_t> off(T.ncell + 1, 0), el(n);
+  for (int64_t i = 0; i < n; i++) off[hc[i] + 1]++;
+  for (int64_t k = 0; k < T.ncell; k++) off[k + 1] += off[k];
+  {
+    std::vector<int32_t> fill(off.begin(), off.end() - 1);
+    for (int64_t i = 0; i < n; i++) el[fill[hc[i]]++] = (int32_t)i;
+  }
+  T.nfixed = 0;
+  for (int32_t f : fixed) T.nfixed += f != 0;
+  T.cell_off.upload(off.data(), off.size(), s);
+  T.cell_el.upload(el.data(), el.size(), s);
+  // tables: fine corner k of the element at sub position (a, b, c) sits at (a, b, c) + off[k] in its coarse box
+  std::vector<double> K;
+  const gpz_material &mat = c.mats[c.h_el_mat[vol->elems[0]]];
+  khat_elasticity(*vol, hr, mat.nu, K);
+  T.mufac = 1.0 / (2.0 + 2.0 * mat.nu);
+  T.E0 = mat.E;
+  static const int off8[8][3] = {{0, 0, 0}, {1, 0, 0}, {1, 1, 0}, {0, 1, 0}, {0, 0, 1}, {1, 0, 1}, {1, 1, 1}, {0, 1, 1}};
+  const int ss = T.s, nsub = ss * ss * ss;
+  std::vector<double> tab((size_t)nsub * 576);
+  for (int sub = 0; sub < nsub; sub++) {
+    const int sa = sub % ss, sb = (sub / ss) % ss, sc = sub / (ss * ss);
+    double W[8][8];  // fine corner k -> coarse corner cn
+    for (int k = 0; k < 8; k++) {
+      const double t[3] = {(double)(sa + off8[k][0]) / ss, (double)(sb + off8[k][1]) / ss,
+                           (double)(sc + off8[k][2]) / ss};
+      for (int cn = 0; cn < 8; cn++) {
+        double w = 1.0;
+        for (int d = 0; d < 3; d++) w *= off8[cn][d] ? t[d] : 1.0 - t[d];
+        W[k][cn] = w;
+      }
+    }
+    double *Tt = tab.data() + (size_t)sub * 576;
+    for (int r = 0; r < 24; r++)
+      for (int q = 0; q < 24; q++) {
+        const int rn = r / 3, rs = r % 3, qn = q / 3, qs = q % 3;
+        double acc = 0.0;
+        for (int k = 0; k < 8; k++) {
+          if (W[k][rn] == 0.0) continue;
+          for (int kk = 0; kk < 8; kk++)
+            acc += W[k][rn] * K[(size_t)(3 * k + rs) * 81 + 3 * kk + qs] * W[kk][qn];
+        }
+        Tt[r * 24 + q] = acc;
+      }
+  }
+  T.tsub.upload(tab.data(), tab.size(), s);
+  T.ac.alloc((size_t)T.nc * T.nc);
+  T.acinv32.alloc((size_t)T.nc * T.nc);
+  T.piv.alloc(2 * T.nc);
+  T.rc.alloc(T.nc);
+  T.zc.alloc(T.nc);
+  T.z32.alloc(std::max<int64_t>(c.neq, 1));
+  T.rc.zero(s);
+  GPZ_CUDA_TRY(cudaStreamSynchronize(s));
+  T.ready = true;
+  return GPZ_OK;
+}
+
+// Coarse matrix of the current assembly (per coarse box sum_e mu_e T[sub_e]),
+// removed nodes, in-place FP64 Gauss-Jordan inverse, FP32 copy (symmetrised).
+void two_level_assemble(Ctx &c) {
+  TwoLevel &T = c.tl;
+  cudaStream_t s = c.stream;
+  Bucket *vol = nullptr;
+  for (Bucket *b : c.buckets)
+    if (!b->key.is_bc) vol = b;
+  T.ac.zero(s);
+  k_tl_cells<<<(unsigned)T.ncell, 256, 0, s>>>(T.cell_off.p, T.cell_el.p, T.el_sub.p, vol->d_elems.p, c.d_coef.p,
+                                               T.E0, T.mufac, T.tsub.p, T.m[0], T.m[1], T.nc, T.ac.p);
+  c.launches++;
+  const int64_t nn = T.nc * T.nc;
+  k_tl_fixrows<<<grid_for(nn, 256), 256, 0, s>>>(T.nc, T.cfix.p, T.ac.p);
+  c.launches++;
+  for (int64_t k = 0; k < T.nc; k++) {
+    k_tl_gj_save<<<grid_for(2 * T.nc, 256), 256, 0, s>>>(T.nc, k, T.ac.p, T.piv.p);
+    k_tl_gj_step<<<grid_for(nn, 256), 256, 0, s>>>(T.nc, k, T.ac.p, T.piv.p, c.d_err.p);
+  }
+  c.launches += 2 * T.nc;
+  k_tl_to32<<<grid_for(nn, 256), 256, 0, s>>>(T.nc, T.ac.p, T.acinv32.p);
+  c.launches++;
+  GPZ_CUDA_TRY(cudaGetLastError());
+  check_device_flag(c, "two-level coarse matrix");
+  T.have_inv = true;
+}
+
 // Build the element records of the matrix-free operator; false when the mesh
 // is not made of uniform Q2 hex elasticity elements plus penalty / traction faces.
 bool matfree_build(Ctx &c) {
   MatFree &M = c.mf;
   M.ready = false;
+  M.gm_ready = false;
   if (c.nstate != 3) return false;
   Bucket *vol = nullptr;
   std::vector<Bucket *> faces;
@@ -1218,12 +1926,14 @@ bool matfree_build(Ctx &c) {
     M.grid_tc = std::max(1, std::min(kGridBlocks, nsm));  // one 187 KB CTA per SM, persistent over tiles
   }
   M.grid_sf = mf_grid(k_mf_hex27_sf, kSfThreads);
+  M.gm_ready = gm_tables(c, *vol, m.nu);
   M.ready = true;
   return true;
 }
 
 // q4 = A p4 (q4 zeroed by the caller), p.q and alpha as the block SpMV kernels;
-// tensor: the tcgen05 3xTF32 volume kernel instead of the CUDA-core one
+// mode 1: the tcgen05 3xTF32 volume kernel, 2: sum-factorised, 3: the shared
+// element matrix on the tensor cores, 0: the CUDA-core element kernel
 void matfree_spmv(Ctx &c, cudaStream_t s, int mode) {
   MatFree &M = c.mf;
   SolverWork &w = c.sw;
@@ -1239,6 +1949,9 @@ void matfree_spmv(Ctx &c, cudaStream_t s, int mode) {
   if (mode == 1)
     k_mf_hex27_tc<<<M.grid_tc, kTcThreads, OFF_TC_END, s>>>(M.nvol, M.vxyz.p, M.vrows.p, M.vlm.p, M.vgeo.p, M.vdphi.p,
                                                             M.vw.p, p4, q4, fe, c.d_err.p, R);
+  else if (mode == 3)
+    k_mf_hex27_gm<<<M.grid_gm, kGmThreads, GM_END, s>>>(M.nvol, M.vrows.p, M.vlm.p, (const float4 *)M.gm_b.p, p4, q4, fe,
+                                                        c.d_err.p, R);
   else if (mode == 2)
     k_mf_hex27_sf<<<M.grid_sf, kSfThreads, 0, s>>>(M.nvol, M.vxyz.p, M.vrows.p, M.vlm.p, M.vgeo.p, M.sf_tab.p,
                                                    M.sf_idx.p, p4, q4, fe, R);

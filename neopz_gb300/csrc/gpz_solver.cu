@@ -1079,6 +1079,473 @@ __global__ void __launch_bounds__(kThreads) k_mx_r32(const double *__restrict__ 
   }
 }
 
+// ---- variable-size block Jacobi: whole connect blocks of any size
+// (TPZBlockDiagonal of TPZBlockDiagonalStructMatrix, overlap = true) or the
+// node-set blocks of TPZNodesetCompute (TPZSparseBlockDiagonal, overlap =
+// false), Analysis/TPZAnalysis.cpp:1008-1107.  The vector kernels of CG and the
+// mixed CG walk blocks: one thread per block updates the block's equations
+// and applies the block's inverse to them (blocks of 3 to a few dozen
+// equations; the thread re-reads its own writes).
+struct VBlk {
+  const int64_t *off;   // [nb + 1] into eq
+  const int64_t *eq;    // the blocks' equations
+  const int64_t *ioff;  // [nb] first entry of the block's inverse
+  const double *inv;    // FP64 inverses, row-major
+  const float *inv32;   // FP32 copies (mixed CG)
+  int64_t nb;
+};
+
+// z_i = sum_j inv[i][j] r[eq_j] for the n equations of one block (n <= kVbMax)
+constexpr int kVbMax = 96;
+
+// Gather block b of the matrix (full CSR) into its inverse slot, then invert
+// it in place by Gauss-Jordan elimination without pivoting (the
+// TPZFMatrix::Decompose_LU of TPZSparseBlockDiagonal does not pivot either).
+// One warp per block: lanes over the rows for the gather, over the columns of
+// each row for the elimination.  A zero or non-finite pivot sets err.
+__global__ void __launch_bounds__(kThreads) k_vb_inv(const int64_t *__restrict__ ia, const int32_t *__restrict__ ja,
+                                                     const double *__restrict__ a, VBlk V,
+                                                     const int32_t *__restrict__ eqblk,
+                                                     const int32_t *__restrict__ eqloc, double *__restrict__ inv,
+                                                     int *__restrict__ err) {
+  const int lane = threadIdx.x & 31;
+  const int64_t wstep = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  for (int64_t b = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; b < V.nb; b += wstep) {
+    const int64_t o = V.off[b];
+    const int n = (int)(V.off[b + 1] - o);
+    double *M = inv + V.ioff[b];
+    if (n > kVbMax) {
+      if (lane == 0) atomicOr(err, 1 << 15);
+      continue;
+    }
+    for (int k = lane; k < n * n; k += 32) M[k] = 0.0;
+    __syncwarp();
+    for (int i = lane; i < n; i += 32) {
+      const int64_t e = V.eq[o + i];
+      for (int64_t k = ia[e]; k < ia[e + 1]; k++) {
+        const int32_t col = ja[k];
+        if (eqblk[col] == (int32_t)b) M[i * n + eqloc[col]] = a[k];
+      }
+    }
+    __syncwarp();
+    bool bad = false;
+    for (int k = 0; k < n; k++) {
+      const double piv = M[k * n + k];
+      bad = bad || !(piv != 0.0) || !isfinite(piv);
+      const double pinv = 1.0 / piv;
+      __syncwarp();
+      for (int j = lane; j < n; j += 32) M[k * n + j] = (j == k ? 1.0 : M[k * n + j]) * pinv;
+      __syncwarp();
+      for (int i = 0; i < n; i++) {
+        if (i == k) continue;
+        const double f = M[i * n + k];
+        __syncwarp();
+        for (int j = lane; j < n; j += 32) M[i * n + j] = (j == k ? 0.0 : M[i * n + j]) - f * M[k * n + j];
+        __syncwarp();
+      }
+    }
+    if (bad && lane == 0) atomicOr(err, 256);
+  }
+}
+
+// equation -> (block, position) maps for the gather above
+__global__ void k_vb_maps(VBlk V, int32_t *__restrict__ eqblk, int32_t *__restrict__ eqloc) {
+  const int64_t b = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (b >= V.nb) return;
+  for (int64_t k = V.off[b]; k < V.off[b + 1]; k++) {
+    eqblk[V.eq[k]] = (int32_t)b;
+    eqloc[V.eq[k]] = (int32_t)(k - V.off[b]);
+  }
+}
+
+// z = M r over the variable blocks (gpz_precond_apply)
+__global__ void __launch_bounds__(kThreads) k_vb_apply(const double *__restrict__ r, VBlk V, double *__restrict__ z) {
+  for (int64_t b = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; b < V.nb; b += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t o = V.off[b];
+    const int n = (int)(V.off[b + 1] - o);
+    const double *B = V.inv + V.ioff[b];
+    for (int i = 0; i < n; i++) {
+      double acc = 0.0;
+      for (int j = 0; j < n; j++) acc += B[i * n + j] * r[V.eq[o + j]];
+      z[V.eq[o + i]] = acc;
+    }
+  }
+}
+
+// z = M r for the point or 3x3 block Jacobi preconditioner
+__global__ void __launch_bounds__(kThreads) k_prec_apply(const double *__restrict__ r, Prec M, int64_t nunits,
+                                                         double *__restrict__ z) {
+  const int bs = M.block ? 3 : 1;
+  for (int64_t u = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; u < nunits; u += (int64_t)gridDim.x * blockDim.x) {
+    double t[3];
+    apply_prec(M, r, u, t);
+    for (int k = 0; k < bs; k++) z[u * bs + k] = t[k];
+  }
+}
+
+// FP64 CG, kernel B: p = M r + beta p (p = M r at the first iteration / after a restart)
+__global__ void __launch_bounds__(kThreads) k_vb_p(const double *__restrict__ r, VBlk V, double *__restrict__ p, Red R) {
+  if (!active(R.iscal)) return;
+  const bool first = R.iscal[I_IT] == 0 || R.iscal[I_RESTART] != 0;
+  const double beta = first ? 0.0 : R.scal[S_BETA];
+  for (int64_t b = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; b < V.nb; b += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t o = V.off[b];
+    const int n = (int)(V.off[b + 1] - o);
+    const double *B = V.inv + V.ioff[b];
+    for (int i = 0; i < n; i++) {
+      double z = 0.0;
+      for (int j = 0; j < n; j++) z += B[i * n + j] * r[V.eq[o + j]];
+      const int64_t e = V.eq[o + i];
+      p[e] = first ? z : z + beta * p[e];
+    }
+  }
+}
+
+// FP64 CG, kernel D: x += alpha p; r -= alpha q; rho' = r.(M r), rr = r.r (epilogue of k_cg_update)
+__global__ void __launch_bounds__(kThreads) k_vb_update(double *__restrict__ x, double *__restrict__ r,
+                                                        const double *__restrict__ p, const double *__restrict__ q,
+                                                        VBlk V, Red R) {
+  if (!active(R.iscal)) return;
+  const double pq = R.scal[S_PQ];
+  const double alpha = R.scal[S_ALPHA];
+  double rz = 0.0, rr = 0.0;
+  for (int64_t b = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; b < V.nb; b += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t o = V.off[b];
+    const int n = (int)(V.off[b + 1] - o);
+    for (int i = 0; i < n; i++) {
+      const int64_t e = V.eq[o + i];
+      x[e] = x[e] + alpha * p[e];
+      const double ri = r[e] - alpha * q[e];
+      r[e] = ri;
+      rr += ri * ri;
+    }
+    const double *B = V.inv + V.ioff[b];
+    for (int i = 0; i < n; i++) {
+      double z = 0.0;
+      for (int j = 0; j < n; j++) z += B[i * n + j] * r[V.eq[o + j]];
+      rz += r[V.eq[o + i]] * z;
+    }
+  }
+  double v[2] = {rz, rr}, tot[2];
+  if (grid_reduce<2>(v, R, tot) && threadIdx.x == 0) {
+    double *s = R.scal;
+    int64_t *is = R.iscal;
+    if (!(pq > 0.0) || !isfinite(tot[1]) || !isfinite(tot[0])) is[I_BREAK] = 1;
+    s[S_RHO1] = s[S_RHO];
+    s[S_RHO] = tot[0];
+    s[S_BETA] = tot[0] / s[S_RHO1];
+    s[S_RR] = tot[1];
+    if (tot[1] > s[S_MAXRR]) s[S_MAXRR] = tot[1];
+    const double resid = sqrt(tot[1]) / s[S_NORMB];
+    s[S_RESID] = resid;
+    is[I_IT] += 1;
+    is[I_RESTART] = 0;
+    if (is[I_BREAK]) is[I_CONV] = 2;
+    else if (resid <= s[S_TOL]) is[I_CONV] = 1;
+  }
+}
+
+// rho = r.(M r) after the initial residual (epilogue of k_precond_dot)
+__global__ void __launch_bounds__(kThreads) k_vb_dot(const double *__restrict__ r, VBlk V, Red R) {
+  if (R.iscal[I_UPDATE] != 2) return;
+  double rz = 0.0;
+  for (int64_t b = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; b < V.nb; b += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t o = V.off[b];
+    const int n = (int)(V.off[b + 1] - o);
+    const double *B = V.inv + V.ioff[b];
+    for (int i = 0; i < n; i++) {
+      double z = 0.0;
+      for (int j = 0; j < n; j++) z += B[i * n + j] * r[V.eq[o + j]];
+      rz += r[V.eq[o + i]] * z;
+    }
+  }
+  double v[1] = {rz}, tot[1];
+  if (grid_reduce<1>(v, R, tot) && threadIdx.x == 0) {
+    double *s = R.scal;
+    int64_t *is = R.iscal;
+    if (is[I_IT] > 0 && (tot[0] > 4.0 * s[S_RHO] || tot[0] < 0.25 * s[S_RHO])) {
+      is[I_RESTART] = 1;
+      is[I_NRESTART] += 1;
+    }
+    s[S_RHO] = tot[0];
+    s[S_BETA] = s[S_RHO1] != 0.0 ? tot[0] / s[S_RHO1] : 0.0;
+    is[I_UPDATE] = 0;
+  }
+}
+
+// mixed CG: p = M r + beta p in FP32 (p and the atomically accumulated q padded like k_mx_p)
+__global__ void __launch_bounds__(kThreads) k_vb32_p(const float *__restrict__ r, VBlk V, float *__restrict__ p,
+                                                     int padded, float *__restrict__ qzero, Red R) {
+  if (!active(R.iscal)) return;
+  const bool first = R.iscal[I_IT] == 0 || R.iscal[I_RESTART] != 0;
+  const float beta = first ? 0.f : (float)R.scal[S_BETA];
+  for (int64_t b = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; b < V.nb; b += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t o = V.off[b];
+    const int n = (int)(V.off[b + 1] - o);
+    const float *B = V.inv32 + V.ioff[b];
+    for (int i = 0; i < n; i++) {
+      float z = 0.f;
+      for (int j = 0; j < n; j++) z = fmaf(B[i * n + j], r[V.eq[o + j]], z);
+      const int64_t jj = pidx(V.eq[o + i], padded);
+      p[jj] = first ? z : fmaf(beta, p[jj], z);
+      if (qzero) qzero[jj] = 0.f;
+    }
+  }
+}
+
+// mixed CG: dx += alpha p; r -= alpha q; rho' = r.(M r), rr = r.r (epilogue of k_mx_update)
+__global__ void __launch_bounds__(kThreads) k_vb32_update(float *__restrict__ dx, float *__restrict__ r,
+                                                          const float *__restrict__ p, const float *__restrict__ q,
+                                                          VBlk V, int padded, int qpad, Red R) {
+  if (!active(R.iscal)) return;
+  const double pq = R.scal[S_PQ];
+  const float alpha = (float)R.scal[S_ALPHA];
+  KSum rz, rr;
+  for (int64_t b = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; b < V.nb; b += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t o = V.off[b];
+    const int n = (int)(V.off[b + 1] - o);
+    for (int i = 0; i < n; i++) {
+      const int64_t e = V.eq[o + i];
+      dx[e] = fmaf(alpha, p[pidx(e, padded)], dx[e]);
+      const float ri = fmaf(-alpha, q[pidx(e, qpad)], r[e]);
+      r[e] = ri;
+      rr.add(ri * ri);
+    }
+    const float *B = V.inv32 + V.ioff[b];
+    for (int i = 0; i < n; i++) {
+      float z = 0.f;
+      for (int j = 0; j < n; j++) z = fmaf(B[i * n + j], r[V.eq[o + j]], z);
+      rz.add(r[V.eq[o + i]] * z);
+    }
+  }
+  double v[2] = {rz.get(), rr.get()}, tot[2];
+  if (grid_reduce<2>(v, R, tot) && threadIdx.x == 0) {
+    double *s = R.scal;
+    int64_t *is = R.iscal;
+    if (!(pq > 0.0) || !isfinite(tot[1]) || !isfinite(tot[0])) is[I_BREAK] = 1;
+    s[S_RHO1] = s[S_RHO];
+    s[S_RHO] = tot[0];
+    s[S_BETA] = tot[0] / s[S_RHO1];
+    s[S_RR] = tot[1];
+    if (tot[1] > s[S_MAXRR]) s[S_MAXRR] = tot[1];
+    const double resid = sqrt(tot[1]) / s[S_NORMB];
+    s[S_RESID] = resid;
+    is[I_IT] += 1;
+    is[I_RESTART] = 0;
+    if (is[I_BREAK]) is[I_CONV] = 2;
+    else if (resid <= s[S_TOL] || tot[1] < s[S_DELTA2] * s[S_MAXRR]) is[I_UPDATE] = 1;
+  }
+}
+
+// mixed CG: r32 = r64 after a true-residual computation; rho = r.(M r), restart rule (epilogue of k_mx_r32)
+__global__ void __launch_bounds__(kThreads) k_vb32_r32(const double *__restrict__ r64, float *__restrict__ r32, VBlk V,
+                                                       Red R) {
+  if (R.iscal[I_UPDATE] != 2) return;
+  KSum rz;
+  for (int64_t b = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; b < V.nb; b += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t o = V.off[b];
+    const int n = (int)(V.off[b + 1] - o);
+    for (int i = 0; i < n; i++) r32[V.eq[o + i]] = (float)r64[V.eq[o + i]];
+    const float *B = V.inv32 + V.ioff[b];
+    for (int i = 0; i < n; i++) {
+      float z = 0.f;
+      for (int j = 0; j < n; j++) z = fmaf(B[i * n + j], r32[V.eq[o + j]], z);
+      rz.add(r32[V.eq[o + i]] * z);
+    }
+  }
+  double v[1] = {rz.get()}, tot[1];
+  if (grid_reduce<1>(v, R, tot) && threadIdx.x == 0) {
+    double *s = R.scal;
+    int64_t *is = R.iscal;
+    if (is[I_IT] > 0 && (tot[0] > 4.0 * s[S_RHO] || tot[0] < 0.25 * s[S_RHO])) {
+      is[I_RESTART] = 1;
+      is[I_NRESTART] += 1;
+    }
+    s[S_RHO] = tot[0];
+    s[S_BETA] = s[S_RHO1] != 0.0 ? tot[0] / s[S_RHO1] : 0.0;
+    is[I_UPDATE] = 0;
+  }
+}
+
+// ---- two-level block Jacobi (mixed CG): z = B^-1 r + P Ac^-1 P^T r, B the 3x3
+// connect blocks, P trilinear from the coarse nodes to the vertex connects
+// (see TwoLevel).  One application: k_tl_restrict (rc = P^T r), k_tl_csolve
+// (zc = Ac^-1 rc, dense FP32), k_tl_z (z, rho = r.z, beta); then k_tl_p.
+struct TlView {
+  const int32_t *vtx_eq, *brow_vtx, *cfix;
+  const float *acinv;
+  float *rc, *zc, *z;
+  int nvx, nvy, nvz, s, mx, my, mz;
+  int64_t nc;
+};
+
+// coarse position of lattice vertex v: box (I, J, K) and its local offsets
+__device__ __forceinline__ void tl_locate(const TlView &T, int64_t v, int &I, int &J, int &K, float &tx, float &ty,
+                                          float &tz) {
+  const int vi = (int)(v % T.nvx), vj = (int)((v / T.nvx) % T.nvy), vk = (int)(v / ((int64_t)T.nvx * T.nvy));
+  I = min(vi / T.s, T.mx - 1);
+  J = min(vj / T.s, T.my - 1);
+  K = min(vk / T.s, T.mz - 1);
+  const float is = 1.0f / (float)T.s;
+  tx = (float)(vi - I * T.s) * is;
+  ty = (float)(vj - J * T.s) * is;
+  tz = (float)(vk - K * T.s) * is;
+}
+constexpr int kTlMaxSmem = 3072;  // coarse dofs kept in shared memory by the restriction (>= the largest system)
+
+__global__ void __launch_bounds__(kThreads) k_tl_restrict(const float *__restrict__ r, TlView T, Red R) {
+  if (!active(R.iscal)) return;
+  __shared__ float sr[kTlMaxSmem];
+  for (int64_t k = threadIdx.x; k < T.nc; k += blockDim.x) sr[k] = 0.f;
+  __syncthreads();
+  const int64_t nv = (int64_t)T.nvx * T.nvy * T.nvz;
+  for (int64_t v = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; v < nv; v += (int64_t)gridDim.x * blockDim.x) {
+    const int32_t eq = T.vtx_eq[v];
+    if (eq < 0) continue;
+    int I, J, K;
+    float t[3];
+    tl_locate(T, v, I, J, K, t[0], t[1], t[2]);
+    const float r0 = r[eq], r1 = r[eq + 1], r2 = r[eq + 2];
+#pragma unroll
+    for (int cn = 0; cn < 8; cn++) {
+      const int bx = cn & 1, by = (cn >> 1) & 1, bz = cn >> 2;
+      const float w = (bx ? t[0] : 1.f - t[0]) * (by ? t[1] : 1.f - t[1]) * (bz ? t[2] : 1.f - t[2]);
+      if (w == 0.f) continue;
+      const int64_t nd = (I + bx) + (int64_t)(T.mx + 1) * ((J + by) + (int64_t)(T.my + 1) * (K + bz));
+      atomicAdd(&sr[3 * nd], w * r0);
+      atomicAdd(&sr[3 * nd + 1], w * r1);
+      atomicAdd(&sr[3 * nd + 2], w * r2);
+    }
+  }
+  __syncthreads();
+  for (int64_t k = threadIdx.x; k < T.nc; k += blockDim.x)
+    if (sr[k] != 0.f) atomicAdd(&T.rc[k], sr[k]);
+}
+
+// zc = Ac^-1 rc (removed nodes: zero); one warp per coarse row
+__global__ void __launch_bounds__(kThreads) k_tl_csolve(TlView T, Red R) {
+  if (!active(R.iscal)) return;
+  const int lane = threadIdx.x & 31;
+  for (int64_t row = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; row < T.nc;
+       row += ((int64_t)gridDim.x * blockDim.x) >> 5) {
+    float acc = 0.f;
+    const float *a = T.acinv + row * T.nc;
+    for (int64_t j = lane; j < T.nc; j += 32) acc = fmaf(a[j], __ldcg(&T.rc[j]), acc);
+    for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+    if (lane == 0) T.zc[row] = T.cfix[row / 3] ? 0.f : acc;
+  }
+}
+
+// z = B^-1 r + P zc per 3x3 block row; rho = r.z (KSum), beta; after a residual
+// replacement (I_UPDATE 2, set by k_reliable or the initial residual) the
+// direction restarts when the replaced residual's norm differs from the
+// recursive one by more than 2x; rc cleared for the next application.
+__global__ void __launch_bounds__(kThreads) k_tl_z(const float *__restrict__ r, Prec32 M, TlView T, int64_t nunits,
+                                                   Red R) {
+  if (!active(R.iscal)) return;
+  KSum rz;
+  for (int64_t u = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; u < nunits; u += (int64_t)gridDim.x * blockDim.x) {
+    float z[3];
+    apply_prec32(M, r, u, z);
+    const int32_t v = T.brow_vtx[u];
+    if (v >= 0) {
+      int I, J, K;
+      float t[3];
+      tl_locate(T, v, I, J, K, t[0], t[1], t[2]);
+#pragma unroll
+      for (int cn = 0; cn < 8; cn++) {
+        const int bx = cn & 1, by = (cn >> 1) & 1, bz = cn >> 2;
+        const float w = (bx ? t[0] : 1.f - t[0]) * (by ? t[1] : 1.f - t[1]) * (bz ? t[2] : 1.f - t[2]);
+        if (w == 0.f) continue;
+        const int64_t nd = (I + bx) + (int64_t)(T.mx + 1) * ((J + by) + (int64_t)(T.my + 1) * (K + bz));
+        z[0] = fmaf(w, __ldcg(&T.zc[3 * nd]), z[0]);
+        z[1] = fmaf(w, __ldcg(&T.zc[3 * nd + 1]), z[1]);
+        z[2] = fmaf(w, __ldcg(&T.zc[3 * nd + 2]), z[2]);
+      }
+    }
+#pragma unroll
+    for (int k = 0; k < 3; k++) {
+      T.z[3 * u + k] = z[k];
+      rz.add(r[3 * u + k] * z[k]);
+    }
+  }
+  for (int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < T.nc; k += (int64_t)gridDim.x * blockDim.x)
+    T.rc[k] = 0.f;
+  double v[1] = {rz.get()}, tot[1];
+  if (grid_reduce<1>(v, R, tot) && threadIdx.x == 0) {
+    double *s = R.scal;
+    int64_t *is = R.iscal;
+    if (!isfinite(tot[0]) || !(tot[0] > 0.0)) {
+      is[I_BREAK] = 1;
+      is[I_CONV] = 2;
+    }
+    if (is[I_UPDATE] == 2) {
+      const double q = s[S_RRREC] > 0.0 ? s[S_TRUERR] / s[S_RRREC] : 1.0;
+      if (is[I_IT] > 0 && (q > 4.0 || q < 0.25)) {
+        is[I_RESTART] = 1;
+        is[I_NRESTART] += 1;
+      }
+      is[I_UPDATE] = 0;
+    }
+    s[S_RHO1] = s[S_RHO];
+    s[S_RHO] = tot[0];
+    s[S_BETA] = s[S_RHO1] != 0.0 ? tot[0] / s[S_RHO1] : 0.0;
+  }
+}
+
+// p = z + beta p (p = z at the first iteration / after a restart)
+__global__ void __launch_bounds__(kThreads) k_tl_p(const float *__restrict__ z, float *__restrict__ p, int padded,
+                                                   float *__restrict__ qzero, int64_t n, Red R) {
+  if (!active(R.iscal)) return;
+  const bool first = R.iscal[I_IT] == 0 || R.iscal[I_RESTART] != 0;
+  const float beta = first ? 0.f : (float)R.scal[S_BETA];
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t j = pidx(i, padded);
+    p[j] = first ? z[i] : fmaf(beta, p[j], z[i]);
+    if (qzero) qzero[j] = 0.f;
+  }
+}
+
+// dx += alpha p; r -= alpha q; rr (the recursive ||r||^2 kept for the restart rule); the
+// reliable-update request as k_mx_update; rho follows in k_tl_z
+__global__ void __launch_bounds__(kThreads) k_tl_update(float *__restrict__ dx, float *__restrict__ r,
+                                                        const float *__restrict__ p, const float *__restrict__ q,
+                                                        int padded, int qpad, int64_t n, Red R) {
+  if (!active(R.iscal)) return;
+  const double pq = R.scal[S_PQ];
+  const float alpha = (float)R.scal[S_ALPHA];
+  KSum rr;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    dx[i] = fmaf(alpha, p[pidx(i, padded)], dx[i]);
+    const float ri = fmaf(-alpha, q[pidx(i, qpad)], r[i]);
+    r[i] = ri;
+    rr.add(ri * ri);
+  }
+  double v[1] = {rr.get()}, tot[1];
+  if (grid_reduce<1>(v, R, tot) && threadIdx.x == 0) {
+    double *s = R.scal;
+    int64_t *is = R.iscal;
+    if (!(pq > 0.0) || !isfinite(tot[0])) is[I_BREAK] = 1;
+    s[S_RR] = tot[0];
+    s[S_RRREC] = tot[0];
+    if (tot[0] > s[S_MAXRR]) s[S_MAXRR] = tot[0];
+    const double resid = sqrt(tot[0]) / s[S_NORMB];
+    s[S_RESID] = resid;
+    is[I_IT] += 1;
+    is[I_RESTART] = 0;
+    if (is[I_BREAK]) is[I_CONV] = 2;
+    else if (resid <= s[S_TOL] || tot[0] < s[S_DELTA2] * s[S_MAXRR]) is[I_UPDATE] = 1;
+  }
+}
+
+// r32 = r64 after a true-residual computation (I_UPDATE 2; k_tl_z then forms rho and clears the flag)
+__global__ void __launch_bounds__(kThreads) k_tl_r32(const double *__restrict__ r64, float *__restrict__ r32, int64_t n,
+                                                     Red R) {
+  if (R.iscal[I_UPDATE] != 2) return;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    r32[i] = (float)r64[i];
+}
+
 __global__ void k_to_f32(const double *__restrict__ a, float *__restrict__ b, int64_t n) {
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
     b[i] = (float)a[i];
@@ -1739,7 +2206,7 @@ Red red_of(Ctx &c);
 // one launch of the FP32 3x3 SpMV variant v: q32 = A32 pm
 void launch_spmv32(Ctx &c, int v, const Ctx::Sell &S, Red R, cudaStream_t s) {
   SolverWork &w = c.sw;
-  if (v == 5 || v == 6 || v == 7) {
+  if (v >= 5 && v <= 8) {
     matfree_spmv(c, s, v - 5);  // element by element (gpz_matfree.cu), counts its own launches
     return;
   }
@@ -1819,11 +2286,15 @@ void tune_spmv32(Ctx &c, int only, bool timing) {
   };
   float best_mf = -1.f;
   std::string pruned;
-  if (timing && only < 0 && (want0(5) || want0(6) || want0(7)) && matfree_build(c)) {
+  if (timing && only < 0 && (want0(5) || want0(6) || want0(7) || want0(8)) && matfree_build(c)) {
     res.push_back({5, 0, time_it(5, cand[0])});
     if (c.mf.sf_ready) res.push_back({7, 0, time_it(7, cand[0])});
     res.push_back({6, 0, time_it(6, cand[0])});
     check_device_flag(c, "tensor-core matrix-free operator");
+    if (c.mf.gm_ready) {
+      res.push_back({8, 0, time_it(8, cand[0])});
+      check_device_flag(c, "shared-element-matrix tensor-core operator");
+    }
     for (const Res &r : res) best_mf = best_mf < 0.f ? r.ms : std::min(best_mf, r.ms);
   }
   auto want = [&](int v) {
@@ -1886,12 +2357,16 @@ void tune_spmv32(Ctx &c, int only, bool timing) {
     GPZ_CUDA_TRY(cudaGetLastError());
     res.push_back({4, 0, time_it(4, cand[0])});
   }
-  if (best_mf < 0.f && (want0(5) || want0(6) || want0(7)) && matfree_build(c)) {
+  if (best_mf < 0.f && (want0(5) || want0(6) || want0(7) || want0(8)) && matfree_build(c)) {
     if (want0(5)) res.push_back({5, 0, time_it(5, cand[0])});
     if (want0(7) && c.mf.sf_ready) res.push_back({7, 0, time_it(7, cand[0])});
     if (want0(6)) {
       res.push_back({6, 0, time_it(6, cand[0])});
       check_device_flag(c, "tensor-core matrix-free operator");
+    }
+    if (want0(8) && c.mf.gm_ready) {
+      res.push_back({8, 0, time_it(8, cand[0])});
+      check_device_flag(c, "shared-element-matrix tensor-core operator");
     }
   }
   if (res.empty()) res.push_back({0, 0, time_it(0, cand[0])});
@@ -1915,6 +2390,7 @@ void tune_spmv32(Ctx &c, int only, bool timing) {
                      : res[i].v == 5 ? "matrix_free_elements"
                      : res[i].v == 6 ? "matrix_free_tcgen05_3xtf32"
                      : res[i].v == 7 ? "matrix_free_sum_factorised"
+                     : res[i].v == 8 ? "matrix_free_shared_matrix_tcgen05"
                                      : "sliced_ell";
     rep += std::string(i ? ", " : "") + "\"" + nm + (res[i].v == 2 ? "_w" + std::to_string(res[i].window) : "") +
            "\": " + std::to_string(res[i].ms);
@@ -1923,9 +2399,9 @@ void tune_spmv32(Ctx &c, int only, bool timing) {
   if (c.d_uptr.p) {
     GPZ_CUDA_TRY(cudaMemcpy(&nu, c.d_uptr.p + c.nbrow, sizeof(int64_t), cudaMemcpyDeviceToHost));
   }
-  const char *names[8] = {"block_csr", "block_csr_2rows", "sliced_ell", "block_csr_tma_staged",
+  const char *names[9] = {"block_csr", "block_csr_2rows", "sliced_ell", "block_csr_tma_staged",
                           "upper_blocks_float4_atomics", "matrix_free_elements", "matrix_free_tcgen05_3xtf32",
-                          "matrix_free_sum_factorised"};
+                          "matrix_free_sum_factorised", "matrix_free_shared_matrix_tcgen05"};
   if (!pruned.empty()) rep += ", \"pruned_by_byte_floor_ms\": {" + pruned + "}";
   c.tune_report = rep + ", \"chosen\": \"" + names[res[best].v] + "\", \"block_rows\": " + std::to_string(c.nbrow) +
                   ", \"blocks_full\": " + std::to_string(c.nnz / 9) + ", \"blocks_upper\": " + std::to_string(nu) +
@@ -2001,6 +2477,94 @@ void build_block_jacobi(Ctx &c) {
   c.have_bjinv = true;
 }
 
+// every connect block holds 0 or 3 equations: the 3x3 block path applies
+bool connect_blocks_are_3(const Ctx &c) {
+  if (!blocks_are_3(c)) return false;
+  for (int32_t s : c.h_block_size)
+    if (s != 0 && s != 3) return false;
+  return true;
+}
+
+// Blocks of the variable-size block Jacobi: kind GPZ_PRECOND_BLOCK_JACOBI = one
+// block per connect (TPZBlockDiagonalStructMatrix, StrMatrix/pzbdstrmatrix.cpp:
+// 13-97), GPZ_PRECOND_NODESET_JACOBI = the node-set blocks of the element
+// graph (gpz_nodeset_blocks, TPZNodesetCompute); then the inverses of the
+// assembled matrix's diagonal blocks on the device.
+void build_vblocks(Ctx &c, int kind) {
+  GPZ_REQUIRE(!c.flt.active && c.neq > 0, GPZ_E_INVALID,
+              "block Jacobi with whole connect / node-set blocks: not available under an equation filter");
+  cudaStream_t s = c.stream;
+  if (c.vb_kind != kind) {
+    std::vector<int64_t> off(1, 0), eq;
+    const int64_t nconn = (int64_t)c.h_block_size.size();
+    if (kind == GPZ_PRECOND_BLOCK_JACOBI) {
+      for (int64_t cn = 0; cn < nconn; cn++) {
+        if (c.h_block_size[cn] <= 0) continue;
+        for (int32_t k = 0; k < c.h_block_size[cn]; k++) eq.push_back(c.h_block_pos[cn] + k);
+        off.push_back((int64_t)eq.size());
+      }
+    } else {
+      // TPZCompMesh::ComputeElGraph: every element's side connects
+      const int64_t nel = (int64_t)c.h_el_type.size();
+      std::vector<int64_t> gi(nel + 1, 0), g;
+      for (int64_t e = 0; e < nel; e++) {
+        const int t = c.h_el_type[e];
+        const int ns = t == GPZ_EL_LINE ? 3 : (t == GPZ_EL_QUAD ? 9 : 27);
+        for (int k = 0; k < ns; k++) g.push_back(c.h_el_conn[e * 27 + k]);
+        gi[e + 1] = (int64_t)g.size();
+      }
+      std::vector<int64_t> bsz(c.h_block_size.begin(), c.h_block_size.end());
+      std::vector<int64_t> bi(nconn + 1), be(std::max<int64_t>(c.neq, 1));
+      std::vector<int> col(std::max<int64_t>(nconn, 1));
+      int64_t nb = 0;
+      int ncol = 0;
+      const int rc = gpz_nodeset_blocks(nconn, nel, gi.data(), g.data(), c.h_block_pos.data(), bsz.data(), c.neq,
+                                        bi.data(), be.data(), &nb, col.data(), &ncol, nullptr, nullptr);
+      GPZ_REQUIRE(rc == GPZ_OK, rc, "node-set blocks of the element graph");
+      off.assign(bi.begin(), bi.begin() + nb + 1);
+      eq.assign(be.begin(), be.begin() + off[nb]);
+    }
+    const int64_t nb = (int64_t)off.size() - 1;
+    std::vector<int64_t> ioff(std::max<int64_t>(nb, 1), 0);
+    int64_t tot = 0;
+    int maxn = 0;
+    for (int64_t b = 0; b < nb; b++) {
+      const int64_t n = off[b + 1] - off[b];
+      GPZ_REQUIRE(n <= kVbMax, GPZ_E_INVALID, "block Jacobi: a block larger than 96 equations");
+      ioff[b] = tot;
+      tot += n * n;
+      maxn = std::max(maxn, (int)n);
+    }
+    c.d_vb_off.upload(off.data(), off.size(), s);
+    c.d_vb_eq.upload(eq.data(), std::max<size_t>(eq.size(), 1), s);
+    c.d_vb_ioff.upload(ioff.data(), ioff.size(), s);
+    c.d_vb_inv.alloc(std::max<int64_t>(tot, 1));
+    c.d_vb_eqblk.alloc(std::max<int64_t>(c.neq, 1));
+    c.d_vb_eqloc.alloc(std::max<int64_t>(c.neq, 1));
+    GPZ_CUDA_TRY(cudaMemsetAsync(c.d_vb_eqblk.p, 0xff, c.d_vb_eqblk.n * sizeof(int32_t), s));  // -1: no block
+    c.vb_nb = nb;
+    c.vb_maxn = maxn;
+    const VBlk V{c.d_vb_off.p, c.d_vb_eq.p, c.d_vb_ioff.p, nullptr, nullptr, nb};
+    k_vb_maps<<<grid_for(std::max<int64_t>(nb, 1), 256), 256, 0, s>>>(V, c.d_vb_eqblk.p, c.d_vb_eqloc.p);
+    c.launches++;
+    GPZ_CUDA_TRY(cudaStreamSynchronize(s));  // the host arrays above go out of scope
+    c.vb_kind = kind;
+    c.d_vb_inv32.release();
+  }
+  const VBlk V{c.d_vb_off.p, c.d_vb_eq.p, c.d_vb_ioff.p, nullptr, nullptr, c.vb_nb};
+  k_vb_inv<<<grid_for(std::max<int64_t>(c.vb_nb, 1) * 32, 256), 256, 0, s>>>(c.d_ia.p, c.d_ja.p, c.d_a.p, V,
+                                                                              c.d_vb_eqblk.p, c.d_vb_eqloc.p,
+                                                                              c.d_vb_inv.p, c.d_err.p);
+  c.launches++;
+  GPZ_CUDA_TRY(cudaGetLastError());
+  check_device_flag(c, "block Jacobi inverses");
+  c.have_vbinv = true;
+}
+
+VBlk vblk_of(const Ctx &c) {
+  return VBlk{c.d_vb_off.p, c.d_vb_eq.p, c.d_vb_ioff.p, c.d_vb_inv.p, c.d_vb_inv32.p, c.vb_nb};
+}
+
 // ---- solver workspace and the iteration plan
 
 void alloc_work(Ctx &c, bool mixed) {
@@ -2028,27 +2592,67 @@ Red red_of(Ctx &c) { return Red{c.sw.partial.p, c.sw.counter.p, c.sw.scal.p, c.s
 
 struct Plan {
   bool mixed, block, bsr;
+  bool vb = false;  // variable-size block Jacobi
+  bool tl = false;  // two-level block Jacobi (mixed CG)
+  TlView T;
   int tpr, tpr32;
   int64_t nunits;
   Prec M;
   Prec32 M32;
+  VBlk V;
 };
+
+// one application of the two-level preconditioner to r32 (after a possible residual refresh)
+void launch_tl_apply(Ctx &c, const Plan &P, Red R, cudaStream_t s) {
+  SolverWork &w = c.sw;
+  k_tl_r32<<<wave(k_tl_r32), kThreads, 0, s>>>(w.r.p, w.r32.p, c.neq, R);
+  int dev = 0, nsm = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+  k_tl_restrict<<<std::max(1, 2 * nsm), kThreads, 0, s>>>(w.r32.p, P.T, R);
+  k_tl_csolve<<<wave(k_tl_csolve), kThreads, 0, s>>>(P.T, R);
+  k_tl_z<<<wave(k_tl_z), kThreads, 0, s>>>(w.r32.p, P.M32, P.T, P.nunits, R);
+  c.launches += 4;
+}
 
 void launch_iteration(Ctx &c, const Plan &P) {
   SolverWork &w = c.sw;
   Red R = red_of(c);
   if (!P.mixed) {
-    k_cg_p<<<wave(k_cg_p), kThreads, 0, c.stream>>>(w.r.p, P.M, w.p.p, P.nunits, R);
+    if (P.vb) k_vb_p<<<wave(k_vb_p), kThreads, 0, c.stream>>>(w.r.p, P.V, w.p.p, R);
+    else k_cg_p<<<wave(k_cg_p), kThreads, 0, c.stream>>>(w.r.p, P.M, w.p.p, P.nunits, R);
     GPZ_TPR_SWITCH(P.tpr, (k_cg_spmv<T, false><<<wave(k_cg_spmv<T, false>), kThreads, 0, c.stream>>>(
                               c.d_ia.p, c.d_ja.p, c.d_a.p, nullptr, w.p.p, nullptr, w.q.p, c.neq, R)));
-    k_cg_update<<<wave(k_cg_update), kThreads, 0, c.stream>>>(w.x.p, w.r.p, w.p.p, w.q.p, P.M, P.nunits, 0, R);
+    if (P.vb) k_vb_update<<<wave(k_vb_update), kThreads, 0, c.stream>>>(w.x.p, w.r.p, w.p.p, w.q.p, P.V, R);
+    else k_cg_update<<<wave(k_cg_update), kThreads, 0, c.stream>>>(w.x.p, w.r.p, w.p.p, w.q.p, P.M, P.nunits, 0, R);
     c.launches += 3;
     return;
   }
   const int padded = P.bsr ? 1 : 0;
-  const bool sym = P.bsr && c.spmv32_variant >= 4;  // 4..7: q accumulated with atomics
-  k_mx_p<<<wave(k_mx_p), kThreads, 0, c.stream>>>(w.r32.p, P.M32, w.pm.p, padded, sym ? w.q32.p : nullptr, P.nunits,
-                                                  R);
+  const bool sym = P.bsr && c.spmv32_variant >= 4;  // 4..8: q accumulated with atomics
+  if (P.tl) {
+    k_tl_p<<<wave(k_tl_p), kThreads, 0, c.stream>>>(P.T.z, w.pm.p, padded, sym ? w.q32.p : nullptr, c.neq, R);
+    if (P.bsr) {
+      launch_spmv32(c, c.spmv32_variant, c.sell, R, c.stream);
+      c.launches--;
+    } else {
+      GPZ_TPR_SWITCH(P.tpr32, (k_mx_csr<T><<<wave(k_mx_csr<T>), kThreads, 0, c.stream>>>(
+                                  c.d_ia.p, c.d_ja.p, c.d_a32.p, w.pm.p, w.q32.p, c.neq, R)));
+    }
+    k_tl_update<<<wave(k_tl_update), kThreads, 0, c.stream>>>(w.dx32.p, w.r32.p, w.pm.p, w.q32.p, padded,
+                                                              sym ? 1 : 0, c.neq, R);
+    k_mx_foldx<<<wave(k_mx_foldx), kThreads, 0, c.stream>>>(w.x.p, w.dx32.p, c.neq, 0, R);
+    GPZ_TPR_SWITCH(P.tpr, (k_reliable<T><<<wave(k_reliable<T>), kThreads, 0, c.stream>>>(
+                              c.d_ia.p, c.d_ja.p, c.d_a.p, w.x.p, w.b.p, w.r.p, c.neq, R)));
+    launch_tl_apply(c, P, R, c.stream);
+    c.launches += 5;
+    return;
+  }
+  if (P.vb)
+    k_vb32_p<<<wave(k_vb32_p), kThreads, 0, c.stream>>>(w.r32.p, P.V, w.pm.p, padded, sym ? w.q32.p : nullptr, R);
+  else
+    k_mx_p<<<wave(k_mx_p), kThreads, 0, c.stream>>>(w.r32.p, P.M32, w.pm.p, padded, sym ? w.q32.p : nullptr,
+                                                    P.nunits, R);
   if (P.bsr) {
     launch_spmv32(c, c.spmv32_variant, c.sell, R, c.stream);
     c.launches--;
@@ -2056,12 +2660,17 @@ void launch_iteration(Ctx &c, const Plan &P) {
     GPZ_TPR_SWITCH(P.tpr32, (k_mx_csr<T><<<wave(k_mx_csr<T>), kThreads, 0, c.stream>>>(c.d_ia.p, c.d_ja.p, c.d_a32.p,
                                                                                       w.pm.p, w.q32.p, c.neq, R)));
   }
-  k_mx_update<<<wave(k_mx_update), kThreads, 0, c.stream>>>(w.dx32.p, w.r32.p, w.pm.p, w.q32.p, P.M32, padded,
-                                                            sym ? 1 : 0, P.nunits, R);
+  if (P.vb)
+    k_vb32_update<<<wave(k_vb32_update), kThreads, 0, c.stream>>>(w.dx32.p, w.r32.p, w.pm.p, w.q32.p, P.V, padded,
+                                                                  sym ? 1 : 0, R);
+  else
+    k_mx_update<<<wave(k_mx_update), kThreads, 0, c.stream>>>(w.dx32.p, w.r32.p, w.pm.p, w.q32.p, P.M32, padded,
+                                                              sym ? 1 : 0, P.nunits, R);
   k_mx_foldx<<<wave(k_mx_foldx), kThreads, 0, c.stream>>>(w.x.p, w.dx32.p, c.neq, 0, R);
   GPZ_TPR_SWITCH(P.tpr, (k_reliable<T><<<wave(k_reliable<T>), kThreads, 0, c.stream>>>(c.d_ia.p, c.d_ja.p, c.d_a.p,
                                                                                         w.x.p, w.b.p, w.r.p, c.neq, R)));
-  k_mx_r32<<<wave(k_mx_r32), kThreads, 0, c.stream>>>(w.r.p, w.r32.p, P.M32, P.nunits, R);
+  if (P.vb) k_vb32_r32<<<wave(k_vb32_r32), kThreads, 0, c.stream>>>(w.r.p, w.r32.p, P.V, R);
+  else k_mx_r32<<<wave(k_mx_r32), kThreads, 0, c.stream>>>(w.r.p, w.r32.p, P.M32, P.nunits, R);
   c.launches += 6;
 }
 
@@ -2564,12 +3173,24 @@ int solve(Ctx &c, const gpz_solver_opts &o, gpz_solve_report &rep) {
     return solve_learned(c, o, rep, o.solver == GPZ_SOLVER_LEARNED_MIXED_FCG);
   const bool mixed = o.solver == GPZ_SOLVER_MIXED_CG;
   GPZ_REQUIRE(o.solver == GPZ_SOLVER_CG || mixed, GPZ_E_INVALID, "solver kind not available");
-  GPZ_REQUIRE(o.precond == GPZ_PRECOND_JACOBI || o.precond == GPZ_PRECOND_BLOCK_JACOBI || o.precond == 0,
+  GPZ_REQUIRE(o.precond == GPZ_PRECOND_JACOBI || o.precond == GPZ_PRECOND_BLOCK_JACOBI ||
+                  o.precond == GPZ_PRECOND_NODESET_JACOBI || o.precond == GPZ_PRECOND_TWO_LEVEL || o.precond == 0,
               GPZ_E_INVALID, "preconditioner not available");
-  const bool block = o.precond == GPZ_PRECOND_BLOCK_JACOBI;
+  const bool tl = o.precond == GPZ_PRECOND_TWO_LEVEL;
+  GPZ_REQUIRE(!tl || mixed, GPZ_E_INVALID, "the two-level preconditioner is built for the mixed CG");
+  if (tl && !c.tl.ready)
+    GPZ_REQUIRE(two_level_build(c) == GPZ_OK, GPZ_E_INVALID,
+                "two-level preconditioner: needs one uniform grid of axis-aligned Q2 hex elasticity elements "
+                "(3 equations per connect, no equation filter) and at most 3000 coarse equations");
+  // whole connect blocks of other sizes than 3, and the node-set blocks: variable-size block Jacobi
+  const bool vb = o.precond == GPZ_PRECOND_NODESET_JACOBI ||
+                  (o.precond == GPZ_PRECOND_BLOCK_JACOBI && !connect_blocks_are_3(c));
+  const bool block = (o.precond == GPZ_PRECOND_BLOCK_JACOBI && !vb) || tl;
   if (mixed && (!c.have_a32 || (o.spmv_variant >= 0 && c.have_bsr3 && o.spmv_variant != c.spmv32_variant)))
     make_fp32_copy(c, o.spmv_variant);
   if (block && !c.have_bjinv) build_block_jacobi(c);
+  if (vb && (!c.have_vbinv || c.vb_kind != o.precond)) build_vblocks(c, o.precond);
+  if (tl && !c.tl.have_inv) two_level_assemble(c);
   alloc_work(c, mixed);
   SolverWork &w = c.sw;
   cudaStream_t s = c.stream;
@@ -2581,9 +3202,13 @@ int solve(Ctx &c, const gpz_solver_opts &o, gpz_solve_report &rep) {
   P.tpr32 = pick_tpr32(c.nnz, c.neq);
   P.nunits = block ? c.neq / 3 : c.neq;
   P.M = Prec{c.d_dinv.p, block ? c.d_bjinv.p : nullptr, block ? 1 : 0};
+  P.vb = vb;
   if (mixed) {
     // FP32 copies of the preconditioner
-    if (block) {
+    if (vb) {
+      if (!c.d_vb_inv32.p || c.d_vb_inv32.n != c.d_vb_inv.n) c.d_vb_inv32.alloc(c.d_vb_inv.n);
+      k_to_f32<<<wave(k_to_f32), kThreads, 0, s>>>(c.d_vb_inv.p, c.d_vb_inv32.p, (int64_t)c.d_vb_inv.n);
+    } else if (block) {
       c.d_bjinv32.alloc((size_t)P.nunits * 9);
       k_to_f32<<<wave(k_to_f32), kThreads, 0, s>>>(c.d_bjinv.p, c.d_bjinv32.p, (int64_t)P.nunits * 9);
     } else {
@@ -2594,6 +3219,14 @@ int solve(Ctx &c, const gpz_solver_opts &o, gpz_solve_report &rep) {
     P.M32 = Prec32{block ? nullptr : c.d_dinv32.p, block ? c.d_bjinv32.p : nullptr, block ? 1 : 0};
     w.dx32.zero(s);
     w.pm.zero(s);
+  }
+  P.V = vblk_of(c);
+  P.tl = tl;
+  if (tl) {
+    TwoLevel &T = c.tl;
+    P.T = TlView{T.vtx_eq.p, T.brow_vtx.p, T.cfix.p, T.acinv32.p, T.rc.p, T.zc.p, T.z32.p, (int)T.lx[0] + 1,
+                 (int)T.lx[1] + 1, (int)T.lx[2] + 1, T.s, T.m[0], T.m[1], T.m[2], T.nc};
+    T.rc.zero(s);
   }
   const int batch = o.check_every > 0 ? o.check_every : 32;
 
@@ -2614,13 +3247,18 @@ int solve(Ctx &c, const gpz_solver_opts &o, gpz_solve_report &rep) {
   GPZ_TPR_SWITCH(P.tpr, (k_cg_init<T><<<wave(k_cg_init<T>), kThreads, 0, s>>>(c.d_ia.p, c.d_ja.p, c.d_a.p, w.x.p,
                                                                                w.b.p, w.r.p, c.neq, o.from_current,
                                                                                R)));
-  if (mixed) k_mx_r32<<<wave(k_mx_r32), kThreads, 0, s>>>(w.r.p, w.r32.p, P.M32, P.nunits, R);
+  if (tl) {
+    launch_tl_apply(c, P, R, s);
+    c.launches -= 1;  // with k_cg_init: five launches
+  } else if (mixed && vb) k_vb32_r32<<<wave(k_vb32_r32), kThreads, 0, s>>>(w.r.p, w.r32.p, P.V, R);
+  else if (mixed) k_mx_r32<<<wave(k_mx_r32), kThreads, 0, s>>>(w.r.p, w.r32.p, P.M32, P.nunits, R);
+  else if (vb) k_vb_dot<<<wave(k_vb_dot), kThreads, 0, s>>>(w.r.p, P.V, R);
   else k_precond_dot<<<wave(k_precond_dot), kThreads, 0, s>>>(w.r.p, P.M, P.nunits, R);
   c.launches += 2;
   GPZ_CUDA_TRY(cudaGetLastError());
 
   cudaGraphExec_t exec = nullptr;
-  const int per_iter = mixed ? 6 : 3;
+  const int per_iter = tl ? 9 : (mixed ? 6 : 3);
   if (o.use_graph) {
     cudaGraph_t g;
     GPZ_CUDA_TRY(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
@@ -2678,6 +3316,66 @@ int solve(Ctx &c, const gpz_solver_opts &o, gpz_solve_report &rep) {
   if (hstate[I_BREAK]) return GPZ_E_BREAKDOWN;
   if (cancelled && hstate[I_CONV] == 0) return GPZ_CANCELLED;
   return hstate[I_CONV] == 1 ? GPZ_OK : GPZ_NOT_CONVERGED;
+}
+
+// z = M r for a CG preconditioner of the assembled system (host FP64 vectors):
+// what one application inside GPZ_SOLVER_CG (FP64: Jacobi, block Jacobi,
+// node-set blocks) or GPZ_SOLVER_MIXED_CG (FP32: the two-level preconditioner) computes
+void precond_apply(Ctx &c, int precond, const double *hr, double *hz) {
+  GPZ_REQUIRE(precond == GPZ_PRECOND_JACOBI || precond == GPZ_PRECOND_BLOCK_JACOBI ||
+                  precond == GPZ_PRECOND_NODESET_JACOBI || precond == GPZ_PRECOND_TWO_LEVEL,
+              GPZ_E_INVALID, "preconditioner kind");
+  cudaStream_t s = c.stream;
+  const bool tl = precond == GPZ_PRECOND_TWO_LEVEL;
+  const bool vb = precond == GPZ_PRECOND_NODESET_JACOBI ||
+                  (precond == GPZ_PRECOND_BLOCK_JACOBI && !connect_blocks_are_3(c));
+  const bool block = (precond == GPZ_PRECOND_BLOCK_JACOBI && !vb) || tl;
+  if (tl) {
+    if (!c.have_a32) make_fp32_copy(c, -1);
+    if (!c.tl.ready)
+      GPZ_REQUIRE(two_level_build(c) == GPZ_OK, GPZ_E_INVALID, "two-level preconditioner: not a uniform Q2 hex grid");
+    if (!c.tl.have_inv) two_level_assemble(c);
+  }
+  if (block && !c.have_bjinv) build_block_jacobi(c);
+  if (vb && (!c.have_vbinv || c.vb_kind != precond)) build_vblocks(c, precond);
+  alloc_work(c, tl);
+  SolverWork &w = c.sw;
+  GPZ_CUDA_TRY(cudaMemcpyAsync(w.r.p, hr, c.neq * sizeof(double), cudaMemcpyHostToDevice, s));
+  if (tl) {
+    Plan P;
+    P.nunits = c.neq / 3;
+    c.d_bjinv32.alloc((size_t)P.nunits * 9);
+    k_to_f32<<<wave(k_to_f32), kThreads, 0, s>>>(c.d_bjinv.p, c.d_bjinv32.p, (int64_t)P.nunits * 9);
+    P.M32 = Prec32{nullptr, c.d_bjinv32.p, 1};
+    TwoLevel &T = c.tl;
+    P.T = TlView{T.vtx_eq.p, T.brow_vtx.p, T.cfix.p, T.acinv32.p, T.rc.p, T.zc.p, T.z32.p, (int)T.lx[0] + 1,
+                 (int)T.lx[1] + 1, (int)T.lx[2] + 1, T.s, T.m[0], T.m[1], T.m[2], T.nc};
+    T.rc.zero(s);
+    double hs[S_NSCAL] = {0};
+    int64_t hi[I_NISCAL] = {0};
+    hi[I_MAXIT] = 1;
+    hi[I_UPDATE] = 2;  // r32 = r
+    GPZ_CUDA_TRY(cudaMemcpyAsync(w.scal.p, hs, sizeof(hs), cudaMemcpyHostToDevice, s));
+    GPZ_CUDA_TRY(cudaMemcpyAsync(w.iscal.p, hi, sizeof(hi), cudaMemcpyHostToDevice, s));
+    launch_tl_apply(c, P, red_of(c), s);
+    c.launches++;
+    std::vector<float> z(c.neq);
+    GPZ_CUDA_TRY(cudaMemcpyAsync(z.data(), T.z32.p, c.neq * sizeof(float), cudaMemcpyDeviceToHost, s));
+    GPZ_CUDA_TRY(cudaStreamSynchronize(s));
+    for (int64_t i = 0; i < c.neq; i++) hz[i] = z[i];
+  } else {
+    if (vb) {
+      k_vb_apply<<<wave(k_vb_apply), kThreads, 0, s>>>(w.r.p, vblk_of(c), w.q.p);
+    } else {
+      const Prec M{c.d_dinv.p, block ? c.d_bjinv.p : nullptr, block ? 1 : 0};
+      k_prec_apply<<<wave(k_prec_apply), kThreads, 0, s>>>(w.r.p, M, block ? c.neq / 3 : c.neq, w.q.p);
+    }
+    c.launches++;
+    GPZ_CUDA_TRY(cudaMemcpyAsync(hz, w.q.p, c.neq * sizeof(double), cudaMemcpyDeviceToHost, s));
+    GPZ_CUDA_TRY(cudaStreamSynchronize(s));
+  }
+  GPZ_CUDA_TRY(cudaGetLastError());
+  check_device_flag(c, "preconditioner application");
 }
 
 // y = A32 x with the mixed CG's FP32 operator in its current layout (the

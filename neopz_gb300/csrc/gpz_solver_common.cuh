@@ -31,7 +31,8 @@ int wave(K kernel) {
 
 // device scalar slots
 // alpha and beta are formed once, by the CTA that finishes the reduction they depend on
-enum { S_RHO = 0, S_RHO1, S_PQ, S_RR, S_NORMB, S_TOL, S_MAXRR, S_DELTA2, S_RESID, S_TRUERR, S_ALPHA, S_BETA, S_NSCAL };
+enum { S_RHO = 0, S_RHO1, S_PQ, S_RR, S_NORMB, S_TOL, S_MAXRR, S_DELTA2, S_RESID, S_TRUERR, S_ALPHA, S_BETA, S_RRREC,
+       S_NSCAL };
 enum { I_CONV = 0, I_IT, I_MAXIT, I_UPDATE, I_NUPD, I_SP64, I_SP32, I_BREAK, I_RESTART, I_NRESTART, I_NISCAL };
 
 struct Red {

@@ -21,7 +21,7 @@ GPZ_F_NONE, GPZ_F_CONST, GPZ_F_SINPROD, GPZ_F_QUADRATIC = 0, 1, 2, 3
 GPZ_PREC_FP64, GPZ_PREC_MIXED = 0, 1
 GPZ_SOLVER_CG, GPZ_SOLVER_GMRES, GPZ_SOLVER_MIXED_CG, GPZ_SOLVER_LEARNED_FCG, GPZ_SOLVER_LEARNED_MIXED_FCG = 1, 2, 3, 4, 5
 GPZ_SOLVER_JACOBI = 6
-GPZ_PRECOND_JACOBI, GPZ_PRECOND_BLOCK_JACOBI = 1, 2
+GPZ_PRECOND_JACOBI, GPZ_PRECOND_BLOCK_JACOBI, GPZ_PRECOND_NODESET_JACOBI, GPZ_PRECOND_TWO_LEVEL = 1, 2, 3, 4
 GPZ_KERNEL_SPMV_FP64, GPZ_KERNEL_SPMV_FP32, GPZ_KERNEL_ASSEMBLE = 1, 2, 3
 BIGNUMBER = 10.0 ** 17 * 2 / 3  # TPZMaterial::fBigNumber default for double
 
@@ -91,6 +91,9 @@ def lib():
         vp, i64, i32, dp = ctypes.c_void_p, ctypes.c_int64, ctypes.c_int, ctypes.c_double
         L.gpz_ctx_create.argtypes = [_P(vp), i32]
         L.gpz_ctx_destroy.argtypes = [vp]
+        L.gpz_two_level_config.argtypes = [vp, i32]
+        L.gpz_two_level_info.argtypes = [vp, vp]
+        L.gpz_precond_apply.argtypes = [vp, i32, vp, vp]
         L.gpz_get_error_string.restype = ctypes.c_char_p
         L.gpz_get_error_string.argtypes = [i32]
         L.gpz_last_error_detail.restype = ctypes.c_char_p
@@ -475,6 +478,21 @@ class Context:
         l0, l1 = ctypes.c_double(), ctypes.c_double()
         self._check(lib().gpz_learned_train(self.h, steps, lr, ctypes.byref(l0), ctypes.byref(l1)))
         return l0.value, l1.value
+
+    def precond_apply(self, precond, r):
+        r = np.ascontiguousarray(r, np.float64)
+        z = np.zeros(self.neq)
+        self._check(lib().gpz_precond_apply(self.h, int(precond), _p(r), _p(z)))
+        return z
+
+    def two_level_config(self, coarse_boxes):
+        self._check(lib().gpz_two_level_config(self.h, int(coarse_boxes)))
+
+    def two_level_info(self):
+        v = np.zeros(9, np.int64)
+        self._check(lib().gpz_two_level_info(self.h, _p(v)))
+        return dict(fine_cells=v[0:3].tolist(), s=int(v[3]), coarse_boxes=v[4:7].tolist(), coarse_eqs=int(v[7]),
+                    removed_nodes=int(v[8]))
 
     def solution(self):
         """The device solution of the last solve (gpz_solution_download)."""

@@ -164,7 +164,8 @@ def test_mixed_cg_reaches_true_fp64_residual(built, case):
 
 @pytest.mark.parametrize("case", ["elast3d_p1", "elast3d_p2", "elast3d_hp"])
 def test_block_jacobi_pcg_matches_oracle(built, case):
-    """Connect-block (3x3) Jacobi CG against the oracle's TPZBlockDiagonal-preconditioned CG."""
+    """Connect-block Jacobi CG against the oracle's TPZBlockDiagonal-preconditioned CG over the same connect
+    blocks (3x3 at p <= 2; whole blocks of 3 to 24 equations on the hp mesh)."""
     g = _gpz()
     mk_o, mk_g = built[case]
     om, grid = mk_o(), mk_g()
@@ -176,7 +177,12 @@ def test_block_jacobi_pcg_matches_oracle(built, case):
     sol = ctx.solve(precond=g.GPZ_PRECOND_BLOCK_JACOBI, tol=tol, max_iter=20000)
     oia, oja = om.pattern(True)
     oa, of = om.assemble(True, oia, oja)
-    ref = O.cg_block_jacobi(True, oia, oja, oa, of, 3, 20000, tol)
+    # the connect blocks of TPZBlockDiagonalStructMatrix: 3 equations each at p <= 2, 3 to 24 on the hp mesh
+    bp, bs = om.blocks()
+    keep = bs > 0
+    bi = np.concatenate([[0], np.cumsum(bs[keep])]).astype(np.int64)
+    be = np.concatenate([np.arange(p, p + n) for p, n in zip(bp[keep], bs[keep])]).astype(np.int64)
+    ref = O.cg_sparse_block_jacobi(True, oia, oja, oa, of, bi, be, 20000, tol)
     assert sol["rc"] == 0 and ref["rc"] == 0
     assert np.linalg.norm(sol["x"] - ref["x"]) <= 1e-8 * np.linalg.norm(ref["x"])
     assert abs(sol["iterations"] - ref["iters"]) <= max(3, 0.1 * ref["iters"]), (sol["iterations"], ref["iters"])
@@ -201,7 +207,7 @@ def test_mixed_block_jacobi_bsr3(built):
     ctx.close()
 
 
-@pytest.mark.parametrize("variant", [0, 1, 2, 3, 4, 5, 6, 7])
+@pytest.mark.parametrize("variant", [0, 1, 2, 3, 4, 5, 6, 7, 8])
 def test_mixed_spmv_variants_converge(built, variant):
     """Every layout / kernel the SpMV autotuner can pick gives the same converged solution."""
     g = _gpz()
@@ -336,12 +342,12 @@ def test_assembly_graph_replay(built):
     ctx.close()
 
 
-@pytest.mark.parametrize("variant", [0, 1, 2, 3, 4, 5, 6, 7])
+@pytest.mark.parametrize("variant", [0, 1, 2, 3, 4, 5, 6, 7, 8])
 def test_fp32_operator_layouts_match_fp64_spmv(built, variant):
     """Every FP32 operator layout of the mixed CG (block CSR, two rows, sliced ELL, TMA-staged, upper blocks
-    with atomics, matrix-free elements on CUDA cores, on the tensor cores in 3xTF32 and sum-factorised on
-    Lagrange nodal values) applies the assembled
-    operator: within 1e-5 of the FP64 CSR SpMV,
+    with atomics, matrix-free elements on CUDA cores, on the tensor cores in 3xTF32, sum-factorised on
+    Lagrange nodal values, and the shared element matrix of a uniform grid as one tcgen05 3xTF32 GEMM per tile)
+    applies the assembled operator: within 1e-5 of the FP64 CSR SpMV,
     normwise and on the non-penalty rows alone."""
     g = _gpz()
     rng = np.random.default_rng(12)
@@ -361,6 +367,32 @@ def test_fp32_operator_layouts_match_fp64_spmv(built, variant):
     diag = np.array([a[ia[i]:ia[i + 1]][ja[ia[i]:ia[i + 1]] == i][0] for i in range(grid.neq)])
     inner = diag < 1e6 * np.median(diag)  # rows without the 1e12 penalty
     assert np.linalg.norm((y32 - y64)[inner]) <= 1e-5 * np.linalg.norm(y64[inner])
+    if variant == 8:  # a uniform grid: the shared element matrix is offered and is the operator applied
+        assert ctx.tuning_report()["chosen"] == "matrix_free_shared_matrix_tcgen05"
+    ctx.close()
+
+
+def test_shared_element_matrix_operator_more_tiles_than_sms(built):
+    """The shared-element-matrix operator over more tiles of 128 elements than there are CTAs (each CTA
+    loops over tiles, alternating its two TMEM accumulators) and a ragged last tile: 30^3 elements, 211 tiles."""
+    g = _gpz()
+    rng = np.random.default_rng(13)
+    n = 30
+    grid = g.elasticity3d(n, 2, E=np.exp(rng.standard_normal(n ** 3)))
+    ctx = g.Context(0)
+    ctx.upload_mesh(grid)
+    ctx.build_pattern(False)
+    ctx.assemble(g.GPZ_PREC_MIXED)
+    x = rng.standard_normal(grid.neq)
+    y64 = ctx.spmv(x)
+    y32 = ctx.spmv_fp32(x, 8)
+    assert ctx.tuning_report()["chosen"] == "matrix_free_shared_matrix_tcgen05"
+    assert np.linalg.norm(y32 - y64) <= 1e-5 * np.linalg.norm(y64)
+    sol = ctx.solve(solver=g.GPZ_SOLVER_MIXED_CG, precond=g.GPZ_PRECOND_BLOCK_JACOBI, tol=1e-8, reliable_delta=1e-2,
+                    spmv_variant=8)
+    ref = ctx.solve(tol=1e-12, max_iter=50000)
+    assert sol["rc"] == 0 and sol["true_resid"] <= 1e-8
+    assert np.linalg.norm(sol["x"] - ref["x"]) <= 1e-8 * np.linalg.norm(ref["x"])
     ctx.close()
 
 
@@ -392,6 +424,8 @@ def test_distorted_mesh_general_quadrature_path(built):
     assert np.max(np.abs(f - of)) <= 1e-12 * np.max(np.abs(of))
     x = rng.standard_normal(grid.neq)
     y64 = ctx.spmv(x)
-    for v in (0, 4, 5, 6, 7):
+    for v in (0, 4, 5, 6, 7, 8):
         assert np.linalg.norm(ctx.spmv_fp32(x, v) - y64) <= 1e-5 * np.linalg.norm(y64), v
+        if v == 8:  # elements of different Jacobians: no shared element matrix, another layout applies
+            assert ctx.tuning_report()["chosen"] != "matrix_free_shared_matrix_tcgen05"
     ctx.close()

@@ -278,9 +278,10 @@ def test_nodeset_rejects_bad_input(g):
 
 def test_hp_block_jacobi_variants_in_the_oracle(g):
     """On an hp mesh (4^3 hexes, p in {1,2,3}) the reference's connect blocks (TPZBlockDiagonalStructMatrix: one
-    block of nshape x 3 equations per connect, 3 to 24 here) and the per-shape 3x3 blocks that
-    GPZ_PRECOND_BLOCK_JACOBI applies on the device give the same solution and CG iteration counts within 5%
-    (264 and 271 to 1e-8); the node-set blocks of overlap = false need markedly fewer (189)."""
+    block of nshape x 3 equations per connect, 3 to 24 here; what GPZ_PRECOND_BLOCK_JACOBI applies in the device
+    CG) and the per-shape 3x3 blocks (the device GMRES's split of a larger connect block) give the same solution
+    and CG iteration counts within 5% (264 and 271 to 1e-8); the node-set blocks of overlap = false need
+    markedly fewer (189)."""
     n = 4
     orders = g.hp_orders(n ** 3, 3)
     E = g.lognormal(n ** 3, 0.5, 3)
