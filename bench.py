@@ -3,15 +3,15 @@
 One step = the hot path over the synthetic system: global assembly into the
 CSR (FP64 parity assembly + the FP32 operator of the inner solves) and the
 iterative solve to a TRUE FP64 residual below 1e-8 with the learned + mixed
-flexible PCG (the committed elasticity weights, FP32 operator and recurrence,
-FP64 true-residual replacement).  `value` is device time with the mesh and
-pattern resident in HBM (CUDA events on the library's stream); `e2e` is the
-same pipeline through the public C ABI from host buffers (mesh upload, pattern
-build, assembly, weights, solve, solution download).  The plain FP64
-Jacobi-PCG of the reference (same algorithm, on the GPU) is timed once beside
-it as the path's own baseline, and the mixed block-Jacobi CG without the
-learned correction (`--path mixed` times it as the step) once as the other
-comparison.
+flexible PCG (the committed elasticity weights on the two-level block-Jacobi
+base, FP32 operator and recurrence, FP64 true-residual replacement).  `value`
+is device time with the mesh and pattern resident in HBM (CUDA events on the
+library's stream); `e2e` is the same pipeline through the public C ABI from
+host buffers (mesh upload, pattern build, assembly, weights, solve, solution
+download).  The plain FP64 Jacobi-PCG of the reference (same algorithm, on the
+GPU) is timed once beside it as the path's own baseline; the mixed two-level
+CG (the same method without the network) and the mixed block-Jacobi CG are
+timed once each as the other comparisons (`--path` picks the timed one).
 
 Usage: python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference] [--n 64]
 """
@@ -32,6 +32,23 @@ sys.path.insert(0, ROOT)
 METRIC = "s to ||r||/||b||<1e-8: learned+mixed PCG vs FP64 Jacobi-PCG (GB300); elem/s"
 LEARNED_WEIGHTS = os.path.join(ROOT, "neopz_gb300", "data", "learned_elasticity3d_q2.npy")
 LEARNED_RANK = 8
+LEARNED_BASE = 4  # GPZ_PRECOND_TWO_LEVEL: the base under the learned correction
+# solver paths of a step: the metric's learned + mixed flexible PCG (the correction on the two-level base), the
+# mixed CG with that base alone (the method without the network), the mixed block-Jacobi CG, the FP64 Jacobi-PCG
+PATH_KEY = {"learned": "learned_mixed_fcg", "two_level": "mixed_two_level_cg", "mixed": "mixed_block_jacobi_cg",
+            "fp64": "fp64_jacobi_pcg"}
+PATH_CHECK = {"learned": 16, "two_level": 16, "mixed": 64, "fp64": 64}  # iterations per convergence check
+PATH_DESC = {
+    "learned": ("FP64 assembly + FP32 operator ({op}); learned + mixed flexible PCG: learned element-to-node "
+                "correction (rank {rank}, weights {weights}, trained on the GPU) on the two-level block-Jacobi base "
+                "(3x3 connect blocks + Galerkin coarse grid), FP32 recurrence, FP64 x/dots/alpha/beta, reliable "
+                "FP64 true-residual updates"),
+    "two_level": ("FP64 assembly + FP32 operator ({op}); mixed CG with the two-level block-Jacobi preconditioner "
+                  "(3x3 connect blocks + Galerkin coarse grid of 8^3 boxes, coarse inverse on the device), FP32 "
+                  "recurrence, FP64 x/dots, reliable FP64 true-residual updates"),
+    "mixed": ("FP64 assembly + FP32 operator ({op}); mixed CG with connect-block (3x3) Jacobi, FP32 recurrence, "
+              "FP64 x/dots, reliable FP64 true-residual updates"),
+    "fp64": "FP64 assembly; FP64 Jacobi-PCG (the reference's algorithm)"}
 TOL = 1e-8
 ERR_REF_TOL = 1e-12  # true residual of the FP64 solve the solution errors are measured against
 SEED = 5
@@ -57,8 +74,9 @@ def parse():
     ap.add_argument("--no-sloan", action="store_true", help="skip the host graph legs (Sloan renumbering, node-set blocks)")
     ap.add_argument("--spmv-variant", type=int, default=-1,
                     help="FP32 operator of the mixed solves: -1 autotuned, else the gpz_solver_opts spmv_variant")
-    ap.add_argument("--path", default="learned", choices=["learned", "mixed"],
-                    help="solver of the timed step: learned + mixed flexible PCG, or mixed block-Jacobi CG")
+    ap.add_argument("--path", default="learned", choices=["learned", "two_level", "mixed"],
+                    help="solver of the timed step: learned + mixed flexible PCG on the two-level base, the mixed "
+                         "two-level CG, or the mixed block-Jacobi CG")
     return ap.parse_args()
 
 
@@ -177,17 +195,20 @@ def run_gpu(args):
     ctx.learned_init(rank=LEARNED_RANK, seed=0)
     ctx.set_learned_params(weights)
 
-    def step(mixed=True, learned=None):
-        learned = args.path == "learned" if learned is None else learned
-        ctx.assemble(gpz.GPZ_PREC_MIXED if mixed else gpz.GPZ_PREC_FP64)
-        if mixed and learned:
-            return ctx.solve(solver=gpz.GPZ_SOLVER_LEARNED_MIXED_FCG, tol=TOL, max_iter=200000, reliable_delta=1e-2,
-                             check_every=64, want_x=False, spmv_variant=args.spmv_variant)
-        if mixed:
-            return ctx.solve(solver=gpz.GPZ_SOLVER_MIXED_CG, precond=gpz.GPZ_PRECOND_BLOCK_JACOBI, tol=TOL,
-                             max_iter=200000, reliable_delta=1e-2, check_every=64, want_x=False,
-                             spmv_variant=args.spmv_variant)
-        return ctx.solve(solver=gpz.GPZ_SOLVER_CG, tol=TOL, max_iter=200000, check_every=64, want_x=False)
+    def step(path=None):
+        """One step: assembly (FP64 matrix + the FP32 operator of the mixed paths) and the solve to a true FP64
+        ||r||/||b|| < 1e-8 on `path` (the timed one by default)."""
+        path = args.path if path is None else path
+        ctx.assemble(gpz.GPZ_PREC_FP64 if path == "fp64" else gpz.GPZ_PREC_MIXED)
+        kw = dict(tol=TOL, max_iter=200000, check_every=PATH_CHECK[path], want_x=False)
+        if path == "learned":
+            return ctx.solve(solver=gpz.GPZ_SOLVER_LEARNED_MIXED_FCG, precond=LEARNED_BASE, reliable_delta=1e-2,
+                             spmv_variant=args.spmv_variant, **kw)
+        if path in ("two_level", "mixed"):
+            pre = gpz.GPZ_PRECOND_TWO_LEVEL if path == "two_level" else gpz.GPZ_PRECOND_BLOCK_JACOBI
+            return ctx.solve(solver=gpz.GPZ_SOLVER_MIXED_CG, precond=pre, reliable_delta=1e-2,
+                             spmv_variant=args.spmv_variant, **kw)
+        return ctx.solve(solver=gpz.GPZ_SOLVER_CG, **kw)
 
     def timed(fn):
         torch.cuda.synchronize()
@@ -207,7 +228,7 @@ def run_gpu(args):
     if not args.no_fp64_baseline:
         with torch.cuda.stream(stream):
             e0.record(stream)
-        fp64 = step(mixed=False)
+        fp64 = step("fp64")
         with torch.cuda.stream(stream):
             e1.record(stream)
         torch.cuda.synchronize()
@@ -236,10 +257,13 @@ def run_gpu(args):
     t_step = max_over_ranks(t_step, world, "cuda")
     last = reps[-1]
     x_step = ctx.solution()  # the last timed step's solution (outside the timed region)
-    # the other mixed path, once: block-Jacobi CG without the learned correction (or the learned one
-    # when the step is the block-Jacobi CG)
-    other, t_other = timed(lambda: step(learned=args.path != "learned"))
-    x_other = ctx.solution()
+    # the other mixed paths, one step each (after a warm-up step): the two-level CG without the network (the
+    # method without the learned correction) and the block-Jacobi CG
+    others = {}
+    for path in [q for q in ("learned", "two_level", "mixed") if q != args.path]:
+        step(path)
+        r, t = timed(lambda: step(path))
+        others[path] = (r, t, ctx.solution())
     # solution error against the FP64 solution: the FP64 Jacobi-PCG (the parity-tested path, the same algorithm
     # as the reference's CG) run to a true residual of 1e-12, well below the 1e-8 stop of the compared solves
     accuracy = {}
@@ -253,8 +277,7 @@ def run_gpu(args):
                                    f"fixtures) to a true residual {ERR_REF_TOL:g}: {tight['iterations']} iterations, "
                                    f"true residual {tight['true_resid']:.3g}"),
             "value_path": float(np.linalg.norm(x_step - xr) / nr),
-            ("mixed_block_jacobi_cg" if args.path == "learned" else "learned_mixed_fcg"):
-                float(np.linalg.norm(x_other - xr) / nr),
+            **{PATH_KEY[q]: float(np.linalg.norm(v[2] - xr) / nr) for q, v in others.items()},
             "fp64_jacobi_pcg": float(np.linalg.norm(x_fp64 - xr) / nr) if x_fp64 is not None else None,
             "bar": 1e-8}
         del xr, tight
@@ -360,15 +383,15 @@ def run_gpu(args):
         mark("pattern")
         c2.assemble(gpz.GPZ_PREC_MIXED)
         mark("assembly_and_operator_autotune")
+        kw = dict(tol=TOL, max_iter=200000, reliable_delta=1e-2, check_every=PATH_CHECK[args.path], want_x=True)
         if args.path == "learned":
             c2.learned_init(rank=LEARNED_RANK, seed=0)
             c2.set_learned_params(weights)
             mark("learned_setup")
-            r2 = c2.solve(solver=gpz.GPZ_SOLVER_LEARNED_MIXED_FCG, tol=TOL, max_iter=200000, reliable_delta=1e-2,
-                          check_every=64, want_x=True)
+            r2 = c2.solve(solver=gpz.GPZ_SOLVER_LEARNED_MIXED_FCG, precond=LEARNED_BASE, **kw)
         else:
-            r2 = c2.solve(solver=gpz.GPZ_SOLVER_MIXED_CG, precond=gpz.GPZ_PRECOND_BLOCK_JACOBI, tol=TOL,
-                          max_iter=200000, reliable_delta=1e-2, check_every=64, want_x=True)
+            r2 = c2.solve(solver=gpz.GPZ_SOLVER_MIXED_CG, precond=gpz.GPZ_PRECOND_TWO_LEVEL if args.path ==
+                          "two_level" else gpz.GPZ_PRECOND_BLOCK_JACOBI, **kw)
         torch.cuda.synchronize()
         mark("solve_and_download")
         e2e_times.append(time.perf_counter() - t0)
@@ -385,12 +408,9 @@ def run_gpu(args):
         "config": {"workload": f"3D linear elasticity {n}^3 hex Q2 (TPZElasticity3D), E lognormal(sigma=1) seed {SEED}, "
                                "nu=0.3, clamped z=0 (penalty), traction (0,0,-1) on z=1",
                    "neq": neq, "nnz_full": nnz, "nnz_upper": nnz_upper, "elements": nel, "volume_elements": nvol,
-                   "path": (f"FP64 assembly; learned + mixed flexible PCG: learned element-to-node correction (rank "
-                            f"{LEARNED_RANK}, weights {os.path.relpath(LEARNED_WEIGHTS, ROOT)}, trained on the GPU) "
-                            f"on Jacobi, FP32 operator chosen by the autotuner ({chosen}), FP32 recurrence, FP64 "
-                            "x/dots/alpha/beta, reliable FP64 true-residual updates" if args.path == "learned" else
-                            f"FP64 assembly; CG with the FP32 inner operator chosen by the autotuner ({chosen}), "
-                            "FP64 x/dots, reliable FP64 true-residual updates; connect-block (3x3) Jacobi"),
+                   "path": PATH_DESC[args.path].format(rank=LEARNED_RANK, weights=os.path.relpath(LEARNED_WEIGHTS,
+                                                                                                   ROOT),
+                                                      op=chosen),
                    "l2": "inputs larger than L2 (matrix > 129 MB)",
                    "parallelism": f"replicas x{world}"},
         "solution_rel_err_vs_fp64": accuracy.get("value_path"),
@@ -400,10 +420,12 @@ def run_gpu(args):
                   "spmv_fp64": last["spmv_fp64"], "restarts": last["restarts"], "solve_s": last["seconds"]},
         "fp64_jacobi_pcg": {"seconds": t_fp64, "iterations": fp64["iterations"], "true_resid": fp64["true_resid"],
                             "speedup_of_value": (t_fp64 / t_step) if t_fp64 else None},
-        ("mixed_block_jacobi_cg" if args.path == "learned" else "learned_mixed_fcg"): {
-            "seconds": round(t_other, 6), "iterations": other["iterations"], "true_resid": other["true_resid"],
-            "solve_s": other["seconds"], "speedup_vs_fp64_jacobi_pcg": (t_fp64 / t_other) if t_fp64 else None,
-            "note": "one step (assembly + solve), timed once after the timed steps"},
+        **{PATH_KEY[q]: {"seconds": round(t, 6), "iterations": r["iterations"], "true_resid": r["true_resid"],
+                         "solve_s": r["seconds"], "speedup_vs_fp64_jacobi_pcg": (t_fp64 / t) if t_fp64 else None,
+                         "path": PATH_DESC[q].format(rank=LEARNED_RANK, weights=os.path.relpath(LEARNED_WEIGHTS,
+                                                                                                   ROOT), op=chosen),
+                         "note": "one step (assembly + solve), timed once after the timed steps"}
+           for q, (r, t, _) in others.items()},
         "assembly": {"fp64_seconds": t_asm, "elements_per_s": nel / t_asm, "volume_elements_per_s": nvol / t_asm,
                      "pattern_build_s": t_pattern, "host_mesh_build_s": t_mesh},
         "e2e": {"value": round(t_e2e, 6) if t_e2e else None, "unit": "s", "phases_s": e2e_best, "h2d_bytes_per_step": int(b_in + (weights.nbytes if args.path == "learned" else 0)),
@@ -614,33 +636,56 @@ def cpu_baseline(iters_full, n_full):
 
 
 def run_reference(args):
+    """The reference arm on the host cores, at the benchmark's own size: the oracle (the reference's algorithm
+    restated and pinned to the reference library's fixtures) builds the full 64^3 system once -- the
+    TPZSSpStructMatrix pattern (timed) and the TPZStructMatrixOR assembly on every host thread (timed) --
+    and every step times one Jacobi-PCG iteration of it (TPZSYsmpMatrix::MultAdd is serial, the Jacobi step
+    with its extra Residual SpMV, as the reference runs them).  value = pattern + assembly + the FP64
+    Jacobi-PCG iteration count to 1e-8 x the median step: extrapolated in the iteration count only."""
     rank, world, local = dist_info()
     if rank != 0:
         return
     from oracle import oracle as O
     O.build()
     threads = os.cpu_count() or 1
-    iters = JACOBI_ITERS_64_DEFAULT
-    vals = []
-    for _ in range(args.warmup):
-        cpu_sample(8, iters, args.n, threads, cg_iters=10)
+    n = args.n
+    E = np.exp(np.random.default_rng(SEED).standard_normal(n ** 3))
     t0 = time.perf_counter()
-    last = None
+    m = O.elasticity3d(n, 2, E=E, body_force=(0.0, 0.0, 0.0))
+    ia, ja = m.pattern(True)
+    t_pattern = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    a, f = m.assemble(True, ia, ja, nthreads=threads)
+    t_asm = time.perf_counter() - t0
+    for _ in range(args.warmup):  # warm-up: one SpMV each (the memory of the matrix paged in)
+        O.spmv(True, ia, ja, a, f)
+    its = []
+    t0 = time.perf_counter()
     for _ in range(args.steps):
-        v, last = cpu_sample(12, iters, args.n, threads)
-        vals.append(v)
+        t1 = time.perf_counter()
+        O.cg_jacobi(True, ia, ja, a, f, 1, 0.0, jacobi_residual=True)
+        its.append(time.perf_counter() - t1)
     wall = time.perf_counter() - t0
-    value = statistics.median(vals)
+    t_it = statistics.median(its)
+    iters = JACOBI_ITERS_64_DEFAULT if n == 64 else None
+    if iters is None:  # another size: the oracle's own count (small sizes only)
+        iters = O.cg_jacobi(True, ia, ja, a, f, 200000, TOL)["iters"]
+    value = t_pattern + t_asm + iters * t_it
+    sample = (f"oracle at the full {n}^3 size ({len(ia) - 1} equations, {len(ja)} stored upper entries): pattern "
+              f"{t_pattern:.1f} s, threaded OR assembly {t_asm:.1f} s ({m.ncel / t_asm:.0f} elements/s, {threads} "
+              f"threads), {t_it:.2f} s per serial Jacobi-PCG iteration (median of {args.steps}); extrapolated to "
+              f"{iters} iterations, the FP64 Jacobi-PCG count to 1e-8 of this system measured on the GB300 with the "
+              "same algorithm")
     out = {"metric": METRIC, "value": round(value, 2), "unit": "s", "n_gpus": world, "steps": args.steps,
            "warmup": args.warmup, "ms_per_step": round(wall / args.steps * 1e3, 1), "higher_is_better": False,
            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic", "impl": "reference",
-           "config": {"workload": f"3D linear elasticity {args.n}^3 hex Q2, E lognormal(sigma=1), nu=0.3, clamped "
-                                  "base, top traction", "parallelism": "host threads"},
+           "config": {"workload": f"3D linear elasticity {n}^3 hex Q2, E lognormal(sigma=1) seed {SEED}, nu=0.3, "
+                                  "clamped base, top traction", "parallelism": "host threads",
+                      "same_config": True},
            "cpu_baseline": {"value": round(value, 2), "unit": "s", "cores": threads, "kind": "port",
-                            "sample": f"oracle (restated reference algorithm) on a 12^3 instance per step, "
-                                      f"extrapolated to {args.n}^3 with {iters} Jacobi-PCG iterations "
-                                      f"({last['asm_el_per_s']:.0f} assembly el/s, "
-                                      f"{last['t_cg_iter']*1e3:.1f} ms/iteration at 12^3)"},
+                            "sample": sample},
+           "phases_s": {"pattern": round(t_pattern, 2), "assembly": round(t_asm, 2),
+                        "jacobi_pcg_iteration": round(t_it, 3), "iterations": iters},
            "e2e": {"value": round(value, 2), "unit": "s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(out))
 

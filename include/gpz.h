@@ -137,6 +137,20 @@ int gpz_mesh_upload(gpz_ctx *ctx, const gpz_mesh_desc *desc);
 int gpz_sloan_resequence(int64_t nnodes, int64_t nel, const int64_t *elgraphindex, const int64_t *elgraph,
                          int64_t *perm_gather, int64_t *perm_scatter);
 
+/* ---- element colouring of the atomic-free scatter --------------------------------
+ * The colouring gpz_mesh_upload gives the elements (the idea of
+ * TPZStructMatrix::ComputeElementColors, StrMatrix/TPZStructMatrix.cpp:104-161):
+ * greedy first fit in element order; elements sharing a non-empty connect get
+ * different colours, so one colour's elements write disjoint rows and CSR
+ * slots and the assembly launches one colour at a time without atomics.
+ * Host code, no context and no GPU.  Inputs: ComputeElGraph's lists as for
+ * gpz_sloan_resequence (the connects of every element) and the connects'
+ * block sizes (NShape x NState; empty connects impose nothing).  Outputs:
+ * colours[nel], *ncolours.  GPZ_E_INVALID for a connect out of range or more
+ * than 64 colours. */
+int gpz_element_colours(int64_t nel, const int64_t *elgraphindex, const int64_t *elgraph, int64_t nconnects,
+                        const int64_t *block_size, int32_t *colours, int32_t *ncolours);
+
 /* ---- node-set blocks of the block-Jacobi preconditioner ----------------------
  * Replaces the block construction of TPZAnalysis::BuildPreconditioner(
  * EBlockJacobi, overlap = false) (Analysis/TPZAnalysis.cpp:1008-1085):
@@ -288,7 +302,8 @@ int gpz_set_killed(gpz_ctx *ctx, int killed);
 
 typedef struct {
   int32_t solver;          /* GPZ_SOLVER_* */
-  int32_t precond;         /* GPZ_PRECOND_* */
+  int32_t precond;         /* GPZ_PRECOND_*; for the learned solvers the base under the correction
+                              (GPZ_PRECOND_JACOBI, or BLOCK_JACOBI / TWO_LEVEL with the mixed one) */
   int64_t max_iter;
   double tol;              /* stop when ||r||/||b|| <= tol (recursive r, as cg.h:100);
                               GPZ_SOLVER_JACOBI: when ||b - A x|| <= tol */
@@ -420,6 +435,13 @@ int gpz_learned_loss_grad(gpz_ctx *ctx, double *loss, float *grad, int64_t n);
 /* `steps` Adam steps (learning rate lr) on the current pairs; the losses
  * before the first and the last step. */
 int gpz_learned_train(gpz_ctx *ctx, int steps, double lr, double *loss_first, double *loss_last);
+/* Base preconditioner the correction is trained on and solved with (the
+ * solver's opts.precond): 0 / GPZ_PRECOND_JACOBI (M r = S(alpha u + ...) as
+ * above), GPZ_PRECOND_BLOCK_JACOBI (alpha B^-1 r with the 3x3 connect blocks
+ * in place of alpha D^-1 r) or GPZ_PRECOND_TWO_LEVEL (the same plus the
+ * coarse correction P Ac^-1 P^T r, which the training takes off the error
+ * targets).  Clears the training pairs: collect or set them after this call. */
+int gpz_learned_set_base(gpz_ctx *ctx, int precond);
 
 /* ---- allocation-free solve -------------------------------------------------
  * No counterpart in the reference (its CG allocates its work vectors on every

@@ -613,27 +613,17 @@ void build_buckets(Ctx &c, const gpz_mesh_desc &d) {
     }
     el_bucket[e] = bi;
   }
-  // greedy first-fit colouring by shared non-empty connects (the idea of
-  // TPZStructMatrix::ComputeElementColors, StrMatrix/TPZStructMatrix.cpp:104-161)
-  std::vector<uint64_t> used(c.nconnects, 0);
-  std::vector<int> colour(c.nel, 0);
-  int ncol = 0;
+  // greedy first-fit colouring by shared non-empty connects (gpz_element_colours)
+  std::vector<int64_t> gi(c.nel + 1, 0), g, bsz(d.block_size, d.block_size + c.nconnects);
   for (int64_t e = 0; e < c.nel; e++) {
-    int ns = topo(d.el_type[e]).nsides;
-    uint64_t mask = 0;
-    for (int s = 0; s < ns; s++) {
-      int64_t cn = d.el_conn[e * 27 + s];
-      if (d.block_size[cn] > 0) mask |= used[cn];
-    }
-    GPZ_REQUIRE(~mask != 0, GPZ_E_INVALID, "more than 64 element colours");
-    int col = __builtin_ctzll(~mask);
-    colour[e] = col;
-    ncol = std::max(ncol, col + 1);
-    for (int s = 0; s < ns; s++) {
-      int64_t cn = d.el_conn[e * 27 + s];
-      if (d.block_size[cn] > 0) used[cn] |= (1ull << col);
-    }
+    const int ns = topo(d.el_type[e]).nsides;
+    for (int s = 0; s < ns; s++) g.push_back(d.el_conn[e * 27 + s]);
+    gi[e + 1] = (int64_t)g.size();
   }
+  std::vector<int32_t> colour(c.nel, 0);
+  int32_t ncol = 0;
+  const int crc = gpz_element_colours(c.nel, gi.data(), g.data(), c.nconnects, bsz.data(), colour.data(), &ncol);
+  GPZ_REQUIRE(crc == GPZ_OK, GPZ_E_INVALID, "element colouring: a connect out of range or more than 64 colours");
   c.ncolours = ncol;
   for (Bucket *b : c.buckets) b->colour_begin.assign(ncol + 1, 0);
   for (int64_t e = 0; e < c.nel; e++) c.buckets[el_bucket[e]]->colour_begin[colour[e] + 1]++;

@@ -149,6 +149,10 @@ struct Learned {
   DBuf<double> pr, pe, pz, pw, paw, pg;      // [P][neq] residuals, errors, M r, masked error of M r, A w, dL/dz
   DBuf<double> pscal;                        // [P][2] e^T A e, loss
   DBuf<double> aterm;                        // [P] alpha-gradient terms
+  // base preconditioner the correction is trained on: 0 point Jacobi (alpha D^-1 r), or
+  // GPZ_PRECOND_BLOCK_JACOBI / GPZ_PRECOND_TWO_LEVEL: alpha B^-1 r (+ the coarse part, taken off the targets)
+  int base = 0;
+  DBuf<double> pb, ones;                     // [P][neq] B^-1 r_j; [neq] ones
 };
 
 // ---------------------------------------------------------------- matrix-free operator
@@ -366,6 +370,8 @@ void spmv_device(Ctx &c, const double *x, double *y, double alpha, double beta, 
 int solve(Ctx &c, const gpz_solver_opts &o, gpz_solve_report &rep);
 void spmv32_apply(Ctx &c, int variant, const double *hx, double *hy);
 void precond_apply(Ctx &c, int precond, const double *hr, double *hz);
+void base_block_apply(Ctx &c, const double *r, double *z);   // device vectors: z = B^-1 r (3x3 connect blocks)
+void base_coarse_apply(Ctx &c, const double *r, double *z);  // device vectors: z = P Ac^-1 P^T r (two-level)
 int collect_cg_pairs(Ctx &c, int npairs, double tol, int64_t max_iter, double *R, double *X, double *xstar,
                      int64_t *iters);
 // matfree.cu

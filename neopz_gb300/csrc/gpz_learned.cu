@@ -334,6 +334,15 @@ __global__ void __launch_bounds__(kT) k_ln_apply_z(LnView L, const double *__res
   const double alpha = exp((double)*L.loga);
   for (int64_t i = gthread(); i < L.n; i += nthread()) z[i] = ln_node_z<double>(L, r, alpha, i);
 }
+// z = alpha pb + correction: the preconditioner on a block base (pb = B^-1 r precomputed)
+__global__ void __launch_bounds__(kT) k_ln_apply_zb(LnView L, const double *__restrict__ pb, double *__restrict__ z) {
+  const double alpha = exp((double)*L.loga);
+  for (int64_t i = gthread(); i < L.n; i += nthread()) z[i] = alpha * pb[i] + (double)ln_node_corr(L, i);
+}
+__global__ void __launch_bounds__(kT) k_ln_fill(int64_t n, double v, double *__restrict__ x) {
+  for (int64_t i = gthread(); i < n; i += nthread()) x[i] = v;
+}
+
 // sum_i g_i (r_i / a_ii): the derivative of g^T z w.r.t. alpha, per pair
 __global__ void __launch_bounds__(kT) k_ln_dot3_part(int64_t n, const double *__restrict__ g,
                                                      const double *__restrict__ dinv, const double *__restrict__ r,
@@ -692,6 +701,31 @@ void alloc_pairs(Ctx &c, int P) {
   L.npairs = P;
 }
 
+// Training on a block base: pb_j = B^-1 r_j for every pair, and with the
+// two-level base the coarse part P Ac^-1 P^T r_j taken off the target e_j
+// (the correction is trained for what the base leaves); the pair norms follow
+// the new targets.
+void prepare_base(Ctx &c) {
+  Learned &L = c.ln;
+  if (L.base == 0 || L.npairs == 0) return;
+  const int64_t n = c.neq;
+  L.pb.alloc((size_t)L.npairs * n);
+  L.ones.alloc(n);
+  k_ln_fill<<<grid_t(n), kT, 0, c.stream>>>(n, 1.0, L.ones.p);
+  c.launches++;
+  for (int j = 0; j < L.npairs; j++) {
+    const double *r = L.pr.p + (size_t)j * n;
+    base_block_apply(c, r, L.pb.p + (size_t)j * n);
+    if (L.base == GPZ_PRECOND_TWO_LEVEL) {
+      double *tmp = L.pw.p + (size_t)j * n;  // scratch: overwritten by every loss evaluation
+      base_coarse_apply(c, r, tmp);
+      k_ln_axpy<<<grid_t(n), kT, 0, c.stream>>>(n, -1.0, tmp, L.pe.p + (size_t)j * n, L.pe.p + (size_t)j * n);
+      c.launches++;
+    }
+  }
+  GPZ_CUDA_TRY(cudaGetLastError());
+}
+
 // mean loss over the pairs; with want_grad the parameter gradient lands in ln.grad
 double loss_and_grad(Ctx &c, bool want_grad) {
   Learned &L = c.ln;
@@ -701,7 +735,14 @@ double loss_and_grad(Ctx &c, bool want_grad) {
   for (int j = 0; j < L.npairs; j++) {
     const double *r = L.pr.p + (size_t)j * n;
     double *z = L.pz.p + (size_t)j * n, *w = L.pw.p + (size_t)j * n, *aw = L.paw.p + (size_t)j * n;
-    apply_M(c, r, z);
+    if (L.base) {
+      LnView v = view_of(c);
+      k_ln_apply_t<<<grid_t(L.E * L.R), kT, 0, c.stream>>>(v, r);
+      k_ln_apply_zb<<<grid_t(n), kT, 0, c.stream>>>(v, L.pb.p + (size_t)j * n, z);
+      c.launches += 2;
+    } else {
+      apply_M(c, r, z);
+    }
     k_ln_masked_diff<<<grid_t(n), kT, 0, c.stream>>>(n, L.mask.p, z, L.pe.p + (size_t)j * n, w);
     spmv_device(c, w, aw, 1.0, 0.0, nullptr);
     dot(c, w, aw, L.pscal.p + 2 * j + 1);
@@ -714,7 +755,9 @@ double loss_and_grad(Ctx &c, bool want_grad) {
     backward(c);
     const Offs o = offs_of(L.NS * L.R);
     for (int j = 0; j < L.npairs; j++) {
-      k_ln_dot3_part<<<kRedBlocks, kT, 0, c.stream>>>(n, L.pg.p + (size_t)j * n, c.d_dinv.p, L.pr.p + (size_t)j * n,
+      // d(g^T z)/d(log alpha) = alpha g^T (base r): base r = D^-1 r, or the block base pb
+      k_ln_dot3_part<<<kRedBlocks, kT, 0, c.stream>>>(n, L.pg.p + (size_t)j * n, L.base ? L.ones.p : c.d_dinv.p,
+                                                      L.base ? L.pb.p + (size_t)j * n : L.pr.p + (size_t)j * n,
                                                       L.red.p);
       k_ln_dot_fin<<<1, 32, 0, c.stream>>>(kRedBlocks, L.red.p, L.aterm.p + j);
     }
@@ -908,9 +951,24 @@ int gpz_learned_collect(gpz_ctx *ctx, int npairs, double tol, int64_t max_iter, 
     GPZ_CUDA_TRY(cudaGetLastError());
     gpz::refresh_features(c);
     gpz::scaling(c);
+    gpz::prepare_base(c);
     gpz::pair_norms(c);
     GPZ_CUDA_TRY(cudaStreamSynchronize(c.stream));
     if (cg_iterations) *cg_iterations = its;
+    return GPZ_OK;
+  });
+}
+
+int gpz_learned_set_base(gpz_ctx *ctx, int precond) {
+  return guarded_ln(ctx, [&](Ctx &c) {
+    GPZ_REQUIRE(c.ln.ready, GPZ_E_NOT_READY, "learned preconditioner not initialised");
+    GPZ_REQUIRE(precond == 0 || precond == GPZ_PRECOND_JACOBI || precond == GPZ_PRECOND_BLOCK_JACOBI ||
+                    precond == GPZ_PRECOND_TWO_LEVEL,
+                GPZ_E_INVALID, "base preconditioner");
+    GPZ_REQUIRE(precond <= GPZ_PRECOND_JACOBI || (c.nstate == 3 && !c.flt.active), GPZ_E_INVALID,
+                "a block base needs 3 equations per connect");
+    c.ln.base = precond == GPZ_PRECOND_JACOBI ? 0 : precond;
+    c.ln.npairs = 0;  // pairs are prepared for one base: collect or set them again
     return GPZ_OK;
   });
 }
@@ -928,6 +986,7 @@ int gpz_learned_set_pairs(gpz_ctx *ctx, int npairs, const double *r, const doubl
     GPZ_CUDA_TRY(cudaMemcpyAsync(L.pe.p, e, bytes, cudaMemcpyHostToDevice, c.stream));
     gpz::refresh_features(c);
     gpz::scaling(c);
+    gpz::prepare_base(c);
     gpz::pair_norms(c);
     GPZ_CUDA_TRY(cudaStreamSynchronize(c.stream));
     return GPZ_OK;

@@ -1393,7 +1393,11 @@ __device__ __forceinline__ void tl_locate(const TlView &T, int64_t v, int &I, in
 }
 constexpr int kTlMaxSmem = 3072;  // coarse dofs kept in shared memory by the restriction (>= the largest system)
 
-__global__ void __launch_bounds__(kThreads) k_tl_restrict(const float *__restrict__ r, TlView T, Red R) {
+// rc = P^T r; r64 (optional): after a residual replacement (I_UPDATE 2) the
+// FP64 residual is read instead of r (the learned flexible CG refreshes r
+// only in its z kernel, which runs after this one)
+__global__ void __launch_bounds__(kThreads) k_tl_restrict(const float *__restrict__ r, const double *__restrict__ r64,
+                                                          TlView T, Red R) {
   if (!active(R.iscal)) return;
   __shared__ float sr[kTlMaxSmem];
   for (int64_t k = threadIdx.x; k < T.nc; k += blockDim.x) sr[k] = 0.f;
@@ -1405,7 +1409,9 @@ __global__ void __launch_bounds__(kThreads) k_tl_restrict(const float *__restric
     int I, J, K;
     float t[3];
     tl_locate(T, v, I, J, K, t[0], t[1], t[2]);
-    const float r0 = r[eq], r1 = r[eq + 1], r2 = r[eq + 2];
+    const bool fresh = r64 && R.iscal[I_UPDATE] == 2;
+    const float r0 = fresh ? (float)r64[eq] : r[eq], r1 = fresh ? (float)r64[eq + 1] : r[eq + 1],
+                r2 = fresh ? (float)r64[eq + 2] : r[eq + 2];
 #pragma unroll
     for (int cn = 0; cn < 8; cn++) {
       const int bx = cn & 1, by = (cn >> 1) & 1, bz = cn >> 2;
@@ -2003,7 +2009,8 @@ __global__ void __launch_bounds__(kThreads) k_lfb_z3(LnView L, const int64_t *__
                                                      const int32_t *__restrict__ bsize, int64_t nconn,
                                                      const double *__restrict__ r64, float *__restrict__ r32,
                                                      const float *__restrict__ q32, int qpad, float *__restrict__ z32,
-                                                     Red R) {
+                                                     const float *__restrict__ bjinv32, TlView T,
+                                                     float *__restrict__ zb, Red R) {
   if (!active(R.iscal)) return;
   const bool first = R.iscal[I_IT] == 0;
   const bool fresh = R.iscal[I_UPDATE] == 2;
@@ -2012,6 +2019,39 @@ __global__ void __launch_bounds__(kThreads) k_lfb_z3(LnView L, const int64_t *__
   for (int64_t cn = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; cn < nconn; cn += (int64_t)gridDim.x * blockDim.x) {
     if (bsize[cn] != 3) continue;
     const int64_t eq0 = bpos[cn];
+    // the base preconditioner of this connect: point Jacobi, or its 3x3 block plus the coarse correction
+    float rv[3], bz[3] = {0.f, 0.f, 0.f};
+#pragma unroll
+    for (int j = 0; j < 3; j++) {
+      rv[j] = fresh ? (float)r64[eq0 + j] : r32[eq0 + j];
+      if (fresh) r32[eq0 + j] = rv[j];
+    }
+    if (bjinv32) {
+      const float *Bk = bjinv32 + 9 * (eq0 / 3);
+#pragma unroll
+      for (int j = 0; j < 3; j++) bz[j] = fmaf(Bk[3 * j], rv[0], fmaf(Bk[3 * j + 1], rv[1], Bk[3 * j + 2] * rv[2]));
+    } else {
+#pragma unroll
+      for (int j = 0; j < 3; j++) bz[j] = L.dinv32[eq0 + j] * rv[j];
+    }
+    float cz[3] = {0.f, 0.f, 0.f};
+    if (T.zc) {
+      const int32_t v = T.brow_vtx[eq0 / 3];
+      if (v >= 0) {
+        int I, J, K;
+        float t[3];
+        tl_locate(T, v, I, J, K, t[0], t[1], t[2]);
+#pragma unroll
+        for (int c8 = 0; c8 < 8; c8++) {
+          const int bx = c8 & 1, by = (c8 >> 1) & 1, bz8 = c8 >> 2;
+          const float w = (bx ? t[0] : 1.f - t[0]) * (by ? t[1] : 1.f - t[1]) * (bz8 ? t[2] : 1.f - t[2]);
+          if (w == 0.f) continue;
+          const int64_t nd = (I + bx) + (int64_t)(T.mx + 1) * ((J + by) + (int64_t)(T.my + 1) * (K + bz8));
+#pragma unroll
+          for (int j = 0; j < 3; j++) cz[j] = fmaf(w, __ldcg(&T.zc[3 * nd + j]), cz[j]);
+        }
+      }
+    }
     const int64_t c0 = ce_ptr[cn], m = ce_ptr[cn + 1] - c0;
     const int64_t p0 = L.ne_ptr[eq0], p1 = L.ne_ptr[eq0 + 1], p2 = L.ne_ptr[eq0 + 2];
     float a[3] = {0.f, 0.f, 0.f};
@@ -2031,17 +2071,11 @@ __global__ void __launch_bounds__(kThreads) k_lfb_z3(LnView L, const int64_t *__
 #pragma unroll
     for (int j = 0; j < 3; j++) {
       const int64_t i = eq0 + j;
-      float ri;
-      if (fresh) {
-        ri = (float)r64[i];
-        r32[i] = ri;
-      } else {
-        ri = r32[i];
-      }
-      const float di = L.dinv32[i];
-      const float zi = fmaf(alpha * di, ri, L.mdsq[i] * a[j]);
-      const float ji = di * ri;
+      const float ri = rv[j];
+      const float zi = fmaf(alpha, bz[j], L.mdsq[i] * a[j]) + cz[j];
+      const float ji = bz[j] + cz[j];  // the base alone: the fallback direction
       z32[i] = zi;
+      if (zb) zb[i] = ji;
       zr.add(zi * ri);
       jr.add(ji * ri);
       if (!first) {
@@ -2062,17 +2096,23 @@ __global__ void __launch_bounds__(kThreads) k_lfb_z3(LnView L, const int64_t *__
     s[S_BETA] = first ? 0.0 : -(ok ? tot[1] : tot[3]) / s[S_PQ];
     if (is[I_UPDATE] == 2) is[I_UPDATE] = 0;
   }
+  if (T.zc)  // the coarse residual starts from zero at the next application
+    for (int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < T.nc; k += (int64_t)gridDim.x * blockDim.x)
+      T.rc[k] = 0.f;
 }
 
+// p = z + beta p; in an iteration that fell back (I_RESTART) z is the base preconditioner's alone:
+// zb when given, else the point Jacobi D^-1 r
 __global__ void __launch_bounds__(kThreads) k_lfb_p(const float *__restrict__ z32, const float *__restrict__ r32,
-                                                    const float *__restrict__ dinv32, float *__restrict__ p32,
-                                                    float *__restrict__ q32, int qpad, int qzero, int64_t n, Red R) {
+                                                    const float *__restrict__ dinv32, const float *__restrict__ zb,
+                                                    float *__restrict__ p32, float *__restrict__ q32, int qpad,
+                                                    int qzero, int64_t n, Red R) {
   if (!active(R.iscal)) return;
   const bool jac = R.iscal[I_RESTART] != 0;
   const bool first = R.iscal[I_IT] == 0;
   const float beta = (float)R.scal[S_BETA];
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
-    const float zi = jac ? dinv32[i] * r32[i] : z32[i];
+    const float zi = jac ? (zb ? zb[i] : dinv32[i] * r32[i]) : z32[i];
     const int64_t k = pidx(i, 1);
     p32[k] = first ? zi : fmaf(beta, p32[k], zi);
     if (qzero) q32[pidx(i, qpad)] = 0.f;
@@ -2609,7 +2649,7 @@ void launch_tl_apply(Ctx &c, const Plan &P, Red R, cudaStream_t s) {
   int dev = 0, nsm = 0;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
-  k_tl_restrict<<<std::max(1, 2 * nsm), kThreads, 0, s>>>(w.r32.p, P.T, R);
+  k_tl_restrict<<<std::max(1, 2 * nsm), kThreads, 0, s>>>(w.r32.p, nullptr, P.T, R);
   k_tl_csolve<<<wave(k_tl_csolve), kThreads, 0, s>>>(P.T, R);
   k_tl_z<<<wave(k_tl_z), kThreads, 0, s>>>(w.r32.p, P.M32, P.T, P.nunits, R);
   c.launches += 4;
@@ -2862,11 +2902,51 @@ int solve_learned(Ctx &c, const gpz_solver_opts &o, gpz_solve_report &rep, bool 
   bool by_connect = blk && c.ln.R == 8;
   for (int64_t cn = 0; cn < c.nconnects && by_connect; cn++)
     by_connect = c.h_block_size[cn] == 0 || c.h_block_size[cn] == 3;
+  // base preconditioner under the learned correction: point Jacobi (precond 0 / JACOBI), the 3x3 connect
+  // blocks (BLOCK_JACOBI) or the two-level block Jacobi (TWO_LEVEL); the blocks need the connect-wise kernel
+  GPZ_REQUIRE(o.precond == 0 || o.precond == GPZ_PRECOND_JACOBI || o.precond == GPZ_PRECOND_BLOCK_JACOBI ||
+                  o.precond == GPZ_PRECOND_TWO_LEVEL,
+              GPZ_E_INVALID, "learned flexible CG: base preconditioner not available");
+  const bool lblock = o.precond == GPZ_PRECOND_BLOCK_JACOBI || o.precond == GPZ_PRECOND_TWO_LEVEL;
+  const bool ltl = o.precond == GPZ_PRECOND_TWO_LEVEL;
+  GPZ_REQUIRE(!lblock || by_connect, GPZ_E_INVALID,
+              "learned flexible CG with a block base: needs the FP32 3x3-block operator (3 equations per connect) "
+              "and rank 8");
+  if (ltl && !c.tl.ready)
+    GPZ_REQUIRE(two_level_build(c) == GPZ_OK, GPZ_E_INVALID,
+                "two-level base: needs one uniform grid of axis-aligned Q2 hex elasticity elements");
+  if (ltl && !c.tl.have_inv) two_level_assemble(c);
+  if (lblock) {
+    if (!c.have_bjinv) build_block_jacobi(c);
+    c.d_bjinv32.alloc((size_t)(c.neq / 3) * 9);
+    k_to_f32<<<wave(k_to_f32), kThreads, 0, s>>>(c.d_bjinv.p, c.d_bjinv32.p, (int64_t)(c.neq / 3) * 9);
+    c.launches++;
+  }
+  TlView TV{};
+  float *zb = nullptr;
+  if (ltl) {
+    TwoLevel &T = c.tl;
+    TV = TlView{T.vtx_eq.p, T.brow_vtx.p, T.cfix.p, T.acinv32.p, T.rc.p, T.zc.p, T.z32.p, (int)T.lx[0] + 1,
+                (int)T.lx[1] + 1, (int)T.lx[2] + 1, T.s, T.m[0], T.m[1], T.m[2], T.nc};
+    T.rc.zero(s);
+    zb = T.z32.p;
+  }
+  int nsm = 0;
+  {
+    int dev = 0;
+    GPZ_CUDA_TRY(cudaGetDevice(&dev));
+    GPZ_CUDA_TRY(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
+  }
   auto apply_z32 = [&]() {
+    if (ltl) {  // the coarse correction of the current residual first
+      k_tl_restrict<<<std::max(1, 2 * nsm), kThreads, 0, s>>>(w.r32.p, w.r.p, TV, R);
+      k_tl_csolve<<<wave(k_tl_csolve), kThreads, 0, s>>>(TV, R);
+      c.launches += 2;
+    }
     if (by_connect)
       k_lfb_z3<<<wave(k_lfb_z3), kThreads, 0, s>>>(L, c.ln.ce_ptr.p, c.ln.ce_idx.p, c.d_block_pos.p,
                                                    c.d_block_size.p, c.nconnects, w.r.p, w.r32.p, w.q32.p, qpad,
-                                                   w.z32.p, R);
+                                                   w.z32.p, lblock ? c.d_bjinv32.p : nullptr, TV, zb, R);
     else
       k_lfb_z<<<wave(k_lfb_z), kThreads, 0, s>>>(L, w.r.p, w.r32.p, w.q32.p, qpad, w.z32.p, R);
     c.launches++;
@@ -2880,8 +2960,8 @@ int solve_learned(Ctx &c, const gpz_solver_opts &o, gpz_solve_report &rep, bool 
                                                                                     w.x.p, w.b.p, w.r.p, c.neq, R)));
       k_fcg_t<<<wave(k_fcg_t), kThreads, 0, s>>>(L, w.r.p, w.r32.p, R);
       apply_z32();
-      k_lfb_p<<<wave(k_lfb_p), kThreads, 0, s>>>(w.z32.p, w.r32.p, L.dinv32, w.pm.p, w.q32.p, qpad, qpad, c.neq,
-                                                 R);
+      k_lfb_p<<<wave(k_lfb_p), kThreads, 0, s>>>(w.z32.p, w.r32.p, L.dinv32, zb, w.pm.p, w.q32.p, qpad, qpad,
+                                                 c.neq, R);
       c.launches += 5;
       return;
     }
@@ -2923,8 +3003,8 @@ int solve_learned(Ctx &c, const gpz_solver_opts &o, gpz_solve_report &rep, bool 
     k_fcg_t<<<wave(k_fcg_t), kThreads, 0, s>>>(L, w.r.p, w.r32.p, R);  // k_cg_init leaves I_UPDATE = 2: FP64 r
     if (blk) {
       apply_z32();
-      k_lfb_p<<<wave(k_lfb_p), kThreads, 0, s>>>(w.z32.p, w.r32.p, L.dinv32, w.pm.p, w.q32.p, qpad, qpad, c.neq,
-                                                 R);
+      k_lfb_p<<<wave(k_lfb_p), kThreads, 0, s>>>(w.z32.p, w.r32.p, L.dinv32, zb, w.pm.p, w.q32.p, qpad, qpad,
+                                                 c.neq, R);
       c.launches -= 1;
     } else {
       k_fcg_z<<<wave(k_fcg_z), kThreads, 0, s>>>(L, w.r.p, w.q.p, c.d_dinv.p, w.z.p, R);
@@ -3316,6 +3396,63 @@ int solve(Ctx &c, const gpz_solver_opts &o, gpz_solve_report &rep) {
   if (hstate[I_BREAK]) return GPZ_E_BREAKDOWN;
   if (cancelled && hstate[I_CONV] == 0) return GPZ_CANCELLED;
   return hstate[I_CONV] == 1 ? GPZ_OK : GPZ_NOT_CONVERGED;
+}
+
+// Base pieces for training the learned correction on a block base (device
+// vectors, FP64 out): z = B^-1 r over the 3x3 connect blocks, and the coarse
+// part P Ac^-1 P^T r of the two-level preconditioner (FP32 inside).
+void base_block_apply(Ctx &c, const double *r, double *z) {
+  if (!c.have_bjinv) build_block_jacobi(c);
+  const Prec M{c.d_dinv.p, c.d_bjinv.p, 1};
+  k_prec_apply<<<wave(k_prec_apply), kThreads, 0, c.stream>>>(r, M, c.neq / 3, z);
+  c.launches++;
+}
+
+__global__ void __launch_bounds__(kThreads) k_tl_coarse_only(TlView T, int64_t nunits, double *__restrict__ z) {
+  for (int64_t u = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; u < nunits; u += (int64_t)gridDim.x * blockDim.x) {
+    float cz[3] = {0.f, 0.f, 0.f};
+    const int32_t v = T.brow_vtx[u];
+    if (v >= 0) {
+      int I, J, K;
+      float t[3];
+      tl_locate(T, v, I, J, K, t[0], t[1], t[2]);
+      for (int c8 = 0; c8 < 8; c8++) {
+        const int bx = c8 & 1, by = (c8 >> 1) & 1, bz = c8 >> 2;
+        const float w = (bx ? t[0] : 1.f - t[0]) * (by ? t[1] : 1.f - t[1]) * (bz ? t[2] : 1.f - t[2]);
+        if (w == 0.f) continue;
+        const int64_t nd = (I + bx) + (int64_t)(T.mx + 1) * ((J + by) + (int64_t)(T.my + 1) * (K + bz));
+        for (int j = 0; j < 3; j++) cz[j] = fmaf(w, __ldcg(&T.zc[3 * nd + j]), cz[j]);
+      }
+    }
+    for (int j = 0; j < 3; j++) z[3 * u + j] = cz[j];
+  }
+  for (int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < T.nc; k += (int64_t)gridDim.x * blockDim.x)
+    T.rc[k] = 0.f;
+}
+
+void base_coarse_apply(Ctx &c, const double *r, double *z) {
+  GPZ_REQUIRE(c.tl.ready || two_level_build(c) == GPZ_OK, GPZ_E_INVALID,
+              "two-level base: needs one uniform grid of axis-aligned Q2 hex elasticity elements");
+  if (!c.tl.have_inv) two_level_assemble(c);
+  alloc_work(c, true);
+  SolverWork &w = c.sw;
+  TwoLevel &T = c.tl;
+  const TlView TV{T.vtx_eq.p, T.brow_vtx.p, T.cfix.p, T.acinv32.p, T.rc.p, T.zc.p, T.z32.p, (int)T.lx[0] + 1,
+                  (int)T.lx[1] + 1, (int)T.lx[2] + 1, T.s, T.m[0], T.m[1], T.m[2], T.nc};
+  int64_t hi[I_NISCAL] = {0};
+  hi[I_MAXIT] = 1;
+  hi[I_UPDATE] = 2;  // the restriction reads the FP64 residual
+  GPZ_CUDA_TRY(cudaMemcpyAsync(w.iscal.p, hi, sizeof(hi), cudaMemcpyHostToDevice, c.stream));
+  T.rc.zero(c.stream);
+  int dev = 0, nsm = 0;
+  GPZ_CUDA_TRY(cudaGetDevice(&dev));
+  GPZ_CUDA_TRY(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
+  const Red R = red_of(c);
+  k_tl_restrict<<<std::max(1, 2 * nsm), kThreads, 0, c.stream>>>(w.r32.p, r, TV, R);
+  k_tl_csolve<<<wave(k_tl_csolve), kThreads, 0, c.stream>>>(TV, R);
+  k_tl_coarse_only<<<wave(k_tl_coarse_only), kThreads, 0, c.stream>>>(TV, c.neq / 3, z);
+  c.launches += 3;
+  GPZ_CUDA_TRY(cudaGetLastError());
 }
 
 // z = M r for a CG preconditioner of the assembled system (host FP64 vectors):

@@ -94,6 +94,7 @@ def lib():
         L.gpz_two_level_config.argtypes = [vp, i32]
         L.gpz_two_level_info.argtypes = [vp, vp]
         L.gpz_precond_apply.argtypes = [vp, i32, vp, vp]
+        L.gpz_learned_set_base.argtypes = [vp, i32]
         L.gpz_get_error_string.restype = ctypes.c_char_p
         L.gpz_get_error_string.argtypes = [i32]
         L.gpz_last_error_detail.restype = ctypes.c_char_p
@@ -114,6 +115,7 @@ def lib():
         L.gpz_equation_filter.argtypes = [vp, i64, vp]
         L.gpz_sloan_resequence.argtypes = [i64, i64, vp, vp, vp, vp]
         L.gpz_nodeset_blocks.argtypes = [i64, i64, vp, vp, vp, vp, i64, vp, vp, _P(i64), vp, _P(i32), vp, vp]
+        L.gpz_element_colours.argtypes = [i64, vp, vp, i64, vp, vp, _P(i32)]
         L.gpz_matrix_download.argtypes = [vp, vp]
         L.gpz_rhs_download.argtypes = [vp, vp]
         L.gpz_rhs_upload.argtypes = [vp, vp]
@@ -458,6 +460,9 @@ class Context:
         p = np.ascontiguousarray(p, np.float32)
         self._check(lib().gpz_learned_set_params(self.h, _p(p), len(p)))
 
+    def learned_set_base(self, precond):
+        self._check(lib().gpz_learned_set_base(self.h, int(precond)))
+
     def learned_collect(self, npairs=16, tol=1e-12, max_iter=200000):
         its = ctypes.c_int64()
         self._check(lib().gpz_learned_collect(self.h, npairs, tol, max_iter, ctypes.byref(its)))
@@ -534,6 +539,20 @@ def sloan_resequence(nnodes, elgraphindex, elgraph):
     if rc != GPZ_OK:
         raise GpzError(rc, lib().gpz_get_error_string(rc).decode())
     return g, s
+
+
+def element_colours(elgraphindex, elgraph, block_size):
+    """The element colouring of the atomic-free scatter (gpz_element_colours): (colours [nel], ncolours)."""
+    ei = np.ascontiguousarray(elgraphindex, np.int64)
+    eg = np.ascontiguousarray(elgraph, np.int64)
+    bs = np.ascontiguousarray(block_size, np.int64)
+    nel = len(ei) - 1
+    col = np.zeros(max(nel, 1), np.int32)
+    nc = ctypes.c_int32(0)
+    rc = lib().gpz_element_colours(nel, _p(ei), _p(eg), len(bs), _p(bs), _p(col), ctypes.byref(nc))
+    if rc != 0:
+        raise GpzError(rc, lib().gpz_get_error_string(rc).decode())
+    return col[:nel], nc.value
 
 
 def nodeset_blocks(nnodes, elgraphindex, elgraph, block_pos, block_size, neq):

@@ -53,18 +53,24 @@ def context_for(grid, rank=4, seed=0, params=None):
     return ctx
 
 
-def validate(ctx, grid, coef_of_seed, seeds, tol=1e-8):
-    """Learned flexible-CG iterations summed over validation fields."""
+def validate(ctx, grid, coef_of_seed, seeds, tol=1e-8, base=gpz.GPZ_PRECOND_JACOBI):
+    """Learned flexible-CG iterations summed over validation fields: the FP64 solver on the Jacobi base, the
+    mixed one (FP32 operator) on a block base, which only it applies."""
     its = 0
     for s in seeds:
         ctx.set_coef(grid, coef_of_seed(s))
-        ctx.assemble()
-        its += ctx.solve(solver=gpz.GPZ_SOLVER_LEARNED_FCG, tol=tol, want_x=False)["iterations"]
+        if base == gpz.GPZ_PRECOND_JACOBI:
+            ctx.assemble()
+            its += ctx.solve(solver=gpz.GPZ_SOLVER_LEARNED_FCG, tol=tol, want_x=False)["iterations"]
+        else:
+            ctx.assemble(gpz.GPZ_PREC_MIXED)
+            its += ctx.solve(solver=gpz.GPZ_SOLVER_LEARNED_MIXED_FCG, precond=base, tol=tol, reliable_delta=1e-2,
+                             want_x=False)["iterations"]
     return its
 
 
 def train(ctx, grid, coef_of_seed, seeds, steps=8, lr=3e-3, npairs=16, tol=1e-12, log_every=0, lr_final=None,
-          val_seeds=(20000, 20001), val_every=50):
+          val_seeds=(20000, 20001), val_every=50, base=gpz.GPZ_PRECOND_JACOBI):
     """Online training over the fields of `seeds` (learning rate decayed from lr to lr_final on a cosine).
 
     The energy-norm loss flattens early while the parameters can keep drifting in directions that
@@ -78,9 +84,10 @@ def train(ctx, grid, coef_of_seed, seeds, steps=8, lr=3e-3, npairs=16, tol=1e-12
     first = last = None
     history = []
     best = None
+    ctx.learned_set_base(base)
     for i, s in enumerate(seeds):
         ctx.set_coef(grid, coef_of_seed(s))
-        ctx.assemble()
+        ctx.assemble(gpz.GPZ_PREC_FP64 if base == gpz.GPZ_PRECOND_JACOBI else gpz.GPZ_PREC_MIXED)
         ctx.learned_collect(npairs=npairs, tol=tol)
         li = lr_final + (lr - lr_final) * 0.5 * (1 + math.cos(math.pi * i / max(1, len(seeds) - 1)))
         l0, l1 = ctx.learned_train(steps=steps, lr=li)
@@ -88,7 +95,7 @@ def train(ctx, grid, coef_of_seed, seeds, steps=8, lr=3e-3, npairs=16, tol=1e-12
         last = l1
         done = i + 1
         if val_seeds and (done % val_every == 0 or done == len(seeds)):
-            its = validate(ctx, grid, coef_of_seed, val_seeds)
+            its = validate(ctx, grid, coef_of_seed, val_seeds, base=base)
             history.append({"fields": done, "validation_iterations": its, "loss": l1})
             if best is None or its < best[0]:
                 best = (its, ctx.learned_params(), done)
@@ -125,6 +132,23 @@ def evaluate(ctx, grid, coef_of_seed, seeds, tol=1e-8, precond=gpz.GPZ_PRECOND_J
     return out
 
 
+def evaluate_mixed(ctx, grid, coef_of_seed, seeds, base, tol=1e-8):
+    """The mixed CG on `base` against the learned + mixed flexible CG on the same base (the method without the
+    network against the method with it), same FP32 operator, same true FP64 residual."""
+    out = []
+    for s in seeds:
+        ctx.set_coef(grid, coef_of_seed(s))
+        ctx.assemble(gpz.GPZ_PREC_MIXED)
+        kw = dict(tol=tol, reliable_delta=1e-2, want_x=False)
+        for _ in range(2):  # the second of each is timed (graphs instantiated, caches warm)
+            b = ctx.solve(solver=gpz.GPZ_SOLVER_MIXED_CG, precond=base, **kw)
+            m = ctx.solve(solver=gpz.GPZ_SOLVER_LEARNED_MIXED_FCG, precond=base, **kw)
+        out.append(dict(seed=s, base_iterations=b["iterations"], base_seconds=b["seconds"],
+                        learned_iterations=m["iterations"], learned_seconds=m["seconds"],
+                        learned_true_resid=m["true_resid"], fallbacks=m["restarts"], rc=m["rc"]))
+    return out
+
+
 def main(argv=None):
     ap = argparse.ArgumentParser(description=__doc__.split("\n\n")[0])
     ap.add_argument("--workload", choices=sorted(WORKLOADS), default="darcy2d")
@@ -141,27 +165,35 @@ def main(argv=None):
     ap.add_argument("--block", action="store_true", help="also evaluate against block-Jacobi PCG")
     ap.add_argument("--val-every", type=int, default=50, help="validation (checkpoint selection) interval in fields")
     ap.add_argument("--weights", default="", help="start from these parameters (with --fields 0: evaluate only)")
+    ap.add_argument("--base", choices=["jacobi", "block", "two_level"], default="jacobi",
+                    help="base preconditioner under the correction (block bases: the mixed solver, elasticity)")
     ap.add_argument("--out", default="")
     a = ap.parse_args(argv)
     grid, coef = WORKLOADS[a.workload](a.n, a.p)
     ctx = context_for(grid, a.rank, a.init_seed, np.load(a.weights) if a.weights else None)
     first = last = None
     secs, hist = 0.0, []
+    base = {"jacobi": gpz.GPZ_PRECOND_JACOBI, "block": gpz.GPZ_PRECOND_BLOCK_JACOBI,
+            "two_level": gpz.GPZ_PRECOND_TWO_LEVEL}[a.base]
     if a.fields > 0:
         first, last, secs, hist = train(ctx, grid, coef, range(1, a.fields + 1), a.steps, a.lr, a.pairs,
-                                        log_every=max(1, a.fields // 10), val_every=a.val_every)
+                                        log_every=max(1, a.fields // 10), val_every=a.val_every, base=base)
     params = ctx.learned_params()
     if a.out:
         os.makedirs(os.path.dirname(os.path.abspath(a.out)), exist_ok=True)
         np.save(a.out, params)
     res = dict(workload=a.workload, n=a.n, p=a.p, fields=a.fields, steps=a.steps, lr=a.lr, pairs=a.pairs,
-               rank=a.rank, loss_first=first, loss_last=last, train_seconds=round(secs, 1), validation=hist)
+               rank=a.rank, base=a.base, loss_first=first, loss_last=last, train_seconds=round(secs, 1),
+               validation=hist)
     if a.eval:
         if a.eval_n and a.eval_n != a.n:
             ctx.close()
             grid, coef = WORKLOADS[a.workload](a.eval_n, a.p)
             ctx = context_for(grid, a.rank, a.init_seed, params)
-        res["eval"] = evaluate(ctx, grid, coef, range(10000, 10000 + a.eval))
+        if base == gpz.GPZ_PRECOND_JACOBI:
+            res["eval"] = evaluate(ctx, grid, coef, range(10000, 10000 + a.eval))
+        else:
+            res["eval"] = evaluate_mixed(ctx, grid, coef, range(10000, 10000 + a.eval), base)
         if a.block:
             res["eval_block"] = evaluate(ctx, grid, coef, range(10000, 10000 + a.eval),
                                          precond=gpz.GPZ_PRECOND_BLOCK_JACOBI)

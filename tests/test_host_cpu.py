@@ -321,3 +321,33 @@ def test_cxx_program_uses_the_c_abi(g, tmp_path):
     assert out[0] == "nodeset 0 3 1 0 2 1"
     assert out[1].startswith("sloan 0 ") and sorted(map(int, out[1].split()[2:])) == [0, 1, 2]
     assert out[2] == ("context 0" if torch.cuda.is_available() else "context -8")  # -8: GPZ_E_NO_DEVICE
+
+
+@pytest.mark.parametrize("case", ["poisson2d_q2", "elast3d_q2", "elast3d_hp", "darcy2d_q3"])
+def test_element_colouring_invariant(g, case):
+    """The colouring of the atomic-free scatter (gpz_element_colours, what gpz_mesh_upload colours the buckets
+    with): no two elements of one colour share a non-empty connect -- so one colour's elements write disjoint
+    rows and CSR slots -- and every colour below the count is used.  A uniform grid needs the 2^d colours of its
+    cell parities (4 for quads, 8 for hexes, boundary elements included)."""
+    if case == "poisson2d_q2":
+        grid, want = g.poisson2d(12, 2), 4
+    elif case == "elast3d_q2":
+        grid, want = g.elasticity3d(6, 2), 8
+    elif case == "elast3d_hp":
+        grid, want = g.elasticity3d_hp(5, g.hp_orders(125, 3)), 8
+    else:
+        grid, want = g.darcy(2, 9, 3, g.lognormal(81, 1.0, 2)), 4
+    ei, eg = grid.element_graph()
+    nn, bp, bs = _blocks_of(grid)
+    col, nc = g.element_colours(ei, eg, bs)
+    assert nc == want and set(col.tolist()) == set(range(nc))
+    owner = {}
+    for e in range(len(ei) - 1):
+        for cn in eg[ei[e]:ei[e + 1]]:
+            if bs[cn] == 0:
+                continue
+            key = (int(cn), int(col[e]))
+            assert key not in owner, f"elements {owner.get(key)} and {e} share connect {cn} in colour {col[e]}"
+            owner[key] = e
+    with pytest.raises(g.GpzError):
+        g.element_colours(ei, np.where(eg == eg[0], nn, eg), bs)  # a connect out of range
