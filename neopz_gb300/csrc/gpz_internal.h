@@ -204,7 +204,7 @@ struct TwoLevel {
   DBuf<int32_t> cell_off, cell_el, el_sub;   // volume elements grouped by coarse box; sub position
   DBuf<double> tsub;                         // [s^3][24][24] P^T Khat_vv P for mu = 1
   DBuf<int32_t> cfix;                        // [nnode] 1: removed (touches a penalty equation)
-  DBuf<double> ac, piv;                      // [nc][nc] coarse matrix, then its inverse; pivot row / column
+  DBuf<double> ac;                           // [nc][nc] coarse matrix, then its inverse
   DBuf<float> acinv32;                       // [nc][nc]
   DBuf<float> rc, zc, z32;                   // coarse residual / correction, preconditioned residual
 };

@@ -1407,28 +1407,107 @@ __global__ void k_tl_fixrows(int64_t nc, const int32_t *__restrict__ cfix, doubl
   if (cfix[i / 3] || cfix[j / 3]) ac[t] = i == j ? 1.0 : 0.0;
 }
 
-// in-place Gauss-Jordan inversion of the SPD coarse matrix, no pivoting: step k
-// in two launches, the pivot row and column saved first
-__global__ void k_tl_gj_save(int64_t n, int64_t k, const double *__restrict__ A, double *__restrict__ piv) {
-  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (t < n) piv[t] = A[k * n + t];
-  else if (t < 2 * n) piv[t] = A[(t - n) * n + k];
+// Blocked in-place Gauss-Jordan inversion of the SPD coarse matrix (no
+// pivoting), FP64, pivot blocks of kGjB rows.  With A = [[D, R], [C, E]] for
+// the current pivot block D: D <- P = D^-1 (k_gj_diag), R <- P R (k_gj_row),
+// E <- E - C (P R) (k_gj_trail, with the original C), C <- -C P (k_gj_col).
+constexpr int kGjB = 32;
+
+// P = D^-1 of the pivot block, Gauss-Jordan in shared memory by one CTA
+__global__ void __launch_bounds__(256) k_gj_diag(int64_t n, int64_t k0, double *__restrict__ A,
+                                                 int *__restrict__ err) {
+  __shared__ double D[kGjB][kGjB + 1];
+  const int b = (int)min((int64_t)kGjB, n - k0);
+  for (int t = threadIdx.x; t < b * b; t += blockDim.x) D[t / b][t % b] = A[(k0 + t / b) * n + k0 + t % b];
+  __syncthreads();
+  for (int k = 0; k < b; k++) {
+    const double piv = D[k][k];
+    if (threadIdx.x == 0 && !(piv > 0.0)) atomicOr(err, 1 << 18);
+    const double ip = 1.0 / piv;
+    __syncthreads();
+    if (threadIdx.x < b) D[k][threadIdx.x] = (threadIdx.x == k ? 1.0 : D[k][threadIdx.x]) * ip;
+    __syncthreads();
+    for (int t = threadIdx.x; t < b * b; t += blockDim.x) {
+      const int i = t / b, j = t % b;
+      if (i == k) continue;
+      const double f = D[i][k];
+      // every thread reads D[i][k] before any writes it: the column k entries are written last, below
+      if (j != k) D[i][j] -= f * D[k][j];
+    }
+    __syncthreads();
+    for (int i = threadIdx.x; i < b; i += blockDim.x)
+      if (i != k) D[i][k] = -D[i][k] * D[k][k];
+    __syncthreads();
+  }
+  for (int t = threadIdx.x; t < b * b; t += blockDim.x) A[(k0 + t / b) * n + k0 + t % b] = D[t / b][t % b];
 }
-__global__ void k_tl_gj_step(int64_t n, int64_t k, double *__restrict__ A, const double *__restrict__ piv,
-                             int *__restrict__ err) {
-  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= n * n) return;
-  const int64_t i = t / n, j = t % n;
-  const double p = piv[k];
-  if (t == 0 && !(p > 0.0)) atomicOr(err, 1 << 18);
-  const double ip = 1.0 / p;
-  double v;
-  if (i == k && j == k) v = ip;
-  else if (i == k) v = piv[j] * ip;
-  else if (j == k) v = -piv[n + i] * ip;
-  else v = A[t] - piv[n + i] * piv[j] * ip;
-  A[t] = v;
+
+// R <- P R: row panel (rows k0.., the columns outside the block), one thread per column
+__global__ void __launch_bounds__(256) k_gj_row(int64_t n, int64_t k0, double *__restrict__ A) {
+  __shared__ double P[kGjB][kGjB];
+  const int b = (int)min((int64_t)kGjB, n - k0);
+  for (int t = threadIdx.x; t < b * b; t += blockDim.x) P[t / b][t % b] = A[(k0 + t / b) * n + k0 + t % b];
+  __syncthreads();
+  const int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= n || (j >= k0 && j < k0 + b)) return;
+  double r[kGjB];
+  for (int t = 0; t < b; t++) r[t] = A[(k0 + t) * n + j];
+  for (int i = 0; i < b; i++) {
+    double acc = 0.0;
+    for (int t = 0; t < b; t++) acc += P[i][t] * r[t];
+    A[(k0 + i) * n + j] = acc;
+  }
 }
+
+// E <- E - C R' over 64 x 64 tiles of the matrix outside the pivot rows and columns (R' = the updated
+// row panel, C = the column panel not updated yet); each thread a 4 x 4 sub-tile
+__global__ void __launch_bounds__(256) k_gj_trail(int64_t n, int64_t k0, double *__restrict__ A) {
+  __shared__ double Cs[64][kGjB + 1], Rs[kGjB][64 + 1];
+  const int b = (int)min((int64_t)kGjB, n - k0);
+  const int64_t i0 = (int64_t)blockIdx.y * 64, j0 = (int64_t)blockIdx.x * 64;
+  for (int t = threadIdx.x; t < 64 * kGjB; t += blockDim.x) {
+    const int r = t / kGjB, c = t % kGjB;
+    Cs[r][c] = (i0 + r < n && c < b) ? A[(i0 + r) * n + k0 + c] : 0.0;
+  }
+  for (int t = threadIdx.x; t < kGjB * 64; t += blockDim.x) {
+    const int r = t / 64, c = t % 64;
+    Rs[r][c] = (r < b && j0 + c < n) ? A[(k0 + r) * n + j0 + c] : 0.0;
+  }
+  __syncthreads();
+  const int ti = (threadIdx.x / 16) * 4, tj = (threadIdx.x % 16) * 4;
+  double acc[4][4] = {};
+  for (int t = 0; t < b; t++)
+#pragma unroll
+    for (int u = 0; u < 4; u++)
+#pragma unroll
+      for (int v = 0; v < 4; v++) acc[u][v] += Cs[ti + u][t] * Rs[t][tj + v];
+#pragma unroll
+  for (int u = 0; u < 4; u++)
+#pragma unroll
+    for (int v = 0; v < 4; v++) {
+      const int64_t i = i0 + ti + u, j = j0 + tj + v;
+      if (i >= n || j >= n || (i >= k0 && i < k0 + b) || (j >= k0 && j < k0 + b)) continue;
+      A[i * n + j] -= acc[u][v];
+    }
+}
+
+// C <- -C P: column panel (rows outside the block, columns k0..), one thread per row
+__global__ void __launch_bounds__(256) k_gj_col(int64_t n, int64_t k0, double *__restrict__ A) {
+  __shared__ double P[kGjB][kGjB];
+  const int b = (int)min((int64_t)kGjB, n - k0);
+  for (int t = threadIdx.x; t < b * b; t += blockDim.x) P[t / b][t % b] = A[(k0 + t / b) * n + k0 + t % b];
+  __syncthreads();
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n || (i >= k0 && i < k0 + b)) return;
+  double c[kGjB];
+  for (int t = 0; t < b; t++) c[t] = A[i * n + k0 + t];
+  for (int j = 0; j < b; j++) {
+    double acc = 0.0;
+    for (int t = 0; t < b; t++) acc += c[t] * P[t][j];
+    A[i * n + k0 + j] = -acc;
+  }
+}
+
 __global__ void k_tl_to32(int64_t n, const double *__restrict__ A, float *__restrict__ B) {
   const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= n * n) return;
@@ -1816,7 +1895,6 @@ int two_level_build(Ctx &c) {
   T.tsub.upload(tab.data(), tab.size(), s);
   T.ac.alloc((size_t)T.nc * T.nc);
   T.acinv32.alloc((size_t)T.nc * T.nc);
-  T.piv.alloc(2 * T.nc);
   T.rc.alloc(T.nc);
   T.zc.alloc(T.nc);
   T.z32.alloc(std::max<int64_t>(c.neq, 1));
@@ -1827,7 +1905,7 @@ int two_level_build(Ctx &c) {
 }
 
 // Coarse matrix of the current assembly (per coarse box sum_e mu_e T[sub_e]),
-// removed nodes, in-place FP64 Gauss-Jordan inverse, FP32 copy (symmetrised).
+// removed nodes, blocked in-place FP64 Gauss-Jordan inverse, FP32 copy (symmetrised).
 void two_level_assemble(Ctx &c) {
   TwoLevel &T = c.tl;
   cudaStream_t s = c.stream;
@@ -1841,11 +1919,14 @@ void two_level_assemble(Ctx &c) {
   const int64_t nn = T.nc * T.nc;
   k_tl_fixrows<<<grid_for(nn, 256), 256, 0, s>>>(T.nc, T.cfix.p, T.ac.p);
   c.launches++;
-  for (int64_t k = 0; k < T.nc; k++) {
-    k_tl_gj_save<<<grid_for(2 * T.nc, 256), 256, 0, s>>>(T.nc, k, T.ac.p, T.piv.p);
-    k_tl_gj_step<<<grid_for(nn, 256), 256, 0, s>>>(T.nc, k, T.ac.p, T.piv.p, c.d_err.p);
+  const unsigned tiles = (unsigned)((T.nc + 63) / 64);
+  for (int64_t k0 = 0; k0 < T.nc; k0 += kGjB) {
+    k_gj_diag<<<1, 256, 0, s>>>(T.nc, k0, T.ac.p, c.d_err.p);
+    k_gj_row<<<grid_for(T.nc, 256), 256, 0, s>>>(T.nc, k0, T.ac.p);
+    k_gj_trail<<<dim3(tiles, tiles), 256, 0, s>>>(T.nc, k0, T.ac.p);
+    k_gj_col<<<grid_for(T.nc, 256), 256, 0, s>>>(T.nc, k0, T.ac.p);
+    c.launches += 4;
   }
-  c.launches += 2 * T.nc;
   k_tl_to32<<<grid_for(nn, 256), 256, 0, s>>>(T.nc, T.ac.p, T.acinv32.p);
   c.launches++;
   GPZ_CUDA_TRY(cudaGetLastError());

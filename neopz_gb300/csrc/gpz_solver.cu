@@ -2564,7 +2564,21 @@ void build_vblocks(Ctx &c, int kind) {
       off.assign(bi.begin(), bi.begin() + nb + 1);
       eq.assign(be.begin(), be.begin() + off[nb]);
     }
-    const int64_t nb = (int64_t)off.size() - 1;
+    int64_t nb = (int64_t)off.size() - 1;
+    {  // blocks of one size next to each other (largest first): a warp's threads walk blocks of one size
+      std::vector<int64_t> order(nb);
+      for (int64_t b = 0; b < nb; b++) order[b] = b;
+      std::stable_sort(order.begin(), order.end(),
+                       [&](int64_t x, int64_t y) { return off[x + 1] - off[x] > off[y + 1] - off[y]; });
+      std::vector<int64_t> off2(1, 0), eq2;
+      eq2.reserve(eq.size());
+      for (int64_t b : order) {
+        eq2.insert(eq2.end(), eq.begin() + off[b], eq.begin() + off[b + 1]);
+        off2.push_back((int64_t)eq2.size());
+      }
+      off.swap(off2);
+      eq.swap(eq2);
+    }
     std::vector<int64_t> ioff(std::max<int64_t>(nb, 1), 0);
     int64_t tot = 0;
     int maxn = 0;

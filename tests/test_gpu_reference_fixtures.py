@@ -104,3 +104,49 @@ def test_gpu_learned_mixed_error_against_reference(g, name):
     err = RC.rel_err(sol["x"], fx)
     assert err <= MIXED_ERR, err
     ctx.close()
+
+
+@pytest.fixture(scope="module")
+def abi_driver(g, tmp_path_factory):
+    """tests/abi_driver.cpp compiled against include/gpz.h and the host grid builder alone."""
+    import subprocess
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    build = os.path.join(root, "neopz_gb300", "_build")
+    exe = str(tmp_path_factory.mktemp("abi") / "abi_driver")
+    subprocess.run(["g++", "-std=c++17", "-O1", "-I" + os.path.join(root, "include"),
+                    "-I" + os.path.join(root, "neopz_gb300", "host"), os.path.join(root, "tests", "abi_driver.cpp"),
+                    "-L" + build, "-lgpzhost", "-lgpz", "-Wl,-rpath," + build, "-o", exe], check=True)
+    return exe
+
+
+@pytest.mark.parametrize("name", RC.names())
+def test_cxx_program_drives_the_gpu_path(abi_driver, name, tmp_path):
+    """A C++ program using include/gpz.h alone (tests/abi_driver.cpp) runs upload -> pattern -> assemble ->
+    FP64 Jacobi-PCG -> mixed CG -> downloads; its pattern, values, load vector and solutions match the reference
+    library's fixture with the tolerances of the Python-driven tests above."""
+    import json
+    import subprocess
+    fx = RC.load(name)
+    args = [abi_driver, str(fx["case"]), str(int(fx["n"])), str(int(fx["p"])), str(int(fx["sym"])),
+            repr(float(fx["tol"])) if "tol" in fx else "0", str(tmp_path)]
+    if "coef" in fx:
+        np.ascontiguousarray(fx["coef"], np.float64).tofile(tmp_path / "coef.bin")
+        args.append(str(tmp_path / "coef.bin"))
+    elif "orders" in fx:
+        args.append("-")
+    if "orders" in fx:
+        np.ascontiguousarray(fx["orders"], np.int32).tofile(tmp_path / "orders.bin")
+        args.append(str(tmp_path / "orders.bin"))
+    subprocess.run(args, check=True)
+    info = json.load(open(tmp_path / "info.json"))
+    rd = lambda f, t: np.fromfile(tmp_path / f, t)  # noqa: E731
+    RC.check_system(fx, rd("ia.bin", np.int64), rd("ja.bin", np.int64), rd("a.bin", np.float64),
+                    rd("f.bin", np.float64))
+    if "x" in fx:
+        ref_it = int(fx["cg_iterations"])
+        margin = 0.3 if str(fx["case"]) == "poisson2d" else 0.1
+        assert info["cg_rc"] == 0 and abs(info["cg_iterations"] - ref_it) <= max(3, margin * ref_it)
+        assert RC.rel_err(rd("x.bin", np.float64), fx) <= 1e-8
+        assert info["mixed_rc"] == 0 and info["mixed_true_resid"] <= 1e-8
+        assert RC.rel_err(rd("x_mixed.bin", np.float64), fx) <= MIXED_ERR
+    assert info["launches"] > 0  # the library's own kernels ran
