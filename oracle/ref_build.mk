@@ -34,7 +34,20 @@ $(OUT)/obj/%.o: $(REF)/%.cpp
 $(OUT)/libpzref.so: $(OBJS)
 	g++ -shared -o $@ $(OBJS) -lpthread -latomic
 
-$(OUT)/ref_harness: $(HERE)/ref_harness.cpp $(OUT)/libpzref.so
+$(OUT)/ref_harness: $(HERE)/ref_harness.cpp $(HERE)/ref_cases.h $(OUT)/libpzref.so
 	g++ $(CXXFLAGS) -o $@ $< -L$(OUT) -lpzref -Wl,-rpath,'$$ORIGIN' -lpthread -latomic
 
-.PHONY: all
+# tests/binding_check.cpp: the NeoPZ-side binding (neopz_gb300/neopz_binding)
+# compiled against the reference headers, linked with libpzref and the GPU
+# library (neopz_gb300/_build, made by the package build)
+ROOT := $(HERE)/..
+GPZ_BUILD := $(ROOT)/neopz_gb300/_build
+$(OUT)/binding_check: $(ROOT)/tests/binding_check.cpp $(ROOT)/tests/grid_cases.h $(HERE)/ref_cases.h \
+    $(ROOT)/neopz_gb300/neopz_binding/gpz_neopz.h $(ROOT)/include/gpz.h $(OUT)/libpzref.so
+	g++ $(CXXFLAGS) -I$(HERE) -I$(ROOT)/include -I$(ROOT)/neopz_gb300/host -I$(ROOT)/neopz_gb300/neopz_binding \
+	  -o $@ $< -L$(OUT) -lpzref -L$(GPZ_BUILD) -lgpzhost -lgpz -Wl,-rpath,'$$ORIGIN' -Wl,-rpath,$(abspath $(GPZ_BUILD)) \
+	  -lpthread -latomic
+
+binding: $(OUT)/binding_check
+
+.PHONY: all binding

@@ -9,46 +9,14 @@
 // them with the reference library's own fixtures (tests/golden/ref_*.npz).
 //
 // Usage: abi_driver CASE N P SYM TOL OUTDIR [COEF_FILE|-] [ORDER_FILE]
-//   CASE: poisson2d | darcy2d | darcy3d | elast3d_c5 | elast3d_hp
+//   CASE: poisson2d | darcy2d | darcy3d | elast3d | elast3d_c5 | elast3d_hp (tests/grid_cases.h)
 #include <cmath>
 #include <cstdio>
 #include <cstring>
 #include <string>
 #include <vector>
 
-#include "gpz.h"
-#include "pz_grid.h"
-
-static const double kBig = 1e17 * 2.0 / 3.0;  // TPZMaterial::fBigNumber
-
-static gpz_material material(int kind, int dim, double fx, double fy, double fz, int forcing, int porder) {
-  gpz_material m;
-  std::memset(&m, 0, sizeof(m));
-  m.kind = kind;
-  m.dim = dim;
-  m.scale = 1.0;
-  m.E = 1.0;
-  m.nu = 0.3;
-  m.coef_const = 1.0;
-  m.force[0] = fx;
-  m.force[1] = fy;
-  m.force[2] = fz;
-  m.forcing = forcing;
-  m.forcing_porder = porder;
-  m.bignumber = kBig;
-  return m;
-}
-
-static gpz_bc bc(int type, double v0, double v1, double v2) {
-  gpz_bc b;
-  std::memset(&b, 0, sizeof(b));
-  b.type = type;
-  b.material = 0;
-  b.val2[0] = v0;
-  b.val2[1] = v1;
-  b.val2[2] = v2;
-  return b;
-}
+#include "grid_cases.h"
 
 template <class T>
 static std::vector<T> read_file(const char *path, size_t n) {
@@ -88,47 +56,14 @@ int main(int argc, char **argv) {
   const int n = std::atoi(argv[2]), p = std::atoi(argv[3]), sym = std::atoi(argv[4]);
   const double tol = std::atof(argv[5]);
   const std::string out = argv[6];
-  const bool is3d = cs == "darcy3d" || cs == "elast3d_c5" || cs == "elast3d_hp";
+  const bool is3d = grid_case_is3d(cs);
   const int64_t ncell = is3d ? (int64_t)n * n * n : (int64_t)n * n;
   std::vector<double> coef;
   std::vector<int32_t> order;
   if (argc > 7 && std::string(argv[7]) != "-") coef = read_file<double>(argv[7], ncell);
   if (argc > 8) order = read_file<int32_t>(argv[8], ncell);
 
-  gpzh_grid_spec s;
-  std::memset(&s, 0, sizeof(s));
-  s.dim = is3d ? 3 : 2;
-  for (int d = 0; d < 3; d++) {
-    s.ndiv[d] = d < s.dim ? n : 1;
-    s.minX[d] = 0.0;
-    s.maxX[d] = d < s.dim ? 1.0 : 0.0;
-  }
-  s.create_bc = 1;
-  s.default_order = p;
-  s.nmat = 1;
-  s.mat_id[0] = 1;
-  const int mats3[7] = {1, -1, -1, -1, -1, -1, -1}, mats2[5] = {1, -1, -1, -1, -1},
-            c5[7] = {1, -1, -2, -2, -2, -2, -3}, hp[7] = {1, -1, -2, -2, -2, -2, -2};
-  const int *mid = cs == "elast3d_c5" ? c5 : cs == "elast3d_hp" ? hp : is3d ? mats3 : mats2;
-  for (int k = 0; k < (is3d ? 7 : 5); k++) s.matids[k] = mid[k];
-  s.nbc = 1;
-  s.bc_id[0] = -1;
-  s.bcs[0] = bc(0, 0, 0, 0);
-  if (cs == "poisson2d") {
-    s.mats[0] = material(GPZ_MAT_POISSON, 2, 1.0, 0, 0, GPZ_F_SINPROD, 2);
-  } else if (cs == "darcy2d" || cs == "darcy3d") {
-    s.mats[0] = material(GPZ_MAT_DARCY, s.dim, 1.0, 0, 0, GPZ_F_CONST, 0);
-  } else {
-    s.mats[0] = material(GPZ_MAT_ELAST3D, 3, 0, 0, cs == "elast3d_c5" ? 0.0 : -1.0, GPZ_F_CONST, 0);
-    if (cs == "elast3d_c5") {
-      s.nbc = 2;
-      s.bc_id[1] = -3;
-      s.bcs[1] = bc(1, 0, 0, -1.0);
-    }
-  }
-  if (!coef.empty()) s.elem_coef = coef.data();
-  if (!order.empty()) s.elem_order = order.data();
-  void *grid = gpzh_grid_build(&s);
+  void *grid = grid_case(cs, n, p, coef.empty() ? nullptr : coef.data(), order.empty() ? nullptr : order.data());
   if (!grid) {
     std::fprintf(stderr, "grid build failed\n");
     return 3;
