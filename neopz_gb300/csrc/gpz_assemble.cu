@@ -53,6 +53,11 @@ struct ElemArgs {
   double *a, *f;
   int64_t nnz, neq;
   int *err;
+  // shared element matrix (a volume bucket whose elements are translates of one box): K_e = s_e kref
+  // (s_e the element's coefficient, kref the matrix at coefficient 1), F_e = fref when the forcing is constant
+  const double *kref, *fref;
+  // reference mode: the first element's matrix at coefficient 1 and its load vector into these dense arrays
+  double *kdense, *fdense;
 };
 
 // Geometric Jacobian at one point: returns |detJ| and fills jinv (row-major dim x dim)
@@ -191,15 +196,16 @@ __global__ void __launch_bounds__(256) k_elem_fp64(ElemArgs P, HpArgs H, const i
   }
   __shared__ int sAff;
   __shared__ double sJi[3][3], sDet;
+  const bool shared = !BC && P.kref != nullptr, dense = !BC && P.kdense != nullptr;
   if (tid == 0) {
-    sOffBase = P.rhs_only ? 0 : P.offbase[e];
+    sOffBase = (P.rhs_only || dense) ? 0 : P.offbase[e];
     double cf = P.kind == GPZ_MAT_ELAST3D ? P.E : P.coef_const;
     if (!BC && P.coef) cf = P.coef[e];
-    sCoef = cf;
+    sCoef = dense && P.kind != GPZ_MAT_POISSON ? 1.0 : cf;  // the reference matrix is at coefficient 1
     sAff = 0;
   }
   __syncthreads();
-  if (!BC && DIM == 3 && P.ghat != nullptr && tid == 0) {
+  if (!BC && !shared && DIM == 3 && P.ghat != nullptr && tid == 0) {
     // affine hex: the trilinear map's xi.eta, xi.zeta, eta.zeta and xi.eta.zeta
     // coefficients vanish, the Jacobian is constant and the element Gram is
     // |J| Jinv^T G Jinv with the bucket's reference Gram G
@@ -235,8 +241,9 @@ __global__ void __launch_bounds__(256) k_elem_fp64(ElemArgs P, HpArgs H, const i
   __syncthreads();
   const bool aff = sAff != 0;
 
-  // per-point geometry
-  for (int q = tid; q < nq; q += blockDim.x) {
+  // per-point geometry (a shared element matrix with a constant forcing needs none)
+  const bool geo = !(shared && P.fref != nullptr);
+  for (int q = tid; geo && q < nq; q += blockDim.x) {
     double pt[3] = {0, 0, 0};
     // reference point recovered from the corner table is not needed: use dcorner at the point
     // (the bucket tables hold the point implicitly through phi of the corner shapes)
@@ -255,7 +262,7 @@ __global__ void __launch_bounds__(256) k_elem_fp64(ElemArgs P, HpArgs H, const i
       for (int k = 0; k < nc; k++) x += phic[k] * sC[k * 3 + j];
       sX[q * 3 + j] = x;
     }
-    if (!BC && !aff) {
+    if (!BC && !aff && !shared) {
       // store jinv temporarily in sG is not possible; compute gradients directly
       for (int a = 0; a < NSH; a++) {
         const int fa = HP ? sIdx[a] : a;
@@ -275,7 +282,9 @@ __global__ void __launch_bounds__(256) k_elem_fp64(ElemArgs P, HpArgs H, const i
     int a = idx / NST, s = idx % NST;
     const int fa = HP ? sIdx[a] : a;
     double acc = 0.0;
-    if (!BC) {
+    if (shared && P.fref != nullptr) {
+      acc = P.fref[idx];
+    } else if (!BC) {
       for (int q = 0; q < nq; q++) {
         double fv[3];
         forcing_at(P, &sX[q * 3], fv);
@@ -289,6 +298,10 @@ __global__ void __launch_bounds__(256) k_elem_fp64(ElemArgs P, HpArgs H, const i
       for (int q = 0; q < nq; q++) m += P.phi[q * NT + fa] * sW[q];
       if (P.bc_type == 0) acc = P.big * P.val2[s] * m;
       else if (P.bc_type == 1) acc = P.val2[s] * m * (P.kind == GPZ_MAT_POISSON ? P.scale : 1.0);
+    }
+    if (dense) {
+      P.fdense[idx] = acc;
+      continue;
     }
     int64_t row = sRow[a] + s;
     if (row < 0 || row >= P.neq) {
@@ -312,7 +325,12 @@ __global__ void __launch_bounds__(256) k_elem_fp64(ElemArgs P, HpArgs H, const i
     const int a = idx / NSH, b = idx % NSH;
     if (a > b) continue;
     double K[NST][NST];
-    if (BC) {
+    if (shared) {
+      const int nd = NSH * NST;
+      const double cs = P.kind == GPZ_MAT_POISSON ? 1.0 : coef;
+      for (int s = 0; s < NST; s++)
+        for (int t = 0; t < NST; t++) K[s][t] = cs * P.kref[(size_t)(a * NST + s) * nd + b * NST + t];
+    } else if (BC) {
       const int fa = HP ? sIdx[a] : a, fb = HP ? sIdx[b] : b;
       double m = 0.0;
       for (int q = 0; q < nq; q++) m += sW[q] * P.phi[q * NT + fa] * P.phi[q * NT + fb];
@@ -359,6 +377,15 @@ __global__ void __launch_bounds__(256) k_elem_fp64(ElemArgs P, HpArgs H, const i
       for (int s = 0; s < NST; s++)
         for (int t = 0; t < NST; t++)
           K[s][t] = (s == t) ? (tr - S[s][s]) * C1 + S[s][s] * C3 : S[t][s] * C1 - S[s][t] * C2;
+    }
+    if (dense) {
+      const int nd = NSH * NST;
+      for (int s = 0; s < NST; s++)
+        for (int t = 0; t < NST; t++) {
+          P.kdense[(size_t)(a * NST + s) * nd + b * NST + t] = K[s][t];
+          P.kdense[(size_t)(b * NST + t) * nd + a * NST + s] = K[s][t];
+        }
+      continue;
     }
     // scatter the (a,b) block and, off the diagonal, its transpose into (b,a)
     const int sa = sSide[a], sb = sSide[b];
@@ -716,7 +743,56 @@ ElemArgs args_of(Ctx &c, const Bucket *b) {
   P.nnz = flt ? c.flt.m_nnz : c.nnz;
   P.neq = c.neq_mesh;
   P.err = c.d_err.p;
+  if (b->shared == 1) {
+    P.kref = b->d_kref.p;
+    P.fref = (m->forcing == GPZ_F_CONST || m->forcing == GPZ_F_NONE) ? b->d_fref.p : nullptr;
+  }
   return P;
+}
+
+// 1 in *flag when an element of the list is not a translate of the first: its
+// trilinear map has xi.eta, xi.zeta, eta.zeta or xi.eta.zeta terms, or its
+// gradient (the xi, eta, zeta terms) differs from the first element's, by more
+// than 1e-13 of the element's extent
+__device__ __forceinline__ void hex_map_terms(const int64_t *__restrict__ el_nodes, const double *__restrict__ xyz,
+                                              int64_t e, double (&t)[3][7], double &ext) {
+  const signed char sg[8][3] = {{-1, -1, -1}, {1, -1, -1}, {1, 1, -1}, {-1, 1, -1},
+                                {-1, -1, 1},  {1, -1, 1},  {1, 1, 1},  {-1, 1, 1}};
+  ext = 0.0;
+  for (int j = 0; j < 3; j++) {
+    for (int d = 0; d < 7; d++) t[j][d] = 0.0;
+    double mn = 1e300, mx = -1e300;
+    for (int k = 0; k < 8; k++) {
+      const double x = xyz[el_nodes[e * 8 + k] * 3 + j];
+      const int a = sg[k][0], b = sg[k][1], c = sg[k][2];
+      t[j][0] += a * x;
+      t[j][1] += b * x;
+      t[j][2] += c * x;
+      t[j][3] += a * b * x;
+      t[j][4] += a * c * x;
+      t[j][5] += b * c * x;
+      t[j][6] += a * b * c * x;
+      mn = fmin(mn, x);
+      mx = fmax(mx, x);
+    }
+    ext = fmax(ext, mx - mn);
+  }
+}
+
+__global__ void k_translates(const int64_t *__restrict__ elems, int64_t n, const int64_t *__restrict__ el_nodes,
+                             const double *__restrict__ xyz, int *__restrict__ flag) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  double t0[3][7], t[3][7], ext0, ext;
+  hex_map_terms(el_nodes, xyz, elems[0], t0, ext0);
+  hex_map_terms(el_nodes, xyz, elems[i], t, ext);
+  const double tol = 1e-13 * ext;
+  bool ok = ext > 0.0;
+  for (int j = 0; j < 3; j++) {
+    for (int d = 0; d < 3; d++) ok = ok && fabs(t[j][d] - t0[j][d]) <= tol;
+    for (int d = 3; d < 7; d++) ok = ok && fabs(t[j][d]) <= tol;
+  }
+  if (!ok) atomicOr(flag, 1);
 }
 
 // element integration + scatter of every bucket, colour by colour; the hp
@@ -751,10 +827,52 @@ void launch_elements(Ctx &c, int threads, bool rhs_only = false, bool set_attrs 
   }
 }
 
+// Shared element matrices: a volume hex bucket (not an hp class) whose elements
+// are all translates of its first element gets that element's matrix at
+// coefficient 1 (kref) and its load vector (fref), computed once by the element
+// kernel in its dense mode; the bucket's assembly then scales kref by each
+// element's coefficient (K is linear in E, k; TPZElasticity3D's C1, C2, C3 are
+// proportional to E) instead of integrating it, and takes fref as the load
+// vector when the forcing is constant.
+void shared_setup(Ctx &c) {
+  cudaStream_t s = c.stream;
+  for (Bucket *b : c.buckets) {
+    if (b->shared >= 0) continue;
+    b->shared = 0;
+    if (b->hp || b->key.is_bc || b->key.type != GPZ_EL_HEX || b->elems.empty()) continue;
+    const int64_t n = (int64_t)b->elems.size();
+    DBuf<int> flag;
+    flag.alloc(1);
+    flag.zero(s);
+    k_translates<<<grid_for(n, 256), 256, 0, s>>>(b->d_elems.p, n, c.d_el_nodes.p, c.d_xyz.p, flag.p);
+    c.launches++;
+    int h = 1;
+    GPZ_CUDA_TRY(cudaMemcpyAsync(&h, flag.p, sizeof(int), cudaMemcpyDeviceToHost, s));
+    GPZ_CUDA_TRY(cudaStreamSynchronize(s));
+    if (h) continue;
+    const int nd = b->nshape * c.nstate;
+    b->d_kref.alloc((size_t)nd * nd);
+    b->d_fref.alloc((size_t)nd);
+    ElemArgs P = args_of(c, b);
+    P.kdense = b->d_kref.p;
+    P.fdense = b->d_fref.p;
+    const size_t sh = smem_bytes(b->nshape, b->dim, b->nq, false);
+    ElemKernel k = select_kernel(b->key.type, b->nshape, c.nstate, false);
+    if (sh > 48 * 1024) GPZ_CUDA_TRY(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sh));
+    HpArgs H{nullptr, nullptr, nullptr};
+    k<<<1, 128, sh, s>>>(P, H, b->d_elems.p, 1);
+    c.launches++;
+    GPZ_CUDA_TRY(cudaGetLastError());
+    check_device_flag(c, "reference element matrix");
+    b->shared = 1;
+  }
+}
+
 }  // namespace
 
 void assemble_fp64(Ctx &c) {
   cudaStream_t s = c.stream;
+  shared_setup(c);
   const bool flt = c.flt.active;
   c.d_a.alloc(std::max<int64_t>(c.nnz, 1));
   if (flt) c.flt.m_a.alloc(std::max<int64_t>(c.flt.m_nnz, 1));
@@ -838,6 +956,7 @@ void assemble_fp64(Ctx &c) {
 // load vector alone (TPZStructMatrix::Assemble(rhs), StrMatrix/pzstrmatrixor.cpp:75-103):
 // the same element kernels, stopped before the element matrix
 void assemble_rhs(Ctx &c) {
+  shared_setup(c);
   c.d_f.alloc(std::max<int64_t>(c.neq_mesh, 1));
   c.d_f.zero(c.stream);
   launch_elements(c, 0, true);

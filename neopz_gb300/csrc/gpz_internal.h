@@ -101,6 +101,10 @@ struct Bucket {
   DBuf<int32_t> d_act_n;
   int threads = 128;                         // block size (autotuned for hp classes)
   bool tuned = false;
+  // shared element matrix: 1 when every element is a translate of the first (same affine
+  // Jacobian), so K_e = coefficient_e x kref; -1 before the check
+  int shared = -1;
+  DBuf<double> d_kref, d_fref;               // [ndof][ndof] at coefficient 1, [ndof] load vector
 };
 
 // ---------------------------------------------------------------- solver workspace

@@ -170,7 +170,7 @@ __global__ void __launch_bounds__(kThreads) k_mf_faces(int64_t n, const float *_
         for (int s = 0; s < 3; s++) y[s] += st[wp][q][s] * ph;
       }
       en.add(y[0] * u.x + y[1] * u.y + y[2] * u.z);
-      atomicAdd(&q4[row], make_float4(y[0], y[1], y[2], 0.f));
+      red_add_f4(&q4[row], make_float4(y[0], y[1], y[2], 0.f));
     }
     __syncwarp();
   }
@@ -325,7 +325,7 @@ __global__ void __launch_bounds__(kMfThreads, 3) k_mf_hex27(int64_t n, const flo
         y2 += t2.x * g.x + t2.y * g.y + t2.z * g.z;
       }
       en.add(y0 * u.x + y1 * u.y + y2 * u.z);
-      atomicAdd(&q4[row_i], make_float4(y0, y1, y2, 0.f));
+      red_add_f4(&q4[row_i], make_float4(y0, y1, y2, 0.f));
     }
     __syncwarp();
   }
@@ -645,7 +645,7 @@ __global__ void __launch_bounds__(kSfThreads, 5) k_mf_hex27_sf(int64_t n, const 
         y2 = fmaf(cv[k], W.v[o + 6], y2);
       }
       en.add(y0 * u.x + y1 * u.y + y2 * u.z);
-      atomicAdd(&q4[row_i], make_float4(y0, y1, y2, 0.f));
+      red_add_f4(&q4[row_i], make_float4(y0, y1, y2, 0.f));
     }
     __syncwarp();
   }
@@ -1003,7 +1003,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_mf_hex27_tc(int64_t n, const 
       if (e >= n) continue;
       const int r0 = (le / kTcElW) * 32 + 3 * (le % kTcElW);
       const float4 v = make_float4(st1[(r0 + 0) * 32 + a], st1[(r0 + 1) * 32 + a], st1[(r0 + 2) * 32 + a], 0.f);
-      atomicAdd(&q4[rows[e * 27 + a]], v);
+      red_add_f4(&q4[rows[e * 27 + a]], v);
     }
     parity ^= 1u;
   }
@@ -1036,23 +1036,39 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_mf_hex27_tc(int64_t n, const 
 // with U the elements' gathered coefficients: tcgen05.mma kind::tf32 with the
 // 3xTF32 split (hi.hi + hi.lo + lo.hi, FP32 accumulation in TMEM), M = 128
 // elements, N = 96 (81 rows), K = 88 (81 columns), both operands K-major
-// without swizzle.  Thread t gathers half of element (t mod 128)'s row (shapes
-// [0, 12) or [12, 27)) and later scatters half of its results (TMEM columns
-// [0, 48) or [48, 96)) with float4 atomics, scaled by mu_e; the element energy
-// mu_e Y[e] . U[e] gives p.q.  Two TMEM accumulator pairs (hi.hi and the
-// correction products, 4 x 128 of the 512 columns: one CTA per SM) let the
-// MMAs of the next tile run while the current tile's results are scattered.  Every wait is
-// bounded: on a timeout the kernel records an error flag, waits (bounded) for
-// the MMAs in flight, frees its TMEM and leaves.
-constexpr int kGmThreads = 256;
+// without swizzle.
+//
+// The work is gathers of p and float4 atomics into q (the MMAs take ~1 us of a
+// tile's time), so the CTA (one per SM, persistent over tiles) is split into
+// two groups of 8 warps that run a two-stage pipeline:
+//   gatherers: copy the tile's block rows into shared memory (one coalesced
+//     13.8 KB block: the row array is padded to whole tiles), gather U (thread t
+//     takes shapes [0, 12) or [12, 27) of element t mod 128), split it hi / lo
+//     into the A operand, and one thread issues the MMAs of tile k into TMEM
+//     accumulator pair k mod 2 and commits them to mma_done[k mod 2];
+//   scatterers: copy the same rows into their own buffer, wait for
+//     mma_done, read their lane quarter's results (warp w: elements
+//     32 (w mod 4) + lane, columns [0, 48) or [48, 96)), add mu_e Y[e] to q
+//     with float4 atomics, accumulate the element energy mu_e Y[e] . U[e]
+//     (p . q) and arrive on tmem_free[k mod 2].
+// Gathering tile k + 1 overlaps the scattering of tile k; the A operand is
+// rewritten only after mma_done of the previous tile, an accumulator pair only
+// after tmem_free of the tile two back.  Every wait is bounded: a timeout sets
+// a shared abort flag that ends every other wait, the groups leave their loops
+// together (votes over named barriers), the MMAs in flight are waited for
+// (bounded), the TMEM is freed and an error flag recorded.
+constexpr int kGmThreads = 512;             // 8 gatherer + 8 scatterer warps
+constexpr int kGmGroup = 256;
 constexpr int kGmEl = 128;                  // elements per tile (MMA M)
 constexpr int kGmK = 88, kGmN = 96;         // padded K (81) and N (81)
-constexpr int kGmSplit = 12;                // gather: shapes [0, 12) by threads 0..127, [12, 27) by 128..255
+constexpr int kGmSplit = 12;                // gather: shapes [0, 12) by group threads 0..127, [12, 27) by 128..255
 constexpr uint32_t kGmSmall = 128;          // TMEM column offset of the correction accumulator
 constexpr int64_t kTlMaxNc = 3000;          // largest coarse system of the two-level preconditioner
-constexpr uint32_t kGmB = kGmN * kGmK * 4, kGmA = kGmEl * kGmK * 4;
-constexpr uint32_t GM_BH = 0, GM_BL = kGmB, GM_AH = 2 * kGmB, GM_AL = 2 * kGmB + kGmA, GM_END = 2 * kGmB + 2 * kGmA;
-static_assert(GM_AH % 1024 == 0 && GM_AL % 1024 == 0 && GM_END % 1024 == 0, "operand alignment");
+constexpr uint32_t kGmB = kGmN * kGmK * 4, kGmA = kGmEl * kGmK * 4, kGmR = kGmEl * kNS * 4;
+constexpr uint32_t GM_BH = 0, GM_BL = kGmB, GM_AH = 2 * kGmB, GM_AL = 2 * kGmB + kGmA;
+constexpr uint32_t GM_RG = 2 * kGmB + 2 * kGmA, GM_RS = GM_RG + kGmR, GM_END = GM_RS + kGmR;
+static_assert(GM_AH % 1024 == 0 && GM_AL % 1024 == 0 && GM_RG % 16 == 0 && kGmR % 16 == 0, "operand alignment");
+static_assert(GM_END <= 227 * 1024, "shared memory");
 
 __device__ __forceinline__ float4 tf32_split4(float4 v, float4 &lo) {
   float4 h;
@@ -1067,23 +1083,53 @@ __device__ __forceinline__ float4 tf32_split4(float4 v, float4 &lo) {
   return h;
 }
 
+// barrier `id` over n threads; true in every participant when v is true in all
+__device__ __forceinline__ bool gm_vote(int id, int n, bool v) {
+  uint32_t r;
+  asm volatile("{\n.reg .pred p, q;\nsetp.ne.u32 q, %1, 0;\nbar.red.and.pred p, %2, %3, q;\nselp.u32 %0, 1, 0, p;\n}\n"
+               : "=r"(r)
+               : "r"((uint32_t)v), "r"(id), "r"(n)
+               : "memory");
+  return r != 0;
+}
+__device__ __forceinline__ void gm_bar(int id, int n) { asm volatile("bar.sync %0, %1;" ::"r"(id), "r"(n) : "memory"); }
+
+// bounded wait on an mbarrier phase that also ends when another thread has aborted
+__device__ __forceinline__ bool gm_wait(uint64_t *mb, uint32_t parity, volatile int *abort) {
+  for (int it = 0; it < kTcWaitTries; it++) {
+    uint32_t done;
+    asm volatile("{\n.reg .pred p;\nmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\nselp.u32 %0, 1, 0, p;\n}\n"
+                 : "=r"(done)
+                 : "r"(tc_smem(mb)), "r"(parity));
+    if (done) return true;
+    if (*abort) return false;
+  }
+  *abort = 1;
+  return false;
+}
+
+// the tile's block rows [128][27] into shared memory (coalesced; padded tiles)
+__device__ __forceinline__ void gm_rows(unsigned char *dst, const int4 *__restrict__ rows4, int64_t tile, int gl) {
+  constexpr int n4 = (int)(kGmR / 16);
+  const int4 *src = rows4 + (size_t)tile * n4;
+#pragma unroll
+  for (int i = gl; i < n4; i += kGmGroup) ((int4 *)dst)[i] = src[i];
+}
+
 // Half of one element's row of U: shapes [A0, A1) -> columns [3 A0, 3 A1),
-// the last half also writes the zero padding up to K.  Rows of elements past
-// the end are zero.
+// the last half also writes the zero padding up to K.  Rows of padding
+// elements (-1) are zero.
 template <int A0, int A1>
-__device__ __forceinline__ void gm_gather(unsigned char *sm, int64_t e, bool valid, int le,
-                                          const int32_t *__restrict__ rows, const float4 *__restrict__ p4) {
+__device__ __forceinline__ void gm_gather(unsigned char *sm, const int32_t *rw, int le, const float4 *__restrict__ p4) {
   constexpr int NA = A1 - A0, K0 = 3 * A0, K1 = A1 == kNS ? kGmK : 3 * A1, NV = K1 - K0;
   static_assert(K0 % 4 == 0 && NV % 4 == 0, "16-byte chunks");
-  int32_t r[NA];
-#pragma unroll
-  for (int a = 0; a < NA; a++) r[a] = valid ? rows[e * kNS + A0 + a] : -1;
   float v[NV];
 #pragma unroll
   for (int k = 0; k < NV; k++) v[k] = 0.f;
 #pragma unroll
   for (int a = 0; a < NA; a++) {
-    const float4 pv = r[a] >= 0 ? p4[r[a]] : make_float4(0.f, 0.f, 0.f, 0.f);
+    const int32_t r = rw[le * kNS + A0 + a];
+    const float4 pv = r >= 0 ? p4[r] : make_float4(0.f, 0.f, 0.f, 0.f);
     v[3 * a] = pv.x;
     v[3 * a + 1] = pv.y;
     v[3 * a + 2] = pv.z;
@@ -1099,29 +1145,48 @@ __device__ __forceinline__ void gm_gather(unsigned char *sm, int64_t e, bool val
 }
 
 // Half of one element's results: TMEM columns [C0, C0 + 48) of the warp's
-// lane quarter (lane = element), shapes [A0, A1).
+// lane quarter (lane = element), shapes [A0, A1), read 16 columns at a time
+// (a shape whose three columns straddle two reads takes the last two of the
+// previous one); the p loads of a read's shapes are issued together.
 template <int C0, int A0, int A1>
-__device__ __forceinline__ void gm_scatter(uint32_t taddr, int64_t e, bool valid, const int32_t *__restrict__ rows,
+__device__ __forceinline__ void gm_scatter(uint32_t taddr, int64_t e, bool valid, const int32_t *rw, int le,
                                            const float *__restrict__ rlm, const float4 *__restrict__ p4,
                                            float4 *__restrict__ q4, KSum &en) {
-  float y[48], ys[16];
+  const float mu = valid ? rlm[2 * e + 1] : 0.f;
+  float prev[2] = {0.f, 0.f};
 #pragma unroll
   for (int c = 0; c < 48; c += 16) {
-    tc_ld16(taddr + C0 + c, y + c);
-    tc_ld16(taddr + kGmSmall + C0 + c, ys);
+    float t[16], u[16];
+    tc_ld16(taddr + C0 + c, t);
+    tc_ld16(taddr + kGmSmall + C0 + c, u);
 #pragma unroll
-    for (int j = 0; j < 16; j++) y[c + j] += ys[j];
-  }
-  if (!valid) return;
-  const float mu = rlm[2 * e + 1];
+    for (int j = 0; j < 16; j++) t[j] += u[j];
+    if (valid) {
+      int32_t r[A1 - A0];
+      float4 pv[A1 - A0];
 #pragma unroll
-  for (int a = A0; a < A1; a++) {
-    const int j = 3 * a - C0;
-    const int32_t r = rows[e * kNS + a];
-    const float4 pv = p4[r];
-    const float4 yv = make_float4(mu * y[j], mu * y[j + 1], mu * y[j + 2], 0.f);
-    en.add(yv.x * pv.x + yv.y * pv.y + yv.z * pv.z);
-    atomicAdd(&q4[r], yv);
+      for (int a = A0; a < A1; a++) {
+        const int j2 = 3 * a + 2 - C0;  // the shape's last column: handled in the read that holds it
+        if (j2 >= c && j2 < c + 16) {
+          r[a - A0] = rw[le * kNS + a];
+          pv[a - A0] = p4[r[a - A0]];
+        }
+      }
+#pragma unroll
+      for (int a = A0; a < A1; a++) {
+        const int j0 = 3 * a - C0, j2 = j0 + 2;
+        if (j2 >= c && j2 < c + 16) {
+          float yc[3];
+#pragma unroll
+          for (int d = 0; d < 3; d++) yc[d] = j0 + d >= c ? t[j0 + d - c] : prev[j0 + d - c + 2];
+          const float4 yv = make_float4(mu * yc[0], mu * yc[1], mu * yc[2], 0.f);
+          en.add(yv.x * pv[a - A0].x + yv.y * pv[a - A0].y + yv.z * pv[a - A0].z);
+          red_add_f4(&q4[r[a - A0]], yv);
+        }
+      }
+    }
+    prev[0] = t[14];
+    prev[1] = t[15];
   }
 }
 
@@ -1141,6 +1206,7 @@ __device__ __forceinline__ void gm_mma(uint32_t tm, uint32_t ah, uint32_t al, ui
   }
 }
 
+// rows: [ntile * 128][27] block rows, -1 past the n elements
 __global__ void __launch_bounds__(kGmThreads, 1) k_mf_hex27_gm(int64_t n, const int32_t *__restrict__ rows,
                                                                const float *__restrict__ rlm,
                                                                const float4 *__restrict__ bsplit,
@@ -1150,83 +1216,89 @@ __global__ void __launch_bounds__(kGmThreads, 1) k_mf_hex27_gm(int64_t n, const 
   if (!active(R.iscal)) return;
   extern __shared__ __align__(1024) unsigned char sm[];
   __shared__ uint32_t s_tmem;
-  __shared__ __align__(8) uint64_t s_mb[2];
+  __shared__ volatile int s_abort;
+  __shared__ __align__(8) uint64_t s_done[2], s_free[2];
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-  const int le = tid & (kGmEl - 1), half = tid >> 7;
+  const bool gatherer = tid < kGmGroup;
+  const int gl = tid & (kGmGroup - 1);
+  const int4 *rows4 = (const int4 *)rows;
   // Khat hi / lo, already in the operand layout
   for (uint32_t i = tid; i < 2 * kGmB / 16; i += kGmThreads) ((float4 *)(sm + GM_BH))[i] = bsplit[i];
+  asm volatile("fence.proxy.async.shared::cta;");  // B is read by the MMAs (async proxy)
   if (warp == 0) {
     asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(tc_smem(&s_tmem)), "r"(512));
     asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
   }
   if (tid == 0) {
-    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(tc_smem(&s_mb[0])));
-    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(tc_smem(&s_mb[1])));
+    s_abort = 0;
+    for (int b = 0; b < 2; b++) {
+      asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(tc_smem(&s_done[b])));
+      asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(tc_smem(&s_free[b])), "r"(kGmGroup));
+    }
     asm volatile("fence.mbarrier_init.release.cluster;");
   }
-  const uint32_t ah = tc_smem(sm + GM_AH), al = tc_smem(sm + GM_AL), bh = tc_smem(sm + GM_BH),
-                 bl = tc_smem(sm + GM_BL);
-  int64_t tile = blockIdx.x;
-  const int64_t ntile = (n + kGmEl - 1) / kGmEl;
-  if (tile < ntile) {
-    const int64_t e = tile * kGmEl + le;
-    if (half == 0) gm_gather<0, kGmSplit>(sm, e, e < n, le, rows, p4);
-    else gm_gather<kGmSplit, kNS>(sm, e, e < n, le, rows, p4);
-  }
-  asm volatile("fence.proxy.async.shared::cta;");
   asm volatile("tcgen05.fence::before_thread_sync;");
   __syncthreads();
   asm volatile("tcgen05.fence::after_thread_sync;");
   const uint32_t tm = s_tmem;
-  if (tile < ntile && tid == 0) {
-    gm_mma(tm, ah, al, bh, bl);
-    tc_commit(&s_mb[0]);
-  }
+  const uint32_t ah = tc_smem(sm + GM_AH), al = tc_smem(sm + GM_AL), bh = tc_smem(sm + GM_BH),
+                 bl = tc_smem(sm + GM_BL);
+  const int64_t ntile = (n + kGmEl - 1) / kGmEl;
   KSum en;
-  uint32_t phase[2] = {0u, 0u};
-  int it = 0;
-  bool failed = false;
-  for (; tile < ntile; tile += gridDim.x, it++) {
-    const int b = it & 1;
-    const bool ok = tc_wait(&s_mb[b], phase[b]);
-    if (__syncthreads_or(!ok)) {
-      failed = true;
-      break;
+  int last = -1;  // the issuer's last committed tile
+  if (gatherer) {
+    const int le = gl & (kGmEl - 1), half = gl >> 7;
+    const int32_t *rw = (const int32_t *)(sm + GM_RG);
+    int k = 0;
+    for (int64_t tile = blockIdx.x; tile < ntile; tile += gridDim.x, k++) {
+      const int b = k & 1;
+      gm_rows(sm + GM_RG, rows4, tile, gl);  // the previous tile's rows were last read before its MMA issue
+      bool ok = true;
+      if (gl == 0 && k >= 2) ok = gm_wait(&s_free[b], (uint32_t)((k - 2) >> 1) & 1u, &s_abort);
+      if (ok && k >= 1) ok = gm_wait(&s_done[(k - 1) & 1], (uint32_t)((k - 1) >> 1) & 1u, &s_abort);
+      if (!gm_vote(1, kGmGroup, ok)) break;  // also orders the row copies before their reads
+      if (half == 0) gm_gather<0, kGmSplit>(sm, rw, le, p4);
+      else gm_gather<kGmSplit, kNS>(sm, rw, le, p4);
+      asm volatile("fence.proxy.async.shared::cta;");
+      gm_bar(1, kGmGroup);
+      if (gl == 0) {
+        asm volatile("tcgen05.fence::after_thread_sync;");
+        gm_mma(tm + (uint32_t)b * 256u, ah, al, bh, bl);
+        tc_commit(&s_done[b]);
+        last = k;
+      }
     }
-    phase[b] ^= 1u;
-    asm volatile("tcgen05.fence::after_thread_sync;");
-    // the operand U is free: the next tile's gather, then its MMAs into the other accumulator
-    const int64_t next = tile + gridDim.x;
-    if (next < ntile) {
-      const int64_t e = next * kGmEl + le;
-      if (half == 0) gm_gather<0, kGmSplit>(sm, e, e < n, le, rows, p4);
-      else gm_gather<kGmSplit, kNS>(sm, e, e < n, le, rows, p4);
+  } else {
+    const int sw = warp - kGmGroup / 32, quarter = sw & 3, half = sw >> 2, le = quarter * 32 + lane;
+    const int32_t *rw = (const int32_t *)(sm + GM_RS);
+    int k = 0;
+    for (int64_t tile = blockIdx.x; tile < ntile; tile += gridDim.x, k++) {
+      const int b = k & 1;
+      gm_rows(sm + GM_RS, rows4, tile, gl);
+      const bool ok = gm_wait(&s_done[b], (uint32_t)(k >> 1) & 1u, &s_abort);
+      if (!gm_vote(2, kGmGroup, ok)) break;  // uniform exit; orders the row copies before their reads
+      asm volatile("tcgen05.fence::after_thread_sync;");
+      const int64_t e = tile * kGmEl + le;
+      const uint32_t taddr = tm + ((uint32_t)(quarter * 32) << 16) + (uint32_t)b * 256u;
+      if (half == 0) gm_scatter<0, 0, 16>(taddr, e, e < n, rw, le, rlm, p4, q4, en);
+      else gm_scatter<48, 16, kNS>(taddr, e, e < n, rw, le, rlm, p4, q4, en);
+      asm volatile("tcgen05.fence::before_thread_sync;");
+      asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(tc_smem(&s_free[b])) : "memory");
+      gm_bar(2, kGmGroup);  // the rows buffer is rewritten next
     }
-    asm volatile("fence.proxy.async.shared::cta;");
-    asm volatile("tcgen05.fence::before_thread_sync;");
-    __syncthreads();
-    asm volatile("tcgen05.fence::after_thread_sync;");
-    if (next < ntile && tid == 0) {
-      gm_mma(tm + (uint32_t)(b ^ 1) * 256u, ah, al, bh, bl);
-      tc_commit(&s_mb[b ^ 1]);
-    }
-    // this tile's results: warp w reads TMEM lanes 32 (w mod 4) .. + 31 (its elements)
-    const int64_t e = tile * kGmEl + le;
-    const uint32_t taddr = tm + ((uint32_t)((warp & 3) * 32) << 16) + (uint32_t)b * 256u;
-    if (half == 0) gm_scatter<0, 0, 16>(taddr, e, e < n, rows, rlm, p4, q4, en);
-    else gm_scatter<48, 16, kNS>(taddr, e, e < n, rows, rlm, p4, q4, en);
-    asm volatile("tcgen05.fence::before_thread_sync;");
   }
-  if (failed) {
-    if (tid == 0) atomicOr(err, 16384);
+  __syncthreads();
+  const bool failed = s_abort != 0;
+  if (failed && tid == 0) {
+    atomicOr(err, 16384);
     // the MMAs in flight write the accumulators: let them finish (bounded) before the TMEM is released
-    tc_wait(&s_mb[it & 1], phase[it & 1]);
+    if (last >= 0) tc_wait(&s_done[last & 1], (uint32_t)(last >> 1) & 1u);
   }
   asm volatile("tcgen05.fence::before_thread_sync;");
   __syncthreads();
   if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tm), "r"(512));
   double v[1] = {failed ? 0.0 : en.get()}, tot[1];
-  if (grid_reduce<1>(v, R, tot) && threadIdx.x == 0) {
+  if (grid_reduce<1, kGmThreads / 32>(v, R, tot) && threadIdx.x == 0) {
     const double pq = tot[0] + (face_energy ? *face_energy : 0.0);
     R.scal[S_PQ] = pq;
     R.scal[S_ALPHA] = R.scal[S_RHO] / pq;
@@ -1967,7 +2039,10 @@ bool matfree_build(Ctx &c) {
   };
   M.nvol = (int64_t)vol->elems.size();
   M.vxyz.alloc((size_t)M.nvol * 24);
-  M.vrows.alloc((size_t)M.nvol * kNS);
+  // block rows padded to whole tiles of the shared-matrix kernel with -1 (it copies a tile's rows as one block)
+  const size_t vrows_n = (size_t)((M.nvol + kGmEl - 1) / kGmEl) * kGmEl * kNS;
+  M.vrows.alloc(vrows_n);
+  GPZ_CUDA_TRY(cudaMemsetAsync(M.vrows.p, 0xFF, vrows_n * sizeof(int32_t), s));
   M.vlm.alloc((size_t)M.nvol * 2);
   M.vgeo.alloc((size_t)M.nvol * 10);
   f32(vol->dphi, M.vdphi);

@@ -871,7 +871,7 @@ __global__ void __launch_bounds__(kThreads) k_mx_sym3(const int64_t *__restrict_
         t.y = fmaf(m01, xi.x, fmaf(m11, xi.y, m21 * xi.z));
         t.z = fmaf(m02, xi.x, fmaf(m12, xi.y, m22 * xi.z));
         t.w = 0.f;
-        atomicAdd(&q4[J], t);
+        red_add_f4(&q4[J], t);
         pq.add(2.f * d);
       } else {
         pq.add(d);
@@ -882,7 +882,7 @@ __global__ void __launch_bounds__(kThreads) k_mx_sym3(const int64_t *__restrict_
       a1 += __shfl_xor_sync(0xffffffffu, a1, o);
       a2 += __shfl_xor_sync(0xffffffffu, a2, o);
     }
-    if (lane == 0) atomicAdd(&q4[I], make_float4(a0, a1, a2, 0.f));
+    if (lane == 0) red_add_f4(&q4[I], make_float4(a0, a1, a2, 0.f));
   }
   double vv[1] = {pq.get()}, tot[1];
   if (grid_reduce<1>(vv, R, tot) && threadIdx.x == 0) {

@@ -42,6 +42,15 @@ struct Red {
   int64_t *iscal;
 };
 
+// q += v as one vector reduction in L2 without a returned value (the float4
+// atomicAdd returns the old value, whose registers the thread then holds until
+// the response arrives)
+__device__ __forceinline__ void red_add_f4(float4 *p, float4 v) {
+  asm volatile("red.relaxed.gpu.global.add.v4.f32 [%0], {%1, %2, %3, %4};" ::"l"(p), "f"(v.x), "f"(v.y), "f"(v.z),
+               "f"(v.w)
+               : "memory");
+}
+
 __device__ __forceinline__ double warp_sum(double v) {
   for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
   return v;
@@ -53,10 +62,10 @@ __device__ __forceinline__ float warp_sumf(float v) {
 
 // Block-reduce NV values, publish the block partial, and return true in the
 // last block to finish (after which tot[] holds the grid totals, summed in
-// block order).
-template <int NV>
+// block order).  CTAs of up to MAXW warps.
+template <int NV, int MAXW = kThreads / 32>
 __device__ bool grid_reduce(double (&v)[NV], const Red &R, double (&tot)[NV]) {
-  __shared__ double sh[NV][kThreads / 32];
+  __shared__ double sh[NV][MAXW];
   __shared__ bool last;
   int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   for (int k = 0; k < NV; k++) {
@@ -67,7 +76,7 @@ __device__ bool grid_reduce(double (&v)[NV], const Red &R, double (&tot)[NV]) {
   if (threadIdx.x == 0) {
     for (int k = 0; k < NV; k++) {
       double s = 0.0;
-      for (int i = 0; i < (int)(blockDim.x >> 5); i++) s += sh[k][i];  // CTAs of up to kThreads
+      for (int i = 0; i < (int)(blockDim.x >> 5); i++) s += sh[k][i];
       R.partial[(size_t)blockIdx.x * 4 + k] = s;
     }
     __threadfence();
@@ -89,7 +98,7 @@ __device__ bool grid_reduce(double (&v)[NV], const Red &R, double (&tot)[NV]) {
   __syncthreads();
   for (int k = 0; k < NV; k++) {
     double s = 0.0;
-    for (int i = 0; i < (int)(blockDim.x >> 5); i++) s += sh[k][i];  // CTAs of up to kThreads
+    for (int i = 0; i < (int)(blockDim.x >> 5); i++) s += sh[k][i];
     tot[k] = s;
   }
   if (threadIdx.x == 0) *R.counter = 0u;

@@ -62,11 +62,29 @@ def _cases():
         # hp: per-element orders in {1,2,3}, shared sides at the largest (batched run-time kernels)
         "elast3d_hp": (lambda: O.elasticity3d_hp(3, o3, E=E3h), lambda: g.elasticity3d_hp(3, o3, E=E3h)),
         "darcy2d_hp": (lambda: O.darcy_hp(6, o2, k2h), lambda: g.darcy_hp(6, o2, k2h)),
+        # a translated, non-cubic box of hexes with a position-dependent load: the shared element matrix
+        # (every element a translate of the first) with per-element load vectors
+        "poisson3d_box_p2": (lambda: _poisson3d_box_oracle(), lambda: _poisson3d_box_gpz(g)),
     }
 
 
+_BOX = dict(n=(3, 4, 2), lo=(0.25, -0.5, 1.0), hi=(1.0, 0.5, 1.3))
+
+
+def _poisson3d_box_oracle():
+    mats = [O.material(1, O.ORC_POISSON, 3, scale=1.5, forcing=O.ORC_F_SINPROD, force=(1.0, 0, 0), forcing_porder=2)]
+    return O.OracleMesh(3, _BOX["n"], _BOX["lo"], _BOX["hi"], [1, -1, -1, -1, -1, -1, -1], True, 2, mats,
+                        [O.bc(-1, 1, 0)])
+
+
+def _poisson3d_box_gpz(g):
+    mats = [(1, g.material(g.GPZ_MAT_POISSON, 3, scale=1.5, forcing=g.GPZ_F_SINPROD, force=(1.0, 0, 0),
+                           forcing_porder=2))]
+    return g.Grid(3, _BOX["n"], _BOX["lo"], _BOX["hi"], [1, -1, -1, -1, -1, -1, -1], True, 2, mats, [(-1, g.bc(0, 0))])
+
+
 CASES = ["poisson2d_p1", "poisson2d_p2", "poisson2d_p3", "darcy2d_p2", "darcy3d_p2", "elast3d_p1", "elast3d_p2",
-         "elast3d_p3", "elast3d_hp", "darcy2d_hp"]
+         "elast3d_p3", "elast3d_hp", "darcy2d_hp", "poisson3d_box_p2"]
 
 
 @pytest.fixture(scope="module")
