@@ -303,9 +303,10 @@ def run_gpu(args):
         nblk = 0
         l2_atomics = 27 * nvol + 9 * nface
         if chosen == "matrix_free_shared_matrix_tcgen05":
-            kern = ("k_mf_hex27_gm: matrix-free Q2 elasticity on a uniform grid, K_e = mu_e Khat as one tcgen05 "
-                    "kind::tf32 3xTF32 GEMM per tile of 128 elements (M 128, N 96, K 88), float4 atomics (block rows "
-                    "+ mu per element and one pass of p and q are its HBM bytes)")
+            kern = ("k_mf_hex27_gm: matrix-free Q2 elasticity on a translated grid, K_e = mu_e Khat as one tcgen05 "
+                    "kind::tf32 3xTF32 GEMM per tile of 128 elements (M 128, N 96, K 88), gatherer and scatterer warp "
+                    "groups, float4 vector reductions into q (block rows + mu per element and one pass of p and q are "
+                    "its HBM bytes)")
             # algorithmic FLOPs: the 81 x 81 product per element; the MMAs execute 3 products of the padded tile
             mf_flops = nvol * 2 * 81 * 81 + nface * 2 * 9 * 9 * 6
             mma_flops = -(-nvol // 128) * 3 * 2 * 128 * 96 * 88

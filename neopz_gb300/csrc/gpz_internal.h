@@ -209,8 +209,10 @@ struct TwoLevel {
   DBuf<double> tsub;                         // [s^3][24][24] P^T Khat_vv P for mu = 1
   DBuf<int32_t> cfix;                        // [nnode] 1: removed (touches a penalty equation)
   DBuf<double> ac;                           // [nc][nc] coarse matrix, then its inverse
-  DBuf<float> acinv32;                       // [nc][nc]
+  DBuf<float> acinv32;                       // [nc][ldc] (rows padded to 16 bytes)
+  int64_t ldc = 0;
   DBuf<float> rc, zc, z32;                   // coarse residual / correction, preconditioned residual
+  DBuf<float> boxpart;                       // [ncell][8 corners][3] the restriction's per-box sums
 };
 
 // ---------------------------------------------------------------- the context

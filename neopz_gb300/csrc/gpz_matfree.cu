@@ -711,13 +711,24 @@ __device__ __forceinline__ void tc_mma(uint32_t tm, uint64_t a, uint64_t b, uint
 __device__ __forceinline__ void tc_commit(uint64_t *mb) {
   asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(tc_smem(mb)));
 }
-__device__ __forceinline__ bool tc_wait(uint64_t *mb, uint32_t parity) {
-  uint32_t done = 0;
-  for (int it = 0; it < kTcWaitTries && !done; it++)
-    asm volatile("{\n.reg .pred p;\nmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\nselp.u32 %0, 1, 0, p;\n}\n"
-                 : "=r"(done)
-                 : "r"(tc_smem(mb)), "r"(parity));
+// non-blocking test of an mbarrier phase: the waits below poll it with a short
+// sleep instead of the potentially-suspending try_wait, so a waiting thread is
+// never parked for a system-dependent time after the phase has completed
+__device__ __forceinline__ bool mb_test(uint64_t *mb, uint32_t parity) {
+  uint32_t done;
+  asm volatile("{\n.reg .pred p;\nmbarrier.test_wait.parity.shared::cta.b64 p, [%1], %2;\nselp.u32 %0, 1, 0, p;\n}\n"
+               : "=r"(done)
+               : "r"(tc_smem(mb)), "r"(parity)
+               : "memory");
   return done != 0;
+}
+// bounded wait (kTcWaitTries polls of at most ~0.1 us apart)
+__device__ __forceinline__ bool tc_wait(uint64_t *mb, uint32_t parity) {
+  for (int it = 0; it < kTcWaitTries; it++) {
+    if (mb_test(mb, parity)) return true;
+    if (it > 16) __nanosleep(64);
+  }
+  return false;
 }
 __device__ __forceinline__ void tc_ld16(uint32_t taddr, float *v) {
   uint32_t r[16];
@@ -1097,12 +1108,9 @@ __device__ __forceinline__ void gm_bar(int id, int n) { asm volatile("bar.sync %
 // bounded wait on an mbarrier phase that also ends when another thread has aborted
 __device__ __forceinline__ bool gm_wait(uint64_t *mb, uint32_t parity, volatile int *abort) {
   for (int it = 0; it < kTcWaitTries; it++) {
-    uint32_t done;
-    asm volatile("{\n.reg .pred p;\nmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\nselp.u32 %0, 1, 0, p;\n}\n"
-                 : "=r"(done)
-                 : "r"(tc_smem(mb)), "r"(parity));
-    if (done) return true;
+    if (mb_test(mb, parity)) return true;
     if (*abort) return false;
+    if (it > 16) __nanosleep(64);
   }
   *abort = 1;
   return false;
@@ -1133,6 +1141,20 @@ __device__ __forceinline__ void gm_gather(unsigned char *sm, const int32_t *rw, 
     v[3 * a] = pv.x;
     v[3 * a + 1] = pv.y;
     v[3 * a + 2] = pv.z;
+  }
+  if (A0 == 0) {
+    // Khat annihilates translations (the eight corner shapes sum to one, the others vanish at the
+    // corners): subtracting corner 0's value from the corner coefficients leaves Y unchanged and
+    // makes the TF32 split's error relative to the element's variation instead of its mean, so smooth
+    // fields (where the element contributions nearly cancel) keep FP32 accuracy
+    static_assert(A1 >= 8, "the first half holds the eight corner shapes");
+    const float c0 = v[0], c1 = v[1], c2 = v[2];
+#pragma unroll
+    for (int a = 0; a < 8; a++) {
+      v[3 * a] -= c0;
+      v[3 * a + 1] -= c1;
+      v[3 * a + 2] -= c2;
+    }
   }
 #pragma unroll
   for (int c = 0; c < NV / 4; c++) {
@@ -1580,11 +1602,12 @@ __global__ void __launch_bounds__(256) k_gj_col(int64_t n, int64_t k0, double *_
   }
 }
 
-__global__ void k_tl_to32(int64_t n, const double *__restrict__ A, float *__restrict__ B) {
+// B[i][j] (rows of ldc floats, zero past column n) = the symmetrised FP32 copy of A
+__global__ void k_tl_to32(int64_t n, int64_t ldc, const double *__restrict__ A, float *__restrict__ B) {
   const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= n * n) return;
-  const int64_t i = t / n, j = t % n;
-  B[t] = (float)(0.5 * (A[t] + A[j * n + i]));
+  if (t >= n * ldc) return;
+  const int64_t i = t / ldc, j = t % ldc;
+  B[t] = j < n ? (float)(0.5 * (A[i * n + j] + A[j * n + i])) : 0.f;
 }
 
 template <class K>
@@ -1893,6 +1916,7 @@ int two_level_build(Ctx &c) {
   T.ncell = (int64_t)T.m[0] * T.m[1] * T.m[2];
   const int nvx = (int)T.lx[0] + 1, nvy = (int)T.lx[1] + 1;
   const int64_t nv = (int64_t)nvx * nvy * (T.lx[2] + 1);
+  if (nv >= INT32_MAX) return GPZ_E_INVALID;  // the application kernels index the vertex lattice in 32 bits
   T.vtx_eq.alloc(nv);
   GPZ_CUDA_TRY(cudaMemsetAsync(T.vtx_eq.p, 0xff, nv * sizeof(int32_t), s));
   T.el_sub.alloc(n);
@@ -1966,9 +1990,11 @@ int two_level_build(Ctx &c) {
   }
   T.tsub.upload(tab.data(), tab.size(), s);
   T.ac.alloc((size_t)T.nc * T.nc);
-  T.acinv32.alloc((size_t)T.nc * T.nc);
+  T.ldc = (T.nc + 3) / 4 * 4;
+  T.acinv32.alloc((size_t)T.nc * T.ldc);
   T.rc.alloc(T.nc);
   T.zc.alloc(T.nc);
+  T.boxpart.alloc((size_t)T.ncell * 24);
   T.z32.alloc(std::max<int64_t>(c.neq, 1));
   T.rc.zero(s);
   GPZ_CUDA_TRY(cudaStreamSynchronize(s));
@@ -1999,7 +2025,7 @@ void two_level_assemble(Ctx &c) {
     k_gj_col<<<grid_for(T.nc, 256), 256, 0, s>>>(T.nc, k0, T.ac.p);
     c.launches += 4;
   }
-  k_tl_to32<<<grid_for(nn, 256), 256, 0, s>>>(T.nc, T.ac.p, T.acinv32.p);
+  k_tl_to32<<<grid_for(T.nc * T.ldc, 256), 256, 0, s>>>(T.nc, T.ldc, T.ac.p, T.acinv32.p);
   c.launches++;
   GPZ_CUDA_TRY(cudaGetLastError());
   check_device_flag(c, "two-level coarse matrix");
@@ -2073,7 +2099,8 @@ bool matfree_build(Ctx &c) {
   check_device_flag(c, "matrix-free records");
   M.sf_ready = sf_tables(c, *vol);
   M.grid_vol = mf_grid(k_mf_hex27, kMfThreads);
-  M.grid_face = mf_grid(k_mf_faces, kThreads);
+  // a warp per face: no more CTAs than the faces fill (every CTA takes part in the energy's grid reduction)
+  M.grid_face = (int)std::max<int64_t>(1, std::min<int64_t>(mf_grid(k_mf_faces, kThreads), (M.nface + kWarps - 1) / kWarps));
   GPZ_CUDA_TRY(cudaFuncSetAttribute(k_mf_hex27_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)OFF_TC_END));
   {
     int dev = 0, nsm = 0;

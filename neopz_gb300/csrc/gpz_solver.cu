@@ -1373,16 +1373,22 @@ __global__ void __launch_bounds__(kThreads) k_vb32_r32(const double *__restrict_
 // (zc = Ac^-1 rc, dense FP32), k_tl_z (z, rho = r.z, beta); then k_tl_p.
 struct TlView {
   const int32_t *vtx_eq, *brow_vtx, *cfix;
-  const float *acinv;
+  const float *acinv;  // [nc][ldc], rows padded to 16 bytes
   float *rc, *zc, *z;
   int nvx, nvy, nvz, s, mx, my, mz;
-  int64_t nc;
+  int64_t nc, ldc;
+  float *boxpart;      // [mx my mz][8][3]
 };
+TlView tl_view(TwoLevel &T) {
+  return TlView{T.vtx_eq.p, T.brow_vtx.p, T.cfix.p, T.acinv32.p, T.rc.p, T.zc.p, T.z32.p, (int)T.lx[0] + 1,
+                (int)T.lx[1] + 1, (int)T.lx[2] + 1, T.s, T.m[0], T.m[1], T.m[2], T.nc, T.ldc, T.boxpart.p};
+}
 
 // coarse position of lattice vertex v: box (I, J, K) and its local offsets
 __device__ __forceinline__ void tl_locate(const TlView &T, int64_t v, int &I, int &J, int &K, float &tx, float &ty,
                                           float &tz) {
-  const int vi = (int)(v % T.nvx), vj = (int)((v / T.nvx) % T.nvy), vk = (int)(v / ((int64_t)T.nvx * T.nvy));
+  const int v32 = (int)v;  // the vertex lattice has fewer than 2^31 vertices (two_level_build checks)
+  const int vi = v32 % T.nvx, vj = (v32 / T.nvx) % T.nvy, vk = v32 / (T.nvx * T.nvy);
   I = min(vi / T.s, T.mx - 1);
   J = min(vj / T.s, T.my - 1);
   K = min(vk / T.s, T.mz - 1);
@@ -1395,50 +1401,99 @@ constexpr int kTlMaxSmem = 3072;  // coarse dofs kept in shared memory by the re
 
 // rc = P^T r; r64 (optional): after a residual replacement (I_UPDATE 2) the
 // FP64 residual is read instead of r (the learned flexible CG refreshes r
-// only in its z kernel, which runs after this one)
+// only in its z kernel, which runs after this one).  One CTA per coarse box:
+// the box's own vertices (lattice ranges [I s, (I + 1) s) per direction, the
+// last box also the upper boundary, as tl_locate assigns them) give its eight
+// corners' 24 sums, reduced in the CTA without atomics; the last CTA to finish
+// adds the boxes' sums into rc node by node in a fixed order (deterministic).
 __global__ void __launch_bounds__(kThreads) k_tl_restrict(const float *__restrict__ r, const double *__restrict__ r64,
                                                           TlView T, Red R) {
   if (!active(R.iscal)) return;
-  __shared__ float sr[kTlMaxSmem];
-  for (int64_t k = threadIdx.x; k < T.nc; k += blockDim.x) sr[k] = 0.f;
-  __syncthreads();
-  const int64_t nv = (int64_t)T.nvx * T.nvy * T.nvz;
-  for (int64_t v = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; v < nv; v += (int64_t)gridDim.x * blockDim.x) {
+  __shared__ float sred[kThreads / 32][24];
+  __shared__ bool last;
+  const int box = blockIdx.x;
+  const int I = box % T.mx, J = (box / T.mx) % T.my, K = box / (T.mx * T.my);
+  const int x0 = I * T.s, y0 = J * T.s, z0 = K * T.s;
+  const int cx = (I == T.mx - 1 ? T.nvx : x0 + T.s) - x0, cy = (J == T.my - 1 ? T.nvy : y0 + T.s) - y0,
+            cz = (K == T.mz - 1 ? T.nvz : z0 + T.s) - z0;
+  const float is = 1.0f / (float)T.s;
+  const bool fresh = r64 && R.iscal[I_UPDATE] == 2;
+  float acc[24];
+#pragma unroll
+  for (int k = 0; k < 24; k++) acc[k] = 0.f;
+  for (int t = threadIdx.x; t < cx * cy * cz; t += blockDim.x) {
+    const int li = t % cx, lj = (t / cx) % cy, lk = t / (cx * cy);
+    const int64_t v = (x0 + li) + (int64_t)T.nvx * ((y0 + lj) + (int64_t)T.nvy * (z0 + lk));
     const int32_t eq = T.vtx_eq[v];
     if (eq < 0) continue;
-    int I, J, K;
-    float t[3];
-    tl_locate(T, v, I, J, K, t[0], t[1], t[2]);
-    const bool fresh = r64 && R.iscal[I_UPDATE] == 2;
     const float r0 = fresh ? (float)r64[eq] : r[eq], r1 = fresh ? (float)r64[eq + 1] : r[eq + 1],
                 r2 = fresh ? (float)r64[eq + 2] : r[eq + 2];
+    const float tx = (float)li * is, ty = (float)lj * is, tz = (float)lk * is;
 #pragma unroll
     for (int cn = 0; cn < 8; cn++) {
-      const int bx = cn & 1, by = (cn >> 1) & 1, bz = cn >> 2;
-      const float w = (bx ? t[0] : 1.f - t[0]) * (by ? t[1] : 1.f - t[1]) * (bz ? t[2] : 1.f - t[2]);
-      if (w == 0.f) continue;
-      const int64_t nd = (I + bx) + (int64_t)(T.mx + 1) * ((J + by) + (int64_t)(T.my + 1) * (K + bz));
-      atomicAdd(&sr[3 * nd], w * r0);
-      atomicAdd(&sr[3 * nd + 1], w * r1);
-      atomicAdd(&sr[3 * nd + 2], w * r2);
+      const float w = ((cn & 1) ? tx : 1.f - tx) * ((cn & 2) ? ty : 1.f - ty) * ((cn & 4) ? tz : 1.f - tz);
+      acc[3 * cn] = fmaf(w, r0, acc[3 * cn]);
+      acc[3 * cn + 1] = fmaf(w, r1, acc[3 * cn + 1]);
+      acc[3 * cn + 2] = fmaf(w, r2, acc[3 * cn + 2]);
     }
   }
+  const int lane = threadIdx.x & 31, wp = threadIdx.x >> 5;
+#pragma unroll
+  for (int k = 0; k < 24; k++) {
+    const float sum = warp_sumf(acc[k]);
+    if (lane == 0) sred[wp][k] = sum;
+  }
   __syncthreads();
-  for (int64_t k = threadIdx.x; k < T.nc; k += blockDim.x)
-    if (sr[k] != 0.f) atomicAdd(&T.rc[k], sr[k]);
+  if (threadIdx.x < 24) {
+    float sum = 0.f;
+    for (int w = 0; w < (int)(blockDim.x >> 5); w++) sum += sred[w][threadIdx.x];
+    T.boxpart[(size_t)box * 24 + threadIdx.x] = sum;
+  }
+  __threadfence();
+  __syncthreads();
+  if (threadIdx.x == 0) last = atomicAdd(R.counter, 1u) == gridDim.x - 1;
+  __syncthreads();
+  if (!last) return;
+  __threadfence();
+  const volatile float *bp = T.boxpart;
+  const int nx = T.mx + 1, ny = T.my + 1;
+  for (int64_t k = threadIdx.x; k < T.nc; k += blockDim.x) {
+    const int node = (int)(k / 3), comp = (int)(k % 3);
+    const int a = node % nx, b = (node / nx) % ny, c = node / (nx * ny);
+    float sum = 0.f;
+    for (int cn = 0; cn < 8; cn++) {
+      const int bi = a - (cn & 1), bj = b - ((cn >> 1) & 1), bk = c - (cn >> 2);
+      if (bi < 0 || bj < 0 || bk < 0 || bi >= T.mx || bj >= T.my || bk >= T.mz) continue;
+      sum += bp[((size_t)(bi + T.mx * (bj + T.my * bk))) * 24 + cn * 3 + comp];
+    }
+    T.rc[k] = sum;
+  }
+  if (threadIdx.x == 0) *R.counter = 0u;
 }
 
-// zc = Ac^-1 rc (removed nodes: zero); one warp per coarse row
+// zc = Ac^-1 rc (removed nodes: zero); one warp per coarse row, float4 loads of
+// the padded rows (the padding columns are zero) against rc staged in shared memory
 __global__ void __launch_bounds__(kThreads) k_tl_csolve(TlView T, Red R) {
   if (!active(R.iscal)) return;
+  __shared__ __align__(16) float src[kTlMaxSmem];
+  for (int64_t k = threadIdx.x; k < T.ldc; k += blockDim.x) src[k] = k < T.nc ? T.rc[k] : 0.f;
+  __syncthreads();
   const int lane = threadIdx.x & 31;
+  const int64_t n4 = T.ldc / 4;
   for (int64_t row = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; row < T.nc;
        row += ((int64_t)gridDim.x * blockDim.x) >> 5) {
-    float acc = 0.f;
-    const float *a = T.acinv + row * T.nc;
-    for (int64_t j = lane; j < T.nc; j += 32) acc = fmaf(a[j], __ldcg(&T.rc[j]), acc);
-    for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
-    if (lane == 0) T.zc[row] = T.cfix[row / 3] ? 0.f : acc;
+    float acc[4] = {0.f, 0.f, 0.f, 0.f};
+    const float4 *a = (const float4 *)(T.acinv + row * T.ldc);
+    for (int64_t j = lane; j < n4; j += 32) {
+      const float4 v = a[j], x = ((const float4 *)src)[j];
+      acc[0] = fmaf(v.x, x.x, acc[0]);
+      acc[1] = fmaf(v.y, x.y, acc[1]);
+      acc[2] = fmaf(v.z, x.z, acc[2]);
+      acc[3] = fmaf(v.w, x.w, acc[3]);
+    }
+    float t = (acc[0] + acc[1]) + (acc[2] + acc[3]);
+    for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
+    if (lane == 0) T.zc[row] = T.cfix[row / 3] ? 0.f : t;
   }
 }
 
@@ -1449,6 +1504,10 @@ __global__ void __launch_bounds__(kThreads) k_tl_csolve(TlView T, Red R) {
 __global__ void __launch_bounds__(kThreads) k_tl_z(const float *__restrict__ r, Prec32 M, TlView T, int64_t nunits,
                                                    Red R) {
   if (!active(R.iscal)) return;
+  // the coarse correction (at most kTlMaxSmem values) staged in shared memory: each vertex row reads 24 of them
+  __shared__ float szc[kTlMaxSmem];
+  for (int64_t k = threadIdx.x; k < T.nc; k += blockDim.x) szc[k] = T.zc[k];
+  __syncthreads();
   KSum rz;
   for (int64_t u = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; u < nunits; u += (int64_t)gridDim.x * blockDim.x) {
     float z[3];
@@ -1463,10 +1522,10 @@ __global__ void __launch_bounds__(kThreads) k_tl_z(const float *__restrict__ r, 
         const int bx = cn & 1, by = (cn >> 1) & 1, bz = cn >> 2;
         const float w = (bx ? t[0] : 1.f - t[0]) * (by ? t[1] : 1.f - t[1]) * (bz ? t[2] : 1.f - t[2]);
         if (w == 0.f) continue;
-        const int64_t nd = (I + bx) + (int64_t)(T.mx + 1) * ((J + by) + (int64_t)(T.my + 1) * (K + bz));
-        z[0] = fmaf(w, __ldcg(&T.zc[3 * nd]), z[0]);
-        z[1] = fmaf(w, __ldcg(&T.zc[3 * nd + 1]), z[1]);
-        z[2] = fmaf(w, __ldcg(&T.zc[3 * nd + 2]), z[2]);
+        const int nd = (I + bx) + (T.mx + 1) * ((J + by) + (T.my + 1) * (K + bz));
+        z[0] = fmaf(w, szc[3 * nd], z[0]);
+        z[1] = fmaf(w, szc[3 * nd + 1], z[1]);
+        z[2] = fmaf(w, szc[3 * nd + 2], z[2]);
       }
     }
 #pragma unroll
@@ -2660,10 +2719,7 @@ struct Plan {
 void launch_tl_apply(Ctx &c, const Plan &P, Red R, cudaStream_t s) {
   SolverWork &w = c.sw;
   k_tl_r32<<<wave(k_tl_r32), kThreads, 0, s>>>(w.r.p, w.r32.p, c.neq, R);
-  int dev = 0, nsm = 0;
-  cudaGetDevice(&dev);
-  cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
-  k_tl_restrict<<<std::max(1, 2 * nsm), kThreads, 0, s>>>(w.r32.p, nullptr, P.T, R);
+  k_tl_restrict<<<P.T.mx * P.T.my * P.T.mz, kThreads, 0, s>>>(w.r32.p, nullptr, P.T, R);
   k_tl_csolve<<<wave(k_tl_csolve), kThreads, 0, s>>>(P.T, R);
   k_tl_z<<<wave(k_tl_z), kThreads, 0, s>>>(w.r32.p, P.M32, P.T, P.nunits, R);
   c.launches += 4;
@@ -2940,20 +2996,13 @@ int solve_learned(Ctx &c, const gpz_solver_opts &o, gpz_solve_report &rep, bool 
   float *zb = nullptr;
   if (ltl) {
     TwoLevel &T = c.tl;
-    TV = TlView{T.vtx_eq.p, T.brow_vtx.p, T.cfix.p, T.acinv32.p, T.rc.p, T.zc.p, T.z32.p, (int)T.lx[0] + 1,
-                (int)T.lx[1] + 1, (int)T.lx[2] + 1, T.s, T.m[0], T.m[1], T.m[2], T.nc};
+    TV = tl_view(T);
     T.rc.zero(s);
     zb = T.z32.p;
   }
-  int nsm = 0;
-  {
-    int dev = 0;
-    GPZ_CUDA_TRY(cudaGetDevice(&dev));
-    GPZ_CUDA_TRY(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
-  }
   auto apply_z32 = [&]() {
     if (ltl) {  // the coarse correction of the current residual first
-      k_tl_restrict<<<std::max(1, 2 * nsm), kThreads, 0, s>>>(w.r32.p, w.r.p, TV, R);
+      k_tl_restrict<<<TV.mx * TV.my * TV.mz, kThreads, 0, s>>>(w.r32.p, w.r.p, TV, R);
       k_tl_csolve<<<wave(k_tl_csolve), kThreads, 0, s>>>(TV, R);
       c.launches += 2;
     }
@@ -3318,8 +3367,7 @@ int solve(Ctx &c, const gpz_solver_opts &o, gpz_solve_report &rep) {
   P.tl = tl;
   if (tl) {
     TwoLevel &T = c.tl;
-    P.T = TlView{T.vtx_eq.p, T.brow_vtx.p, T.cfix.p, T.acinv32.p, T.rc.p, T.zc.p, T.z32.p, (int)T.lx[0] + 1,
-                 (int)T.lx[1] + 1, (int)T.lx[2] + 1, T.s, T.m[0], T.m[1], T.m[2], T.nc};
+    P.T = tl_view(T);
     T.rc.zero(s);
   }
   const int batch = o.check_every > 0 ? o.check_every : 32;
@@ -3451,18 +3499,13 @@ void base_coarse_apply(Ctx &c, const double *r, double *z) {
   alloc_work(c, true);
   SolverWork &w = c.sw;
   TwoLevel &T = c.tl;
-  const TlView TV{T.vtx_eq.p, T.brow_vtx.p, T.cfix.p, T.acinv32.p, T.rc.p, T.zc.p, T.z32.p, (int)T.lx[0] + 1,
-                  (int)T.lx[1] + 1, (int)T.lx[2] + 1, T.s, T.m[0], T.m[1], T.m[2], T.nc};
+  const TlView TV = tl_view(T);
   int64_t hi[I_NISCAL] = {0};
   hi[I_MAXIT] = 1;
   hi[I_UPDATE] = 2;  // the restriction reads the FP64 residual
   GPZ_CUDA_TRY(cudaMemcpyAsync(w.iscal.p, hi, sizeof(hi), cudaMemcpyHostToDevice, c.stream));
-  T.rc.zero(c.stream);
-  int dev = 0, nsm = 0;
-  GPZ_CUDA_TRY(cudaGetDevice(&dev));
-  GPZ_CUDA_TRY(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
   const Red R = red_of(c);
-  k_tl_restrict<<<std::max(1, 2 * nsm), kThreads, 0, c.stream>>>(w.r32.p, r, TV, R);
+  k_tl_restrict<<<TV.mx * TV.my * TV.mz, kThreads, 0, c.stream>>>(w.r32.p, r, TV, R);
   k_tl_csolve<<<wave(k_tl_csolve), kThreads, 0, c.stream>>>(TV, R);
   k_tl_coarse_only<<<wave(k_tl_coarse_only), kThreads, 0, c.stream>>>(TV, c.neq / 3, z);
   c.launches += 3;
@@ -3499,8 +3542,7 @@ void precond_apply(Ctx &c, int precond, const double *hr, double *hz) {
     k_to_f32<<<wave(k_to_f32), kThreads, 0, s>>>(c.d_bjinv.p, c.d_bjinv32.p, (int64_t)P.nunits * 9);
     P.M32 = Prec32{nullptr, c.d_bjinv32.p, 1};
     TwoLevel &T = c.tl;
-    P.T = TlView{T.vtx_eq.p, T.brow_vtx.p, T.cfix.p, T.acinv32.p, T.rc.p, T.zc.p, T.z32.p, (int)T.lx[0] + 1,
-                 (int)T.lx[1] + 1, (int)T.lx[2] + 1, T.s, T.m[0], T.m[1], T.m[2], T.nc};
+    P.T = tl_view(T);
     T.rc.zero(s);
     double hs[S_NSCAL] = {0};
     int64_t hi[I_NISCAL] = {0};
