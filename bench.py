@@ -55,6 +55,9 @@ SEED = 5
 # HBM bytes per stored block measured by ncu for the SpMV kernels (32^3 case):
 # k_mx_sym3 375.6 MB read + 3.3 MB written over 8,624,609 upper blocks
 NCU_TRAFFIC_PER_BLOCK = {"upper_blocks_float4_atomics": (375.615488e6 + 3.251968e6) / 8624609}
+# the shared-element-matrix operator on the 40^3 case (64,000 volume elements, one launch inside a solve):
+# dram__bytes_read.sum + dram__bytes_write.sum per volume element (profiles/matfree_shared_matrix_elasticity_q2.txt)
+NCU_TRAFFIC_PER_ELEMENT = {"matrix_free_shared_matrix_tcgen05": (24.5696e6 + 0.0) / 64000}
 
 
 def parse():
@@ -339,11 +342,13 @@ def run_gpu(args):
     pk = peaks()
     hbm = pk.get("hbm_gbs", 6800.0)
     ach = bytes32 / (ms32 * 1e-3) / 1e9
-    # ncu capture of this kernel on the 32^3 case (dram__bytes_read.sum + dram__bytes_write.sum per launch),
-    # scaled by stored blocks to this size (traffic grows in proportion to the blocks streamed)
+    # ncu capture of this kernel on a smaller case (dram__bytes_read.sum + dram__bytes_write.sum per launch),
+    # scaled to this size by the stored blocks or the volume elements it streams
     traffic = None
     if chosen in NCU_TRAFFIC_PER_BLOCK:
         traffic = int(NCU_TRAFFIC_PER_BLOCK[chosen] * nblk)
+    elif chosen in NCU_TRAFFIC_PER_ELEMENT:
+        traffic = int(NCU_TRAFFIC_PER_ELEMENT[chosen] * nvol)
 
     # exact-solution error norms (TPZAnalysis::PostProcessError) of the last solution kept on the device,
     # against u = 0: the norms (energy, L2, H1 semi) of the solution itself, the load having no closed-form
@@ -536,8 +541,9 @@ def sloan_leg(gpz, n):
 
 def poisson3d_leg(gpz, dev, n=64):
     """The 3D scalar workload: -div(k grad u) = 1 on the unit cube, 64^3 Q2 hexes (2,146,689 equations),
-    k lognormal(sigma=1) per element (seed 1), u = 0 on the boundary: FP64 assembly, then the mixed CG (FP32
-    CSR values, Jacobi) and the FP64 Jacobi-PCG, both to a true FP64 residual 1e-8."""
+    k lognormal(sigma=1) per element (seed 1), u = 0 on the boundary: FP64 assembly, then the mixed CG (the FP32
+    operator the autotuner picks: the FP32 CSR copy or the scalar shared-element-matrix tcgen05 kernel; Jacobi)
+    and the FP64 Jacobi-PCG, both to a true FP64 residual 1e-8."""
     k = gpz.lognormal(n ** 3, 1.0, 1)
     grid = gpz.darcy(3, n, 2, k)
     ctx = gpz.Context(dev)
@@ -547,15 +553,20 @@ def poisson3d_leg(gpz, dev, n=64):
     ms = ctx.time_kernel(gpz.GPZ_KERNEL_ASSEMBLE, 3)
     f64 = ctx.solve(tol=TOL, max_iter=200000, check_every=64, want_x=False)
     ctx.assemble(gpz.GPZ_PREC_MIXED)
-    mx = ctx.solve(solver=gpz.GPZ_SOLVER_MIXED_CG, tol=TOL, max_iter=200000, reliable_delta=1e-2, check_every=64,
-                   want_x=False)
+    for _ in range(2):  # the second is timed (graphs instantiated)
+        mx = ctx.solve(solver=gpz.GPZ_SOLVER_MIXED_CG, tol=TOL, max_iter=200000, reliable_delta=1e-2,
+                       check_every=64, want_x=False)
+    tune = ctx.tuning_report()
+    op_ms = ctx.time_kernel(gpz.GPZ_KERNEL_SPMV_FP32, 20)
     ctx.close()
     return {"workload": f"3D Darcy/Poisson {n}^3 hex Q2, k lognormal(sigma=1) seed 1, u = 0 on the boundary (penalty)",
             "neq": grid.neq, "nnz_upper": nnz, "assembly_fp64_s": ms / 1e3, "volume_elements_per_s": n ** 3 / (ms / 1e3),
             "fp64_jacobi_pcg": {"iterations": f64["iterations"], "seconds": f64["seconds"],
                                 "true_resid": f64["true_resid"]},
             "mixed_cg": {"iterations": mx["iterations"], "seconds": mx["seconds"], "true_resid": mx["true_resid"],
-                         "speedup_vs_fp64_jacobi_pcg": f64["seconds"] / mx["seconds"] if mx["seconds"] else None}}
+                         "speedup_vs_fp64_jacobi_pcg": f64["seconds"] / mx["seconds"] if mx["seconds"] else None,
+                         "fp32_operator": tune.get("chosen"), "operator_autotune_ms": tune,
+                         "operator_ms_per_launch": op_ms}}
 
 
 def learned_leg(gpz, dev, n=256, seeds=(10000, 10001, 10002)):

@@ -318,7 +318,9 @@ typedef struct {
                               6 the same on the tensor cores (tcgen05, 3xTF32),
                               7 the same sum-factorised on Lagrange nodal values,
                               8 the same when every element has one affine Jacobian (uniform grid):
-                                K_e = mu_e Khat as one tcgen05 3xTF32 GEMM per tile of elements */
+                                K_e = mu_e Khat as one tcgen05 3xTF32 GEMM per tile of elements;
+                              scalar problems (Poisson, Darcy): 0 the FP32 CSR copy, 9 the scalar
+                                counterpart of 8 (3D Q2 hexes, K_e = k_e Khat, penalty faces) */
 } gpz_solver_opts;
 
 typedef struct {
@@ -392,6 +394,14 @@ int gpz_error_evaluate(gpz_ctx *ctx, int32_t exact_order, const double *sol, con
 /* JSON text of the SpMV autotuner's measurements (ms per launch of every
  * candidate layout / kernel of the mixed CG) for the assembled system. */
 int gpz_tuning_report(gpz_ctx *ctx, char *buf, int64_t len);
+/* On-disk cache of the autotuners' choices (the FP32 operator layout of the
+ * mixed solves, the block size of the hp element kernels): with a file set, a
+ * pattern whose key (tuner, device, sizes, a hash of the mesh connectivity,
+ * tuner version) is in the file takes the stored choice instead of timing the
+ * candidates, and a new measurement is appended (JSON lines; the reports then
+ * carry "cached": true).  NULL: no cache (the default).  An unreadable or
+ * unwritable file only means the tuners measure again. */
+int gpz_tuning_cache(gpz_ctx *ctx, const char *path);
 /* JSON text of the element batching: uniform-order buckets (compile-time
  * kernels), hp classes (elements of uneven side orders sharing the table of
  * the full element of their largest order, one run-time kernel per class and

@@ -493,7 +493,7 @@ int gpz_spmv(gpz_ctx *ctx, double alpha, const double *x, double beta, const dou
 int gpz_spmv_fp32(gpz_ctx *ctx, int variant, const double *x, double *y) {
   return guarded(ctx, [&](Ctx &c) {
     GPZ_REQUIRE(c.have_matrix, GPZ_E_NOT_READY, "not assembled");
-    GPZ_REQUIRE(x && y && variant >= -1 && variant <= 8, GPZ_E_INVALID, "arguments");
+    GPZ_REQUIRE(x && y && variant >= -1 && variant <= 9, GPZ_E_INVALID, "arguments");
     spmv32_apply(c, variant, x, y);
     return GPZ_OK;
   });
@@ -557,6 +557,13 @@ int gpz_time_kernel(gpz_ctx *ctx, int which, int reps, double *ms_per_launch) {
     } else {
       GPZ_REQUIRE(false, GPZ_E_INVALID, "kernel id");
     }
+    return GPZ_OK;
+  });
+}
+
+int gpz_tuning_cache(gpz_ctx *ctx, const char *path) {
+  return guarded(ctx, [&](Ctx &c) {
+    c.tune_cache = path ? std::string(path) : std::string();
     return GPZ_OK;
   });
 }

@@ -883,6 +883,20 @@ void assemble_fp64(Ctx &c) {
   // summation order) and keep the fastest
   bool tune = false;
   for (Bucket *b : c.buckets) tune |= b->hp && !b->tuned;
+  std::string key;
+  if (tune && !c.tune_cache.empty()) {
+    key = tune_key(c, "hp_block");
+    const int cached = tune_cache_lookup(c, key);
+    if (cached > 0) {  // a block size stored by an earlier run on this device and mesh
+      for (Bucket *b : c.buckets)
+        if (b->hp) {
+          b->threads = cached;
+          b->tuned = true;
+        }
+      c.asm_tune_report = "{\"cached\": true, \"chosen\": " + std::to_string(cached) + "}";
+      tune = false;
+    }
+  }
   if (tune) {
     const int cand[3] = {64, 128, 256};
     float best = 1e30f;
@@ -914,6 +928,7 @@ void assemble_fp64(Ctx &c) {
         b->tuned = true;
       }
     c.asm_tune_report = rep + ", \"chosen\": " + std::to_string(best_t) + "}";
+    if (!key.empty()) tune_cache_store(c, key, best_t, c.asm_tune_report);
   }
   c.d_dinv.alloc(std::max<int64_t>(c.neq, 1));
   auto body = [&](bool set_attrs) {

@@ -186,6 +186,22 @@ struct MatFree {
   DBuf<int> gm_flag;
 };
 
+// scalar shared element matrix (3D Q2 Darcy / Poisson on translated grids):
+// K_e = k_e Khat, Khat (27 x 27, coefficient 1) split into TF32 hi / lo
+struct MatFree1 {
+  bool ready = false;
+  int64_t nvol = 0, nface = 0;
+  int ntab = 0, grid = 1, grid_face = 1;
+  DBuf<int32_t> vrows;                       // [ntile * 128][27] equations, -1 padding
+  DBuf<float> vcoef;                         // [ntile * 128] element coefficient (k, or 1)
+  DBuf<float> b;                             // [2][32 x 32] Khat hi, lo (K-major core matrices)
+  DBuf<float> fxyz, ftabs;                   // penalty faces: corners, stacked per-bucket tables
+  DBuf<int32_t> frows;
+  DBuf<uint8_t> ftab;                        // table of each face
+  DBuf<double> energy;
+  float big = 0.f;
+};
+
 // ---------------------------------------------------------------- two-level preconditioner
 // Additive two-level block Jacobi for uniform Q2 hex grids (every volume
 // element a translate of one axis-aligned box): M = B^-1 + P Ac^-1 P^T with B
@@ -311,6 +327,7 @@ struct Ctx {
   uint32_t tma_vcap = 0, tma_ccap = 0;       // shared-memory stage capacities of the TMA-staged kernel
   int tma_grid = 1;
   std::string tune_report;
+  std::string tune_cache;                    // file of autotuner choices (gpz_tuning_cache), empty: none
   int64_t nbrow = 0;
   DBuf<int64_t> d_bptr, d_uptr;              // block CSR and its upper triangle: [nbrow+1]
   DBuf<int32_t> d_ucol;
@@ -344,6 +361,7 @@ struct Ctx {
   bool have_solution = false;
   Learned ln;
   MatFree mf;
+  MatFree1 mf1;
   ErrorEval er;
 
   ~Ctx();
@@ -382,6 +400,8 @@ int collect_cg_pairs(Ctx &c, int npairs, double tol, int64_t max_iter, double *R
                      int64_t *iters);
 // matfree.cu
 bool matfree_build(Ctx &c);
+bool matfree1_build(Ctx &c);
+void matfree1_spmv(Ctx &c, cudaStream_t s, const float *p, float *q);
 int two_level_build(Ctx &c);     // geometry part (once per mesh); GPZ_OK or GPZ_E_INVALID when not a uniform grid
 void two_level_assemble(Ctx &c); // coarse matrix and its inverse for the current assembly
 void matfree_spmv(Ctx &c, cudaStream_t s, int mode);  // 0 CUDA cores, 1 tcgen05, 2 sum-factorised, 3 shared matrix
@@ -391,6 +411,11 @@ void ensure_node_incidence(Ctx &c);                // features, scaling and fact
 // scan.cu
 void exclusive_scan_i64(const int64_t *in, int64_t *out, int64_t n, cudaStream_t s, Ctx &c);
 void check_device_flag(Ctx &c, const char *where);
+// on-disk cache of the autotuners' choices (gpz_tune_cache.cpp): the key of the
+// current mesh, pattern and device for one tuner; a stored choice or -1; a new one
+std::string tune_key(Ctx &c, const char *tuner);
+int tune_cache_lookup(const Ctx &c, const std::string &key);
+void tune_cache_store(const Ctx &c, const std::string &key, int choice, const std::string &report);
 
 inline int grid_for(int64_t n, int threads) {
   int64_t g = (n + threads - 1) / threads;

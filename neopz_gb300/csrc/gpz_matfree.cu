@@ -2032,6 +2032,370 @@ void two_level_assemble(Ctx &c) {
   T.have_inv = true;
 }
 
+// ---------------------------------------------------------------- scalar shared element matrix (3D Q2 Darcy / Poisson)
+// The scalar counterpart of k_mf_hex27_gm for TPZMatPoisson / TPZDarcyFlow on a
+// grid of translated Q2 hexes: K_e = k_e Khat (27 x 27; Khat the assembly's
+// reference element matrix at coefficient 1, the Poisson scale included), so the
+// operator over a tile of 128 elements is Y = U Khat^T: tcgen05.mma kind::tf32,
+// 3xTF32, M 128, N 32, K 32.  A 256-thread CTA (three per SM, persistent over
+// tiles) runs the same two-stage pipeline as the elasticity kernel with one
+// thread per element in each group: 4 gatherer warps (rows copied as one block,
+// the element's 27 values gathered, the translation removed -- Khat annihilates
+// constants -- and split into the A operand; thread 0 issues the MMAs into
+// accumulator pair k mod 2) and 4 scatterer warps (lane quarter = warp, 32
+// columns read from TMEM, k_e Y added to q with scalar reductions, the element
+// energy for p.q).  The penalty faces of every Dirichlet side are applied by
+// k_mf_faces1 before it.
+namespace {
+constexpr int kG1Threads = 256, kG1Group = 128, kG1El = 128, kG1K = 32, kG1N = 32;
+constexpr uint32_t kG1Small = 32;  // TMEM column offset of the correction accumulator (buffer b at 64 b)
+constexpr uint32_t kG1B = kG1N * kG1K * 4, kG1A = kG1El * kG1K * 4, kG1R = kG1El * kNS * 4;
+constexpr uint32_t G1_BH = 0, G1_BL = kG1B, G1_AH = 2048 * 4, G1_AL = G1_AH + kG1A;
+constexpr uint32_t G1_RG = G1_AL + kG1A, G1_RS = G1_RG + kG1R, G1_END = G1_RS + kG1R;
+static_assert(G1_AH >= 2 * kG1B && G1_AH % 1024 == 0 && G1_AL % 1024 == 0 && G1_RG % 16 == 0, "operand alignment");
+constexpr int kF1MaxTab = 16;  // face tables (one per penalty face bucket)
+
+__device__ __forceinline__ void red_add_f1(float *p, float v) {
+  asm volatile("red.relaxed.gpu.global.add.f32 [%0], %1;" ::"l"(p), "f"(v) : "memory");
+}
+
+// rows[i][a] (equation of shape a), coef[i] (the element's k, or 1), padded to whole tiles with -1 / 0
+__global__ void k_mf1_records(int64_t n, const int64_t *__restrict__ elems, const int64_t *__restrict__ el_conn,
+                              const int64_t *__restrict__ bpos, const int *__restrict__ sside,
+                              const int *__restrict__ sk, const double *__restrict__ coef, double cconst,
+                              int32_t *__restrict__ rows, float *__restrict__ rcoef) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const int64_t e = elems[i];
+  for (int a = 0; a < kNS; a++) rows[i * kNS + a] = (int32_t)(bpos[el_conn[e * 27 + sside[a]]] + sk[a]);
+  rcoef[i] = (float)(coef ? coef[e] : cconst);
+}
+
+// face records of a scalar problem: corners [i][4][3] and the equation of each of the 9 shapes
+__global__ void k_mf1_face_records(int64_t n, const int64_t *__restrict__ elems, const int64_t *__restrict__ el_nodes,
+                                   const double *__restrict__ xyz, const int64_t *__restrict__ el_conn,
+                                   const int64_t *__restrict__ bpos, const int *__restrict__ sside,
+                                   const int *__restrict__ sk, float *__restrict__ rxyz, int32_t *__restrict__ rows) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const int64_t e = elems[i];
+  for (int k = 0; k < 4; k++)
+    for (int j = 0; j < 3; j++) rxyz[(i * 4 + k) * 3 + j] = (float)xyz[el_nodes[e * 8 + k] * 3 + j];
+  for (int a = 0; a < kFS; a++) rows[i * kFS + a] = (int32_t)(bpos[el_conn[e * 27 + sside[a]]] + sk[a]);
+}
+
+// penalty faces of a scalar problem: y_a += big sum_q w |J| phi_a phi_b u_b, one warp per face, the face's
+// table (its bucket's shapes, gradients and weights) by index; their energy to *energy
+__global__ void __launch_bounds__(kThreads) k_mf_faces1(int64_t n, const float *__restrict__ rxyz,
+                                                        const int32_t *__restrict__ rows, const uint8_t *__restrict__ tab,
+                                                        const float *__restrict__ tabs, int ntab, float big,
+                                                        const float *__restrict__ p, float *__restrict__ q,
+                                                        double *__restrict__ energy, Red R) {
+  if (!active(R.iscal)) return;
+  constexpr int kTab = kFQ * kFS + kFQ * 2 * kFS + kFQ;  // phi, dphi, w
+  __shared__ float st[kF1MaxTab * kTab];
+  __shared__ float su[kWarps][kFS], sc[kWarps][12], sq[kWarps][kFQ];
+  for (int k = threadIdx.x; k < ntab * kTab; k += blockDim.x) st[k] = tabs[k];
+  __syncthreads();
+  const int lane = threadIdx.x & 31, wp = threadIdx.x >> 5;
+  KSum en;
+  for (int64_t i = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; i < n;
+       i += ((int64_t)gridDim.x * blockDim.x) >> 5) {
+    const float *T = st + (int)tab[i] * kTab, *phi = T, *dphi = T + kFQ * kFS, *w = dphi + kFQ * 2 * kFS;
+    int32_t row = 0;
+    float u = 0.f;
+    if (lane < kFS) {
+      row = rows[i * kFS + lane];
+      u = p[row];
+      su[wp][lane] = u;
+    }
+    if (lane < 12) sc[wp][lane] = rxyz[i * 12 + lane];
+    __syncwarp();
+    if (lane < kFQ) {
+      const int qp = lane;
+      float g0[3] = {0.f, 0.f, 0.f}, g1[3] = {0.f, 0.f, 0.f};
+      for (int k = 0; k < 4; k++)
+        for (int j = 0; j < 3; j++) {
+          g0[j] += sc[wp][k * 3 + j] * dphi[(qp * 2 + 0) * kFS + k];
+          g1[j] += sc[wp][k * 3 + j] * dphi[(qp * 2 + 1) * kFS + k];
+        }
+      const float cx = g0[1] * g1[2] - g0[2] * g1[1], cy = g0[2] * g1[0] - g0[0] * g1[2],
+                  cz = g0[0] * g1[1] - g0[1] * g1[0];
+      float uq = 0.f;
+      for (int b = 0; b < kFS; b++) uq += phi[qp * kFS + b] * su[wp][b];
+      sq[wp][qp] = big * w[qp] * sqrtf(cx * cx + cy * cy + cz * cz) * uq;
+    }
+    __syncwarp();
+    if (lane < kFS) {
+      float y = 0.f;
+      for (int qp = 0; qp < kFQ; qp++) y += sq[wp][qp] * phi[qp * kFS + lane];
+      en.add(y * u);
+      red_add_f1(&q[row], y);
+    }
+    __syncwarp();
+  }
+  double v[1] = {en.get()}, tot[1];
+  if (grid_reduce<1>(v, R, tot) && threadIdx.x == 0) *energy = tot[0];
+}
+
+__device__ __forceinline__ void g1_mma(uint32_t tm, uint32_t ah, uint32_t al, uint32_t bh, uint32_t bl) {
+  const uint32_t id = (1u << 4) | (2u << 7) | (2u << 10) | ((uint32_t)(kG1N >> 3) << 17) | ((uint32_t)(kG1El >> 4) << 24);
+  constexpr uint32_t sbo = (kG1K / 4) * 128;
+#pragma unroll 1
+  for (int k = 0; k < kG1K / 8; k++) {
+    const uint64_t dah = tc_desc(ah + k * 256, sbo), dal = tc_desc(al + k * 256, sbo);
+    const uint64_t dbh = tc_desc(bh + k * 256, sbo), dbl = tc_desc(bl + k * 256, sbo);
+    tc_mma(tm + kG1Small, dal, dbh, id, k > 0);
+    tc_mma(tm + kG1Small, dah, dbl, id, 1u);
+    tc_mma(tm, dah, dbh, id, k > 0);
+  }
+}
+
+// rows: [ntile * 128][27] equations, -1 past the n elements; coef [ntile * 128]
+__global__ void __launch_bounds__(kG1Threads, 2) k_mf_hex27_gm1(int64_t n, const int32_t *__restrict__ rows,
+                                                                const float *__restrict__ coef,
+                                                                const float4 *__restrict__ bsplit,
+                                                                const float *__restrict__ p, float *__restrict__ q,
+                                                                const double *__restrict__ face_energy,
+                                                                int *__restrict__ err, Red R) {
+  if (!active(R.iscal)) return;
+  extern __shared__ __align__(1024) unsigned char sm[];
+  __shared__ uint32_t s_tmem;
+  __shared__ volatile int s_abort;
+  __shared__ __align__(8) uint64_t s_done[2], s_free[2];
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const bool gatherer = tid < kG1Group;
+  const int gl = tid & (kG1Group - 1);
+  const int4 *rows4 = (const int4 *)rows;
+  for (uint32_t i = tid; i < 2 * kG1B / 16; i += kG1Threads) ((float4 *)(sm + G1_BH))[i] = bsplit[i];
+  asm volatile("fence.proxy.async.shared::cta;");
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(tc_smem(&s_tmem)), "r"(128));
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+  }
+  if (tid == 0) {
+    s_abort = 0;
+    for (int b = 0; b < 2; b++) {
+      asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(tc_smem(&s_done[b])));
+      asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(tc_smem(&s_free[b])), "r"(kG1Group));
+    }
+    asm volatile("fence.mbarrier_init.release.cluster;");
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;");
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;");
+  const uint32_t tm = s_tmem;
+  const uint32_t ah = tc_smem(sm + G1_AH), al = tc_smem(sm + G1_AL), bh = tc_smem(sm + G1_BH),
+                 bl = tc_smem(sm + G1_BL);
+  const int64_t ntile = (n + kG1El - 1) / kG1El;
+  constexpr int n4 = (int)(kG1R / 16);
+  KSum en;
+  int last = -1;
+  if (gatherer) {
+    const int32_t *rw = (const int32_t *)(sm + G1_RG);
+    int k = 0;
+    for (int64_t tile = blockIdx.x; tile < ntile; tile += gridDim.x, k++) {
+      const int b = k & 1;
+      for (int i = gl; i < n4; i += kG1Group) ((int4 *)(sm + G1_RG))[i] = rows4[(size_t)tile * n4 + i];
+      bool ok = true;
+      if (gl == 0 && k >= 2) ok = gm_wait(&s_free[b], (uint32_t)((k - 2) >> 1) & 1u, &s_abort);
+      if (ok && k >= 1) ok = gm_wait(&s_done[(k - 1) & 1], (uint32_t)((k - 1) >> 1) & 1u, &s_abort);
+      if (!gm_vote(1, kG1Group, ok)) break;
+      float v[kG1K];
+#pragma unroll
+      for (int a = 0; a < kG1K; a++) v[a] = 0.f;
+#pragma unroll
+      for (int a = 0; a < kNS; a++) {
+        const int32_t r = rw[gl * kNS + a];
+        v[a] = r >= 0 ? p[r] : 0.f;
+      }
+      // Khat annihilates constants (the corner shapes sum to one): remove corner 0's value from the
+      // corner coefficients so the TF32 split's error is relative to the element's variation
+      const float c0 = v[0];
+#pragma unroll
+      for (int a = 0; a < 8; a++) v[a] -= c0;
+#pragma unroll
+      for (int c = 0; c < kG1K / 4; c++) {
+        float4 lo;
+        const float4 hi = tf32_split4(make_float4(v[4 * c], v[4 * c + 1], v[4 * c + 2], v[4 * c + 3]), lo);
+        const uint32_t off = kmaj(gl, 4 * c, kG1K);
+        *(float4 *)(sm + G1_AH + off) = hi;
+        *(float4 *)(sm + G1_AL + off) = lo;
+      }
+      asm volatile("fence.proxy.async.shared::cta;");
+      gm_bar(1, kG1Group);
+      if (gl == 0) {
+        asm volatile("tcgen05.fence::after_thread_sync;");
+        g1_mma(tm + (uint32_t)b * 64u, ah, al, bh, bl);
+        tc_commit(&s_done[b]);
+        last = k;
+      }
+    }
+  } else {
+    const int32_t *rw = (const int32_t *)(sm + G1_RS);
+    const int quarter = warp - kG1Group / 32, le = quarter * 32 + lane;
+    int k = 0;
+    for (int64_t tile = blockIdx.x; tile < ntile; tile += gridDim.x, k++) {
+      const int b = k & 1;
+      for (int i = gl; i < n4; i += kG1Group) ((int4 *)(sm + G1_RS))[i] = rows4[(size_t)tile * n4 + i];
+      const bool ok = gm_wait(&s_done[b], (uint32_t)(k >> 1) & 1u, &s_abort);
+      if (!gm_vote(2, kG1Group, ok)) break;
+      asm volatile("tcgen05.fence::after_thread_sync;");
+      const uint32_t taddr = tm + ((uint32_t)(quarter * 32) << 16) + (uint32_t)b * 64u;
+      float y[32], t[16];
+      tc_ld16(taddr, y);
+      tc_ld16(taddr + 16, y + 16);
+      tc_ld16(taddr + kG1Small, t);
+#pragma unroll
+      for (int j = 0; j < 16; j++) y[j] += t[j];
+      tc_ld16(taddr + kG1Small + 16, t);
+#pragma unroll
+      for (int j = 0; j < 16; j++) y[16 + j] += t[j];
+      const int64_t e = tile * kG1El + le;
+      if (e < n) {
+        const float ke = coef[e];
+#pragma unroll
+        for (int a = 0; a < kNS; a++) {
+          const int32_t r = rw[le * kNS + a];
+          const float ya = ke * y[a];
+          en.add(ya * p[r]);
+          red_add_f1(&q[r], ya);
+        }
+      }
+      asm volatile("tcgen05.fence::before_thread_sync;");
+      asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(tc_smem(&s_free[b])) : "memory");
+      gm_bar(2, kG1Group);
+    }
+  }
+  __syncthreads();
+  const bool failed = s_abort != 0;
+  if (failed && tid == 0) {
+    atomicOr(err, 16384);
+    if (last >= 0) tc_wait(&s_done[last & 1], (uint32_t)(last >> 1) & 1u);
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;");
+  __syncthreads();
+  if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tm), "r"(128));
+  double vv[1] = {failed ? 0.0 : en.get()}, tot[1];
+  if (grid_reduce<1>(vv, R, tot) && threadIdx.x == 0) {
+    const double pq = tot[0] + (face_energy ? *face_energy : 0.0);
+    R.scal[S_PQ] = pq;
+    R.scal[S_ALPHA] = R.scal[S_RHO] / pq;
+    R.iscal[I_SP32]++;
+  }
+}
+}  // namespace
+
+// Records of the scalar shared-matrix operator; false when the mesh is not one
+// bucket of translated Q2 hexes of a scalar material (its reference matrix from
+// the shared-matrix assembly) with penalty-Dirichlet or Neumann quad faces.
+bool matfree1_build(Ctx &c) {
+  MatFree1 &M = c.mf1;
+  M.ready = false;
+  if (c.nstate != 1 || c.dim != 3 || c.flt.active) return false;
+  Bucket *vol = nullptr;
+  std::vector<Bucket *> faces;
+  for (Bucket *b : c.buckets) {
+    if (b->hp) return false;
+    const int mi = c.h_el_mat[b->elems[0]];
+    if (!b->key.is_bc) {
+      if (vol || b->key.type != GPZ_EL_HEX || b->nshape != kNS || b->shared != 1 ||
+          (b->key.mat_kind != GPZ_MAT_POISSON && b->key.mat_kind != GPZ_MAT_DARCY))
+        return false;
+      vol = b;
+    } else {
+      const gpz_bc &bc = c.bcs[-mi - 1];
+      if (bc.type == 1) continue;  // Neumann: load vector only
+      if (bc.type != 0 || b->key.type != GPZ_EL_QUAD || b->nshape != kFS || b->nq != kFQ) return false;
+      faces.push_back(b);
+    }
+  }
+  if (!vol || (int)faces.size() > kF1MaxTab) return false;
+  cudaStream_t s = c.stream;
+  const gpz_material &m = c.mats[c.h_el_mat[vol->elems[0]]];
+  M.nvol = (int64_t)vol->elems.size();
+  const size_t npad = (size_t)((M.nvol + kG1El - 1) / kG1El) * kG1El;
+  M.vrows.alloc(npad * kNS);
+  GPZ_CUDA_TRY(cudaMemsetAsync(M.vrows.p, 0xFF, npad * kNS * sizeof(int32_t), s));
+  M.vcoef.alloc(npad);
+  M.vcoef.zero(s);
+  const bool darcy = m.kind == GPZ_MAT_DARCY;
+  k_mf1_records<<<grid_for(M.nvol, 256), 256, 0, s>>>(M.nvol, vol->d_elems.p, c.d_el_conn.p, c.d_block_pos.p,
+                                                      vol->d_shape_side.p, vol->d_shape_k.p,
+                                                      darcy ? c.d_coef.p : nullptr, darcy ? m.coef_const : 1.0,
+                                                      M.vrows.p, M.vcoef.p);
+  c.launches++;
+  // Khat: the shared-matrix assembly's reference element matrix (coefficient 1), split into TF32 hi / lo
+  std::vector<double> K((size_t)kNS * kNS);
+  GPZ_CUDA_TRY(cudaMemcpyAsync(K.data(), vol->d_kref.p, K.size() * sizeof(double), cudaMemcpyDeviceToHost, s));
+  GPZ_CUDA_TRY(cudaStreamSynchronize(s));
+  std::vector<float> hl(2 * kG1B / 4, 0.f);
+  for (int nn = 0; nn < kNS; nn++)
+    for (int k = 0; k < kNS; k++) {
+      const double v = K[(size_t)nn * kNS + k];
+      const float hi = tf32_round_host((float)v);
+      const float lo = tf32_round_host((float)(v - (double)hi));
+      const uint32_t off = kmaj(nn, k, kG1K) / 4;
+      hl[off] = hi;
+      hl[kG1B / 4 + off] = lo;
+    }
+  M.b.upload(hl.data(), hl.size(), s);
+  // penalty faces: records of every Dirichlet bucket, each with its own table
+  M.nface = 0;
+  for (Bucket *f : faces) M.nface += (int64_t)f->elems.size();
+  M.ntab = (int)faces.size();
+  if (M.nface) {
+    M.fxyz.alloc((size_t)M.nface * 12);
+    M.frows.alloc((size_t)M.nface * kFS);
+    M.ftab.alloc((size_t)M.nface);
+    std::vector<float> tabs;
+    std::vector<uint8_t> ftab;
+    int64_t off = 0;
+    for (int t = 0; t < (int)faces.size(); t++) {
+      Bucket *f = faces[t];
+      const int64_t nf = (int64_t)f->elems.size();
+      k_mf1_face_records<<<grid_for(nf, 256), 256, 0, s>>>(nf, f->d_elems.p, c.d_el_nodes.p, c.d_xyz.p,
+                                                           c.d_el_conn.p, c.d_block_pos.p, f->d_shape_side.p,
+                                                           f->d_shape_k.p, M.fxyz.p + off * 12, M.frows.p + off * kFS);
+      c.launches++;
+      for (double x : f->phi) tabs.push_back((float)x);
+      for (double x : f->dphi) tabs.push_back((float)x);
+      for (double x : f->w) tabs.push_back((float)x);
+      ftab.insert(ftab.end(), (size_t)nf, (uint8_t)t);
+      off += nf;
+    }
+    M.ftab.upload(ftab.data(), ftab.size(), s);
+    M.ftabs.upload(tabs.data(), tabs.size(), s);
+    M.energy.alloc(1);
+  }
+  M.big = (float)m.bignumber;
+  GPZ_CUDA_TRY(cudaGetLastError());
+  check_device_flag(c, "scalar matrix-free records");
+  GPZ_CUDA_TRY(cudaFuncSetAttribute(k_mf_hex27_gm1, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)G1_END));
+  int dev = 0, nsm = 0;
+  GPZ_CUDA_TRY(cudaGetDevice(&dev));
+  GPZ_CUDA_TRY(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
+  M.grid = std::max(1, std::min(kGridBlocks, 2 * nsm));  // two 67 KB CTAs per SM
+  M.grid_face = (int)std::max<int64_t>(1, std::min<int64_t>(mf_grid(k_mf_faces1, kThreads), (M.nface + kWarps - 1) / kWarps));
+  M.ready = true;
+  return true;
+}
+
+// q = A32 p for the scalar shared-matrix operator (q zeroed by the caller), p.q and alpha
+void matfree1_spmv(Ctx &c, cudaStream_t s, const float *p, float *q) {
+  MatFree1 &M = c.mf1;
+  SolverWork &w = c.sw;
+  Red R{w.partial.p, w.counter.p, w.scal.p, w.iscal.p};
+  if (M.nface) {
+    k_mf_faces1<<<M.grid_face, kThreads, 0, s>>>(M.nface, M.fxyz.p, M.frows.p, M.ftab.p, M.ftabs.p, M.ntab, M.big, p,
+                                                 q, M.energy.p, R);
+    c.launches++;
+  }
+  k_mf_hex27_gm1<<<M.grid, kG1Threads, G1_END, s>>>(M.nvol, M.vrows.p, M.vcoef.p, (const float4 *)M.b.p, p, q,
+                                                    M.nface ? M.energy.p : nullptr, c.d_err.p, R);
+  c.launches++;
+}
+
 // Build the element records of the matrix-free operator; false when the mesh
 // is not made of uniform Q2 hex elasticity elements plus penalty / traction faces.
 bool matfree_build(Ctx &c) {

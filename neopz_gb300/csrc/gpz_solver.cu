@@ -2330,6 +2330,9 @@ void launch_spmv32(Ctx &c, int v, const Ctx::Sell &S, Red R, cudaStream_t s) {
   c.launches++;
 }
 
+const char *spmv32_name(int v);
+void tune_scalar32(Ctx &c, int only, bool timing);
+
 // Autotuner of the mixed CG's SpMV: every candidate layout / kernel is built
 // and timed (CUDA events, 5 launches after 2 warm-up launches) on this matrix;
 // the fastest is kept and the other layouts are released.
@@ -2498,11 +2501,8 @@ void tune_spmv32(Ctx &c, int only, bool timing) {
   if (c.d_uptr.p) {
     GPZ_CUDA_TRY(cudaMemcpy(&nu, c.d_uptr.p + c.nbrow, sizeof(int64_t), cudaMemcpyDeviceToHost));
   }
-  const char *names[9] = {"block_csr", "block_csr_2rows", "sliced_ell", "block_csr_tma_staged",
-                          "upper_blocks_float4_atomics", "matrix_free_elements", "matrix_free_tcgen05_3xtf32",
-                          "matrix_free_sum_factorised", "matrix_free_shared_matrix_tcgen05"};
   if (!pruned.empty()) rep += ", \"pruned_by_byte_floor_ms\": {" + pruned + "}";
-  c.tune_report = rep + ", \"chosen\": \"" + names[res[best].v] + "\", \"block_rows\": " + std::to_string(c.nbrow) +
+  c.tune_report = rep + ", \"chosen\": \"" + spmv32_name(res[best].v) + "\", \"block_rows\": " + std::to_string(c.nbrow) +
                   ", \"blocks_full\": " + std::to_string(c.nnz / 9) + ", \"blocks_upper\": " + std::to_string(nu) +
                   "}";
   finish_layout(c, cand, res[best].window == windows[0] ? 0 : 1);
@@ -2535,6 +2535,13 @@ void finish_layout(Ctx &c, Ctx::Sell *cand, int k) {
   }
 }
 
+const char *spmv32_name(int v) {
+  static const char *names[9] = {"block_csr", "block_csr_2rows", "sliced_ell", "block_csr_tma_staged",
+                                 "upper_blocks_float4_atomics", "matrix_free_elements", "matrix_free_tcgen05_3xtf32",
+                                 "matrix_free_sum_factorised", "matrix_free_shared_matrix_tcgen05"};
+  return v >= 0 && v < 9 ? names[v] : "unknown";
+}
+
 void make_fp32_copy(Ctx &c, int variant) {
   c.have_bsr3 = false;
   if (blocks_are_3(c)) {
@@ -2550,17 +2557,99 @@ void make_fp32_copy(Ctx &c, int variant) {
     check_device_flag(c, "3x3 block CSR");
     c.have_bsr3 = true;
     c.d_a32.release();
+    std::string key;
+    int cached = -1;
+    if (variant < 0 && c.spmv32_tuned < 0 && !c.tune_cache.empty()) {
+      key = tune_key(c, "spmv32");
+      cached = tune_cache_lookup(c, key);
+    }
     if (variant < 0 && c.spmv32_tuned >= 0) {
       tune_spmv32(c, c.spmv32_tuned, false);  // same pattern: rebuild the chosen layout only
+    } else if (cached >= 0) {
+      tune_spmv32(c, cached, false);  // a choice stored by an earlier run on this device and mesh
+      c.spmv32_tuned = c.spmv32_variant;
+      c.tune_report = std::string("{\"cached\": true, \"chosen\": \"") + spmv32_name(c.spmv32_variant) +
+                      "\", \"block_rows\": " + std::to_string(c.nbrow) + "}";
     } else {
       tune_spmv32(c, variant, true);
-      if (variant < 0) c.spmv32_tuned = c.spmv32_variant;
+      if (variant < 0) {
+        c.spmv32_tuned = c.spmv32_variant;
+        if (!key.empty()) tune_cache_store(c, key, c.spmv32_variant, c.tune_report);
+      }
     }
   } else {
     c.d_a32.alloc(std::max<int64_t>(c.nnz, 1));
     to_fp32(c);
+    std::string key;
+    int cached = -1;
+    if (variant < 0 && c.spmv32_tuned < 0 && !c.tune_cache.empty()) {
+      key = tune_key(c, "spmv32");
+      cached = tune_cache_lookup(c, key);
+    }
+    const int want = variant >= 0 ? variant : c.spmv32_tuned >= 0 ? c.spmv32_tuned : cached;
+    tune_scalar32(c, want, want < 0);
+    if (variant < 0) {
+      if (c.spmv32_tuned < 0 && !key.empty() && cached < 0) tune_cache_store(c, key, c.spmv32_variant, c.tune_report);
+      c.spmv32_tuned = c.spmv32_variant;
+    }
   }
   c.have_a32 = true;
+}
+
+// FP32 operator of the scalar mixed CG: the FP32 CSR copy (k_mx_csr, variant 0)
+// or, on translated Q2 hex grids, the scalar shared-matrix tcgen05 operator
+// (variant 9); with timing, both are timed on this system (CUDA events, 5
+// launches after 2) and the faster kept, else `only` is taken (-1: the CSR).
+void tune_scalar32(Ctx &c, int only, bool timing) {
+  c.spmv32_variant = 0;
+  const bool mf = (timing || only == 9) && matfree1_build(c);
+  if (!mf) {
+    if (timing) c.tune_report = "{\"csr_fp32\": null, \"chosen\": \"csr_fp32\"}";
+    return;
+  }
+  if (!timing) {
+    c.spmv32_variant = 9;
+    return;
+  }
+  cudaStream_t s = c.stream;
+  alloc_work(c, true);
+  SolverWork &w = c.sw;
+  std::vector<float> ones(w.pm.n, 1.0f);
+  GPZ_CUDA_TRY(cudaMemcpyAsync(w.pm.p, ones.data(), ones.size() * sizeof(float), cudaMemcpyHostToDevice, s));
+  int64_t hi[I_NISCAL] = {0};
+  hi[I_MAXIT] = 1;
+  GPZ_CUDA_TRY(cudaMemcpyAsync(w.iscal.p, hi, sizeof(hi), cudaMemcpyHostToDevice, s));
+  Red R = red_of(c);
+  cudaEvent_t e0, e1;
+  GPZ_CUDA_TRY(cudaEventCreate(&e0));
+  GPZ_CUDA_TRY(cudaEventCreate(&e1));
+  float ms[2] = {0.f, 0.f};
+  for (int v = 0; v < 2; v++) {
+    auto launch = [&]() {
+      if (v == 1) {
+        matfree1_spmv(c, s, w.pm.p, w.q32.p);
+      } else {
+        GPZ_TPR_SWITCH(pick_tpr32(c.nnz, c.neq), (k_mx_csr<T><<<wave(k_mx_csr<T>), kThreads, 0, s>>>(
+                                                     c.d_ia.p, c.d_ja.p, c.d_a32.p, w.pm.p, w.q32.p, c.neq, R)));
+        c.launches++;
+      }
+    };
+    for (int i = 0; i < 2; i++) launch();
+    GPZ_CUDA_TRY(cudaEventRecord(e0, s));
+    for (int i = 0; i < 5; i++) launch();
+    GPZ_CUDA_TRY(cudaEventRecord(e1, s));
+    GPZ_CUDA_TRY(cudaEventSynchronize(e1));
+    GPZ_CUDA_TRY(cudaGetLastError());
+    cudaEventElapsedTime(&ms[v], e0, e1);
+    ms[v] /= 5;
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  check_device_flag(c, "scalar shared-element-matrix tensor-core operator");
+  c.spmv32_variant = ms[1] < ms[0] ? 9 : 0;
+  c.tune_report = "{\"csr_fp32\": " + std::to_string(ms[0]) + ", \"matrix_free_shared_matrix_tcgen05_scalar\": " +
+                  std::to_string(ms[1]) + ", \"chosen\": \"" +
+                  (c.spmv32_variant == 9 ? "matrix_free_shared_matrix_tcgen05_scalar" : "csr_fp32") + "\"}";
 }
 
 void build_block_jacobi(Ctx &c) {
@@ -2705,6 +2794,7 @@ Red red_of(Ctx &c) { return Red{c.sw.partial.p, c.sw.counter.p, c.sw.scal.p, c.s
 
 struct Plan {
   bool mixed, block, bsr;
+  bool mf1 = false;  // scalar shared-matrix operator (spmv variant 9)
   bool vb = false;  // variable-size block Jacobi
   bool tl = false;  // two-level block Jacobi (mixed CG)
   TlView T;
@@ -2758,13 +2848,16 @@ void launch_iteration(Ctx &c, const Plan &P) {
     c.launches += 5;
     return;
   }
+  float *qz = (sym || P.mf1) ? w.q32.p : nullptr;  // q accumulated with atomics: zeroed with p
   if (P.vb)
-    k_vb32_p<<<wave(k_vb32_p), kThreads, 0, c.stream>>>(w.r32.p, P.V, w.pm.p, padded, sym ? w.q32.p : nullptr, R);
+    k_vb32_p<<<wave(k_vb32_p), kThreads, 0, c.stream>>>(w.r32.p, P.V, w.pm.p, padded, qz, R);
   else
-    k_mx_p<<<wave(k_mx_p), kThreads, 0, c.stream>>>(w.r32.p, P.M32, w.pm.p, padded, sym ? w.q32.p : nullptr,
-                                                    P.nunits, R);
+    k_mx_p<<<wave(k_mx_p), kThreads, 0, c.stream>>>(w.r32.p, P.M32, w.pm.p, padded, qz, P.nunits, R);
   if (P.bsr) {
     launch_spmv32(c, c.spmv32_variant, c.sell, R, c.stream);
+    c.launches--;
+  } else if (P.mf1) {
+    matfree1_spmv(c, c.stream, w.pm.p, w.q32.p);
     c.launches--;
   } else {
     GPZ_TPR_SWITCH(P.tpr32, (k_mx_csr<T><<<wave(k_mx_csr<T>), kThreads, 0, c.stream>>>(c.d_ia.p, c.d_ja.p, c.d_a32.p,
@@ -2937,7 +3030,8 @@ int solve_gmres(Ctx &c, const gpz_solver_opts &o, gpz_solve_report &rep) {
 // only on that true residual.
 int solve_learned(Ctx &c, const gpz_solver_opts &o, gpz_solve_report &rep, bool mixed) {
   GPZ_REQUIRE(!c.flt.active, GPZ_E_INVALID, "learned preconditioner: not available under an equation filter");
-  if (mixed && (!c.have_a32 || (o.spmv_variant >= 0 && c.have_bsr3 && o.spmv_variant != c.spmv32_variant)))
+  if (mixed && (!c.have_a32 || (o.spmv_variant >= 0 && (c.have_bsr3 || c.nstate == 1) &&
+                                o.spmv_variant != c.spmv32_variant)))
     make_fp32_copy(c, o.spmv_variant);
   learned_prepare(c);
   // scalar problems: FP32 CSR (k_lfcg_spmv); 3 states: the mixed CG's FP32
@@ -3329,7 +3423,8 @@ int solve(Ctx &c, const gpz_solver_opts &o, gpz_solve_report &rep) {
   const bool vb = o.precond == GPZ_PRECOND_NODESET_JACOBI ||
                   (o.precond == GPZ_PRECOND_BLOCK_JACOBI && !connect_blocks_are_3(c));
   const bool block = (o.precond == GPZ_PRECOND_BLOCK_JACOBI && !vb) || tl;
-  if (mixed && (!c.have_a32 || (o.spmv_variant >= 0 && c.have_bsr3 && o.spmv_variant != c.spmv32_variant)))
+  if (mixed && (!c.have_a32 || (o.spmv_variant >= 0 && (c.have_bsr3 || c.nstate == 1) &&
+                                o.spmv_variant != c.spmv32_variant)))
     make_fp32_copy(c, o.spmv_variant);
   if (block && !c.have_bjinv) build_block_jacobi(c);
   if (vb && (!c.have_vbinv || c.vb_kind != o.precond)) build_vblocks(c, o.precond);
@@ -3341,6 +3436,7 @@ int solve(Ctx &c, const gpz_solver_opts &o, gpz_solve_report &rep) {
   P.mixed = mixed;
   P.block = block;
   P.bsr = mixed && c.have_bsr3;
+  P.mf1 = mixed && !c.have_bsr3 && c.spmv32_variant == 9 && c.mf1.ready;
   P.tpr = pick_tpr(c.nnz, c.neq);
   P.tpr32 = pick_tpr32(c.nnz, c.neq);
   P.nunits = block ? c.neq / 3 : c.neq;
@@ -3574,7 +3670,8 @@ void precond_apply(Ctx &c, int precond, const double *hr, double *hz) {
 // y = A32 x with the mixed CG's FP32 operator in its current layout (the
 // autotuned one, or `variant` >= 0), from and to host FP64 vectors
 void spmv32_apply(Ctx &c, int variant, const double *hx, double *hy) {
-  if (!c.have_a32 || (variant >= 0 && c.have_bsr3 && variant != c.spmv32_variant)) make_fp32_copy(c, variant);
+  if (!c.have_a32 || (variant >= 0 && (c.have_bsr3 || c.nstate == 1) && variant != c.spmv32_variant))
+    make_fp32_copy(c, variant);
   alloc_work(c, true);
   SolverWork &w = c.sw;
   cudaStream_t s = c.stream;
@@ -3593,6 +3690,8 @@ void spmv32_apply(Ctx &c, int variant, const double *hx, double *hy) {
   Red R = red_of(c);
   if (c.have_bsr3) {
     launch_spmv32(c, c.spmv32_variant, c.sell, R, s);
+  } else if (c.spmv32_variant == 9 && c.mf1.ready) {
+    matfree1_spmv(c, s, w.pm.p, w.q32.p);
   } else {
     GPZ_TPR_SWITCH(pick_tpr32(c.nnz, c.neq), (k_mx_csr<T><<<wave(k_mx_csr<T>), kThreads, 0, s>>>(
                                                  c.d_ia.p, c.d_ja.p, c.d_a32.p, w.pm.p, w.q32.p, c.neq, R)));
@@ -3630,6 +3729,9 @@ double time_spmv(Ctx &c, bool f32, int reps) {
   auto launch = [&]() {
     if (f32 && c.have_bsr3) {
       launch_spmv32(c, c.spmv32_variant, c.sell, R, s);
+      c.launches--;
+    } else if (f32 && c.spmv32_variant == 9 && c.mf1.ready) {
+      matfree1_spmv(c, s, w.pm.p, w.q32.p);
       c.launches--;
     } else if (f32) {
       GPZ_TPR_SWITCH(pick_tpr32(c.nnz, c.neq), (k_mx_csr<T><<<wave(k_mx_csr<T>), kThreads, 0, s>>>(c.d_ia.p, c.d_ja.p, c.d_a32.p, w.pm.p,

@@ -110,6 +110,7 @@ def lib():
         L.gpz_pattern_info.argtypes = [vp, _P(i64), _P(i64)]
         L.gpz_time_kernel.argtypes = [vp, i32, i32, _P(dp)]
         L.gpz_tuning_report.argtypes = [vp, ctypes.c_char_p, i64]
+        L.gpz_tuning_cache.argtypes = [vp, ctypes.c_char_p]
         L.gpz_assemble.argtypes = [vp, i32]
         L.gpz_set_killed.argtypes = [vp, i32]
         L.gpz_equation_filter.argtypes = [vp, i64, vp]
@@ -341,6 +342,11 @@ class Context:
         ms = ctypes.c_double()
         self._check(lib().gpz_time_kernel(self.h, which, reps, ctypes.byref(ms)))
         return ms.value
+
+    def tuning_cache(self, path):
+        """File of the autotuners' choices kept across runs (gpz_tuning_cache); None: no cache."""
+        self._cache_path = None if path is None else str(path).encode()
+        self._check(lib().gpz_tuning_cache(self.h, self._cache_path))
 
     def tuning_report(self):
         import json
