@@ -36,8 +36,8 @@ LEARNED_BASE = 4  # GPZ_PRECOND_TWO_LEVEL: the base under the learned correction
 # solver paths of a step: the metric's learned + mixed flexible PCG (the correction on the two-level base), the
 # mixed CG with that base alone (the method without the network), the mixed block-Jacobi CG, the FP64 Jacobi-PCG
 PATH_KEY = {"learned": "learned_mixed_fcg", "two_level": "mixed_two_level_cg", "mixed": "mixed_block_jacobi_cg",
-            "fp64": "fp64_jacobi_pcg"}
-PATH_CHECK = {"learned": 16, "two_level": 16, "mixed": 64, "fp64": 64}  # iterations per convergence check
+            "learned_block": "learned_mixed_fcg_block_jacobi", "fp64": "fp64_jacobi_pcg"}
+PATH_CHECK = {"learned": 16, "two_level": 16, "mixed": 64, "learned_block": 64, "fp64": 64}  # per convergence check
 PATH_DESC = {
     "learned": ("FP64 assembly + FP32 operator ({op}); learned + mixed flexible PCG: learned element-to-node "
                 "correction (rank {rank}, weights {weights}, trained on the GPU) on the two-level block-Jacobi base "
@@ -48,6 +48,8 @@ PATH_DESC = {
                   "recurrence, FP64 x/dots, reliable FP64 true-residual updates"),
     "mixed": ("FP64 assembly + FP32 operator ({op}); mixed CG with connect-block (3x3) Jacobi, FP32 recurrence, "
               "FP64 x/dots, reliable FP64 true-residual updates"),
+    "learned_block": ("FP64 assembly + FP32 operator ({op}); learned + mixed flexible PCG with the same network on "
+                      "the connect-block (3x3) Jacobi base: the ablation against mixed_block_jacobi_cg"),
     "fp64": "FP64 assembly; FP64 Jacobi-PCG (the reference's algorithm)"}
 TOL = 1e-8
 ERR_REF_TOL = 1e-12  # true residual of the FP64 solve the solution errors are measured against
@@ -74,6 +76,9 @@ def parse():
     ap.add_argument("--no-hp", action="store_true", help="skip the hp (uneven-order) assembly leg")
     ap.add_argument("--hp-n", type=int, default=40, help="hexes per direction of the hp leg")
     ap.add_argument("--no-poisson3d", action="store_true", help="skip the 3D scalar (64^3 Q2 Darcy) leg")
+    ap.add_argument("--poisson3d-n", type=int, default=64, help="hexes per direction of the 3D scalar leg")
+    ap.add_argument("--poisson3d-variant", type=int, default=-1,
+                    help="FP32 operator of the 3D scalar leg: -1 autotuned, 0 the FP32 CSR, 9 the shared matrix")
     ap.add_argument("--no-sloan", action="store_true", help="skip the host graph legs (Sloan renumbering, node-set blocks)")
     ap.add_argument("--spmv-variant", type=int, default=-1,
                     help="FP32 operator of the mixed solves: -1 autotuned, else the gpz_solver_opts spmv_variant")
@@ -207,6 +212,9 @@ def run_gpu(args):
         if path == "learned":
             return ctx.solve(solver=gpz.GPZ_SOLVER_LEARNED_MIXED_FCG, precond=LEARNED_BASE, reliable_delta=1e-2,
                              spmv_variant=args.spmv_variant, **kw)
+        if path == "learned_block":
+            return ctx.solve(solver=gpz.GPZ_SOLVER_LEARNED_MIXED_FCG, precond=gpz.GPZ_PRECOND_BLOCK_JACOBI,
+                             reliable_delta=1e-2, spmv_variant=args.spmv_variant, **kw)
         if path in ("two_level", "mixed"):
             pre = gpz.GPZ_PRECOND_TWO_LEVEL if path == "two_level" else gpz.GPZ_PRECOND_BLOCK_JACOBI
             return ctx.solve(solver=gpz.GPZ_SOLVER_MIXED_CG, precond=pre, reliable_delta=1e-2,
@@ -261,9 +269,9 @@ def run_gpu(args):
     last = reps[-1]
     x_step = ctx.solution()  # the last timed step's solution (outside the timed region)
     # the other mixed paths, one step each (after a warm-up step): the two-level CG without the network (the
-    # method without the learned correction) and the block-Jacobi CG
+    # method without the learned correction), the block-Jacobi CG, and the network on the block-Jacobi base
     others = {}
-    for path in [q for q in ("learned", "two_level", "mixed") if q != args.path]:
+    for path in [q for q in ("learned", "two_level", "mixed", "learned_block") if q != args.path]:
         step(path)
         r, t = timed(lambda: step(path))
         others[path] = (r, t, ctx.solution())
@@ -459,7 +467,7 @@ def run_gpu(args):
     if rank == 0 and not args.no_sloan:
         out["sloan_renumbering"], out["nodeset_blocks"] = sloan_leg(gpz, n)
     if rank == 0 and not args.no_poisson3d:
-        out["poisson3d"] = poisson3d_leg(gpz, dev)
+        out["poisson3d"] = poisson3d_leg(gpz, dev, args.poisson3d_n, args.poisson3d_variant)
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         out["cpu_baseline"] = cpu_baseline(fp64["iterations"], n)
     if rank == 0:
@@ -539,7 +547,7 @@ def sloan_leg(gpz, n):
     return sloan, nodeset
 
 
-def poisson3d_leg(gpz, dev, n=64):
+def poisson3d_leg(gpz, dev, n=64, variant=-1):
     """The 3D scalar workload: -div(k grad u) = 1 on the unit cube, 64^3 Q2 hexes (2,146,689 equations),
     k lognormal(sigma=1) per element (seed 1), u = 0 on the boundary: FP64 assembly, then the mixed CG (the FP32
     operator the autotuner picks: the FP32 CSR copy or the scalar shared-element-matrix tcgen05 kernel; Jacobi)
@@ -555,7 +563,7 @@ def poisson3d_leg(gpz, dev, n=64):
     ctx.assemble(gpz.GPZ_PREC_MIXED)
     for _ in range(2):  # the second is timed (graphs instantiated)
         mx = ctx.solve(solver=gpz.GPZ_SOLVER_MIXED_CG, tol=TOL, max_iter=200000, reliable_delta=1e-2,
-                       check_every=64, want_x=False)
+                       check_every=64, want_x=False, spmv_variant=variant)
     tune = ctx.tuning_report()
     op_ms = ctx.time_kernel(gpz.GPZ_KERNEL_SPMV_FP32, 20)
     ctx.close()

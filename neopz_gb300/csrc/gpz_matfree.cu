@@ -1116,12 +1116,22 @@ __device__ __forceinline__ bool gm_wait(uint64_t *mb, uint32_t parity, volatile 
   return false;
 }
 
+// a streamed 16-byte load that does not allocate in L1 (the L1 left beside the
+// operands keeps the gathered p values instead)
+__device__ __forceinline__ int4 ld_stream4(const int4 *p) {
+  int4 v;
+  asm volatile("ld.global.nc.L1::no_allocate.v4.s32 {%0, %1, %2, %3}, [%4];"
+               : "=r"(v.x), "=r"(v.y), "=r"(v.z), "=r"(v.w)
+               : "l"(p));
+  return v;
+}
+
 // the tile's block rows [128][27] into shared memory (coalesced; padded tiles)
 __device__ __forceinline__ void gm_rows(unsigned char *dst, const int4 *__restrict__ rows4, int64_t tile, int gl) {
   constexpr int n4 = (int)(kGmR / 16);
   const int4 *src = rows4 + (size_t)tile * n4;
 #pragma unroll
-  for (int i = gl; i < n4; i += kGmGroup) ((int4 *)dst)[i] = src[i];
+  for (int i = gl; i < n4; i += kGmGroup) ((int4 *)dst)[i] = ld_stream4(src + i);
 }
 
 // Half of one element's row of U: shapes [A0, A1) -> columns [3 A0, 3 A1),
@@ -2196,7 +2206,7 @@ __global__ void __launch_bounds__(kG1Threads, 2) k_mf_hex27_gm1(int64_t n, const
     int k = 0;
     for (int64_t tile = blockIdx.x; tile < ntile; tile += gridDim.x, k++) {
       const int b = k & 1;
-      for (int i = gl; i < n4; i += kG1Group) ((int4 *)(sm + G1_RG))[i] = rows4[(size_t)tile * n4 + i];
+      for (int i = gl; i < n4; i += kG1Group) ((int4 *)(sm + G1_RG))[i] = ld_stream4(rows4 + (size_t)tile * n4 + i);
       bool ok = true;
       if (gl == 0 && k >= 2) ok = gm_wait(&s_free[b], (uint32_t)((k - 2) >> 1) & 1u, &s_abort);
       if (ok && k >= 1) ok = gm_wait(&s_done[(k - 1) & 1], (uint32_t)((k - 1) >> 1) & 1u, &s_abort);
@@ -2237,7 +2247,7 @@ __global__ void __launch_bounds__(kG1Threads, 2) k_mf_hex27_gm1(int64_t n, const
     int k = 0;
     for (int64_t tile = blockIdx.x; tile < ntile; tile += gridDim.x, k++) {
       const int b = k & 1;
-      for (int i = gl; i < n4; i += kG1Group) ((int4 *)(sm + G1_RS))[i] = rows4[(size_t)tile * n4 + i];
+      for (int i = gl; i < n4; i += kG1Group) ((int4 *)(sm + G1_RS))[i] = ld_stream4(rows4 + (size_t)tile * n4 + i);
       const bool ok = gm_wait(&s_done[b], (uint32_t)(k >> 1) & 1u, &s_abort);
       if (!gm_vote(2, kG1Group, ok)) break;
       asm volatile("tcgen05.fence::after_thread_sync;");
