@@ -402,6 +402,16 @@ int gpz_tuning_report(gpz_ctx *ctx, char *buf, int64_t len);
  * carry "cached": true).  NULL: no cache (the default).  An unreadable or
  * unwritable file only means the tuners measure again. */
 int gpz_tuning_cache(gpz_ctx *ctx, const char *path);
+/* Launch mode of the element kernels: -1 autotuned at the first assembly of a
+ * mesh (both timed on one full assembly, the faster kept), 0 a launch per
+ * element bucket and colour (a CTA per element; the default), 1 one persistent
+ * launch per bucket over all its colours: resident CTAs take elements from a
+ * work counter in colour order, an element of colour c waits (bounded) until
+ * every element of the earlier colours is done -- the OT scheduler of
+ * TPZStructMatrixOT (StrMatrix/pzstrmatrixot.cpp:486-551) on the device.  The
+ * matrices agree to the last bits (the order of the contributions of different
+ * buckets to one entry differs). */
+int gpz_assembly_mode(gpz_ctx *ctx, int mode);
 /* JSON text of the element batching: uniform-order buckets (compile-time
  * kernels), hp classes (elements of uneven side orders sharing the table of
  * the full element of their largest order, one run-time kernel per class and

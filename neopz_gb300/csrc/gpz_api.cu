@@ -177,6 +177,9 @@ int gpz_mesh_upload(gpz_ctx *ctx, const gpz_mesh_desc *d) {
     c.have_vbinv = false;
     c.vb_kind = 0;
     c.tl.ready = c.tl.have_inv = false;
+    if (c.asm_mode_auto) c.asm_queue = -1;  // an autotuned launch mode is timed again for the new buckets
+    c.asm_mode_report.clear();
+    c.asm_tune_report.clear();
     drop_assembly_graph(c);
     return GPZ_OK;
   });
@@ -316,7 +319,8 @@ int gpz_assembly_report(gpz_ctx *ctx, char *buf, int64_t len) {
     std::string r = "{\"uniform_buckets\": " + std::to_string(nb) + ", \"uniform_elements\": " + std::to_string(eun) +
                     ", \"hp_classes\": " + std::to_string(nhp) + ", \"hp_elements\": " + std::to_string(ehp) +
                     ", \"colours\": " + std::to_string(c.ncolours) + ", \"hp_block_size_ms\": " +
-                    (c.asm_tune_report.empty() ? std::string("null") : c.asm_tune_report) + "}";
+                    (c.asm_tune_report.empty() ? std::string("null") : c.asm_tune_report) + ", \"launch_mode_ms\": " +
+                    (c.asm_mode_report.empty() ? std::string("null") : c.asm_mode_report) + "}";
     GPZ_REQUIRE((int64_t)r.size() < len, GPZ_E_INVALID, "buffer too small");
     std::copy(r.begin(), r.end(), buf);
     buf[r.size()] = 0;
@@ -557,6 +561,17 @@ int gpz_time_kernel(gpz_ctx *ctx, int which, int reps, double *ms_per_launch) {
     } else {
       GPZ_REQUIRE(false, GPZ_E_INVALID, "kernel id");
     }
+    return GPZ_OK;
+  });
+}
+
+int gpz_assembly_mode(gpz_ctx *ctx, int mode) {
+  return guarded(ctx, [&](Ctx &c) {
+    GPZ_REQUIRE(mode >= -1 && mode <= 1, GPZ_E_INVALID, "mode: -1 autotuned, 0 per colour, 1 persistent");
+    c.asm_queue = mode;
+    c.asm_mode_auto = mode < 0;
+    c.asm_mode_report = mode < 0 ? std::string() : std::string("{\"set\": \"") + (mode ? "persistent" : "per_colour") + "\"}";
+    drop_assembly_graph(c);  // the captured launches follow the mode
     return GPZ_OK;
   });
 }

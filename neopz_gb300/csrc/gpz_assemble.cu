@@ -155,12 +155,15 @@ struct HpArgs {
 // are among those of the same side at the class order, with the same values),
 // listed per element in H.  Any block size that is a multiple of 32 works; the
 // hp classes' block size is autotuned.
-template <int NSH_T, int DIM, int NST, bool BC, bool HP>
-__global__ void __launch_bounds__(256) k_elem_fp64(ElemArgs P, HpArgs H, const int64_t *__restrict__ elems,
-                                                   int64_t nelems) {
+// One element's matrix and load vector, scattered into the CSR (or, in the
+// reference mode, into dense arrays).  In the queue kernel below the
+// read-modify-writes of the matrix and the load vector read through L2 (ld.cg):
+// one CTA handles elements of several colours there, and a line cached in its
+// SM's L1 by an earlier colour may since have been changed by another SM.
+template <int NSH_T, int DIM, int NST, bool BC, bool HP, bool QUEUE>
+__device__ __forceinline__ void elem_body(const ElemArgs &P, const HpArgs &H, const int64_t *__restrict__ elems,
+                                          int64_t ie) {
   extern __shared__ double sm[];
-  const int64_t ie = blockIdx.x;
-  if (ie >= nelems) return;
   const int NT = NSH_T > 0 ? NSH_T : P.nshape;  // shapes of the table (its row stride)
   const int NSH = HP ? H.n[ie] : NT;            // shapes of this element
   const int nq = P.nq;
@@ -308,7 +311,7 @@ __global__ void __launch_bounds__(256) k_elem_fp64(ElemArgs P, HpArgs H, const i
       atomicOr(P.err, 16);
       continue;
     }
-    P.f[row] += acc;
+    P.f[row] = (QUEUE ? __ldcg(P.f + row) : P.f[row]) + acc;
   }
   if ((BC && P.bc_type != 0) || P.rhs_only) return;
 
@@ -396,36 +399,101 @@ __global__ void __launch_bounds__(256) k_elem_fp64(ElemArgs P, HpArgs H, const i
       continue;
     }
     const int ka = sK[a] * NST, kb = sK[b] * NST;
+    // the block's (and its transpose's) slots are distinct entries of the CSR: every old value is loaded
+    // before the first store, so the loads are in flight together instead of one per store
+    int64_t slot[2][NST][NST];
+    double old[2][NST][NST];
+    bool bad = false;
+#pragma unroll
     for (int s = 0; s < NST; s++) {
-      const int64_t ra = sRow[a] + s;
-      const int64_t base = P.ia[ra] + oab + kb;
-      for (int t = 0; t < NST; t++) {
-        double v = K[s][t];
-        if (fabs(v) < 1.e-12) continue;
-        int64_t slot = base + t;
-        if (slot < 0 || slot >= P.nnz) {
-          atomicOr(P.err, 64);
-          continue;
-        }
-        P.a[slot] += v;
-      }
+      const int64_t base = P.ia[sRow[a] + s] + oab + kb;
+#pragma unroll
+      for (int t = 0; t < NST; t++) slot[0][s][t] = base + t;
     }
-    if (a != b) {
-      for (int t = 0; t < NST; t++) {
-        const int64_t rb = sRow[b] + t;
-        const int64_t base = P.ia[rb] + oba + ka;
-        for (int s = 0; s < NST; s++) {
-          double v = K[s][t];
-          if (fabs(v) < 1.e-12) continue;
-          int64_t slot = base + s;
-          if (slot < 0 || slot >= P.nnz) {
-            atomicOr(P.err, 64);
-            continue;
+#pragma unroll
+    for (int t = 0; t < NST; t++) {
+      const int64_t base = P.ia[sRow[b] + t] + oba + ka;
+#pragma unroll
+      for (int s = 0; s < NST; s++) slot[1][s][t] = base + s;
+    }
+#pragma unroll
+    for (int h = 0; h < 2; h++)
+#pragma unroll
+      for (int s = 0; s < NST; s++)
+#pragma unroll
+        for (int t = 0; t < NST; t++) {
+          const int64_t q = slot[h][s][t];
+          const bool use = fabs(K[s][t]) >= 1.e-12 && (h == 0 || a != b);
+          bad |= use && (q < 0 || q >= P.nnz);
+          old[h][s][t] = use && q >= 0 && q < P.nnz ? (QUEUE ? __ldcg(P.a + q) : P.a[q]) : 0.0;
+        }
+    if (bad) atomicOr(P.err, 64);
+#pragma unroll
+    for (int h = 0; h < 2; h++)
+#pragma unroll
+      for (int s = 0; s < NST; s++)
+#pragma unroll
+        for (int t = 0; t < NST; t++) {
+          const int64_t q = slot[h][s][t];
+          if (fabs(K[s][t]) >= 1.e-12 && (h == 0 || a != b) && q >= 0 && q < P.nnz) P.a[q] = old[h][s][t] + K[s][t];
+        }
+  }
+}
+
+// one CTA per element (a launch per bucket and colour)
+template <int NSH_T, int DIM, int NST, bool BC, bool HP>
+__global__ void __launch_bounds__(256) k_elem_fp64(ElemArgs P, HpArgs H, const int64_t *__restrict__ elems,
+                                                   int64_t nelems) {
+  const int64_t ie = blockIdx.x;
+  if (ie >= nelems) return;
+  elem_body<NSH_T, DIM, NST, BC, HP, false>(P, H, elems, ie);
+}
+
+// Persistent form (one launch per bucket, every colour): resident CTAs take the
+// bucket's elements from a work counter in colour order; an element of colour c
+// starts once every element of the earlier colours is done (a second counter;
+// elements of one colour share no connect, so the scatter needs no atomics).
+// Items are taken in order and each is held by a running CTA, so every wait
+// ends; it is bounded all the same, and a wait that gives up sets an error flag
+// and stops its CTA.
+struct QueueArgs {
+  unsigned long long *next, *done;  // work counter, finished elements
+  const int64_t *cbeg;              // [ncol + 1] colour boundaries in the bucket's element list
+  int ncol;
+};
+constexpr int kQueueWaitTries = 1 << 24;
+
+template <int NSH_T, int DIM, int NST, bool BC, bool HP>
+__global__ void __launch_bounds__(256) k_elem_fp64_queue(ElemArgs P, HpArgs H, const int64_t *__restrict__ elems,
+                                                         int64_t nelems, QueueArgs Q) {
+  __shared__ int64_t s_item;
+  for (;;) {
+    if (threadIdx.x == 0) {
+      int64_t it = (int64_t)atomicAdd(Q.next, 1ull);
+      if (it < nelems) {
+        int c = 0;
+        while (c + 1 < Q.ncol && Q.cbeg[c + 1] <= it) c++;
+        const unsigned long long need = (unsigned long long)Q.cbeg[c];
+        int tries = 0;
+        while (*(volatile unsigned long long *)Q.done < need) {
+          if (++tries > kQueueWaitTries) {
+            atomicOr(P.err, 32768);
+            it = nelems;  // give up: this CTA stops
+            break;
           }
-          P.a[slot] += v;
+          __nanosleep(128);
         }
+        __threadfence();  // the earlier colours' writes before this element's reads
       }
+      s_item = it;
     }
+    __syncthreads();
+    const int64_t it = s_item;
+    if (it >= nelems) return;
+    elem_body<NSH_T, DIM, NST, BC, HP, true>(P, H, elems, it);
+    __threadfence();  // this element's writes before it is counted done
+    __syncthreads();
+    if (threadIdx.x == 0) atomicAdd(Q.done, 1ull);
   }
 }
 
@@ -435,14 +503,19 @@ size_t smem_bytes(int nsh, int dim, int nq, bool bc) {
 }
 
 typedef void (*ElemKernel)(ElemArgs, HpArgs, const int64_t *, int64_t);
+typedef void (*QueueKernel)(ElemArgs, HpArgs, const int64_t *, int64_t, QueueArgs);
+struct Kernels {
+  ElemKernel one = nullptr;    // a CTA per element, a launch per colour
+  QueueKernel queue = nullptr;  // persistent, every colour in one launch
+};
 
-template <int NSH, int DIM, int NST, bool BC>
-ElemKernel pick() {
-  return k_elem_fp64<NSH, DIM, NST, BC, false>;
+template <int NSH, int DIM, int NST, bool BC, bool HP = false>
+Kernels pick() {
+  return Kernels{k_elem_fp64<NSH, DIM, NST, BC, HP>, k_elem_fp64_queue<NSH, DIM, NST, BC, HP>};
 }
 
 // compile-time shape counts of the uniform-order elements; nullptr: use the batched run-time kernel
-ElemKernel select_kernel(int type, int nshape, int nstate, bool bc) {
+Kernels select_kernel(int type, int nshape, int nstate, bool bc) {
   // volume hexes (3D) and quads (2D); boundary quads (3D faces) and lines (2D edges)
   if (type == GPZ_EL_HEX && !bc) {
     if (nstate == 1) {
@@ -476,16 +549,16 @@ ElemKernel select_kernel(int type, int nshape, int nstate, bool bc) {
     if (nshape == 3) return pick<3, 1, 1, true>();
     if (nshape == 4) return pick<4, 1, 1, true>();
   }
-  return nullptr;
+  return Kernels{};
 }
 
 // the run-time kernel of an hp class
-ElemKernel select_hp(int type, int nstate, bool bc) {
-  if (type == GPZ_EL_HEX && !bc) return nstate == 1 ? k_elem_fp64<0, 3, 1, false, true> : k_elem_fp64<0, 3, 3, false, true>;
-  if (type == GPZ_EL_QUAD && !bc && nstate == 1) return k_elem_fp64<0, 2, 1, false, true>;
-  if (type == GPZ_EL_QUAD && bc) return nstate == 1 ? k_elem_fp64<0, 2, 1, true, true> : k_elem_fp64<0, 2, 3, true, true>;
-  if (type == GPZ_EL_LINE && bc && nstate == 1) return k_elem_fp64<0, 1, 1, true, true>;
-  return nullptr;
+Kernels select_hp(int type, int nstate, bool bc) {
+  if (type == GPZ_EL_HEX && !bc) return nstate == 1 ? pick<0, 3, 1, false, true>() : pick<0, 3, 3, false, true>();
+  if (type == GPZ_EL_QUAD && !bc && nstate == 1) return pick<0, 2, 1, false, true>();
+  if (type == GPZ_EL_QUAD && bc) return nstate == 1 ? pick<0, 2, 1, true, true>() : pick<0, 2, 3, true, true>();
+  if (type == GPZ_EL_LINE && bc && nstate == 1) return pick<0, 1, 1, true, true>();
+  return Kernels{};
 }
 
 __global__ void k_extract_diag(const double *__restrict__ a, const int64_t *__restrict__ diagpos, int64_t neq,
@@ -557,7 +630,7 @@ void build_buckets(Ctx &c, const gpz_mesh_desc &d) {
     if (!k.hp) {
       int n = t.ncorner;
       for (int s = t.ncorner; s < t.nsides; s++) n += side_nshape(k.type, s, k.orders[s - t.ncorner]);
-      if (!select_kernel(k.type, n, c.nstate, k.is_bc)) k.hp = 1;  // no compile-time kernel: same table, run-time path
+      if (!select_kernel(k.type, n, c.nstate, k.is_bc).one) k.hp = 1;  // no compile-time kernel: same table, run-time path
     }
     if (k.hp) {
       // active shapes of this element among the class table's: corners, then per
@@ -631,8 +704,8 @@ void build_buckets(Ctx &c, const gpz_mesh_desc &d) {
               }
       }
       b->hp = k.hp != 0;
-      GPZ_REQUIRE(b->hp ? select_hp(k.type, c.nstate, k.is_bc) != nullptr
-                        : select_kernel(k.type, b->nshape, c.nstate, k.is_bc) != nullptr,
+      GPZ_REQUIRE(b->hp ? select_hp(k.type, c.nstate, k.is_bc).one != nullptr
+                        : select_kernel(k.type, b->nshape, c.nstate, k.is_bc).one != nullptr,
                   GPZ_E_UNSUPPORTED_ELEMENT, "no kernel for this element bucket");
       c.buckets.push_back(b);
     } else {
@@ -690,6 +763,8 @@ void build_buckets(Ctx &c, const gpz_mesh_desc &d) {
     b->d_shape_side.upload(b->shape_side.data(), b->shape_side.size(), c.stream);
     b->d_shape_k.upload(b->shape_k.data(), b->shape_k.size(), c.stream);
     b->d_elems.upload(b->elems.data(), b->elems.size(), c.stream);
+    b->d_cbeg.upload(b->colour_begin.data(), b->colour_begin.size(), c.stream);
+    b->d_q.alloc(2);
   }
   GPZ_CUDA_TRY(cudaStreamSynchronize(c.stream));
 }
@@ -796,9 +871,47 @@ __global__ void k_translates(const int64_t *__restrict__ elems, int64_t n, const
 }
 
 // element integration + scatter of every bucket, colour by colour; the hp
-// classes run with `threads` (0: the class's tuned block size)
-void launch_elements(Ctx &c, int threads, bool rhs_only = false, bool set_attrs = true) {
+// classes run with `threads` (0: the class's tuned block size).  queue: one
+// persistent launch per bucket over all its colours instead (k_elem_fp64_queue).
+void launch_elements(Ctx &c, int threads, bool rhs_only = false, bool set_attrs = true, bool queue = false) {
   cudaStream_t s = c.stream;
+  if (queue) {
+    int dev = 0, nsm = 0;
+    if (set_attrs) {
+      GPZ_CUDA_TRY(cudaGetDevice(&dev));
+      GPZ_CUDA_TRY(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
+    }
+    for (Bucket *b : c.buckets) {
+      const int64_t ne = (int64_t)b->elems.size();
+      if (!ne) continue;
+      ElemArgs P = args_of(c, b);
+      P.rhs_only = rhs_only ? 1 : 0;
+      const size_t sh = smem_bytes(b->nshape, b->dim, b->nq, b->key.is_bc);
+      const Kernels K = b->hp ? select_hp(b->key.type, c.nstate, b->key.is_bc)
+                              : select_kernel(b->key.type, b->nshape, c.nstate, b->key.is_bc);
+      HpArgs H{nullptr, nullptr, nullptr};
+      int nt = 128;
+      if (b->hp) {
+        H.full = b->d_act_full.p;
+        H.k = b->d_act_k.p;
+        H.n = b->d_act_n.p;
+        nt = threads > 0 ? threads : b->threads;
+      }
+      if (set_attrs) {  // resident CTAs for this block size (kept for the captured replays)
+        if (sh > 48 * 1024)
+          GPZ_CUDA_TRY(cudaFuncSetAttribute(K.queue, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sh));
+        int per = 0;
+        GPZ_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, K.queue, nt, sh));
+        b->qgrid = (int)std::max<int64_t>(1, std::min<int64_t>(ne, (int64_t)std::max(per, 1) * nsm));
+      }
+      b->d_q.zero(s);
+      const QueueArgs Q{b->d_q.p, b->d_q.p + 1, b->d_cbeg.p, c.ncolours};
+      K.queue<<<b->qgrid, nt, sh, s>>>(P, H, b->d_elems.p, ne, Q);
+      c.launches++;
+      GPZ_CUDA_TRY(cudaGetLastError());
+    }
+    return;
+  }
   for (int col = 0; col < c.ncolours; col++) {
     for (Bucket *b : c.buckets) {
       int64_t e0 = b->colour_begin[col], e1 = b->colour_begin[col + 1];
@@ -810,13 +923,13 @@ void launch_elements(Ctx &c, int threads, bool rhs_only = false, bool set_attrs 
       HpArgs H{nullptr, nullptr, nullptr};
       int nt = 128;
       if (b->hp) {
-        k = select_hp(b->key.type, c.nstate, b->key.is_bc);
+        k = select_hp(b->key.type, c.nstate, b->key.is_bc).one;
         H.full = b->d_act_full.p + e0 * kMaxShapes;
         H.k = b->d_act_k.p + e0 * kMaxShapes;
         H.n = b->d_act_n.p + e0;
         nt = threads > 0 ? threads : b->threads;
       } else {
-        k = select_kernel(b->key.type, b->nshape, c.nstate, b->key.is_bc);
+        k = select_kernel(b->key.type, b->nshape, c.nstate, b->key.is_bc).one;
       }
       if (sh > 48 * 1024 && set_attrs)
         GPZ_CUDA_TRY(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sh));
@@ -857,7 +970,7 @@ void shared_setup(Ctx &c) {
     P.kdense = b->d_kref.p;
     P.fdense = b->d_fref.p;
     const size_t sh = smem_bytes(b->nshape, b->dim, b->nq, false);
-    ElemKernel k = select_kernel(b->key.type, b->nshape, c.nstate, false);
+    ElemKernel k = select_kernel(b->key.type, b->nshape, c.nstate, false).one;
     if (sh > 48 * 1024) GPZ_CUDA_TRY(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sh));
     HpArgs H{nullptr, nullptr, nullptr};
     k<<<1, 128, sh, s>>>(P, H, b->d_elems.p, 1);
@@ -930,11 +1043,51 @@ void assemble_fp64(Ctx &c) {
     c.asm_tune_report = rep + ", \"chosen\": " + std::to_string(best_t) + "}";
     if (!key.empty()) tune_cache_store(c, key, best_t, c.asm_tune_report);
   }
+  // launch mode: a launch per bucket and colour, or one persistent launch per bucket over all its colours
+  // (the work-counter kernel); one full assembly timed in each after a warm-up, the faster kept.  The
+  // element kernel and the order of the contributions within a bucket are the same; across buckets the
+  // persistent mode adds one bucket after the other, so the sums agree to the last bits only.
+  if (c.asm_queue < 0) {
+    std::string key;
+    int cached = -1;
+    if (!c.tune_cache.empty()) {
+      key = tune_key(c, "asm_mode");
+      cached = tune_cache_lookup(c, key);
+    }
+    if (cached >= 0) {
+      c.asm_queue = cached;
+      c.asm_mode_report = std::string("{\"cached\": true, \"chosen\": \"") +
+                          (cached ? "persistent" : "per_colour") + "\"}";
+    } else {
+      cudaEvent_t e0, e1;
+      GPZ_CUDA_TRY(cudaEventCreate(&e0));
+      GPZ_CUDA_TRY(cudaEventCreate(&e1));
+      float ms[2] = {0.f, 0.f};
+      for (int q = 0; q < 2; q++)
+        for (int rep = 0; rep < 2; rep++) {
+          target.zero(s);
+          c.d_f.zero(s);
+          GPZ_CUDA_TRY(cudaEventRecord(e0, s));
+          launch_elements(c, 0, false, true, q == 1);
+          GPZ_CUDA_TRY(cudaEventRecord(e1, s));
+          GPZ_CUDA_TRY(cudaEventSynchronize(e1));
+          cudaEventElapsedTime(&ms[q], e0, e1);
+        }
+      cudaEventDestroy(e0);
+      cudaEventDestroy(e1);
+      check_device_flag(c, "element assembly launch modes");
+      c.asm_queue = ms[1] < ms[0] ? 1 : 0;
+      c.asm_mode_report = "{\"per_colour\": " + std::to_string(ms[0]) + ", \"persistent\": " +
+                          std::to_string(ms[1]) + ", \"chosen\": \"" +
+                          (c.asm_queue ? "persistent" : "per_colour") + "\"}";
+      if (!key.empty()) tune_cache_store(c, key, c.asm_queue, c.asm_mode_report);
+    }
+  }
   c.d_dinv.alloc(std::max<int64_t>(c.neq, 1));
   auto body = [&](bool set_attrs) {
     target.zero(s);
     c.d_f.zero(s);
-    launch_elements(c, 0, false, set_attrs);
+    launch_elements(c, 0, false, set_attrs, c.asm_queue == 1);
     if (flt) {
       filter_values(c);
       filter_zero_inactive(c, c.d_f.p);
@@ -974,7 +1127,7 @@ void assemble_rhs(Ctx &c) {
   shared_setup(c);
   c.d_f.alloc(std::max<int64_t>(c.neq_mesh, 1));
   c.d_f.zero(c.stream);
-  launch_elements(c, 0, true);
+  launch_elements(c, 0, true, true, c.asm_queue == 1);
   if (c.flt.active) filter_zero_inactive(c, c.d_f.p);
 }
 

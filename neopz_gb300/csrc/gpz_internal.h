@@ -105,6 +105,10 @@ struct Bucket {
   // Jacobian), so K_e = coefficient_e x kref; -1 before the check
   int shared = -1;
   DBuf<double> d_kref, d_fref;               // [ndof][ndof] at coefficient 1, [ndof] load vector
+  // persistent launch over all colours: colour boundaries, work / done counters, resident CTAs
+  DBuf<int64_t> d_cbeg;
+  DBuf<unsigned long long> d_q;
+  int qgrid = 1;
 };
 
 // ---------------------------------------------------------------- solver workspace
@@ -279,6 +283,10 @@ struct Ctx {
   cudaGraphExec_t asm_graph = nullptr;       // captured assembly of the current pattern (replayed)
   int64_t asm_graph_launches = 0;
   std::string asm_tune_report;               // block-size timings of the hp element kernels
+  int asm_queue = 0;                         // 1: persistent launches per bucket, 0: a launch per colour (the
+                                             // default), -1: timed at the next assembly (gpz_assembly_mode)
+  bool asm_mode_auto = false;                // the launch mode is autotuned (gpz_assembly_mode(-1))
+  std::string asm_mode_report;               // the timings of the two launch modes
   int ncolours = 0;
   DBuf<int> d_err;                           // device-side check flag
 

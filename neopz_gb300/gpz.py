@@ -111,6 +111,7 @@ def lib():
         L.gpz_time_kernel.argtypes = [vp, i32, i32, _P(dp)]
         L.gpz_tuning_report.argtypes = [vp, ctypes.c_char_p, i64]
         L.gpz_tuning_cache.argtypes = [vp, ctypes.c_char_p]
+        L.gpz_assembly_mode.argtypes = [vp, ctypes.c_int]
         L.gpz_assemble.argtypes = [vp, i32]
         L.gpz_set_killed.argtypes = [vp, i32]
         L.gpz_equation_filter.argtypes = [vp, i64, vp]
@@ -342,6 +343,10 @@ class Context:
         ms = ctypes.c_double()
         self._check(lib().gpz_time_kernel(self.h, which, reps, ctypes.byref(ms)))
         return ms.value
+
+    def assembly_mode(self, mode):
+        """-1 autotuned, 0 a launch per element bucket and colour (the default), 1 persistent per bucket."""
+        self._check(lib().gpz_assembly_mode(self.h, int(mode)))
 
     def tuning_cache(self, path):
         """File of the autotuners' choices kept across runs (gpz_tuning_cache); None: no cache."""
