@@ -228,7 +228,8 @@ struct TwoLevel {
   DBuf<int32_t> cell_off, cell_el, el_sub;   // volume elements grouped by coarse box; sub position
   DBuf<double> tsub;                         // [s^3][24][24] P^T Khat_vv P for mu = 1
   DBuf<int32_t> cfix;                        // [nnode] 1: removed (touches a penalty equation)
-  DBuf<double> ac;                           // [nc][nc] coarse matrix, then its inverse
+  DBuf<double> ac;                           // [nc][nc] coarse matrix (FP64 sums)
+  DBuf<float> ac32;                          // [nc][nc] its FP32 copy, then the inverse
   DBuf<float> acinv32;                       // [nc][ldc] (rows padded to 16 bytes)
   int64_t ldc = 0;
   DBuf<float> rc, zc, z32;                   // coarse residual / correction, preconditioned residual

@@ -1518,23 +1518,23 @@ __global__ void k_tl_fixrows(int64_t nc, const int32_t *__restrict__ cfix, doubl
 constexpr int kGjB = 32;
 
 // P = D^-1 of the pivot block, Gauss-Jordan in shared memory by one CTA
-__global__ void __launch_bounds__(256) k_gj_diag(int64_t n, int64_t k0, double *__restrict__ A,
-                                                 int *__restrict__ err) {
-  __shared__ double D[kGjB][kGjB + 1];
+template <class T>
+__global__ void __launch_bounds__(256) k_gj_diag(int64_t n, int64_t k0, T *__restrict__ A, int *__restrict__ err) {
+  __shared__ T D[kGjB][kGjB + 1];
   const int b = (int)min((int64_t)kGjB, n - k0);
   for (int t = threadIdx.x; t < b * b; t += blockDim.x) D[t / b][t % b] = A[(k0 + t / b) * n + k0 + t % b];
   __syncthreads();
   for (int k = 0; k < b; k++) {
-    const double piv = D[k][k];
-    if (threadIdx.x == 0 && !(piv > 0.0)) atomicOr(err, 1 << 18);
-    const double ip = 1.0 / piv;
+    const T piv = D[k][k];
+    if (threadIdx.x == 0 && !(piv > T(0))) atomicOr(err, 1 << 18);
+    const T ip = T(1) / piv;
     __syncthreads();
-    if (threadIdx.x < b) D[k][threadIdx.x] = (threadIdx.x == k ? 1.0 : D[k][threadIdx.x]) * ip;
+    if (threadIdx.x < b) D[k][threadIdx.x] = (threadIdx.x == k ? T(1) : D[k][threadIdx.x]) * ip;
     __syncthreads();
     for (int t = threadIdx.x; t < b * b; t += blockDim.x) {
       const int i = t / b, j = t % b;
       if (i == k) continue;
-      const double f = D[i][k];
+      const T f = D[i][k];
       // every thread reads D[i][k] before any writes it: the column k entries are written last, below
       if (j != k) D[i][j] -= f * D[k][j];
     }
@@ -1547,17 +1547,18 @@ __global__ void __launch_bounds__(256) k_gj_diag(int64_t n, int64_t k0, double *
 }
 
 // R <- P R: row panel (rows k0.., the columns outside the block), one thread per column
-__global__ void __launch_bounds__(256) k_gj_row(int64_t n, int64_t k0, double *__restrict__ A) {
-  __shared__ double P[kGjB][kGjB];
+template <class T>
+__global__ void __launch_bounds__(256) k_gj_row(int64_t n, int64_t k0, T *__restrict__ A) {
+  __shared__ T P[kGjB][kGjB];
   const int b = (int)min((int64_t)kGjB, n - k0);
   for (int t = threadIdx.x; t < b * b; t += blockDim.x) P[t / b][t % b] = A[(k0 + t / b) * n + k0 + t % b];
   __syncthreads();
   const int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (j >= n || (j >= k0 && j < k0 + b)) return;
-  double r[kGjB];
+  T r[kGjB];
   for (int t = 0; t < b; t++) r[t] = A[(k0 + t) * n + j];
   for (int i = 0; i < b; i++) {
-    double acc = 0.0;
+    T acc = T(0);
     for (int t = 0; t < b; t++) acc += P[i][t] * r[t];
     A[(k0 + i) * n + j] = acc;
   }
@@ -1565,21 +1566,22 @@ __global__ void __launch_bounds__(256) k_gj_row(int64_t n, int64_t k0, double *_
 
 // E <- E - C R' over 64 x 64 tiles of the matrix outside the pivot rows and columns (R' = the updated
 // row panel, C = the column panel not updated yet); each thread a 4 x 4 sub-tile
-__global__ void __launch_bounds__(256) k_gj_trail(int64_t n, int64_t k0, double *__restrict__ A) {
-  __shared__ double Cs[64][kGjB + 1], Rs[kGjB][64 + 1];
+template <class T>
+__global__ void __launch_bounds__(256) k_gj_trail(int64_t n, int64_t k0, T *__restrict__ A) {
+  __shared__ T Cs[64][kGjB + 1], Rs[kGjB][64 + 1];
   const int b = (int)min((int64_t)kGjB, n - k0);
   const int64_t i0 = (int64_t)blockIdx.y * 64, j0 = (int64_t)blockIdx.x * 64;
   for (int t = threadIdx.x; t < 64 * kGjB; t += blockDim.x) {
     const int r = t / kGjB, c = t % kGjB;
-    Cs[r][c] = (i0 + r < n && c < b) ? A[(i0 + r) * n + k0 + c] : 0.0;
+    Cs[r][c] = (i0 + r < n && c < b) ? A[(i0 + r) * n + k0 + c] : T(0);
   }
   for (int t = threadIdx.x; t < kGjB * 64; t += blockDim.x) {
     const int r = t / 64, c = t % 64;
-    Rs[r][c] = (r < b && j0 + c < n) ? A[(k0 + r) * n + j0 + c] : 0.0;
+    Rs[r][c] = (r < b && j0 + c < n) ? A[(k0 + r) * n + j0 + c] : T(0);
   }
   __syncthreads();
   const int ti = (threadIdx.x / 16) * 4, tj = (threadIdx.x % 16) * 4;
-  double acc[4][4] = {};
+  T acc[4][4] = {};
   for (int t = 0; t < b; t++)
 #pragma unroll
     for (int u = 0; u < 4; u++)
@@ -1596,28 +1598,37 @@ __global__ void __launch_bounds__(256) k_gj_trail(int64_t n, int64_t k0, double 
 }
 
 // C <- -C P: column panel (rows outside the block, columns k0..), one thread per row
-__global__ void __launch_bounds__(256) k_gj_col(int64_t n, int64_t k0, double *__restrict__ A) {
-  __shared__ double P[kGjB][kGjB];
+template <class T>
+__global__ void __launch_bounds__(256) k_gj_col(int64_t n, int64_t k0, T *__restrict__ A) {
+  __shared__ T P[kGjB][kGjB];
   const int b = (int)min((int64_t)kGjB, n - k0);
   for (int t = threadIdx.x; t < b * b; t += blockDim.x) P[t / b][t % b] = A[(k0 + t / b) * n + k0 + t % b];
   __syncthreads();
   const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n || (i >= k0 && i < k0 + b)) return;
-  double c[kGjB];
+  T c[kGjB];
   for (int t = 0; t < b; t++) c[t] = A[i * n + k0 + t];
   for (int j = 0; j < b; j++) {
-    double acc = 0.0;
+    T acc = T(0);
     for (int t = 0; t < b; t++) acc += c[t] * P[t][j];
     A[i * n + k0 + j] = -acc;
   }
 }
 
-// B[i][j] (rows of ldc floats, zero past column n) = the symmetrised FP32 copy of A
-__global__ void k_tl_to32(int64_t n, int64_t ldc, const double *__restrict__ A, float *__restrict__ B) {
+// B = the symmetrised FP32 copy of the FP64 n x n matrix A
+__global__ void k_tl_sym32(int64_t n, const double *__restrict__ A, float *__restrict__ B) {
+  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= n * n) return;
+  const int64_t i = t / n, j = t % n;
+  B[t] = (float)(0.5 * (A[i * n + j] + A[j * n + i]));
+}
+
+// B[i][j] (rows of ldc floats, zero past column n) = the symmetrised A (n x n, FP32)
+__global__ void k_tl_pad32(int64_t n, int64_t ldc, const float *__restrict__ A, float *__restrict__ B) {
   const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= n * ldc) return;
   const int64_t i = t / ldc, j = t % ldc;
-  B[t] = j < n ? (float)(0.5 * (A[i * n + j] + A[j * n + i])) : 0.f;
+  B[t] = j < n ? 0.5f * (A[i * n + j] + A[j * n + i]) : 0.f;
 }
 
 template <class K>
@@ -2012,8 +2023,9 @@ int two_level_build(Ctx &c) {
   return GPZ_OK;
 }
 
-// Coarse matrix of the current assembly (per coarse box sum_e mu_e T[sub_e]),
-// removed nodes, blocked in-place FP64 Gauss-Jordan inverse, FP32 copy (symmetrised).
+// Coarse matrix of the current assembly (per coarse box sum_e mu_e T[sub_e], FP64),
+// removed nodes, then its inverse by blocked in-place Gauss-Jordan on the
+// symmetrised FP32 copy, padded rows for the coarse solve.
 void two_level_assemble(Ctx &c) {
   TwoLevel &T = c.tl;
   cudaStream_t s = c.stream;
@@ -2027,15 +2039,20 @@ void two_level_assemble(Ctx &c) {
   const int64_t nn = T.nc * T.nc;
   k_tl_fixrows<<<grid_for(nn, 256), 256, 0, s>>>(T.nc, T.cfix.p, T.ac.p);
   c.launches++;
+  // the inverse in FP32 (the FP32 pipe is many times the FP64 one here, and the inverse is applied in
+  // FP32): Gauss-Jordan without pivoting is stable on the SPD coarse matrix
+  T.ac32.alloc((size_t)T.nc * T.nc);
+  k_tl_sym32<<<grid_for(nn, 256), 256, 0, s>>>(T.nc, T.ac.p, T.ac32.p);
+  c.launches++;
   const unsigned tiles = (unsigned)((T.nc + 63) / 64);
   for (int64_t k0 = 0; k0 < T.nc; k0 += kGjB) {
-    k_gj_diag<<<1, 256, 0, s>>>(T.nc, k0, T.ac.p, c.d_err.p);
-    k_gj_row<<<grid_for(T.nc, 256), 256, 0, s>>>(T.nc, k0, T.ac.p);
-    k_gj_trail<<<dim3(tiles, tiles), 256, 0, s>>>(T.nc, k0, T.ac.p);
-    k_gj_col<<<grid_for(T.nc, 256), 256, 0, s>>>(T.nc, k0, T.ac.p);
+    k_gj_diag<float><<<1, 256, 0, s>>>(T.nc, k0, T.ac32.p, c.d_err.p);
+    k_gj_row<float><<<grid_for(T.nc, 256), 256, 0, s>>>(T.nc, k0, T.ac32.p);
+    k_gj_trail<float><<<dim3(tiles, tiles), 256, 0, s>>>(T.nc, k0, T.ac32.p);
+    k_gj_col<float><<<grid_for(T.nc, 256), 256, 0, s>>>(T.nc, k0, T.ac32.p);
     c.launches += 4;
   }
-  k_tl_to32<<<grid_for(T.nc * T.ldc, 256), 256, 0, s>>>(T.nc, T.ldc, T.ac.p, T.acinv32.p);
+  k_tl_pad32<<<grid_for(T.nc * T.ldc, 256), 256, 0, s>>>(T.nc, T.ldc, T.ac32.p, T.acinv32.p);
   c.launches++;
   GPZ_CUDA_TRY(cudaGetLastError());
   check_device_flag(c, "two-level coarse matrix");
