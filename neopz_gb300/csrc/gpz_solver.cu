@@ -2546,23 +2546,26 @@ void make_fp32_copy(Ctx &c, int variant) {
   c.have_bsr3 = false;
   if (blocks_are_3(c)) {
     c.nbrow = c.neq / 3;
-    // block CSR
-    c.d_bptr.alloc(c.nbrow + 1);
-    c.d_bcol.alloc(std::max<int64_t>(c.nnz / 9, 1) + 16);  // slack for 16-byte rounded bulk copies
-    c.d_bval.alloc(std::max<int64_t>(c.nnz, 1) + 16);
-    k_build_bsr3<<<grid_for(c.nbrow * 32, 256), 256, 0, c.stream>>>(c.d_ia.p, c.d_ja.p, c.d_a.p, c.nbrow, c.d_bptr.p,
-                                                                    c.d_bcol.p, c.d_bval.p, c.d_err.p);
-    c.launches++;
-    GPZ_CUDA_TRY(cudaGetLastError());
-    check_device_flag(c, "3x3 block CSR");
-    c.have_bsr3 = true;
-    c.d_a32.release();
     std::string key;
     int cached = -1;
     if (variant < 0 && c.spmv32_tuned < 0 && !c.tune_cache.empty()) {
       key = tune_key(c, "spmv32");
       cached = tune_cache_lookup(c, key);
     }
+    // the block CSR: the source of every assembled layout; a known matrix-free choice does not read it
+    const int known = variant >= 0 ? variant : c.spmv32_tuned >= 0 ? c.spmv32_tuned : cached;
+    if (!(known >= 5 && known <= 8)) {
+      c.d_bptr.alloc(c.nbrow + 1);
+      c.d_bcol.alloc(std::max<int64_t>(c.nnz / 9, 1) + 16);  // slack for 16-byte rounded bulk copies
+      c.d_bval.alloc(std::max<int64_t>(c.nnz, 1) + 16);
+      k_build_bsr3<<<grid_for(c.nbrow * 32, 256), 256, 0, c.stream>>>(c.d_ia.p, c.d_ja.p, c.d_a.p, c.nbrow,
+                                                                      c.d_bptr.p, c.d_bcol.p, c.d_bval.p, c.d_err.p);
+      c.launches++;
+      GPZ_CUDA_TRY(cudaGetLastError());
+      check_device_flag(c, "3x3 block CSR");
+    }
+    c.have_bsr3 = true;
+    c.d_a32.release();
     if (variant < 0 && c.spmv32_tuned >= 0) {
       tune_spmv32(c, c.spmv32_tuned, false);  // same pattern: rebuild the chosen layout only
     } else if (cached >= 0) {
