@@ -485,9 +485,10 @@ def hp_leg(gpz, dev, n=40):
     E = gpz.lognormal(n ** 3, 0.5, 3)
     grid = gpz.elasticity3d_hp(n, orders, E=E)
     ctx = gpz.Context(dev)
+    ctx.assembly_mode(-1)  # time both launch modes (per colour, persistent) on the first assembly
     ctx.upload_mesh(grid)
     nnz = ctx.build_pattern(True)
-    ctx.assemble()  # the first assembly runs the hp kernels' block-size autotuner
+    ctx.assemble()  # the first assembly runs the hp kernels' block-size and launch-mode autotuners
     ms = ctx.time_kernel(gpz.GPZ_KERNEL_ASSEMBLE, 3)
     rep = ctx.assembly_report()
     ctx.assemble(gpz.GPZ_PREC_MIXED)

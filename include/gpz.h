@@ -222,6 +222,24 @@ int gpz_pattern_download(gpz_ctx *ctx, int64_t *IA, int64_t *JA);
 #define GPZ_PREC_FP64 0
 #define GPZ_PREC_MIXED 1
 int gpz_assemble(gpz_ctx *ctx, int precision);
+/* Source of the FP32 values that GPZ_PREC_MIXED gives the inner solves (no
+ * counterpart in the reference, whose matrices have one precision):
+ * GPZ_FP32_ROUNDED (the default) rounds the FP64 matrix; GPZ_FP32_ELEMENTS
+ * forms every element matrix again in FP32 -- the volume hexes as one tcgen05
+ * GEMM per element (the gradient Gram X X^T, X[(i,a)][q] = sqrt(w|J|) dphi_a/dx_i,
+ * 3xTF32 split, FP32 accumulation; the material's blocks formed from it as
+ * TPZMatPoisson / TPZDarcyFlow / TPZElasticity3D::Contribute form them), the
+ * other element types by the FP64 element kernel with an FP32 scatter -- and
+ * adds them into the FP32 CSR.  The FP64 matrix (true residual, parity) is
+ * assembled either way; under an equation filter the values are rounded.  The
+ * assembly report's "fp32_elements" gives the element counts and the pass's time. */
+#define GPZ_FP32_ROUNDED 0
+#define GPZ_FP32_ELEMENTS 1
+int gpz_fp32_elements(gpz_ctx *ctx, int source);
+/* The FP32 full-CSR values (nnz floats) of the last GPZ_PREC_MIXED assembly:
+ * the scalar problems' FP32 CSR, or the FP32 element pass's values.
+ * GPZ_E_NOT_READY when the FP32 operator holds its values in another layout. */
+int gpz_matrix_fp32_download(gpz_ctx *ctx, float *A);
 /* Download the assembled values (nnz doubles) and the load vector (neq). */
 /* Load vector only (TPZStructMatrix::Assemble(rhs, gui), StrMatrix/pzstrmatrixor.cpp:75-103;
  * TPZLinearAnalysis::AssembleResidual): the same element kernels stopped

@@ -174,6 +174,8 @@ int gpz_mesh_upload(gpz_ctx *ctx, const gpz_mesh_desc *d) {
     c.er.reset();
     c.have_mesh = true;
     c.have_pattern = c.have_matrix = c.have_solution = c.have_a32 = c.have_bjinv = c.have_rhs = false;
+    c.a32_tensor = false;
+    c.fp32_report.clear();
     c.have_vbinv = false;
     c.vb_kind = 0;
     c.tl.ready = c.tl.have_inv = false;
@@ -248,6 +250,7 @@ int gpz_equation_filter(gpz_ctx *ctx, int64_t nactive, const int64_t *active) {
     c.have_matrix = false;
     c.have_solution = false;
     c.have_a32 = false;
+    c.a32_tensor = false;
     c.have_bsr3 = false;
     c.have_bjinv = false;
     c.have_vbinv = false;
@@ -320,7 +323,8 @@ int gpz_assembly_report(gpz_ctx *ctx, char *buf, int64_t len) {
                     ", \"hp_classes\": " + std::to_string(nhp) + ", \"hp_elements\": " + std::to_string(ehp) +
                     ", \"colours\": " + std::to_string(c.ncolours) + ", \"hp_block_size_ms\": " +
                     (c.asm_tune_report.empty() ? std::string("null") : c.asm_tune_report) + ", \"launch_mode_ms\": " +
-                    (c.asm_mode_report.empty() ? std::string("null") : c.asm_mode_report) + "}";
+                    (c.asm_mode_report.empty() ? std::string("null") : c.asm_mode_report) + ", \"fp32_elements\": " +
+                    (c.fp32_report.empty() ? std::string("null") : c.fp32_report) + "}";
     GPZ_REQUIRE((int64_t)r.size() < len, GPZ_E_INVALID, "buffer too small");
     std::copy(r.begin(), r.end(), buf);
     buf[r.size()] = 0;
@@ -365,7 +369,12 @@ int gpz_assemble(gpz_ctx *ctx, int precision) {
     if (c.killed.load()) return GPZ_CANCELLED;  // StrMatrix/pzstrmatrixor.cpp:490
     GPZ_REQUIRE(precision == GPZ_PREC_FP64 || precision == GPZ_PREC_MIXED, GPZ_E_INVALID, "precision");
     assemble_fp64(c);
-    if (precision == GPZ_PREC_MIXED) make_fp32_copy(c);
+    if (precision == GPZ_PREC_MIXED) {
+      // the FP32 values: element matrices formed again in FP32 (the tensor cores for the hexes), or the
+      // FP64 matrix rounded; under an equation filter always the latter
+      if (c.fp32_src == 1 && !c.flt.active) assemble_fp32_elements(c);
+      make_fp32_copy(c);
+    }
     GPZ_CUDA_TRY(cudaStreamSynchronize(c.stream));
     check_device_flag(c, "assembly");
     c.have_matrix = true;
@@ -572,6 +581,26 @@ int gpz_assembly_mode(gpz_ctx *ctx, int mode) {
     c.asm_mode_auto = mode < 0;
     c.asm_mode_report = mode < 0 ? std::string() : std::string("{\"set\": \"") + (mode ? "persistent" : "per_colour") + "\"}";
     drop_assembly_graph(c);  // the captured launches follow the mode
+    return GPZ_OK;
+  });
+}
+
+int gpz_fp32_elements(gpz_ctx *ctx, int source) {
+  return guarded(ctx, [&](Ctx &c) {
+    GPZ_REQUIRE(source == GPZ_FP32_ROUNDED || source == GPZ_FP32_ELEMENTS, GPZ_E_INVALID, "source");
+    c.fp32_src = source;
+    return GPZ_OK;
+  });
+}
+
+int gpz_matrix_fp32_download(gpz_ctx *ctx, float *A) {
+  return guarded(ctx, [&](Ctx &c) {
+    GPZ_REQUIRE(A, GPZ_E_INVALID, "null output");
+    GPZ_REQUIRE(c.have_a32 && c.d_a32.p && (int64_t)c.d_a32.n >= c.nnz, GPZ_E_NOT_READY,
+                "no FP32 CSR values (assemble with GPZ_PREC_MIXED; with 3x3 blocks they are kept only from the "
+                "FP32 element pass)");
+    if (c.nnz) GPZ_CUDA_TRY(cudaMemcpyAsync(A, c.d_a32.p, c.nnz * sizeof(float), cudaMemcpyDeviceToHost, c.stream));
+    GPZ_CUDA_TRY(cudaStreamSynchronize(c.stream));
     return GPZ_OK;
   });
 }

@@ -51,6 +51,7 @@ struct ElemArgs {
   const int64_t *ia, *offbase;
   const int32_t *off;
   double *a, *f;
+  float *a32;  // the FP32 element pass: matrix into this FP32 CSR, no load vector
   int64_t nnz, neq;
   int *err;
   // shared element matrix (a volume bucket whose elements are translates of one box): K_e = s_e kref
@@ -156,11 +157,12 @@ struct HpArgs {
 // listed per element in H.  Any block size that is a multiple of 32 works; the
 // hp classes' block size is autotuned.
 // One element's matrix and load vector, scattered into the CSR (or, in the
-// reference mode, into dense arrays).  In the queue kernel below the
+// reference mode, into dense arrays; with F32, the matrix alone into the FP32
+// CSR of the mixed solves).  In the queue kernel below the
 // read-modify-writes of the matrix and the load vector read through L2 (ld.cg):
 // one CTA handles elements of several colours there, and a line cached in its
 // SM's L1 by an earlier colour may since have been changed by another SM.
-template <int NSH_T, int DIM, int NST, bool BC, bool HP, bool QUEUE>
+template <int NSH_T, int DIM, int NST, bool BC, bool HP, bool QUEUE, bool F32 = false>
 __device__ __forceinline__ void elem_body(const ElemArgs &P, const HpArgs &H, const int64_t *__restrict__ elems,
                                           int64_t ie) {
   extern __shared__ double sm[];
@@ -281,7 +283,7 @@ __device__ __forceinline__ void elem_body(const ElemArgs &P, const HpArgs &H, co
 
   const double coef = sCoef;
   // ---- load vector
-  for (int idx = tid; idx < NSH * NST; idx += blockDim.x) {
+  for (int idx = tid; !F32 && idx < NSH * NST; idx += blockDim.x) {
     int a = idx / NST, s = idx % NST;
     const int fa = HP ? sIdx[a] : a;
     double acc = 0.0;
@@ -399,6 +401,41 @@ __device__ __forceinline__ void elem_body(const ElemArgs &P, const HpArgs &H, co
       continue;
     }
     const int ka = sK[a] * NST, kb = sK[b] * NST;
+    if (F32) {
+      int64_t slot[2][NST][NST];
+      float old[2][NST][NST];
+      bool bad = false;
+#pragma unroll
+      for (int s = 0; s < NST; s++)
+#pragma unroll
+        for (int t = 0; t < NST; t++) {
+          slot[0][s][t] = P.ia[sRow[a] + s] + oab + kb + t;
+          slot[1][s][t] = P.ia[sRow[b] + t] + oba + ka + s;
+        }
+#pragma unroll
+      for (int h = 0; h < 2; h++)
+#pragma unroll
+        for (int s = 0; s < NST; s++)
+#pragma unroll
+          for (int t = 0; t < NST; t++) {
+            const int64_t q = slot[h][s][t];
+            const bool use = fabs(K[s][t]) >= 1.e-12 && (h == 0 || a != b);
+            bad |= use && (q < 0 || q >= P.nnz);
+            old[h][s][t] = use && q >= 0 && q < P.nnz ? P.a32[q] : 0.f;
+          }
+      if (bad) atomicOr(P.err, 64);
+#pragma unroll
+      for (int h = 0; h < 2; h++)
+#pragma unroll
+        for (int s = 0; s < NST; s++)
+#pragma unroll
+          for (int t = 0; t < NST; t++) {
+            const int64_t q = slot[h][s][t];
+            if (fabs(K[s][t]) >= 1.e-12 && (h == 0 || a != b) && q >= 0 && q < P.nnz)
+              P.a32[q] = old[h][s][t] + (float)K[s][t];
+          }
+      continue;
+    }
     // the block's (and its transpose's) slots are distinct entries of the CSR: every old value is loaded
     // before the first store, so the loads are in flight together instead of one per store
     int64_t slot[2][NST][NST];
@@ -447,6 +484,15 @@ __global__ void __launch_bounds__(256) k_elem_fp64(ElemArgs P, HpArgs H, const i
   const int64_t ie = blockIdx.x;
   if (ie >= nelems) return;
   elem_body<NSH_T, DIM, NST, BC, HP, false>(P, H, elems, ie);
+}
+
+// the FP32 element pass of the element types the tensor-core kernel does not take
+template <int NSH_T, int DIM, int NST, bool BC, bool HP>
+__global__ void __launch_bounds__(256) k_elem_f32(ElemArgs P, HpArgs H, const int64_t *__restrict__ elems,
+                                                  int64_t nelems) {
+  const int64_t ie = blockIdx.x;
+  if (ie >= nelems) return;
+  elem_body<NSH_T, DIM, NST, BC, HP, false, true>(P, H, elems, ie);
 }
 
 // Persistent form (one launch per bucket, every colour): resident CTAs take the
@@ -550,6 +596,41 @@ Kernels select_kernel(int type, int nshape, int nstate, bool bc) {
     if (nshape == 4) return pick<4, 1, 1, true>();
   }
   return Kernels{};
+}
+
+// FP64 integration with the FP32 scatter: boundary elements and 2D quads (the
+// volume hexes go to the tensor-core kernel)
+template <int NSH, int DIM, int NST, bool BC, bool HP = false>
+ElemKernel pick32() {
+  return k_elem_f32<NSH, DIM, NST, BC, HP>;
+}
+ElemKernel select_f32(int type, int nshape, int nstate, bool bc, bool hp) {
+  if (type == GPZ_EL_QUAD && !bc && nstate == 1) {
+    if (hp) return pick32<0, 2, 1, false, true>();
+    if (nshape == 4) return pick32<4, 2, 1, false>();
+    if (nshape == 9) return pick32<9, 2, 1, false>();
+    if (nshape == 16) return pick32<16, 2, 1, false>();
+  }
+  if (type == GPZ_EL_QUAD && bc) {
+    if (nstate == 1) {
+      if (hp) return pick32<0, 2, 1, true, true>();
+      if (nshape == 4) return pick32<4, 2, 1, true>();
+      if (nshape == 9) return pick32<9, 2, 1, true>();
+      if (nshape == 16) return pick32<16, 2, 1, true>();
+    } else {
+      if (hp) return pick32<0, 2, 3, true, true>();
+      if (nshape == 4) return pick32<4, 2, 3, true>();
+      if (nshape == 9) return pick32<9, 2, 3, true>();
+      if (nshape == 16) return pick32<16, 2, 3, true>();
+    }
+  }
+  if (type == GPZ_EL_LINE && bc && nstate == 1) {
+    if (hp) return pick32<0, 1, 1, true, true>();
+    if (nshape == 2) return pick32<2, 1, 1, true>();
+    if (nshape == 3) return pick32<3, 1, 1, true>();
+    if (nshape == 4) return pick32<4, 1, 1, true>();
+  }
+  return nullptr;
 }
 
 // the run-time kernel of an hp class
@@ -1116,6 +1197,7 @@ void assemble_fp64(Ctx &c) {
   }
   GPZ_CUDA_TRY(cudaGetLastError());
   c.have_a32 = false;
+  c.a32_tensor = false;
   c.have_bjinv = false;
   c.have_vbinv = false;
   c.tl.have_inv = false;
@@ -1135,6 +1217,63 @@ void to_fp32(Ctx &c) {
   k_to_fp32<<<152 * 8, 256, 0, c.stream>>>(c.d_a.p, c.d_a32.p, c.nnz);
   c.launches++;
   GPZ_CUDA_TRY(cudaGetLastError());
+}
+
+// The FP32 element pass of the mixed assembly: every element's matrix formed
+// again in FP32 and added into the FP32 full CSR d_a32, colour by colour -- the
+// volume hexes as 3xTF32 tcgen05 products (gpz_elem_tc.cu), the other element
+// types (penalty faces, 2D quads) by the FP64 element kernel with an FP32
+// scatter.  The FP32 operator of the mixed solves is then built from these
+// values instead of rounding the FP64 matrix.
+void assemble_fp32_elements(Ctx &c) {
+  cudaStream_t s = c.stream;
+  c.d_a32.alloc(std::max<int64_t>(c.nnz, 1));
+  cudaEvent_t e0, e1;
+  GPZ_CUDA_TRY(cudaEventCreate(&e0));
+  GPZ_CUDA_TRY(cudaEventCreate(&e1));
+  GPZ_CUDA_TRY(cudaEventRecord(e0, s));
+  c.d_a32.zero(s);
+  int64_t ntc = 0, ncc = 0;
+  for (int col = 0; col < c.ncolours; col++) {
+    for (Bucket *b : c.buckets) {
+      const int64_t b0 = b->colour_begin[col], b1 = b->colour_begin[col + 1];
+      if (b1 == b0) continue;
+      if (elem_tc_supported(c, b)) {
+        elem_tc_launch(c, b, b0, b1, s);
+        ntc += b1 - b0;
+        continue;
+      }
+      const ElemKernel k = select_f32(b->key.type, b->nshape, c.nstate, b->key.is_bc, b->hp);
+      GPZ_REQUIRE(k != nullptr, GPZ_E_UNSUPPORTED_ELEMENT, "no FP32 element kernel for this bucket");
+      ElemArgs P = args_of(c, b);
+      P.kref = P.fref = nullptr;
+      P.a32 = c.d_a32.p;
+      const size_t sh = smem_bytes(b->nshape, b->dim, b->nq, b->key.is_bc);
+      HpArgs H{nullptr, nullptr, nullptr};
+      int nt = 128;
+      if (b->hp) {
+        H.full = b->d_act_full.p + b0 * kMaxShapes;
+        H.k = b->d_act_k.p + b0 * kMaxShapes;
+        H.n = b->d_act_n.p + b0;
+        nt = b->threads;
+      }
+      if (sh > 48 * 1024) GPZ_CUDA_TRY(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sh));
+      k<<<(unsigned)(b1 - b0), nt, sh, s>>>(P, H, b->d_elems.p + b0, b1 - b0);
+      c.launches++;
+      GPZ_CUDA_TRY(cudaGetLastError());
+      ncc += b1 - b0;
+    }
+  }
+  GPZ_CUDA_TRY(cudaEventRecord(e1, s));
+  GPZ_CUDA_TRY(cudaEventSynchronize(e1));
+  float ms = 0.f;
+  cudaEventElapsedTime(&ms, e0, e1);
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  check_device_flag(c, "FP32 element matrices");
+  c.a32_tensor = true;
+  c.fp32_report = "{\"source\": \"element_matrices_fp32\", \"tensor_core_elements\": " + std::to_string(ntc) +
+                  ", \"cuda_core_elements\": " + std::to_string(ncc) + ", \"ms\": " + std::to_string(ms) + "}";
 }
 
 }  // namespace gpz

@@ -109,6 +109,9 @@ struct Bucket {
   DBuf<int64_t> d_cbeg;
   DBuf<unsigned long long> d_q;
   int qgrid = 1;
+  // tensor-core FP32 element matrices (gpz_elem_tc.cu): FP32 tables, dynamic shared memory, resident CTAs
+  DBuf<float> d_dphi32, d_w32;
+  int tc_smem = 0, tc_resident = 0;
 };
 
 // ---------------------------------------------------------------- solver workspace
@@ -326,6 +329,11 @@ struct Ctx {
   DBuf<double> d_a, d_f, d_dinv;
   DBuf<float> d_a32;                         // FP32 CSR copy for the inner solves
   bool have_a32 = false;
+  // source of the FP32 values (gpz_fp32_elements): 0 rounded from the FP64 matrix, 1 element matrices
+  // formed again in FP32 (3xTF32 tensor-core products on the hexes) into d_a32 at each mixed assembly
+  int fp32_src = 0;
+  bool a32_tensor = false;                   // d_a32 holds the FP32 element pass of the current assembly
+  std::string fp32_report;
   // FP32 3x3 blocks for the mixed CG (instead of d_a32), in the layout the
   // SpMV autotuner measured fastest on this matrix
   bool have_bsr3 = false;
@@ -397,6 +405,10 @@ void assemble_fp64(Ctx &c);
 void assemble_rhs(Ctx &c);
 void make_fp32_copy(Ctx &c, int variant = -1);
 void to_fp32(Ctx &c);
+void assemble_fp32_elements(Ctx &c);  // FP32 element matrices into d_a32 (the tensor cores for the hexes)
+// elem_tc.cu
+bool elem_tc_supported(const Ctx &c, const Bucket *b);
+void elem_tc_launch(Ctx &c, Bucket *b, int64_t e0, int64_t e1, cudaStream_t s);
 void build_block_jacobi(Ctx &c);
 // solver.cu
 void spmv_device(Ctx &c, const double *x, double *y, double alpha, double beta, const double *yin);

@@ -26,6 +26,7 @@
 #include "gpz_internal.h"
 #include "gpz_shapes.h"
 #include "gpz_solver_common.cuh"
+#include "gpz_tc.cuh"
 
 namespace gpz {
 
@@ -683,63 +684,6 @@ constexpr uint32_t OFF_ST1 = OFF_GEO + kTcEl * 10 * 4;
 constexpr uint32_t OFF_TC_END = OFF_ST1 + 128 * 32 * 4;  // results staging (phase-2 rows)
 constexpr int kTcGather = kTcEl * 32 / kTcThreads;        // (element, shape) items per thread
 constexpr int kTcItems = (kTcEl * 27 + kTcThreads - 1) / kTcThreads;  // (element, point) items per thread
-constexpr int kTcWaitTries = 1 << 22;
-
-__device__ __forceinline__ uint32_t tc_smem(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
-__host__ __device__ __forceinline__ uint32_t kmaj(int r, int k, int kcols) {
-  return ((uint32_t)(r >> 3) * (uint32_t)(kcols >> 2) + (uint32_t)(k >> 2)) * 128u + (uint32_t)(r & 7) * 16u +
-         (uint32_t)(k & 3) * 4u;
-}
-__device__ __forceinline__ uint64_t tc_desc(uint32_t saddr, uint32_t sbo) {
-  return (uint64_t)((saddr >> 4) & 0x3FFF) | ((uint64_t)((128u >> 4) & 0x3FFF) << 16) |
-         ((uint64_t)((sbo >> 4) & 0x3FFF) << 32) | ((uint64_t)1 << 46);
-}
-__device__ __forceinline__ float tf32_rna(float x) {
-  uint32_t r;
-  asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(r) : "f"(x));
-  return __uint_as_float(r);
-}
-__device__ __forceinline__ void st_split(unsigned char *hi, unsigned char *lo, uint32_t off, float v) {
-  const float h = tf32_rna(v);
-  *(float *)(hi + off) = h;
-  *(float *)(lo + off) = tf32_rna(v - h);
-}
-__device__ __forceinline__ void tc_mma(uint32_t tm, uint64_t a, uint64_t b, uint32_t idesc, uint32_t acc) {
-  asm volatile("{\n.reg .pred p;\nsetp.ne.b32 p, %4, 0;\ntcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n}\n" ::"r"(tm),
-               "l"(a), "l"(b), "r"(idesc), "r"(acc));
-}
-__device__ __forceinline__ void tc_commit(uint64_t *mb) {
-  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(tc_smem(mb)));
-}
-// non-blocking test of an mbarrier phase: the waits below poll it with a short
-// sleep instead of the potentially-suspending try_wait, so a waiting thread is
-// never parked for a system-dependent time after the phase has completed
-__device__ __forceinline__ bool mb_test(uint64_t *mb, uint32_t parity) {
-  uint32_t done;
-  asm volatile("{\n.reg .pred p;\nmbarrier.test_wait.parity.shared::cta.b64 p, [%1], %2;\nselp.u32 %0, 1, 0, p;\n}\n"
-               : "=r"(done)
-               : "r"(tc_smem(mb)), "r"(parity)
-               : "memory");
-  return done != 0;
-}
-// bounded wait (kTcWaitTries polls of at most ~0.1 us apart)
-__device__ __forceinline__ bool tc_wait(uint64_t *mb, uint32_t parity) {
-  for (int it = 0; it < kTcWaitTries; it++) {
-    if (mb_test(mb, parity)) return true;
-    if (it > 16) __nanosleep(64);
-  }
-  return false;
-}
-__device__ __forceinline__ void tc_ld16(uint32_t taddr, float *v) {
-  uint32_t r[16];
-  asm volatile("tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
-               : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
-                 "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
-               : "r"(taddr));
-  asm volatile("tcgen05.wait::ld.sync.aligned;");
-#pragma unroll
-  for (int j = 0; j < 16; j++) v[j] = __uint_as_float(r[j]);
-}
 
 // U rows of a tile (the nodal values, split hi / lo), its corners and (lambda, mu);
 // every load is issued before the first store
@@ -1512,7 +1456,7 @@ __global__ void k_tl_fixrows(int64_t nc, const int32_t *__restrict__ cfix, doubl
 }
 
 // Blocked in-place Gauss-Jordan inversion of the SPD coarse matrix (no
-// pivoting), FP64, pivot blocks of kGjB rows.  With A = [[D, R], [C, E]] for
+// pivoting), in the element type T (the set-up runs it in FP32), pivot blocks of kGjB rows.  With A = [[D, R], [C, E]] for
 // the current pivot block D: D <- P = D^-1 (k_gj_diag), R <- P R (k_gj_row),
 // E <- E - C (P R) (k_gj_trail, with the original C), C <- -C P (k_gj_col).
 constexpr int kGjB = 32;
@@ -2064,7 +2008,7 @@ void two_level_assemble(Ctx &c) {
 // grid of translated Q2 hexes: K_e = k_e Khat (27 x 27; Khat the assembly's
 // reference element matrix at coefficient 1, the Poisson scale included), so the
 // operator over a tile of 128 elements is Y = U Khat^T: tcgen05.mma kind::tf32,
-// 3xTF32, M 128, N 32, K 32.  A 256-thread CTA (three per SM, persistent over
+// 3xTF32, M 128, N 32, K 32.  A 256-thread CTA (two per SM, persistent over
 // tiles) runs the same two-stage pipeline as the elasticity kernel with one
 // thread per element in each group: 4 gatherer warps (rows copied as one block,
 // the element's 27 values gathered, the translation removed -- Khat annihilates

@@ -385,8 +385,9 @@ __global__ void __launch_bounds__(kThreads) k_jac_resid(const int64_t *__restric
 }
 
 // ---- setup kernels for the mixed path and the block preconditioner
+template <typename TA>
 __global__ void k_build_bsr3(const int64_t *__restrict__ ia, const int32_t *__restrict__ ja,
-                             const double *__restrict__ a, int64_t nbrow, int64_t *__restrict__ bptr,
+                             const TA *__restrict__ a, int64_t nbrow, int64_t *__restrict__ bptr,
                              int32_t *__restrict__ bcol, float *__restrict__ bval, int *__restrict__ err) {
   const int lane = threadIdx.x & 31;
   const int64_t I = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) / 32;
@@ -412,8 +413,9 @@ __global__ void k_build_bsr3(const int64_t *__restrict__ ia, const int32_t *__re
 
 // fill the sliced-ELL planes from the full FP64 CSR (rows 3I..3I+2 of block
 // row I share their columns; block column j covers columns 3j'..3j'+2)
+template <typename TA>
 __global__ void k_fill_sell3(const int64_t *__restrict__ ia, const int32_t *__restrict__ ja,
-                             const double *__restrict__ a, const int64_t *__restrict__ soff,
+                             const TA *__restrict__ a, const int64_t *__restrict__ soff,
                              const int32_t *__restrict__ slen, const int32_t *__restrict__ sperm, int64_t nslice,
                              int64_t plane, int32_t *__restrict__ scol, float *__restrict__ sval, int *__restrict__ err) {
   const int64_t g = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -2291,9 +2293,12 @@ void build_sell(Ctx &c, Ctx::Sell &S, int64_t window) {
   S.soff.upload(soff.data(), soff.size(), c.stream);
   S.scol.alloc(std::max<int64_t>(S.plane, 1));
   S.sval.alloc((size_t)std::max<int64_t>(S.plane, 1) * 9);
-  k_fill_sell3<<<grid_for(S.nslice * 32, 256), 256, 0, c.stream>>>(c.d_ia.p, c.d_ja.p, c.d_a.p, S.soff.p, S.slen.p,
-                                                                   S.sperm.p, S.nslice, S.plane, S.scol.p, S.sval.p,
-                                                                   c.d_err.p);
+  if (c.a32_tensor)
+    k_fill_sell3<float><<<grid_for(S.nslice * 32, 256), 256, 0, c.stream>>>(
+        c.d_ia.p, c.d_ja.p, c.d_a32.p, S.soff.p, S.slen.p, S.sperm.p, S.nslice, S.plane, S.scol.p, S.sval.p, c.d_err.p);
+  else
+    k_fill_sell3<double><<<grid_for(S.nslice * 32, 256), 256, 0, c.stream>>>(
+        c.d_ia.p, c.d_ja.p, c.d_a.p, S.soff.p, S.slen.p, S.sperm.p, S.nslice, S.plane, S.scol.p, S.sval.p, c.d_err.p);
   c.launches++;
   GPZ_CUDA_TRY(cudaGetLastError());
   check_device_flag(c, "sliced ELL of 3x3 blocks");
@@ -2558,14 +2563,18 @@ void make_fp32_copy(Ctx &c, int variant) {
       c.d_bptr.alloc(c.nbrow + 1);
       c.d_bcol.alloc(std::max<int64_t>(c.nnz / 9, 1) + 16);  // slack for 16-byte rounded bulk copies
       c.d_bval.alloc(std::max<int64_t>(c.nnz, 1) + 16);
-      k_build_bsr3<<<grid_for(c.nbrow * 32, 256), 256, 0, c.stream>>>(c.d_ia.p, c.d_ja.p, c.d_a.p, c.nbrow,
-                                                                      c.d_bptr.p, c.d_bcol.p, c.d_bval.p, c.d_err.p);
+      if (c.a32_tensor)  // the FP32 element pass of this assembly
+        k_build_bsr3<float><<<grid_for(c.nbrow * 32, 256), 256, 0, c.stream>>>(
+            c.d_ia.p, c.d_ja.p, c.d_a32.p, c.nbrow, c.d_bptr.p, c.d_bcol.p, c.d_bval.p, c.d_err.p);
+      else
+        k_build_bsr3<double><<<grid_for(c.nbrow * 32, 256), 256, 0, c.stream>>>(
+            c.d_ia.p, c.d_ja.p, c.d_a.p, c.nbrow, c.d_bptr.p, c.d_bcol.p, c.d_bval.p, c.d_err.p);
       c.launches++;
       GPZ_CUDA_TRY(cudaGetLastError());
       check_device_flag(c, "3x3 block CSR");
     }
     c.have_bsr3 = true;
-    c.d_a32.release();
+    if (!c.a32_tensor) c.d_a32.release();  // (the FP32 element values stay: a later rebuild reads them)
     if (variant < 0 && c.spmv32_tuned >= 0) {
       tune_spmv32(c, c.spmv32_tuned, false);  // same pattern: rebuild the chosen layout only
     } else if (cached >= 0) {
@@ -2581,8 +2590,10 @@ void make_fp32_copy(Ctx &c, int variant) {
       }
     }
   } else {
-    c.d_a32.alloc(std::max<int64_t>(c.nnz, 1));
-    to_fp32(c);
+    if (!c.a32_tensor) {
+      c.d_a32.alloc(std::max<int64_t>(c.nnz, 1));
+      to_fp32(c);
+    }
     std::string key;
     int cached = -1;
     if (variant < 0 && c.spmv32_tuned < 0 && !c.tune_cache.empty()) {

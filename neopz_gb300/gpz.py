@@ -19,6 +19,7 @@ GPZ_EL_LINE, GPZ_EL_QUAD, GPZ_EL_HEX = 1, 2, 3
 GPZ_MAT_POISSON, GPZ_MAT_DARCY, GPZ_MAT_ELAST3D = 1, 2, 3
 GPZ_F_NONE, GPZ_F_CONST, GPZ_F_SINPROD, GPZ_F_QUADRATIC = 0, 1, 2, 3
 GPZ_PREC_FP64, GPZ_PREC_MIXED = 0, 1
+GPZ_FP32_ROUNDED, GPZ_FP32_ELEMENTS = 0, 1
 GPZ_SOLVER_CG, GPZ_SOLVER_GMRES, GPZ_SOLVER_MIXED_CG, GPZ_SOLVER_LEARNED_FCG, GPZ_SOLVER_LEARNED_MIXED_FCG = 1, 2, 3, 4, 5
 GPZ_SOLVER_JACOBI = 6
 GPZ_PRECOND_JACOBI, GPZ_PRECOND_BLOCK_JACOBI, GPZ_PRECOND_NODESET_JACOBI, GPZ_PRECOND_TWO_LEVEL = 1, 2, 3, 4
@@ -112,6 +113,8 @@ def lib():
         L.gpz_tuning_report.argtypes = [vp, ctypes.c_char_p, i64]
         L.gpz_tuning_cache.argtypes = [vp, ctypes.c_char_p]
         L.gpz_assembly_mode.argtypes = [vp, ctypes.c_int]
+        L.gpz_fp32_elements.argtypes = [vp, ctypes.c_int]
+        L.gpz_matrix_fp32_download.argtypes = [vp, vp]
         L.gpz_assemble.argtypes = [vp, i32]
         L.gpz_set_killed.argtypes = [vp, i32]
         L.gpz_equation_filter.argtypes = [vp, i64, vp]
@@ -347,6 +350,17 @@ class Context:
     def assembly_mode(self, mode):
         """-1 autotuned, 0 a launch per element bucket and colour (the default), 1 persistent per bucket."""
         self._check(lib().gpz_assembly_mode(self.h, int(mode)))
+
+    def fp32_elements(self, source):
+        """Source of the FP32 values of GPZ_PREC_MIXED: GPZ_FP32_ROUNDED (the FP64 matrix rounded, the default)
+        or GPZ_FP32_ELEMENTS (element matrices formed again in FP32: 3xTF32 tcgen05 products on the hexes)."""
+        self._check(lib().gpz_fp32_elements(self.h, int(source)))
+
+    def matrix_fp32(self):
+        """FP32 values of the last mixed assembly on the full CSR pattern (gpz_matrix_fp32_download)."""
+        a = np.zeros(self.nnz_full(), dtype=np.float32)
+        self._check(lib().gpz_matrix_fp32_download(self.h, _p(a)))
+        return a
 
     def tuning_cache(self, path):
         """File of the autotuners' choices kept across runs (gpz_tuning_cache); None: no cache."""
