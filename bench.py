@@ -494,12 +494,34 @@ def hp_leg(gpz, dev, n=40):
     ctx.assemble(gpz.GPZ_PREC_MIXED)
     sol = ctx.solve(solver=gpz.GPZ_SOLVER_MIXED_CG, precond=gpz.GPZ_PRECOND_BLOCK_JACOBI, tol=TOL, max_iter=200000,
                     reliable_delta=1e-2, check_every=64, want_x=False)
+    fp32 = fp32_element_pass(gpz, ctx, precond=gpz.GPZ_PRECOND_BLOCK_JACOBI)
     ctx.close()
     return {"workload": f"3D elasticity {n}^3 hexes, p uniform in {{1,2,3}} per element (seed 3, max rule on shared "
                         "sides), E lognormal(sigma=0.5) seed 3, nu=0.3, body force (0,0,-1), clamped z=0",
             "neq": grid.neq, "nnz_upper": nnz, "elements": grid.nel, "assembly_fp64_s": ms / 1e3,
             "elements_per_s": grid.nel / (ms / 1e3), "batching": rep,
             "mixed_cg": {"iterations": sol["iterations"], "true_resid": sol["true_resid"], "seconds": sol["seconds"],
+                         "rc": sol["rc"]},
+            "fp32_element_pass": fp32}
+
+
+def fp32_element_pass(gpz, ctx, precond, variant=-1):
+    """The FP32 element pass (gpz_fp32_elements: the hexes' element matrices as 3xTF32 tcgen05 GEMMs, into the
+    FP32 CSR of the mixed solves) on an assembled context: its time (CUDA events, the second of two mixed
+    assemblies) and the mixed CG over the FP32 operator built from it, beside the same solve over the rounded
+    FP64 matrix."""
+    ctx.fp32_elements(gpz.GPZ_FP32_ELEMENTS)
+    for _ in range(2):
+        ctx.assemble(gpz.GPZ_PREC_MIXED)
+    rep = ctx.assembly_report()["fp32_elements"]
+    sol = ctx.solve(solver=gpz.GPZ_SOLVER_MIXED_CG, precond=precond, tol=TOL, max_iter=200000, reliable_delta=1e-2,
+                    check_every=64, want_x=False, spmv_variant=variant)
+    ctx.fp32_elements(gpz.GPZ_FP32_ROUNDED)
+    return {"pass_ms": rep["ms"], "tensor_core_elements": rep["tensor_core_elements"],
+            "cuda_core_elements": rep["cuda_core_elements"],
+            "tensor_core_elements_per_s": rep["tensor_core_elements"] / (rep["ms"] / 1e3) if rep["ms"] else None,
+            "fp32_operator": ctx.tuning_report().get("chosen"),
+            "mixed_cg": {"iterations": sol["iterations"], "seconds": sol["seconds"], "true_resid": sol["true_resid"],
                          "rc": sol["rc"]}}
 
 
@@ -567,6 +589,7 @@ def poisson3d_leg(gpz, dev, n=64, variant=-1):
                        check_every=64, want_x=False, spmv_variant=variant)
     tune = ctx.tuning_report()
     op_ms = ctx.time_kernel(gpz.GPZ_KERNEL_SPMV_FP32, 20)
+    fp32 = fp32_element_pass(gpz, ctx, gpz.GPZ_PRECOND_JACOBI, variant=0)  # the CSR copy reads the pass's values
     ctx.close()
     return {"workload": f"3D Darcy/Poisson {n}^3 hex Q2, k lognormal(sigma=1) seed 1, u = 0 on the boundary (penalty)",
             "neq": grid.neq, "nnz_upper": nnz, "assembly_fp64_s": ms / 1e3, "volume_elements_per_s": n ** 3 / (ms / 1e3),
@@ -575,7 +598,8 @@ def poisson3d_leg(gpz, dev, n=64, variant=-1):
             "mixed_cg": {"iterations": mx["iterations"], "seconds": mx["seconds"], "true_resid": mx["true_resid"],
                          "speedup_vs_fp64_jacobi_pcg": f64["seconds"] / mx["seconds"] if mx["seconds"] else None,
                          "fp32_operator": tune.get("chosen"), "operator_autotune_ms": tune,
-                         "operator_ms_per_launch": op_ms}}
+                         "operator_ms_per_launch": op_ms},
+            "fp32_element_pass": fp32}
 
 
 def learned_leg(gpz, dev, n=256, seeds=(10000, 10001, 10002)):

@@ -1272,8 +1272,14 @@ void assemble_fp32_elements(Ctx &c) {
   cudaEventDestroy(e1);
   check_device_flag(c, "FP32 element matrices");
   c.a32_tensor = true;
+  std::string per;
+  for (const Bucket *b : c.buckets)
+    if (b->tc_per_sm > 0)
+      per += std::string(per.empty() ? "" : ", ") + "\"" + std::to_string(b->nshape) + (b->hp ? "_hp" : "") +
+             "\": " + std::to_string(b->tc_per_sm);
   c.fp32_report = "{\"source\": \"element_matrices_fp32\", \"tensor_core_elements\": " + std::to_string(ntc) +
-                  ", \"cuda_core_elements\": " + std::to_string(ncc) + ", \"ms\": " + std::to_string(ms) + "}";
+                  ", \"cuda_core_elements\": " + std::to_string(ncc) + ", \"ms\": " + std::to_string(ms) +
+                  ", \"ctas_per_sm\": {" + per + "}}";
 }
 
 }  // namespace gpz

@@ -20,12 +20,14 @@
 // Jacobians are formed in FP32 from corner coordinates taken relative to the
 // element's first corner.
 //
-// A CTA of 8 warps is persistent over the elements of one bucket and colour:
-// per element it builds X (hi, lo) in shared memory, one thread issues the MMAs
-// and commits to an mbarrier, all wait (bounded; a timeout sets an error flag
-// and ends the CTA after the MMAs in flight are waited for), the accumulator is
-// staged through shared memory (over the operands, which the MMAs no longer
-// read) and scattered.  TMEM columns per CTA: 32 (Q1), 128 (Q2), 512 (Q3, two
+// A CTA of 8 warps (16 for the order-3 table) is persistent over the elements
+// of one bucket and colour: per element it builds X (hi, lo) in shared memory,
+// one thread issues the MMAs and commits to an mbarrier, and the next element's
+// connectivity and corners are loaded while they run; all wait (bounded; a
+// timeout sets an error flag and ends the CTA after the MMAs in flight are
+// waited for), the accumulator is staged through shared memory (over the
+// operands, which the MMAs no longer read) and scattered through the element's
+// offset table, read into shared memory with its rows' starts.  TMEM columns per CTA: 32 (Q1), 128 (Q2), 512 (Q3, two
 // row tiles); the launcher sizes the dynamic shared memory so that the CTAs
 // resident on one SM never ask for more than the SM's 512 columns.
 #include <algorithm>
@@ -39,7 +41,9 @@ namespace gpz {
 
 namespace {
 
-constexpr int kEtThreads = 256;  // 8 warps: warps w and w + 4 share TMEM lane quarter w
+// threads per CTA: 8 warps, 16 for the order-3 table (one CTA per SM there: 512 TMEM columns, 154 KB of
+// operands); warps w, w + 4, ... share TMEM lane quarter w % 4
+__host__ __device__ constexpr int et_threads(int nt) { return nt >= 64 ? 512 : 256; }
 constexpr int kEtMaxQ = 64;      // integration points (hex 4 x 4 x 4)
 constexpr int kErrEtRange = 1 << 19, kErrEtWait = 1 << 20;
 
@@ -78,12 +82,48 @@ __host__ __device__ inline uint32_t et_region(int nt, int kp) {
   const uint32_t stage = (uint32_t)et_rows(nt) * (uint32_t)(et_np(nt) + 4) * 4u;
   return ((ops > stage ? ops : stage) + 1023u) / 1024u * 1024u;
 }
+constexpr int kEtSides = 27;  // sides of a hex (the offset table is kEtSides^2)
 __host__ __device__ inline uint32_t et_smem(int nt, int kp) {
-  return et_region(nt, kp) + kEtMaxQ * 9 * 4 + 24 * 4 + (uint32_t)nt * 8 + 3u * (uint32_t)nt * 4 + 64;
+  return et_region(nt, kp) + kEtMaxQ * 9 * 4 + 24 * 4 + (uint32_t)nt * 8 + 3u * (uint32_t)nt * 4 +
+         kEtSides * kEtSides * 4 + 8 + 3u * (uint32_t)nt * 8 + 64;
+}
+
+// One element's data, loaded by every thread for its own part: corner coordinate tid (tid < 24, relative to
+// corner 0), shape tid's first equation, side, table index and index inside its side (tid < nsh), and (thread 0)
+// the offset-table start and the coefficient.  Loaded for the next element while the MMAs of the current one run.
+struct EtElem {
+  float cx;
+  int64_t row, offbase;
+  int side, fa, ka, nsh;
+  double cf;
+};
+
+template <int NT, bool HP>
+__device__ __forceinline__ EtElem et_fetch(const EtArgs &P, const EtHp &H, const int64_t *__restrict__ elems,
+                                           int64_t ie, int tid) {
+  EtElem r{};
+  const int64_t e = elems[ie];
+  r.nsh = HP ? H.n[ie] : NT;
+  if (tid < 24) {
+    const int k = tid / 3, j = tid % 3;
+    const int64_t node = P.el_nodes[e * 8 + k], node0 = P.el_nodes[e * 8];
+    r.cx = (float)(P.xyz[node * 3 + j] - P.xyz[node0 * 3 + j]);
+  }
+  if (tid < r.nsh) {
+    r.fa = HP ? (int)H.full[ie * kMaxShapes + tid] : tid;
+    r.ka = HP ? (int)H.k[ie * kMaxShapes + tid] : P.sk[tid];
+    r.side = P.sside[r.fa];
+    r.row = P.bpos[P.el_conn[e * 27 + r.side]] + (int64_t)r.ka * P.nst;
+  }
+  if (tid == 0) {
+    r.offbase = P.offbase[e];
+    r.cf = P.coef ? P.coef[e] : (P.kind == GPZ_MAT_ELAST3D ? P.E : P.coef_const);
+  }
+  return r;
 }
 
 template <int NT, bool HP>
-__global__ void __launch_bounds__(kEtThreads) k_elem_tc(EtArgs P, EtHp H, const int64_t *__restrict__ elems,
+__global__ void __launch_bounds__(et_threads(NT)) k_elem_tc(EtArgs P, EtHp H, const int64_t *__restrict__ elems,
                                                         int64_t n) {
   constexpr int R = et_rows(NT), MT = et_mt(NT), NP = et_np(NT), LD = NP + 4;
   constexpr uint32_t COLS = et_cols(NT);
@@ -92,6 +132,7 @@ __global__ void __launch_bounds__(kEtThreads) k_elem_tc(EtArgs P, EtHp H, const 
   __shared__ __align__(8) uint64_t s_mb;
   __shared__ float s_c[3];
   __shared__ int64_t s_offbase;
+  __shared__ int s_nsh;
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const int kp = P.kp;
   const uint32_t opsz = (uint32_t)MT * 128u * (uint32_t)kp * 4u;  // bytes of one operand copy
@@ -102,6 +143,10 @@ __global__ void __launch_bounds__(kEtThreads) k_elem_tc(EtArgs P, EtHp H, const 
   float *sCx = sMq + kEtMaxQ * 9;       // [8][3] corners relative to corner 0
   int64_t *sRow = (int64_t *)(sCx + 24);
   int *sSide = (int *)(sRow + NT), *sIdx = sSide + NT, *sK = sIdx + NT;
+  int *sOff = sK + NT;                                                          // [27][27] side-pair offsets
+  int64_t *sIa = (int64_t *)(((uintptr_t)(sOff + kEtSides * kEtSides) + 7) & ~(uintptr_t)7);  // [NT][3] row starts
+  constexpr int kEtThreads = et_threads(NT);
+  static_assert(NT < kEtThreads, "one thread per shape");
 
   if (warp == 0) {
     asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(tc_smem(&s_tmem)),
@@ -122,26 +167,20 @@ __global__ void __launch_bounds__(kEtThreads) k_elem_tc(EtArgs P, EtHp H, const 
   uint32_t phase = 0;
   bool failed = false;
 
+  EtElem nx{};
+  if (blockIdx.x < n) nx = et_fetch<NT, HP>(P, H, elems, blockIdx.x, tid);
   for (int64_t ie = blockIdx.x; ie < n; ie += gridDim.x) {
-    const int64_t e = elems[ie];
-    const int nsh = HP ? H.n[ie] : NT;
-    if (tid < 24) {
-      const int k = tid / 3, j = tid % 3;
-      const int64_t node = P.el_nodes[e * 8 + k], node0 = P.el_nodes[e * 8];
-      sCx[tid] = (float)(P.xyz[node * 3 + j] - P.xyz[node0 * 3 + j]);
-    }
-    for (int a = tid; a < nsh; a += kEtThreads) {
-      const int fa = HP ? (int)H.full[ie * kMaxShapes + a] : a;
-      const int ka = HP ? (int)H.k[ie * kMaxShapes + a] : P.sk[a];
-      const int side = P.sside[fa];
-      sRow[a] = P.bpos[P.el_conn[e * 27 + side]] + (int64_t)ka * P.nst;
-      sSide[a] = side;
-      sIdx[a] = fa;
-      sK[a] = ka;
+    if (tid < 24) sCx[tid] = nx.cx;
+    if (tid < nx.nsh) {
+      sRow[tid] = nx.row;
+      sSide[tid] = nx.side;
+      sIdx[tid] = nx.fa;
+      sK[tid] = nx.ka;
     }
     if (tid == 0) {
-      s_offbase = P.offbase[e];
-      const double cf = P.coef ? P.coef[e] : (P.kind == GPZ_MAT_ELAST3D ? P.E : P.coef_const);
+      s_nsh = nx.nsh;
+      s_offbase = nx.offbase;
+      const double cf = nx.cf;
       if (P.kind == GPZ_MAT_ELAST3D) {
         const double nu = P.nu;
         s_c[0] = (float)(cf / (2. + 2. * nu));                          // C1 = mu
@@ -153,6 +192,13 @@ __global__ void __launch_bounds__(kEtThreads) k_elem_tc(EtArgs P, EtHp H, const 
       }
     }
     __syncthreads();
+    const int nsh = s_nsh;
+    // the element's side-pair offset table and its rows' starts, read once (the scatter looks them up)
+    for (int i = tid; i < P.nsides * P.nsides; i += kEtThreads) sOff[i] = P.off[s_offbase + i];
+    for (int i = tid; i < nsh * P.nst; i += kEtThreads) {
+      const int64_t row = sRow[i / P.nst] + i % P.nst;
+      sIa[i] = (row >= 0 && row < P.neq) ? P.ia[row] : -1;
+    }
     // per point: the Jacobian from the corner shapes' gradients (the table's first 8 shapes)
     for (int q = tid; q < P.nq; q += kEtThreads) {
       float a[3][3] = {{0.f, 0.f, 0.f}, {0.f, 0.f, 0.f}, {0.f, 0.f, 0.f}};
@@ -216,6 +262,7 @@ __global__ void __launch_bounds__(kEtThreads) k_elem_tc(EtArgs P, EtHp H, const 
       }
       tc_commit(&s_mb);
     }
+    if (ie + gridDim.x < n) nx = et_fetch<NT, HP>(P, H, elems, ie + gridDim.x, tid);  // in flight during the MMAs
     const bool ok = tc_wait(&s_mb, phase);
     if (__syncthreads_or(!ok)) {
       failed = true;
@@ -225,12 +272,12 @@ __global__ void __launch_bounds__(kEtThreads) k_elem_tc(EtArgs P, EtHp H, const 
     asm volatile("tcgen05.fence::after_thread_sync;");
     // accumulator rows -> staging (float4 stores; the row stride LD = 4 mod 32 words keeps them conflict-free)
     {
-      const int quarter = warp & 3, half = warp >> 2;
+      const int quarter = warp & 3, part = warp >> 2, nparts = kEtThreads / 128;
 #pragma unroll 1
       for (int t = 0; t < MT; t++) {
         const int r = t * 128 + quarter * 32 + lane;
 #pragma unroll 1
-        for (int c0 = half * 16; c0 < NP; c0 += 32) {
+        for (int c0 = part * 16; c0 < NP; c0 += 16 * nparts) {
           float v[16];
           tc_ld16(tm + ((uint32_t)(quarter * 32) << 16) + (uint32_t)(t * NP + c0), v);
           if (r < R) {
@@ -266,7 +313,6 @@ __global__ void __launch_bounds__(kEtThreads) k_elem_tc(EtArgs P, EtHp H, const 
     // the element's rows into the FP32 CSR: a task is a shape a and 32 shapes b (one per lane)
     const int nbc = (nsh + 31) >> 5, ns = P.nsides;
     const float C1 = s_c[0], C2 = s_c[1], C3 = s_c[2];
-    const int64_t ob = s_offbase;
     for (int task = warp; task < nsh * nbc; task += kEtThreads / 32) {
       const int a = task / nbc, b = (task - a * nbc) * 32 + lane;
       if (b >= nsh) continue;
@@ -276,14 +322,13 @@ __global__ void __launch_bounds__(kEtThreads) k_elem_tc(EtArgs P, EtHp H, const 
 #pragma unroll
         for (int j = 0; j < 3; j++) S[i][j] = pst[(size_t)(i * NT + a) * LD + j * NT + b];
       const float tr = S[0][0] + S[1][1] + S[2][2];
-      const int32_t oab = P.off[ob + sSide[a] * ns + sSide[b]];
+      const int32_t oab = sOff[sSide[a] * ns + sSide[b]];
       if (oab < 0) {
         atomicOr(P.err, kErrEtRange);
         continue;
       }
       if (P.nst == 1) {
-        const int64_t row = sRow[a];
-        const int64_t slot = (row >= 0 && row < P.neq) ? P.ia[row] + oab + sK[b] : -1;
+        const int64_t slot = sIa[a] >= 0 ? sIa[a] + oab + sK[b] : -1;
         const float v = C1 * tr;
         if (slot < 0 || slot >= P.nnz) {
           atomicOr(P.err, kErrEtRange);
@@ -302,8 +347,7 @@ __global__ void __launch_bounds__(kEtThreads) k_elem_tc(EtArgs P, EtHp H, const 
       bool bad = false;
 #pragma unroll
       for (int s = 0; s < 3; s++) {
-        const int64_t row = sRow[a] + s;
-        slot[s] = (row >= 0 && row < P.neq) ? P.ia[row] + oab + (int64_t)sK[b] * 3 : -1;
+        slot[s] = sIa[a * 3 + s] >= 0 ? sIa[a * 3 + s] + oab + (int64_t)sK[b] * 3 : -1;
         bad |= slot[s] < 0 || slot[s] + 2 >= P.nnz;
       }
       if (bad) {
@@ -361,24 +405,37 @@ void elem_tc_launch(Ctx &c, Bucket *b, int64_t e0, int64_t e1, cudaStream_t s) {
     b->d_w32.upload(w.data(), w.size(), s);
   }
   if (b->tc_smem == 0) {
-    int dev = 0, nsm = 0;
+    int dev = 0, nsm = 0, smem_sm = 0, reserved = 0;
     GPZ_CUDA_TRY(cudaGetDevice(&dev));
     GPZ_CUDA_TRY(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
+    GPZ_CUDA_TRY(cudaDeviceGetAttribute(&smem_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev));
+    GPZ_CUDA_TRY(cudaDeviceGetAttribute(&reserved, cudaDevAttrReservedSharedMemoryPerBlock, dev));
     uint32_t smem = et_smem(nt, kp);
     const int cols = et_cols(nt);
     constexpr uint32_t kMaxDyn = 225u * 1024u;  // 227 KB per CTA less the static shared memory
     GPZ_REQUIRE(smem <= kMaxDyn, GPZ_E_UNSUPPORTED_ELEMENT, "tensor-core element kernel: shared memory");
     GPZ_CUDA_TRY(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kMaxDyn));
-    int per = 0;
-    // the CTAs resident on one SM must not ask for more than its 512 TMEM columns (an allocation would wait)
-    for (;;) {
-      GPZ_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k, kEtThreads, smem));
-      if (per * cols <= 512 || smem + 2048 > kMaxDyn) break;
+    cudaFuncAttributes fa{};
+    GPZ_CUDA_TRY(cudaFuncGetAttributes(&fa, k));
+    // resident CTAs per SM from the kernel's registers (allocated per warp in units of 256), the threads and
+    // the shared memory; the CTAs resident on one SM must not ask for more than its 512 TMEM columns (an
+    // allocation would wait for another CTA to end), so the shared memory is padded until they cannot
+    const int regs_warp = (fa.numRegs * 32 + 255) / 256 * 256;
+    const int nth = et_threads(nt);
+    const int per_regs = regs_warp > 0 ? 65536 / (regs_warp * (nth / 32)) : 8;
+    auto per_of = [&](uint32_t sm) {
+      const int per_smem = (int)((uint32_t)smem_sm / (sm + (uint32_t)fa.sharedSizeBytes + (uint32_t)reserved));
+      return std::min(std::min(per_regs, 2048 / nth), per_smem);
+    };
+    int per = per_of(smem);
+    while (per * cols > 512 && smem + 2048 <= kMaxDyn) {
       smem += 2048;
+      per = per_of(smem);
     }
     GPZ_REQUIRE(per >= 1 && per * cols <= 512, GPZ_E_CUDA, "tensor-core element kernel: no resident CTA");
     b->tc_smem = (int)smem;
     b->tc_resident = per * nsm;
+    b->tc_per_sm = per;
   }
   EtArgs P{};
   P.dphi = b->d_dphi32.p;
@@ -415,7 +472,7 @@ void elem_tc_launch(Ctx &c, Bucket *b, int64_t e0, int64_t e1, cudaStream_t s) {
   }
   const int64_t ne = e1 - e0;
   const unsigned grid = (unsigned)std::max<int64_t>(1, std::min<int64_t>(ne, b->tc_resident));
-  k<<<grid, kEtThreads, (size_t)b->tc_smem, s>>>(P, H, b->d_elems.p + e0, ne);
+  k<<<grid, et_threads(nt), (size_t)b->tc_smem, s>>>(P, H, b->d_elems.p + e0, ne);
   c.launches++;
   GPZ_CUDA_TRY(cudaGetLastError());
 }

@@ -111,7 +111,7 @@ struct Bucket {
   int qgrid = 1;
   // tensor-core FP32 element matrices (gpz_elem_tc.cu): FP32 tables, dynamic shared memory, resident CTAs
   DBuf<float> d_dphi32, d_w32;
-  int tc_smem = 0, tc_resident = 0;
+  int tc_smem = 0, tc_resident = 0, tc_per_sm = 0;
 };
 
 // ---------------------------------------------------------------- solver workspace
