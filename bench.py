@@ -393,6 +393,8 @@ def run_gpu(args):
         mark("context")
         c2.upload_mesh(grid)
         mark("mesh_upload")
+        ph["mesh_upload_parts_ms"] = c2.assembly_report().get("mesh_upload_ms")
+        tp = time.perf_counter()
         c2.build_pattern(True)
         mark("pattern")
         c2.assemble(gpz.GPZ_PREC_MIXED)
@@ -400,8 +402,9 @@ def run_gpu(args):
         kw = dict(tol=TOL, max_iter=200000, reliable_delta=1e-2, check_every=PATH_CHECK[args.path], want_x=True)
         if args.path == "learned":
             c2.learned_init(rank=LEARNED_RANK, seed=0)
-            c2.set_learned_params(weights)
             mark("learned_setup")
+            c2.set_learned_params(weights)
+            mark("learned_weights")
             r2 = c2.solve(solver=gpz.GPZ_SOLVER_LEARNED_MIXED_FCG, precond=LEARNED_BASE, **kw)
         else:
             r2 = c2.solve(solver=gpz.GPZ_SOLVER_MIXED_CG, precond=gpz.GPZ_PRECOND_TWO_LEVEL if args.path ==

@@ -1,4 +1,5 @@
 // C ABI entry points (include/gpz.h).  No exception crosses this boundary.
+#include <chrono>
 #include <algorithm>
 #include <cstring>
 
@@ -117,6 +118,7 @@ int gpz_mesh_upload(gpz_ctx *ctx, const gpz_mesh_desc *d) {
     GPZ_REQUIRE(d->nstate == 1 || d->nstate == 3, GPZ_E_INVALID, "nstate");
     GPZ_REQUIRE(d->nel >= 0 && d->nnodes >= 0 && d->nconnects >= 0 && d->neq >= 0, GPZ_E_INVALID, "sizes");
     GPZ_REQUIRE(d->neq < INT32_MAX, GPZ_E_INVALID, "neq must fit 32-bit column indices");
+    const auto t0 = std::chrono::steady_clock::now();
     GPZ_REQUIRE(d->node_xyz && d->el_type && d->el_mat && d->el_nodes && d->el_order && d->el_conn &&
                     d->conn_order && d->block_pos && d->block_size && (d->nmat == 0 || d->mats),
                 GPZ_E_INVALID, "null array");
@@ -143,6 +145,7 @@ int gpz_mesh_upload(gpz_ctx *ctx, const gpz_mesh_desc *d) {
       }
       GPZ_REQUIRE(d->el_order[e] >= 1 && d->el_order[e] <= 3, GPZ_E_UNSUPPORTED_ELEMENT, "order must be 1..3");
     }
+    const auto t1 = std::chrono::steady_clock::now();
     c.dim = d->dim;
     c.nstate = d->nstate;
     c.nel = d->nel;
@@ -170,7 +173,15 @@ int gpz_mesh_upload(gpz_ctx *ctx, const gpz_mesh_desc *d) {
     c.d_block_pos.upload(d->block_pos, d->nconnects, s);
     if (d->el_coef) c.d_coef.upload(d->el_coef, d->nel, s);
     else c.d_coef.release();
+    GPZ_CUDA_TRY(cudaStreamSynchronize(s));
+    const auto t2 = std::chrono::steady_clock::now();
     build_buckets(c, *d);
+    const auto t3 = std::chrono::steady_clock::now();
+    auto ms = [](std::chrono::steady_clock::time_point a, std::chrono::steady_clock::time_point b) {
+      return std::to_string(std::chrono::duration<double, std::milli>(b - a).count());
+    };
+    c.upload_report = "{\"checks\": " + ms(t0, t1) + ", \"copies\": " + ms(t1, t2) + ", \"buckets\": " + ms(t2, t3) +
+                      ", \"bucket_parts\": " + c.bucket_report + "}";
     c.er.reset();
     c.have_mesh = true;
     c.have_pattern = c.have_matrix = c.have_solution = c.have_a32 = c.have_bjinv = c.have_rhs = false;
@@ -324,7 +335,8 @@ int gpz_assembly_report(gpz_ctx *ctx, char *buf, int64_t len) {
                     ", \"colours\": " + std::to_string(c.ncolours) + ", \"hp_block_size_ms\": " +
                     (c.asm_tune_report.empty() ? std::string("null") : c.asm_tune_report) + ", \"launch_mode_ms\": " +
                     (c.asm_mode_report.empty() ? std::string("null") : c.asm_mode_report) + ", \"fp32_elements\": " +
-                    (c.fp32_report.empty() ? std::string("null") : c.fp32_report) + "}";
+                    (c.fp32_report.empty() ? std::string("null") : c.fp32_report) + ", \"mesh_upload_ms\": " +
+                    (c.upload_report.empty() ? std::string("null") : c.upload_report) + "}";
     GPZ_REQUIRE((int64_t)r.size() < len, GPZ_E_INVALID, "buffer too small");
     std::copy(r.begin(), r.end(), buf);
     buf[r.size()] = 0;

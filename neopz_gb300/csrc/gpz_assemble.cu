@@ -11,8 +11,10 @@
 // so the read-modify-write needs no atomics.  Entries with |v| < 1e-12 are
 // skipped exactly as TPZSYsmpMatrix::AddKel does (Matrix/pzsysmp.cpp:369-411).
 #include <algorithm>
+#include <chrono>
 #include <cmath>
 #include <map>
+#include <memory>
 
 #include "gpz_internal.h"
 #include "gpz_shapes.h"
@@ -659,12 +661,14 @@ __global__ void k_to_fp32(const double *__restrict__ a, float *__restrict__ b, i
 void build_buckets(Ctx &c, const gpz_mesh_desc &d) {
   for (Bucket *b : c.buckets) delete b;
   c.buckets.clear();
-  std::map<BucketKey, int> index;
-  std::vector<int> el_bucket(c.nel, -1);
-  std::vector<uint8_t> act_full((size_t)c.nel * kMaxShapes, 0), act_k((size_t)c.nel * kMaxShapes, 0);
+  const auto t0 = std::chrono::steady_clock::now();
+  // rows of the hp elements' active shapes (written and read for hp elements only)
+  std::unique_ptr<uint8_t[]> act_full(new uint8_t[(size_t)c.nel * kMaxShapes]),
+      act_k(new uint8_t[(size_t)c.nel * kMaxShapes]);
   std::vector<int32_t> act_n(c.nel, 0);
-  for (int64_t e = 0; e < c.nel; e++) {
-    BucketKey k{};
+  // the bucket key of element e, and for an hp element its active shapes
+  auto key_of = [&](int64_t e, BucketKey &k) {
+    k = BucketKey{};
     k.type = d.el_type[e];
     GPZ_REQUIRE(k.type == GPZ_EL_LINE || k.type == GPZ_EL_QUAD || k.type == GPZ_EL_HEX, GPZ_E_UNSUPPORTED_ELEMENT,
                 "element type");
@@ -689,17 +693,16 @@ void build_buckets(Ctx &c, const gpz_mesh_desc &d) {
     // IntegrationRuleOrder(MaxOrder): the largest order of the element's connects
     // (hp sides set by SetSideOrder re-run AdjustIntegrationRule,
     // Mesh/pzinterpolationspace.cpp:69-83); equal to the element's p when p is uniform
-    int p = 1;
-    for (int s = t.ncorner; s < t.nsides; s++) p = std::max(p, (int)d.conn_order[d.el_conn[e * 27 + s]]);
-    if (k.is_bc || m->kind == GPZ_MAT_ELAST3D) k.intorder = 2 * p;
-    else k.intorder = (p < m->forcing_porder) ? m->forcing_porder + p : 2 * p;
     int eorder[19];
+    int p = 1;
     bool uniform = true;
     for (int s = t.ncorner; s < t.nsides; s++) {
-      int64_t cn = d.el_conn[e * 27 + s];
-      eorder[s - t.ncorner] = d.conn_order[cn];
-      uniform &= eorder[s - t.ncorner] == p;
+      eorder[s - t.ncorner] = d.conn_order[d.el_conn[e * 27 + s]];
+      p = std::max(p, eorder[s - t.ncorner]);
     }
+    for (int s = t.ncorner; s < t.nsides; s++) uniform &= eorder[s - t.ncorner] == p;
+    if (k.is_bc || m->kind == GPZ_MAT_ELAST3D) k.intorder = 2 * p;
+    else k.intorder = (p < m->forcing_porder) ? m->forcing_porder + p : 2 * p;
     // uniform elements keep their own tables; an element of uneven side orders
     // joins the hp class of its largest order, whose table is the full element
     k.hp = uniform ? 0 : 1;
@@ -718,6 +721,8 @@ void build_buckets(Ctx &c, const gpz_mesh_desc &d) {
       // side its order-o functions, found by their Chebyshev index tuple
       int n = 0;
       uint8_t *rf = &act_full[e * kMaxShapes], *rk = &act_k[e * kMaxShapes];
+      std::fill(rf, rf + kMaxShapes, (uint8_t)0);
+      std::fill(rk, rk + kMaxShapes, (uint8_t)0);
       for (int a = 0; a < t.ncorner; a++, n++) {
         rf[n] = (uint8_t)a;
         rk[n] = 0;
@@ -739,73 +744,124 @@ void build_buckets(Ctx &c, const gpz_mesh_desc &d) {
       }
       act_n[e] = n;
     }
-    auto it = index.find(k);
-    int bi;
-    if (it == index.end()) {
-      bi = (int)c.buckets.size();
-      index[k] = bi;
-      Bucket *b = new Bucket();
-      b->key = k;
-      b->nsides = t.nsides;
-      b->ncorner = t.ncorner;
-      b->dim = t.dim;
-      b->nstate = c.nstate;
-      std::vector<double> pts;
-      gauss_rule(k.type, k.intorder, pts, b->w);
-      b->nq = (int)b->w.size();
-      GPZ_REQUIRE(b->nq <= kMaxQp, GPZ_E_UNSUPPORTED_ELEMENT, "too many integration points");
-      double phi[kMaxShapes], dphi[3 * kMaxShapes];
-      int so[kMaxShapes], sk[kMaxShapes];
-      for (int q = 0; q < b->nq; q++) {
-        int n = eval_shapes(k.type, k.orders, k.trans, &pts[q * t.dim], phi, dphi, kMaxShapes, so, sk);
-        if (q == 0) {
-          b->nshape = n;
-          b->shape_side.assign(so, so + n);
-          b->shape_k.assign(sk, sk + n);
-          b->phi.resize((size_t)b->nq * n);
-          b->dphi.resize((size_t)b->nq * t.dim * n);
-        }
-        for (int a = 0; a < n; a++) {
-          b->phi[q * n + a] = phi[a];
-          for (int dd = 0; dd < t.dim; dd++) b->dphi[(q * t.dim + dd) * n + a] = dphi[dd * kMaxShapes + a];
-        }
+  };
+  // a new bucket's shape tables (quadrature, shapes and gradients per point, the reference Gram of volume hexes)
+  auto make_bucket = [&](const BucketKey &k) {
+    const ElemTopo &t = topo(k.type);
+    Bucket *b = new Bucket();
+    b->key = k;
+    b->nsides = t.nsides;
+    b->ncorner = t.ncorner;
+    b->dim = t.dim;
+    b->nstate = c.nstate;
+    std::vector<double> pts;
+    gauss_rule(k.type, k.intorder, pts, b->w);
+    b->nq = (int)b->w.size();
+    if (b->nq > kMaxQp) {
+      delete b;
+      throw Error{GPZ_E_UNSUPPORTED_ELEMENT, "too many integration points"};
+    }
+    double phi[kMaxShapes], dphi[3 * kMaxShapes];
+    int so[kMaxShapes], sk[kMaxShapes];
+    for (int q = 0; q < b->nq; q++) {
+      int n = eval_shapes(k.type, k.orders, k.trans, &pts[q * t.dim], phi, dphi, kMaxShapes, so, sk);
+      if (q == 0) {
+        b->nshape = n;
+        b->shape_side.assign(so, so + n);
+        b->shape_k.assign(sk, sk + n);
+        b->phi.resize((size_t)b->nq * n);
+        b->dphi.resize((size_t)b->nq * t.dim * n);
       }
-      b->ndof = b->nshape * c.nstate;
-      if (k.type == GPZ_EL_HEX && !k.is_bc) {
-        const int nt = b->nshape;
-        b->ghat.assign((size_t)nt * nt * 9, 0.0);
-        for (int a = 0; a < nt; a++)
+      for (int a = 0; a < n; a++) {
+        b->phi[q * n + a] = phi[a];
+        for (int dd = 0; dd < t.dim; dd++) b->dphi[(q * t.dim + dd) * n + a] = dphi[dd * kMaxShapes + a];
+      }
+    }
+    b->ndof = b->nshape * c.nstate;
+    if (k.type == GPZ_EL_HEX && !k.is_bc) {
+      // compensated (Neumaier) double sums over the points, shape rows on the host threads (a software
+      // long double, as on aarch64, is ~100x slower for the order-3 tables)
+      const int nt = b->nshape;
+      b->ghat.assign((size_t)nt * nt * 9, 0.0);
+      host_parallel(nt, [&](int64_t a0, int64_t a1) {
+        for (int64_t a = a0; a < a1; a++)
           for (int bb = 0; bb < nt; bb++)
             for (int i = 0; i < 3; i++)
               for (int j = 0; j < 3; j++) {
-                long double acc = 0.0L;
-                for (int q = 0; q < b->nq; q++)
-                  acc += (long double)b->w[q] * b->dphi[(q * 3 + i) * nt + a] * b->dphi[(q * 3 + j) * nt + bb];
-                b->ghat[((size_t)a * nt + bb) * 9 + i * 3 + j] = (double)acc;
+                double sum = 0.0, comp = 0.0;
+                for (int q = 0; q < b->nq; q++) {
+                  const double x = b->w[q] * b->dphi[(q * 3 + i) * nt + a] * b->dphi[(q * 3 + j) * nt + bb];
+                  const double t = sum + x;
+                  comp += std::fabs(sum) >= std::fabs(x) ? (sum - t) + x : (x - t) + sum;
+                  sum = t;
+                }
+                b->ghat[((size_t)a * nt + bb) * 9 + i * 3 + j] = sum + comp;
               }
-      }
-      b->hp = k.hp != 0;
-      GPZ_REQUIRE(b->hp ? select_hp(k.type, c.nstate, k.is_bc).one != nullptr
-                        : select_kernel(k.type, b->nshape, c.nstate, k.is_bc).one != nullptr,
-                  GPZ_E_UNSUPPORTED_ELEMENT, "no kernel for this element bucket");
-      c.buckets.push_back(b);
-    } else {
-      bi = it->second;
+      }, 8);
     }
-    el_bucket[e] = bi;
-  }
+    b->hp = k.hp != 0;
+    const bool ok = b->hp ? select_hp(k.type, c.nstate, k.is_bc).one != nullptr
+                          : select_kernel(k.type, b->nshape, c.nstate, k.is_bc).one != nullptr;
+    if (!ok) {
+      delete b;
+      throw Error{GPZ_E_UNSUPPORTED_ELEMENT, "no kernel for this element bucket"};
+    }
+    return b;
+  };
+  // keys in parallel over chunks of elements (each chunk's distinct keys in first-occurrence order), then
+  // buckets created in the order of their first element, as one pass over the elements would
+  const int64_t nchunk = std::max<int64_t>(1, std::min<int64_t>(256, c.nel / 4096));
+  std::vector<std::map<BucketKey, int>> ckey(nchunk);
+  std::vector<std::vector<const BucketKey *>> corder(nchunk);
+  std::vector<int32_t> el_key(c.nel, 0);
+  host_parallel(
+      nchunk,
+      [&](int64_t c0, int64_t c1) {
+        BucketKey k;
+        for (int64_t ch = c0; ch < c1; ch++) {
+          const BucketKey *last = nullptr;
+          int last_i = -1;
+          for (int64_t e = c.nel * ch / nchunk; e < c.nel * (ch + 1) / nchunk; e++) {
+            key_of(e, k);
+            if (!last || *last < k || k < *last) {
+              auto it = ckey[ch].find(k);
+              if (it == ckey[ch].end()) {
+                it = ckey[ch].emplace(k, (int)corder[ch].size()).first;
+                corder[ch].push_back(&it->first);
+              }
+              last = &it->first;
+              last_i = it->second;
+            }
+            el_key[e] = last_i;
+          }
+        }
+      },
+      1);
+  std::map<BucketKey, int> index;
+  std::vector<std::vector<int>> remap(nchunk);
+  for (int64_t ch = 0; ch < nchunk; ch++)
+    for (const BucketKey *k : corder[ch]) {
+      auto it = index.find(*k);
+      if (it == index.end()) {
+        it = index.emplace(*k, (int)c.buckets.size()).first;
+        c.buckets.push_back(make_bucket(*k));
+      }
+      remap[ch].push_back(it->second);
+    }
+  std::vector<int> el_bucket(c.nel, -1);
+  host_parallel(nchunk, [&](int64_t c0, int64_t c1) {
+    for (int64_t ch = c0; ch < c1; ch++)
+      for (int64_t e = c.nel * ch / nchunk; e < c.nel * (ch + 1) / nchunk; e++) el_bucket[e] = remap[ch][el_key[e]];
+  }, 1);
+  const auto t1 = std::chrono::steady_clock::now();
   // greedy first-fit colouring by shared non-empty connects (gpz_element_colours)
-  std::vector<int64_t> gi(c.nel + 1, 0), g, bsz(d.block_size, d.block_size + c.nconnects);
-  for (int64_t e = 0; e < c.nel; e++) {
-    const int ns = topo(d.el_type[e]).nsides;
-    for (int s = 0; s < ns; s++) g.push_back(d.el_conn[e * 27 + s]);
-    gi[e + 1] = (int64_t)g.size();
-  }
+  int nsides_of_type[4] = {0, topo(GPZ_EL_LINE).nsides, topo(GPZ_EL_QUAD).nsides, topo(GPZ_EL_HEX).nsides};
   std::vector<int32_t> colour(c.nel, 0);
   int32_t ncol = 0;
-  const int crc = gpz_element_colours(c.nel, gi.data(), g.data(), c.nconnects, bsz.data(), colour.data(), &ncol);
+  const int crc = colour_mesh_elements(d, nsides_of_type, colour.data(), &ncol);
   GPZ_REQUIRE(crc == GPZ_OK, GPZ_E_INVALID, "element colouring: a connect out of range or more than 64 colours");
   c.ncolours = ncol;
+  const auto t2 = std::chrono::steady_clock::now();
   for (Bucket *b : c.buckets) b->colour_begin.assign(ncol + 1, 0);
   for (int64_t e = 0; e < c.nel; e++) c.buckets[el_bucket[e]]->colour_begin[colour[e] + 1]++;
   for (Bucket *b : c.buckets) {
@@ -848,6 +904,12 @@ void build_buckets(Ctx &c, const gpz_mesh_desc &d) {
     b->d_q.alloc(2);
   }
   GPZ_CUDA_TRY(cudaStreamSynchronize(c.stream));
+  const auto t3 = std::chrono::steady_clock::now();
+  auto ms = [](std::chrono::steady_clock::time_point a, std::chrono::steady_clock::time_point b) {
+    return std::to_string(std::chrono::duration<double, std::milli>(b - a).count());
+  };
+  c.bucket_report = "{\"keys\": " + ms(t0, t1) + ", \"colouring\": " + ms(t1, t2) + ", \"lists_tables\": " +
+                    ms(t2, t3) + "}";
 }
 
 namespace {

@@ -3,7 +3,10 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <algorithm>
 #include <atomic>
+#include <exception>
+#include <thread>
 #include <string>
 #include <vector>
 
@@ -291,6 +294,7 @@ struct Ctx {
                                              // default), -1: timed at the next assembly (gpz_assembly_mode)
   bool asm_mode_auto = false;                // the launch mode is autotuned (gpz_assembly_mode(-1))
   std::string asm_mode_report;               // the timings of the two launch modes
+  std::string upload_report, bucket_report;  // host-side timings of the last mesh upload (ms)
   int ncolours = 0;
   DBuf<int> d_err;                           // device-side check flag
 
@@ -401,6 +405,8 @@ void filter_zero_inactive(Ctx &c, double *f_mesh);
 void filter_values(Ctx &c);     // condensed values from the mesh-level ones (c.flt.keep)
 // assemble.cu
 void build_buckets(Ctx &c, const gpz_mesh_desc &d);
+// greedy first-fit element colours (gpz_colour.cpp); nsides_of_type[type] sides per element type
+int colour_mesh_elements(const gpz_mesh_desc &d, const int *nsides_of_type, int32_t *colours, int32_t *ncolours);
 void assemble_fp64(Ctx &c);
 void assemble_rhs(Ctx &c);
 void make_fp32_copy(Ctx &c, int variant = -1);
@@ -437,6 +443,33 @@ void check_device_flag(Ctx &c, const char *where);
 std::string tune_key(Ctx &c, const char *tuner);
 int tune_cache_lookup(const Ctx &c, const std::string &key);
 void tune_cache_store(const Ctx &c, const std::string &key, int choice, const std::string &report);
+
+// body(begin, end) over contiguous chunks of [0, n) on up to 16 host threads (one when n < min_chunk);
+// an exception thrown by a chunk is rethrown in the caller after every thread has joined (the lowest chunk's)
+template <class F>
+void host_parallel(int64_t n, F &&body, int64_t min_chunk = 16384) {
+  unsigned nt = std::thread::hardware_concurrency();
+  nt = std::max(1u, std::min(nt, 16u));
+  if (n < 2 * min_chunk) nt = 1;
+  if (nt == 1) {
+    if (n > 0) body((int64_t)0, n);
+    return;
+  }
+  std::vector<std::exception_ptr> err(nt);
+  std::vector<std::thread> th;
+  th.reserve(nt);
+  for (unsigned t = 0; t < nt; t++)
+    th.emplace_back([&, t]() {
+      try {
+        body(n * (int64_t)t / (int64_t)nt, n * (int64_t)(t + 1) / (int64_t)nt);
+      } catch (...) {
+        err[t] = std::current_exception();
+      }
+    });
+  for (auto &x : th) x.join();
+  for (auto &x : err)
+    if (x) std::rethrow_exception(x);
+}
 
 inline int grid_for(int64_t n, int threads) {
   int64_t g = (n + threads - 1) / threads;

@@ -23,6 +23,8 @@
 //   L = mean_j (M r_j - e_j)^T A (M r_j - e_j) / e_j^T A e_j,
 // over the non-Dirichlet equations (both vectors masked), evaluated with the
 // FP64 CSR matrix.
+#include <algorithm>
+#include <atomic>
 #include <cmath>
 #include <vector>
 
@@ -432,6 +434,25 @@ double normal01(uint64_t &s) {  // Box-Muller on two 53-bit uniforms
 
 int sides_of(int type) { return type == GPZ_EL_HEX ? 27 : (type == GPZ_EL_QUAD ? 9 : 3); }
 
+// dest[k][0 .. NS): the equations of volume element k, its connects in side order, each connect's block
+__global__ void k_ln_dest(int64_t E, int ns, int NS, const int32_t *__restrict__ ec, const int64_t *__restrict__ bpos,
+                          const int32_t *__restrict__ bsize, int32_t *__restrict__ dest, int *__restrict__ err) {
+  const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= E) return;
+  int32_t *d = dest + k * NS;
+  int cnt = 0;
+  for (int s = 0; s < ns; s++) {
+    const int32_t cn = ec[k * ns + s];
+    const int n = bsize[cn];
+    if (cnt + n > NS) {
+      atomicOr(err, 1 << 21);
+      return;
+    }
+    for (int j = 0; j < n; j++) d[cnt + j] = (int32_t)(bpos[cn] + j);
+    cnt += n;
+  }
+}
+
 void setup_mesh(Ctx &c, int R) {
   Learned &L = c.ln;
   GPZ_REQUIRE(c.have_mesh, GPZ_E_NOT_READY, "no mesh");
@@ -449,22 +470,25 @@ void setup_mesh(Ctx &c, int R) {
   GPZ_REQUIRE(!L.h_vel.empty(), GPZ_E_INVALID, "no volume elements");
   const int ns = sides_of(vtype);
   const int64_t E = (int64_t)L.h_vel.size();
-  std::vector<int32_t> ec((size_t)E * ns), dest;
-  dest.reserve((size_t)E * 3 * ns);
-  int NS = -1;
-  for (int64_t k = 0; k < E; k++) {
-    const int64_t e = L.h_vel[k];
-    int cnt = 0;
-    for (int s = 0; s < ns; s++) {
-      const int64_t cn = c.h_el_conn[e * 27 + s];
-      ec[k * ns + s] = (int32_t)cn;
-      for (int j = 0; j < c.h_block_size[cn]; j++) dest.push_back((int32_t)(c.h_block_pos[cn] + j));
-      cnt += c.h_block_size[cn];
+  // equations per element (every volume element the same count), the elements' connects
+  int NS = 0;
+  for (int s = 0; s < ns; s++) NS += c.h_block_size[c.h_el_conn[L.h_vel[0] * 27 + s]];
+  std::vector<int32_t> ec((size_t)E * ns);
+  std::atomic<int> uneven{0};
+  host_parallel(E, [&](int64_t k0, int64_t k1) {
+    for (int64_t k = k0; k < k1; k++) {
+      const int64_t e = L.h_vel[k];
+      int cnt = 0;
+      for (int s = 0; s < ns; s++) {
+        const int64_t cn = c.h_el_conn[e * 27 + s];
+        ec[k * ns + s] = (int32_t)cn;
+        cnt += c.h_block_size[cn];
+      }
+      if (cnt != NS) uneven.store(1, std::memory_order_relaxed);
     }
-    if (NS < 0) NS = cnt;
-    GPZ_REQUIRE(cnt == NS, GPZ_E_UNSUPPORTED_ELEMENT,
-                "learned preconditioner: all volume elements must have the same number of equations");
-  }
+  });
+  GPZ_REQUIRE(!uneven.load(), GPZ_E_UNSUPPORTED_ELEMENT,
+              "learned preconditioner: all volume elements must have the same number of equations");
   GPZ_REQUIRE(NS >= 1 && NS <= kMaxNS && NS * R * (kH + 1) * 4 <= 200 * 1024, GPZ_E_UNSUPPORTED_ELEMENT,
               "learned preconditioner: too many equations per element");
   GPZ_REQUIRE(E * NS * R < (int64_t)INT32_MAX, GPZ_E_INVALID, "learned preconditioner: mesh too large");
@@ -481,21 +505,35 @@ void setup_mesh(Ctx &c, int R) {
       for (int j = 0; j < c.h_block_size[cn]; j++) mask[c.h_block_pos[cn] + j] = 0.0;
     }
   }
-  // connect -> volume elements
+  // connect -> volume elements, each connect's elements in increasing order (counted and filled on the host
+  // threads, then each short list sorted: the same lists as one pass over the elements)
   std::vector<int64_t> ce_ptr(c.nconnects + 1, 0);
-  for (int64_t k = 0; k < E * ns; k++) ce_ptr[ec[k] + 1]++;
+  host_parallel(E * ns, [&](int64_t i0, int64_t i1) {
+    for (int64_t i = i0; i < i1; i++) __atomic_fetch_add(&ce_ptr[ec[i] + 1], (int64_t)1, __ATOMIC_RELAXED);
+  });
   for (int64_t i = 0; i < c.nconnects; i++) ce_ptr[i + 1] += ce_ptr[i];
   std::vector<int32_t> ce_idx(ce_ptr.back());
   {
     std::vector<int64_t> f(ce_ptr.begin(), ce_ptr.end() - 1);
-    for (int64_t k = 0; k < E; k++)
-      for (int s = 0; s < ns; s++) ce_idx[f[ec[k * ns + s]]++] = (int32_t)k;
+    host_parallel(E, [&](int64_t k0, int64_t k1) {
+      for (int64_t k = k0; k < k1; k++)
+        for (int s = 0; s < ns; s++)
+          ce_idx[__atomic_fetch_add(&f[ec[k * ns + s]], (int64_t)1, __ATOMIC_RELAXED)] = (int32_t)k;
+    });
+    host_parallel(c.nconnects, [&](int64_t i0, int64_t i1) {
+      for (int64_t i = i0; i < i1; i++) std::sort(ce_idx.begin() + ce_ptr[i], ce_idx.begin() + ce_ptr[i + 1]);
+    });
   }
   cudaStream_t st = c.stream;
   L.ec.upload(ec.data(), ec.size(), st);
   L.ce_ptr.upload(ce_ptr.data(), ce_ptr.size(), st);
   L.ce_idx.upload(ce_idx.data(), std::max<size_t>(ce_idx.size(), 1), st);
-  L.dest.upload(dest.data(), dest.size(), st);
+  // each element's equations, in TPZElementMatrix::ComputeDestinationIndices order, built on the device
+  L.dest.alloc((size_t)E * NS);
+  k_ln_dest<<<grid_for(E, 256), 256, 0, st>>>(E, ns, NS, L.ec.p, c.d_block_pos.p, c.d_block_size.p, L.dest.p,
+                                               c.d_err.p);
+  c.launches++;
+  GPZ_CUDA_TRY(cudaGetLastError());
   L.have_ne = false;
   L.mask.upload(mask.data(), mask.size(), st);
   L.dsq.alloc(std::max<int64_t>(c.neq, 1));
@@ -517,6 +555,7 @@ void setup_mesh(Ctx &c, int R) {
   L.nparams = o.total;
   L.ready = true;
   GPZ_CUDA_TRY(cudaStreamSynchronize(st));
+  check_device_flag(c, "learned element equations");
   ensure_node_incidence(c);
 }
 
