@@ -258,7 +258,7 @@ int gpz_spmv(gpz_ctx *ctx, double alpha, const double *x, double beta, const dou
 
 /* y = A32 x with the FP32 operator of the mixed solvers (host FP64 vectors):
  * the layout the SpMV autotuner chose, or `variant` (GPZ solver option
- * spmv_variant, 0..8) for 3-state problems; the FP32 CSR copy otherwise. */
+ * spmv_variant, 0..8 or 10) for 3-state problems; the FP32 CSR copy, or 9, otherwise. */
 int gpz_spmv_fp32(gpz_ctx *ctx, int variant, const double *x, double *y);
 
 /* ---- cancellation ---------------------------------------------------------
@@ -337,6 +337,9 @@ typedef struct {
                               7 the same sum-factorised on Lagrange nodal values,
                               8 the same when every element has one affine Jacobian (uniform grid):
                                 K_e = mu_e Khat as one tcgen05 3xTF32 GEMM per tile of elements;
+                              10 8 over lattice blocks of 8 x 8 x 2 elements (the translated elements fill
+                                a lattice): the block's connect values and results in shared memory, plain
+                                stores inside the block, reductions on its faces;
                               scalar problems (Poisson, Darcy): 0 the FP32 CSR copy, 9 the scalar
                                 counterpart of 8 (3D Q2 hexes, K_e = k_e Khat, penalty faces) */
 } gpz_solver_opts;

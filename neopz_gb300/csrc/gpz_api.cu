@@ -518,7 +518,7 @@ int gpz_spmv(gpz_ctx *ctx, double alpha, const double *x, double beta, const dou
 int gpz_spmv_fp32(gpz_ctx *ctx, int variant, const double *x, double *y) {
   return guarded(ctx, [&](Ctx &c) {
     GPZ_REQUIRE(c.have_matrix, GPZ_E_NOT_READY, "not assembled");
-    GPZ_REQUIRE(x && y && variant >= -1 && variant <= 9, GPZ_E_INVALID, "arguments");
+    GPZ_REQUIRE(x && y && variant >= -1 && variant <= 10, GPZ_E_INVALID, "arguments");
     spmv32_apply(c, variant, x, y);
     return GPZ_OK;
   });

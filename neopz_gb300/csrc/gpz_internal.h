@@ -170,6 +170,13 @@ struct Learned {
 };
 
 // ---------------------------------------------------------------- matrix-free operator
+// lattice blocks of the tiled shared-element-matrix operator (gpz_matfree.cu, k_mf_hex27_gt)
+struct GtArgs {
+  int mx, my, mz;            // elements per lattice direction
+  int ntx, nty, ntz;         // blocks of 8 x 8 x 2 elements per direction
+  int8_t off[27][3];         // doubled-lattice offset of each Q2 shape's connect
+};
+
 // Element records of the FP32 matrix-free elasticity operator (gpz_matfree.cu),
 // a candidate of the mixed CG's SpMV autotuner.
 struct MatFree {
@@ -194,6 +201,13 @@ struct MatFree {
   DBuf<float> gm_b;                          // [2][96 x 88] hi, lo (K-major core matrices)
   DBuf<double> gm_ref;                       // element 0's Jinv (9) and |det J|
   DBuf<int> gm_flag;
+  // the same operator over lattice blocks (the translated elements fill a lattice of their edge vectors)
+  bool gt_ready = false;
+  int grid_gt = 1;
+  GtArgs gt{};
+  DBuf<int32_t> gt_nmap;                     // [(2 mx + 1)(2 my + 1)(2 mz + 1)] block row of each lattice connect
+  DBuf<float> gt_emu;                        // [mx my mz] mu of the element of each lattice cell (-1: none)
+  DBuf<uint8_t> gt_face;                     // [block rows] 1 on a penalty face
 };
 
 // scalar shared element matrix (3D Q2 Darcy / Poisson on translated grids):
@@ -431,7 +445,8 @@ bool matfree1_build(Ctx &c);
 void matfree1_spmv(Ctx &c, cudaStream_t s, const float *p, float *q);
 int two_level_build(Ctx &c);     // geometry part (once per mesh); GPZ_OK or GPZ_E_INVALID when not a uniform grid
 void two_level_assemble(Ctx &c); // coarse matrix and its inverse for the current assembly
-void matfree_spmv(Ctx &c, cudaStream_t s, int mode);  // 0 CUDA cores, 1 tcgen05, 2 sum-factorised, 3 shared matrix
+void matfree_spmv(Ctx &c, cudaStream_t s, int mode);  // 0 CUDA cores, 1 tcgen05, 2 sum-factorised, 3 shared matrix,
+                                                      // 4 shared matrix over lattice blocks
 // learned.cu
 void learned_prepare(Ctx &c);
 void ensure_node_incidence(Ctx &c);                // features, scaling and factors F for the assembled system

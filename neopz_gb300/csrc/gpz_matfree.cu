@@ -21,6 +21,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstring>
+#include <type_traits>
 #include <vector>
 
 #include "gpz_internal.h"
@@ -1282,6 +1283,336 @@ __global__ void __launch_bounds__(kGmThreads, 1) k_mf_hex27_gm(int64_t n, const 
   }
 }
 
+// ---------------------------------------------------------------- the same operator over lattice tiles
+// On a grid whose elements are translates of one element along three lattice
+// vectors (element e's corner 0 at x0 + i a1 + j a2 + k a3) every Q2 connect
+// sits at a point of the doubled lattice (2i + ox, 2j + oy, 2k + oz), ox, oy,
+// oz in {0, 1, 2} by side.  A CTA then takes blocks of 8 x 8 x 2 elements (one
+// M = 128 tile of the Khat GEMM): a block's 17 x 17 x 5 connect values are read
+// once into shared memory and the A operand is built from them; the results are
+// added into a shared-memory tile with shared-memory atomics, and the connects
+// strictly inside the block, which belong to no other block, are written with
+// plain stores, those on its faces (and those on penalty faces, which the face
+// kernel has already added into q) with vector reductions.  Per element that is
+// ~11 global reads and ~6 global writes instead of the 27 gathers and 27
+// reductions of k_mf_hex27_gm; the MMAs, the 3xTF32 split and the translation
+// subtraction are the same.  Like k_mf_hex27_gm the CTA runs two warp groups
+// in a two-stage pipeline over blocks:
+//   loaders (warps 0..7): the block's connect values (loaded into registers
+//     while the previous block's MMAs ran) into shared memory, the A rows, the
+//     MMAs into TMEM accumulator pair k mod 2, committed to mma_done;
+//   writers (warps 8..15): wait for mma_done, add mu_e Y into result tile
+//     k mod 2, release the accumulators (tmem_free), then write the block out;
+//     p . q is summed there as sum over the block's connects of p_n . y_n.
+// Waits are bounded and end together on a shared abort flag, as in k_mf_hex27_gm.
+constexpr int kGtThreads = 512;  // 8 loader + 8 writer warps
+constexpr int kGtGroup = 256;
+constexpr int kGtTx = 8, kGtTy = 8, kGtTz = 2;  // elements per block (8 x 8 x 2 = 128 = one tile)
+constexpr int kGtNx = 2 * kGtTx + 1, kGtNy = 2 * kGtTy + 1, kGtNz = 2 * kGtTz + 1;
+constexpr int kGtNodes = kGtNx * kGtNy * kGtNz;  // 1445
+constexpr int kGtPre = (kGtNodes + kGtGroup - 1) / kGtGroup;  // connects per group thread
+// shared-memory tiles: one plane per component, slot (x / 2 + (x odd) 9) + 20 (y + 17 z): the 32 lanes of a
+// warp (elements (lx, ly) of one layer, one shape) then hit 32 distinct banks
+constexpr int kGtP = 20, kGtSlots = kGtP * kGtNy * kGtNz;            // 1700 slots per plane
+constexpr uint32_t kGtYt = 3 * kGtSlots * 4;                          // one tile: float [3][kGtSlots]
+constexpr uint32_t GT_UT = 2 * kGmB + 2 * kGmA;                       // the connect values
+constexpr uint32_t GT_YT = GT_UT + kGtYt;                             // two result tiles
+constexpr uint32_t GT_MU = GT_YT + 2 * kGtYt;                         // float [2][128] mu of the blocks' elements
+constexpr uint32_t GT_END = GT_MU + 2 * kGmEl * 4;
+static_assert(GT_UT % 16 == 0 && GT_END <= 225 * 1024, "shared memory");
+static_assert(kGtTx * kGtTy * kGtTz == kGmEl, "one tile per block");
+
+static_assert(kNS == 27, "GtArgs holds 27 shapes");
+
+__device__ __forceinline__ int gt_slot(int x, int y, int z) { return (x >> 1) + (x & 1) * 9 + kGtP * (y + kGtNy * z); }
+
+struct GtBlock {
+  int tx, ty, tz, ex, ey, ez;  // block position, elements present per direction
+};
+__device__ __forceinline__ GtBlock gt_block(const GtArgs &G, int64_t tile) {
+  GtBlock b;
+  b.tx = (int)(tile % G.ntx);
+  b.ty = (int)((tile / G.ntx) % G.nty);
+  b.tz = (int)(tile / ((int64_t)G.ntx * G.nty));
+  b.ex = min(kGtTx, G.mx - kGtTx * b.tx);
+  b.ey = min(kGtTy, G.my - kGtTy * b.ty);
+  b.ez = min(kGtTz, G.mz - kGtTz * b.tz);
+  return b;
+}
+// block row of connect n of a block (-1: none)
+__device__ __forceinline__ int32_t gt_row(const GtArgs &G, const GtBlock &b, const int32_t *__restrict__ nmap, int n) {
+  const int x = n % kGtNx, y = (n / kGtNx) % kGtNy, z = n / (kGtNx * kGtNy);
+  if (n >= kGtNodes || x > 2 * b.ex || y > 2 * b.ey || z > 2 * b.ez) return -1;
+  const int64_t NX = 2 * G.mx + 1, NY = 2 * G.my + 1;
+  return nmap[(2 * kGtTx * b.tx + x) + NX * ((2 * kGtTy * b.ty + y) + NY * (int64_t)(2 * kGtTz * b.tz + z))];
+}
+
+// nmap: [(2 mx + 1)(2 my + 1)(2 mz + 1)] block row of each lattice connect (-1: none);
+// emu: [mx my mz] mu of the element at each lattice cell (-1: none); face: [block rows] 1 on penalty faces
+__global__ void __launch_bounds__(kGtThreads, 1) k_mf_hex27_gt(GtArgs G, const int32_t *__restrict__ nmap,
+                                                               const float *__restrict__ emu,
+                                                               const uint8_t *__restrict__ face,
+                                                               const float4 *__restrict__ bsplit,
+                                                               const float4 *__restrict__ p4, float4 *__restrict__ q4,
+                                                               const double *__restrict__ face_energy,
+                                                               int *__restrict__ err, Red R) {
+  if (!active(R.iscal)) return;
+  extern __shared__ __align__(1024) unsigned char sm[];
+  __shared__ uint32_t s_tmem;
+  __shared__ volatile int s_abort;
+  __shared__ __align__(8) uint64_t s_done[2], s_free[2];
+  __shared__ int8_t s_off[kNS][3];
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const bool loader = tid < kGtGroup;
+  const int gl = tid & (kGtGroup - 1);
+  float *ut = (float *)(sm + GT_UT);
+  if (tid == 0) {  // constant indices: the kernel parameter is not copied to local memory
+#pragma unroll
+    for (int a = 0; a < kNS; a++)
+#pragma unroll
+      for (int r = 0; r < 3; r++) s_off[a][r] = G.off[a][r];
+  }
+  for (uint32_t i = tid; i < 2 * kGmB / 16; i += kGtThreads) ((float4 *)(sm + GM_BH))[i] = bsplit[i];
+  for (uint32_t i = tid; i < 2 * kGtYt / 4; i += kGtThreads) ((float *)(sm + GT_YT))[i] = 0.f;
+  asm volatile("fence.proxy.async.shared::cta;");
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(tc_smem(&s_tmem)), "r"(512));
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+  }
+  if (tid == 0) {
+    s_abort = 0;
+    for (int b = 0; b < 2; b++) {
+      asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(tc_smem(&s_done[b])));
+      asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(tc_smem(&s_free[b])), "r"(kGtGroup));
+    }
+    asm volatile("fence.mbarrier_init.release.cluster;");
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;");
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;");
+  const uint32_t tm = s_tmem;
+  const uint32_t ah = tc_smem(sm + GM_AH), al = tc_smem(sm + GM_AL), bh = tc_smem(sm + GM_BH),
+                 bl = tc_smem(sm + GM_BL);
+  const int64_t ntile = (int64_t)G.ntx * G.nty * G.ntz;
+  KSum en;
+  int last = -1;  // the issuer's last committed block
+  if (loader) {
+    int32_t pbr[kGtPre];
+    float4 pval[kGtPre];
+    float pmu = 0.f;
+    auto fetch = [&](int64_t tile) {
+      const GtBlock b = gt_block(G, tile);
+#pragma unroll
+      for (int i = 0; i < kGtPre; i++) pbr[i] = gt_row(G, b, nmap, gl + i * kGtGroup);
+#pragma unroll
+      for (int i = 0; i < kGtPre; i++) pval[i] = pbr[i] >= 0 ? p4[pbr[i]] : make_float4(0.f, 0.f, 0.f, 0.f);
+      pmu = 0.f;
+      if (gl < kGmEl) {
+        const int lx = gl % kGtTx, ly = (gl / kGtTx) % kGtTy, lz = gl / (kGtTx * kGtTy);
+        if (lx < b.ex && ly < b.ey && lz < b.ez)
+          pmu = emu[(int64_t)(kGtTx * b.tx + lx) + (int64_t)G.mx * ((kGtTy * b.ty + ly) + (int64_t)G.my * (kGtTz * b.tz + lz))];
+      }
+    };
+    if (blockIdx.x < ntile) fetch(blockIdx.x);
+    int k = 0;
+    for (int64_t tile = blockIdx.x; tile < ntile; tile += gridDim.x, k++) {
+      const int bf = k & 1;
+      bool ok = true;
+      if (gl == 0 && k >= 2) ok = gm_wait(&s_free[bf], (uint32_t)((k - 2) >> 1) & 1u, &s_abort);
+      if (ok && k >= 1) ok = gm_wait(&s_done[(k - 1) & 1], (uint32_t)((k - 1) >> 1) & 1u, &s_abort);  // A free
+      if (!gm_vote(1, kGtGroup, ok)) break;
+      // the block's values (the previous block's A rows, the only reader of ut, are built)
+#pragma unroll
+      for (int i = 0; i < kGtPre; i++) {
+        const int n = gl + i * kGtGroup;
+        if (n < kGtNodes) {
+          const int sl = gt_slot(n % kGtNx, (n / kGtNx) % kGtNy, n / (kGtNx * kGtNy));
+          ut[sl] = pval[i].x;
+          ut[kGtSlots + sl] = pval[i].y;
+          ut[2 * kGtSlots + sl] = pval[i].z;
+        }
+      }
+      if (gl < kGmEl) ((float *)(sm + GT_MU))[bf * kGmEl + gl] = pmu > 0.f ? pmu : 0.f;
+      gm_bar(1, kGtGroup);
+      {
+        // A rows: thread (element le, half): shapes [0, kGmSplit) with the translation removed, or the rest
+        const int le = gl & (kGmEl - 1), half = gl >> 7;
+        const int lx = le % kGtTx, ly = (le / kGtTx) % kGtTy, lz = le / (kGtTx * kGtTy);
+        const bool live = ((const float *)(sm + GT_MU))[bf * kGmEl + le] > 0.f;
+        auto gather = [&](auto A0c, auto A1c) {
+          constexpr int A0 = decltype(A0c)::value, A1 = decltype(A1c)::value;
+          constexpr int K0 = 3 * A0, K1 = A1 == kNS ? kGmK : 3 * A1, NV = K1 - K0;
+          float v[NV];
+#pragma unroll
+          for (int kk = 0; kk < NV; kk++) v[kk] = 0.f;
+          if (live) {
+#pragma unroll
+            for (int a = A0; a < A1; a++) {
+              const int sl = gt_slot(2 * lx + s_off[a][0], 2 * ly + s_off[a][1], 2 * lz + s_off[a][2]);
+              v[3 * (a - A0)] = ut[sl];
+              v[3 * (a - A0) + 1] = ut[kGtSlots + sl];
+              v[3 * (a - A0) + 2] = ut[2 * kGtSlots + sl];
+            }
+          }
+          if (A0 == 0) {  // Khat annihilates translations: corner 0's value off the corner coefficients
+            const float c0 = v[0], c1 = v[1], c2 = v[2];
+#pragma unroll
+            for (int a = 0; a < 8; a++) {
+              v[3 * a] -= c0;
+              v[3 * a + 1] -= c1;
+              v[3 * a + 2] -= c2;
+            }
+          }
+#pragma unroll
+          for (int c4 = 0; c4 < NV / 4; c4++) {
+            float4 lo;
+            const float4 hi = tf32_split4(make_float4(v[4 * c4], v[4 * c4 + 1], v[4 * c4 + 2], v[4 * c4 + 3]), lo);
+            const uint32_t off = kmaj(le, K0 + 4 * c4, kGmK);
+            *(float4 *)(sm + GM_AH + off) = hi;
+            *(float4 *)(sm + GM_AL + off) = lo;
+          }
+        };
+        if (half == 0) gather(std::integral_constant<int, 0>(), std::integral_constant<int, kGmSplit>());
+        else gather(std::integral_constant<int, kGmSplit>(), std::integral_constant<int, kNS>());
+      }
+      asm volatile("fence.proxy.async.shared::cta;");
+      gm_bar(1, kGtGroup);
+      if (gl == 0) {
+        asm volatile("tcgen05.fence::after_thread_sync;");
+        gm_mma(tm + (uint32_t)bf * 256u, ah, al, bh, bl);
+        tc_commit(&s_done[bf]);
+        last = k;
+      }
+      if (tile + gridDim.x < ntile) fetch(tile + gridDim.x);  // in flight during the MMAs
+    }
+  } else {
+    const int sw = warp - kGtGroup / 32, quarter = sw & 3, h = sw >> 2, le = quarter * 32 + lane;
+    const int lx = le % kGtTx, ly = (le / kGtTx) % kGtTy, lz = le / (kGtTx * kGtTy);
+    int k = 0;
+    for (int64_t tile = blockIdx.x; tile < ntile; tile += gridDim.x, k++) {
+      const int bf = k & 1;
+      float *yt = (float *)(sm + GT_YT + bf * kGtYt);
+      const bool ok = gm_wait(&s_done[bf], (uint32_t)(k >> 1) & 1u, &s_abort);
+      if (!gm_vote(2, kGtGroup, ok)) break;
+      asm volatile("tcgen05.fence::after_thread_sync;");
+      {
+        // warp w reads its lane quarter (element 32 (w mod 4) + lane), columns [48 h, 48 h + 48) = shapes
+        // [16 h, 16 h + 16), and adds mu_e Y into result tile k mod 2
+        const uint32_t taddr = tm + ((uint32_t)(quarter * 32) << 16) + (uint32_t)bf * 256u + (uint32_t)(48 * h);
+        float y[48];
+#pragma unroll
+        for (int c = 0; c < 48; c += 16) {
+          float t[16], u[16];
+          tc_ld16(taddr + c, t);
+          tc_ld16(taddr + kGmSmall + c, u);
+#pragma unroll
+          for (int j = 0; j < 16; j++) y[c + j] = t[j] + u[j];
+        }
+        const float mu = ((const float *)(sm + GT_MU))[bf * kGmEl + le];
+        if (mu > 0.f) {
+#pragma unroll
+          for (int j = 0; j < 16; j++) {
+            const int a = 16 * h + j;
+            if (a < kNS) {
+              const int sl = gt_slot(2 * lx + s_off[a][0], 2 * ly + s_off[a][1], 2 * lz + s_off[a][2]);
+              atomicAdd(&yt[sl], mu * y[3 * j]);
+              atomicAdd(&yt[kGtSlots + sl], mu * y[3 * j + 1]);
+              atomicAdd(&yt[2 * kGtSlots + sl], mu * y[3 * j + 2]);
+            }
+          }
+        }
+      }
+      asm volatile("tcgen05.fence::before_thread_sync;");
+      asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(tc_smem(&s_free[bf])) : "memory");
+      gm_bar(2, kGtGroup);
+      // the block into q (plain stores strictly inside, reductions on its faces and on penalty faces); p . q
+      const GtBlock b = gt_block(G, tile);
+      int32_t br[kGtPre];
+#pragma unroll
+      for (int i = 0; i < kGtPre; i++) br[i] = gt_row(G, b, nmap, gl + i * kGtGroup);
+#pragma unroll
+      for (int i = 0; i < kGtPre; i++) {
+        const int n = gl + i * kGtGroup;
+        if (br[i] < 0) continue;
+        const int x = n % kGtNx, y = (n / kGtNx) % kGtNy, z = n / (kGtNx * kGtNy);
+        const int sl = gt_slot(x, y, z);
+        const float4 v = make_float4(yt[sl], yt[kGtSlots + sl], yt[2 * kGtSlots + sl], 0.f);
+        yt[sl] = yt[kGtSlots + sl] = yt[2 * kGtSlots + sl] = 0.f;  // for block k + 2
+        const float4 pv = p4[br[i]];
+        en.add(v.x * pv.x + v.y * pv.y + v.z * pv.z);
+        const bool inside = x > 0 && x < 2 * b.ex && y > 0 && y < 2 * b.ey && z > 0 && z < 2 * b.ez && !face[br[i]];
+        if (inside) q4[br[i]] = v;
+        else red_add_f4(&q4[br[i]], v);
+      }
+      gm_bar(2, kGtGroup);
+    }
+  }
+  __syncthreads();
+  const bool failed = s_abort != 0;
+  if (failed && tid == 0) {
+    atomicOr(err, 16384);
+    if (last >= 0) tc_wait(&s_done[last & 1], (uint32_t)(last >> 1) & 1u);
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;");
+  __syncthreads();
+  if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tm), "r"(512));
+  double v[1] = {failed ? 0.0 : en.get()}, tot[1];
+  if (grid_reduce<1, kGtThreads / 32>(v, R, tot) && threadIdx.x == 0) {
+    const double pq = tot[0] + (face_energy ? *face_energy : 0.0);
+    R.scal[S_PQ] = pq;
+    R.scal[S_ALPHA] = R.scal[S_RHO] / pq;
+    R.iscal[I_SP32]++;
+  }
+}
+
+// lattice position of each volume element's corner 0: t = Ainv (x - x0), integer to 1e-6
+__global__ void k_gt_lattice(int64_t n, const int64_t *__restrict__ elems, const int64_t *__restrict__ el_nodes,
+                             const double *__restrict__ xyz, double x0, double y0, double z0, const double *__restrict__ ainv,
+                             int32_t *__restrict__ lat, int *__restrict__ lmm, int *__restrict__ flag) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const int64_t node = el_nodes[elems[i] * 8];
+  const double d[3] = {xyz[node * 3] - x0, xyz[node * 3 + 1] - y0, xyz[node * 3 + 2] - z0};
+  for (int r = 0; r < 3; r++) {
+    const double t = ainv[3 * r] * d[0] + ainv[3 * r + 1] * d[1] + ainv[3 * r + 2] * d[2];
+    const long long li = llround(t);
+    if (fabs(t - (double)li) > 1e-6 || li < -(1ll << 20) || li > (1ll << 20)) atomicOr(flag, 1);
+    lat[i * 3 + r] = (int)li;
+    atomicMin(&lmm[r], (int)li);
+    atomicMax(&lmm[3 + r], (int)li);
+  }
+}
+
+// the connect map of the doubled lattice and the elements' mu per lattice cell; flag 2 when two elements
+// share a cell, one lattice point gets two connects or one connect two lattice points (its block's plain
+// stores would then not be the only writes of that connect)
+__global__ void k_gt_maps(int64_t n, const int32_t *__restrict__ lat, const int32_t *__restrict__ rows,
+                          const float *__restrict__ rlm, GtArgs G, int lx0, int ly0, int lz0, int32_t *__restrict__ nmap,
+                          float *__restrict__ emu, int32_t *__restrict__ owner, int *__restrict__ flag) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const int I = lat[i * 3] - lx0, J = lat[i * 3 + 1] - ly0, K = lat[i * 3 + 2] - lz0;
+  const int64_t cell = (int64_t)I + (int64_t)G.mx * (J + (int64_t)G.my * K);
+  if (atomicCAS((int *)&emu[cell], __float_as_int(-1.f), __float_as_int(rlm[2 * i + 1])) != __float_as_int(-1.f))
+    atomicOr(flag, 2);
+  const int NX = 2 * G.mx + 1, NY = 2 * G.my + 1;
+  for (int a = 0; a < kNS; a++) {
+    const int32_t r = rows[i * kNS + a];
+    const int64_t idx = (int64_t)(2 * I + G.off[a][0]) + (int64_t)NX * ((2 * J + G.off[a][1]) + (int64_t)NY * (2 * K + G.off[a][2]));
+    const int old = atomicCAS(&nmap[idx], -1, r);
+    if (old != -1 && old != r) atomicOr(flag, 2);
+    if (r >= 0) {
+      const int ow = atomicCAS(&owner[r], -1, (int)idx);
+      if (ow != -1 && ow != (int)idx) atomicOr(flag, 2);
+    }
+  }
+}
+
+__global__ void k_gt_faces(int64_t n, const int32_t *__restrict__ frows, uint8_t *__restrict__ face) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n && frows[i] >= 0) face[frows[i]] = 1;
+}
+
 // The FP64 affine Jacobian of every volume element against element 0's: flag 1
 // when one is not affine or differs (the shared element matrix does not apply);
 // element 0's Jinv (row-major, Jinv[j][d] = d xi_j / d x_d) and |det J| to ref.
@@ -1780,6 +2111,111 @@ static bool gm_tables(Ctx &c, const Bucket &vol, double nu) {
   GPZ_CUDA_TRY(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
   M.grid_gm = std::max(1, std::min(kGridBlocks, nsm));  // one CTA per SM, persistent over tiles
   GPZ_CUDA_TRY(cudaStreamSynchronize(s));
+  return true;
+}
+
+// The lattice maps of the tiled operator (k_mf_hex27_gt): false when the
+// translated elements do not fill a lattice of their edge vectors
+// a1 = x1 - x0, a2 = x3 - x0, a3 = x4 - x0 (corner numbering of TPZGeoCube).
+static bool gt_build(Ctx &c, const Bucket &vol) {
+  MatFree &M = c.mf;
+  M.gt_ready = false;
+  cudaStream_t s = c.stream;
+  const int64_t n = M.nvol;
+  int64_t nd[8];
+  GPZ_CUDA_TRY(cudaMemcpy(nd, c.d_el_nodes.p + vol.elems[0] * 8, sizeof(nd), cudaMemcpyDeviceToHost));
+  double X[8][3];
+  for (int k = 0; k < 8; k++) GPZ_CUDA_TRY(cudaMemcpy(X[k], c.d_xyz.p + nd[k] * 3, 3 * sizeof(double), cudaMemcpyDeviceToHost));
+  double A[3][3];  // columns a1, a2, a3
+  for (int r = 0; r < 3; r++) {
+    A[r][0] = X[1][r] - X[0][r];
+    A[r][1] = X[3][r] - X[0][r];
+    A[r][2] = X[4][r] - X[0][r];
+  }
+  const double det = A[0][0] * (A[1][1] * A[2][2] - A[1][2] * A[2][1]) - A[0][1] * (A[1][0] * A[2][2] - A[1][2] * A[2][0]) +
+                     A[0][2] * (A[1][0] * A[2][1] - A[1][1] * A[2][0]);
+  if (!(std::fabs(det) > 0.0)) return false;
+  double inv[9];
+  inv[0] = (A[1][1] * A[2][2] - A[1][2] * A[2][1]) / det;
+  inv[1] = (A[0][2] * A[2][1] - A[0][1] * A[2][2]) / det;
+  inv[2] = (A[0][1] * A[1][2] - A[0][2] * A[1][1]) / det;
+  inv[3] = (A[1][2] * A[2][0] - A[1][0] * A[2][2]) / det;
+  inv[4] = (A[0][0] * A[2][2] - A[0][2] * A[2][0]) / det;
+  inv[5] = (A[0][2] * A[1][0] - A[0][0] * A[1][2]) / det;
+  inv[6] = (A[1][0] * A[2][1] - A[1][1] * A[2][0]) / det;
+  inv[7] = (A[0][1] * A[2][0] - A[0][0] * A[2][1]) / det;
+  inv[8] = (A[0][0] * A[1][1] - A[0][1] * A[1][0]) / det;
+  DBuf<double> dinv;
+  DBuf<int32_t> lat;
+  DBuf<int> lmm, flag;
+  dinv.upload(inv, 9, s);
+  lat.alloc((size_t)n * 3);
+  lmm.alloc(6);
+  flag.alloc(1);
+  flag.zero(s);
+  const int init[6] = {1 << 30, 1 << 30, 1 << 30, -(1 << 30), -(1 << 30), -(1 << 30)};
+  GPZ_CUDA_TRY(cudaMemcpyAsync(lmm.p, init, sizeof(init), cudaMemcpyHostToDevice, s));
+  k_gt_lattice<<<grid_for(n, 256), 256, 0, s>>>(n, vol.d_elems.p, c.d_el_nodes.p, c.d_xyz.p, X[0][0], X[0][1], X[0][2],
+                                                dinv.p, lat.p, lmm.p, flag.p);
+  c.launches++;
+  int hm[6], hf = 0;
+  GPZ_CUDA_TRY(cudaMemcpyAsync(hm, lmm.p, sizeof(hm), cudaMemcpyDeviceToHost, s));
+  GPZ_CUDA_TRY(cudaMemcpyAsync(&hf, flag.p, sizeof(int), cudaMemcpyDeviceToHost, s));
+  GPZ_CUDA_TRY(cudaStreamSynchronize(s));
+  if (hf) return false;
+  GtArgs G{};
+  G.mx = hm[3] - hm[0] + 1;
+  G.my = hm[4] - hm[1] + 1;
+  G.mz = hm[5] - hm[2] + 1;
+  const int64_t ncell = (int64_t)G.mx * G.my * G.mz;
+  const int64_t nnode = (int64_t)(2 * G.mx + 1) * (2 * G.my + 1) * (2 * G.mz + 1);
+  if (ncell < n || ncell > 8 * n || nnode >= INT32_MAX) return false;  // a sparse lattice: the tiles would be mostly empty
+  G.ntx = (G.mx + kGtTx - 1) / kGtTx;
+  G.nty = (G.my + kGtTy - 1) / kGtTy;
+  G.ntz = (G.mz + kGtTz - 1) / kGtTz;
+  // shape a's connect: the mean of its side's corners on the doubled lattice
+  static const int co[8][3] = {{0, 0, 0}, {1, 0, 0}, {1, 1, 0}, {0, 1, 0}, {0, 0, 1}, {1, 0, 1}, {1, 1, 1}, {0, 1, 1}};
+  const ElemTopo &t = topo(GPZ_EL_HEX);
+  for (int a = 0; a < kNS; a++) {
+    const int sd = vol.shape_side[a];
+    const int nn = t.side_nnode[sd];
+    for (int r = 0; r < 3; r++) {
+      int sum = 0;
+      for (int k = 0; k < nn; k++) sum += 2 * co[t.side_node[sd][k]][r];
+      if (sum % nn) return false;
+      G.off[a][r] = (int8_t)(sum / nn);
+    }
+  }
+  M.gt_nmap.alloc(nnode);
+  GPZ_CUDA_TRY(cudaMemsetAsync(M.gt_nmap.p, 0xff, nnode * sizeof(int32_t), s));
+  M.gt_emu.alloc(ncell);
+  {
+    std::vector<float> neg(ncell, -1.f);
+    M.gt_emu.upload(neg.data(), neg.size(), s);
+  }
+  DBuf<int32_t> owner;
+  owner.alloc(std::max<int64_t>(c.neq / 3, 1));
+  GPZ_CUDA_TRY(cudaMemsetAsync(owner.p, 0xff, owner.n * sizeof(int32_t), s));
+  k_gt_maps<<<grid_for(n, 256), 256, 0, s>>>(n, lat.p, M.vrows.p, M.vlm.p, G, hm[0], hm[1], hm[2], M.gt_nmap.p,
+                                             M.gt_emu.p, owner.p, flag.p);
+  c.launches++;
+  M.gt_face.alloc(std::max<int64_t>(c.neq / 3, 1));
+  M.gt_face.zero(s);
+  if (M.nface) {
+    k_gt_faces<<<grid_for(M.nface * kFS, 256), 256, 0, s>>>(M.nface * kFS, M.frows.p, M.gt_face.p);
+    c.launches++;
+  }
+  GPZ_CUDA_TRY(cudaMemcpyAsync(&hf, flag.p, sizeof(int), cudaMemcpyDeviceToHost, s));
+  GPZ_CUDA_TRY(cudaStreamSynchronize(s));
+  GPZ_CUDA_TRY(cudaGetLastError());
+  if (hf) return false;
+  M.gt = G;
+  GPZ_CUDA_TRY(cudaFuncSetAttribute(k_mf_hex27_gt, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)GT_END));
+  int dev = 0, nsm = 0;
+  GPZ_CUDA_TRY(cudaGetDevice(&dev));
+  GPZ_CUDA_TRY(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
+  M.grid_gt = (int)std::max<int64_t>(1, std::min<int64_t>(std::min(kGridBlocks, nsm), (int64_t)G.ntx * G.nty * G.ntz));
+  M.gt_ready = true;
   return true;
 }
 
@@ -2445,6 +2881,7 @@ bool matfree_build(Ctx &c) {
   }
   M.grid_sf = mf_grid(k_mf_hex27_sf, kSfThreads);
   M.gm_ready = gm_tables(c, *vol, m.nu);
+  M.gt_ready = M.gm_ready && gt_build(c, *vol);
   M.ready = true;
   return true;
 }
@@ -2470,6 +2907,9 @@ void matfree_spmv(Ctx &c, cudaStream_t s, int mode) {
   else if (mode == 3)
     k_mf_hex27_gm<<<M.grid_gm, kGmThreads, GM_END, s>>>(M.nvol, M.vrows.p, M.vlm.p, (const float4 *)M.gm_b.p, p4, q4, fe,
                                                         c.d_err.p, R);
+  else if (mode == 4)
+    k_mf_hex27_gt<<<M.grid_gt, kGtThreads, GT_END, s>>>(M.gt, M.gt_nmap.p, M.gt_emu.p, M.gt_face.p,
+                                                        (const float4 *)M.gm_b.p, p4, q4, fe, c.d_err.p, R);
   else if (mode == 2)
     k_mf_hex27_sf<<<M.grid_sf, kSfThreads, 0, s>>>(M.nvol, M.vxyz.p, M.vrows.p, M.vlm.p, M.vgeo.p, M.sf_tab.p,
                                                    M.sf_idx.p, p4, q4, fe, R);

@@ -2310,8 +2310,8 @@ Red red_of(Ctx &c);
 // one launch of the FP32 3x3 SpMV variant v: q32 = A32 pm
 void launch_spmv32(Ctx &c, int v, const Ctx::Sell &S, Red R, cudaStream_t s) {
   SolverWork &w = c.sw;
-  if (v >= 5 && v <= 8) {
-    matfree_spmv(c, s, v - 5);  // element by element (gpz_matfree.cu), counts its own launches
+  if ((v >= 5 && v <= 8) || v == 10) {
+    matfree_spmv(c, s, v == 10 ? 4 : v - 5);  // element by element (gpz_matfree.cu), counts its own launches
     return;
   }
   if (v == 0) {
@@ -2393,7 +2393,7 @@ void tune_spmv32(Ctx &c, int only, bool timing) {
   };
   float best_mf = -1.f;
   std::string pruned;
-  if (timing && only < 0 && (want0(5) || want0(6) || want0(7) || want0(8)) && matfree_build(c)) {
+  if (timing && only < 0 && (want0(5) || want0(6) || want0(7) || want0(8) || want0(10)) && matfree_build(c)) {
     res.push_back({5, 0, time_it(5, cand[0])});
     if (c.mf.sf_ready) res.push_back({7, 0, time_it(7, cand[0])});
     res.push_back({6, 0, time_it(6, cand[0])});
@@ -2401,6 +2401,10 @@ void tune_spmv32(Ctx &c, int only, bool timing) {
     if (c.mf.gm_ready) {
       res.push_back({8, 0, time_it(8, cand[0])});
       check_device_flag(c, "shared-element-matrix tensor-core operator");
+    }
+    if (c.mf.gt_ready) {
+      res.push_back({10, 0, time_it(10, cand[0])});
+      check_device_flag(c, "shared-element-matrix operator over lattice blocks");
     }
     for (const Res &r : res) best_mf = best_mf < 0.f ? r.ms : std::min(best_mf, r.ms);
   }
@@ -2464,7 +2468,7 @@ void tune_spmv32(Ctx &c, int only, bool timing) {
     GPZ_CUDA_TRY(cudaGetLastError());
     res.push_back({4, 0, time_it(4, cand[0])});
   }
-  if (best_mf < 0.f && (want0(5) || want0(6) || want0(7) || want0(8)) && matfree_build(c)) {
+  if (best_mf < 0.f && (want0(5) || want0(6) || want0(7) || want0(8) || want0(10)) && matfree_build(c)) {
     if (want0(5)) res.push_back({5, 0, time_it(5, cand[0])});
     if (want0(7) && c.mf.sf_ready) res.push_back({7, 0, time_it(7, cand[0])});
     if (want0(6)) {
@@ -2474,6 +2478,10 @@ void tune_spmv32(Ctx &c, int only, bool timing) {
     if (want0(8) && c.mf.gm_ready) {
       res.push_back({8, 0, time_it(8, cand[0])});
       check_device_flag(c, "shared-element-matrix tensor-core operator");
+    }
+    if (want0(10) && c.mf.gt_ready) {
+      res.push_back({10, 0, time_it(10, cand[0])});
+      check_device_flag(c, "shared-element-matrix operator over lattice blocks");
     }
   }
   if (res.empty()) res.push_back({0, 0, time_it(0, cand[0])});
@@ -2498,7 +2506,8 @@ void tune_spmv32(Ctx &c, int only, bool timing) {
                      : res[i].v == 6 ? "matrix_free_tcgen05_3xtf32"
                      : res[i].v == 7 ? "matrix_free_sum_factorised"
                      : res[i].v == 8 ? "matrix_free_shared_matrix_tcgen05"
-                                     : "sliced_ell";
+                     : res[i].v == 10 ? "matrix_free_shared_matrix_lattice_blocks"
+                                      : "sliced_ell";
     rep += std::string(i ? ", " : "") + "\"" + nm + (res[i].v == 2 ? "_w" + std::to_string(res[i].window) : "") +
            "\": " + std::to_string(res[i].ms);
   }
@@ -2541,10 +2550,11 @@ void finish_layout(Ctx &c, Ctx::Sell *cand, int k) {
 }
 
 const char *spmv32_name(int v) {
-  static const char *names[9] = {"block_csr", "block_csr_2rows", "sliced_ell", "block_csr_tma_staged",
-                                 "upper_blocks_float4_atomics", "matrix_free_elements", "matrix_free_tcgen05_3xtf32",
-                                 "matrix_free_sum_factorised", "matrix_free_shared_matrix_tcgen05"};
-  return v >= 0 && v < 9 ? names[v] : "unknown";
+  static const char *names[11] = {"block_csr", "block_csr_2rows", "sliced_ell", "block_csr_tma_staged",
+                                  "upper_blocks_float4_atomics", "matrix_free_elements", "matrix_free_tcgen05_3xtf32",
+                                  "matrix_free_sum_factorised", "matrix_free_shared_matrix_tcgen05",
+                                  "matrix_free_shared_matrix_tcgen05_scalar", "matrix_free_shared_matrix_lattice_blocks"};
+  return v >= 0 && v < 11 ? names[v] : "unknown";
 }
 
 void make_fp32_copy(Ctx &c, int variant) {
@@ -2559,7 +2569,7 @@ void make_fp32_copy(Ctx &c, int variant) {
     }
     // the block CSR: the source of every assembled layout; a known matrix-free choice does not read it
     const int known = variant >= 0 ? variant : c.spmv32_tuned >= 0 ? c.spmv32_tuned : cached;
-    if (!(known >= 5 && known <= 8)) {
+    if (!((known >= 5 && known <= 8) || known == 10)) {
       c.d_bptr.alloc(c.nbrow + 1);
       c.d_bcol.alloc(std::max<int64_t>(c.nnz / 9, 1) + 16);  // slack for 16-byte rounded bulk copies
       c.d_bval.alloc(std::max<int64_t>(c.nnz, 1) + 16);

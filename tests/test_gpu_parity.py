@@ -225,7 +225,7 @@ def test_mixed_block_jacobi_bsr3(built):
     ctx.close()
 
 
-@pytest.mark.parametrize("variant", [0, 1, 2, 3, 4, 5, 6, 7, 8])
+@pytest.mark.parametrize("variant", [0, 1, 2, 3, 4, 5, 6, 7, 8, 10])
 def test_mixed_spmv_variants_converge(built, variant):
     """Every layout / kernel the SpMV autotuner can pick gives the same converged solution."""
     g = _gpz()
@@ -360,7 +360,7 @@ def test_assembly_graph_replay(built):
     ctx.close()
 
 
-@pytest.mark.parametrize("variant", [0, 1, 2, 3, 4, 5, 6, 7, 8])
+@pytest.mark.parametrize("variant", [0, 1, 2, 3, 4, 5, 6, 7, 8, 10])
 def test_fp32_operator_layouts_match_fp64_spmv(built, variant):
     """Every FP32 operator layout of the mixed CG (block CSR, two rows, sliced ELL, TMA-staged, upper blocks
     with atomics, matrix-free elements on CUDA cores, on the tensor cores in 3xTF32, sum-factorised on
@@ -387,6 +387,40 @@ def test_fp32_operator_layouts_match_fp64_spmv(built, variant):
     assert np.linalg.norm((y32 - y64)[inner]) <= 1e-5 * np.linalg.norm(y64[inner])
     if variant == 8:  # a uniform grid: the shared element matrix is offered and is the operator applied
         assert ctx.tuning_report()["chosen"] == "matrix_free_shared_matrix_tcgen05"
+    if variant == 10:  # the same over lattice blocks (5^3 elements: partial blocks in every direction)
+        assert ctx.tuning_report()["chosen"] == "matrix_free_shared_matrix_lattice_blocks"
+    ctx.close()
+
+
+@pytest.mark.parametrize("shape", [(17, 9, 5), (16, 16, 4), (30, 30, 30)])
+def test_shared_matrix_operator_over_lattice_blocks(built, shape):
+    """The shared-element-matrix operator over lattice blocks of 8 x 8 x 2 elements: full and partial blocks,
+    more blocks than CTAs (30^3: 960 blocks), and a box of unequal sides.  It applies the assembled operator
+    (1e-5 against the FP64 SpMV, the same bar as the tile operator it restructures) and the mixed CG over it
+    reaches a true 1e-8 with the solution within 1e-8 of the FP64 solution."""
+    g = _gpz()
+    rng = np.random.default_rng(17)
+    nx, ny, nz = shape
+    mats = [(1, g.material(g.GPZ_MAT_ELAST3D, 3, E=1.0, nu=0.3, force=(0.0, 0.0, -1.0), forcing=g.GPZ_F_CONST))]
+    grid = g.Grid(3, (nx, ny, nz), (0, 0, 0), (1.0, 0.7, 0.4), [1, -1, -2, -2, -2, -2, -2], True, 2, mats,
+                  [(-1, g.bc(0, 0))], elem_coef=np.exp(rng.standard_normal(nx * ny * nz)))
+    ctx = g.Context(0)
+    ctx.upload_mesh(grid)
+    ctx.build_pattern(False)
+    ctx.assemble(g.GPZ_PREC_MIXED)
+    x = rng.standard_normal(grid.neq)
+    y64 = ctx.spmv(x)
+    y32 = ctx.spmv_fp32(x, 10)
+    assert ctx.tuning_report()["chosen"] == "matrix_free_shared_matrix_lattice_blocks"
+    assert np.linalg.norm(y32 - y64) <= 1e-5 * np.linalg.norm(y64)
+    y8 = ctx.spmv_fp32(x, 8)  # the tile operator: same products, another summation order
+    assert np.linalg.norm(y32 - y8) <= 1e-6 * np.linalg.norm(y64)
+    if nx * ny * nz <= 17 * 9 * 5:
+        sol = ctx.solve(solver=g.GPZ_SOLVER_MIXED_CG, precond=g.GPZ_PRECOND_BLOCK_JACOBI, tol=1e-8,
+                        reliable_delta=1e-2, spmv_variant=10)
+        ref = ctx.solve(tol=1e-12, max_iter=50000)
+        assert sol["rc"] == 0 and sol["true_resid"] <= 1e-8
+        assert np.linalg.norm(sol["x"] - ref["x"]) <= 1e-8 * np.linalg.norm(ref["x"])
     ctx.close()
 
 
