@@ -59,7 +59,9 @@ SEED = 5
 NCU_TRAFFIC_PER_BLOCK = {"upper_blocks_float4_atomics": (375.615488e6 + 3.251968e6) / 8624609}
 # the shared-element-matrix operator on the 40^3 case (64,000 volume elements, one launch inside a solve):
 # dram__bytes_read.sum + dram__bytes_write.sum per volume element (profiles/matfree_shared_matrix_elasticity_q2.txt)
-NCU_TRAFFIC_PER_ELEMENT = {"matrix_free_shared_matrix_tcgen05": (24.5696e6 + 0.0) / 64000}
+NCU_TRAFFIC_PER_ELEMENT = {"matrix_free_shared_matrix_tcgen05": (24.5696e6 + 0.0) / 64000,
+                           # the lattice-block operator on the same 40^3 case (profiles/matfree_lattice_blocks_elasticity_q2.txt)
+                           "matrix_free_shared_matrix_lattice_blocks": (17.261312e6 + 0.0) / 64000}
 
 
 def parse():
@@ -304,7 +306,7 @@ def run_gpu(args):
     chosen = tune.get("chosen", "block_csr")
     mf_flops = None
     matfree = chosen in ("matrix_free_elements", "matrix_free_sum_factorised", "matrix_free_tcgen05_3xtf32",
-                         "matrix_free_shared_matrix_tcgen05")
+                         "matrix_free_shared_matrix_tcgen05", "matrix_free_shared_matrix_lattice_blocks")
     mma_flops = None
     if matfree:
         # element records (corners 96 B, block rows 108 B, lambda/mu 8 B, affine geometry 40 B), penalty-face
@@ -321,6 +323,15 @@ def run_gpu(args):
             # algorithmic FLOPs: the 81 x 81 product per element; the MMAs execute 3 products of the padded tile
             mf_flops = nvol * 2 * 81 * 81 + nface * 2 * 9 * 9 * 6
             mma_flops = -(-nvol // 128) * 3 * 2 * 128 * 96 * 88
+        elif chosen == "matrix_free_shared_matrix_lattice_blocks":
+            kern = ("k_mf_hex27_gt: the same K_e = mu_e Khat tcgen05 3xTF32 GEMM over lattice blocks of 8 x 8 x 2 "
+                    "elements: a block's connect values and results in shared memory, plain stores inside the block, "
+                    "float4 reductions on its faces, loader and writer warp groups pipelined over blocks (mu per "
+                    "element, the lattice connect map and one pass of p and q are its HBM bytes)")
+            mf_flops = nvol * 2 * 81 * 81 + nface * 2 * 9 * 9 * 6
+            mma_flops = -(-nvol // 128) * 3 * 2 * 128 * 96 * 88
+            # reductions: the connects on block faces (17 x 17 x 5 box less its 15 x 15 x 3 inside) and penalty faces
+            l2_atomics = -(-n // 8) * -(-n // 8) * -(-n // 2) * (17 * 17 * 5 - 15 * 15 * 3) + 9 * nface
         elif chosen == "matrix_free_sum_factorised":
             kern = ("k_mf_hex27_sf: matrix-free Q2 elasticity, sum-factorised on Lagrange nodal values, one warp per "
                     "element (CUDA-core FP32; records + one pass of p and q are its HBM bytes)")
@@ -346,6 +357,8 @@ def run_gpu(args):
     if matfree:
         rec = 108 + 8 if chosen == "matrix_free_shared_matrix_tcgen05" else 96 + 108 + 8 + 40
         bytes32 = nvol * rec + nface * (48 + 36) + nbrow * 16 + nbrow * 16
+        if chosen == "matrix_free_shared_matrix_lattice_blocks":  # mu per element; connect map and face flag per row
+            bytes32 = nvol * 4 + nbrow * (4 + 1) + nface * (48 + 36) + nbrow * 16 + nbrow * 16
     bytes64 = nnz * (8 + 4) + (neq + 1) * 8 + neq * 8 + neq * 8 + neq * 8
     pk = peaks()
     hbm = pk.get("hbm_gbs", 6800.0)

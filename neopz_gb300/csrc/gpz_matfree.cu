@@ -1488,6 +1488,21 @@ __global__ void __launch_bounds__(kGtThreads, 1) k_mf_hex27_gt(GtArgs G, const i
   } else {
     const int sw = warp - kGtGroup / 32, quarter = sw & 3, h = sw >> 2, le = quarter * 32 + lane;
     const int lx = le % kGtTx, ly = (le / kGtTx) % kGtTy, lz = le / (kGtTx * kGtTy);
+    // the block's connect rows (bit 30: on a penalty face) and p values for the write-out and p . q, loaded
+    // for the next block while this one's MMAs and results are waited for
+    int32_t br[kGtPre];
+    float4 pv[kGtPre];
+    auto fetch = [&](int64_t tile) {
+      const GtBlock b = gt_block(G, tile);
+#pragma unroll
+      for (int i = 0; i < kGtPre; i++) br[i] = gt_row(G, b, nmap, gl + i * kGtGroup);
+#pragma unroll
+      for (int i = 0; i < kGtPre; i++) {
+        pv[i] = br[i] >= 0 ? p4[br[i]] : make_float4(0.f, 0.f, 0.f, 0.f);
+        if (br[i] >= 0 && face[br[i]]) br[i] |= 1 << 30;
+      }
+    };
+    if (blockIdx.x < ntile) fetch(blockIdx.x);
     int k = 0;
     for (int64_t tile = blockIdx.x; tile < ntile; tile += gridDim.x, k++) {
       const int bf = k & 1;
@@ -1527,24 +1542,21 @@ __global__ void __launch_bounds__(kGtThreads, 1) k_mf_hex27_gt(GtArgs G, const i
       gm_bar(2, kGtGroup);
       // the block into q (plain stores strictly inside, reductions on its faces and on penalty faces); p . q
       const GtBlock b = gt_block(G, tile);
-      int32_t br[kGtPre];
-#pragma unroll
-      for (int i = 0; i < kGtPre; i++) br[i] = gt_row(G, b, nmap, gl + i * kGtGroup);
 #pragma unroll
       for (int i = 0; i < kGtPre; i++) {
         const int n = gl + i * kGtGroup;
         if (br[i] < 0) continue;
         const int x = n % kGtNx, y = (n / kGtNx) % kGtNy, z = n / (kGtNx * kGtNy);
         const int sl = gt_slot(x, y, z);
+        const int32_t r = br[i] & ~(1 << 30);
         const float4 v = make_float4(yt[sl], yt[kGtSlots + sl], yt[2 * kGtSlots + sl], 0.f);
-        yt[sl] = yt[kGtSlots + sl] = yt[2 * kGtSlots + sl] = 0.f;  // for block k + 2
-        const float4 pv = p4[br[i]];
-        en.add(v.x * pv.x + v.y * pv.y + v.z * pv.z);
-        const bool inside = x > 0 && x < 2 * b.ex && y > 0 && y < 2 * b.ey && z > 0 && z < 2 * b.ez && !face[br[i]];
-        if (inside) q4[br[i]] = v;
-        else red_add_f4(&q4[br[i]], v);
+        yt[sl] = yt[kGtSlots + sl] = yt[2 * kGtSlots + sl] = 0.f;  // for block k + 2 (after the writers' next vote)
+        en.add(v.x * pv[i].x + v.y * pv[i].y + v.z * pv[i].z);
+        const bool inside = x > 0 && x < 2 * b.ex && y > 0 && y < 2 * b.ey && z > 0 && z < 2 * b.ez && !(br[i] & (1 << 30));
+        if (inside) q4[r] = v;
+        else red_add_f4(&q4[r], v);
       }
-      gm_bar(2, kGtGroup);
+      if (tile + gridDim.x < ntile) fetch(tile + gridDim.x);
     }
   }
   __syncthreads();
