@@ -124,27 +124,35 @@ int gpz_mesh_upload(gpz_ctx *ctx, const gpz_mesh_desc *d) {
                 GPZ_E_INVALID, "null array");
     // TPZBlock positions are consecutive in sequence-number order; the pattern
     // builder relies on it (columns sorted by connect = sorted by equation).
-    int64_t pos = 0;
-    for (int64_t i = 0; i < d->nconnects; i++) {
-      GPZ_REQUIRE(d->block_pos[i] == pos, GPZ_E_INVALID, "block positions must be consecutive in connect order");
-      GPZ_REQUIRE(d->block_size[i] >= 0, GPZ_E_INVALID, "block size");
-      pos += d->block_size[i];
-    }
-    GPZ_REQUIRE(pos == d->neq, GPZ_E_INVALID, "sum of block sizes != neq");
-    for (int64_t e = 0; e < d->nel; e++) {
-      int t = d->el_type[e];
-      GPZ_REQUIRE(t == GPZ_EL_LINE || t == GPZ_EL_QUAD || t == GPZ_EL_HEX, GPZ_E_UNSUPPORTED_ELEMENT, "element type");
-      const ElemTopo &tp = topo(t);
-      for (int k = 0; k < tp.ncorner; k++) {
-        int64_t nd = d->el_nodes[e * 8 + k];
-        GPZ_REQUIRE(nd >= 0 && nd < d->nnodes, GPZ_E_INVALID, "corner node index");
+    // (checked on the host threads; the first failing chunk's message is the one reported)
+    GPZ_REQUIRE(d->nconnects == 0 || d->block_pos[0] == 0, GPZ_E_INVALID,
+                "block positions must be consecutive in connect order");
+    GPZ_REQUIRE(d->nconnects > 0 || d->neq == 0, GPZ_E_INVALID, "sum of block sizes != neq");
+    host_parallel(d->nconnects, [&](int64_t i0, int64_t i1) {
+      for (int64_t i = i0; i < i1; i++) {
+        GPZ_REQUIRE(d->block_size[i] >= 0, GPZ_E_INVALID, "block size");
+        const int64_t next = i + 1 < d->nconnects ? d->block_pos[i + 1] : d->neq;
+        GPZ_REQUIRE(d->block_pos[i] + d->block_size[i] == next, GPZ_E_INVALID,
+                    i + 1 < d->nconnects ? "block positions must be consecutive in connect order"
+                                         : "sum of block sizes != neq");
       }
-      for (int s = 0; s < tp.nsides; s++) {
-        int64_t cn = d->el_conn[e * 27 + s];
-        GPZ_REQUIRE(cn >= 0 && cn < d->nconnects, GPZ_E_INVALID, "connect index");
+    });
+    host_parallel(d->nel, [&](int64_t e0, int64_t e1) {
+      for (int64_t e = e0; e < e1; e++) {
+        int t = d->el_type[e];
+        GPZ_REQUIRE(t == GPZ_EL_LINE || t == GPZ_EL_QUAD || t == GPZ_EL_HEX, GPZ_E_UNSUPPORTED_ELEMENT, "element type");
+        const ElemTopo &tp = topo(t);
+        for (int k = 0; k < tp.ncorner; k++) {
+          int64_t nd = d->el_nodes[e * 8 + k];
+          GPZ_REQUIRE(nd >= 0 && nd < d->nnodes, GPZ_E_INVALID, "corner node index");
+        }
+        for (int s = 0; s < tp.nsides; s++) {
+          int64_t cn = d->el_conn[e * 27 + s];
+          GPZ_REQUIRE(cn >= 0 && cn < d->nconnects, GPZ_E_INVALID, "connect index");
+        }
+        GPZ_REQUIRE(d->el_order[e] >= 1 && d->el_order[e] <= 3, GPZ_E_UNSUPPORTED_ELEMENT, "order must be 1..3");
       }
-      GPZ_REQUIRE(d->el_order[e] >= 1 && d->el_order[e] <= 3, GPZ_E_UNSUPPORTED_ELEMENT, "order must be 1..3");
-    }
+    });
     const auto t1 = std::chrono::steady_clock::now();
     c.dim = d->dim;
     c.nstate = d->nstate;
@@ -277,9 +285,18 @@ int gpz_pattern_build(gpz_ctx *ctx, int sym, int64_t *nnz_out) {
   return guarded(ctx, [&](Ctx &c) {
     GPZ_REQUIRE(c.have_mesh, GPZ_E_NOT_READY, "no mesh");
     c.neq = c.neq_mesh;
+    const auto t0 = std::chrono::steady_clock::now();
     build_pattern(c);
+    const auto t1 = std::chrono::steady_clock::now();
     build_upper(c);
+    const auto t2 = std::chrono::steady_clock::now();
     build_element_offsets(c);
+    const auto t3 = std::chrono::steady_clock::now();
+    auto ms = [](std::chrono::steady_clock::time_point a, std::chrono::steady_clock::time_point b) {
+      return std::to_string(std::chrono::duration<double, std::milli>(b - a).count());
+    };
+    c.pattern_report = "{\"full_csr\": " + ms(t0, t1) + ", \"upper_and_diagonal\": " + ms(t1, t2) +
+                       ", \"element_offsets\": " + ms(t2, t3) + "}";
     if (c.flt.active) condense_pattern(c);
     c.user_sym = sym ? 1 : 0;
     c.have_pattern = true;
@@ -336,7 +353,8 @@ int gpz_assembly_report(gpz_ctx *ctx, char *buf, int64_t len) {
                     (c.asm_tune_report.empty() ? std::string("null") : c.asm_tune_report) + ", \"launch_mode_ms\": " +
                     (c.asm_mode_report.empty() ? std::string("null") : c.asm_mode_report) + ", \"fp32_elements\": " +
                     (c.fp32_report.empty() ? std::string("null") : c.fp32_report) + ", \"mesh_upload_ms\": " +
-                    (c.upload_report.empty() ? std::string("null") : c.upload_report) + "}";
+                    (c.upload_report.empty() ? std::string("null") : c.upload_report) + ", \"pattern_ms\": " +
+                    (c.pattern_report.empty() ? std::string("null") : c.pattern_report) + "}";
     GPZ_REQUIRE((int64_t)r.size() < len, GPZ_E_INVALID, "buffer too small");
     std::copy(r.begin(), r.end(), buf);
     buf[r.size()] = 0;
@@ -451,10 +469,11 @@ namespace {
 __global__ void k_gather_upper(const double *__restrict__ a, const int64_t *__restrict__ diagpos,
                                const int64_t *__restrict__ ia, const int64_t *__restrict__ ia_up, int64_t neq,
                                double *__restrict__ out) {
-  int64_t r = blockIdx.x;
+  const int64_t r = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;  // a warp per row
+  const int lane = threadIdx.x & 31;
   if (r >= neq) return;
-  int64_t d = diagpos[r], n = ia[r + 1] - d, o = ia_up[r];
-  for (int64_t k = threadIdx.x; k < n; k += blockDim.x) out[o + k] = a[d + k];
+  const int64_t d = diagpos[r], n = ia[r + 1] - d, o = ia_up[r];
+  for (int64_t k = lane; k < n; k += 32) out[o + k] = a[d + k];
 }
 }  // namespace
 
@@ -468,7 +487,7 @@ int gpz_matrix_download(gpz_ctx *ctx, double *A) {
       DBuf<double> up;
       up.alloc(std::max<int64_t>(c.nnz_upper, 1));
       if (c.neq) {
-        k_gather_upper<<<(unsigned)c.neq, 128, 0, c.stream>>>(c.d_a.p, c.d_diagpos.p, c.d_ia.p, c.d_ia_up.p, c.neq,
+        k_gather_upper<<<grid_for(c.neq * 32, 256), 256, 0, c.stream>>>(c.d_a.p, c.d_diagpos.p, c.d_ia.p, c.d_ia_up.p, c.neq,
                                                               up.p);
         c.launches++;
         GPZ_CUDA_TRY(cudaGetLastError());

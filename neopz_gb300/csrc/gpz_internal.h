@@ -309,6 +309,7 @@ struct Ctx {
   bool asm_mode_auto = false;                // the launch mode is autotuned (gpz_assembly_mode(-1))
   std::string asm_mode_report;               // the timings of the two launch modes
   std::string upload_report, bucket_report;  // host-side timings of the last mesh upload (ms)
+  std::string pattern_report;                // stage timings of the last pattern build (ms)
   int ncolours = 0;
   DBuf<int> d_err;                           // device-side check flag
 

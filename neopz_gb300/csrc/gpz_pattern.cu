@@ -245,13 +245,15 @@ __global__ void k_diagpos(const int64_t *__restrict__ ia, const int32_t *__restr
   if (uplen) uplen[r] = ia[r + 1] - k;
 }
 
+// a warp per row (a CTA per row launched millions of small CTAs)
 __global__ void k_fill_upper(const int64_t *__restrict__ ia, const int32_t *__restrict__ ja,
                              const int64_t *__restrict__ diagpos, const int64_t *__restrict__ ia_up, int64_t neq,
                              int32_t *__restrict__ ja_up) {
-  int64_t r = (int64_t)blockIdx.x;
+  const int64_t r = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
   if (r >= neq) return;
-  int64_t d = diagpos[r], n = ia[r + 1] - d, o = ia_up[r];
-  for (int64_t k = threadIdx.x; k < n; k += blockDim.x) ja_up[o + k] = ja[d + k];
+  const int64_t d = diagpos[r], n = ia[r + 1] - d, o = ia_up[r];
+  for (int64_t k = lane; k < n; k += 32) ja_up[o + k] = ja[d + k];
 }
 
 // Offset of block B inside the rows of block A, for every side pair of every
@@ -365,7 +367,8 @@ void build_upper(Ctx &c) {
   GPZ_CUDA_TRY(cudaStreamSynchronize(s));
   c.d_ja_up.alloc(std::max<int64_t>(c.nnz_upper, 1));
   if (c.neq > 0) {
-    k_fill_upper<<<(unsigned)c.neq, 128, 0, s>>>(c.d_ia.p, c.d_ja.p, c.d_diagpos.p, c.d_ia_up.p, c.neq, c.d_ja_up.p);
+    k_fill_upper<<<grid_for(c.neq * 32, 256), 256, 0, s>>>(c.d_ia.p, c.d_ja.p, c.d_diagpos.p, c.d_ia_up.p, c.neq,
+                                                           c.d_ja_up.p);
     c.launches++;
     GPZ_CUDA_TRY(cudaGetLastError());
   }
