@@ -119,6 +119,54 @@ __global__ void k_mf_records(int64_t n, const int64_t *__restrict__ elems, const
 }
 
 // penalty faces: y_a += big sum_q w |J| phi_a phi_b u_b; their energy goes to *energy
+// One penalty face by one warp: big sum_q w |J| phi_a (sum_b phi_b u_b) added to q, its energy to en.
+// sphi / sd / sw: the face tables in shared memory; su, sc, st: the warp's own scratch.
+__device__ __forceinline__ void mf_face(int64_t i, int lane, const float *sphi, const float *sd, const float *sw,
+                                        float (*su)[4], float *sc, float (*st)[4], float big,
+                                        const float *__restrict__ rxyz, const int32_t *__restrict__ rows,
+                                        const float4 *__restrict__ p4, float4 *__restrict__ q4, KSum &en) {
+  int32_t row = 0;
+  float4 u = make_float4(0.f, 0.f, 0.f, 0.f);
+  if (lane < kFS) {
+    row = rows[i * kFS + lane];
+    u = p4[row];
+    su[lane][0] = u.x;
+    su[lane][1] = u.y;
+    su[lane][2] = u.z;
+  }
+  if (lane < 12) sc[lane] = rxyz[i * 12 + lane];
+  __syncwarp();
+  if (lane < kFQ) {
+    const int q = lane;
+    float g0[3] = {0.f, 0.f, 0.f}, g1[3] = {0.f, 0.f, 0.f};
+    for (int k = 0; k < 4; k++)
+      for (int j = 0; j < 3; j++) {
+        g0[j] += sc[k * 3 + j] * sd[(q * 2 + 0) * kFS + k];
+        g1[j] += sc[k * 3 + j] * sd[(q * 2 + 1) * kFS + k];
+      }
+    const float cx = g0[1] * g1[2] - g0[2] * g1[1], cy = g0[2] * g1[0] - g0[0] * g1[2],
+                cz = g0[0] * g1[1] - g0[1] * g1[0];
+    const float wd = big * sw[q] * sqrtf(cx * cx + cy * cy + cz * cz);
+    float uq[3] = {0.f, 0.f, 0.f};
+    for (int b = 0; b < kFS; b++) {
+      const float ph = sphi[q * kFS + b];
+      for (int s = 0; s < 3; s++) uq[s] += ph * su[b][s];
+    }
+    for (int s = 0; s < 3; s++) st[q][s] = wd * uq[s];
+  }
+  __syncwarp();
+  if (lane < kFS) {
+    float y[3] = {0.f, 0.f, 0.f};
+    for (int q = 0; q < kFQ; q++) {
+      const float ph = sphi[q * kFS + lane];
+      for (int s = 0; s < 3; s++) y[s] += st[q][s] * ph;
+    }
+    en.add(y[0] * u.x + y[1] * u.y + y[2] * u.z);
+    red_add_f4(&q4[row], make_float4(y[0], y[1], y[2], 0.f));
+  }
+  __syncwarp();
+}
+
 __global__ void __launch_bounds__(kThreads) k_mf_faces(int64_t n, const float *__restrict__ rxyz,
                                                        const int32_t *__restrict__ rows, const float *__restrict__ phi,
                                                        const float *__restrict__ dphi, const float *__restrict__ w,
@@ -134,48 +182,8 @@ __global__ void __launch_bounds__(kThreads) k_mf_faces(int64_t n, const float *_
   const int lane = threadIdx.x & 31, wp = threadIdx.x >> 5;
   KSum en;
   for (int64_t i = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; i < n;
-       i += ((int64_t)gridDim.x * blockDim.x) >> 5) {
-    int32_t row = 0;
-    float4 u = make_float4(0.f, 0.f, 0.f, 0.f);
-    if (lane < kFS) {
-      row = rows[i * kFS + lane];
-      u = p4[row];
-      su[wp][lane][0] = u.x;
-      su[wp][lane][1] = u.y;
-      su[wp][lane][2] = u.z;
-    }
-    if (lane < 12) sc[wp][lane] = rxyz[i * 12 + lane];
-    __syncwarp();
-    if (lane < kFQ) {
-      const int q = lane;
-      float g0[3] = {0.f, 0.f, 0.f}, g1[3] = {0.f, 0.f, 0.f};
-      for (int k = 0; k < 4; k++)
-        for (int j = 0; j < 3; j++) {
-          g0[j] += sc[wp][k * 3 + j] * sd[(q * 2 + 0) * kFS + k];
-          g1[j] += sc[wp][k * 3 + j] * sd[(q * 2 + 1) * kFS + k];
-        }
-      const float cx = g0[1] * g1[2] - g0[2] * g1[1], cy = g0[2] * g1[0] - g0[0] * g1[2],
-                  cz = g0[0] * g1[1] - g0[1] * g1[0];
-      const float wd = big * sw[q] * sqrtf(cx * cx + cy * cy + cz * cz);
-      float uq[3] = {0.f, 0.f, 0.f};
-      for (int b = 0; b < kFS; b++) {
-        const float ph = sphi[q * kFS + b];
-        for (int s = 0; s < 3; s++) uq[s] += ph * su[wp][b][s];
-      }
-      for (int s = 0; s < 3; s++) st[wp][q][s] = wd * uq[s];
-    }
-    __syncwarp();
-    if (lane < kFS) {
-      float y[3] = {0.f, 0.f, 0.f};
-      for (int q = 0; q < kFQ; q++) {
-        const float ph = sphi[q * kFS + lane];
-        for (int s = 0; s < 3; s++) y[s] += st[wp][q][s] * ph;
-      }
-      en.add(y[0] * u.x + y[1] * u.y + y[2] * u.z);
-      red_add_f4(&q4[row], make_float4(y[0], y[1], y[2], 0.f));
-    }
-    __syncwarp();
-  }
+       i += ((int64_t)gridDim.x * blockDim.x) >> 5)
+    mf_face(i, lane, sphi, sd, sw, su[wp], sc[wp], st[wp], big, rxyz, rows, p4, q4, en);
   double v[1] = {en.get()}, tot[1];
   if (grid_reduce<1>(v, R, tot) && threadIdx.x == 0) *energy = tot[0];
 }
@@ -1349,19 +1357,27 @@ __device__ __forceinline__ int32_t gt_row(const GtArgs &G, const GtBlock &b, con
 
 // nmap: [(2 mx + 1)(2 my + 1)(2 mz + 1)] block row of each lattice connect (-1: none);
 // emu: [mx my mz] mu of the element at each lattice cell (-1: none); face: [block rows] 1 on penalty faces
+struct GtFaces {  // the penalty faces, applied by the same CTAs before the blocks (k_mf_faces' work)
+  int64_t n;
+  const float *rxyz, *phi, *dphi, *w;
+  const int32_t *rows;
+  float big;
+};
+
 __global__ void __launch_bounds__(kGtThreads, 1) k_mf_hex27_gt(GtArgs G, const int32_t *__restrict__ nmap,
                                                                const float *__restrict__ emu,
                                                                const uint8_t *__restrict__ face,
                                                                const float4 *__restrict__ bsplit,
                                                                const float4 *__restrict__ p4, float4 *__restrict__ q4,
-                                                               const double *__restrict__ face_energy,
-                                                               int *__restrict__ err, Red R) {
+                                                               GtFaces F, int *__restrict__ err, Red R) {
   if (!active(R.iscal)) return;
   extern __shared__ __align__(1024) unsigned char sm[];
   __shared__ uint32_t s_tmem;
   __shared__ volatile int s_abort;
   __shared__ __align__(8) uint64_t s_done[2], s_free[2];
   __shared__ int8_t s_off[kNS][3];
+  __shared__ float s_fphi[kFQ * kFS], s_fd[kFQ * 2 * kFS], s_fw[kFQ];
+  __shared__ float s_fu[kGtThreads / 32][kFS][4], s_fc[kGtThreads / 32][12], s_ft[kGtThreads / 32][kFQ][4];
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const bool loader = tid < kGtGroup;
   const int gl = tid & (kGtGroup - 1);
@@ -1387,6 +1403,9 @@ __global__ void __launch_bounds__(kGtThreads, 1) k_mf_hex27_gt(GtArgs G, const i
     }
     asm volatile("fence.mbarrier_init.release.cluster;");
   }
+  for (int k = tid; k < kFQ * kFS; k += kGtThreads) s_fphi[k] = F.phi[k];
+  for (int k = tid; k < kFQ * 2 * kFS; k += kGtThreads) s_fd[k] = F.dphi[k];
+  if (tid < kFQ) s_fw[tid] = F.w[tid];
   asm volatile("tcgen05.fence::before_thread_sync;");
   __syncthreads();
   asm volatile("tcgen05.fence::after_thread_sync;");
@@ -1395,6 +1414,9 @@ __global__ void __launch_bounds__(kGtThreads, 1) k_mf_hex27_gt(GtArgs G, const i
                  bl = tc_smem(sm + GM_BL);
   const int64_t ntile = (int64_t)G.ntx * G.nty * G.ntz;
   KSum en;
+  // the penalty faces (their connects are written by the blocks with reductions, never with plain stores)
+  for (int64_t i = (int64_t)blockIdx.x * (kGtThreads / 32) + warp; i < F.n; i += (int64_t)gridDim.x * (kGtThreads / 32))
+    mf_face(i, lane, s_fphi, s_fd, s_fw, s_fu[warp], s_fc[warp], s_ft[warp], F.big, F.rxyz, F.rows, p4, q4, en);
   int last = -1;  // the issuer's last committed block
   if (loader) {
     int32_t pbr[kGtPre];
@@ -1570,7 +1592,7 @@ __global__ void __launch_bounds__(kGtThreads, 1) k_mf_hex27_gt(GtArgs G, const i
   if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tm), "r"(512));
   double v[1] = {failed ? 0.0 : en.get()}, tot[1];
   if (grid_reduce<1, kGtThreads / 32>(v, R, tot) && threadIdx.x == 0) {
-    const double pq = tot[0] + (face_energy ? *face_energy : 0.0);
+    const double pq = tot[0];
     R.scal[S_PQ] = pq;
     R.scal[S_ALPHA] = R.scal[S_RHO] / pq;
     R.iscal[I_SP32]++;
@@ -2907,7 +2929,7 @@ void matfree_spmv(Ctx &c, cudaStream_t s, int mode) {
   Red R{w.partial.p, w.counter.p, w.scal.p, w.iscal.p};
   const float4 *p4 = (const float4 *)w.pm.p;
   float4 *q4 = (float4 *)w.q32.p;
-  if (M.nface) {
+  if (M.nface && mode != 4) {  // (the lattice-block kernel applies the faces itself)
     k_mf_faces<<<M.grid_face, kThreads, 0, s>>>(M.nface, M.fxyz.p, M.frows.p, M.fphi.p, M.fdphi.p, M.fw.p, M.big, p4,
                                                 q4, M.energy.p, R);
     c.launches++;
@@ -2920,8 +2942,9 @@ void matfree_spmv(Ctx &c, cudaStream_t s, int mode) {
     k_mf_hex27_gm<<<M.grid_gm, kGmThreads, GM_END, s>>>(M.nvol, M.vrows.p, M.vlm.p, (const float4 *)M.gm_b.p, p4, q4, fe,
                                                         c.d_err.p, R);
   else if (mode == 4)
-    k_mf_hex27_gt<<<M.grid_gt, kGtThreads, GT_END, s>>>(M.gt, M.gt_nmap.p, M.gt_emu.p, M.gt_face.p,
-                                                        (const float4 *)M.gm_b.p, p4, q4, fe, c.d_err.p, R);
+    k_mf_hex27_gt<<<M.grid_gt, kGtThreads, GT_END, s>>>(
+        M.gt, M.gt_nmap.p, M.gt_emu.p, M.gt_face.p, (const float4 *)M.gm_b.p, p4, q4,
+        GtFaces{M.nface, M.fxyz.p, M.fphi.p, M.fdphi.p, M.fw.p, M.frows.p, M.big}, c.d_err.p, R);
   else if (mode == 2)
     k_mf_hex27_sf<<<M.grid_sf, kSfThreads, 0, s>>>(M.nvol, M.vxyz.p, M.vrows.p, M.vlm.p, M.vgeo.p, M.sf_tab.p,
                                                    M.sf_idx.p, p4, q4, fe, R);

@@ -392,18 +392,23 @@ def test_fp32_operator_layouts_match_fp64_spmv(built, variant):
     ctx.close()
 
 
-@pytest.mark.parametrize("shape", [(17, 9, 5), (16, 16, 4), (30, 30, 30)])
+@pytest.mark.parametrize("shape", [(17, 9, 5), (16, 16, 4), (30, 30, 30), (12, 10, 6, "sheared")])
 def test_shared_matrix_operator_over_lattice_blocks(built, shape):
     """The shared-element-matrix operator over lattice blocks of 8 x 8 x 2 elements: full and partial blocks,
-    more blocks than CTAs (30^3: 960 blocks), and a box of unequal sides.  It applies the assembled operator
+    more blocks than CTAs (30^3: 960 blocks), a box of unequal sides and a sheared one (lattice vectors not
+    orthogonal).  It applies the assembled operator
     (1e-5 against the FP64 SpMV, the same bar as the tile operator it restructures) and the mixed CG over it
     reaches a true 1e-8 with the solution within 1e-8 of the FP64 solution."""
     g = _gpz()
     rng = np.random.default_rng(17)
-    nx, ny, nz = shape
+    nx, ny, nz = shape[:3]
     mats = [(1, g.material(g.GPZ_MAT_ELAST3D, 3, E=1.0, nu=0.3, force=(0.0, 0.0, -1.0), forcing=g.GPZ_F_CONST))]
     grid = g.Grid(3, (nx, ny, nz), (0, 0, 0), (1.0, 0.7, 0.4), [1, -1, -2, -2, -2, -2, -2], True, 2, mats,
                   [(-1, g.bc(0, 0))], elem_coef=np.exp(rng.standard_normal(nx * ny * nz)))
+    if len(shape) > 3:  # a sheared box: the elements stay translates, the lattice vectors are not orthogonal
+        xyz = grid.nodes()
+        xyz[:, 0] += 0.3 * xyz[:, 1] + 0.2 * xyz[:, 2]
+        xyz[:, 1] += 0.15 * xyz[:, 2]
     ctx = g.Context(0)
     ctx.upload_mesh(grid)
     ctx.build_pattern(False)
