@@ -215,7 +215,7 @@ struct MatFree {
 struct MatFree1 {
   bool ready = false;
   int64_t nvol = 0, nface = 0;
-  int ntab = 0, grid = 1, grid_face = 1;
+  int ntab = 0, grid = 1;
   DBuf<int32_t> vrows;                       // [ntile * 128][27] equations, -1 padding
   DBuf<float> vcoef;                         // [ntile * 128] element coefficient (k, or 1)
   DBuf<float> b;                             // [2][32 x 32] Khat hi, lo (K-major core matrices)

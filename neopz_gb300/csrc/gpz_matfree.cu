@@ -118,7 +118,6 @@ __global__ void k_mf_records(int64_t n, const int64_t *__restrict__ elems, const
   }
 }
 
-// penalty faces: y_a += big sum_q w |J| phi_a phi_b u_b; their energy goes to *energy
 // One penalty face by one warp: big sum_q w |J| phi_a (sum_b phi_b u_b) added to q, its energy to en.
 // sphi / sd / sw: the face tables in shared memory; su, sc, st: the warp's own scratch.
 __device__ __forceinline__ void mf_face(int64_t i, int lane, const float *sphi, const float *sd, const float *sw,
@@ -167,6 +166,7 @@ __device__ __forceinline__ void mf_face(int64_t i, int lane, const float *sphi, 
   __syncwarp();
 }
 
+// penalty faces: y_a += big sum_q w |J| phi_a phi_b u_b; their energy goes to *energy
 __global__ void __launch_bounds__(kThreads) k_mf_faces(int64_t n, const float *__restrict__ rxyz,
                                                        const int32_t *__restrict__ rows, const float *__restrict__ phi,
                                                        const float *__restrict__ dphi, const float *__restrict__ w,
@@ -2485,8 +2485,8 @@ void two_level_assemble(Ctx &c) {
 // constants -- and split into the A operand; thread 0 issues the MMAs into
 // accumulator pair k mod 2) and 4 scatterer warps (lane quarter = warp, 32
 // columns read from TMEM, k_e Y added to q with scalar reductions, the element
-// energy for p.q).  The penalty faces of every Dirichlet side are applied by
-// k_mf_faces1 before it.
+// energy for p.q).  The penalty faces of every Dirichlet side (one table per
+// face bucket) are applied by the same CTAs before the tiles, a warp per face.
 namespace {
 constexpr int kG1Threads = 256, kG1Group = 128, kG1El = 128, kG1K = 32, kG1N = 32;
 constexpr uint32_t kG1Small = 32;  // TMEM column offset of the correction accumulator (buffer b at 64 b)
@@ -2527,57 +2527,46 @@ __global__ void k_mf1_face_records(int64_t n, const int64_t *__restrict__ elems,
 
 // penalty faces of a scalar problem: y_a += big sum_q w |J| phi_a phi_b u_b, one warp per face, the face's
 // table (its bucket's shapes, gradients and weights) by index; their energy to *energy
-__global__ void __launch_bounds__(kThreads) k_mf_faces1(int64_t n, const float *__restrict__ rxyz,
-                                                        const int32_t *__restrict__ rows, const uint8_t *__restrict__ tab,
-                                                        const float *__restrict__ tabs, int ntab, float big,
-                                                        const float *__restrict__ p, float *__restrict__ q,
-                                                        double *__restrict__ energy, Red R) {
-  if (!active(R.iscal)) return;
-  constexpr int kTab = kFQ * kFS + kFQ * 2 * kFS + kFQ;  // phi, dphi, w
-  __shared__ float st[kF1MaxTab * kTab];
-  __shared__ float su[kWarps][kFS], sc[kWarps][12], sq[kWarps][kFQ];
-  for (int k = threadIdx.x; k < ntab * kTab; k += blockDim.x) st[k] = tabs[k];
-  __syncthreads();
-  const int lane = threadIdx.x & 31, wp = threadIdx.x >> 5;
-  KSum en;
-  for (int64_t i = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; i < n;
-       i += ((int64_t)gridDim.x * blockDim.x) >> 5) {
-    const float *T = st + (int)tab[i] * kTab, *phi = T, *dphi = T + kFQ * kFS, *w = dphi + kFQ * 2 * kFS;
-    int32_t row = 0;
-    float u = 0.f;
-    if (lane < kFS) {
-      row = rows[i * kFS + lane];
-      u = p[row];
-      su[wp][lane] = u;
-    }
-    if (lane < 12) sc[wp][lane] = rxyz[i * 12 + lane];
-    __syncwarp();
-    if (lane < kFQ) {
-      const int qp = lane;
-      float g0[3] = {0.f, 0.f, 0.f}, g1[3] = {0.f, 0.f, 0.f};
-      for (int k = 0; k < 4; k++)
-        for (int j = 0; j < 3; j++) {
-          g0[j] += sc[wp][k * 3 + j] * dphi[(qp * 2 + 0) * kFS + k];
-          g1[j] += sc[wp][k * 3 + j] * dphi[(qp * 2 + 1) * kFS + k];
-        }
-      const float cx = g0[1] * g1[2] - g0[2] * g1[1], cy = g0[2] * g1[0] - g0[0] * g1[2],
-                  cz = g0[0] * g1[1] - g0[1] * g1[0];
-      float uq = 0.f;
-      for (int b = 0; b < kFS; b++) uq += phi[qp * kFS + b] * su[wp][b];
-      sq[wp][qp] = big * w[qp] * sqrtf(cx * cx + cy * cy + cz * cz) * uq;
-    }
-    __syncwarp();
-    if (lane < kFS) {
-      float y = 0.f;
-      for (int qp = 0; qp < kFQ; qp++) y += sq[wp][qp] * phi[qp * kFS + lane];
-      en.add(y * u);
-      red_add_f1(&q[row], y);
-    }
-    __syncwarp();
+constexpr int kF1Tab = kFQ * kFS + kFQ * 2 * kFS + kFQ;  // one face table: phi, dphi, w
+
+// One penalty face of a scalar problem by one warp (table T in shared memory; su, sc, sq: the warp's scratch)
+__device__ __forceinline__ void mf_face1(int64_t i, int lane, const float *T, float *su, float *sc, float *sq,
+                                         float big, const float *__restrict__ rxyz, const int32_t *__restrict__ rows,
+                                         const float *__restrict__ p, float *__restrict__ q, KSum &en) {
+  const float *phi = T, *dphi = T + kFQ * kFS, *w = dphi + kFQ * 2 * kFS;
+  int32_t row = 0;
+  float u = 0.f;
+  if (lane < kFS) {
+    row = rows[i * kFS + lane];
+    u = p[row];
+    su[lane] = u;
   }
-  double v[1] = {en.get()}, tot[1];
-  if (grid_reduce<1>(v, R, tot) && threadIdx.x == 0) *energy = tot[0];
+  if (lane < 12) sc[lane] = rxyz[i * 12 + lane];
+  __syncwarp();
+  if (lane < kFQ) {
+    const int qp = lane;
+    float g0[3] = {0.f, 0.f, 0.f}, g1[3] = {0.f, 0.f, 0.f};
+    for (int k = 0; k < 4; k++)
+      for (int j = 0; j < 3; j++) {
+        g0[j] += sc[k * 3 + j] * dphi[(qp * 2 + 0) * kFS + k];
+        g1[j] += sc[k * 3 + j] * dphi[(qp * 2 + 1) * kFS + k];
+      }
+    const float cx = g0[1] * g1[2] - g0[2] * g1[1], cy = g0[2] * g1[0] - g0[0] * g1[2],
+                cz = g0[0] * g1[1] - g0[1] * g1[0];
+    float uq = 0.f;
+    for (int b = 0; b < kFS; b++) uq += phi[qp * kFS + b] * su[b];
+    sq[qp] = big * w[qp] * sqrtf(cx * cx + cy * cy + cz * cz) * uq;
+  }
+  __syncwarp();
+  if (lane < kFS) {
+    float y = 0.f;
+    for (int qp = 0; qp < kFQ; qp++) y += sq[qp] * phi[qp * kFS + lane];
+    en.add(y * u);
+    red_add_f1(&q[row], y);
+  }
+  __syncwarp();
 }
+
 
 __device__ __forceinline__ void g1_mma(uint32_t tm, uint32_t ah, uint32_t al, uint32_t bh, uint32_t bl) {
   const uint32_t id = (1u << 4) | (2u << 7) | (2u << 10) | ((uint32_t)(kG1N >> 3) << 17) | ((uint32_t)(kG1El >> 4) << 24);
@@ -2593,22 +2582,33 @@ __device__ __forceinline__ void g1_mma(uint32_t tm, uint32_t ah, uint32_t al, ui
 }
 
 // rows: [ntile * 128][27] equations, -1 past the n elements; coef [ntile * 128]
+struct G1Faces {  // the penalty faces, applied by the same CTAs before the tiles
+  int64_t n;
+  const float *rxyz, *tabs;
+  const int32_t *rows;
+  const uint8_t *tab;
+  int ntab;
+  float big;
+};
+
 __global__ void __launch_bounds__(kG1Threads, 2) k_mf_hex27_gm1(int64_t n, const int32_t *__restrict__ rows,
                                                                 const float *__restrict__ coef,
                                                                 const float4 *__restrict__ bsplit,
                                                                 const float *__restrict__ p, float *__restrict__ q,
-                                                                const double *__restrict__ face_energy,
-                                                                int *__restrict__ err, Red R) {
+                                                                G1Faces F, int *__restrict__ err, Red R) {
   if (!active(R.iscal)) return;
   extern __shared__ __align__(1024) unsigned char sm[];
   __shared__ uint32_t s_tmem;
   __shared__ volatile int s_abort;
   __shared__ __align__(8) uint64_t s_done[2], s_free[2];
+  __shared__ float s_ft[kF1MaxTab * kF1Tab];
+  __shared__ float s_fu[kG1Threads / 32][kFS], s_fc[kG1Threads / 32][12], s_fq[kG1Threads / 32][kFQ];
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const bool gatherer = tid < kG1Group;
   const int gl = tid & (kG1Group - 1);
   const int4 *rows4 = (const int4 *)rows;
   for (uint32_t i = tid; i < 2 * kG1B / 16; i += kG1Threads) ((float4 *)(sm + G1_BH))[i] = bsplit[i];
+  for (int k = tid; k < F.ntab * kF1Tab; k += kG1Threads) s_ft[k] = F.tabs[k];
   asm volatile("fence.proxy.async.shared::cta;");
   if (warp == 0) {
     asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(tc_smem(&s_tmem)), "r"(128));
@@ -2631,6 +2631,9 @@ __global__ void __launch_bounds__(kG1Threads, 2) k_mf_hex27_gm1(int64_t n, const
   const int64_t ntile = (n + kG1El - 1) / kG1El;
   constexpr int n4 = (int)(kG1R / 16);
   KSum en;
+  // the penalty faces first (the tiles add into q with reductions only, so the order does not matter)
+  for (int64_t f = (int64_t)blockIdx.x * (kG1Threads / 32) + warp; f < F.n; f += (int64_t)gridDim.x * (kG1Threads / 32))
+    mf_face1(f, lane, s_ft + (int)F.tab[f] * kF1Tab, s_fu[warp], s_fc[warp], s_fq[warp], F.big, F.rxyz, F.rows, p, q, en);
   int last = -1;
   if (gatherer) {
     const int32_t *rw = (const int32_t *)(sm + G1_RG);
@@ -2719,7 +2722,7 @@ __global__ void __launch_bounds__(kG1Threads, 2) k_mf_hex27_gm1(int64_t n, const
   if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tm), "r"(128));
   double vv[1] = {failed ? 0.0 : en.get()}, tot[1];
   if (grid_reduce<1>(vv, R, tot) && threadIdx.x == 0) {
-    const double pq = tot[0] + (face_energy ? *face_energy : 0.0);
+    const double pq = tot[0];
     R.scal[S_PQ] = pq;
     R.scal[S_ALPHA] = R.scal[S_RHO] / pq;
     R.iscal[I_SP32]++;
@@ -2817,7 +2820,6 @@ bool matfree1_build(Ctx &c) {
   GPZ_CUDA_TRY(cudaGetDevice(&dev));
   GPZ_CUDA_TRY(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
   M.grid = std::max(1, std::min(kGridBlocks, 2 * nsm));  // two 67 KB CTAs per SM
-  M.grid_face = (int)std::max<int64_t>(1, std::min<int64_t>(mf_grid(k_mf_faces1, kThreads), (M.nface + kWarps - 1) / kWarps));
   M.ready = true;
   return true;
 }
@@ -2827,13 +2829,10 @@ void matfree1_spmv(Ctx &c, cudaStream_t s, const float *p, float *q) {
   MatFree1 &M = c.mf1;
   SolverWork &w = c.sw;
   Red R{w.partial.p, w.counter.p, w.scal.p, w.iscal.p};
-  if (M.nface) {
-    k_mf_faces1<<<M.grid_face, kThreads, 0, s>>>(M.nface, M.fxyz.p, M.frows.p, M.ftab.p, M.ftabs.p, M.ntab, M.big, p,
-                                                 q, M.energy.p, R);
-    c.launches++;
-  }
-  k_mf_hex27_gm1<<<M.grid, kG1Threads, G1_END, s>>>(M.nvol, M.vrows.p, M.vcoef.p, (const float4 *)M.b.p, p, q,
-                                                    M.nface ? M.energy.p : nullptr, c.d_err.p, R);
+  // (the penalty faces are applied by the same CTAs)
+  k_mf_hex27_gm1<<<M.grid, kG1Threads, G1_END, s>>>(
+      M.nvol, M.vrows.p, M.vcoef.p, (const float4 *)M.b.p, p, q,
+      G1Faces{M.nface, M.fxyz.p, M.ftabs.p, M.frows.p, M.ftab.p, M.ntab, M.big}, c.d_err.p, R);
   c.launches++;
 }
 
