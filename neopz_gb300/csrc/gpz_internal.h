@@ -381,12 +381,15 @@ struct Ctx {
   bool have_bjinv = false;
   // variable-size block Jacobi (whole connect blocks of any size, or the
   // node-set blocks): block b holds equations vb_eq[vb_off[b] .. vb_off[b+1])
-  // and its inverse (row-major) at vb_inv[vb_ioff[b]]
+  // and its inverse (row-major) at vb_inv[vb_ioff[b]]; the FP32 copy of the
+  // mixed CG is column-major.  Tile t (one CTA of the FP32 kernels) holds
+  // blocks vb_tile[t] .. vb_tile[t+1], at most 256 equations.
   int vb_kind = 0;                           // 0 none, GPZ_PRECOND_BLOCK_JACOBI or GPZ_PRECOND_NODESET_JACOBI
-  int64_t vb_nb = 0;
+  int64_t vb_nb = 0, vb_ntile = 0;
   int vb_maxn = 0;
-  DBuf<int64_t> d_vb_off, d_vb_eq, d_vb_ioff;
+  DBuf<int64_t> d_vb_off, d_vb_eq, d_vb_ioff, d_vb_tile;
   DBuf<int32_t> d_vb_eqblk, d_vb_eqloc;      // equation -> block, position inside it
+  DBuf<int32_t> d_vb_posblk;                 // position in vb_eq -> block
   DBuf<double> d_vb_inv;
   DBuf<float> d_vb_inv32;
   bool have_vbinv = false;

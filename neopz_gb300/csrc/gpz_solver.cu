@@ -1084,17 +1084,21 @@ __global__ void __launch_bounds__(kThreads) k_mx_r32(const double *__restrict__ 
 // ---- variable-size block Jacobi: whole connect blocks of any size
 // (TPZBlockDiagonal of TPZBlockDiagonalStructMatrix, overlap = true) or the
 // node-set blocks of TPZNodesetCompute (TPZSparseBlockDiagonal, overlap =
-// false), Analysis/TPZAnalysis.cpp:1008-1107.  The vector kernels of CG and the
-// mixed CG walk blocks: one thread per block updates the block's equations
-// and applies the block's inverse to them (blocks of 3 to a few dozen
-// equations; the thread re-reads its own writes).
+// false), Analysis/TPZAnalysis.cpp:1008-1107.  The FP64 vector kernels of CG
+// walk blocks: one thread per block updates the block's equations and applies
+// the block's inverse to them (blocks of 3 to a few dozen equations; the
+// thread re-reads its own writes); the FP32 kernels of the mixed CG below take
+// one thread per equation.
 struct VBlk {
-  const int64_t *off;   // [nb + 1] into eq
-  const int64_t *eq;    // the blocks' equations
-  const int64_t *ioff;  // [nb] first entry of the block's inverse
-  const double *inv;    // FP64 inverses, row-major
-  const float *inv32;   // FP32 copies (mixed CG)
+  const int64_t *off;     // [nb + 1] into eq
+  const int64_t *eq;      // the blocks' equations
+  const int64_t *ioff;    // [nb] first entry of the block's inverse
+  const double *inv;      // FP64 inverses, row-major
+  const float *inv32;     // FP32 copies (mixed CG), column-major
   int64_t nb;
+  const int64_t *tile;    // [ntile + 1] first block of each tile of at most kThreads equations
+  const int32_t *posblk;  // position in eq -> block
+  int64_t ntile;
 };
 
 // z_i = sum_j inv[i][j] r[eq_j] for the n equations of one block (n <= kVbMax)
@@ -1275,23 +1279,69 @@ __global__ void __launch_bounds__(kThreads) k_vb_dot(const double *__restrict__ 
   }
 }
 
+// The FP32 kernels of the mixed CG take one thread per equation: a CTA walks
+// tiles of whole blocks (at most kThreads equations), puts the tile's residual
+// into shared memory and each thread forms its row of the block's product from
+// there, the inverse read column by column (inv32 is column-major, so a
+// block's threads read consecutive words).
+
+// inv32[ioff + j n + i] = inv[ioff + i n + j] in FP32
+__global__ void __launch_bounds__(kThreads) k_vb_inv32t(VBlk V, float *__restrict__ inv32) {
+  const int64_t npos = V.nb > 0 ? V.off[V.nb] : 0;
+  for (int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < npos; k += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t b = V.posblk[k], o = V.off[b];
+    const int n = (int)(V.off[b + 1] - o), i = (int)(k - o);
+    const double *B = V.inv + V.ioff[b];
+    float *T = inv32 + V.ioff[b];
+    for (int j = 0; j < n; j++) T[j * n + i] = (float)B[i * n + j];
+  }
+}
+
+// this thread's equation in tile t: n = 0 past the tile's end; s0 = the
+// block's first slot in the tile's shared residual (the thread's own slot is
+// threadIdx.x)
+struct VbRow {
+  int64_t e;
+  int n, i, s0;
+  const float *Bt;
+};
+__device__ __forceinline__ VbRow vb_row(const VBlk &V, int64_t t) {
+  VbRow w{0, 0, 0, 0, nullptr};
+  const int64_t k0 = V.off[V.tile[t]], k = k0 + threadIdx.x;
+  if (k < V.off[V.tile[t + 1]]) {
+    const int64_t b = V.posblk[k], o = V.off[b];
+    w.n = (int)(V.off[b + 1] - o);
+    w.i = (int)(k - o);
+    w.s0 = (int)(o - k0);
+    w.e = V.eq[k];
+    w.Bt = V.inv32 + V.ioff[b];
+  }
+  return w;
+}
+__device__ __forceinline__ float vb_rowdot(const VbRow &w, const float *sh) {
+  float z = 0.f;
+  for (int j = 0; j < w.n; j++) z = fmaf(w.Bt[j * w.n + w.i], sh[w.s0 + j], z);
+  return z;
+}
+
 // mixed CG: p = M r + beta p in FP32 (p and the atomically accumulated q padded like k_mx_p)
 __global__ void __launch_bounds__(kThreads) k_vb32_p(const float *__restrict__ r, VBlk V, float *__restrict__ p,
                                                      int padded, float *__restrict__ qzero, Red R) {
+  __shared__ float sh[kThreads];
   if (!active(R.iscal)) return;
   const bool first = R.iscal[I_IT] == 0 || R.iscal[I_RESTART] != 0;
   const float beta = first ? 0.f : (float)R.scal[S_BETA];
-  for (int64_t b = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; b < V.nb; b += (int64_t)gridDim.x * blockDim.x) {
-    const int64_t o = V.off[b];
-    const int n = (int)(V.off[b + 1] - o);
-    const float *B = V.inv32 + V.ioff[b];
-    for (int i = 0; i < n; i++) {
-      float z = 0.f;
-      for (int j = 0; j < n; j++) z = fmaf(B[i * n + j], r[V.eq[o + j]], z);
-      const int64_t jj = pidx(V.eq[o + i], padded);
+  for (int64_t t = blockIdx.x; t < V.ntile; t += gridDim.x) {
+    const VbRow w = vb_row(V, t);
+    if (w.n) sh[threadIdx.x] = r[w.e];
+    __syncthreads();
+    if (w.n) {
+      const float z = vb_rowdot(w, sh);
+      const int64_t jj = pidx(w.e, padded);
       p[jj] = first ? z : fmaf(beta, p[jj], z);
       if (qzero) qzero[jj] = 0.f;
     }
+    __syncthreads();
   }
 }
 
@@ -1299,26 +1349,24 @@ __global__ void __launch_bounds__(kThreads) k_vb32_p(const float *__restrict__ r
 __global__ void __launch_bounds__(kThreads) k_vb32_update(float *__restrict__ dx, float *__restrict__ r,
                                                           const float *__restrict__ p, const float *__restrict__ q,
                                                           VBlk V, int padded, int qpad, Red R) {
+  __shared__ float sh[kThreads];
   if (!active(R.iscal)) return;
   const double pq = R.scal[S_PQ];
   const float alpha = (float)R.scal[S_ALPHA];
   KSum rz, rr;
-  for (int64_t b = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; b < V.nb; b += (int64_t)gridDim.x * blockDim.x) {
-    const int64_t o = V.off[b];
-    const int n = (int)(V.off[b + 1] - o);
-    for (int i = 0; i < n; i++) {
-      const int64_t e = V.eq[o + i];
-      dx[e] = fmaf(alpha, p[pidx(e, padded)], dx[e]);
-      const float ri = fmaf(-alpha, q[pidx(e, qpad)], r[e]);
-      r[e] = ri;
+  for (int64_t t = blockIdx.x; t < V.ntile; t += gridDim.x) {
+    const VbRow w = vb_row(V, t);
+    float ri = 0.f;
+    if (w.n) {
+      dx[w.e] = fmaf(alpha, p[pidx(w.e, padded)], dx[w.e]);
+      ri = fmaf(-alpha, q[pidx(w.e, qpad)], r[w.e]);
+      r[w.e] = ri;
       rr.add(ri * ri);
+      sh[threadIdx.x] = ri;
     }
-    const float *B = V.inv32 + V.ioff[b];
-    for (int i = 0; i < n; i++) {
-      float z = 0.f;
-      for (int j = 0; j < n; j++) z = fmaf(B[i * n + j], r[V.eq[o + j]], z);
-      rz.add(r[V.eq[o + i]] * z);
-    }
+    __syncthreads();
+    if (w.n) rz.add(ri * vb_rowdot(w, sh));
+    __syncthreads();
   }
   double v[2] = {rz.get(), rr.get()}, tot[2];
   if (grid_reduce<2>(v, R, tot) && threadIdx.x == 0) {
@@ -1342,18 +1390,20 @@ __global__ void __launch_bounds__(kThreads) k_vb32_update(float *__restrict__ dx
 // mixed CG: r32 = r64 after a true-residual computation; rho = r.(M r), restart rule (epilogue of k_mx_r32)
 __global__ void __launch_bounds__(kThreads) k_vb32_r32(const double *__restrict__ r64, float *__restrict__ r32, VBlk V,
                                                        Red R) {
+  __shared__ float sh[kThreads];
   if (R.iscal[I_UPDATE] != 2) return;
   KSum rz;
-  for (int64_t b = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; b < V.nb; b += (int64_t)gridDim.x * blockDim.x) {
-    const int64_t o = V.off[b];
-    const int n = (int)(V.off[b + 1] - o);
-    for (int i = 0; i < n; i++) r32[V.eq[o + i]] = (float)r64[V.eq[o + i]];
-    const float *B = V.inv32 + V.ioff[b];
-    for (int i = 0; i < n; i++) {
-      float z = 0.f;
-      for (int j = 0; j < n; j++) z = fmaf(B[i * n + j], r32[V.eq[o + j]], z);
-      rz.add(r32[V.eq[o + i]] * z);
+  for (int64_t t = blockIdx.x; t < V.ntile; t += gridDim.x) {
+    const VbRow w = vb_row(V, t);
+    float ri = 0.f;
+    if (w.n) {
+      ri = (float)r64[w.e];
+      r32[w.e] = ri;
+      sh[threadIdx.x] = ri;
     }
+    __syncthreads();
+    if (w.n) rz.add(ri * vb_rowdot(w, sh));
+    __syncthreads();
   }
   double v[1] = {rz.get()}, tot[1];
   if (grid_reduce<1>(v, R, tot) && threadIdx.x == 0) {
@@ -2761,9 +2811,21 @@ void build_vblocks(Ctx &c, int kind) {
       tot += n * n;
       maxn = std::max(maxn, (int)n);
     }
+    // tiles of whole consecutive blocks with at most kThreads equations (one CTA
+    // of the FP32 kernels each), and position -> block
+    std::vector<int64_t> tile(1, 0);
+    std::vector<int32_t> posblk(std::max<size_t>(eq.size(), 1), 0);
+    for (int64_t b = 0; b < nb; b++) {
+      for (int64_t k = off[b]; k < off[b + 1]; k++) posblk[k] = (int32_t)b;
+      if (off[b + 1] - off[tile.back()] > kThreads) tile.push_back(b);
+    }
+    if (nb > 0) tile.push_back(nb);
     c.d_vb_off.upload(off.data(), off.size(), s);
     c.d_vb_eq.upload(eq.data(), std::max<size_t>(eq.size(), 1), s);
     c.d_vb_ioff.upload(ioff.data(), ioff.size(), s);
+    c.d_vb_tile.upload(tile.data(), tile.size(), s);
+    c.d_vb_posblk.upload(posblk.data(), posblk.size(), s);
+    c.vb_ntile = (int64_t)tile.size() - 1;
     c.d_vb_inv.alloc(std::max<int64_t>(tot, 1));
     c.d_vb_eqblk.alloc(std::max<int64_t>(c.neq, 1));
     c.d_vb_eqloc.alloc(std::max<int64_t>(c.neq, 1));
@@ -2788,7 +2850,8 @@ void build_vblocks(Ctx &c, int kind) {
 }
 
 VBlk vblk_of(const Ctx &c) {
-  return VBlk{c.d_vb_off.p, c.d_vb_eq.p, c.d_vb_ioff.p, c.d_vb_inv.p, c.d_vb_inv32.p, c.vb_nb};
+  return VBlk{c.d_vb_off.p, c.d_vb_eq.p,     c.d_vb_ioff.p, c.d_vb_inv.p, c.d_vb_inv32.p,
+              c.vb_nb,      c.d_vb_tile.p, c.d_vb_posblk.p, c.vb_ntile};
 }
 
 // ---- solver workspace and the iteration plan
@@ -3470,7 +3533,7 @@ int solve(Ctx &c, const gpz_solver_opts &o, gpz_solve_report &rep) {
     // FP32 copies of the preconditioner
     if (vb) {
       if (!c.d_vb_inv32.p || c.d_vb_inv32.n != c.d_vb_inv.n) c.d_vb_inv32.alloc(c.d_vb_inv.n);
-      k_to_f32<<<wave(k_to_f32), kThreads, 0, s>>>(c.d_vb_inv.p, c.d_vb_inv32.p, (int64_t)c.d_vb_inv.n);
+      k_vb_inv32t<<<wave(k_vb_inv32t), kThreads, 0, s>>>(vblk_of(c), c.d_vb_inv32.p);
     } else if (block) {
       c.d_bjinv32.alloc((size_t)P.nunits * 9);
       k_to_f32<<<wave(k_to_f32), kThreads, 0, s>>>(c.d_bjinv.p, c.d_bjinv32.p, (int64_t)P.nunits * 9);
