@@ -13,6 +13,7 @@ double time_spmv(Ctx &c, bool f32, int reps);
 void drop_assembly_graph(Ctx &c) {
   if (c.asm_graph) cudaGraphExecDestroy(c.asm_graph);
   c.asm_graph = nullptr;
+  c.rp_bucket = nullptr;  // chosen again, with the pattern, by the next assembly
 }
 
 Ctx::~Ctx() {
@@ -354,7 +355,13 @@ int gpz_assembly_report(gpz_ctx *ctx, char *buf, int64_t len) {
                     (c.asm_mode_report.empty() ? std::string("null") : c.asm_mode_report) + ", \"fp32_elements\": " +
                     (c.fp32_report.empty() ? std::string("null") : c.fp32_report) + ", \"mesh_upload_ms\": " +
                     (c.upload_report.empty() ? std::string("null") : c.upload_report) + ", \"pattern_ms\": " +
-                    (c.pattern_report.empty() ? std::string("null") : c.pattern_report) + "}";
+                    (c.pattern_report.empty() ? std::string("null") : c.pattern_report) + ", \"row_owner_pass\": " +
+                    (c.rp_bucket ? "{\"elements\": " + std::to_string(c.rp_bucket->elems.size()) +
+                                       ", \"longest_row\": " + std::to_string(c.rp_lmax) +
+                                       ", \"warps_per_cta\": " + std::to_string(c.rp_warps) +
+                                       ", \"matrix_cleared\": " + (c.rp_full ? "false" : "true") + "}"
+                                 : std::string("null")) +
+                    "}";
     GPZ_REQUIRE((int64_t)r.size() < len, GPZ_E_INVALID, "buffer too small");
     std::copy(r.begin(), r.end(), buf);
     buf[r.size()] = 0;

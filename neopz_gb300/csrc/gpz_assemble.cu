@@ -661,6 +661,7 @@ __global__ void k_to_fp32(const double *__restrict__ a, float *__restrict__ b, i
 void build_buckets(Ctx &c, const gpz_mesh_desc &d) {
   for (Bucket *b : c.buckets) delete b;
   c.buckets.clear();
+  c.rp_bucket = nullptr;
   const auto t0 = std::chrono::steady_clock::now();
   // rows of the hp elements' active shapes (written and read for hp elements only)
   std::unique_ptr<uint8_t[]> act_full(new uint8_t[(size_t)c.nel * kMaxShapes]),
@@ -1013,6 +1014,378 @@ __global__ void k_translates(const int64_t *__restrict__ elems, int64_t n, const
   if (!ok) atomicOr(flag, 1);
 }
 
+// ---- row-owner assembly of a shared-matrix bucket.  With K_e = c_e kref the
+// matrix rows of one unit (the nstate equations of one shape of one connect)
+// are sums over the unit's incidences (element e, shape a) of c_e times row a
+// of kref: one warp per unit adds them in shared memory, column block by
+// column block through the element's slot-offset table, and writes the rows
+// once, whole and coalesced.  The coloured scatter instead reads and writes
+// every row once per colour of the elements around it, and the rows (10 GB
+// for 64^3 Q2 elasticity) do not stay in L2 between colours.  The products
+// are those of the scatter (kref is symmetric, so row b of the transposed
+// block is row b of kref) with the same |K| >= 1e-12 rule; only the order of
+// the sums over a unit's elements differs.  The load vector stays with the
+// element kernels (their load-vector-only mode), so that it keeps the order of
+// TPZStructMatrix::Assemble(rhs).
+constexpr int kRpMaxInc = 64;
+
+__global__ void k_rp_incidences(int pass, const int64_t *__restrict__ elems, int64_t ne, int nsh,
+                                const int *__restrict__ sside, const int *__restrict__ sk,
+                                const int64_t *__restrict__ el_conn, const int64_t *__restrict__ bpos, int nst,
+                                int64_t nunits, unsigned long long *__restrict__ cnt,
+                                const int64_t *__restrict__ ptr, int64_t *__restrict__ inc, int *__restrict__ bad) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < ne * nsh; i += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t ie = i / nsh;
+    const int a = (int)(i - ie * nsh);
+    const int64_t row = bpos[el_conn[elems[ie] * 27 + sside[a]]] + (int64_t)sk[a] * nst;
+    const int64_t u = row / nst;
+    if (row < 0 || row % nst != 0 || u >= nunits) {
+      atomicOr(bad, 1);
+      continue;
+    }
+    const unsigned long long k = atomicAdd(cnt + u, 1ull);
+    if (pass == 1) inc[ptr[u] + (int64_t)k] = (ie << 8) | a;
+  }
+}
+
+// each unit's incidences in increasing order (a fixed order of the sums)
+__global__ void k_rp_sort(const int64_t *__restrict__ ptr, int64_t nunits, int64_t *__restrict__ inc,
+                          int *__restrict__ bad) {
+  for (int64_t u = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; u < nunits; u += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t p0 = ptr[u], n = ptr[u + 1] - p0;
+    if (n > kRpMaxInc) {
+      atomicOr(bad, 2);
+      continue;
+    }
+    for (int64_t i = 1; i < n; i++) {
+      const int64_t v = inc[p0 + i];
+      int64_t j = i - 1;
+      while (j >= 0 && inc[p0 + j] > v) {
+        inc[p0 + j + 1] = inc[p0 + j];
+        j--;
+      }
+      inc[p0 + j + 1] = v;
+    }
+  }
+}
+
+// the longest row of the units, units without incidences, units whose rows differ in length
+__global__ void k_rp_rows(const int64_t *__restrict__ ptr, int64_t nunits, const int64_t *__restrict__ ia, int nst,
+                          int *__restrict__ out /* lmax, empty, uneven */) {
+  for (int64_t u = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; u < nunits; u += (int64_t)gridDim.x * blockDim.x) {
+    if (ptr[u + 1] == ptr[u]) {
+      atomicOr(out + 1, 1);
+      continue;
+    }
+    const int64_t L = ia[u * nst + 1] - ia[u * nst];
+    for (int s = 1; s < nst; s++)
+      if (ia[u * nst + s + 1] - ia[u * nst + s] != L) atomicOr(out + 2, 1);
+    atomicMax(out, L < (1 << 30) ? (int)L : (1 << 30));
+  }
+}
+
+// An incidence as the row pass reads it, one 16-byte load: the element's row
+// of slot offsets for the shape's side (offbase[e] + side * nsides), the
+// element (its coefficient is read at run time) and the shape.
+struct RpRec {
+  int64_t orow;
+  int32_t e, a;
+};
+
+__global__ void k_rp_records(const int64_t *__restrict__ inc, int64_t n, const int64_t *__restrict__ elems,
+                             const int64_t *__restrict__ offbase, const int *__restrict__ sside, int ns,
+                             RpRec *__restrict__ rec) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t code = inc[i];
+    const int64_t e = elems[code >> 8];
+    const int a = (int)(code & 255);
+    rec[i] = RpRec{offbase[e] + (int64_t)sside[a] * ns, (int32_t)e, a};
+  }
+}
+
+// Before each row pass: the range of |c_e| over the bucket, and kref with the
+// entries that the |c_e kref| >= 1e-12 rule drops for every c_e in that range
+// set to zero (kp).  amb = 1 when some entry is kept for part of the range
+// only; the row pass then applies the rule product by product.
+// GB300's FP64 rate bounds the row pass: without the test each kept entry
+// costs one multiply and one add (Q2 elasticity: 942 of kref's 6561 entries
+// are rounding-level and are dropped whatever the coefficient).
+// rng[0], rng[1]: the bit patterns of min and max |c_e| (non-negative doubles
+// order as their bits), set beforehand to a huge value and to 0
+__global__ void __launch_bounds__(256) k_rp_range(ElemArgs P, const int64_t *__restrict__ elems, int64_t ne,
+                                                  unsigned long long *__restrict__ rng) {
+  double lo = 1e300, hi = 0.0;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < ne; i += (int64_t)gridDim.x * blockDim.x) {
+    double cf = P.kind == GPZ_MAT_ELAST3D ? P.E : P.coef_const;
+    if (P.coef) cf = P.coef[elems[i]];
+    const double cs = fabs(P.kind == GPZ_MAT_POISSON ? 1.0 : cf);
+    lo = fmin(lo, cs);
+    hi = fmax(hi, cs);
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    lo = fmin(lo, __shfl_xor_sync(0xffffffffu, lo, o));
+    hi = fmax(hi, __shfl_xor_sync(0xffffffffu, hi, o));
+  }
+  if ((threadIdx.x & 31) == 0) {
+    atomicMin(rng, (unsigned long long)__double_as_longlong(lo));
+    atomicMax(rng + 1, (unsigned long long)__double_as_longlong(hi));
+  }
+}
+
+__global__ void k_rp_prune(const double *__restrict__ kref, int n, const unsigned long long *__restrict__ rng,
+                           double *__restrict__ kp, int *__restrict__ amb) {
+  const double lo = __longlong_as_double((long long)rng[0]), hi = __longlong_as_double((long long)rng[1]);
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const double k = kref[i], ak = fabs(k);
+    // margins of 1e-12 relative cover the rounding of the product and of these tests
+    const bool never = ak * hi * (1.0 + 1e-12) < 1e-12, always = ak * lo * (1.0 - 1e-12) >= 1e-12;
+    kp[i] = never ? 0.0 : k;
+    if (!never && !always) atomicOr(amb, 1);
+  }
+}
+
+// One warp per unit, persistent; the next unit's bounds and row start are
+// loaded while the current one runs.  A unit's incidences go in chunks of up
+// to 8: lanes 0..7 load a chunk's records and coefficients at once and shuffle
+// them to the warp, every lane issues the chunk's offset loads for its column
+// shapes together, and the additions run incidence by incidence with a warp
+// barrier between them (two elements' shapes may share a column), each
+// block's nine old values read before its nine stores.  The rows of a unit
+// are consecutive and of equal length, so row s starts at ia[u NST] + s L.
+// kref sits in shared memory when it fits (kref_sh).
+template <int NST>
+__global__ void __launch_bounds__(512) k_rowpass(ElemArgs P, const int64_t *__restrict__ ptr,
+                                                 const RpRec *__restrict__ rec, const double *__restrict__ kp,
+                                                 const int *__restrict__ amb_p, int64_t nunits, int lmax,
+                                                 int kref_sh) {
+  extern __shared__ double rp_sm[];
+  const int nsh = P.nshape, nd = nsh * NST;
+  const double *kref = kp;
+  double *acc_base = rp_sm;
+  if (kref_sh) {
+    for (int i = threadIdx.x; i < nd * nd; i += blockDim.x) rp_sm[i] = kp[i];
+    kref = rp_sm;
+    acc_base = rp_sm + nd * nd;
+    __syncthreads();
+  }
+  const bool amb = *amb_p != 0;
+  const long long kTiny = __double_as_longlong(1.e-12);
+  const unsigned FULL = 0xffffffffu;
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  double *acc = acc_base + (size_t)wid * NST * lmax;
+  const int64_t nw = (int64_t)gridDim.x * (blockDim.x >> 5);
+  int64_t u = (int64_t)blockIdx.x * (blockDim.x >> 5) + wid;
+  int64_t np0 = 0, np1 = 0, nrb = 0, nre = 0;
+  if (u < nunits) {
+    np0 = ptr[u];
+    np1 = ptr[u + 1];
+    nrb = P.ia[u * NST];
+    nre = P.ia[u * NST + 1];
+  }
+  for (; u < nunits; u += nw) {
+    const int64_t p0 = np0, p1 = np1, rb = nrb;
+    const int L = (int)(nre - nrb);
+    if (u + nw < nunits) {
+      np0 = ptr[u + nw];
+      np1 = ptr[u + nw + 1];
+      nrb = P.ia[(u + nw) * NST];
+      nre = P.ia[(u + nw) * NST + 1];
+    }
+    if (p0 == p1) continue;
+    if (L > lmax) {  // the host sized the accumulators from these rows
+      if (lane == 0) atomicOr(P.err, 64);
+      continue;
+    }
+    for (int j = lane; j < NST * L; j += 32) acc[j] = 0.0;
+    __syncwarp();
+    for (int64_t pc = p0; pc < p1; pc += 8) {
+      const int m = (int)(p1 - pc < 8 ? p1 - pc : 8);
+      int a_l = 0;
+      int64_t ob_l = 0;
+      double cs_l = 0.0;
+      if (lane < m) {
+        const RpRec r = rec[pc + lane];
+        a_l = r.a;
+        ob_l = r.orow;
+        double cf = P.kind == GPZ_MAT_ELAST3D ? P.E : P.coef_const;
+        if (P.coef) cf = P.coef[r.e];
+        cs_l = P.kind == GPZ_MAT_POISSON ? 1.0 : cf;
+      }
+      int64_t obj[8];
+#pragma unroll
+      for (int j = 0; j < 8; j++) obj[j] = __shfl_sync(FULL, ob_l, j);
+      for (int bb = 0; bb < nsh; bb += 32) {
+        const int b = bb + lane;
+        const bool act = b < nsh;
+        const int sb = act ? P.sside[b] : 0, kb = act ? P.sk[b] * NST : 0;
+        int32_t ofs[8];
+#pragma unroll
+        for (int j = 0; j < 8; j++) ofs[j] = (act && j < m) ? P.off[obj[j] + sb] : 0;
+#pragma unroll
+        for (int j = 0; j < 8; j++) {
+          const int aj = __shfl_sync(FULL, a_l, j);
+          const double csj = __shfl_sync(FULL, cs_l, j);
+          const bool first = j == 0 && pc == p0;  // the unit's first incidence: 0 + v is v, a store
+          if (j < m && act) {
+            const int o = ofs[j] + kb;
+            if (ofs[j] < 0 || o + NST > L) {
+              atomicOr(P.err, 32);
+            } else {
+              const double *kr = kref + (size_t)(aj * NST) * nd + b * NST;
+              double k[NST][NST], old[NST][NST];
+#pragma unroll
+              for (int s = 0; s < NST; s++)
+#pragma unroll
+                for (int t = 0; t < NST; t++) {
+                  k[s][t] = kr[s * nd + t];
+                  old[s][t] = acc[s * L + o + t];
+                }
+              if (!amb) {  // kept entries pass the rule for every coefficient of the bucket: no test;
+                           // product and sum rounded apart (never fused), as the scatter forms them
+#pragma unroll
+                for (int s = 0; s < NST; s++)
+#pragma unroll
+                  for (int t = 0; t < NST; t++)
+                    if (__double_as_longlong(k[s][t]) << 1) {
+                      const double v = __dmul_rn(csj, k[s][t]);
+                      acc[s * L + o + t] = first ? v : __dadd_rn(old[s][t], v);
+                    }
+              } else {  // the rule per product, compared on the bits (|v| >= 1e-12 for finite v)
+#pragma unroll
+                for (int s = 0; s < NST; s++)
+#pragma unroll
+                  for (int t = 0; t < NST; t++) {
+                    const double v = __dmul_rn(csj, k[s][t]);
+                    if ((__double_as_longlong(v) & 0x7fffffffffffffffLL) >= kTiny)
+                      acc[s * L + o + t] = first ? v : __dadd_rn(old[s][t], v);
+                  }
+              }
+            }
+          }
+          __syncwarp();
+        }
+      }
+    }
+#pragma unroll
+    for (int s = 0; s < NST; s++) {
+      double *dst = P.a + rb + (int64_t)s * L;
+      for (int j = lane; j < L; j += 32) dst[j] = acc[s * L + j];
+    }
+    __syncwarp();
+  }
+}
+
+constexpr int kRpSmem = 220 * 1024;
+
+// Incidence lists of the largest shared-matrix bucket (mesh-dependent, built
+// once), then, for the current pattern, its longest row and whether its units
+// cover every equation.  Leaves c.rp_bucket null when no bucket qualifies.
+void rowpass_prepare(Ctx &c) {
+  cudaStream_t s = c.stream;
+  c.rp_bucket = nullptr;
+  const int nst = c.nstate;
+  if (c.flt.active || (nst != 1 && nst != 3) || c.neq_mesh % nst != 0) return;
+  Bucket *best = nullptr;
+  for (Bucket *b : c.buckets)
+    if (b->shared == 1 && b->rowpass != 0 && b->nshape <= 64 && (!best || b->elems.size() > best->elems.size()))
+      best = b;
+  if (!best) return;
+  Bucket *b = best;
+  const int64_t nunits = c.neq_mesh / nst, ne = (int64_t)b->elems.size();
+  DBuf<int> flags;
+  flags.alloc(4);
+  if (b->rowpass < 0) {
+    DBuf<unsigned long long> cnt;
+    cnt.alloc(nunits + 1);
+    cnt.zero(s);
+    flags.zero(s);
+    const unsigned g = (unsigned)std::min<int64_t>(grid_for(ne * b->nshape, 256), 152 * 16);
+    k_rp_incidences<<<g, 256, 0, s>>>(0, b->d_elems.p, ne, b->nshape, b->d_shape_side.p, b->d_shape_k.p,
+                                      c.d_el_conn.p, c.d_block_pos.p, nst, nunits, cnt.p, nullptr, nullptr, flags.p);
+    c.launches++;
+    b->d_rp_ptr.alloc(nunits + 1);
+    exclusive_scan_i64((const int64_t *)cnt.p, b->d_rp_ptr.p, nunits + 1, s, c);
+    b->d_rp_inc.alloc(std::max<int64_t>(ne * b->nshape, 1));
+    cnt.zero(s);
+    k_rp_incidences<<<g, 256, 0, s>>>(1, b->d_elems.p, ne, b->nshape, b->d_shape_side.p, b->d_shape_k.p,
+                                      c.d_el_conn.p, c.d_block_pos.p, nst, nunits, cnt.p, b->d_rp_ptr.p,
+                                      b->d_rp_inc.p, flags.p);
+    c.launches++;
+    k_rp_sort<<<grid_for(nunits, 256), 256, 0, s>>>(b->d_rp_ptr.p, nunits, b->d_rp_inc.p, flags.p);
+    c.launches++;
+    GPZ_CUDA_TRY(cudaGetLastError());
+    int h = 0;
+    GPZ_CUDA_TRY(cudaMemcpyAsync(&h, flags.p, sizeof(int), cudaMemcpyDeviceToHost, s));
+    GPZ_CUDA_TRY(cudaStreamSynchronize(s));
+    b->rowpass = h ? 0 : 1;
+    if (!b->rowpass) {
+      b->d_rp_ptr.release();
+      b->d_rp_inc.release();
+      return;
+    }
+  }
+  const int64_t ninc = ne * b->nshape;
+  b->d_rp_rec.alloc(std::max<int64_t>(ninc, 1) * 2);  // RpRec, 16 bytes each
+  const int64_t ndk = (int64_t)b->nshape * nst;
+  b->d_rp_kp.alloc(ndk * ndk + 3);  // the pruned kref, then the |c_e| range and the flag amb
+  k_rp_records<<<grid_for(ninc, 256), 256, 0, s>>>(b->d_rp_inc.p, ninc, b->d_elems.p, c.d_offbase.p,
+                                                    b->d_shape_side.p, b->nsides, (RpRec *)b->d_rp_rec.p);
+  c.launches++;
+  flags.zero(s);
+  k_rp_rows<<<grid_for(nunits, 256), 256, 0, s>>>(b->d_rp_ptr.p, nunits, c.d_ia.p, nst, flags.p);
+  c.launches++;
+  GPZ_CUDA_TRY(cudaGetLastError());
+  int h[3] = {0, 0, 0};
+  GPZ_CUDA_TRY(cudaMemcpyAsync(h, flags.p, 3 * sizeof(int), cudaMemcpyDeviceToHost, s));
+  GPZ_CUDA_TRY(cudaStreamSynchronize(s));
+  const int64_t per_warp = (int64_t)nst * h[0] * (int64_t)sizeof(double);
+  const int64_t nd = (int64_t)b->nshape * nst, kref_bytes = nd * nd * (int64_t)sizeof(double);
+  const bool kref_sh = kref_bytes <= 64 * 1024 && kref_bytes + per_warp <= kRpSmem;
+  const int64_t room = kRpSmem - (kref_sh ? kref_bytes : 0);
+  if (h[2] || h[0] <= 0 || per_warp > room) return;
+  const int warps = (int)std::min<int64_t>(16, room / per_warp);
+  const size_t sh = (size_t)warps * per_warp + (kref_sh ? (size_t)kref_bytes : 0);
+  auto k = nst == 3 ? k_rowpass<3> : k_rowpass<1>;
+  GPZ_CUDA_TRY(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sh));
+  int dev = 0, nsm = 0, per = 0;
+  GPZ_CUDA_TRY(cudaGetDevice(&dev));
+  GPZ_CUDA_TRY(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
+  GPZ_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k, warps * 32, sh));
+  c.rp_lmax = h[0];
+  c.rp_warps = warps;
+  c.rp_kref_sh = kref_sh ? 1 : 0;
+  c.rp_smem = (int)sh;
+  c.rp_grid = std::max(1, per) * std::max(1, nsm);
+  c.rp_full = h[1] == 0;
+  c.rp_bucket = b;
+}
+
+void launch_rowpass(Ctx &c) {
+  Bucket *b = c.rp_bucket;
+  const ElemArgs P = args_of(c, b);
+  const int64_t nunits = c.neq_mesh / c.nstate;
+  const size_t sh = (size_t)c.rp_smem;
+  const RpRec *rec = (const RpRec *)b->d_rp_rec.p;
+  const int nd = b->nshape * c.nstate;
+  double *kp = b->d_rp_kp.p;
+  unsigned long long *rng = (unsigned long long *)(kp + (size_t)nd * nd);
+  int *amb = (int *)(rng + 2);
+  const int64_t ne = (int64_t)b->elems.size();
+  GPZ_CUDA_TRY(cudaMemsetAsync(rng, 0x7f, sizeof(unsigned long long), c.stream));  // about 1.4e306
+  GPZ_CUDA_TRY(cudaMemsetAsync(rng + 1, 0, sizeof(unsigned long long) + sizeof(int), c.stream));
+  k_rp_range<<<(unsigned)std::min<int64_t>(grid_for(ne, 256), 152 * 4), 256, 0, c.stream>>>(P, b->d_elems.p, ne, rng);
+  k_rp_prune<<<grid_for((int64_t)nd * nd, 256), 256, 0, c.stream>>>(P.kref, nd * nd, rng, kp, amb);
+  c.launches += 2;
+  if (c.nstate == 3)
+    k_rowpass<3><<<c.rp_grid, c.rp_warps * 32, sh, c.stream>>>(P, b->d_rp_ptr.p, rec, kp, amb, nunits,
+                                                                c.rp_lmax, c.rp_kref_sh);
+  else
+    k_rowpass<1><<<c.rp_grid, c.rp_warps * 32, sh, c.stream>>>(P, b->d_rp_ptr.p, rec, kp, amb, nunits,
+                                                                c.rp_lmax, c.rp_kref_sh);
+  c.launches++;
+  GPZ_CUDA_TRY(cudaGetLastError());
+}
+
 // element integration + scatter of every bucket, colour by colour; the hp
 // classes run with `threads` (0: the class's tuned block size).  queue: one
 // persistent launch per bucket over all its colours instead (k_elem_fp64_queue).
@@ -1029,6 +1402,7 @@ void launch_elements(Ctx &c, int threads, bool rhs_only = false, bool set_attrs 
       if (!ne) continue;
       ElemArgs P = args_of(c, b);
       P.rhs_only = rhs_only ? 1 : 0;
+      if (b == c.rp_bucket) P.rhs_only = 1;  // the matrix came from k_rowpass
       const size_t sh = smem_bytes(b->nshape, b->dim, b->nq, b->key.is_bc);
       const Kernels K = b->hp ? select_hp(b->key.type, c.nstate, b->key.is_bc)
                               : select_kernel(b->key.type, b->nshape, c.nstate, b->key.is_bc);
@@ -1061,6 +1435,7 @@ void launch_elements(Ctx &c, int threads, bool rhs_only = false, bool set_attrs 
       if (e1 == e0) continue;
       ElemArgs P = args_of(c, b);
       P.rhs_only = rhs_only ? 1 : 0;
+      if (b == c.rp_bucket) P.rhs_only = 1;
       size_t sh = smem_bytes(b->nshape, b->dim, b->nq, b->key.is_bc);
       ElemKernel k;
       HpArgs H{nullptr, nullptr, nullptr};
@@ -1129,6 +1504,7 @@ void shared_setup(Ctx &c) {
 void assemble_fp64(Ctx &c) {
   cudaStream_t s = c.stream;
   shared_setup(c);
+  if (!c.asm_graph) rowpass_prepare(c);  // a new pattern (or the first assembly)
   const bool flt = c.flt.active;
   c.d_a.alloc(std::max<int64_t>(c.nnz, 1));
   if (flt) c.flt.m_a.alloc(std::max<int64_t>(c.flt.m_nnz, 1));
@@ -1228,8 +1604,9 @@ void assemble_fp64(Ctx &c) {
   }
   c.d_dinv.alloc(std::max<int64_t>(c.neq, 1));
   auto body = [&](bool set_attrs) {
-    target.zero(s);
+    if (!c.rp_bucket || !c.rp_full) target.zero(s);
     c.d_f.zero(s);
+    if (c.rp_bucket) launch_rowpass(c);
     launch_elements(c, 0, false, set_attrs, c.asm_queue == 1);
     if (flt) {
       filter_values(c);

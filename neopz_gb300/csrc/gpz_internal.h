@@ -108,6 +108,14 @@ struct Bucket {
   // Jacobian), so K_e = coefficient_e x kref; -1 before the check
   int shared = -1;
   DBuf<double> d_kref, d_fref;               // [ndof][ndof] at coefficient 1, [ndof] load vector
+  // row-owner assembly of a shared-matrix bucket (k_rowpass): per unit of nstate
+  // equations (one shape of one connect) the bucket's (element, shape)
+  // incidences, sorted, packed as (index in elems << 8 | shape); -1 before the
+  // lists are built, 0 when the bucket does not qualify
+  int rowpass = -1;
+  DBuf<int64_t> d_rp_ptr, d_rp_inc;
+  DBuf<int64_t> d_rp_rec;  // per incidence, for the current pattern: slot-offset row, element, shape
+  DBuf<double> d_rp_kp;    // kref without the entries the 1e-12 rule always drops, then a flag
   // persistent launch over all colours: colour boundaries, work / done counters, resident CTAs
   DBuf<int64_t> d_cbeg;
   DBuf<unsigned long long> d_q;
@@ -302,6 +310,12 @@ struct Ctx {
   DBuf<int32_t> d_el_type, d_el_mat, d_block_size, d_conn_order;
   std::vector<Bucket *> buckets;
   cudaGraphExec_t asm_graph = nullptr;       // captured assembly of the current pattern (replayed)
+  // the bucket whose matrix the row-owner pass assembles (null: every bucket
+  // scatters), its longest row, warps per CTA and whether its rows cover every
+  // equation (then the matrix needs no clearing); set with the pattern
+  Bucket *rp_bucket = nullptr;
+  int rp_lmax = 0, rp_warps = 0, rp_grid = 0, rp_kref_sh = 0, rp_smem = 0;
+  bool rp_full = false;
   int64_t asm_graph_launches = 0;
   std::string asm_tune_report;               // block-size timings of the hp element kernels
   int asm_queue = 0;                         // 1: persistent launches per bucket, 0: a launch per colour (the
