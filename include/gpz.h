@@ -437,7 +437,12 @@ int gpz_assembly_mode(gpz_ctx *ctx, int mode);
  * kernels), hp classes (elements of uneven side orders sharing the table of
  * the full element of their largest order, one run-time kernel per class and
  * colour), colours, and the hp kernels' block-size autotuner timings (ms of one
- * assembly per candidate). */
+ * assembly per candidate); the FP32 element pass, the mesh upload and pattern
+ * stage timings; and "row_owner_pass": the bucket of hexes that are all
+ * translates of one element (K_e = c_e K_1) whose matrix is assembled row by
+ * row -- one warp per connect sums its elements' rows and writes the connect's
+ * rows once -- before the other buckets scatter into it (its elements, the
+ * longest row, warps per CTA, whether the matrix is cleared first), or null. */
 int gpz_assembly_report(gpz_ctx *ctx, char *buf, int64_t len);
 
 /* ---- coefficient update -------------------------------------------------
