@@ -1538,7 +1538,7 @@ void assemble_fp64(Ctx &c) {
     GPZ_CUDA_TRY(cudaEventCreate(&e0));
     GPZ_CUDA_TRY(cudaEventCreate(&e1));
     for (int i = 0; i < 3; i++) {
-      target.zero(s);
+      if (!c.rp_bucket || !c.rp_full) target.zero(s);
       c.d_f.zero(s);
       GPZ_CUDA_TRY(cudaEventRecord(e0, s));
       launch_elements(c, cand[i]);
@@ -1584,7 +1584,7 @@ void assemble_fp64(Ctx &c) {
       float ms[2] = {0.f, 0.f};
       for (int q = 0; q < 2; q++)
         for (int rep = 0; rep < 2; rep++) {
-          target.zero(s);
+          if (!c.rp_bucket || !c.rp_full) target.zero(s);  // timing only: a covering row pass rewrites every row
           c.d_f.zero(s);
           GPZ_CUDA_TRY(cudaEventRecord(e0, s));
           launch_elements(c, 0, false, true, q == 1);
